@@ -1,0 +1,285 @@
+"""ctypes access to the two CPU oracles.  TEST INFRASTRUCTURE ONLY.
+
+* ``RefOracle``  -- the reference photoNs-2.0 FMM sources compiled in place
+  (oracle/_ref/libphotons_ref.so, see oracle/Makefile and ref_harness.c).
+  Exists only where the reference tree is present.
+* ``PortOracle`` -- this project's own C restatement of the same pass
+  (oracle/photons_oracle.c -> oracle/_build/libphotons_oracle.so).  It is
+  pinned against ``RefOracle`` and the committed golden fixtures, and it is
+  the CPU baseline on machines without the reference.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may use
+this module; the product never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_SO = os.path.join(HERE, "_ref", "libphotons_ref.so")
+PORT_SO = os.path.join(HERE, "_build", "libphotons_oracle.so")
+
+NMULTI = 20
+LIST_KINDS = {"p2p": 0, "m2l": 1, "p2p_ext": 2, "m2l_ext": 3}
+COUNTER_NAMES = [
+    "idxP2P", "idxM2L", "walk_m2l_count", "p2p_count_remote", "NLEAF", "NNODE",
+    "nleaf", "nnode", "first_leaf", "first_node", "direct_local_start",
+    "n_p2p", "n_m2l", "n_p2p_ext", "n_m2l_ext", "n_images",
+]
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_lp = C.POINTER(C.c_longlong)
+
+
+def _ptr(a, t=_dp):
+    return a.ctypes.data_as(t) if a is not None else None
+
+
+def build_port():
+    subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+
+
+def build_ref():
+    subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+
+
+def ref_available():
+    return os.path.exists(REF_SO)
+
+
+class PassResult(dict):
+    """pos (tree order), acc_task (after the local task phase), acc, counters, lists."""
+
+
+class _Base:
+    def _lists(self, lib, prefix):
+        out = {}
+        for name, k in LIST_KINDS.items():
+            n = getattr(lib, prefix + "list_size")(k)
+            t = np.empty(n, np.int32)
+            s = np.empty(n, np.int32)
+            im = np.empty(n, np.int32)
+            if n:
+                getattr(lib, prefix + "list_copy")(k, _ptr(t, _ip), _ptr(s, _ip), _ptr(im, _ip))
+            out[name] = (t, s, im)
+        return out
+
+    def _tree(self, lib, prefix, counters):
+        nl, nn = int(counters["nleaf"]), int(counters["nnode"])
+        lip = np.empty((nl, 2), np.int32)
+        lgeom = np.empty((nl, 6), np.float64)
+        lM = np.empty((nl, NMULTI), np.float64)
+        lL = np.empty((nl, NMULTI), np.float64)
+        ninfo = np.empty((nn, 3), np.int32)
+        ngeom = np.empty((nn, 7), np.float64)
+        nM = np.empty((nn, NMULTI), np.float64)
+        nL = np.empty((nn, NMULTI), np.float64)
+        getattr(lib, prefix + "copy_leaves")(_ptr(lip, _ip), _ptr(lgeom), _ptr(lM), _ptr(lL))
+        getattr(lib, prefix + "copy_nodes")(_ptr(ninfo, _ip), _ptr(ngeom), _ptr(nM), _ptr(nL))
+        return dict(leaf_ipart=lip[:, 0].copy(), leaf_npart=lip[:, 1].copy(),
+                    leaf_center=lgeom[:, :3].copy(), leaf_width=lgeom[:, 3:].copy(),
+                    leaf_M=lM, leaf_L=lL,
+                    node_npart=ninfo[:, 0].copy(), node_son=ninfo[:, 1:].copy(),
+                    node_split=ngeom[:, 0].copy(), node_center=ngeom[:, 1:4].copy(),
+                    node_width=ngeom[:, 4:].copy(), node_M=nM, node_L=nL)
+
+
+class RefOracle(_Base):
+    def __init__(self):
+        if not ref_available():
+            raise FileNotFoundError(REF_SO)
+        lib = C.CDLL(REF_SO)
+        lib.ref_run.restype = C.c_double
+        lib.ref_run.argtypes = [C.c_int, _dp, C.c_double, C.c_int, C.c_double, C.c_double,
+                                C.c_double, C.c_double, C.c_double, C.c_int, _dp, _dp, _dp, _lp]
+        lib.ref_list_size.restype = C.c_long
+        lib.ref_list_size.argtypes = [C.c_int]
+        lib.ref_list_copy.argtypes = [C.c_int, _ip, _ip, _ip]
+        lib.ref_copy_leaves.argtypes = [_ip, _dp, _dp, _dp]
+        lib.ref_copy_nodes.argtypes = [_ip, _dp, _dp, _dp]
+        lib.ref_m2l.argtypes = [C.c_double] * 3 + [_dp, _dp, C.c_double]
+        lib.ref_m2m.argtypes = [C.c_double] * 3 + [_dp, _dp]
+        lib.ref_l2l.argtypes = [C.c_double] * 3 + [_dp, _dp]
+        lib.ref_acceptance.restype = C.c_int
+        lib.ref_acceptance.argtypes = [_dp, _dp, _dp, C.c_double, C.c_double]
+        self.lib = lib
+
+    def run(self, pos, p, capture=True, tree=True):
+        pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+        n = pos.shape[0]
+        pos_out = np.empty_like(pos)
+        acc_task = np.empty_like(pos)
+        acc = np.empty_like(pos)
+        cnt = np.zeros(16, np.int64)
+        secs = self.lib.ref_run(n, _ptr(pos), p["boxsize"], p["maxleaf"], p["theta"], p["rs"],
+                                p["rcut"], p["eps"], p["mass"], int(capture), _ptr(pos_out),
+                                _ptr(acc_task), _ptr(acc), _ptr(cnt, _lp))
+        counters = dict(zip(COUNTER_NAMES, (int(c) for c in cnt)))
+        r = PassResult(pos=pos_out, acc_task=acc_task, acc=acc, counters=counters, seconds=secs)
+        if capture:
+            r["lists"] = self._lists(self.lib, "ref_")
+        if tree:
+            r["tree"] = self._tree(self.lib, "ref_", counters)
+        return r
+
+    def m2l(self, d, M, rs):
+        L = np.zeros(NMULTI)
+        M = np.ascontiguousarray(M, np.float64)
+        self.lib.ref_m2l(d[0], d[1], d[2], _ptr(M), _ptr(L), rs)
+        return L
+
+    def m2m(self, d, M):
+        out = np.zeros(NMULTI)
+        M = np.ascontiguousarray(M, np.float64)
+        self.lib.ref_m2m(d[0], d[1], d[2], _ptr(M), _ptr(out))
+        return out
+
+    def l2l(self, d, L):
+        out = np.zeros(NMULTI)
+        L = np.ascontiguousarray(L, np.float64)
+        self.lib.ref_l2l(d[0], d[1], d[2], _ptr(L), _ptr(out))
+        return out
+
+    def acceptance(self, wi, wj, dist, theta, rcut):
+        a = [np.ascontiguousarray(x, np.float64) for x in (wi, wj, dist)]
+        return self.lib.ref_acceptance(_ptr(a[0]), _ptr(a[1]), _ptr(a[2]), theta, rcut)
+
+
+class PortOracle(_Base):
+    """This project's C restatement (oracle/photons_oracle.c)."""
+
+    def __init__(self, build=True):
+        if build and not os.path.exists(PORT_SO):
+            build_port()
+        lib = C.CDLL(PORT_SO)
+        lib.po_create.restype = C.c_void_p
+        lib.po_destroy.argtypes = [C.c_void_p]
+        lib.po_run.restype = C.c_int
+        lib.po_run.argtypes = [C.c_void_p, C.c_void_p, C.c_int, _dp, _dp]
+        lib.po_counters.argtypes = [C.c_void_p, _lp]
+        lib.po_particles.argtypes = [C.c_void_p, _dp, _dp, _dp, _ip]
+        lib.po_list_size.restype = C.c_long
+        lib.po_list_size.argtypes = [C.c_void_p, C.c_int]
+        lib.po_list_copy.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _ip]
+        lib.po_copy_leaves.argtypes = [C.c_void_p, _ip, _dp, _dp, _dp]
+        lib.po_copy_nodes.argtypes = [C.c_void_p, _ip, _dp, _dp, _dp]
+        lib.po_m2l.argtypes = [C.c_double] * 3 + [_dp, _dp, C.c_double]
+        lib.po_m2m.argtypes = [C.c_double] * 3 + [_dp, _dp]
+        lib.po_l2l.argtypes = [C.c_double] * 3 + [_dp, _dp]
+        lib.po_p2m.argtypes = [C.c_int, _dp, C.c_double, _dp, _dp]
+        lib.po_l2p.argtypes = [C.c_int, _dp, _dp, _dp, _dp]
+        lib.po_acceptance.restype = C.c_int
+        lib.po_acceptance.argtypes = [_dp, _dp, _dp, C.c_double, C.c_double]
+        lib.po_direct_sum.restype = C.c_int
+        lib.po_direct_sum.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, _ip, C.c_double, _dp]
+        self.lib = lib
+        self.state = C.c_void_p(lib.po_create())
+
+    def __del__(self):
+        try:
+            self.lib.po_destroy(self.state)
+        except Exception:
+            pass
+
+    @staticmethod
+    def _params(p, nthreads=1, capture=True, images=True):
+        class P(C.Structure):
+            _fields_ = [("boxsize", C.c_double), ("theta", C.c_double), ("rs", C.c_double),
+                        ("rcut", C.c_double), ("eps", C.c_double), ("mass", C.c_double),
+                        ("maxleaf", C.c_int), ("nthreads", C.c_int), ("capture", C.c_int),
+                        ("images", C.c_int)]
+        return P(p["boxsize"], p["theta"], p["rs"], p["rcut"], p["eps"], p["mass"],
+                 int(p["maxleaf"]), int(nthreads), int(capture), int(images))
+
+    def run(self, pos, p, capture=True, tree=True, nthreads=1, images=True):
+        pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+        n = pos.shape[0]
+        prm = self._params(p, nthreads, capture, images)
+        secs = C.c_double(0.0)
+        rc = self.lib.po_run(self.state, C.byref(prm), n, _ptr(pos), C.byref(secs))
+        if rc != 0:
+            raise RuntimeError(f"oracle pass failed with code {rc}")
+        cnt = np.zeros(16, np.int64)
+        self.lib.po_counters(self.state, _ptr(cnt, _lp))
+        counters = dict(zip(COUNTER_NAMES, (int(c) for c in cnt)))
+        pos_out = np.empty_like(pos)
+        acc_task = np.empty_like(pos)
+        acc = np.empty_like(pos)
+        perm = np.empty(n, np.int32)
+        self.lib.po_particles(self.state, _ptr(pos_out), _ptr(acc_task), _ptr(acc), _ptr(perm, _ip))
+        r = PassResult(pos=pos_out, acc_task=acc_task, acc=acc, perm=perm, counters=counters,
+                       seconds=secs.value)
+        if capture:
+            out = {}
+            for name, k in LIST_KINDS.items():
+                m = self.lib.po_list_size(self.state, k)
+                t = np.empty(m, np.int32); s = np.empty(m, np.int32); im = np.empty(m, np.int32)
+                if m:
+                    self.lib.po_list_copy(self.state, k, _ptr(t, _ip), _ptr(s, _ip), _ptr(im, _ip))
+                out[name] = (t, s, im)
+            r["lists"] = out
+        if tree:
+            r["tree"] = self._tree_port(counters)
+        return r
+
+    def _tree_port(self, counters):
+        class Shim:
+            pass
+        shim = Shim()
+        shim.po_copy_leaves = lambda *a: self.lib.po_copy_leaves(self.state, *a)
+        shim.po_copy_nodes = lambda *a: self.lib.po_copy_nodes(self.state, *a)
+        return self._tree(shim, "po_", counters)
+
+    def direct_sum(self, pos, p, targets, rmax=None, nthreads=1):
+        pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+        targets = np.ascontiguousarray(targets, np.int32)
+        prm = self._params(p, nthreads)
+        out = np.empty((targets.size, 3))
+        rmax = rmax if rmax is not None else 2.0 * p["rcut"]
+        rc = self.lib.po_direct_sum(C.byref(prm), pos.shape[0], _ptr(pos), targets.size,
+                                    _ptr(targets, _ip), rmax, _ptr(out))
+        if rc != 0:
+            raise RuntimeError(f"direct sum failed with code {rc}")
+        return out
+
+    def m2l(self, d, M, rs):
+        L = np.zeros(NMULTI)
+        M = np.ascontiguousarray(M, np.float64)
+        self.lib.po_m2l(d[0], d[1], d[2], _ptr(M), _ptr(L), rs)
+        return L
+
+    def m2m(self, d, M):
+        out = np.zeros(NMULTI)
+        M = np.ascontiguousarray(M, np.float64)
+        self.lib.po_m2m(d[0], d[1], d[2], _ptr(M), _ptr(out))
+        return out
+
+    def l2l(self, d, L):
+        out = np.zeros(NMULTI)
+        L = np.ascontiguousarray(L, np.float64)
+        self.lib.po_l2l(d[0], d[1], d[2], _ptr(L), _ptr(out))
+        return out
+
+    def p2m(self, pos, mass, center):
+        pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+        c = np.ascontiguousarray(center, np.float64)
+        M = np.zeros(NMULTI)
+        self.lib.po_p2m(pos.shape[0], _ptr(pos), mass, _ptr(c), _ptr(M))
+        return M
+
+    def l2p(self, pos, center, L):
+        pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+        c = np.ascontiguousarray(center, np.float64)
+        L = np.ascontiguousarray(L, np.float64)
+        acc = np.zeros_like(pos)
+        self.lib.po_l2p(pos.shape[0], _ptr(pos), _ptr(c), _ptr(L), _ptr(acc))
+        return acc
+
+    def acceptance(self, wi, wj, dist, theta, rcut):
+        a = [np.ascontiguousarray(x, np.float64) for x in (wi, wj, dist)]
+        return self.lib.po_acceptance(_ptr(a[0]), _ptr(a[1]), _ptr(a[2]), theta, rcut)

@@ -1,0 +1,1016 @@
+/*
+ * CPU restatement of the photoNs-2.0 FMM short-range force pass (the oracle).
+ * TEST INFRASTRUCTURE ONLY -- see photons_oracle.h.
+ *
+ * Every step follows the reference's algorithm; each function names the
+ * reference lines it restates.  Traversals visit pairs in the reference's
+ * depth-first order and per-particle sums are formed in the reference's
+ * order, so on the reference's own inputs this oracle reproduces its tree,
+ * its interaction lists (same order) and, where no M2L occurs, its
+ * accelerations bit for bit.  The multipole operators are written here in
+ * multi-index form (the same Cartesian Taylor expansions as
+ * src/operator.c, summed in a different order), so results that involve
+ * M2L/L2L/L2P agree to rounding.
+ *
+ * Index space (src/fmm.c:200-212): particles [0,N), leaves
+ * [N, N+NLEAF), nodes [N+NLEAF, N+NLEAF+NNODE).
+ */
+#define _GNU_SOURCE
+#include "photons_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <sys/time.h>
+
+#define NM PO_NMULTI
+#define NIMG 27
+
+/* ------------------------------------------------------------------ */
+/* multi-index tables for the order-3 Cartesian expansions             */
+/* ------------------------------------------------------------------ */
+/* Component order of inc/operator.h:24-60: 1, x, y, z, xx, xy, xz, yy, yz,
+   zz, xxx, xxy, xxz, xyy, xyz, xzz, yyy, yyz, yzz, zzz -- graded, and inside
+   a grade ordered by descending x then descending y exponent. */
+static int mi_exp[NM][3];
+static int mi_index[4][4][4];
+static double mi_invfact[NM];    /* 1/(a! b! c!) */
+static int mi_order[NM];
+static int tables_ready = 0;
+
+static void init_tables(void)
+{
+    if (tables_ready) return;
+    static const double fact[4] = {1, 1, 2, 6};
+    int i = 0;
+    for (int k = 0; k <= 3; k++)
+        for (int a = k; a >= 0; a--)
+            for (int b = k - a; b >= 0; b--) {
+                int c = k - a - b;
+                mi_exp[i][0] = a; mi_exp[i][1] = b; mi_exp[i][2] = c;
+                mi_index[a][b][c] = i;
+                mi_invfact[i] = 1.0 / (fact[a] * fact[b] * fact[c]);
+                mi_order[i] = k;
+                i++;
+            }
+    tables_ready = 1;
+}
+
+/* d^g / g! for every multi-index g with |g| <= 3 */
+static void scaled_monomials(double dx, double dy, double dz, double *out)
+{
+    double px[4] = {1, dx, dx * dx, dx * dx * dx};
+    double py[4] = {1, dy, dy * dy, dy * dy * dy};
+    double pz[4] = {1, dz, dz * dz, dz * dz * dz};
+    for (int i = 0; i < NM; i++)
+        out[i] = px[mi_exp[i][0]] * py[mi_exp[i][1]] * pz[mi_exp[i][2]] * mi_invfact[i];
+}
+
+/* P2M, src/operator.c:13-93: M_a = sum_p m (-(x_p - c))^a / a! */
+void po_p2m(int npart, const double *pos, double mass, const double center[3], double *M)
+{
+    init_tables();
+    double mono[NM];
+    for (int i = 0; i < NM; i++) M[i] = 0.0;
+    for (int p = 0; p < npart; p++) {
+        scaled_monomials(-(pos[3 * p] - center[0]), -(pos[3 * p + 1] - center[1]),
+                         -(pos[3 * p + 2] - center[2]), mono);
+        for (int i = 0; i < NM; i++) M[i] += mass * mono[i];
+    }
+}
+
+/* M2M, src/operator.c:96-160 (d = parent centre - child centre):
+   toM_a += sum_{b <= a} M_b d^(a-b)/(a-b)! */
+void po_m2m(double dx, double dy, double dz, const double *M, double *toM)
+{
+    init_tables();
+    double mono[NM], out[NM];
+    scaled_monomials(dx, dy, dz, mono);
+    for (int a = 0; a < NM; a++) {
+        double s = 0.0;
+        for (int b = 0; b < NM; b++) {
+            int g0 = mi_exp[a][0] - mi_exp[b][0], g1 = mi_exp[a][1] - mi_exp[b][1],
+                g2 = mi_exp[a][2] - mi_exp[b][2];
+            if (g0 < 0 || g1 < 0 || g2 < 0) continue;
+            s += M[b] * mono[mi_index[g0][g1][g2]];
+        }
+        out[a] = s;
+    }
+    for (int a = 0; a < NM; a++) toM[a] += out[a];
+}
+
+/*
+ * Radial derivative factors f_k = ((1/r) d/dr)^k phi of the short-range
+ * Green's function phi(r) = erfc(r / (2 rs)) / r (the LONGSHORT branch of
+ * src/operator.c:294-307).  With a = 1/(2 rs), E = exp(-a^2 r^2),
+ * c = 2/sqrt(pi):
+ *   f0 = erfc/r
+ *   f1 = -erfc/r^3 - c a E/r^2
+ *   f2 = 3 erfc/r^5 + 3 c a E/r^4 + 2 c a^3 E/r^2
+ *   f3 = -15 erfc/r^7 - 15 c a E/r^6 - 10 c a^3 E/r^4 - 4 c a^5 E/r^2
+ */
+static void split_factors(double r, double rs, double f[4])
+{
+    double a = 0.5 / rs;
+    double u = a * r;
+    double ce = (2.0 / sqrt(M_PI)) * exp(-u * u);
+    double er = erfc(u);
+    double ir = 1.0 / r, ir2 = ir * ir;
+    double a2 = a * a;
+    f[0] = er * ir;
+    f[1] = -er * ir * ir2 - ce * a * ir2;
+    f[2] = 3.0 * er * ir * ir2 * ir2 + ce * (3.0 * a * ir2 * ir2 + 2.0 * a * a2 * ir2);
+    f[3] = -15.0 * er * ir * ir2 * ir2 * ir2 - ce * (15.0 * a * ir2 * ir2 * ir2 + 10.0 * a * a2 * ir2 * ir2 +
+                                                    4.0 * a * a2 * a2 * ir2);
+}
+
+/* derivative tensor D_g = d^g phi(x), |g| <= 3, from the radial factors:
+   D_g = f_|g| x^g + f_(|g|-1) sum_i C(g_i,2) x^(g - 2 e_i) */
+static void derivative_tensor(double dx, double dy, double dz, const double f[4], double *D)
+{
+    double x[3] = {dx, dy, dz};
+    for (int g = 0; g < NM; g++) {
+        int e0 = mi_exp[g][0], e1 = mi_exp[g][1], e2 = mi_exp[g][2];
+        int k = mi_order[g];
+        double mono = 1.0;
+        for (int i = 0; i < e0; i++) mono *= x[0];
+        for (int i = 0; i < e1; i++) mono *= x[1];
+        for (int i = 0; i < e2; i++) mono *= x[2];
+        double v = f[k] * mono;
+        if (k >= 2) {
+            int e[3] = {e0, e1, e2};
+            for (int d = 0; d < 3; d++) {
+                if (e[d] < 2) continue;
+                double m2 = (double)(e[d] * (e[d] - 1) / 2);
+                double rest = 1.0;
+                for (int dd = 0; dd < 3; dd++) {
+                    int p = e[dd] - (dd == d ? 2 : 0);
+                    for (int i = 0; i < p; i++) rest *= x[dd];
+                }
+                v += f[k - 1] * m2 * rest;
+            }
+        }
+        D[g] = v;
+    }
+}
+
+/* M2L, src/operator.c:255-392 (d = target centre - source centre):
+   toL_b += sum_{|a| <= 3-|b|} M_a D_(a+b) */
+void po_m2l(double dx, double dy, double dz, const double *M, double *toL, double rs)
+{
+    init_tables();
+    double r = sqrt(dx * dx + dy * dy + dz * dz);
+    double f[4], D[NM];
+    split_factors(r, rs, f);
+    derivative_tensor(dx, dy, dz, f, D);
+    for (int b = 0; b < NM; b++) {
+        double s = 0.0;
+        for (int a = 0; a < NM; a++) {
+            if (mi_order[a] + mi_order[b] > 3) continue;
+            int i0 = mi_exp[a][0] + mi_exp[b][0], i1 = mi_exp[a][1] + mi_exp[b][1],
+                i2 = mi_exp[a][2] + mi_exp[b][2];
+            s += M[a] * D[mi_index[i0][i1][i2]];
+        }
+        toL[b] += s;
+    }
+}
+
+/* L2L, src/operator.c:395-494 (d = child centre - parent centre):
+   toL_b += sum_g L_(b+g) d^g/g!,  |b+g| <= 3 */
+void po_l2l(double dx, double dy, double dz, const double *L, double *toL)
+{
+    init_tables();
+    double mono[NM];
+    scaled_monomials(dx, dy, dz, mono);
+    for (int b = 0; b < NM; b++) {
+        double s = 0.0;
+        for (int g = 0; g < NM; g++) {
+            if (mi_order[b] + mi_order[g] > 3) continue;
+            int i0 = mi_exp[b][0] + mi_exp[g][0], i1 = mi_exp[b][1] + mi_exp[g][1],
+                i2 = mi_exp[b][2] + mi_exp[g][2];
+            s += L[mi_index[i0][i1][i2]] * mono[g];
+        }
+        toL[b] += s;
+    }
+}
+
+/* L2P, src/operator.c:197-251: acc_i += sum_{|g|<=2} L_(e_i+g) d^g/g! */
+void po_l2p(int npart, const double *pos, const double center[3], const double *L, double *acc)
+{
+    init_tables();
+    double mono[NM];
+    for (int p = 0; p < npart; p++) {
+        scaled_monomials(pos[3 * p] - center[0], pos[3 * p + 1] - center[1], pos[3 * p + 2] - center[2], mono);
+        for (int i = 0; i < 3; i++) {
+            double s = 0.0;
+            for (int g = 0; g < NM; g++) {
+                if (mi_order[g] > 2) continue;
+                int e[3] = {mi_exp[g][0], mi_exp[g][1], mi_exp[g][2]};
+                e[i] += 1;
+                s += L[mi_index[e[0]][e[1]][e[2]]] * mono[g];
+            }
+            acc[3 * p + i] += s;
+        }
+    }
+}
+
+/* MAC, src/fmm.c:266-326: 1 accept (M2L), 0 open, -1 drop (LONGSHORT). */
+int po_acceptance(const double wi[3], const double wj[3], const double dist[3], double theta, double rcut)
+{
+    double w[3], gap[3];
+    for (int d = 0; d < 3; d++) w[d] = (wi[d] + wj[d]) * 0.5;
+    double dd2 = dist[0] * dist[0] + dist[1] * dist[1] + dist[2] * dist[2];
+    for (int d = 0; d < 3; d++) {
+        gap[d] = fabs(dist[d]) - w[d];
+        if (gap[d] <= 0.0) gap[d] = 0.0;
+    }
+    if (gap[0] + gap[1] + gap[2] < 0.0001) return 0;          /* touching boxes */
+    double dm2 = gap[0] * gap[0] + gap[1] * gap[1] + gap[2] * gap[2];
+    double c2 = rcut * rcut;
+    if (dm2 >= c2) return -1;                                  /* beyond the cutoff */
+    if (dd2 > c2) return 0;
+    double wmax = w[0];
+    if (w[1] > wmax) wmax = w[1];
+    if (w[2] > wmax) wmax = w[2];
+    wmax *= 2;
+    return (wmax * wmax < theta * theta * dd2) ? 1 : 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* state                                                               */
+/* ------------------------------------------------------------------ */
+typedef struct { int npart, ipart; double width[3], center[3], M[NM], L[NM]; } o_leaf;
+typedef struct { int npart, son[2]; double split, width[3], center[3], M[NM], L[NM]; } o_node;
+typedef struct { int *t, *s, *img; long n, cap; } o_list;
+
+struct po_state {
+    po_params p;
+    int n, nleaf_cap, nnode_cap, nleaf, nnode;
+    int first_leaf, first_node;
+    double *pos;      /* tree order, n*3 */
+    int *perm;
+    double *acc, *acc_task;
+    o_leaf *leaf;
+    o_node *node;
+    o_list list[4];
+    long long walk_m2l_count, p2p_count_remote;
+    int err;
+    /* per-image pruning: son[] of the exported copy (-1 when pruned) */
+    double shift[3];
+    int image;
+    int capture;
+};
+
+po_state *po_create(void)
+{
+    init_tables();
+    return (po_state *)calloc(1, sizeof(po_state));
+}
+
+static void free_run(po_state *s)
+{
+    free(s->pos); free(s->perm); free(s->acc); free(s->acc_task);
+    free(s->leaf); free(s->node);
+    s->pos = 0; s->perm = 0; s->acc = 0; s->acc_task = 0; s->leaf = 0; s->node = 0;
+}
+
+void po_destroy(po_state *s)
+{
+    if (!s) return;
+    free_run(s);
+    for (int k = 0; k < 4; k++) { free(s->list[k].t); free(s->list[k].s); free(s->list[k].img); }
+    free(s);
+}
+
+static int list_push(o_list *l, int t, int src, int img)
+{
+    if (l->n == l->cap) {
+        long cap = l->cap ? 2 * l->cap : 1 << 16;
+        int *a = realloc(l->t, sizeof(int) * cap), *b, *c;
+        if (!a) return -1;
+        l->t = a;
+        b = realloc(l->s, sizeof(int) * cap);
+        if (!b) return -1;
+        l->s = b;
+        c = realloc(l->img, sizeof(int) * cap);
+        if (!c) return -1;
+        l->img = c;
+        l->cap = cap;
+    }
+    l->t[l->n] = t; l->s[l->n] = src; l->img[l->n] = img; l->n++;
+    return 0;
+}
+
+#define IS_LEAF(S, id) ((id) < (S)->first_node)
+#define LEAF(S, id) (&(S)->leaf[(id) - (S)->first_leaf])
+#define NODE(S, id) (&(S)->node[(id) - (S)->first_node])
+
+/* ------------------------------------------------------------------ */
+/* kd-tree                                                             */
+/* ------------------------------------------------------------------ */
+static void swap_part(po_state *s, int i, int j)
+{
+    double t[3];
+    memcpy(t, s->pos + 3 * i, sizeof t);
+    memcpy(s->pos + 3 * i, s->pos + 3 * j, sizeof t);
+    memcpy(s->pos + 3 * j, t, sizeof t);
+    int q = s->perm[i]; s->perm[i] = s->perm[j]; s->perm[j] = q;
+}
+
+/*
+ * Mean split of a segment along axis D, src/fmm.c:30-78.  Segments of
+ * fewer than two particles go wholly to the upper side; a pair splits at
+ * its midpoint, ordered.  Otherwise the mean is a sequential sum divided by
+ * the count and the partition is the reference's two-ended swap: scanning
+ * upward, each particle above the mean is exchanged with the next particle
+ * (from the top) that is not above it; the lower part ends where the top
+ * scan stopped.
+ */
+static void mean_split(po_state *s, int D, int start, int length, int cnt[2], double *split)
+{
+    double *x = s->pos;
+    cnt[0] = cnt[1] = 0;
+    if (length < 2) { cnt[1] = length; return; }
+    if (length == 2) {
+        cnt[0] = cnt[1] = 1;
+        double a = x[3 * start + D], b = x[3 * (start + 1) + D];
+        *split = 0.5 * (a + b);
+        if (a > b) swap_part(s, start, start + 1);
+        return;
+    }
+    double sum = 0.0;
+    for (int i = 0; i < length; i++) sum += x[3 * (start + i) + D];
+    double mean = sum / (double)length;
+    int top = length - 1;
+    for (int i = 0; i < top; i++) {
+        if (x[3 * (start + i) + D] > mean) {
+            while (top > i && x[3 * (start + top) + D] > mean) top--;
+            swap_part(s, start + i, start + top);
+        }
+    }
+    cnt[0] = top;
+    cnt[1] = length - top;
+    *split = mean;
+}
+
+/* src/fmm.c:81-120: depth-first build; leaves numbered as met, nodes preorder */
+static void build(po_state *s, int D, int start, int length, int id, int *last_leaf, int *last_node)
+{
+    if (s->err || length == 0) return;
+    o_node *nd = NODE(s, id);
+    nd->npart = length;
+    int cnt[2];
+    double split = 0.0;
+    mean_split(s, D, start, length, cnt, &split);
+    nd->split = split;
+    int ip = start;
+    for (int c = 0; c < 2; c++) {
+        if (cnt[c] <= s->p.maxleaf) {
+            if (*last_leaf - s->first_leaf >= s->nleaf_cap) { s->err = PO_ERR_LEAF_CAPACITY; return; }
+            o_leaf *lf = LEAF(s, *last_leaf);
+            lf->npart = cnt[c];
+            lf->ipart = ip;
+            nd->son[c] = *last_leaf;
+            (*last_leaf)++;
+        } else {
+            (*last_node)++;
+            if (*last_node - s->first_node >= s->nnode_cap) { s->err = PO_ERR_NODE_CAPACITY; return; }
+            nd->son[c] = *last_node;
+            build(s, (D + 1) % 3, ip, cnt[c], *last_node, last_leaf, last_node);
+            nd = NODE(s, id);
+        }
+        ip += cnt[c];
+    }
+}
+
+/* src/fmm.c:123-177: boxes from the split planes */
+static void geometry(po_state *s, int D, int id, double lo[3], double hi[3])
+{
+    o_node *nd = NODE(s, id);
+    for (int d = 0; d < 3; d++) {
+        nd->width[d] = hi[d] - lo[d];
+        nd->center[d] = 0.5 * (hi[d] + lo[d]);
+    }
+    int nD = (D + 1) % 3;
+    for (int c = 0; c < 2; c++) {
+        int ch = nd->son[c];
+        if (IS_LEAF(s, ch)) {
+            o_leaf *lf = LEAF(s, ch);
+            memcpy(lf->width, nd->width, sizeof lf->width);
+            memcpy(lf->center, nd->center, sizeof lf->center);
+            if (c == 0) {
+                lf->width[D] = nd->split - lo[D];
+                lf->center[D] = 0.5 * (lo[D] + nd->split);
+            } else {
+                lf->width[D] = hi[D] - nd->split;
+                lf->center[D] = 0.5 * (hi[D] + nd->split);
+            }
+        } else if (c == 0) {
+            double keep = hi[D];
+            hi[D] = nd->split;
+            geometry(s, nD, ch, lo, hi);
+            hi[D] = keep;
+        } else {
+            double keep = lo[D];
+            lo[D] = nd->split;
+            geometry(s, nD, ch, lo, hi);
+            lo[D] = keep;
+        }
+    }
+}
+
+/* src/operator.c:165-194: multipoles, children in order */
+static void upward(po_state *s, int id)
+{
+    o_node *nd = NODE(s, id);
+    for (int c = 0; c < 2; c++) {
+        int ch = nd->son[c];
+        if (IS_LEAF(s, ch)) {
+            o_leaf *lf = LEAF(s, ch);
+            po_m2m(nd->center[0] - lf->center[0], nd->center[1] - lf->center[1], nd->center[2] - lf->center[2],
+                   lf->M, nd->M);
+        } else {
+            upward(s, ch);
+            o_node *cn = NODE(s, ch);
+            po_m2m(nd->center[0] - cn->center[0], nd->center[1] - cn->center[1], nd->center[2] - cn->center[2],
+                   cn->M, nd->M);
+        }
+    }
+}
+
+/* src/operator.c:498-528: local expansions pushed to children */
+static void downward(po_state *s, int id)
+{
+    o_node *nd = NODE(s, id);
+    for (int c = 0; c < 2; c++) {
+        int ch = nd->son[c];
+        if (!IS_LEAF(s, ch)) {
+            o_node *cn = NODE(s, ch);
+            po_l2l(cn->center[0] - nd->center[0], cn->center[1] - nd->center[1], cn->center[2] - nd->center[2],
+                   nd->L, cn->L);
+            downward(s, ch);
+        } else {
+            o_leaf *lf = LEAF(s, ch);
+            po_l2l(lf->center[0] - nd->center[0], lf->center[1] - nd->center[1], lf->center[2] - nd->center[2],
+                   nd->L, lf->L);
+        }
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* dual-tree walks                                                     */
+/* ------------------------------------------------------------------ */
+static const double *geom_center(po_state *s, int id)
+{
+    return IS_LEAF(s, id) ? LEAF(s, id)->center : NODE(s, id)->center;
+}
+static const double *geom_width(po_state *s, int id)
+{
+    return IS_LEAF(s, id) ? LEAF(s, id)->width : NODE(s, id)->width;
+}
+static double wsum(const double *w) { return w[0] + w[1] + w[2]; }
+
+static void emit(po_state *s, int kind, int t, int src)
+{
+    if (s->err) return;
+    if (kind == PO_LIST_M2L || kind == PO_LIST_M2L_EXT) s->walk_m2l_count++;
+    if (list_push(&s->list[kind], t, src, s->image) != 0) s->err = PO_ERR_NOMEM;
+}
+
+/*
+ * Local walk, src/fmm.c:406-538 (P2P) and src/fmm.c:569-712 (M2L) -- one
+ * traversal, since both walks make identical decisions and differ only in
+ * what they record: a leaf pair (or a leaf with itself) is a P2P task, an
+ * accepted pair is an M2L task.  Node pairs that must be opened open the
+ * side with the larger width sum (the source side on ties).
+ */
+static void walk_local(po_state *s, int im, int jm)
+{
+    if (s->err || im < 0 || jm < 0) return;
+    int il = IS_LEAF(s, im), jl = IS_LEAF(s, jm);
+    if (im == jm) {
+        if (il) { emit(s, PO_LIST_P2P, im, jm); return; }
+        o_node *a = NODE(s, im);
+        walk_local(s, a->son[0], a->son[0]);
+        walk_local(s, a->son[0], a->son[1]);
+        walk_local(s, a->son[1], a->son[0]);
+        walk_local(s, a->son[1], a->son[1]);
+        return;
+    }
+    if (il && jl) { emit(s, PO_LIST_P2P, im, jm); return; }
+    const double *ci = geom_center(s, im), *cj = geom_center(s, jm);
+    double dist[3] = {ci[0] - cj[0], ci[1] - cj[1], ci[2] - cj[2]};
+    /* the reference passes the leaf's width first in mixed pairs */
+    int flag = jl ? po_acceptance(geom_width(s, jm), geom_width(s, im), dist, s->p.theta, s->p.rcut)
+                  : po_acceptance(geom_width(s, im), geom_width(s, jm), dist, s->p.theta, s->p.rcut);
+    if (flag == -1) return;
+    if (flag == 1) { emit(s, PO_LIST_M2L, im, jm); return; }
+    int open_target;
+    if (il) open_target = 0;
+    else if (jl) open_target = 1;
+    else open_target = wsum(NODE(s, im)->width) > wsum(NODE(s, jm)->width);
+    if (open_target) {
+        o_node *a = NODE(s, im);
+        walk_local(s, a->son[0], jm);
+        walk_local(s, a->son[1], jm);
+    } else {
+        o_node *b = NODE(s, jm);
+        walk_local(s, im, b->son[0]);
+        walk_local(s, im, b->son[1]);
+    }
+}
+
+/*
+ * The exported (image) tree, src/remotes.c:60-169: the local tree shifted
+ * by s->shift, with the children of an internal node dropped ("pruned")
+ * when its shifted box is at least rcut from the receiving domain's box, or
+ * when its largest width is below 0.95 theta times that distance.  Leaves
+ * always ship their bodies.  The export is not materialised here: a node
+ * of the image tree is a local node plus the shift, and its pruning is
+ * evaluated where the walk needs it.  At one rank the receiving domain is
+ * the local domain (toptree[0] after connect_local_toptree, i.e. the root
+ * box).
+ */
+static int image_pruned(po_state *s, int id)
+{
+    o_node *nd = NODE(s, id);
+    o_node *root = NODE(s, s->first_node);
+    double dr = 0.0;
+    for (int d = 0; d < 3; d++) {
+        double g = root->center[d] - nd->center[d] - s->shift[d];
+        if (g < 0.0) g = -g;
+        g -= (root->width[d] + nd->width[d]) * 0.5;
+        if (g > 0.0) dr += g * g;
+    }
+    dr = sqrt(dr);
+    double wmax = nd->width[0];
+    if (wmax < nd->width[1]) wmax = nd->width[1];
+    if (wmax < nd->width[2]) wmax = nd->width[2];
+    if (dr >= s->p.rcut) return 1;
+    return wmax < 0.95 * s->p.theta * dr;
+}
+
+/* src/remotes.c:213-372 (P2P) and 405-552 (M2L), one traversal.  The
+   received node is a leaf iff it holds <= MAXLEAF particles; pruned
+   received nodes are interacted by M2L unless dropped. */
+static void walk_image(po_state *s, int im, int jm)
+{
+    if (s->err) return;
+    int il = IS_LEAF(s, im);
+    int jl = IS_LEAF(s, jm);
+    if (il && jl) { emit(s, PO_LIST_P2P_EXT, im, jm); return; }
+    const double *ci = geom_center(s, im), *cj = geom_center(s, jm);
+    double cjs[3] = {cj[0] + s->shift[0], cj[1] + s->shift[1], cj[2] + s->shift[2]};
+    double dist[3] = {ci[0] - cjs[0], ci[1] - cjs[1], ci[2] - cjs[2]};
+    int flag = po_acceptance(geom_width(s, im), geom_width(s, jm), dist, s->p.theta, s->p.rcut);
+    if (flag == -1) return;
+    int pruned = jl ? 0 : image_pruned(s, jm);
+    if (il) {
+        if (flag == 1 || pruned) { emit(s, PO_LIST_M2L_EXT, im, jm); return; }
+        o_node *b = NODE(s, jm);
+        walk_image(s, im, b->son[0]);
+        walk_image(s, im, b->son[1]);
+        return;
+    }
+    if (flag == 1) { emit(s, PO_LIST_M2L_EXT, im, jm); return; }
+    int open_target = jl || pruned || wsum(NODE(s, im)->width) > wsum(NODE(s, jm)->width);
+    if (open_target) {
+        o_node *a = NODE(s, im);
+        walk_image(s, a->son[0], jm);
+        walk_image(s, a->son[1], jm);
+    } else {
+        o_node *b = NODE(s, jm);
+        walk_image(s, im, b->son[0]);
+        walk_image(s, im, b->son[1]);
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* pair kernel and list compute                                        */
+/* ------------------------------------------------------------------ */
+/* Softened, erfc-truncated pair force of src/fmm.c:834-852 and
+   src/remotes.c:30-50, in the same operation order. */
+static inline void pair_force(const double *pj, const double *pi, const po_params *p, double coeff, double *a)
+{
+    double dx0 = pj[0] - pi[0], dx1 = pj[1] - pi[1], dx2 = pj[2] - pi[2];
+    double dr = sqrt(dx0 * dx0 + dx1 * dx1 + dx2 * dx2);
+    double ir3 = (dr < p->eps) ? p->mass / (p->eps * p->eps * p->eps) : p->mass / (dr * dr * dr);
+    double drs = 0.5 * dr / p->rs;
+    ir3 *= (erfc(drs) + coeff * drs * exp(-drs * drs));
+    a[0] += dx0 * ir3;
+    a[1] += dx1 * ir3;
+    a[2] += dx2 * ir3;
+}
+
+/* stable grouping of a list by target (counting sort) */
+static int group_by_target(const o_list *l, int first_id, int nid, long **off_out, long **order_out)
+{
+    long *off = calloc((size_t)nid + 1, sizeof(long));
+    long *order = malloc(sizeof(long) * (l->n ? l->n : 1));
+    if (!off || !order) { free(off); free(order); return -1; }
+    for (long i = 0; i < l->n; i++) off[l->t[i] - first_id + 1]++;
+    for (int i = 0; i < nid; i++) off[i + 1] += off[i];
+    long *fill = malloc(sizeof(long) * ((size_t)nid + 1));
+    if (!fill) { free(off); free(order); return -1; }
+    memcpy(fill, off, sizeof(long) * ((size_t)nid + 1));
+    for (long i = 0; i < l->n; i++) order[fill[l->t[i] - first_id]++] = i;
+    free(fill);
+    *off_out = off;
+    *order_out = order;
+    return 0;
+}
+
+typedef struct {
+    po_state *s;
+    long *off, *order;      /* grouped P2P list */
+    const o_list *l;
+    int ext;                /* 0: local tasks, 1: image tasks */
+    int next;
+    pthread_mutex_t mu;
+} p2p_job;
+
+/* Per target leaf, in list order.  Local tasks sum each task separately and
+   then add it (src/fmm.c:823-868); image tasks add pair by pair
+   (src/remotes.c:26-56). */
+static void p2p_target(p2p_job *J, int lf_index)
+{
+    po_state *s = J->s;
+    const po_params *p = &s->p;
+    double coeff = 2.0 / sqrt(M_PI);
+    o_leaf *T = &s->leaf[lf_index];
+    for (long k = J->off[lf_index]; k < J->off[lf_index + 1]; k++) {
+        long e = J->order[k];
+        o_leaf *S = LEAF(s, J->l->s[e]);
+        if (!J->ext) {
+            for (int q = 0; q < T->npart; q++) {
+                int ip = T->ipart + q;
+                double a[3] = {0, 0, 0};
+                for (int jp = S->ipart; jp < S->ipart + S->npart; jp++) {
+                    if (jp == ip) continue;
+                    pair_force(s->pos + 3 * jp, s->pos + 3 * ip, p, coeff, a);
+                }
+                for (int d = 0; d < 3; d++) s->acc[3 * ip + d] += a[d];
+            }
+        } else {
+            int img = J->l->img[e];
+            double sh[3];
+            int c = 0;
+            for (int mi = -1; mi <= 1; mi++)
+                for (int mj = -1; mj <= 1; mj++)
+                    for (int mk = -1; mk <= 1; mk++) {
+                        if (mi == 0 && mj == 0 && mk == 0) continue;
+                        if (++c == img) { sh[0] = mi * p->boxsize; sh[1] = mj * p->boxsize; sh[2] = mk * p->boxsize; }
+                    }
+            for (int ip = T->ipart; ip < T->ipart + T->npart; ip++)
+                for (int jp = S->ipart; jp < S->ipart + S->npart; jp++) {
+                    double pj[3] = {s->pos[3 * jp] + sh[0], s->pos[3 * jp + 1] + sh[1], s->pos[3 * jp + 2] + sh[2]};
+                    pair_force(pj, s->pos + 3 * ip, p, coeff, s->acc + 3 * ip);
+                }
+        }
+    }
+}
+
+static void *p2p_worker(void *arg)
+{
+    p2p_job *J = arg;
+    for (;;) {
+        pthread_mutex_lock(&J->mu);
+        int i = J->next;
+        J->next += 16;
+        pthread_mutex_unlock(&J->mu);
+        if (i >= J->s->nleaf) break;
+        int e = i + 16 < J->s->nleaf ? i + 16 : J->s->nleaf;
+        for (; i < e; i++) p2p_target(J, i);
+    }
+    return 0;
+}
+
+static int run_p2p(po_state *s, const o_list *l, int ext)
+{
+    p2p_job J;
+    memset(&J, 0, sizeof J);
+    J.s = s; J.l = l; J.ext = ext;
+    if (group_by_target(l, s->first_leaf, s->nleaf, &J.off, &J.order) != 0) return PO_ERR_NOMEM;
+    pthread_mutex_init(&J.mu, 0);
+    int nt = s->p.nthreads > 1 ? s->p.nthreads : 1;
+    if (nt == 1) {
+        p2p_worker(&J);
+    } else {
+        pthread_t *th = malloc(sizeof(pthread_t) * nt);
+        for (int i = 0; i < nt; i++) pthread_create(&th[i], 0, p2p_worker, &J);
+        for (int i = 0; i < nt; i++) pthread_join(th[i], 0);
+        free(th);
+    }
+    pthread_mutex_destroy(&J.mu);
+    free(J.off);
+    free(J.order);
+    return PO_OK;
+}
+
+static void image_shift(const po_params *p, int img, double sh[3])
+{
+    int c = 0;
+    for (int mi = -1; mi <= 1; mi++)
+        for (int mj = -1; mj <= 1; mj++)
+            for (int mk = -1; mk <= 1; mk++) {
+                if (mi == 0 && mj == 0 && mk == 0) continue;
+                if (++c == img) { sh[0] = mi * p->boxsize; sh[1] = mj * p->boxsize; sh[2] = mk * p->boxsize; }
+            }
+}
+
+/* src/fmm.c:875-907 and src/remotes.c:598-628, in list order */
+static void run_m2l(po_state *s, const o_list *l)
+{
+    for (long e = 0; e < l->n; e++) {
+        int im = l->t[e], jm = l->s[e];
+        double sh[3] = {0, 0, 0};
+        if (l->img[e]) image_shift(&s->p, l->img[e], sh);
+        const double *cj = geom_center(s, jm);
+        double cjs[3] = {cj[0] + sh[0], cj[1] + sh[1], cj[2] + sh[2]};
+        const double *ci = geom_center(s, im);
+        const double *M = IS_LEAF(s, jm) ? LEAF(s, jm)->M : NODE(s, jm)->M;
+        double *L = IS_LEAF(s, im) ? LEAF(s, im)->L : NODE(s, im)->L;
+        if (l->img[e])
+            po_m2l(ci[0] - cjs[0], ci[1] - cjs[1], ci[2] - cjs[2], M, L, s->p.rs);
+        else
+            po_m2l(ci[0] - cj[0], ci[1] - cj[1], ci[2] - cj[2], M, L, s->p.rs);
+    }
+}
+
+static double wall(void)
+{
+    struct timeval tv;
+    gettimeofday(&tv, 0);
+    return tv.tv_sec + 1e-6 * tv.tv_usec;
+}
+
+/* the whole pass: src/fmm.c:329-360 (construct), 719-770 (prepare),
+   909-984 (task), 987-1075 (ext) at one rank */
+int po_run(po_state *s, const po_params *p, int n, const double *pos_in, double *seconds)
+{
+    init_tables();
+    if (!s || !p || n < 1 || p->maxleaf < 1) return PO_ERR_ARG;
+    if (n <= p->maxleaf) return PO_ERR_SMALL;
+    free_run(s);
+    for (int k = 0; k < 4; k++) s->list[k].n = 0;
+    s->p = *p;
+    s->n = n;
+    s->err = 0;
+    s->walk_m2l_count = 0;
+    s->p2p_count_remote = 0;
+
+    s->pos = malloc(sizeof(double) * 3 * (size_t)n);
+    s->perm = malloc(sizeof(int) * (size_t)n);
+    s->acc = calloc(3 * (size_t)n, sizeof(double));
+    s->acc_task = calloc(3 * (size_t)n, sizeof(double));
+    /* capacity rule of src/fmm.c:203-209 */
+    int cap = (int)(2.0 * ((double)n) / ((double)p->maxleaf));
+    if (cap > n) cap = n + 1;
+    s->nleaf_cap = s->nnode_cap = cap;
+    s->leaf = calloc((size_t)cap, sizeof(o_leaf));
+    s->node = calloc((size_t)cap, sizeof(o_node));
+    if (!s->pos || !s->perm || !s->acc || !s->acc_task || !s->leaf || !s->node) return PO_ERR_NOMEM;
+    for (int i = 0; i < cap; i++) s->node[i].son[0] = s->node[i].son[1] = -1;
+    memcpy(s->pos, pos_in, sizeof(double) * 3 * (size_t)n);
+    for (int i = 0; i < n; i++) s->perm[i] = i;
+
+    double t0 = wall();
+    s->first_leaf = n;
+    s->first_node = n + cap;
+    int last_leaf = s->first_leaf, last_node = s->first_node;
+    build(s, 0, 0, n, s->first_node, &last_leaf, &last_node);
+    if (s->err) return s->err;
+    s->nleaf = last_leaf - s->first_leaf;
+    s->nnode = last_node - s->first_node + 1;
+    double lo[3] = {0, 0, 0}, hi[3] = {p->boxsize, p->boxsize, p->boxsize};
+    geometry(s, 0, s->first_node, lo, hi);
+    for (int i = 0; i < s->nleaf; i++) {
+        o_leaf *lf = &s->leaf[i];
+        po_p2m(lf->npart, s->pos + 3 * lf->ipart, p->mass, lf->center, lf->M);
+    }
+    upward(s, s->first_node);
+
+    s->image = 0;
+    walk_local(s, s->first_node, s->first_node);
+    if (s->err) return s->err;
+    int rc = run_p2p(s, &s->list[PO_LIST_P2P], 0);
+    if (rc) return rc;
+    run_m2l(s, &s->list[PO_LIST_M2L]);
+    memcpy(s->acc_task, s->acc, sizeof(double) * 3 * (size_t)n);
+
+    if (p->images) {
+        long start_p2p = s->list[PO_LIST_P2P_EXT].n;
+        long start_m2l = s->list[PO_LIST_M2L_EXT].n;
+        for (int img = 1; img < NIMG; img++) {
+            s->image = img;
+            image_shift(p, img, s->shift);
+            walk_image(s, s->first_node, s->first_node);
+            if (s->err) return s->err;
+        }
+        (void)start_p2p; (void)start_m2l;
+        o_list *pe = &s->list[PO_LIST_P2P_EXT];
+        for (long e = 0; e < pe->n; e++)
+            s->p2p_count_remote += (long long)LEAF(s, pe->t[e])->npart * LEAF(s, pe->s[e])->npart;
+        rc = run_p2p(s, pe, 1);
+        if (rc) return rc;
+        run_m2l(s, &s->list[PO_LIST_M2L_EXT]);
+    }
+    downward(s, s->first_node);
+    for (int i = 0; i < s->nleaf; i++) {
+        o_leaf *lf = &s->leaf[i];
+        po_l2p(lf->npart, s->pos + 3 * lf->ipart, lf->center, lf->L, s->acc + 3 * lf->ipart);
+    }
+    if (seconds) *seconds = wall() - t0;
+    return PO_OK;
+}
+
+void po_counters(const po_state *s, long long *c)
+{
+    c[0] = s->list[PO_LIST_P2P].n;
+    c[1] = s->list[PO_LIST_M2L].n;
+    c[2] = s->walk_m2l_count;
+    c[3] = s->p2p_count_remote;
+    c[4] = s->nleaf_cap;
+    c[5] = s->nnode_cap;
+    c[6] = s->nleaf;
+    c[7] = s->nnode;
+    c[8] = s->first_leaf;
+    c[9] = s->first_node;
+    c[10] = 0;
+    c[11] = s->list[PO_LIST_P2P].n;
+    c[12] = s->list[PO_LIST_M2L].n;
+    c[13] = s->list[PO_LIST_P2P_EXT].n;
+    c[14] = s->list[PO_LIST_M2L_EXT].n;
+    c[15] = s->p.images ? NIMG - 1 : 0;
+}
+
+void po_particles(const po_state *s, double *pos, double *acc_task, double *acc, int *perm)
+{
+    size_t b = sizeof(double) * 3 * (size_t)s->n;
+    if (pos) memcpy(pos, s->pos, b);
+    if (acc_task) memcpy(acc_task, s->acc_task, b);
+    if (acc) memcpy(acc, s->acc, b);
+    if (perm) memcpy(perm, s->perm, sizeof(int) * (size_t)s->n);
+}
+
+long po_list_size(const po_state *s, int kind) { return (kind >= 0 && kind < 4) ? s->list[kind].n : -1; }
+
+void po_list_copy(const po_state *s, int kind, int *t, int *src, int *img)
+{
+    const o_list *l = &s->list[kind];
+    memcpy(t, l->t, sizeof(int) * l->n);
+    memcpy(src, l->s, sizeof(int) * l->n);
+    memcpy(img, l->img, sizeof(int) * l->n);
+}
+
+void po_copy_leaves(const po_state *s, int *ip_np, double *geom, double *M, double *L)
+{
+    for (int i = 0; i < s->nleaf; i++) {
+        const o_leaf *p = &s->leaf[i];
+        ip_np[2 * i] = p->ipart; ip_np[2 * i + 1] = p->npart;
+        for (int d = 0; d < 3; d++) { geom[6 * i + d] = p->center[d]; geom[6 * i + 3 + d] = p->width[d]; }
+        memcpy(M + NM * i, p->M, sizeof p->M);
+        memcpy(L + NM * i, p->L, sizeof p->L);
+    }
+}
+
+void po_copy_nodes(const po_state *s, int *info, double *geom, double *M, double *L)
+{
+    for (int i = 0; i < s->nnode; i++) {
+        const o_node *p = &s->node[i];
+        info[3 * i] = p->npart; info[3 * i + 1] = p->son[0]; info[3 * i + 2] = p->son[1];
+        geom[7 * i] = p->split;
+        for (int d = 0; d < 3; d++) { geom[7 * i + 1 + d] = p->center[d]; geom[7 * i + 4 + d] = p->width[d]; }
+        memcpy(M + NM * i, p->M, sizeof p->M);
+        memcpy(L + NM * i, p->L, sizeof p->L);
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* FP64 direct sum (error oracle)                                      */
+/* ------------------------------------------------------------------ */
+typedef struct {
+    const po_params *p;
+    int n, nt;
+    const double *pos;
+    const int *targets;
+    double rmax;
+    double *acc;
+    int ncell;
+    double cell;
+    const int *head, *next;
+    int cursor;
+    pthread_mutex_t mu;
+} ds_job;
+
+static inline double min_image(double d, double L)
+{
+    if (d > 0.5 * L) d -= L;
+    else if (d < -0.5 * L) d += L;
+    return d;
+}
+
+static void ds_one(ds_job *J, int t)
+{
+    const po_params *p = J->p;
+    int i = J->targets[t];
+    const double *pi = J->pos + 3 * i;
+    double coeff = 2.0 / sqrt(M_PI), L = p->boxsize, r2max = J->rmax * J->rmax;
+    double a[3] = {0, 0, 0};
+    int ci[3];
+    for (int d = 0; d < 3; d++) {
+        ci[d] = (int)(pi[d] / J->cell);
+        if (ci[d] >= J->ncell) ci[d] = J->ncell - 1;
+        if (ci[d] < 0) ci[d] = 0;
+    }
+    int span = J->ncell >= 3 ? 1 : 0;
+    int lo = J->ncell >= 3 ? -1 : 0, hi = J->ncell >= 3 ? 1 : 0;
+    (void)span;
+    if (J->ncell < 3) { lo = 0; hi = 0; }
+    for (int ox = lo; ox <= hi; ox++)
+        for (int oy = lo; oy <= hi; oy++)
+            for (int oz = lo; oz <= hi; oz++) {
+                int cx = (ci[0] + ox + J->ncell) % J->ncell, cy = (ci[1] + oy + J->ncell) % J->ncell,
+                    cz = (ci[2] + oz + J->ncell) % J->ncell;
+                int c = (cx * J->ncell + cy) * J->ncell + cz;
+                if (J->ncell < 3) c = -1;
+                int j = (c >= 0) ? J->head[c] : 0;
+                for (; (c >= 0) ? (j >= 0) : (j < J->n); j = (c >= 0) ? J->next[j] : j + 1) {
+                    if (j == i) continue;
+                    const double *pj = J->pos + 3 * j;
+                    double dx0 = min_image(pj[0] - pi[0], L), dx1 = min_image(pj[1] - pi[1], L),
+                           dx2 = min_image(pj[2] - pi[2], L);
+                    double r2 = dx0 * dx0 + dx1 * dx1 + dx2 * dx2;
+                    if (r2 >= r2max) continue;
+                    double dr = sqrt(r2);
+                    double ir3 = (dr < p->eps) ? p->mass / (p->eps * p->eps * p->eps) : p->mass / (dr * dr * dr);
+                    double drs = 0.5 * dr / p->rs;
+                    ir3 *= (erfc(drs) + coeff * drs * exp(-drs * drs));
+                    a[0] += dx0 * ir3; a[1] += dx1 * ir3; a[2] += dx2 * ir3;
+                }
+            }
+    for (int d = 0; d < 3; d++) J->acc[3 * t + d] = a[d];
+}
+
+static void *ds_worker(void *arg)
+{
+    ds_job *J = arg;
+    for (;;) {
+        pthread_mutex_lock(&J->mu);
+        int t = J->cursor;
+        J->cursor += 8;
+        pthread_mutex_unlock(&J->mu);
+        if (t >= J->nt) break;
+        int e = t + 8 < J->nt ? t + 8 : J->nt;
+        for (; t < e; t++) ds_one(J, t);
+    }
+    return 0;
+}
+
+int po_direct_sum(const po_params *p, int n, const double *pos, int nt, const int *targets, double rmax,
+                  double *acc_out)
+{
+    if (!p || n < 1 || nt < 0 || rmax <= 0) return PO_ERR_ARG;
+    ds_job J;
+    memset(&J, 0, sizeof J);
+    J.p = p; J.n = n; J.nt = nt; J.pos = pos; J.targets = targets; J.rmax = rmax; J.acc = acc_out;
+    int ncell = (int)(p->boxsize / rmax);
+    if (ncell > 256) ncell = 256;
+    if (ncell < 1) ncell = 1;
+    J.ncell = ncell;
+    J.cell = p->boxsize / ncell;
+    int *head = NULL, *next = NULL;
+    if (ncell >= 3) {
+        head = malloc(sizeof(int) * (size_t)ncell * ncell * ncell);
+        next = malloc(sizeof(int) * (size_t)n);
+        if (!head || !next) { free(head); free(next); return PO_ERR_NOMEM; }
+        for (long c = 0; c < (long)ncell * ncell * ncell; c++) head[c] = -1;
+        for (int j = n - 1; j >= 0; j--) {
+            int cc[3];
+            for (int d = 0; d < 3; d++) {
+                cc[d] = (int)(pos[3 * j + d] / J.cell);
+                if (cc[d] >= ncell) cc[d] = ncell - 1;
+                if (cc[d] < 0) cc[d] = 0;
+            }
+            int c = (cc[0] * ncell + cc[1]) * ncell + cc[2];
+            next[j] = head[c];
+            head[c] = j;
+        }
+    }
+    J.head = head; J.next = next;
+    pthread_mutex_init(&J.mu, 0);
+    int nth = p->nthreads > 1 ? p->nthreads : 1;
+    if (nth == 1) ds_worker(&J);
+    else {
+        pthread_t *th = malloc(sizeof(pthread_t) * nth);
+        for (int i = 0; i < nth; i++) pthread_create(&th[i], 0, ds_worker, &J);
+        for (int i = 0; i < nth; i++) pthread_join(th[i], 0);
+        free(th);
+    }
+    pthread_mutex_destroy(&J.mu);
+    free(head);
+    free(next);
+    return PO_OK;
+}

@@ -1,0 +1,79 @@
+/*
+ * CPU restatement of the photoNs-2.0 FMM short-range force pass.
+ * TEST INFRASTRUCTURE ONLY (the oracle): used by tests/, by
+ * __graft_entry__.smoke() as the checker, and by bench.py's CPU-baseline
+ * leg.  The product never links it.
+ *
+ * Pinned against the reference sources compiled in place
+ * (oracle/_ref/libphotons_ref.so) and the fixtures in tests/golden/.
+ */
+#ifndef PHOTONS_ORACLE_H
+#define PHOTONS_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PO_NMULTI 20
+
+typedef struct {
+    double boxsize;   /* periodic box side (BOXSIZE) */
+    double theta;     /* opening angle (open_angle) */
+    double rs;        /* split radius (splitRadius) */
+    double rcut;      /* cutoff radius (cutoffRadius) */
+    double eps;       /* softening length (SoftenScale) */
+    double mass;      /* particle mass (MASSPART) */
+    int maxleaf;      /* MAXLEAF */
+    int nthreads;     /* compute threads (>=1) */
+    int capture;      /* keep the interaction lists for inspection */
+    int images;       /* 1: 26 periodic images (PERIODIC_CONDITION), 0: none */
+} po_params;
+
+enum { PO_LIST_P2P = 0, PO_LIST_M2L = 1, PO_LIST_P2P_EXT = 2, PO_LIST_M2L_EXT = 3 };
+
+enum {
+    PO_OK = 0,
+    PO_ERR_ARG = 1,
+    PO_ERR_NOMEM = 2,
+    PO_ERR_LEAF_CAPACITY = 3,   /* more leaves than 2N/MAXLEAF (reference writes past its array) */
+    PO_ERR_NODE_CAPACITY = 4,
+    PO_ERR_SMALL = 5            /* N <= MAXLEAF: the reference's image walk reads undefined memory */
+};
+
+typedef struct po_state po_state;
+
+po_state *po_create(void);
+void po_destroy(po_state *s);
+
+/* One force pass.  Returns PO_OK or an error code; *seconds = wall time. */
+int po_run(po_state *s, const po_params *p, int n, const double *pos_in, double *seconds);
+
+/* counters[16]: idxP2P, idxM2L, walk_m2l_count, p2p_count_remote, NLEAF, NNODE,
+   nleaf, nnode, first_leaf, first_node, direct_local_start(0), n_p2p, n_m2l,
+   n_p2p_ext, n_m2l_ext, n_images, in the reference's index space. */
+void po_counters(const po_state *s, long long *counters);
+/* tree-ordered positions, accelerations after the local task phase and after
+   the full pass, and perm[i] = input index of the particle at position i. */
+void po_particles(const po_state *s, double *pos, double *acc_task, double *acc, int *perm);
+long po_list_size(const po_state *s, int kind);
+void po_list_copy(const po_state *s, int kind, int *target, int *source, int *image);
+void po_copy_leaves(const po_state *s, int *ip_np, double *geom, double *M, double *L);
+void po_copy_nodes(const po_state *s, int *info, double *geom, double *M, double *L);
+
+/* scalar operators with the reference's conventions (operator.c) */
+void po_p2m(int npart, const double *pos, double mass, const double center[3], double *M);
+void po_m2m(double dx, double dy, double dz, const double *M, double *toM);
+void po_m2l(double dx, double dy, double dz, const double *M, double *toL, double rs);
+void po_l2l(double dx, double dy, double dz, const double *L, double *toL);
+void po_l2p(int npart, const double *pos, const double center[3], const double *L, double *acc);
+int po_acceptance(const double wi[3], const double wj[3], const double dist[3], double theta, double rcut);
+
+/* FP64 direct sum of the untruncated split kernel, minimum image, over all
+   sources within rmax of each listed target.  acc_out: nt*3. */
+int po_direct_sum(const po_params *p, int n, const double *pos, int nt, const int *targets,
+                  double rmax, double *acc_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
