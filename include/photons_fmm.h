@@ -1,0 +1,146 @@
+/*
+ * photoNs-2.0 FMM short-range force pass on one GB300 GPU: C ABI.
+ *
+ * Two layers:
+ *
+ *  1. The reference's own entry points, unchanged names and signatures, so
+ *     the reference driver (src/photoNs.c) links this library in place of
+ *     src/fmm.c, src/operator.c and src/remotes.c.  They communicate
+ *     through the reference's globals (part, NPART, MAXLEAF, open_angle,
+ *     splitRadius, cutoffRadius, SoftenScale, MASSPART, BOXSIZE, toptree,
+ *     btree, leaf, ...), which this library also defines so that it can be
+ *     loaded on its own.  Like the reference they print a message and exit
+ *     on a fatal error; photons_gpu_status()/photons_gpu_error() report the
+ *     last error without exiting.
+ *
+ *  2. photons_* extensions: a context-based pass on plain arrays (the call
+ *     benchmarks and tests use), inspection of the tree and lists, batched
+ *     operators, an FP64 direct-sum reference, and timing.
+ *
+ * Only one rank is supported (the reference's single-GPU case); with
+ * PROC_SIZE > 1 the legacy entry points fail.
+ */
+#ifndef PHOTONS_FMM_H
+#define PHOTONS_FMM_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ */
+/* 1. reference entry points                                           */
+/* ------------------------------------------------------------------ */
+
+/* inc/fmm.h:16 -- top-tree geometry of the domain (src/fmm.c:329-360) */
+void fmm_construct(void);
+/* inc/fmm.h:19 -- tree build, multipoles, top-tree connect (src/fmm.c:719-770);
+   permutes part[] into tree order and fills btree/leaf like the reference */
+void fmm_prepare(void);
+/* inc/fmm.h:20 -- local P2P and M2L lists and their evaluation (src/fmm.c:909-984) */
+void fmm_task(void);
+/* inc/fmm.h:21 -- 26 periodic images, L2L and L2P (src/fmm.c:987-1075) */
+void fmm_ext(void);
+/* inc/fmm.h:17 -- release the tree (src/fmm.c:1077-1087) */
+void fmm_deconstruct(void);
+/* inc/fmm.h:10 -- tree build only (src/fmm.c:180-264) */
+void build_localtree(void);
+
+/* inc/operator.h:6-19 -- operators on host data, FP64 (src/operator.c) */
+void p2m(int iPart, int npart, double center[3], double M[]);
+void m2m(double dx, double dy, double dz, double M[], double tM[]);
+void m2l(double dx, double dy, double dz, double M[], double toL[]);
+void l2l(double dx, double dy, double dz, double L[], double toL[]);
+void l2p(int ileaf);
+void walk_m2m(int iNode);
+void walk_l2l(int inode);
+
+/* inc/photoNs.h:325 -- MAC (src/fmm.c:266-326) */
+int acceptance(double wi[3], double wj[3], double dist[3]);
+
+/* inc/remotes.h:16 -- interactions with one shifted copy of the local tree
+   (src/remotes.c:684-751); at one rank idx must be 0 */
+void fmm_remote(int idx, double shift[3]);
+
+/* ------------------------------------------------------------------ */
+/* 2. extensions                                                       */
+/* ------------------------------------------------------------------ */
+
+/* last error of the calling thread: 0 = none */
+int photons_gpu_status(void);
+const char *photons_gpu_error(void);
+void photons_gpu_clear_error(void);
+
+typedef struct photons_params {
+    double boxsize;  /* periodic box side (BOXSIZE) */
+    double theta;    /* opening angle (open_angle) */
+    double rs;       /* split radius (splitRadius) */
+    double rcut;     /* cutoff radius (cutoffRadius) */
+    double eps;      /* softening length (SoftenScale) */
+    double mass;     /* particle mass (MASSPART) */
+    int maxleaf;     /* MAXLEAF */
+    int precision;   /* PHOTONS_FP32_SPLIT or PHOTONS_FP64 */
+    unsigned image_mask; /* bit 0: local tree, bit k (1..26): image k; 0 means all */
+    int flags;       /* PHOTONS_F_* */
+} photons_params;
+
+#define PHOTONS_FP32_SPLIT 0
+#define PHOTONS_FP64 1
+
+/* flags */
+#define PHOTONS_F_DEVICE_IO 1       /* pos/acc pointers are device memory */
+#define PHOTONS_F_TREE_ORDER 2      /* acc returned in tree order (see photons_get_perm) */
+#define PHOTONS_F_NO_FARFIELD 4     /* skip P2M/M2M/M2L/L2L/L2P */
+#define PHOTONS_F_MULTIPOLES 8      /* compute P2M/M2M even when no M2L task exists */
+#define PHOTONS_F_KEEP_LISTS 16     /* keep lists for photons_list_* */
+
+typedef struct photons_ctx photons_ctx;
+
+photons_ctx *photons_create(int device);
+void photons_destroy(photons_ctx *ctx);
+/* launch on this cudaStream_t (NULL: the context's own stream) */
+int photons_set_stream(photons_ctx *ctx, void *cuda_stream);
+
+/* One force pass over n particles: pos[3n] in, acc[3n] out (overwritten).
+   Host or device pointers per PHOTONS_F_DEVICE_IO. */
+int photons_force_pass(photons_ctx *ctx, const photons_params *p, int n, const double *pos, double *acc);
+
+/* counters[32] after a pass: idxP2P, idxM2L, walk_m2l_count, p2p_count_remote,
+   NLEAF, NNODE, nleaf, nnode, first_leaf, first_node, direct_local_start,
+   n_p2p, n_m2l, n_p2p_ext, n_m2l_ext, n_images, local pairs, image pairs,
+   depth, max stack, max stage, pd peak, p2p entries, m2l entries */
+int photons_get_counters(photons_ctx *ctx, long long *counters, int n);
+/* milliseconds of the last pass: total, upload, tree, walk, p2p, farfield, download */
+int photons_get_timings(photons_ctx *ctx, float *ms, int n);
+/* tree-order -> input index */
+int photons_get_perm(photons_ctx *ctx, int *perm);
+/* tree-order positions */
+int photons_get_positions(photons_ctx *ctx, double *pos);
+
+/* the tree in the reference's layout and index space:
+   leaves: ip_np[2*nleaf], geom[6*nleaf] (centre, width), M/L[20*nleaf];
+   nodes: info[3*nnode] (npart, son0, son1), geom[7*nnode] (split, centre, width), M/L */
+int photons_copy_leaves(photons_ctx *ctx, int *ip_np, double *geom, double *M, double *L);
+int photons_copy_nodes(photons_ctx *ctx, int *info, double *geom, double *M, double *L);
+
+/* lists of the last pass (PHOTONS_F_KEEP_LISTS), reference index space;
+   kind 0 local P2P, 1 local M2L, 2 image P2P, 3 image M2L */
+long long photons_list_size(photons_ctx *ctx, int kind);
+int photons_list_copy(photons_ctx *ctx, int kind, int *target, int *source, int *image);
+
+/* batched operators on host arrays, evaluated on the GPU:
+   op 0: L[i] += M2L(d[i], M[i]) with split radius rs
+   op 1: out[i] += M2M(d[i], in[i]);  op 2: out[i] += L2L(d[i], in[i]) */
+int photons_op_batch(int op, int n, const double *d, const double *in, double *inout, double rs);
+
+/* FP64 direct sum of the untruncated split kernel over all sources within
+   rmax (minimum image) for nt targets (input indices); host arrays */
+int photons_direct_sum(const photons_params *p, int n, const double *pos, int nt, const int *targets,
+                       double rmax, double *acc);
+
+/* FP32 FMA throughput probe: returns TFLOP/s measured over ~iters FMAs per thread */
+double photons_fp32_fma_peak(int iters);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

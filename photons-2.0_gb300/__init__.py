@@ -1,0 +1,302 @@
+"""Python host interface to libphotons_fmm.so -- the GB300 FMM short-range
+force pass of photoNs-2.0 (include/photons_fmm.h).
+
+Two ways in, mirroring the C ABI:
+
+* ``ForcePass``   -- the context-based pass on plain arrays
+  (photons_force_pass): positions in, accelerations out, plus counters,
+  timings, the tree and the interaction lists for inspection.
+* ``Reference``   -- the reference's own entry points (fmm_construct,
+  fmm_prepare, fmm_task, fmm_ext, fmm_deconstruct, ...) driven through the
+  reference's globals, exactly as src/photoNs.c drives the CPU FMM.
+
+The CUDA library is required: every call fails loudly when it is missing.
+There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libphotons_fmm.so")
+
+FP32_SPLIT = 0
+FP64 = 1
+
+F_DEVICE_IO = 1
+F_TREE_ORDER = 2
+F_NO_FARFIELD = 4
+F_MULTIPOLES = 8
+F_KEEP_LISTS = 16
+
+NMULTI = 20
+LIST_KINDS = {"p2p": 0, "m2l": 1, "p2p_ext": 2, "m2l_ext": 3}
+COUNTER_NAMES = [
+    "idxP2P", "idxM2L", "walk_m2l_count", "p2p_count_remote", "NLEAF", "NNODE",
+    "nleaf", "nnode", "first_leaf", "first_node", "direct_local_start",
+    "n_p2p", "n_m2l", "n_p2p_ext", "n_m2l_ext", "n_images",
+    "pairs_local", "pairs_image", "depth", "max_stack", "max_stage", "pd_peak",
+    "p2p_entries", "m2l_entries",
+]
+TIMING_NAMES = ["total", "upload", "tree", "walk", "p2p", "farfield", "download"]
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_lp = C.POINTER(C.c_longlong)
+
+
+class Params(C.Structure):
+    _fields_ = [("boxsize", C.c_double), ("theta", C.c_double), ("rs", C.c_double), ("rcut", C.c_double),
+                ("eps", C.c_double), ("mass", C.c_double), ("maxleaf", C.c_int), ("precision", C.c_int),
+                ("image_mask", C.c_uint), ("flags", C.c_int)]
+
+
+class PhotonsError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def library_path():
+    return LIB_PATH
+
+
+def load_library():
+    """Load the CUDA library (build it with build.py / __graft_entry__.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise PhotonsError(f"CUDA library not built: {LIB_PATH} (run __graft_entry__.build())")
+    lib = C.CDLL(LIB_PATH, mode=C.RTLD_GLOBAL)
+    lib.photons_create.restype = C.c_void_p
+    lib.photons_create.argtypes = [C.c_int]
+    lib.photons_destroy.argtypes = [C.c_void_p]
+    lib.photons_set_stream.argtypes = [C.c_void_p, C.c_void_p]
+    lib.photons_force_pass.argtypes = [C.c_void_p, C.POINTER(Params), C.c_int, C.c_void_p, C.c_void_p]
+    lib.photons_get_counters.argtypes = [C.c_void_p, _lp, C.c_int]
+    lib.photons_get_timings.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.c_int]
+    lib.photons_get_perm.argtypes = [C.c_void_p, _ip]
+    lib.photons_get_positions.argtypes = [C.c_void_p, _dp]
+    lib.photons_copy_leaves.argtypes = [C.c_void_p, _ip, _dp, _dp, _dp]
+    lib.photons_copy_nodes.argtypes = [C.c_void_p, _ip, _dp, _dp, _dp]
+    lib.photons_list_size.restype = C.c_longlong
+    lib.photons_list_size.argtypes = [C.c_void_p, C.c_int]
+    lib.photons_list_copy.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _ip]
+    lib.photons_op_batch.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, C.c_double]
+    lib.photons_direct_sum.argtypes = [C.POINTER(Params), C.c_int, _dp, C.c_int, _ip, C.c_double, _dp]
+    lib.photons_fp32_fma_peak.restype = C.c_double
+    lib.photons_fp32_fma_peak.argtypes = [C.c_int]
+    lib.photons_gpu_error.restype = C.c_char_p
+    lib.photons_gpu_status.restype = C.c_int
+    for name in ("fmm_construct", "fmm_prepare", "fmm_task", "fmm_ext", "fmm_deconstruct", "build_localtree"):
+        getattr(lib, name).restype = None
+        getattr(lib, name).argtypes = []
+    lib.acceptance.restype = C.c_int
+    lib.acceptance.argtypes = [_dp, _dp, _dp]
+    lib.fmm_remote.argtypes = [C.c_int, _dp]
+    _lib = lib
+    return lib
+
+
+def _check(rc):
+    if rc != 0:
+        msg = _lib.photons_gpu_error().decode(errors="replace")
+        raise PhotonsError(f"photons error {rc}: {msg}")
+
+
+def _p(a, t=_dp):
+    return a.ctypes.data_as(t)
+
+
+def make_params(p, precision=FP32_SPLIT, image_mask=0, flags=0):
+    """photons_params from a dict with boxsize, theta, rs, rcut, eps, mass, maxleaf."""
+    return Params(float(p["boxsize"]), float(p["theta"]), float(p["rs"]), float(p["rcut"]), float(p["eps"]),
+                  float(p["mass"]), int(p["maxleaf"]), int(precision), int(image_mask), int(flags))
+
+
+class ForcePass:
+    """One GPU context; run() evaluates the short-range force pass."""
+
+    def __init__(self, device=0):
+        self.lib = load_library()
+        h = self.lib.photons_create(device)
+        if not h:
+            raise PhotonsError(self.lib.photons_gpu_error().decode(errors="replace"))
+        self.h = C.c_void_p(h)
+        self.n = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.photons_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr):
+        _check(self.lib.photons_set_stream(self.h, C.c_void_p(stream_ptr)))
+
+    def run(self, pos, p, precision=FP32_SPLIT, image_mask=0, flags=0, out=None):
+        """Host arrays: pos (N,3) float64 -> acc (N,3) float64."""
+        pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+        n = pos.shape[0]
+        acc = out if out is not None else np.empty_like(pos)
+        prm = make_params(p, precision, image_mask, flags & ~F_DEVICE_IO)
+        _check(self.lib.photons_force_pass(self.h, C.byref(prm), n, pos.ctypes.data, acc.ctypes.data))
+        self.n = n
+        return acc
+
+    def run_device(self, pos_ptr, acc_ptr, n, p, precision=FP32_SPLIT, image_mask=0, flags=0):
+        """Device pointers (e.g. torch tensors' data_ptr()), AoS (n,3) float64."""
+        prm = make_params(p, precision, image_mask, flags | F_DEVICE_IO)
+        _check(self.lib.photons_force_pass(self.h, C.byref(prm), int(n), C.c_void_p(pos_ptr), C.c_void_p(acc_ptr)))
+        self.n = n
+
+    def counters(self):
+        v = np.zeros(32, np.int64)
+        _check(self.lib.photons_get_counters(self.h, _p(v, _lp), 32))
+        return dict(zip(COUNTER_NAMES, (int(x) for x in v)))
+
+    def timings(self):
+        v = (C.c_float * 8)()
+        _check(self.lib.photons_get_timings(self.h, v, 8))
+        return dict(zip(TIMING_NAMES, list(v)))
+
+    def perm(self):
+        out = np.empty(self.n, np.int32)
+        _check(self.lib.photons_get_perm(self.h, _p(out, _ip)))
+        return out
+
+    def positions(self):
+        out = np.empty((self.n, 3))
+        _check(self.lib.photons_get_positions(self.h, _p(out)))
+        return out
+
+    def tree(self):
+        c = self.counters()
+        nl, nn = c["nleaf"], c["nnode"]
+        lip = np.empty((nl, 2), np.int32)
+        lg = np.empty((nl, 6))
+        lM = np.empty((nl, NMULTI))
+        lL = np.empty((nl, NMULTI))
+        ni = np.empty((nn, 3), np.int32)
+        ng = np.empty((nn, 7))
+        nM = np.empty((nn, NMULTI))
+        nL = np.empty((nn, NMULTI))
+        _check(self.lib.photons_copy_leaves(self.h, _p(lip, _ip), _p(lg), _p(lM), _p(lL)))
+        _check(self.lib.photons_copy_nodes(self.h, _p(ni, _ip), _p(ng), _p(nM), _p(nL)))
+        return dict(leaf_ipart=lip[:, 0].copy(), leaf_npart=lip[:, 1].copy(), leaf_center=lg[:, :3].copy(),
+                    leaf_width=lg[:, 3:].copy(), leaf_M=lM, leaf_L=lL, node_npart=ni[:, 0].copy(),
+                    node_son=ni[:, 1:].copy(), node_split=ng[:, 0].copy(), node_center=ng[:, 1:4].copy(),
+                    node_width=ng[:, 4:].copy(), node_M=nM, node_L=nL)
+
+    def lists(self):
+        out = {}
+        for name, k in LIST_KINDS.items():
+            m = self.lib.photons_list_size(self.h, k)
+            if m < 0:
+                _check(self.lib.photons_gpu_status() or 6)
+            t = np.empty(m, np.int32)
+            s = np.empty(m, np.int32)
+            im = np.empty(m, np.int32)
+            if m:
+                _check(self.lib.photons_list_copy(self.h, k, _p(t, _ip), _p(s, _ip), _p(im, _ip)))
+            out[name] = (t, s, im)
+        return out
+
+
+def op_batch(op, d, inp, inout, rs=1.0):
+    """Batched operators on the GPU: op 'm2l' (L += M2L(d, M)), 'm2m', 'l2l'."""
+    lib = load_library()
+    code = {"m2l": 0, "m2m": 1, "l2l": 2}[op]
+    d = np.ascontiguousarray(d, np.float64).reshape(-1, 3)
+    inp = np.ascontiguousarray(inp, np.float64).reshape(-1, NMULTI)
+    out = np.ascontiguousarray(inout, np.float64).reshape(-1, NMULTI).copy()
+    _check(lib.photons_op_batch(code, d.shape[0], _p(d), _p(inp), _p(out), float(rs)))
+    return out
+
+
+def direct_sum(pos, p, targets, rmax=None):
+    """FP64 GPU direct sum of the untruncated split kernel for the target subset."""
+    lib = load_library()
+    pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+    targets = np.ascontiguousarray(targets, np.int32)
+    out = np.empty((targets.size, 3))
+    prm = make_params(p)
+    rmax = 2.0 * p["rcut"] if rmax is None else rmax
+    _check(lib.photons_direct_sum(C.byref(prm), pos.shape[0], _p(pos), targets.size, _p(targets, _ip),
+                                  float(rmax), _p(out)))
+    return out
+
+
+def fp32_fma_peak(iters=4096):
+    lib = load_library()
+    v = lib.photons_fp32_fma_peak(int(iters))
+    if v <= 0:
+        raise PhotonsError("FMA probe failed: " + lib.photons_gpu_error().decode(errors="replace"))
+    return v
+
+
+class Reference:
+    """The reference's entry points on the reference's globals."""
+
+    BODY = np.dtype([("pos", "f8", 3), ("acc", "f8", 3), ("vel", "f8", 3), ("acc_pm", "f8", 3)])
+
+    def __init__(self):
+        self.lib = load_library()
+        self._part = None
+
+    def _set(self, ctype, name, value):
+        ctype.in_dll(self.lib, name).value = value
+
+    def _get(self, ctype, name):
+        return ctype.in_dll(self.lib, name).value
+
+    def setup(self, pos, p):
+        """Fill part[] and the parameter globals as src/initial.c would."""
+        pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+        n = pos.shape[0]
+        body = np.zeros(n, self.BODY)
+        body["pos"] = pos
+        self._part = body
+        C.c_void_p.in_dll(self.lib, "part").value = body.ctypes.data
+        self._set(C.c_int, "NPART", n)
+        self._set(C.c_long, "NPART_TOTAL", n)
+        self._set(C.c_int, "PROC_SIZE", 1)
+        self._set(C.c_int, "PROC_RANK", 0)
+        self._set(C.c_double, "BOXSIZE", p["boxsize"])
+        self._set(C.c_int, "MAXLEAF", int(p["maxleaf"]))
+        self._set(C.c_double, "open_angle", p["theta"])
+        self._set(C.c_double, "splitRadius", p["rs"])
+        self._set(C.c_double, "cutoffRadius", p["rcut"])
+        self._set(C.c_double, "SoftenScale", p["eps"])
+        self._set(C.c_double, "MASSPART", p["mass"])
+        for name in ("idxP2P", "idxM2L", "walk_m2l_count", "p2p_count_remote"):
+            self._set(C.c_ulong, name, 0)
+
+    def force_pass(self):
+        """The driver sequence of src/photoNs.c:97-116 (without PM)."""
+        lib = self.lib
+        lib.fmm_construct()
+        lib.fmm_prepare()
+        lib.fmm_task()
+        acc_task = self._part["acc"].copy()
+        lib.fmm_ext()
+        return acc_task
+
+    def part(self):
+        return self._part
+
+    def counters(self):
+        return {k: int(self._get(C.c_ulong, k)) for k in ("idxP2P", "idxM2L", "walk_m2l_count", "p2p_count_remote")}
+
+    def deconstruct(self):
+        self.lib.fmm_deconstruct()

@@ -1,0 +1,696 @@
+// Force-pass context, stage orchestration and the photons_* C ABI.
+//
+// A pass (photons_force_pass) runs, on one stream:
+//   upload -> tree build -> leaf offsets -> dual-tree walk -> P2P
+//   -> [P2M, M2M, M2L, L2L, L2P when any M2L task exists] -> gather/download
+// The reference-named entry points (legacy.cu) reuse the same stages.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "photons_fmm.h"
+#include "api_internal.cuh"
+
+// ------------------------------------------------------------------
+// errors
+// ------------------------------------------------------------------
+static thread_local int g_status = 0;
+static thread_local char g_msg[512] = {0};
+
+int ph_set_error(int code, const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_msg, sizeof g_msg, fmt, ap);
+    va_end(ap);
+    g_status = code;
+    return code;
+}
+
+int ph_set_cuda_error(cudaError_t e, const char *what, const char *file, int line)
+{
+    const char *base = strrchr(file, '/');
+    return ph_set_error(PH_ERR_CUDA, "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), base ? base + 1 : file,
+                        line);
+}
+
+extern "C" int photons_gpu_status(void) { return g_status; }
+extern "C" const char *photons_gpu_error(void) { return g_msg; }
+extern "C" void photons_gpu_clear_error(void)
+{
+    g_status = 0;
+    g_msg[0] = 0;
+}
+
+namespace ph {
+int device_sm_count()
+{
+    static int v = 0;
+    if (!v) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        if (v <= 0) v = 1;
+    }
+    return v;
+}
+}  // namespace ph
+
+// ------------------------------------------------------------------
+// buffers
+// ------------------------------------------------------------------
+template <class T>
+static int dalloc(T *&p, size_t n)
+{
+    if (p) cudaFree(p);
+    p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void **)&p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        p = nullptr;
+        cudaGetLastError();
+        return ph_set_error(PH_ERR_NOMEM, "device allocation of %zu bytes failed: %s", n * sizeof(T),
+                            cudaGetErrorString(e));
+    }
+    return 0;
+}
+
+template <class T>
+static void dfree(T *&p)
+{
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+#define PH_TRY(x)               \
+    do {                        \
+        int rc__ = (x);         \
+        if (rc__) return rc__;  \
+    } while (0)
+
+#define CHUNK_ELEMS 1024
+#define MAX_DEPTH_CAP 2048
+
+static int alloc_particles(photons_ctx *c, int n)
+{
+    if (n <= c->cap_n) return 0;
+    ph::BuildBufs &b = c->b;
+    PH_TRY(dalloc(b.x, n)); PH_TRY(dalloc(b.y, n)); PH_TRY(dalloc(b.z, n));
+    PH_TRY(dalloc(b.perm, n)); PH_TRY(dalloc(b.smallpos, n)); PH_TRY(dalloc(b.bigslot, n));
+    PH_TRY(dalloc(c->pos4, n));
+    PH_TRY(dalloc(c->ax, n)); PH_TRY(dalloc(c->ay, n)); PH_TRY(dalloc(c->az, n));
+    PH_TRY(dalloc(c->io, (size_t)3 * n));
+    b.cap_n = n;
+    c->cap_n = n;
+    return 0;
+}
+
+static int alloc_tree(photons_ctx *c, int n, int cap)
+{
+    int chunks = n / CHUNK_ELEMS + cap + 2;
+    ph::BuildBufs &b = c->b;
+    if (cap > b.cap_nodes) {
+        PH_TRY(dalloc(b.tn_start, cap)); PH_TRY(dalloc(b.tn_len, cap)); PH_TRY(dalloc(b.tn_depth, cap));
+        PH_TRY(dalloc(b.tn_parent, cap)); PH_TRY(dalloc(b.tn_child0, cap)); PH_TRY(dalloc(b.tn_child1, cap));
+        PH_TRY(dalloc(b.tn_mode, cap)); PH_TRY(dalloc(b.tn_S, cap)); PH_TRY(dalloc(b.tn_box, (size_t)6 * cap));
+        PH_TRY(dalloc(b.tn_split, cap)); PH_TRY(dalloc(b.tn_nch, cap)); PH_TRY(dalloc(b.tn_chunk_base, cap));
+        PH_TRY(dalloc(b.tn_nodeflag, cap)); PH_TRY(dalloc(b.tn_leafflag, cap)); PH_TRY(dalloc(b.tn_nodebase, cap));
+        PH_TRY(dalloc(b.tn_leafbase, cap)); PH_TRY(dalloc(b.tn_sub_nodes, cap)); PH_TRY(dalloc(b.tn_sub_leaves, cap));
+        PH_TRY(dalloc(b.tn_pre, cap)); PH_TRY(dalloc(b.tn_lbase, cap));
+        PH_TRY(dalloc(b.tl_start, cap)); PH_TRY(dalloc(b.tl_len, cap)); PH_TRY(dalloc(b.tl_depth, cap));
+        PH_TRY(dalloc(b.tl_parent, cap)); PH_TRY(dalloc(b.tl_final, cap)); PH_TRY(dalloc(b.tl_box, (size_t)6 * cap));
+        b.scan_scratch_elems = ph::scan_scratch_elems(cap > chunks ? cap : chunks) + 8;
+        PH_TRY(dalloc(b.scan_scratch, b.scan_scratch_elems));
+        PH_TRY(dalloc(b.cnt, ph::BC_NCOUNTERS));
+        b.cap_nodes = cap;
+        b.cap_leaves = cap;
+        // unified tree
+        ph::TreeBufs &t = c->t;
+        int cu = 2 * cap + 2;
+        PH_TRY(dalloc(t.ipart, cu)); PH_TRY(dalloc(t.npart, cu)); PH_TRY(dalloc(t.depth, cu));
+        PH_TRY(dalloc(t.parent, cu)); PH_TRY(dalloc(t.son0, cu)); PH_TRY(dalloc(t.son1, cu));
+        PH_TRY(dalloc(t.cx, cu)); PH_TRY(dalloc(t.cy, cu)); PH_TRY(dalloc(t.cz, cu));
+        PH_TRY(dalloc(t.wx, cu)); PH_TRY(dalloc(t.wy, cu)); PH_TRY(dalloc(t.wz, cu));
+        PH_TRY(dalloc(t.wsum, cu)); PH_TRY(dalloc(t.split, cu));
+        PH_TRY(dalloc(t.depth_list, cu));
+        PH_TRY(dalloc(t.depth_off, MAX_DEPTH_CAP + 2));
+        t.max_depth_cap = MAX_DEPTH_CAP;
+        t.cap_u = cu;
+        // per-unified walk bookkeeping and expansions
+        ph::WalkBufs &w = c->w;
+        PH_TRY(dalloc(w.pd_off, cu)); PH_TRY(dalloc(w.pd_cnt, cu));
+        PH_TRY(dalloc(w.p2p_off, cu)); PH_TRY(dalloc(w.p2p_cnt, cu));
+        PH_TRY(dalloc(w.m2l_off, cu)); PH_TRY(dalloc(w.m2l_cnt, cu));
+        PH_TRY(dalloc(c->M, (size_t)cu * PH_NMULTI));
+        PH_TRY(dalloc(c->L, (size_t)cu * PH_NMULTI));
+        c->cap_u = cu;
+    }
+    if (chunks > b.cap_chunks) {
+        PH_TRY(dalloc(b.ch_partial, chunks)); PH_TRY(dalloc(b.ch_cnt, chunks)); PH_TRY(dalloc(b.ch_small_base, chunks));
+        b.cap_chunks = chunks;
+        size_t need = ph::scan_scratch_elems(cap > chunks ? cap : chunks) + 8;
+        if (need > b.scan_scratch_elems) {
+            b.scan_scratch_elems = need;
+            PH_TRY(dalloc(b.scan_scratch, need));
+        }
+    }
+    return 0;
+}
+
+static int alloc_walk(photons_ctx *c, long long p2p_cap, long long pd_cap, long long m2l_cap, int stack_cap,
+                      int stage_cap)
+{
+    ph::WalkBufs &w = c->w;
+    if (!w.ctr) PH_TRY(dalloc(w.ctr, ph::WC_N));
+    if (!c->work_counter) PH_TRY(dalloc(c->work_counter, 4));
+    if (p2p_cap > w.p2p_cap) { PH_TRY(dalloc(w.p2p_pool, p2p_cap)); w.p2p_cap = p2p_cap; }
+    if (pd_cap > w.pd_cap) {
+        PH_TRY(dalloc(w.pd_pool[0], pd_cap));
+        PH_TRY(dalloc(w.pd_pool[1], pd_cap));
+        w.pd_cap = pd_cap;
+    }
+    if (m2l_cap > w.m2l_cap) { PH_TRY(dalloc(w.m2l_pool, m2l_cap)); w.m2l_cap = m2l_cap; }
+    int nwarps = ph::device_sm_count() * 2 * 8;
+    if (stack_cap > w.stack_cap || stage_cap > w.stage_cap || nwarps != w.nwarps) {
+        if (stack_cap < w.stack_cap) stack_cap = w.stack_cap;
+        if (stage_cap < w.stage_cap) stage_cap = w.stage_cap;
+        PH_TRY(dalloc(w.scratch, (size_t)nwarps * (stack_cap + 3 * (size_t)stage_cap)));
+        w.stack_cap = stack_cap;
+        w.stage_cap = stage_cap;
+        w.nwarps = nwarps;
+    }
+    return 0;
+}
+
+static void free_all(photons_ctx *c)
+{
+    ph::BuildBufs &b = c->b;
+    void *ptrs[] = {b.x, b.y, b.z, b.perm, b.smallpos, b.bigslot, b.tn_start, b.tn_len, b.tn_depth, b.tn_parent,
+                    b.tn_child0, b.tn_child1, b.tn_mode, b.tn_S, b.tn_box, b.tn_split, b.tn_nch, b.tn_chunk_base,
+                    b.tn_nodeflag, b.tn_leafflag, b.tn_nodebase, b.tn_leafbase, b.tn_sub_nodes, b.tn_sub_leaves,
+                    b.tn_pre, b.tn_lbase, b.tl_start, b.tl_len, b.tl_depth, b.tl_parent, b.tl_final, b.tl_box,
+                    b.ch_partial, b.ch_cnt, b.ch_small_base, b.cnt, b.scan_scratch, c->t.ipart, c->t.npart,
+                    c->t.depth, c->t.parent, c->t.son0, c->t.son1, c->t.cx, c->t.cy, c->t.cz, c->t.wx, c->t.wy,
+                    c->t.wz, c->t.wsum, c->t.split, c->t.depth_list, c->t.depth_off, c->w.pd_pool[0],
+                    c->w.pd_pool[1], c->w.pd_off, c->w.pd_cnt, c->w.p2p_pool, c->w.p2p_off, c->w.p2p_cnt,
+                    c->w.m2l_pool, c->w.m2l_off, c->w.m2l_cnt, c->w.scratch, c->w.ctr, c->pos4, c->ax, c->ay,
+                    c->az, c->M, c->L, c->io, c->work_counter};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+}
+
+// ------------------------------------------------------------------
+// small kernels
+// ------------------------------------------------------------------
+namespace {
+
+__global__ void k_gather_out(const int *perm, const double *ax, const double *ay, const double *az, int n, double *out,
+                             int tree_order)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int o = tree_order ? i : perm[i];
+        out[3 * o] = ax[i];
+        out[3 * o + 1] = ay[i];
+        out[3 * o + 2] = az[i];
+    }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------
+// stages
+// ------------------------------------------------------------------
+int ph_validate(const photons_params *p, int n)
+{
+    if (!p) return ph_set_error(PH_ERR_ARG, "null parameters");
+    if (n < 1) return ph_set_error(PH_ERR_ARG, "particle count %d < 1", n);
+    if (p->maxleaf < 1 || p->maxleaf > PH_MAX_LEAF)
+        return ph_set_error(PH_ERR_ARG, "MAXLEAF %d outside [1, %d]", p->maxleaf, PH_MAX_LEAF);
+    if (n <= p->maxleaf)
+        return ph_set_error(PH_ERR_SMALL, "N=%d <= MAXLEAF=%d: the reference's image walk treats the root as a leaf "
+                                          "and reads undefined bodies", n, p->maxleaf);
+    if (!(p->boxsize > 0) || !(p->rs > 0) || !(p->rcut > 0) || !(p->eps >= 0) || !(p->theta >= 0) ||
+        !std::isfinite(p->mass))
+        return ph_set_error(PH_ERR_ARG, "invalid force parameters");
+    if (p->precision != PHOTONS_FP32_SPLIT && p->precision != PHOTONS_FP64)
+        return ph_set_error(PH_ERR_ARG, "unknown precision %d", p->precision);
+    if (n >= PH_MAX_UNIFIED / 2) return ph_set_error(PH_ERR_ARG, "N=%d exceeds the 2^26 particle limit", n);
+    return 0;
+}
+
+int ph_stage_build(photons_ctx *c, const photons_params *p, int n, const double *pos, int device_io)
+{
+    PH_TRY(ph_validate(p, n));
+    int cap = (int)(2.0 * ((double)n) / ((double)p->maxleaf));  // src/fmm.c:203-209
+    if (cap > n) cap = n + 1;
+    if (cap < 1) cap = 1;
+    PH_TRY(alloc_particles(c, n));
+    PH_TRY(alloc_tree(c, n, cap));
+    c->pp.boxsize = p->boxsize;
+    c->pp.theta = p->theta;
+    c->pp.rs = p->rs;
+    c->pp.rcut = p->rcut;
+    c->pp.eps = p->eps;
+    c->pp.mass = p->mass;
+    c->pp.maxleaf = p->maxleaf;
+    c->pp.images = 1;
+    c->n = n;
+    c->have_tree = c->have_lists = c->have_multipoles = false;
+    cudaStream_t st = c->stream;
+    const double *src = pos;
+    PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_START], st));
+    if (!device_io) {
+        PH_CUDA_CHECK(cudaMemcpyAsync(c->io, pos, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, st));
+        src = c->io;
+    }
+    PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_UPLOADED], st));
+    PH_TRY(ph::launch_init_particles(c->b, src, n, st));
+    ph::TreeInfo info;
+    info.nleaf_cap = info.nnode_cap = cap;
+    PH_TRY(ph::build_tree(c->b, c->t, c->pp, n, st, info, nullptr));
+    c->info = info;
+    PH_TRY(ph::launch_leaf_offsets(c->b, c->t, info.nleaf, c->pos4, st));
+    PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_TREE], st));
+    c->have_tree = true;
+    return 0;
+}
+
+int ph_stage_walk(photons_ctx *c, unsigned mask)
+{
+    if (!c->have_tree) return ph_set_error(PH_ERR_STATE, "no tree: run the build first");
+    const int n = c->n;
+    long long p2p_cap = c->hint_p2p ? c->hint_p2p : (long long)n * 48 + 4096;
+    long long pd_cap = c->hint_pd ? c->hint_pd : (long long)n * 48 + 4096;
+    long long m2l_cap = c->hint_m2l ? c->hint_m2l : (long long)n * 2 + 4096;
+    int stack_cap = 4096, stage_cap = 16384;
+    for (int attempt = 0; attempt < 6; attempt++) {
+        PH_TRY(alloc_walk(c, p2p_cap, pd_cap, m2l_cap, stack_cap, stage_cap));
+        PH_TRY(ph::walk_lists(c->w, c->t, c->info, c->pp, mask, c->stream, c->ws));
+        unsigned long long fl = c->ws.c[ph::WC_FLAGS];
+        if (!fl) {
+            c->have_lists = true;
+            c->mask = mask;
+            // keep the sizes as hints so a repeated pass allocates once
+            c->hint_p2p = p2p_cap;
+            c->hint_pd = pd_cap;
+            c->hint_m2l = m2l_cap;
+            PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_WALK], c->stream));
+            return 0;
+        }
+        if (fl & PH_FLAG_POOL_OVERFLOW) {
+            long long need = (long long)c->ws.c[ph::WC_P2P_FILL];
+            if (need > c->w.p2p_cap) p2p_cap = need + need / 8 + 4096;
+            need = (long long)c->ws.c[ph::WC_PD_MAX];
+            long long cur = (long long)c->ws.c[ph::WC_PD_FILL0];
+            if ((long long)c->ws.c[ph::WC_PD_FILL1] > cur) cur = (long long)c->ws.c[ph::WC_PD_FILL1];
+            if (cur > need) need = cur;
+            if (need > c->w.pd_cap) pd_cap = need + need / 8 + 4096;
+            need = (long long)c->ws.c[ph::WC_M2L_FILL];
+            if (need > c->w.m2l_cap) m2l_cap = need + need / 8 + 4096;
+        }
+        if (fl & PH_FLAG_STACK_OVERFLOW) stack_cap = c->w.stack_cap * 4;
+        if (fl & PH_FLAG_STAGE_OVERFLOW) {
+            long long need = (long long)c->ws.c[ph::WC_MAX_STAGE];
+            stage_cap = (int)(need > 2LL * c->w.stage_cap ? need + 1024 : 2LL * c->w.stage_cap);
+        }
+    }
+    return ph_set_error(PH_ERR_CAPACITY, "interaction lists did not fit after repeated growth");
+}
+
+int ph_stage_p2p(photons_ctx *c, int precision, int zero)
+{
+    cudaStream_t st = c->stream;
+    const int n = c->n;
+    if (zero) {
+        PH_CUDA_CHECK(cudaMemsetAsync(c->ax, 0, sizeof(double) * n, st));
+        PH_CUDA_CHECK(cudaMemsetAsync(c->ay, 0, sizeof(double) * n, st));
+        PH_CUDA_CHECK(cudaMemsetAsync(c->az, 0, sizeof(double) * n, st));
+    }
+    ph::P2PArgs a;
+    memset(&a, 0, sizeof a);
+    a.ipart = c->t.ipart; a.npart = c->t.npart;
+    a.cx = c->t.cx; a.cy = c->t.cy; a.cz = c->t.cz;
+    a.nleaf = c->info.nleaf;
+    a.p2p_pool = c->w.p2p_pool; a.p2p_off = c->w.p2p_off; a.p2p_cnt = c->w.p2p_cnt;
+    a.pos4 = c->pos4;
+    a.px = c->b.x; a.py = c->b.y; a.pz = c->b.z;
+    a.ax = c->ax; a.ay = c->ay; a.az = c->az;
+    a.work_counter = c->work_counter;
+    a.boxsize = c->pp.boxsize; a.eps = c->pp.eps; a.mass = c->pp.mass; a.rs = c->pp.rs;
+    a.k = ph::make_split_consts(c->pp);
+    PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_P2P_BEGIN], st));
+    PH_TRY(ph::launch_p2p(a, precision == PHOTONS_FP64, st));
+    PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_P2P], st));
+    return 0;
+}
+
+static ph::MultipoleArgs multipole_args(photons_ctx *c)
+{
+    ph::MultipoleArgs a;
+    memset(&a, 0, sizeof a);
+    a.px = c->b.x; a.py = c->b.y; a.pz = c->b.z;
+    a.ipart = c->t.ipart; a.npart = c->t.npart; a.son0 = c->t.son0; a.son1 = c->t.son1; a.parent = c->t.parent;
+    a.cx = c->t.cx; a.cy = c->t.cy; a.cz = c->t.cz;
+    a.nleaf = c->info.nleaf;
+    a.nunified = c->info.nleaf + c->info.nnode;
+    a.ndepth = c->info.depth + 1;
+    a.depth_list = c->t.depth_list;
+    a.depth_off = c->info.depth_off.data();
+    a.m2l_pool = c->w.m2l_pool; a.m2l_off = c->w.m2l_off; a.m2l_cnt = c->w.m2l_cnt;
+    a.M = c->M; a.L = c->L;
+    a.ax = c->ax; a.ay = c->ay; a.az = c->az;
+    a.mass = c->pp.mass; a.rs = c->pp.rs; a.boxsize = c->pp.boxsize;
+    return a;
+}
+
+int ph_stage_multipoles(photons_ctx *c)
+{
+    ph::MultipoleArgs a = multipole_args(c);
+    PH_TRY(ph::run_p2m_m2m(a, c->stream));
+    size_t nu = (size_t)(c->info.nleaf + c->info.nnode);
+    PH_CUDA_CHECK(cudaMemsetAsync(c->L, 0, sizeof(double) * PH_NMULTI * nu, c->stream));
+    c->have_multipoles = true;
+    return 0;
+}
+
+int ph_stage_m2l(photons_ctx *c)
+{
+    ph::MultipoleArgs a = multipole_args(c);
+    return ph::run_m2l(a, c->stream);
+}
+
+int ph_stage_downward(photons_ctx *c)
+{
+    ph::MultipoleArgs a = multipole_args(c);
+    return ph::run_downward(a, c->stream);
+}
+
+int ph_stage_output(photons_ctx *c, double *acc, int device_io, int tree_order)
+{
+    cudaStream_t st = c->stream;
+    const int n = c->n;
+    double *dst = device_io ? acc : c->io;
+    int blocks = ph::device_sm_count() * 8;
+    k_gather_out<<<blocks, 256, 0, st>>>(c->b.perm, c->ax, c->ay, c->az, n, dst, tree_order);
+    PH_CUDA_CHECK(cudaGetLastError());
+    PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_GATHERED], st));
+    if (!device_io)
+        PH_CUDA_CHECK(cudaMemcpyAsync(acc, c->io, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost, st));
+    PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_END], st));
+    return 0;
+}
+
+// ------------------------------------------------------------------
+// C ABI
+// ------------------------------------------------------------------
+extern "C" photons_ctx *photons_create(int device)
+{
+    photons_gpu_clear_error();
+    if (cudaSetDevice(device) != cudaSuccess) {
+        cudaGetLastError();
+        ph_set_error(PH_ERR_CUDA, "cannot use CUDA device %d", device);
+        return nullptr;
+    }
+    photons_ctx *c = new photons_ctx();
+    c->device = device;
+    if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        ph_set_error(PH_ERR_CUDA, "stream creation failed");
+        delete c;
+        return nullptr;
+    }
+    c->stream = c->own_stream;
+    for (int i = 0; i < EV_COUNT; i++) cudaEventCreate(&c->ev[i]);
+    return c;
+}
+
+extern "C" void photons_destroy(photons_ctx *c)
+{
+    if (!c) return;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    free_all(c);
+    for (int i = 0; i < EV_COUNT; i++) cudaEventDestroy(c->ev[i]);
+    cudaStreamDestroy(c->own_stream);
+    delete c;
+}
+
+extern "C" int photons_set_stream(photons_ctx *c, void *stream)
+{
+    if (!c) return ph_set_error(PH_ERR_ARG, "null context");
+    c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+    return 0;
+}
+
+extern "C" int photons_force_pass(photons_ctx *c, const photons_params *p, int n, const double *pos, double *acc)
+{
+    photons_gpu_clear_error();
+    if (!c) return ph_set_error(PH_ERR_ARG, "null context");
+    if (!pos || !acc) return ph_set_error(PH_ERR_ARG, "null particle arrays");
+    cudaSetDevice(c->device);
+    const int dio = p && (p->flags & PHOTONS_F_DEVICE_IO);
+    PH_TRY(ph_stage_build(c, p, n, pos, dio));
+    unsigned mask = p->image_mask ? p->image_mask : ((1u << PH_NIMG) - 1u);
+    PH_TRY(ph_stage_walk(c, mask));
+    PH_TRY(ph_stage_p2p(c, p->precision, 1));
+    bool far = !(p->flags & PHOTONS_F_NO_FARFIELD);
+    unsigned long long nm2l = c->ws.c[ph::WC_M2L_LOCAL] + c->ws.c[ph::WC_M2L_IMAGE];
+    if (far && (nm2l > 0 || (p->flags & PHOTONS_F_MULTIPOLES))) {
+        PH_TRY(ph_stage_multipoles(c));
+        PH_TRY(ph_stage_m2l(c));
+        PH_TRY(ph_stage_downward(c));
+    } else if (p->flags & PHOTONS_F_MULTIPOLES) {
+        PH_TRY(ph_stage_multipoles(c));
+    }
+    PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_FAR], c->stream));
+    PH_TRY(ph_stage_output(c, acc, dio, p->flags & PHOTONS_F_TREE_ORDER));
+    PH_CUDA_CHECK(cudaStreamSynchronize(c->stream));
+    c->last_flags = p->flags;
+    c->precision = p->precision;
+    return 0;
+}
+
+extern "C" int photons_get_counters(photons_ctx *c, long long *out, int n)
+{
+    if (!c || !out) return ph_set_error(PH_ERR_ARG, "null argument");
+    const unsigned long long *w = c->ws.c;
+    long long v[32] = {0};
+    v[0] = (long long)w[ph::WC_P2P_LOCAL];
+    v[1] = (long long)w[ph::WC_M2L_LOCAL];
+    v[2] = (long long)(w[ph::WC_M2L_LOCAL] + w[ph::WC_M2L_IMAGE]);
+    v[3] = (long long)w[ph::WC_PAIRS_IMAGE];
+    v[4] = c->info.nleaf_cap;
+    v[5] = c->info.nnode_cap;
+    v[6] = c->info.nleaf;
+    v[7] = c->info.nnode;
+    v[8] = c->n;
+    v[9] = (long long)c->n + c->info.nleaf_cap;
+    v[10] = 0;
+    v[11] = (long long)w[ph::WC_P2P_LOCAL];
+    v[12] = (long long)w[ph::WC_M2L_LOCAL];
+    v[13] = (long long)w[ph::WC_P2P_IMAGE];
+    v[14] = (long long)w[ph::WC_M2L_IMAGE];
+    int nimg = 0;
+    for (int i = 1; i < PH_NIMG; i++) nimg += (c->mask >> i) & 1;
+    v[15] = nimg;
+    v[16] = (long long)w[ph::WC_PAIRS_LOCAL];
+    v[17] = (long long)w[ph::WC_PAIRS_IMAGE];
+    v[18] = c->info.depth;
+    v[19] = (long long)w[ph::WC_MAX_STACK];
+    v[20] = (long long)w[ph::WC_MAX_STAGE];
+    v[21] = (long long)w[ph::WC_PD_MAX];
+    v[22] = (long long)w[ph::WC_P2P_FILL];
+    v[23] = (long long)w[ph::WC_M2L_FILL];
+    for (int i = 0; i < n && i < 32; i++) out[i] = v[i];
+    return 0;
+}
+
+extern "C" int photons_get_timings(photons_ctx *c, float *ms, int n)
+{
+    if (!c || !ms) return ph_set_error(PH_ERR_ARG, "null argument");
+    float v[8] = {0};
+    cudaEventElapsedTime(&v[0], c->ev[EV_START], c->ev[EV_END]);
+    cudaEventElapsedTime(&v[1], c->ev[EV_START], c->ev[EV_UPLOADED]);
+    cudaEventElapsedTime(&v[2], c->ev[EV_UPLOADED], c->ev[EV_TREE]);
+    cudaEventElapsedTime(&v[3], c->ev[EV_TREE], c->ev[EV_WALK]);
+    cudaEventElapsedTime(&v[4], c->ev[EV_P2P_BEGIN], c->ev[EV_P2P]);
+    cudaEventElapsedTime(&v[5], c->ev[EV_P2P], c->ev[EV_FAR]);
+    cudaEventElapsedTime(&v[6], c->ev[EV_GATHERED], c->ev[EV_END]);
+    cudaGetLastError();
+    for (int i = 0; i < n && i < 8; i++) ms[i] = v[i];
+    return 0;
+}
+
+extern "C" int photons_get_perm(photons_ctx *c, int *perm)
+{
+    if (!c || !perm || !c->have_tree) return ph_set_error(PH_ERR_STATE, "no tree");
+    PH_CUDA_CHECK(cudaMemcpy(perm, c->b.perm, sizeof(int) * c->n, cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+extern "C" int photons_get_positions(photons_ctx *c, double *pos)
+{
+    if (!c || !pos || !c->have_tree) return ph_set_error(PH_ERR_STATE, "no tree");
+    std::vector<double> x(c->n), y(c->n), z(c->n);
+    PH_CUDA_CHECK(cudaMemcpy(x.data(), c->b.x, sizeof(double) * c->n, cudaMemcpyDeviceToHost));
+    PH_CUDA_CHECK(cudaMemcpy(y.data(), c->b.y, sizeof(double) * c->n, cudaMemcpyDeviceToHost));
+    PH_CUDA_CHECK(cudaMemcpy(z.data(), c->b.z, sizeof(double) * c->n, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < c->n; i++) { pos[3 * i] = x[i]; pos[3 * i + 1] = y[i]; pos[3 * i + 2] = z[i]; }
+    return 0;
+}
+
+// host copy of the unified tree
+int ph_download_tree(photons_ctx *c, HostTree &h, bool with_expansions)
+{
+    int nu = c->info.nleaf + c->info.nnode;
+    h.nleaf = c->info.nleaf;
+    h.nnode = c->info.nnode;
+    h.ipart.resize(nu); h.npart.resize(nu); h.son0.resize(nu); h.son1.resize(nu); h.parent.resize(nu);
+    h.cx.resize(nu); h.cy.resize(nu); h.cz.resize(nu); h.wx.resize(nu); h.wy.resize(nu); h.wz.resize(nu);
+    h.split.resize(nu);
+#define DL(dst, src, T) PH_CUDA_CHECK(cudaMemcpy(dst.data(), src, sizeof(T) * nu, cudaMemcpyDeviceToHost))
+    DL(h.ipart, c->t.ipart, int); DL(h.npart, c->t.npart, int); DL(h.son0, c->t.son0, int);
+    DL(h.son1, c->t.son1, int); DL(h.parent, c->t.parent, int);
+    DL(h.cx, c->t.cx, double); DL(h.cy, c->t.cy, double); DL(h.cz, c->t.cz, double);
+    DL(h.wx, c->t.wx, double); DL(h.wy, c->t.wy, double); DL(h.wz, c->t.wz, double);
+    DL(h.split, c->t.split, double);
+#undef DL
+    if (with_expansions) {
+        h.M.assign((size_t)nu * PH_NMULTI, 0.0);
+        h.L.assign((size_t)nu * PH_NMULTI, 0.0);
+        if (c->have_multipoles) {
+            PH_CUDA_CHECK(cudaMemcpy(h.M.data(), c->M, sizeof(double) * PH_NMULTI * nu, cudaMemcpyDeviceToHost));
+            PH_CUDA_CHECK(cudaMemcpy(h.L.data(), c->L, sizeof(double) * PH_NMULTI * nu, cudaMemcpyDeviceToHost));
+        }
+    }
+    return 0;
+}
+
+// unified id -> the reference's index space
+static inline int ref_id(const photons_ctx *c, int u)
+{
+    return u < c->info.nleaf ? c->n + u : c->n + c->info.nleaf_cap + (u - c->info.nleaf);
+}
+
+extern "C" int photons_copy_leaves(photons_ctx *c, int *ip_np, double *geom, double *M, double *L)
+{
+    if (!c || !c->have_tree) return ph_set_error(PH_ERR_STATE, "no tree");
+    HostTree h;
+    PH_TRY(ph_download_tree(c, h, true));
+    for (int u = 0; u < h.nleaf; u++) {
+        if (ip_np) { ip_np[2 * u] = h.ipart[u]; ip_np[2 * u + 1] = h.npart[u]; }
+        if (geom) {
+            double *g = geom + 6 * u;
+            g[0] = h.cx[u]; g[1] = h.cy[u]; g[2] = h.cz[u]; g[3] = h.wx[u]; g[4] = h.wy[u]; g[5] = h.wz[u];
+        }
+        for (int m = 0; m < PH_NMULTI; m++) {
+            if (M) M[PH_NMULTI * u + m] = h.M[(size_t)u * PH_NMULTI + m];
+            if (L) L[PH_NMULTI * u + m] = h.L[(size_t)u * PH_NMULTI + m];
+        }
+    }
+    return 0;
+}
+
+extern "C" int photons_copy_nodes(photons_ctx *c, int *info, double *geom, double *M, double *L)
+{
+    if (!c || !c->have_tree) return ph_set_error(PH_ERR_STATE, "no tree");
+    HostTree h;
+    PH_TRY(ph_download_tree(c, h, true));
+    for (int k = 0; k < h.nnode; k++) {
+        int u = h.nleaf + k;
+        if (info) {
+            info[3 * k] = h.npart[u];
+            info[3 * k + 1] = ref_id(c, h.son0[u]);
+            info[3 * k + 2] = ref_id(c, h.son1[u]);
+        }
+        if (geom) {
+            double *g = geom + 7 * k;
+            g[0] = h.split[u];
+            g[1] = h.cx[u]; g[2] = h.cy[u]; g[3] = h.cz[u]; g[4] = h.wx[u]; g[5] = h.wy[u]; g[6] = h.wz[u];
+        }
+        for (int m = 0; m < PH_NMULTI; m++) {
+            if (M) M[PH_NMULTI * k + m] = h.M[(size_t)u * PH_NMULTI + m];
+            if (L) L[PH_NMULTI * k + m] = h.L[(size_t)u * PH_NMULTI + m];
+        }
+    }
+    return 0;
+}
+
+// lists in the reference's index space, grouped by target
+static int collect_lists(photons_ctx *c, int kind, std::vector<int> *t, std::vector<int> *s, std::vector<int> *im,
+                         long long *count)
+{
+    if (!c || !c->have_lists) return ph_set_error(PH_ERR_STATE, "no lists");
+    int nu = c->info.nleaf + c->info.nnode;
+    bool p2p = (kind == 0 || kind == 2);
+    bool want_image = (kind >= 2);
+    std::vector<long long> off(nu);
+    std::vector<int> cnt(nu);
+    PH_CUDA_CHECK(cudaMemcpy(off.data(), p2p ? c->w.p2p_off : c->w.m2l_off, sizeof(long long) * nu,
+                             cudaMemcpyDeviceToHost));
+    PH_CUDA_CHECK(cudaMemcpy(cnt.data(), p2p ? c->w.p2p_cnt : c->w.m2l_cnt, sizeof(int) * nu, cudaMemcpyDeviceToHost));
+    long long total = (long long)c->ws.c[p2p ? ph::WC_P2P_FILL : ph::WC_M2L_FILL];
+    std::vector<uint32_t> pool((size_t)total);
+    if (total)
+        PH_CUDA_CHECK(cudaMemcpy(pool.data(), p2p ? c->w.p2p_pool : c->w.m2l_pool, sizeof(uint32_t) * total,
+                                 cudaMemcpyDeviceToHost));
+    long long k = 0;
+    int ntargets = p2p ? c->info.nleaf : nu;
+    for (int u = 0; u < ntargets; u++) {
+        for (int j = 0; j < cnt[u]; j++) {
+            uint32_t e = pool[off[u] + j];
+            int img = PH_ENTRY_IMG(e);
+            if ((img != 0) != want_image) continue;
+            if (t) { t->push_back(ref_id(c, u)); s->push_back(ref_id(c, PH_ENTRY_ID(e))); im->push_back(img); }
+            k++;
+        }
+    }
+    *count = k;
+    return 0;
+}
+
+extern "C" long long photons_list_size(photons_ctx *c, int kind)
+{
+    long long n = -1;
+    if (collect_lists(c, kind, nullptr, nullptr, nullptr, &n)) return -1;
+    return n;
+}
+
+extern "C" int photons_list_copy(photons_ctx *c, int kind, int *target, int *source, int *image)
+{
+    std::vector<int> t, s, im;
+    long long n = 0;
+    PH_TRY(collect_lists(c, kind, &t, &s, &im, &n));
+    if (n) {
+        memcpy(target, t.data(), sizeof(int) * n);
+        memcpy(source, s.data(), sizeof(int) * n);
+        memcpy(image, im.data(), sizeof(int) * n);
+    }
+    return 0;
+}
+
+extern "C" int photons_op_batch(int op, int n, const double *d, const double *in, double *inout, double rs)
+{
+    photons_gpu_clear_error();
+    if (n < 0 || op < 0 || op > 2 || (n > 0 && (!d || !in || !inout))) return ph_set_error(PH_ERR_ARG, "bad op batch");
+    if (n == 0) return 0;
+    double *dd = nullptr, *di = nullptr, *dio = nullptr;
+    int rc = 0;
+    if ((rc = dalloc(dd, (size_t)3 * n)) || (rc = dalloc(di, (size_t)PH_NMULTI * n)) ||
+        (rc = dalloc(dio, (size_t)PH_NMULTI * n))) {
+        dfree(dd); dfree(di); dfree(dio);
+        return rc;
+    }
+    cudaMemcpy(dd, d, sizeof(double) * 3 * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(di, in, sizeof(double) * PH_NMULTI * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(dio, inout, sizeof(double) * PH_NMULTI * n, cudaMemcpyHostToDevice);
+    rc = ph::launch_op_batch(op, n, dd, di, dio, rs, 0);
+    if (!rc) {
+        cudaError_t e = cudaMemcpy(inout, dio, sizeof(double) * PH_NMULTI * n, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) rc = ph_set_cuda_error(e, "cudaMemcpy", __FILE__, __LINE__);
+    }
+    dfree(dd); dfree(di); dfree(dio);
+    return rc;
+}

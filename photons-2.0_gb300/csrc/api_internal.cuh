@@ -1,0 +1,70 @@
+// Context and stage functions shared by the photons_* ABI (api.cu) and the
+// reference-named entry points (legacy.cu).
+#pragma once
+
+#include <vector>
+
+#include "fmm_context.cuh"
+#include "multipole.cuh"
+#include "p2p.cuh"
+#include "photons_fmm.h"
+
+enum {
+    PH_OK = 0,
+    PH_ERR_ARG = 1,
+    PH_ERR_CUDA = 2,
+    PH_ERR_NOMEM = 3,
+    PH_ERR_CAPACITY = 4,
+    PH_ERR_SMALL = 5,
+    PH_ERR_STATE = 6,
+    PH_ERR_DEPTH = 7,
+    PH_ERR_UNSUPPORTED = 8
+};
+
+enum {
+    EV_START = 0, EV_UPLOADED, EV_TREE, EV_WALK, EV_P2P_BEGIN, EV_P2P, EV_FAR, EV_GATHERED, EV_END, EV_COUNT
+};
+
+struct photons_ctx {
+    int device = 0;
+    cudaStream_t own_stream = nullptr, stream = nullptr;
+    cudaEvent_t ev[EV_COUNT] = {};
+    ph::BuildBufs b;
+    ph::TreeBufs t;
+    ph::WalkBufs w;
+    float4 *pos4 = nullptr;
+    double *ax = nullptr, *ay = nullptr, *az = nullptr;
+    double *M = nullptr, *L = nullptr;
+    double *io = nullptr;  // 3*cap_n staging for host transfers and gathers
+    int *work_counter = nullptr;
+    int cap_n = 0, cap_u = 0;
+    // last pass
+    PassParams pp{};
+    ph::TreeInfo info;
+    ph::WalkStats ws{};
+    int n = 0;
+    unsigned mask = 0;
+    int last_flags = 0, precision = 0;
+    bool have_tree = false, have_lists = false, have_multipoles = false;
+    long long hint_p2p = 0, hint_pd = 0, hint_m2l = 0;
+};
+
+struct HostTree {
+    int nleaf = 0, nnode = 0;
+    std::vector<int> ipart, npart, son0, son1, parent;
+    std::vector<double> cx, cy, cz, wx, wy, wz, split, M, L;
+};
+
+int ph_validate(const photons_params *p, int n);
+int ph_stage_build(photons_ctx *c, const photons_params *p, int n, const double *pos, int device_io);
+int ph_stage_walk(photons_ctx *c, unsigned mask);
+int ph_stage_p2p(photons_ctx *c, int precision, int zero);
+int ph_stage_multipoles(photons_ctx *c);
+int ph_stage_m2l(photons_ctx *c);
+int ph_stage_downward(photons_ctx *c);
+int ph_stage_output(photons_ctx *c, double *acc, int device_io, int tree_order);
+int ph_download_tree(photons_ctx *c, HostTree &h, bool with_expansions);
+
+namespace ph {
+int launch_init_particles(BuildBufs &b, const double *pos, int n, cudaStream_t st);
+}

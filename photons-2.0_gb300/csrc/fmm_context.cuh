@@ -1,0 +1,112 @@
+// Device buffers of one force-pass context and the host-side entry points
+// of each stage.
+#pragma once
+
+#include <vector>
+
+#include "fmm_internal.cuh"
+
+namespace ph {
+
+// Tree build scratch and results.  "temp" nodes/leaves are numbered in the
+// order the level-synchronous build creates them; the final (reference)
+// numbering is assigned afterwards.
+struct BuildBufs {
+    // particles, tree order after the build
+    double *x = nullptr, *y = nullptr, *z = nullptr;
+    int *perm = nullptr;
+    int *smallpos = nullptr;   // slot -> position of a right-region particle not above the mean
+    int *bigslot = nullptr;    // position -> slot for a left-region particle above the mean (-1 otherwise)
+    // temp nodes
+    int *tn_start = nullptr, *tn_len = nullptr, *tn_depth = nullptr, *tn_parent = nullptr;
+    int *tn_child0 = nullptr, *tn_child1 = nullptr, *tn_mode = nullptr, *tn_S = nullptr;
+    double *tn_box = nullptr;  // [6][cap_nodes]
+    double *tn_split = nullptr;
+    int *tn_nch = nullptr, *tn_chunk_base = nullptr;
+    int *tn_nodeflag = nullptr, *tn_leafflag = nullptr, *tn_nodebase = nullptr, *tn_leafbase = nullptr;
+    int *tn_sub_nodes = nullptr, *tn_sub_leaves = nullptr, *tn_pre = nullptr, *tn_lbase = nullptr;
+    // temp leaves
+    int *tl_start = nullptr, *tl_len = nullptr, *tl_depth = nullptr, *tl_parent = nullptr, *tl_final = nullptr;
+    double *tl_box = nullptr;  // [6][cap_leaves]
+    // chunks
+    double *ch_partial = nullptr;
+    int *ch_cnt = nullptr, *ch_small_base = nullptr;
+    // small device counters
+    int *cnt = nullptr;  // see BuildCounter
+    int *scan_scratch = nullptr;
+    size_t scan_scratch_elems = 0;
+    int cap_nodes = 0, cap_leaves = 0, cap_chunks = 0, cap_n = 0;
+    int *level_begin_h = nullptr;  // host copy, per level
+};
+
+enum BuildCounter {
+    BC_LEVEL_COUNT = 0,   // nodes in the current level
+    BC_W = 1,             // chunks in the current level
+    BC_NEXT_NODES = 2,    // node children created by the current level
+    BC_NEW_LEAVES = 3,    // leaf children created by the current level
+    BC_LEAVES = 4,        // temp leaves so far
+    BC_FLAGS = 5,
+    BC_NCOUNTERS = 8
+};
+
+// Final tree in unified index space (leaves then nodes).
+struct TreeBufs {
+    int cap_u = 0;
+    int *ipart = nullptr, *npart = nullptr, *depth = nullptr, *parent = nullptr;
+    int *son0 = nullptr, *son1 = nullptr;  // unified ids (nodes only)
+    double *cx = nullptr, *cy = nullptr, *cz = nullptr;
+    double *wx = nullptr, *wy = nullptr, *wz = nullptr;
+    double *wsum = nullptr, *split = nullptr;
+    // per-depth lists of unified ids
+    int *depth_off = nullptr;   // [max_depth+2]
+    int *depth_list = nullptr;  // [cap_u]
+    int *depth_cnt = nullptr;   // [max_depth+1]
+    int max_depth_cap = 0;
+};
+
+struct TreeInfo {
+    int nleaf = 0, nnode = 0, depth = 0;  // depth = deepest level index
+    int nleaf_cap = 0, nnode_cap = 0;      // the reference's 2N/MAXLEAF capacity
+    std::vector<int> depth_off;            // host copy of TreeBufs::depth_off
+};
+
+enum WalkCounter {
+    WC_PD_FILL0 = 0, WC_PD_FILL1, WC_P2P_FILL, WC_M2L_FILL,
+    WC_P2P_LOCAL, WC_P2P_IMAGE, WC_M2L_LOCAL, WC_M2L_IMAGE,
+    WC_PAIRS_LOCAL, WC_PAIRS_IMAGE, WC_FLAGS, WC_MAX_STACK, WC_MAX_STAGE, WC_PD_MAX,
+    WC_N
+};
+
+// Interaction lists.  P2P lists are per target leaf, M2L lists per target
+// (leaf or node), push-down lists per node (consumed by its children at the
+// next depth; two pools alternate by depth parity).
+struct WalkBufs {
+    uint32_t *pd_pool[2] = {nullptr, nullptr};
+    long long pd_cap = 0;
+    long long *pd_off = nullptr;
+    int *pd_cnt = nullptr;
+    uint32_t *p2p_pool = nullptr;
+    long long p2p_cap = 0;
+    long long *p2p_off = nullptr;
+    int *p2p_cnt = nullptr;
+    uint32_t *m2l_pool = nullptr;
+    long long m2l_cap = 0;
+    long long *m2l_off = nullptr;
+    int *m2l_cnt = nullptr;
+    uint32_t *scratch = nullptr;  // per resident warp: stack, then three staging areas
+    int nwarps = 0, stack_cap = 0, stage_cap = 0;
+    unsigned long long *ctr = nullptr;  // WalkCounter
+};
+
+struct WalkStats {
+    unsigned long long c[WC_N];
+};
+
+// image_mask: bit 0 the local tree, bit k the k-th periodic image
+int walk_lists(WalkBufs &w, const TreeBufs &t, const TreeInfo &info, const PassParams &p, unsigned image_mask,
+               cudaStream_t st, WalkStats &stats);
+
+int build_tree(BuildBufs &b, TreeBufs &t, const PassParams &p, int n, cudaStream_t st, TreeInfo &info,
+               double *t_ms_phase);
+
+}  // namespace ph

@@ -1,0 +1,363 @@
+// Cartesian multipole operators of order 3 (octupole, 20 components), the
+// expansions of src/operator.c written in multi-index form:
+//   P2M  M_a   = sum_p m (-(x_p - c))^a / a!                 (operator.c:13-93)
+//   M2M  M'_a += sum_{b<=a} M_b d^(a-b)/(a-b)!, d = c' - c    (operator.c:96-194)
+//   M2L  L_b  += sum_{|a|<=3-|b|} M_a D_(a+b)(d), d = c_t - c_s (operator.c:255-392)
+//   L2L  L'_b += sum_g L_(b+g) d^g/g!, d = c' - c              (operator.c:395-528)
+//   L2P  a_i  += sum_{|g|<=2} L_(e_i+g) d^g/g!                 (operator.c:197-251)
+// D is the derivative tensor of the short-range Green's function
+// erfc(r/2rs)/r (the LONGSHORT branch), built from its radial factors
+// f_k = ((1/r) d/dr)^k phi:  D_g = f_|g| x^g + f_(|g|-1) sum_i C(g_i,2) x^(g-2e_i).
+// Component order is the reference's (inc/operator.h:24-60).  All in FP64.
+#include <cmath>
+
+#include "fmm_context.cuh"
+#include "multipole.cuh"
+
+#define MP_TB 128
+
+namespace ph {
+namespace {
+
+struct MITab {
+    int e[PH_NMULTI][3];
+    int ord[PH_NMULTI];
+    double invf[PH_NMULTI];
+    int idx[4][4][4];
+};
+
+constexpr MITab make_mitab()
+{
+    MITab t{};
+    int i = 0;
+    for (int k = 0; k <= 3; k++)
+        for (int a = k; a >= 0; a--)
+            for (int b = k - a; b >= 0; b--) {
+                int c = k - a - b;
+                t.e[i][0] = a; t.e[i][1] = b; t.e[i][2] = c;
+                t.ord[i] = k;
+                double f = 1.0;
+                for (int q = 2; q <= a; q++) f *= q;
+                for (int q = 2; q <= b; q++) f *= q;
+                for (int q = 2; q <= c; q++) f *= q;
+                t.invf[i] = 1.0 / f;
+                t.idx[a][b][c] = i;
+                i++;
+            }
+    return t;
+}
+
+constexpr __device__ MITab h_mi = make_mitab();
+
+__device__ __forceinline__ void scaled_monomials(double dx, double dy, double dz, double *out)
+{
+    double px[4] = {1.0, dx, dx * dx, dx * dx * dx};
+    double py[4] = {1.0, dy, dy * dy, dy * dy * dy};
+    double pz[4] = {1.0, dz, dz * dz, dz * dz * dz};
+#pragma unroll
+    for (int i = 0; i < PH_NMULTI; i++)
+        out[i] = px[h_mi.e[i][0]] * py[h_mi.e[i][1]] * pz[h_mi.e[i][2]] * h_mi.invf[i];
+}
+
+// ---------------- P2M ----------------
+__global__ void k_p2m(const double *px, const double *py, const double *pz, const int *ipart, const int *npart,
+                      const double *cx, const double *cy, const double *cz, int nleaf, double mass, double *M)
+{
+    for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < nleaf; l += gridDim.x * blockDim.x) {
+        double acc[PH_NMULTI];
+#pragma unroll
+        for (int i = 0; i < PH_NMULTI; i++) acc[i] = 0.0;
+        double c0 = cx[l], c1 = cy[l], c2 = cz[l];
+        int ip = ipart[l], np = npart[l];
+        for (int p = ip; p < ip + np; p++) {
+            double mono[PH_NMULTI];
+            scaled_monomials(-(px[p] - c0), -(py[p] - c1), -(pz[p] - c2), mono);
+#pragma unroll
+            for (int i = 0; i < PH_NMULTI; i++) acc[i] += mass * mono[i];
+        }
+#pragma unroll
+        for (int i = 0; i < PH_NMULTI; i++) M[(size_t)l * PH_NMULTI + i] = acc[i];
+    }
+}
+
+// ---------------- M2M (one depth, parents gather their two children) ----------------
+__device__ __forceinline__ void m2m_add(double dx, double dy, double dz, const double *Mc, double *out)
+{
+    double mono[PH_NMULTI];
+    scaled_monomials(dx, dy, dz, mono);
+#pragma unroll
+    for (int a = 0; a < PH_NMULTI; a++) {
+        double s = 0.0;
+#pragma unroll
+        for (int b = 0; b < PH_NMULTI; b++) {
+            const int g0 = h_mi.e[a][0] - h_mi.e[b][0], g1 = h_mi.e[a][1] - h_mi.e[b][1],
+                      g2 = h_mi.e[a][2] - h_mi.e[b][2];
+            if (g0 < 0 || g1 < 0 || g2 < 0) continue;
+            s += Mc[b] * mono[h_mi.idx[g0][g1][g2]];
+        }
+        out[a] += s;
+    }
+}
+
+__global__ void k_m2m_depth(const int *list, int begin, int end, int nleaf, const int *son0, const int *son1,
+                            const double *cx, const double *cy, const double *cz, double *M)
+{
+    for (int i = begin + blockIdx.x * blockDim.x + threadIdx.x; i < end; i += gridDim.x * blockDim.x) {
+        int u = list[i];
+        if (u < nleaf) continue;
+        double out[PH_NMULTI];
+#pragma unroll
+        for (int a = 0; a < PH_NMULTI; a++) out[a] = 0.0;
+        double c0 = cx[u], c1 = cy[u], c2 = cz[u];
+        int ch[2] = {son0[u], son1[u]};
+        for (int k = 0; k < 2; k++) {
+            int c = ch[k];
+            double Mc[PH_NMULTI];
+#pragma unroll
+            for (int a = 0; a < PH_NMULTI; a++) Mc[a] = M[(size_t)c * PH_NMULTI + a];
+            m2m_add(c0 - cx[c], c1 - cy[c], c2 - cz[c], Mc, out);
+        }
+#pragma unroll
+        for (int a = 0; a < PH_NMULTI; a++) M[(size_t)u * PH_NMULTI + a] = out[a];
+    }
+}
+
+// ---------------- M2L ----------------
+// radial factors of erfc(r/2rs)/r; with a = 1/(2rs), E = exp(-a^2 r^2), c = 2/sqrt(pi):
+//   f0 = erfc/r, f1 = -erfc/r^3 - c a E/r^2,
+//   f2 = 3 erfc/r^5 + c E (3a/r^4 + 2a^3/r^2),
+//   f3 = -15 erfc/r^7 - c E (15a/r^6 + 10a^3/r^4 + 4a^5/r^2)
+__device__ __forceinline__ void m2l_add(double dx, double dy, double dz, const double *Ms, double rs, double *L)
+{
+    double r = sqrt(dx * dx + dy * dy + dz * dz);
+    double a = 0.5 / rs, a2 = a * a;
+    double u = a * r;
+    double ce = 1.1283791670955126 * exp(-u * u);
+    double er = erfc(u);
+    double ir = 1.0 / r, ir2 = ir * ir;
+    double f[4];
+    f[0] = er * ir;
+    f[1] = -er * ir * ir2 - ce * a * ir2;
+    f[2] = 3.0 * er * ir * ir2 * ir2 + ce * (3.0 * a * ir2 * ir2 + 2.0 * a * a2 * ir2);
+    f[3] = -15.0 * er * ir * ir2 * ir2 * ir2 - ce * (15.0 * a * ir2 * ir2 * ir2 + 10.0 * a * a2 * ir2 * ir2 +
+                                                    4.0 * a * a2 * a2 * ir2);
+    double x[3] = {dx, dy, dz};
+    double pw[3][4];
+#pragma unroll
+    for (int d = 0; d < 3; d++) { pw[d][0] = 1.0; pw[d][1] = x[d]; pw[d][2] = x[d] * x[d]; pw[d][3] = x[d] * x[d] * x[d]; }
+    double D[PH_NMULTI];
+#pragma unroll
+    for (int g = 0; g < PH_NMULTI; g++) {
+        const int e0 = h_mi.e[g][0], e1 = h_mi.e[g][1], e2 = h_mi.e[g][2], k = h_mi.ord[g];
+        double v = f[k] * pw[0][e0] * pw[1][e1] * pw[2][e2];
+        if (k >= 2) {
+            if (e0 >= 2) v += f[k - 1] * (double)(e0 * (e0 - 1) / 2) * pw[0][e0 - 2] * pw[1][e1] * pw[2][e2];
+            if (e1 >= 2) v += f[k - 1] * (double)(e1 * (e1 - 1) / 2) * pw[0][e0] * pw[1][e1 - 2] * pw[2][e2];
+            if (e2 >= 2) v += f[k - 1] * (double)(e2 * (e2 - 1) / 2) * pw[0][e0] * pw[1][e1] * pw[2][e2 - 2];
+        }
+        D[g] = v;
+    }
+#pragma unroll
+    for (int b = 0; b < PH_NMULTI; b++) {
+        double s = 0.0;
+#pragma unroll
+        for (int aa = 0; aa < PH_NMULTI; aa++) {
+            if (h_mi.ord[aa] + h_mi.ord[b] > 3) continue;
+            s += Ms[aa] * D[h_mi.idx[h_mi.e[aa][0] + h_mi.e[b][0]][h_mi.e[aa][1] + h_mi.e[b][1]]
+                                     [h_mi.e[aa][2] + h_mi.e[b][2]]];
+        }
+        L[b] += s;
+    }
+}
+
+__global__ void k_m2l(int nunified, const uint32_t *pool, const long long *off, const int *cnt, const double *cx,
+                      const double *cy, const double *cz, const double *M, double *Lout, double rs, double boxsize)
+{
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nunified; u += gridDim.x * blockDim.x) {
+        int n = cnt[u];
+        if (n == 0) continue;
+        double L[PH_NMULTI];
+#pragma unroll
+        for (int a = 0; a < PH_NMULTI; a++) L[a] = Lout[(size_t)u * PH_NMULTI + a];
+        double c0 = cx[u], c1 = cy[u], c2 = cz[u];
+        long long o = off[u];
+        for (int k = 0; k < n; k++) {
+            uint32_t e = pool[o + k];
+            int s = PH_ENTRY_ID(e), img = PH_ENTRY_IMG(e);
+            double s0 = cx[s], s1 = cy[s], s2 = cz[s];
+            if (img) {
+                int mi, mj, mk;
+                image_offsets(img, mi, mj, mk);
+                s0 += mi * boxsize; s1 += mj * boxsize; s2 += mk * boxsize;
+            }
+            double Ms[PH_NMULTI];
+#pragma unroll
+            for (int a = 0; a < PH_NMULTI; a++) Ms[a] = M[(size_t)s * PH_NMULTI + a];
+            m2l_add(c0 - s0, c1 - s1, c2 - s2, Ms, rs, L);
+        }
+#pragma unroll
+        for (int a = 0; a < PH_NMULTI; a++) Lout[(size_t)u * PH_NMULTI + a] = L[a];
+    }
+}
+
+// ---------------- L2L (one depth: each member adds its parent's expansion) ----------------
+__global__ void k_l2l_depth(const int *list, int begin, int end, const int *parent, const double *cx,
+                            const double *cy, const double *cz, double *L)
+{
+    for (int i = begin + blockIdx.x * blockDim.x + threadIdx.x; i < end; i += gridDim.x * blockDim.x) {
+        int u = list[i];
+        int p = parent[u];
+        if (p < 0) continue;
+        double mono[PH_NMULTI];
+        scaled_monomials(cx[u] - cx[p], cy[u] - cy[p], cz[u] - cz[p], mono);
+        double Lp[PH_NMULTI];
+#pragma unroll
+        for (int a = 0; a < PH_NMULTI; a++) Lp[a] = L[(size_t)p * PH_NMULTI + a];
+#pragma unroll
+        for (int b = 0; b < PH_NMULTI; b++) {
+            double s = 0.0;
+#pragma unroll
+            for (int g = 0; g < PH_NMULTI; g++) {
+                if (h_mi.ord[b] + h_mi.ord[g] > 3) continue;
+                s += Lp[h_mi.idx[h_mi.e[b][0] + h_mi.e[g][0]][h_mi.e[b][1] + h_mi.e[g][1]][h_mi.e[b][2] + h_mi.e[g][2]]] *
+                     mono[g];
+            }
+            L[(size_t)u * PH_NMULTI + b] += s;
+        }
+    }
+}
+
+// ---------------- L2P ----------------
+__global__ void k_l2p(const double *px, const double *py, const double *pz, const int *ipart, const int *npart,
+                      const double *cx, const double *cy, const double *cz, int nleaf, const double *L, double *ax,
+                      double *ay, double *az)
+{
+    int lane = warp_lane();
+    int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    for (int l = gw; l < nleaf; l += nw) {
+        int ip = ipart[l], np = npart[l];
+        const double *Ll = L + (size_t)l * PH_NMULTI;
+        for (int j = lane; j < np; j += 32) {
+            int p = ip + j;
+            double mono[PH_NMULTI];
+            scaled_monomials(px[p] - cx[l], py[p] - cy[l], pz[p] - cz[l], mono);
+            double F[3];
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                double s = 0.0;
+#pragma unroll
+                for (int g = 0; g < PH_NMULTI; g++) {
+                    if (h_mi.ord[g] > 2) continue;
+                    int e0 = h_mi.e[g][0] + (i == 0), e1 = h_mi.e[g][1] + (i == 1), e2 = h_mi.e[g][2] + (i == 2);
+                    s += Ll[h_mi.idx[e0][e1][e2]] * mono[g];
+                }
+                F[i] = s;
+            }
+            ax[p] += F[0];
+            ay[p] += F[1];
+            az[p] += F[2];
+        }
+    }
+}
+
+inline int grid_for(long long n, int tpb)
+{
+    long long g = (n + tpb - 1) / tpb;
+    long long cap = (long long)device_sm_count() * 16;
+    if (g < 1) g = 1;
+    return (int)(g < cap ? g : cap);
+}
+
+}  // namespace
+
+int run_m2l(const MultipoleArgs &a, cudaStream_t st)
+{
+    k_m2l<<<grid_for(a.nunified, MP_TB), MP_TB, 0, st>>>(a.nunified, a.m2l_pool, a.m2l_off, a.m2l_cnt, a.cx, a.cy,
+                                                         a.cz, a.M, a.L, a.rs, a.boxsize);
+    PH_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
+int run_downward(const MultipoleArgs &a, cudaStream_t st)
+{
+    for (int d = 1; d < a.ndepth; d++) {
+        int b = a.depth_off[d], e = a.depth_off[d + 1];
+        if (e > b)
+            k_l2l_depth<<<grid_for(e - b, MP_TB), MP_TB, 0, st>>>(a.depth_list, b, e, a.parent, a.cx, a.cy, a.cz,
+                                                                  a.L);
+    }
+    k_l2p<<<grid_for((long long)a.nleaf * 32, 256), 256, 0, st>>>(a.px, a.py, a.pz, a.ipart, a.npart, a.cx, a.cy,
+                                                                  a.cz, a.nleaf, a.L, a.ax, a.ay, a.az);
+    PH_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
+int run_p2m_m2m(const MultipoleArgs &a, cudaStream_t st)
+{
+    k_p2m<<<grid_for(a.nleaf, MP_TB), MP_TB, 0, st>>>(a.px, a.py, a.pz, a.ipart, a.npart, a.cx, a.cy, a.cz, a.nleaf,
+                                                       a.mass, a.M);
+    for (int d = a.ndepth - 1; d >= 0; d--) {
+        int b = a.depth_off[d], e = a.depth_off[d + 1];
+        if (e > b)
+            k_m2m_depth<<<grid_for(e - b, MP_TB), MP_TB, 0, st>>>(a.depth_list, b, e, a.nleaf, a.son0, a.son1, a.cx,
+                                                                  a.cy, a.cz, a.M);
+    }
+    PH_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
+// batched single operators (operator-level tests and the operator C-ABI)
+namespace {
+__global__ void k_op_m2l(int n, const double *d, const double *M, double *L, double rs)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double Ms[PH_NMULTI], Lo[PH_NMULTI];
+#pragma unroll
+        for (int a = 0; a < PH_NMULTI; a++) { Ms[a] = M[(size_t)i * PH_NMULTI + a]; Lo[a] = L[(size_t)i * PH_NMULTI + a]; }
+        m2l_add(d[3 * i], d[3 * i + 1], d[3 * i + 2], Ms, rs, Lo);
+#pragma unroll
+        for (int a = 0; a < PH_NMULTI; a++) L[(size_t)i * PH_NMULTI + a] = Lo[a];
+    }
+}
+__global__ void k_op_m2m(int n, const double *d, const double *M, double *out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double Ms[PH_NMULTI], o[PH_NMULTI];
+#pragma unroll
+        for (int a = 0; a < PH_NMULTI; a++) { Ms[a] = M[(size_t)i * PH_NMULTI + a]; o[a] = out[(size_t)i * PH_NMULTI + a]; }
+        m2m_add(d[3 * i], d[3 * i + 1], d[3 * i + 2], Ms, o);
+#pragma unroll
+        for (int a = 0; a < PH_NMULTI; a++) out[(size_t)i * PH_NMULTI + a] = o[a];
+    }
+}
+__global__ void k_op_l2l(int n, const double *d, const double *L, double *out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double mono[PH_NMULTI];
+        scaled_monomials(d[3 * i], d[3 * i + 1], d[3 * i + 2], mono);
+        for (int b = 0; b < PH_NMULTI; b++) {
+            double s = 0.0;
+#pragma unroll
+            for (int g = 0; g < PH_NMULTI; g++) {
+                if (h_mi.ord[b] + h_mi.ord[g] > 3) continue;
+                s += L[(size_t)i * PH_NMULTI + h_mi.idx[h_mi.e[b][0] + h_mi.e[g][0]][h_mi.e[b][1] + h_mi.e[g][1]]
+                                                     [h_mi.e[b][2] + h_mi.e[g][2]]] * mono[g];
+            }
+            out[(size_t)i * PH_NMULTI + b] += s;
+        }
+    }
+}
+}  // namespace
+
+int launch_op_batch(int op, int n, const double *d, const double *in, double *inout, double rs, cudaStream_t st)
+{
+    if (n <= 0) return 0;
+    int g = grid_for(n, MP_TB);
+    if (op == 0) k_op_m2l<<<g, MP_TB, 0, st>>>(n, d, in, inout, rs);
+    else if (op == 1) k_op_m2m<<<g, MP_TB, 0, st>>>(n, d, in, inout);
+    else k_op_l2l<<<g, MP_TB, 0, st>>>(n, d, in, inout);
+    PH_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
+}  // namespace ph

@@ -1,0 +1,32 @@
+// Far-field launch interface.
+#pragma once
+
+#include "fmm_context.cuh"
+
+namespace ph {
+
+struct MultipoleArgs {
+    const double *px, *py, *pz;
+    const int *ipart, *npart, *son0, *son1, *parent;
+    const double *cx, *cy, *cz;
+    int nleaf, nunified, ndepth;
+    const int *depth_list;
+    const int *depth_off;  // host array [ndepth+1]
+    const uint32_t *m2l_pool;
+    const long long *m2l_off;
+    const int *m2l_cnt;
+    double *M, *L;  // [nunified][20]
+    double *ax, *ay, *az;
+    double mass, rs, boxsize;
+};
+
+// M2L of every list, accumulated into L
+int run_m2l(const MultipoleArgs &a, cudaStream_t st);
+// L2L top-down, then L2P accumulated into ax/ay/az
+int run_downward(const MultipoleArgs &a, cudaStream_t st);
+// P2M and M2M only (multipoles for callers that read them)
+int run_p2m_m2m(const MultipoleArgs &a, cudaStream_t st);
+// op: 0 m2l (in = M, inout = L, rs), 1 m2m (in = M, inout = M'), 2 l2l (in = L, inout = L')
+int launch_op_batch(int op, int n, const double *d, const double *in, double *inout, double rs, cudaStream_t st);
+
+}  // namespace ph

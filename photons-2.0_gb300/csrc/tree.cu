@@ -1,0 +1,525 @@
+// kd-tree build on the device.
+//
+// Restates src/fmm.c:30-264 (bksort_inplace, build_kdtree, center_kdtree,
+// build_localtree) as a level-synchronous build: every node of one depth
+// is split in the same set of launches.  Per level:
+//   1. each node's particle range is cut into chunks of CHUNK particles;
+//   2. chunk sums of the split coordinate (axis = depth mod 3) and a
+//      fixed-order reduction give the node's mean;
+//   3. the reference's two-ended swap partition (src/fmm.c:58-72) is
+//      reproduced exactly: with S particles not above the mean, the k-th
+//      particle above the mean counted from the left among positions < S
+//      trades places with the k-th particle not above the mean counted from
+//      the right among positions >= S.  Ranks come from chunk counts, so the
+//      swaps are independent and run in parallel;
+//   4. children with <= MAXLEAF particles become leaves, the others nodes
+//      of the next level; child boxes come from the split plane.
+// Special cases follow the reference: a pair splits at its midpoint and is
+// ordered (src/fmm.c:38-47); if no particle lies above the mean the last
+// one goes to the upper child.
+// Afterwards leaves are renumbered in the reference's depth-first order and
+// nodes in preorder (src/fmm.c:101-118), and geometry is written in the
+// unified index space.
+//
+// The mean is a deterministic parallel sum, not the reference's sequential
+// one, so a mean can differ from the reference's in the last bits; that
+// changes the partition only for a particle within those bits of the mean.
+#include <cstdio>
+#include <vector>
+
+#include "fmm_context.cuh"
+
+#define CHUNK 1024
+#define TB 256
+
+namespace ph {
+namespace {
+
+__device__ __forceinline__ int upper_bound_i32(const int *a, int n, int v)
+{
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (a[mid] <= v) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ const double *axis_ptr(const double *x, const double *y, const double *z, int D)
+{
+    return D == 0 ? x : (D == 1 ? y : z);
+}
+
+__global__ void k_init_root(BuildBufs b, int n, double L)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        b.tn_start[0] = 0;
+        b.tn_len[0] = n;
+        b.tn_depth[0] = 0;
+        b.tn_parent[0] = -1;
+        // root box as src/fmm.c:194-197 derives it from the domain box
+        // (centre 0.5*(L+0), width L-0, src/toptree.c:150-159)
+        double c = 0.5 * (L + 0.0), w = L - 0.0;
+        for (int d = 0; d < 3; d++) {
+            b.tn_box[d * b.cap_nodes] = c - 0.5 * w;
+            b.tn_box[(3 + d) * b.cap_nodes] = c + 0.5 * w;
+        }
+        for (int i = 0; i < BC_NCOUNTERS; i++) b.cnt[i] = 0;
+        b.cnt[BC_LEVEL_COUNT] = 1;
+    }
+}
+
+__global__ void k_init_particles(const double *__restrict__ pos, int n, BuildBufs b)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        b.x[i] = pos[3 * i];
+        b.y[i] = pos[3 * i + 1];
+        b.z[i] = pos[3 * i + 2];
+        b.perm[i] = i;
+    }
+}
+
+
+__global__ void k_level_nch(BuildBufs b, int lb, int C)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x)
+        b.tn_nch[i] = (b.tn_len[lb + i] + CHUNK - 1) / CHUNK;
+}
+
+__global__ void k_chunk_sum(BuildBufs b, int lb, int C, int D)
+{
+    const double *coord = axis_ptr(b.x, b.y, b.z, D);
+    int W = b.cnt[BC_W];
+    int lane = warp_lane();
+    int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    for (int w = gw; w < W; w += nw) {
+        int i = upper_bound_i32(b.tn_chunk_base, C, w) - 1;
+        int t = lb + i;
+        int start = b.tn_start[t], len = b.tn_len[t];
+        int s0 = (w - b.tn_chunk_base[i]) * CHUNK;
+        int s1 = min(len, s0 + CHUNK);
+        double s = 0.0;
+        for (int k = s0 + lane; k < s1; k += 32) s += coord[start + k];
+        s = warp_sum_d(s);
+        if (lane == 0) b.ch_partial[w] = s;
+    }
+}
+
+__global__ void k_node_mean(BuildBufs b, int lb, int C, int D)
+{
+    const double *coord = axis_ptr(b.x, b.y, b.z, D);
+    int lane = warp_lane();
+    int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = gw; i < C; i += nw) {
+        int t = lb + i;
+        int len = b.tn_len[t];
+        if (len == 2) {
+            int start = b.tn_start[t];
+            if (lane == 0) b.tn_split[t] = 0.5 * (coord[start] + coord[start + 1]);
+            continue;
+        }
+        int c0 = b.tn_chunk_base[i], nc = b.tn_nch[i];
+        double s = 0.0;
+        for (int k = lane; k < nc; k += 32) s += b.ch_partial[c0 + k];
+        s = warp_sum_d(s);
+        if (lane == 0) b.tn_split[t] = s / (double)len;
+    }
+}
+
+__global__ void k_chunk_count(BuildBufs b, int lb, int C, int D)
+{
+    const double *coord = axis_ptr(b.x, b.y, b.z, D);
+    int W = b.cnt[BC_W];
+    int lane = warp_lane();
+    int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    for (int w = gw; w < W; w += nw) {
+        int i = upper_bound_i32(b.tn_chunk_base, C, w) - 1;
+        int t = lb + i;
+        int start = b.tn_start[t], len = b.tn_len[t];
+        double mean = b.tn_split[t];
+        int s0 = (w - b.tn_chunk_base[i]) * CHUNK;
+        int s1 = min(len, s0 + CHUNK);
+        int c = 0;
+        for (int k = s0 + lane; k < s1; k += 32) c += !(coord[start + k] > mean);
+        c = __reduce_add_sync(0xffffffffu, c);
+        if (lane == 0) b.ch_cnt[w] = c;
+    }
+}
+
+// per node: prefix of chunk counts, partition sizes, child kinds
+__global__ void k_node_split(BuildBufs b, int lb, int C, int maxleaf)
+{
+    int lane = warp_lane();
+    int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = gw; i < C; i += nw) {
+        int t = lb + i;
+        int len = b.tn_len[t];
+        int c0 = b.tn_chunk_base[i], nc = b.tn_nch[i];
+        int carry = 0;
+        for (int k0 = 0; k0 < nc; k0 += 32) {
+            int k = k0 + lane;
+            int v = (k < nc) ? b.ch_cnt[c0 + k] : 0;
+            int incl = warp_incl_scan(v);
+            if (k < nc) b.ch_small_base[c0 + k] = carry + incl - v;
+            carry += shfl(incl, 31);
+        }
+        if (lane == 0) {
+            int S = carry;
+            int mode, left;
+            if (len == 2) { mode = 2; left = 1; }
+            else if (S == len) { mode = 1; left = len - 1; }
+            else { mode = 0; left = S; }
+            b.tn_S[t] = S;
+            b.tn_mode[t] = mode;
+            int right = len - left;
+            // child sizes are stashed in child codes until the children exist
+            b.tn_child0[t] = left;
+            b.tn_child1[t] = right;
+            b.tn_nodeflag[i] = (left > maxleaf) + (right > maxleaf);
+            b.tn_leafflag[i] = (left <= maxleaf) + (right <= maxleaf);
+        }
+    }
+}
+
+__global__ void k_make_children(BuildBufs b, int lb, int C, int maxleaf, int D)
+{
+    int leaves_before = b.cnt[BC_LEAVES];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
+        int t = lb + i;
+        int start = b.tn_start[t];
+        int depth = b.tn_depth[t];
+        int sizes[2] = {b.tn_child0[t], b.tn_child1[t]};
+        double split = b.tn_split[t];
+        double lo[3], hi[3];
+        for (int d = 0; d < 3; d++) {
+            lo[d] = b.tn_box[d * b.cap_nodes + t];
+            hi[d] = b.tn_box[(3 + d) * b.cap_nodes + t];
+        }
+        int nid = lb + C + b.tn_nodebase[i];
+        int lid = leaves_before + b.tn_leafbase[i];
+        int code[2];
+        int ip = start;
+        for (int c = 0; c < 2; c++) {
+            double clo[3] = {lo[0], lo[1], lo[2]}, chi[3] = {hi[0], hi[1], hi[2]};
+            if (c == 0) chi[D] = split;
+            else clo[D] = split;
+            if (sizes[c] <= maxleaf) {
+                if (lid >= b.cap_leaves) {
+                    atomicOr(&b.cnt[BC_FLAGS], PH_FLAG_LEAF_CAPACITY);
+                    code[c] = ~0;
+                } else {
+                    b.tl_start[lid] = ip;
+                    b.tl_len[lid] = sizes[c];
+                    b.tl_depth[lid] = depth + 1;
+                    b.tl_parent[lid] = t;
+                    for (int d = 0; d < 3; d++) {
+                        b.tl_box[d * b.cap_leaves + lid] = clo[d];
+                        b.tl_box[(3 + d) * b.cap_leaves + lid] = chi[d];
+                    }
+                    code[c] = ~lid;
+                }
+                lid++;
+            } else {
+                if (nid >= b.cap_nodes) {
+                    atomicOr(&b.cnt[BC_FLAGS], PH_FLAG_NODE_CAPACITY);
+                    code[c] = 0;
+                } else {
+                    b.tn_start[nid] = ip;
+                    b.tn_len[nid] = sizes[c];
+                    b.tn_depth[nid] = depth + 1;
+                    b.tn_parent[nid] = t;
+                    for (int d = 0; d < 3; d++) {
+                        b.tn_box[d * b.cap_nodes + nid] = clo[d];
+                        b.tn_box[(3 + d) * b.cap_nodes + nid] = chi[d];
+                    }
+                    code[c] = nid;
+                }
+                nid++;
+            }
+            ip += sizes[c];
+        }
+        b.tn_child0[t] = code[0];
+        b.tn_child1[t] = code[1];
+    }
+}
+
+__global__ void k_level_finish(BuildBufs b)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        b.cnt[BC_LEAVES] += b.cnt[BC_NEW_LEAVES];
+        b.cnt[BC_LEVEL_COUNT] = b.cnt[BC_NEXT_NODES];
+    }
+}
+
+// Ranks for the swap partition.  A particle not above the mean that sits in
+// the right region (p >= S) publishes its position under slot S-1-r (r =
+// its rank among such particles, counted from the left); a particle above
+// the mean in the left region (p < S) records slot p-r (its rank among
+// particles above the mean).  Slot k pairs the k-th from the left with the
+// k-th from the right, which is the order src/fmm.c:60-72 swaps them in.
+__global__ void k_rank(BuildBufs b, int lb, int C, int D)
+{
+    const double *coord = axis_ptr(b.x, b.y, b.z, D);
+    int W = b.cnt[BC_W];
+    int lane = warp_lane();
+    unsigned lt = (1u << lane) - 1u;
+    int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    for (int w = gw; w < W; w += nw) {
+        int i = upper_bound_i32(b.tn_chunk_base, C, w) - 1;
+        int t = lb + i;
+        if (b.tn_mode[t] != 0) continue;
+        int start = b.tn_start[t], len = b.tn_len[t];
+        double mean = b.tn_split[t];
+        int S = b.tn_S[t];
+        int s0 = (w - b.tn_chunk_base[i]) * CHUNK;
+        int s1 = min(len, s0 + CHUNK);
+        int run = b.ch_small_base[w];
+        for (int k0 = s0; k0 < s1; k0 += 32) {
+            int p = k0 + lane;
+            bool in = p < s1;
+            bool small = in && !(coord[start + p] > mean);
+            unsigned m = __ballot_sync(0xffffffffu, small);
+            int r = run + __popc(m & lt);
+            if (in) {
+                if (p < S) b.bigslot[start + p] = small ? -1 : (p - r);
+                else if (small) b.smallpos[start + (S - 1 - r)] = p;
+            }
+            run += __popc(m);
+        }
+    }
+}
+
+__device__ __forceinline__ void swap_particles(BuildBufs &b, int i, int j)
+{
+    double t;
+    t = b.x[i]; b.x[i] = b.x[j]; b.x[j] = t;
+    t = b.y[i]; b.y[i] = b.y[j]; b.y[j] = t;
+    t = b.z[i]; b.z[i] = b.z[j]; b.z[j] = t;
+    int q = b.perm[i]; b.perm[i] = b.perm[j]; b.perm[j] = q;
+}
+
+// Each pair is exchanged by the thread of its left-region member only, so
+// the exchanges are disjoint.
+__global__ void k_swap(BuildBufs b, int lb, int C, int D)
+{
+    const double *coord = axis_ptr(b.x, b.y, b.z, D);
+    int W = b.cnt[BC_W];
+    int lane = warp_lane();
+    int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    for (int w = gw; w < W; w += nw) {
+        int i = upper_bound_i32(b.tn_chunk_base, C, w) - 1;
+        int t = lb + i;
+        int mode = b.tn_mode[t];
+        int start = b.tn_start[t], len = b.tn_len[t];
+        if (mode == 2) {
+            if (lane == 0 && coord[start] > coord[start + 1]) swap_particles(b, start, start + 1);
+            continue;
+        }
+        if (mode != 0) continue;
+        int S = b.tn_S[t];
+        int s0 = (w - b.tn_chunk_base[i]) * CHUNK;
+        int s1 = min(min(len, s0 + CHUNK), S);
+        for (int p = s0 + lane; p < s1; p += 32) {
+            int k = b.bigslot[start + p];
+            if (k >= 0) swap_particles(b, start + p, start + b.smallpos[start + k]);
+        }
+    }
+}
+
+// ---------------- renumbering ----------------
+__global__ void k_subtree_counts(BuildBufs b, int lb, int C)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
+        int t = lb + i;
+        int sn = 1, sl = 0;
+        int c[2] = {b.tn_child0[t], b.tn_child1[t]};
+        for (int k = 0; k < 2; k++) {
+            if (PH_IS_LEAF_CODE(c[k])) sl += 1;
+            else { sn += b.tn_sub_nodes[c[k]]; sl += b.tn_sub_leaves[c[k]]; }
+        }
+        b.tn_sub_nodes[t] = sn;
+        b.tn_sub_leaves[t] = sl;
+    }
+}
+
+// preorder node numbers and depth-first leaf numbers, src/fmm.c:101-118
+__global__ void k_number(BuildBufs b, int lb, int C)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
+        int t = lb + i;
+        if (t == 0) { b.tn_pre[0] = 0; b.tn_lbase[0] = 0; }
+        int pre = b.tn_pre[t], lbase = b.tn_lbase[t];
+        int c0 = b.tn_child0[t], c1 = b.tn_child1[t];
+        int off_nodes, off_leaves;
+        if (PH_IS_LEAF_CODE(c0)) { b.tl_final[~c0] = lbase; off_nodes = 0; off_leaves = 1; }
+        else { b.tn_pre[c0] = pre + 1; b.tn_lbase[c0] = lbase; off_nodes = b.tn_sub_nodes[c0]; off_leaves = b.tn_sub_leaves[c0]; }
+        if (PH_IS_LEAF_CODE(c1)) b.tl_final[~c1] = lbase + off_leaves;
+        else { b.tn_pre[c1] = pre + 1 + off_nodes; b.tn_lbase[c1] = lbase + off_leaves; }
+    }
+}
+
+__device__ __forceinline__ void write_geom(TreeBufs &T, int u, const double *box, int cap, int idx)
+{
+    double lo0 = box[0 * cap + idx], lo1 = box[1 * cap + idx], lo2 = box[2 * cap + idx];
+    double hi0 = box[3 * cap + idx], hi1 = box[4 * cap + idx], hi2 = box[5 * cap + idx];
+    // width = right - left, centre = 0.5*(right + left), src/fmm.c:126-131
+    double w0 = hi0 - lo0, w1 = hi1 - lo1, w2 = hi2 - lo2;
+    T.wx[u] = w0; T.wy[u] = w1; T.wz[u] = w2;
+    T.cx[u] = 0.5 * (hi0 + lo0); T.cy[u] = 0.5 * (hi1 + lo1); T.cz[u] = 0.5 * (hi2 + lo2);
+    T.wsum[u] = w0 + w1 + w2;
+}
+
+__global__ void k_scatter_nodes(BuildBufs b, TreeBufs T, int nnodes, int nleaves)
+{
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nnodes; t += gridDim.x * blockDim.x) {
+        int u = nleaves + b.tn_pre[t];
+        T.ipart[u] = b.tn_start[t];
+        T.npart[u] = b.tn_len[t];
+        T.depth[u] = b.tn_depth[t];
+        int par = b.tn_parent[t];
+        T.parent[u] = par < 0 ? -1 : nleaves + b.tn_pre[par];
+        int c0 = b.tn_child0[t], c1 = b.tn_child1[t];
+        T.son0[u] = PH_IS_LEAF_CODE(c0) ? b.tl_final[~c0] : nleaves + b.tn_pre[c0];
+        T.son1[u] = PH_IS_LEAF_CODE(c1) ? b.tl_final[~c1] : nleaves + b.tn_pre[c1];
+        T.split[u] = b.tn_split[t];
+        write_geom(T, u, b.tn_box, b.cap_nodes, t);
+    }
+}
+
+__global__ void k_scatter_leaves(BuildBufs b, TreeBufs T, int nleaves)
+{
+    for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < nleaves; l += gridDim.x * blockDim.x) {
+        int u = b.tl_final[l];
+        T.ipart[u] = b.tl_start[l];
+        T.npart[u] = b.tl_len[l];
+        T.depth[u] = b.tl_depth[l];
+        T.parent[u] = nleaves + b.tn_pre[b.tl_parent[l]];
+        T.son0[u] = -1;
+        T.son1[u] = -1;
+        T.split[u] = 0.0;
+        write_geom(T, u, b.tl_box, b.cap_leaves, l);
+    }
+}
+
+// depth lists: depth d holds the level-d nodes (temp order) then the leaves
+// created by level d-1 (temp order)
+__global__ void k_depth_lists(BuildBufs b, TreeBufs T, int d, int node_b, int node_c, int leaf_b, int leaf_c,
+                              int off, int nleaves)
+{
+    int tot = node_c + leaf_c;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += gridDim.x * blockDim.x) {
+        int u = (i < node_c) ? nleaves + b.tn_pre[node_b + i] : b.tl_final[leaf_b + (i - node_c)];
+        T.depth_list[off + i] = u;
+    }
+    (void)d;
+}
+
+inline int grid_for(int n, int tpb, int maxblocks)
+{
+    int g = (n + tpb - 1) / tpb;
+    if (g < 1) g = 1;
+    return g < maxblocks ? g : maxblocks;
+}
+
+}  // namespace
+
+int launch_init_particles(BuildBufs &b, const double *pos, int n, cudaStream_t st)
+{
+    k_init_particles<<<device_sm_count() * 8, TB, 0, st>>>(pos, n, b);
+    PH_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
+int build_tree(BuildBufs &b, TreeBufs &T, const PassParams &p, int n, cudaStream_t st, TreeInfo &info,
+               double *t_ms_phase)
+{
+    (void)t_ms_phase;
+    const int sms = device_sm_count();
+    const int maxb = sms * 8;
+    const int L = 0;
+    (void)L;
+    k_init_root<<<1, 1, 0, st>>>(b, n, p.boxsize);
+    PH_CUDA_CHECK(cudaGetLastError());
+
+    std::vector<int> lvl_begin, lvl_count, leaf_begin, leaf_count;
+    int lb = 0;
+    int leaves_total = 0;
+    int h[BC_NCOUNTERS];
+    for (int d = 0;; d++) {
+        PH_CUDA_CHECK(cudaMemcpyAsync(h, b.cnt, sizeof(h), cudaMemcpyDeviceToHost, st));
+        PH_CUDA_CHECK(cudaStreamSynchronize(st));
+        if (h[BC_FLAGS] & PH_FLAG_LEAF_CAPACITY)
+            return ph_set_error(4, "leaf capacity 2N/MAXLEAF=%d exceeded by the mean-split tree", b.cap_leaves);
+        if (h[BC_FLAGS] & PH_FLAG_NODE_CAPACITY)
+            return ph_set_error(4, "node capacity 2N/MAXLEAF=%d exceeded by the mean-split tree", b.cap_nodes);
+        int C = h[BC_LEVEL_COUNT];
+        if (d > 0) {
+            leaf_begin.push_back(leaves_total);
+            leaf_count.push_back(h[BC_LEAVES] - leaves_total);
+            leaves_total = h[BC_LEAVES];
+        } else {
+            leaf_begin.push_back(0);
+            leaf_count.push_back(0);
+        }
+        if (C == 0) break;
+        if (d >= T.max_depth_cap) return ph_set_error(7, "tree deeper than %d levels", T.max_depth_cap);
+        lvl_begin.push_back(lb);
+        lvl_count.push_back(C);
+        int D = d % 3;  // direct_local_start = 0 at one rank; axis cycles (src/fmm.c:99)
+
+        k_level_nch<<<grid_for(C, TB, maxb), TB, 0, st>>>(b, lb, C);
+        scan_exclusive_i32(b.tn_nch, b.tn_chunk_base, b.cnt + BC_LEVEL_COUNT, b.cap_nodes, b.cnt + BC_W,
+                           b.scan_scratch, b.scan_scratch_elems, st);
+        int wgrid = maxb;
+        k_chunk_sum<<<wgrid, TB, 0, st>>>(b, lb, C, D);
+        k_node_mean<<<grid_for(C * 32, TB, maxb), TB, 0, st>>>(b, lb, C, D);
+        k_chunk_count<<<wgrid, TB, 0, st>>>(b, lb, C, D);
+        k_node_split<<<grid_for(C * 32, TB, maxb), TB, 0, st>>>(b, lb, C, p.maxleaf);
+        scan_exclusive_i32(b.tn_nodeflag, b.tn_nodebase, b.cnt + BC_LEVEL_COUNT, b.cap_nodes, b.cnt + BC_NEXT_NODES,
+                           b.scan_scratch, b.scan_scratch_elems, st);
+        scan_exclusive_i32(b.tn_leafflag, b.tn_leafbase, b.cnt + BC_LEVEL_COUNT, b.cap_nodes, b.cnt + BC_NEW_LEAVES,
+                           b.scan_scratch, b.scan_scratch_elems, st);
+        k_make_children<<<grid_for(C, TB, maxb), TB, 0, st>>>(b, lb, C, p.maxleaf, D);
+        k_rank<<<wgrid, TB, 0, st>>>(b, lb, C, D);
+        k_swap<<<wgrid, TB, 0, st>>>(b, lb, C, D);
+        k_level_finish<<<1, 1, 0, st>>>(b);
+        PH_CUDA_CHECK(cudaGetLastError());
+        lb += C;
+    }
+    int nnodes = lb;
+    int nleaves = leaves_total;
+    int nlev = (int)lvl_begin.size();
+    // subtree sizes bottom-up, numbers top-down
+    for (int d = nlev - 1; d >= 0; d--)
+        k_subtree_counts<<<grid_for(lvl_count[d], TB, maxb), TB, 0, st>>>(b, lvl_begin[d], lvl_count[d]);
+    for (int d = 0; d < nlev; d++)
+        k_number<<<grid_for(lvl_count[d], TB, maxb), TB, 0, st>>>(b, lvl_begin[d], lvl_count[d]);
+    k_scatter_nodes<<<grid_for(nnodes, TB, maxb), TB, 0, st>>>(b, T, nnodes, nleaves);
+    k_scatter_leaves<<<grid_for(nleaves, TB, maxb), TB, 0, st>>>(b, T, nleaves);
+    // depth lists: depth d = nodes of level d + leaves created by level d-1
+    int ndepth = nlev + 1;  // leaves can sit one level below the deepest nodes
+    std::vector<int> doff(ndepth + 1, 0);
+    for (int d = 0; d < ndepth; d++) {
+        int nc = d < nlev ? lvl_count[d] : 0;
+        int lc = d < (int)leaf_count.size() ? leaf_count[d] : 0;
+        doff[d + 1] = doff[d] + nc + lc;
+    }
+    for (int d = 0; d < ndepth; d++) {
+        int nc = d < nlev ? lvl_count[d] : 0;
+        int nbeg = d < nlev ? lvl_begin[d] : 0;
+        int lc = d < (int)leaf_count.size() ? leaf_count[d] : 0;
+        int lbeg = d < (int)leaf_begin.size() ? leaf_begin[d] : 0;
+        if (nc + lc == 0) continue;
+        k_depth_lists<<<grid_for(nc + lc, TB, maxb), TB, 0, st>>>(b, T, d, nbeg, nc, lbeg, lc, doff[d], nleaves);
+    }
+    PH_CUDA_CHECK(cudaMemcpyAsync(T.depth_off, doff.data(), sizeof(int) * (ndepth + 1), cudaMemcpyHostToDevice, st));
+    PH_CUDA_CHECK(cudaGetLastError());
+    info.nleaf = nleaves;
+    info.nnode = nnodes;
+    info.depth = ndepth - 1;
+    info.depth_off.assign(doff.begin(), doff.end());
+    return 0;
+}
+
+}  // namespace ph

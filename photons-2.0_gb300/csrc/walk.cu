@@ -1,0 +1,344 @@
+// Dual-tree walk: interaction lists for the local tree and the 26 periodic
+// images in one traversal.
+//
+// Restates the pair rules of src/fmm.c:406-538 (walk_task_p2p),
+// src/fmm.c:569-712 (walk_task_m2l), src/remotes.c:213-372
+// (walk_task_p2p_ext) and src/remotes.c:405-552 (walk_task_m2l_ext).  The
+// P2P and M2L walks of the reference make the same decisions and differ
+// only in what they record, so one traversal records both.  The image
+// walks start from (root, shifted root) and use the sender-side pruning of
+// src/remotes.c:60-169; the pruned copy is not materialised, a node's
+// pruning for an image is evaluated where the walk needs it.
+//
+// Organisation: the walk is processed target-first.  Every pair (a, b)
+// the reference visits is rewritten by one rule that either records it,
+// drops it, opens the source b (pairs (a, b0), (a, b1): same target), or
+// opens the target a (pairs (a0, b), (a1, b)).  Pairs that open the target
+// go to a's push-down list, which both children inherit; the self pair
+// (a, a) of a node pushes down (a0, a) and (a1, a) in the form of its two
+// children.  So the whole walk is: for each depth, for each target at that
+// depth, expand the inherited list with a warp-wide stack until only
+// records and push-downs remain.  The multiset of recorded pairs is the
+// reference's; only their order differs.
+//
+// Acceptance is evaluated in FP64 with explicit round-to-nearest operations
+// (no contraction) so that every decision equals the reference's.
+#include <cstdio>
+#include <cstring>
+
+#include "fmm_context.cuh"
+
+#define WALK_TB 256
+
+namespace ph {
+namespace {
+
+struct Geo {
+    const double *cx, *cy, *cz, *wx, *wy, *wz, *wsum;
+    const int *son0, *son1, *npart, *parent;
+};
+
+// MAC of src/fmm.c:266-326 (LONGSHORT): 1 accept, 0 open, -1 drop
+__device__ __forceinline__ int acceptance_fp64(double wi0, double wi1, double wi2, double wj0, double wj1, double wj2,
+                                               double d0, double d1, double d2, double theta2, double c2)
+{
+    double w0 = __dmul_rn(__dadd_rn(wi0, wj0), 0.5);
+    double w1 = __dmul_rn(__dadd_rn(wi1, wj1), 0.5);
+    double w2 = __dmul_rn(__dadd_rn(wi2, wj2), 0.5);
+    double dd2 = __dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2));
+    double m0 = __dsub_rn(fabs(d0), w0), m1 = __dsub_rn(fabs(d1), w1), m2 = __dsub_rn(fabs(d2), w2);
+    if (m0 <= 0.0) m0 = 0.0;
+    if (m1 <= 0.0) m1 = 0.0;
+    if (m2 <= 0.0) m2 = 0.0;
+    if (__dadd_rn(__dadd_rn(m0, m1), m2) < 0.0001) return 0;
+    double dm2 = __dadd_rn(__dadd_rn(__dmul_rn(m0, m0), __dmul_rn(m1, m1)), __dmul_rn(m2, m2));
+    if (dm2 >= c2) return -1;
+    if (dd2 > c2) return 0;
+    double wmax = w0;
+    if (w1 > wmax) wmax = w1;
+    if (w2 > wmax) wmax = w2;
+    wmax = __dmul_rn(wmax, 2.0);
+    return (__dmul_rn(wmax, wmax) < __dmul_rn(theta2, dd2)) ? 1 : 0;
+}
+
+struct WalkArgs {
+    Geo g;
+    WalkBufs w;
+    const int *depth_list;
+    int list_begin, list_end;
+    int depth, nleaf, root;
+    int nroot;               // entries of the root's list: (root, img) for the selected images
+    int root_img[PH_NIMG];
+    double boxsize, theta2, c2, rcut, theta;
+};
+
+// sender-side pruning of an image node, src/remotes.c:97-158
+__device__ __forceinline__ bool image_pruned(const WalkArgs &A, int b, double s0, double s1, double s2)
+{
+    const Geo &g = A.g;
+    int r = A.root;
+    double sx[3] = {s0, s1, s2};
+    double rc[3] = {g.cx[r], g.cy[r], g.cz[r]}, rw[3] = {g.wx[r], g.wy[r], g.wz[r]};
+    double bc[3] = {g.cx[b], g.cy[b], g.cz[b]}, bw[3] = {g.wx[b], g.wy[b], g.wz[b]};
+    double dr = 0.0;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        double gap = __dsub_rn(__dsub_rn(rc[d], bc[d]), sx[d]);
+        if (gap < 0.0) gap = -gap;
+        gap = __dsub_rn(gap, __dmul_rn(__dadd_rn(rw[d], bw[d]), 0.5));
+        if (gap > 0.0) dr = __dadd_rn(dr, __dmul_rn(gap, gap));
+    }
+    dr = __dsqrt_rn(dr);
+    double wmax = bw[0];
+    if (wmax < bw[1]) wmax = bw[1];
+    if (wmax < bw[2]) wmax = bw[2];
+    if (dr >= A.rcut) return true;
+    return wmax < __dmul_rn(__dmul_rn(0.95, A.theta), dr);
+}
+
+enum { OUT_NONE = 0, OUT_P2P = 1, OUT_M2L = 2, OUT_PUSH = 3, OUT_OPEN = 4, OUT_SELF_PUSH = 5 };
+
+__global__ void __launch_bounds__(WALK_TB) k_walk_level(WalkArgs A)
+{
+    const Geo &g = A.g;
+    WalkBufs &W = A.w;
+    const int lane = warp_lane();
+    const unsigned lt = (1u << lane) - 1u;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    if (gw >= W.nwarps) return;
+    uint32_t *stack = W.scratch + (size_t)gw * (W.stack_cap + 3 * W.stage_cap);
+    uint32_t *st_p2p = stack + W.stack_cap;
+    uint32_t *st_m2l = st_p2p + W.stage_cap;
+    uint32_t *st_pd = st_m2l + W.stage_cap;
+    const int parity = A.depth & 1;
+    unsigned long long c_p2p_loc = 0, c_p2p_img = 0, c_m2l_loc = 0, c_m2l_img = 0, c_pl = 0, c_pi = 0;
+    unsigned flags = 0;
+    int max_stack = 0, max_stage = 0;
+
+    for (int ti = A.list_begin + gw; ti < A.list_end; ti += nw) {
+        const int a = A.depth_list[ti];
+        const bool leaf_a = a < A.nleaf;
+        const double ca0 = g.cx[a], ca1 = g.cy[a], ca2 = g.cz[a];
+        const double wa0 = g.wx[a], wa1 = g.wy[a], wa2 = g.wz[a], wsa = g.wsum[a];
+        const int na = g.npart[a];
+        const int a0 = leaf_a ? -1 : g.son0[a], a1 = leaf_a ? -1 : g.son1[a];
+        const int par = g.parent[a];
+        const uint32_t *input = nullptr;
+        int n_in;
+        if (par < 0) {
+            n_in = A.nroot;
+        } else {
+            input = W.pd_pool[parity ^ 1] + W.pd_off[par];
+            n_in = W.pd_cnt[par];
+        }
+        int top = 0, in_pos = 0;
+        int n_p2p = 0, n_m2l = 0, n_pd = 0;
+        for (;;) {
+            int k;
+            uint32_t e = 0;
+            if (top > 0) {
+                k = min(32, top);
+                top -= k;
+                if (lane < k) e = stack[top + lane];
+            } else if (in_pos < n_in) {
+                k = min(32, n_in - in_pos);
+                if (lane < k) e = input ? input[in_pos + lane] : PH_ENTRY(a, A.root_img[in_pos + lane]);
+                in_pos += k;
+            } else {
+                break;
+            }
+            __syncwarp();
+            int kind = OUT_NONE;
+            int b = PH_ENTRY_ID(e), img = PH_ENTRY_IMG(e);
+            if (lane < k) {
+                const bool leaf_b = b < A.nleaf;
+                if (img == 0 && b == a) {
+                    if (leaf_a) {
+                        kind = OUT_P2P;
+                        c_p2p_loc++;
+                        c_pl += (unsigned long long)na * (na - 1);
+                    } else {
+                        kind = OUT_SELF_PUSH;
+                    }
+                } else if (leaf_a && leaf_b) {
+                    kind = OUT_P2P;
+                    unsigned long long pr = (unsigned long long)na * g.npart[b];
+                    if (img == 0) { c_p2p_loc++; c_pl += pr; }
+                    else { c_p2p_img++; c_pi += pr; }
+                } else {
+                    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+                    int mi, mj, mk;
+                    image_offsets(img, mi, mj, mk);
+                    s0 = mi * A.boxsize; s1 = mj * A.boxsize; s2 = mk * A.boxsize;
+                    // image node centre = local centre + shift (src/remotes.c:123-125)
+                    double cb0 = g.cx[b], cb1 = g.cy[b], cb2 = g.cz[b];
+                    if (img) { cb0 = __dadd_rn(cb0, s0); cb1 = __dadd_rn(cb1, s1); cb2 = __dadd_rn(cb2, s2); }
+                    int flag = acceptance_fp64(wa0, wa1, wa2, g.wx[b], g.wy[b], g.wz[b], __dsub_rn(ca0, cb0),
+                                               __dsub_rn(ca1, cb1), __dsub_rn(ca2, cb2), A.theta2, A.c2);
+                    if (flag == -1) {
+                        kind = OUT_NONE;
+                    } else if (img == 0) {
+                        if (flag == 1) kind = OUT_M2L;
+                        else if (leaf_a) kind = OUT_OPEN;
+                        else if (leaf_b) kind = OUT_PUSH;
+                        else kind = (wsa > g.wsum[b]) ? OUT_PUSH : OUT_OPEN;
+                    } else {
+                        bool pruned = !leaf_b && image_pruned(A, b, s0, s1, s2);
+                        if (leaf_a) kind = (flag == 1 || pruned) ? OUT_M2L : OUT_OPEN;
+                        else if (flag == 1) kind = OUT_M2L;
+                        else kind = (leaf_b || pruned || wsa > g.wsum[b]) ? OUT_PUSH : OUT_OPEN;
+                    }
+                    if (kind == OUT_M2L) {
+                        if (img == 0) c_m2l_loc++;
+                        else c_m2l_img++;
+                    }
+                }
+            }
+            // compaction
+            unsigned mp = __ballot_sync(0xffffffffu, kind == OUT_P2P);
+            unsigned mm = __ballot_sync(0xffffffffu, kind == OUT_M2L);
+            int npush = (kind == OUT_PUSH) ? 1 : (kind == OUT_SELF_PUSH ? 2 : 0);
+            int nopen = (kind == OUT_OPEN) ? 2 : 0;
+            int push_incl = warp_incl_scan(npush);
+            int open_incl = warp_incl_scan(nopen);
+            int push_tot = shfl(push_incl, 31), open_tot = shfl(open_incl, 31);
+            if (kind == OUT_P2P) {
+                int pos = n_p2p + __popc(mp & lt);
+                if (pos < W.stage_cap) st_p2p[pos] = e;
+            } else if (kind == OUT_M2L) {
+                int pos = n_m2l + __popc(mm & lt);
+                if (pos < W.stage_cap) st_m2l[pos] = e;
+            } else if (kind == OUT_PUSH) {
+                int pos = n_pd + push_incl - 1;
+                if (pos < W.stage_cap) st_pd[pos] = e;
+            } else if (kind == OUT_SELF_PUSH) {
+                int pos = n_pd + push_incl - 2;
+                if (pos + 1 < W.stage_cap) {
+                    st_pd[pos] = PH_ENTRY(a0, 0);
+                    st_pd[pos + 1] = PH_ENTRY(a1, 0);
+                }
+            } else if (kind == OUT_OPEN) {
+                int pos = top + open_incl - 2;
+                if (pos + 1 < W.stack_cap) {
+                    stack[pos] = PH_ENTRY(g.son0[b], img);
+                    stack[pos + 1] = PH_ENTRY(g.son1[b], img);
+                }
+            }
+            n_p2p += __popc(mp);
+            n_m2l += __popc(mm);
+            n_pd += push_tot;
+            top += open_tot;
+            if (top > W.stack_cap) {
+                flags |= PH_FLAG_STACK_OVERFLOW;
+                top = W.stack_cap;  // entries beyond were dropped; results are invalid
+            }
+            max_stack = max(max_stack, top);
+            __syncwarp();
+        }
+        int stage_hi = max(n_p2p, max(n_m2l, n_pd));
+        max_stage = max(max_stage, stage_hi);
+        if (stage_hi > W.stage_cap) flags |= PH_FLAG_STAGE_OVERFLOW;
+        // commit staged lists
+        long long off = 0;
+        if (leaf_a) {
+            if (lane == 0) off = (long long)atomicAdd((unsigned long long *)&W.ctr[WC_P2P_FILL], (unsigned long long)n_p2p);
+            off = __shfl_sync(0xffffffffu, off, 0);
+            bool ok = off + n_p2p <= W.p2p_cap && n_p2p <= W.stage_cap;
+            if (!ok) flags |= PH_FLAG_POOL_OVERFLOW;
+            else
+                for (int i = lane; i < n_p2p; i += 32) W.p2p_pool[off + i] = st_p2p[i];
+            if (lane == 0) { W.p2p_off[a] = ok ? off : 0; W.p2p_cnt[a] = ok ? n_p2p : 0; }
+        } else {
+            if (lane == 0) off = (long long)atomicAdd((unsigned long long *)&W.ctr[WC_PD_FILL0 + parity], (unsigned long long)n_pd);
+            off = __shfl_sync(0xffffffffu, off, 0);
+            bool ok = off + n_pd <= W.pd_cap && n_pd <= W.stage_cap;
+            if (!ok) flags |= PH_FLAG_POOL_OVERFLOW;
+            else
+                for (int i = lane; i < n_pd; i += 32) W.pd_pool[parity][off + i] = st_pd[i];
+            if (lane == 0) { W.pd_off[a] = ok ? off : 0; W.pd_cnt[a] = ok ? n_pd : 0; }
+        }
+        if (lane == 0) off = (long long)atomicAdd((unsigned long long *)&W.ctr[WC_M2L_FILL], (unsigned long long)n_m2l);
+        off = __shfl_sync(0xffffffffu, off, 0);
+        {
+            bool ok = off + n_m2l <= W.m2l_cap && n_m2l <= W.stage_cap;
+            if (!ok) flags |= PH_FLAG_POOL_OVERFLOW;
+            else
+                for (int i = lane; i < n_m2l; i += 32) W.m2l_pool[off + i] = st_m2l[i];
+            if (lane == 0) { W.m2l_off[a] = ok ? off : 0; W.m2l_cnt[a] = ok ? n_m2l : 0; }
+        }
+        __syncwarp();
+    }
+    // per-warp counters
+    c_p2p_loc = warp_sum_ll(c_p2p_loc);
+    c_p2p_img = warp_sum_ll(c_p2p_img);
+    c_m2l_loc = warp_sum_ll(c_m2l_loc);
+    c_m2l_img = warp_sum_ll(c_m2l_img);
+    c_pl = warp_sum_ll(c_pl);
+    c_pi = warp_sum_ll(c_pi);
+    if (lane == 0) {
+        if (c_p2p_loc) atomicAdd(&W.ctr[WC_P2P_LOCAL], c_p2p_loc);
+        if (c_p2p_img) atomicAdd(&W.ctr[WC_P2P_IMAGE], c_p2p_img);
+        if (c_m2l_loc) atomicAdd(&W.ctr[WC_M2L_LOCAL], c_m2l_loc);
+        if (c_m2l_img) atomicAdd(&W.ctr[WC_M2L_IMAGE], c_m2l_img);
+        if (c_pl) atomicAdd(&W.ctr[WC_PAIRS_LOCAL], c_pl);
+        if (c_pi) atomicAdd(&W.ctr[WC_PAIRS_IMAGE], c_pi);
+        if (flags) atomicOr(&W.ctr[WC_FLAGS], (unsigned long long)flags);
+        atomicMax(&W.ctr[WC_MAX_STACK], (unsigned long long)max_stack);
+        atomicMax(&W.ctr[WC_MAX_STAGE], (unsigned long long)max_stage);
+    }
+}
+
+__global__ void k_walk_level_done(WalkBufs W, int depth)
+{
+    // the pool written by this depth is read by the next; the next depth
+    // writes the other pool, whose fill starts from zero
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        unsigned long long f = W.ctr[WC_PD_FILL0 + (depth & 1)];
+        if (f > W.ctr[WC_PD_MAX]) W.ctr[WC_PD_MAX] = f;
+        W.ctr[WC_PD_FILL0 + ((depth + 1) & 1)] = 0;
+    }
+}
+
+}  // namespace
+
+int walk_lists(WalkBufs &w, const TreeBufs &t, const TreeInfo &info, const PassParams &p, unsigned image_mask,
+               cudaStream_t st, WalkStats &stats)
+{
+    PH_CUDA_CHECK(cudaMemsetAsync(w.ctr, 0, sizeof(unsigned long long) * WC_N, st));
+    WalkArgs A;
+    memset(&A, 0, sizeof A);
+    A.g.cx = t.cx; A.g.cy = t.cy; A.g.cz = t.cz;
+    A.g.wx = t.wx; A.g.wy = t.wy; A.g.wz = t.wz; A.g.wsum = t.wsum;
+    A.g.son0 = t.son0; A.g.son1 = t.son1; A.g.npart = t.npart; A.g.parent = t.parent;
+    A.w = w;
+    A.depth_list = t.depth_list;
+    A.nleaf = info.nleaf;
+    A.root = info.nleaf;  // node 0 in preorder
+    A.nroot = 0;
+    for (int img = 0; img < PH_NIMG; img++)
+        if (image_mask & (1u << img)) A.root_img[A.nroot++] = img;
+    A.boxsize = p.boxsize;
+    A.theta = p.theta;
+    A.theta2 = p.theta * p.theta;
+    A.rcut = p.rcut;
+    A.c2 = p.rcut * p.rcut;
+    int blocks = (w.nwarps * 32 + WALK_TB - 1) / WALK_TB;
+    for (int d = 0; d <= info.depth; d++) {
+        A.depth = d;
+        A.list_begin = info.depth_off[d];
+        A.list_end = info.depth_off[d + 1];
+        if (A.list_end > A.list_begin) {
+            int need = A.list_end - A.list_begin;
+            int nb = (need * 32 + WALK_TB - 1) / WALK_TB;
+            k_walk_level<<<nb < blocks ? nb : blocks, WALK_TB, 0, st>>>(A);
+        }
+        k_walk_level_done<<<1, 1, 0, st>>>(w, d);
+    }
+    PH_CUDA_CHECK(cudaGetLastError());
+    PH_CUDA_CHECK(cudaMemcpyAsync(stats.c, w.ctr, sizeof(stats.c), cudaMemcpyDeviceToHost, st));
+    PH_CUDA_CHECK(cudaStreamSynchronize(st));
+    return 0;
+}
+
+}  // namespace ph

@@ -1,0 +1,94 @@
+"""Generate the golden fixtures in tests/golden/ by running the reference's
+own FMM sources (compiled in place into oracle/_ref/libphotons_ref.so by
+oracle/Makefile, with the one-rank MPI stand-in) on small seeded inputs.
+
+    make -C oracle ref && python tests/golden/make_golden.py
+
+Each fixture holds the input positions and force parameters, and the
+reference's outputs: the tree-ordered positions (its in-place permutation),
+the accelerations after fmm_task and after fmm_ext, the counters, the tree
+and a digest of every interaction list (full lists for the small cases).
+"""
+from __future__ import annotations
+
+import hashlib
+import importlib.util
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import oracle  # noqa: E402
+
+spec = importlib.util.spec_from_file_location("ics", os.path.join(ROOT, "photons-2.0_gb300", "ics.py"))
+ics = importlib.util.module_from_spec(spec)
+spec.loader.exec_module(ics)
+
+
+def list_digest(t, s, im):
+    key = (t.astype(np.int64) << 34) | (s.astype(np.int64) << 5) | im.astype(np.int64)
+    key.sort()
+    return hashlib.sha256(key.tobytes()).hexdigest()
+
+
+def cases():
+    out = []
+    pos, p = ics.make("grid32", nside=16)
+    out.append(("grid16_leaf16", pos, p, True))
+    pos, p = ics.make("nfw128", nside=16)
+    p["maxleaf"] = 8
+    out.append(("nfw16_leaf8", pos, p, False))
+    pos, p = ics.make("grid32", nside=12)
+    p["maxleaf"] = 4
+    out.append(("grid12_leaf4", pos, p, False))
+    # Exact lattice: many coordinates equal a node's mean.  The cutoff is
+    # kept small against the box because the reference sizes its image
+    # export buffer as 1.1*NNODE entries (src/fmm.c:1004-1011) while the
+    # export holds nodes and leaves; a box mostly within rcut of its faces
+    # overflows that buffer in the reference itself.
+    n = 12
+    L = 12.0
+    g = (np.arange(n) + 0.5) * (L / n)
+    pos = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    p = ics.force_params(pos.shape[0], L, 24, theta=0.5, maxleaf=6)
+    out.append(("lattice12_leaf6", pos, p, True))
+    # one particle per leaf: pair splits at the midpoint
+    rng = np.random.default_rng(11)
+    pos = rng.random((300, 3)) * 20.0
+    p = ics.force_params(300, 20.0, 40, theta=0.5, maxleaf=1)
+    out.append(("random300_leaf1", pos, p, True))
+    return out
+
+
+def main():
+    ref = oracle.RefOracle()
+    for name, pos, p, full in cases():
+        r = ref.run(pos, p, capture=True, tree=True)
+        d = {
+            "pos_in": pos, "pos_tree": r["pos"], "acc_task": r["acc_task"], "acc": r["acc"],
+            "params": np.array([p["boxsize"], p["theta"], p["rs"], p["rcut"], p["eps"], p["mass"], p["maxleaf"]]),
+            "counters": np.array([r["counters"][k] for k in oracle.COUNTER_NAMES], np.int64),
+        }
+        for k, v in r["tree"].items():
+            if k.endswith("_M") or k.endswith("_L"):
+                if full:
+                    d["tree_" + k] = v
+            else:
+                d["tree_" + k] = v
+        for kind, (t, s, im) in r["lists"].items():
+            d["digest_" + kind] = np.array(list_digest(t, s, im))
+            d["ntarget_" + kind] = np.bincount(t - t.min(), minlength=1).astype(np.int32) if t.size else np.zeros(0, np.int32)
+            if full:
+                d["list_" + kind] = np.stack([t, s, im]).astype(np.int32)
+        path = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(path, **d)
+        c = r["counters"]
+        print("%-18s N=%6d p2p=%8d m2l=%6d p2p_ext=%7d m2l_ext=%5d  %6.1f KB" % (
+            name, pos.shape[0], c["idxP2P"], c["idxM2L"], c["n_p2p_ext"], c["n_m2l_ext"], os.path.getsize(path) / 1024))
+
+
+if __name__ == "__main__":
+    main()

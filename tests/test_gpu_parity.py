@@ -1,0 +1,127 @@
+"""GPU force pass against the reference: golden fixtures (reference
+outputs) and the CPU oracle on the same seeded inputs, through the C ABI.
+
+Tolerances: the FP64 GPU variant must match per-particle accelerations to
+1e-10 relative (the reference's FP64 arithmetic in a different summation
+order); interaction-list counts and lists must match exactly.  The FP32
+split variant is checked against the FP64 GPU variant on the same lists:
+median relative error <= 2e-6 and 99th percentile <= 2e-5 here (the north
+star's budget is a median of 1e-4)."""
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+
+pytestmark = pytest.mark.gpu
+
+COUNTERS = ["idxP2P", "idxM2L", "walk_m2l_count", "p2p_count_remote", "NLEAF", "NNODE", "nleaf", "nnode",
+            "first_leaf", "first_node", "direct_local_start", "n_p2p", "n_m2l", "n_p2p_ext", "n_m2l_ext",
+            "n_images"]
+FP64_TOL = 1e-10
+
+
+def digest(t, s, im):
+    key = (t.astype(np.int64) << 34) | (s.astype(np.int64) << 5) | im.astype(np.int64)
+    key.sort()
+    return hashlib.sha256(key.tobytes()).hexdigest()
+
+
+def rel_err(a, b):
+    return np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-300)
+
+
+@pytest.fixture(scope="module")
+def fp(ph):
+    f = ph.ForcePass(0)
+    yield f
+    f.close()
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_fp64_matches_reference_golden(ph, fp, name):
+    g = load_golden(name)
+    acc = fp.run(g["pos_in"], g["p"], precision=ph.FP64, flags=ph.F_TREE_ORDER | ph.F_KEEP_LISTS | ph.F_MULTIPOLES)
+    c = fp.counters()
+    assert [c[k] for k in COUNTERS] == list(g["counters"])
+    # the reference's permutation of part[]
+    assert np.array_equal(fp.positions(), g["pos_tree"])
+    # every interaction list, as a multiset
+    for kind, (t, s, im) in fp.lists().items():
+        assert digest(t, s, im) == str(g["digest_" + kind]), kind
+    # tree: integer structure exact, geometry to the last bits of the mean
+    tr = fp.tree()
+    for k in ("leaf_ipart", "leaf_npart", "node_npart", "node_son"):
+        assert np.array_equal(tr[k], g["tree_" + k]), k
+    for k in ("leaf_center", "leaf_width", "node_center", "node_width", "node_split"):
+        assert np.allclose(tr[k], g["tree_" + k], rtol=1e-13, atol=1e-13 * g["p"]["boxsize"]), k
+    if "tree_node_M" in g:
+        for k in ("leaf_M", "node_M"):
+            ref = g["tree_" + k]
+            assert np.abs(tr[k] - ref).max() <= 1e-11 * (np.abs(ref).max() + 1e-300), k
+    assert rel_err(acc, g["acc"]).max() <= FP64_TOL
+    # local task phase alone (src/fmm.c:909-984): local P2P, no far field
+    acc_task = fp.run(g["pos_in"], g["p"], precision=ph.FP64, image_mask=1,
+                      flags=ph.F_TREE_ORDER | ph.F_NO_FARFIELD)
+    assert rel_err(acc_task, g["acc_task"]).max() <= FP64_TOL
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_fp32_split_precision_golden(ph, fp, name):
+    g = load_golden(name)
+    a64 = fp.run(g["pos_in"], g["p"], precision=ph.FP64)
+    a32 = fp.run(g["pos_in"], g["p"], precision=ph.FP32_SPLIT)
+    e = rel_err(a32, a64)
+    assert np.median(e) <= 2e-6, np.median(e)
+    assert np.percentile(e, 99) <= 2e-5, np.percentile(e, 99)
+
+
+@pytest.mark.parametrize("workload,nside,maxleaf", [("grid32", 32, 16), ("nfw128", 32, 8), ("grid32", 24, 32),
+                                                    ("nfw128", 28, 64)])
+def test_fp64_matches_oracle(ph, fp, ics, port, workload, nside, maxleaf):
+    pos, p = ics.make(workload, nside=nside, maxleaf=maxleaf)
+    r = port.run(pos, p, capture=False, tree=False, nthreads=8)
+    acc = fp.run(pos, p, precision=ph.FP64)
+    c = fp.counters()
+    for k in COUNTERS[:10] + ["n_p2p_ext", "n_m2l_ext"]:
+        assert c[k] == r["counters"][k], k
+    acc_ref = np.empty_like(r["acc"])
+    acc_ref[r["perm"]] = r["acc"]
+    assert rel_err(acc, acc_ref).max() <= FP64_TOL
+
+
+def test_pass_is_deterministic(ph, fp, ics):
+    pos, p = ics.make("nfw128", nside=24, maxleaf=8)
+    for prec in (ph.FP32_SPLIT, ph.FP64):
+        a = fp.run(pos, p, precision=prec)
+        b = fp.run(pos, p, precision=prec)
+        assert np.array_equal(a, b)
+
+
+def test_device_io_matches_host_io(ph, fp, ics):
+    torch = pytest.importorskip("torch")
+    pos, p = ics.make("grid32", nside=16)
+    host = fp.run(pos, p, precision=ph.FP32_SPLIT)
+    dpos = torch.from_numpy(pos).cuda()
+    dacc = torch.empty_like(dpos)
+    torch.cuda.synchronize()
+    fp.run_device(dpos.data_ptr(), dacc.data_ptr(), pos.shape[0], p, precision=ph.FP32_SPLIT)
+    assert np.array_equal(dacc.cpu().numpy(), host)
+
+
+def test_capacity_overflow_is_an_error(ph, fp):
+    pos = np.full((100, 3), 3.0)
+    p = dict(boxsize=10.0, theta=0.5, rs=1.0, rcut=4.5, eps=0.01, mass=1.0, maxleaf=8)
+    with pytest.raises(ph.PhotonsError, match="error 4"):
+        fp.run(pos, p, precision=ph.FP64)
+    # the context stays usable
+    pos2 = np.random.default_rng(0).random((500, 3)) * 10.0
+    fp.run(pos2, p, precision=ph.FP64)
+
+
+def test_too_few_particles_is_an_error(ph, fp):
+    pos = np.random.default_rng(1).random((8, 3))
+    p = dict(boxsize=1.0, theta=0.5, rs=0.1, rcut=0.45, eps=0.01, mass=1.0, maxleaf=8)
+    with pytest.raises(ph.PhotonsError, match="error 5"):
+        fp.run(pos, p)

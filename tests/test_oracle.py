@@ -1,0 +1,145 @@
+"""The CPU oracle (oracle/photons_oracle.c) against the reference: the
+committed golden fixtures (made by the reference's own sources), and the
+reference library itself where its tree is present."""
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+
+COUNTERS = ["idxP2P", "idxM2L", "walk_m2l_count", "p2p_count_remote", "NLEAF", "NNODE", "nleaf", "nnode",
+            "first_leaf", "first_node", "direct_local_start", "n_p2p", "n_m2l", "n_p2p_ext", "n_m2l_ext",
+            "n_images"]
+
+
+def digest(t, s, im):
+    key = (t.astype(np.int64) << 34) | (s.astype(np.int64) << 5) | im.astype(np.int64)
+    key.sort()
+    return hashlib.sha256(key.tobytes()).hexdigest()
+
+
+def rel_err(a, b):
+    return np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-300)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_port_matches_golden(port, name):
+    g = load_golden(name)
+    r = port.run(g["pos_in"], g["p"], capture=True, tree=True, nthreads=4)
+    assert [r["counters"][k] for k in COUNTERS] == list(g["counters"])
+    # the same in-place permutation of the particles
+    assert np.array_equal(r["pos"], g["pos_tree"])
+    assert np.array_equal(g["pos_in"][r["perm"]], r["pos"])
+    for kind, (t, s, im) in r["lists"].items():
+        assert digest(t, s, im) == str(g["digest_" + kind]), kind
+        if "list_" + kind in g:
+            # full lists, in the reference's order
+            assert np.array_equal(np.stack([t, s, im]), g["list_" + kind]), kind
+    # without M2L the sums run in the reference's order: identical bits
+    assert np.array_equal(r["acc_task"], g["acc_task"])
+    if g["counters"][2] == 0:
+        assert np.array_equal(r["acc"], g["acc"])
+    else:
+        assert rel_err(r["acc"], g["acc"]).max() < 1e-12
+    for k in ("leaf_ipart", "leaf_npart", "node_npart", "node_son", "leaf_center", "leaf_width", "node_center",
+              "node_width", "node_split"):
+        assert np.array_equal(r["tree"][k], g["tree_" + k]), k
+    for k in ("leaf_M", "node_M", "leaf_L", "node_L"):
+        if "tree_" + k in g:
+            ref = g["tree_" + k]
+            scale = np.abs(ref).max() + 1e-300
+            assert np.abs(r["tree"][k] - ref).max() <= 1e-12 * scale, k
+
+
+def test_port_threads_bit_identical(port, ics):
+    pos, p = ics.make("grid32", nside=16)
+    a = port.run(pos, p, capture=False, tree=False, nthreads=1)["acc"]
+    b = port.run(pos, p, capture=False, tree=False, nthreads=7)["acc"]
+    assert np.array_equal(a, b)
+
+
+def test_operators_match_reference(oracle_mod, port):
+    if not oracle_mod.ref_available():
+        pytest.skip("reference oracle not built here")
+    ref = oracle_mod.RefOracle()
+    rng = np.random.default_rng(5)
+    for _ in range(50):
+        d = rng.normal(size=3) * 5
+        M = rng.normal(size=20)
+        rs = rng.uniform(0.5, 4.0)
+        a, b = ref.m2l(d, M, rs), port.m2l(d, M, rs)
+        assert np.abs(a - b).max() <= 1e-13 * np.abs(a).max()
+        a, b = ref.m2m(d, M), port.m2m(d, M)
+        assert np.abs(a - b).max() <= 1e-13 * np.abs(a).max()
+        a, b = ref.l2l(d, M), port.l2l(d, M)
+        assert np.abs(a - b).max() <= 1e-13 * np.abs(a).max()
+
+
+def test_acceptance_matches_reference(oracle_mod, port):
+    if not oracle_mod.ref_available():
+        pytest.skip("reference oracle not built here")
+    ref = oracle_mod.RefOracle()
+    rng = np.random.default_rng(9)
+    cases = []
+    for _ in range(3000):
+        wi = rng.uniform(0.1, 4.0, 3)
+        wj = rng.uniform(0.1, 4.0, 3)
+        dist = rng.normal(size=3) * 8
+        cases.append((wi, wj, dist))
+    # touching boxes, exactly adjacent faces
+    for _ in range(200):
+        wi = rng.uniform(0.5, 2.0, 3)
+        wj = rng.uniform(0.5, 2.0, 3)
+        dist = (wi + wj) * 0.5 * rng.choice([-1.0, 0.0, 1.0], 3)
+        cases.append((wi, wj, dist))
+    for theta in (0.3, 0.5, 0.8):
+        for wi, wj, dist in cases:
+            assert ref.acceptance(wi, wj, dist, theta, 10.0) == port.acceptance(wi, wj, dist, theta, 10.0)
+
+
+def test_port_matches_reference_full_c0(oracle_mod, port, ics):
+    """The 32^3 workload against the reference library run here."""
+    if not oracle_mod.ref_available():
+        pytest.skip("reference oracle not built here")
+    pos, p = ics.make("grid32")
+    r = oracle_mod.RefOracle().run(pos, p, capture=False, tree=False)
+    q = port.run(pos, p, capture=False, tree=False, nthreads=8)
+    assert {k: r["counters"][k] for k in COUNTERS[:10]} == {k: q["counters"][k] for k in COUNTERS[:10]}
+    assert np.array_equal(r["acc"], q["acc"])
+
+
+def test_capacity_overflow_is_an_error(port):
+    """Coincident particles defeat the mean split; the reference would write
+    past its 2N/MAXLEAF leaf array (src/fmm.c:203-209)."""
+    pos = np.full((100, 3), 3.0)
+    p = dict(boxsize=10.0, theta=0.5, rs=1.0, rcut=4.5, eps=0.01, mass=1.0, maxleaf=8)
+    with pytest.raises(RuntimeError, match="code [34]"):
+        port.run(pos, p, capture=False, tree=False)
+
+
+def test_too_few_particles_is_an_error(port):
+    pos = np.random.default_rng(1).random((8, 3))
+    p = dict(boxsize=1.0, theta=0.5, rs=0.1, rcut=0.45, eps=0.01, mass=1.0, maxleaf=8)
+    with pytest.raises(RuntimeError, match="code 5"):
+        port.run(pos, p, capture=False, tree=False)
+
+
+def test_direct_sum_small(port):
+    rng = np.random.default_rng(3)
+    L = 10.0
+    pos = rng.random((300, 3)) * L
+    p = dict(boxsize=L, theta=0.5, rs=0.5, rcut=2.25, eps=0.05, mass=2.0, maxleaf=8)
+    targets = np.arange(0, 300, 7, dtype=np.int32)
+    got = port.direct_sum(pos, p, targets, rmax=4.0)
+    from scipy.special import erfc
+    for k, i in enumerate(targets):
+        d = pos - pos[i]
+        d -= L * np.round(d / L)
+        r = np.linalg.norm(d, axis=1)
+        m = (r < 4.0) & (np.arange(300) != i)
+        rr = r[m]
+        u = 0.5 * rr / p["rs"]
+        f = p["mass"] * (erfc(u) + 2 / np.sqrt(np.pi) * u * np.exp(-u * u)) / np.maximum(rr, p["eps"]) ** 3
+        want = (d[m] * f[:, None]).sum(0)
+        assert np.allclose(got[k], want, rtol=1e-12, atol=1e-15)
