@@ -249,6 +249,7 @@ int ph_stage_build(photons_ctx *c, const photons_params *p, int n, const double 
     if (cap < 1) cap = 1;
     PH_TRY(alloc_particles(c, n));
     PH_TRY(alloc_tree(c, n, cap));
+    c->b.rule_cap = cap;
     c->pp.boxsize = p->boxsize;
     c->pp.theta = p->theta;
     c->pp.rs = p->rs;

@@ -36,6 +36,7 @@ struct BuildBufs {
     int *scan_scratch = nullptr;
     size_t scan_scratch_elems = 0;
     int cap_nodes = 0, cap_leaves = 0, cap_chunks = 0, cap_n = 0;
+    int rule_cap = 0;  // this pass's 2N/MAXLEAF capacity (src/fmm.c:203-209), <= cap_nodes
     int *level_begin_h = nullptr;  // host copy, per level
 };
 

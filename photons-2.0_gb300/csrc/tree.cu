@@ -205,7 +205,7 @@ __global__ void k_make_children(BuildBufs b, int lb, int C, int maxleaf, int D)
             if (c == 0) chi[D] = split;
             else clo[D] = split;
             if (sizes[c] <= maxleaf) {
-                if (lid >= b.cap_leaves) {
+                if (lid >= b.rule_cap) {
                     atomicOr(&b.cnt[BC_FLAGS], PH_FLAG_LEAF_CAPACITY);
                     code[c] = ~0;
                 } else {
@@ -221,7 +221,7 @@ __global__ void k_make_children(BuildBufs b, int lb, int C, int maxleaf, int D)
                 }
                 lid++;
             } else {
-                if (nid >= b.cap_nodes) {
+                if (nid >= b.rule_cap) {
                     atomicOr(&b.cnt[BC_FLAGS], PH_FLAG_NODE_CAPACITY);
                     code[c] = 0;
                 } else {
@@ -450,9 +450,9 @@ int build_tree(BuildBufs &b, TreeBufs &T, const PassParams &p, int n, cudaStream
         PH_CUDA_CHECK(cudaMemcpyAsync(h, b.cnt, sizeof(h), cudaMemcpyDeviceToHost, st));
         PH_CUDA_CHECK(cudaStreamSynchronize(st));
         if (h[BC_FLAGS] & PH_FLAG_LEAF_CAPACITY)
-            return ph_set_error(4, "leaf capacity 2N/MAXLEAF=%d exceeded by the mean-split tree", b.cap_leaves);
+            return ph_set_error(4, "leaf capacity 2N/MAXLEAF=%d exceeded by the mean-split tree", b.rule_cap);
         if (h[BC_FLAGS] & PH_FLAG_NODE_CAPACITY)
-            return ph_set_error(4, "node capacity 2N/MAXLEAF=%d exceeded by the mean-split tree", b.cap_nodes);
+            return ph_set_error(4, "node capacity 2N/MAXLEAF=%d exceeded by the mean-split tree", b.rule_cap);
         int C = h[BC_LEVEL_COUNT];
         if (d > 0) {
             leaf_begin.push_back(leaves_total);
