@@ -1,0 +1,334 @@
+"""Benchmark: photoNs-2.0 FMM short-range force pass on GB300.
+
+Workload (the headline configuration): 256^3 = 16,777,216 particles in a
+periodic box L = 500 Mpc/h, grid + Zel'dovich displacement of a Gaussian
+field with P(k) ~ k^-2 (rms displacement 0.5 spacing, seed 3), mesh 256,
+rs = 1.25 cells, rcut = 4.5 rs, theta = 0.5, softening 0.03 spacing.
+Synthetic, seeded; forces exclude G as in the reference.
+
+One step = one full short-range force pass (tree build, dual-tree walk with
+26 periodic images, P2P, far field when any M2L occurs, gather) over the
+resident particles, FP32 split precision.  value = particle-forces/s =
+N / (time per pass).  Inputs (400 MB of FP64 positions) exceed the 126 MB
+L2, so no flush is needed between steps.
+
+    python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
+Under torchrun each rank runs an independent box (seed 3 + rank): replicas,
+weak scaling, no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-forces/s at 256^3 clustered: FP32-split vs FP64 GPU at rel err <=1e-4"
+UNIT = "particle-forces/s"
+FLOPS_PER_PAIR = 36  # fixed work unit per pair interaction
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nside", type=int, default=256)
+    ap.add_argument("--maxleaf", type=int, default=32)
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 GPU comparison pass")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(nside, maxleaf, seed_offset=0):
+    import __graft_entry__ as g
+
+    g.load_package()
+    from photons_gb300 import ics
+
+    L = 500.0 * nside / 256
+    pos = ics.zeldovich(nside, L, -2.0, seed=3 + seed_offset)
+    p = ics.force_params(pos.shape[0], L, nside, theta=0.5, maxleaf=maxleaf)
+    return pos, p
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower().startswith("active")})
+        return {"sm_mhz": float(np.median([r[0] for r in rows])), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline(nthreads=None, target_s=10.0):
+    """The oracle's CPU restatement of the pass, all host threads, on a bounded
+    sample of the same workload (same density and clustering, smaller box)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    oracle.build_port()
+    port = oracle.PortOracle(build=False)
+    nthreads = nthreads or os.cpu_count() or 1
+    nside = 48
+    while True:
+        pos, p = workload(nside, 16)
+        r = port.run(pos, p, capture=False, tree=False, nthreads=nthreads)
+        secs = r["seconds"]
+        if secs * 2.5 > target_s or nside >= 96:
+            break
+        nside = min(96, int(nside * (target_s / max(secs, 1e-3)) ** (1 / 3.0) * 0.9) // 8 * 8 or nside + 16)
+    return {"value": pos.shape[0] / secs, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": "one full pass of the same workload at %d^3 (L=%.1f, leaf 16, reference rules) "
+                      "on the host: %.2f s" % (nside, p["boxsize"], secs)}
+
+
+def run_reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    oracle.build_port()
+    port = oracle.PortOracle(build=False)
+    nthreads = os.cpu_count() or 1
+    nside = 64
+    pos, p = workload(nside, 16)
+    for _ in range(max(0, args.warmup)):
+        port.run(pos, p, capture=False, tree=False, nthreads=nthreads)
+    t = []
+    for _ in range(max(1, args.steps)):
+        r = port.run(pos, p, capture=False, tree=False, nthreads=nthreads)
+        t.append(r["seconds"])
+    secs = float(np.mean(t))
+    v = pos.shape[0] / secs
+    line = {"metric": METRIC, "impl": "reference", "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": secs * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "zeldovich256 sample at %d^3 (same density/clustering), leaf 16" % nside,
+                       "n": int(pos.shape[0]), "boxsize": p["boxsize"], "theta": 0.5},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
+                             "sample": "each step one full pass at %d^3 on %d host threads (the reference's "
+                                       "algorithm restated in C; the reference sources are not on this host)"
+                                       % (nside, nthreads)},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def rel_err(a, b):
+    return np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-300)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference_arm(args)
+        return
+    rank, world, local = dist_env()
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import __graft_entry__ as g
+
+    ph = g.load_package()
+    pos, p = workload(args.nside, args.maxleaf, seed_offset=rank)
+    n = pos.shape[0]
+    fp = ph.ForcePass(local)
+    stream = torch.cuda.current_stream()
+    fp.set_stream(stream.cuda_stream)
+    dpos = torch.from_numpy(pos).to("cuda")
+    dacc = torch.empty_like(dpos)
+    torch.cuda.synchronize()
+
+    def step():
+        fp.run_device(dpos.data_ptr(), dacc.data_ptr(), n, p, precision=ph.FP32_SPLIT)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local) if rank == 0 else None
+    if sampler:
+        sampler.start()
+    launches0 = ph.load_library().photons_launch_count()
+    p2p_ms, phase = [], []
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+        t = fp.timings()
+        p2p_ms.append(t["p2p"])
+        phase.append(t)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    launches = ph.load_library().photons_launch_count() - launches0
+    clocks = sampler.stop() if sampler else None
+    ms = e0.elapsed_time(e1) / args.steps
+    if dist:
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    counters = fp.counters()
+    pairs = counters["pairs_local"] + counters["pairs_image"]
+    value = n * world / (ms * 1e-3)
+
+    # end to end through the C ABI: pinned host buffers in, host buffers out
+    hpos = torch.from_numpy(pos).pin_memory()
+    hacc = torch.empty_like(hpos).pin_memory()
+    hp, ha = hpos.numpy(), hacc.numpy()
+    fp.run(hp, p, precision=ph.FP32_SPLIT, out=ha)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    t0 = time.time()
+    esteps = max(1, min(args.steps, 5))
+    for _ in range(esteps):
+        fp.run(hp, p, precision=ph.FP32_SPLIT, out=ha)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = max(e0.elapsed_time(e1), (time.time() - t0) * 1e3) / esteps
+    acc32 = ha.copy()
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    # roofline of the dominant kernel (P2P, FP32 pipe)
+    peak = ph.fp32_fma_peak(8192)
+    t_p2p = float(np.mean(p2p_ms))
+    achieved = FLOPS_PER_PAIR * pairs / (t_p2p * 1e-3) / 1e12
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "p2p_traffic.json")
+    if os.path.exists(tp):
+        try:
+            tj = json.load(open(tp))
+            traffic = tj.get("bytes_per_launch_scaled")
+        except Exception:
+            traffic = None
+
+    extra = {}
+    if not args.no_fp64:
+        fp.run_device(dpos.data_ptr(), dacc.data_ptr(), n, p, precision=ph.FP64)
+        torch.cuda.synchronize()
+        t64 = fp.timings()
+        acc64 = np.empty_like(pos)
+        e0.record(stream)
+        fp.run(pos, p, precision=ph.FP64, out=acc64)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = e0.elapsed_time(e1)
+        e = rel_err(acc32, acc64)
+        rng = np.random.default_rng(7)
+        tgt = rng.choice(n, 10000, replace=False).astype(np.int32)
+        ds = ph.direct_sum(pos, p, tgt)
+        a32 = rel_err(acc32[tgt], ds)
+        a64 = rel_err(acc64[tgt], ds)
+        extra["fp64_gpu"] = {"value": n / (ms64 * 1e-3), "ms_per_pass": ms64, "p2p_ms": t64["p2p"],
+                             "speedup_fp32_over_fp64": ms64 / ms}
+        extra["errors"] = {
+            "precision_fp32_vs_fp64gpu": {"median": float(np.median(e)), "p99": float(np.percentile(e, 99)),
+                                          "max": float(e.max())},
+            "algorithmic_vs_direct_sum_10k": {
+                "fp32_median": float(np.median(a32)), "fp32_p99": float(np.percentile(a32, 99)),
+                "fp64_median": float(np.median(a64)), "fp64_p99": float(np.percentile(a64, 99)),
+                "direct_sum": "FP64 GPU, untruncated erfc kernel, all sources within 2 rcut, minimum image"}}
+    cpu = None if args.no_cpu else cpu_baseline()
+
+    tmean = {k: float(np.mean([t[k] for t in phase])) for k in phase[0]}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "zeldovich256", "n": n, "boxsize": p["boxsize"], "mesh": args.nside,
+                   "maxleaf": p["maxleaf"], "theta": p["theta"], "rs": p["rs"], "rcut": p["rcut"],
+                   "eps": p["eps"], "precision": "fp32-split (fp64 positions and centre differences)",
+                   "l2": "inputs larger than L2 (positions %.0f MB), no flush" % (n * 24 / 1e6),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": {"bound": "fp32", "kernel": "k_p2p_split", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": "FFMA probe measured in this run (MEASURED_PEAKS.json holds no FP32 figure)",
+                     "work": "%d flops/pair x %d pairs per launch" % (FLOPS_PER_PAIR, pairs),
+                     "p2p_ms": t_p2p},
+        "cpu_baseline": cpu,
+        "e2e": {"value": n / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": n * 24,
+                "d2h_bytes_per_step": n * 24, "ms_per_step": e2e_ms},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "phases_ms": tmean,
+        "counters": {k: counters[k] for k in ("idxP2P", "idxM2L", "walk_m2l_count", "p2p_count_remote", "nleaf",
+                                              "nnode", "pairs_local", "pairs_image", "depth")},
+        "pairs_per_particle": pairs / n,
+    }
+    line.update(extra)
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

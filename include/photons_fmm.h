@@ -137,6 +137,9 @@ int photons_op_batch(int op, int n, const double *d, const double *in, double *i
 int photons_direct_sum(const photons_params *p, int n, const double *pos, int nt, const int *targets,
                        double rmax, double *acc);
 
+/* kernels launched by this library so far (all contexts) */
+unsigned long long photons_launch_count(void);
+
 /* FP32 FMA throughput probe: returns TFLOP/s measured over ~iters FMAs per thread */
 double photons_fp32_fma_peak(int iters);
 

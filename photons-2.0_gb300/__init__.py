@@ -89,6 +89,8 @@ def load_library():
     lib.photons_list_copy.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _ip]
     lib.photons_op_batch.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, C.c_double]
     lib.photons_direct_sum.argtypes = [C.POINTER(Params), C.c_int, _dp, C.c_int, _ip, C.c_double, _dp]
+    lib.photons_launch_count.restype = C.c_ulonglong
+    lib.photons_launch_count.argtypes = []
     lib.photons_fp32_fma_peak.restype = C.c_double
     lib.photons_fp32_fma_peak.argtypes = [C.c_int]
     lib.photons_gpu_error.restype = C.c_char_p

@@ -38,6 +38,7 @@ int ph_set_cuda_error(cudaError_t e, const char *what, const char *file, int lin
 }
 
 extern "C" int photons_gpu_status(void) { return g_status; }
+extern "C" unsigned long long photons_launch_count(void) { return ph::g_launches; }
 extern "C" const char *photons_gpu_error(void) { return g_msg; }
 extern "C" void photons_gpu_clear_error(void)
 {
@@ -46,6 +47,8 @@ extern "C" void photons_gpu_clear_error(void)
 }
 
 namespace ph {
+unsigned long long g_launches = 0;
+
 int device_sm_count()
 {
     static int v = 0;
@@ -395,7 +398,7 @@ int ph_stage_output(photons_ctx *c, double *acc, int device_io, int tree_order)
     const int n = c->n;
     double *dst = device_io ? acc : c->io;
     int blocks = ph::device_sm_count() * 8;
-    k_gather_out<<<blocks, 256, 0, st>>>(c->b.perm, c->ax, c->ay, c->az, n, dst, tree_order);
+    ph::note_launch(), k_gather_out<<<blocks, 256, 0, st>>>(c->b.perm, c->ax, c->ay, c->az, n, dst, tree_order);
     PH_CUDA_CHECK(cudaGetLastError());
     PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_GATHERED], st));
     if (!device_io)

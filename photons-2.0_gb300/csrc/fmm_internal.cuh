@@ -96,6 +96,10 @@ namespace ph {
 
 int device_sm_count();
 
+// number of kernels this library has launched (reported by photons_launch_count)
+extern unsigned long long g_launches;
+inline void note_launch() { g_launches++; }
+
 // exclusive scan of n int32 values (n read on the device from n_ptr, at most
 // cap elements); writes total to *total (device) if total != nullptr.
 void scan_exclusive_i32(const int *in, int *out, const int *n_ptr, int cap, int *total, int *scratch,

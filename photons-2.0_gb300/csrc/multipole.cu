@@ -272,7 +272,7 @@ inline int grid_for(long long n, int tpb)
 
 int run_m2l(const MultipoleArgs &a, cudaStream_t st)
 {
-    k_m2l<<<grid_for(a.nunified, MP_TB), MP_TB, 0, st>>>(a.nunified, a.m2l_pool, a.m2l_off, a.m2l_cnt, a.cx, a.cy,
+    ph::note_launch(), k_m2l<<<grid_for(a.nunified, MP_TB), MP_TB, 0, st>>>(a.nunified, a.m2l_pool, a.m2l_off, a.m2l_cnt, a.cx, a.cy,
                                                          a.cz, a.M, a.L, a.rs, a.boxsize);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
@@ -283,10 +283,10 @@ int run_downward(const MultipoleArgs &a, cudaStream_t st)
     for (int d = 1; d < a.ndepth; d++) {
         int b = a.depth_off[d], e = a.depth_off[d + 1];
         if (e > b)
-            k_l2l_depth<<<grid_for(e - b, MP_TB), MP_TB, 0, st>>>(a.depth_list, b, e, a.parent, a.cx, a.cy, a.cz,
+            ph::note_launch(), k_l2l_depth<<<grid_for(e - b, MP_TB), MP_TB, 0, st>>>(a.depth_list, b, e, a.parent, a.cx, a.cy, a.cz,
                                                                   a.L);
     }
-    k_l2p<<<grid_for((long long)a.nleaf * 32, 256), 256, 0, st>>>(a.px, a.py, a.pz, a.ipart, a.npart, a.cx, a.cy,
+    ph::note_launch(), k_l2p<<<grid_for((long long)a.nleaf * 32, 256), 256, 0, st>>>(a.px, a.py, a.pz, a.ipart, a.npart, a.cx, a.cy,
                                                                   a.cz, a.nleaf, a.L, a.ax, a.ay, a.az);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
@@ -294,12 +294,12 @@ int run_downward(const MultipoleArgs &a, cudaStream_t st)
 
 int run_p2m_m2m(const MultipoleArgs &a, cudaStream_t st)
 {
-    k_p2m<<<grid_for(a.nleaf, MP_TB), MP_TB, 0, st>>>(a.px, a.py, a.pz, a.ipart, a.npart, a.cx, a.cy, a.cz, a.nleaf,
+    ph::note_launch(), k_p2m<<<grid_for(a.nleaf, MP_TB), MP_TB, 0, st>>>(a.px, a.py, a.pz, a.ipart, a.npart, a.cx, a.cy, a.cz, a.nleaf,
                                                        a.mass, a.M);
     for (int d = a.ndepth - 1; d >= 0; d--) {
         int b = a.depth_off[d], e = a.depth_off[d + 1];
         if (e > b)
-            k_m2m_depth<<<grid_for(e - b, MP_TB), MP_TB, 0, st>>>(a.depth_list, b, e, a.nleaf, a.son0, a.son1, a.cx,
+            ph::note_launch(), k_m2m_depth<<<grid_for(e - b, MP_TB), MP_TB, 0, st>>>(a.depth_list, b, e, a.nleaf, a.son0, a.son1, a.cx,
                                                                   a.cy, a.cz, a.M);
     }
     PH_CUDA_CHECK(cudaGetLastError());
@@ -353,9 +353,9 @@ int launch_op_batch(int op, int n, const double *d, const double *in, double *in
 {
     if (n <= 0) return 0;
     int g = grid_for(n, MP_TB);
-    if (op == 0) k_op_m2l<<<g, MP_TB, 0, st>>>(n, d, in, inout, rs);
-    else if (op == 1) k_op_m2m<<<g, MP_TB, 0, st>>>(n, d, in, inout);
-    else k_op_l2l<<<g, MP_TB, 0, st>>>(n, d, in, inout);
+    if (op == 0) ph::note_launch(), k_op_m2l<<<g, MP_TB, 0, st>>>(n, d, in, inout, rs);
+    else if (op == 1) ph::note_launch(), k_op_m2m<<<g, MP_TB, 0, st>>>(n, d, in, inout);
+    else ph::note_launch(), k_op_l2l<<<g, MP_TB, 0, st>>>(n, d, in, inout);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }

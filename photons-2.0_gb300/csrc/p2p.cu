@@ -334,7 +334,7 @@ SplitConsts make_split_consts(const PassParams &p)
 int launch_leaf_offsets(const BuildBufs &b, const TreeBufs &t, int nleaf, float4 *pos4, cudaStream_t st)
 {
     int blocks = device_sm_count() * 8;
-    k_leaf_offsets<<<blocks, 256, 0, st>>>(b.x, b.y, b.z, t.ipart, t.npart, t.cx, t.cy, t.cz, nleaf, pos4);
+    ph::note_launch(), k_leaf_offsets<<<blocks, 256, 0, st>>>(b.x, b.y, b.z, t.ipart, t.npart, t.cx, t.cy, t.cz, nleaf, pos4);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }
@@ -343,8 +343,8 @@ int launch_p2p(const P2PArgs &a, int fp64, cudaStream_t st)
 {
     PH_CUDA_CHECK(cudaMemsetAsync(a.work_counter, 0, sizeof(int), st));
     int blocks = device_sm_count() * (fp64 ? 4 : 4);
-    if (fp64) k_p2p_fp64<<<blocks, P2P_TB, 0, st>>>(a);
-    else k_p2p_split<<<blocks, P2P_TB, 0, st>>>(a);
+    if (fp64) ph::note_launch(), k_p2p_fp64<<<blocks, P2P_TB, 0, st>>>(a);
+    else ph::note_launch(), k_p2p_split<<<blocks, P2P_TB, 0, st>>>(a);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }

@@ -107,9 +107,9 @@ void scan_exclusive_i32(const int *in, int *out, const int *n_ptr, int cap, int 
     (void)scratch_elems;
     int ntiles_cap = (cap + SCAN_TILE - 1) / SCAN_TILE;
     int grid = ntiles_cap < 4 * device_sm_count() ? (ntiles_cap > 0 ? ntiles_cap : 1) : 4 * device_sm_count();
-    k_tile_sums<<<grid, SCAN_THREADS, 0, st>>>(in, n_ptr, scratch);
-    k_scan_tile_sums<<<1, SCAN_THREADS, 0, st>>>(scratch, n_ptr, total);
-    k_tile_scan<<<grid, SCAN_THREADS, 0, st>>>(in, out, n_ptr, scratch);
+    ph::note_launch(), k_tile_sums<<<grid, SCAN_THREADS, 0, st>>>(in, n_ptr, scratch);
+    ph::note_launch(), k_scan_tile_sums<<<1, SCAN_THREADS, 0, st>>>(scratch, n_ptr, total);
+    ph::note_launch(), k_tile_scan<<<grid, SCAN_THREADS, 0, st>>>(in, out, n_ptr, scratch);
 }
 
 }  // namespace ph

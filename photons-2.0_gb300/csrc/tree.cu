@@ -426,7 +426,7 @@ inline int grid_for(int n, int tpb, int maxblocks)
 
 int launch_init_particles(BuildBufs &b, const double *pos, int n, cudaStream_t st)
 {
-    k_init_particles<<<device_sm_count() * 8, TB, 0, st>>>(pos, n, b);
+    ph::note_launch(), k_init_particles<<<device_sm_count() * 8, TB, 0, st>>>(pos, n, b);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }
@@ -439,7 +439,7 @@ int build_tree(BuildBufs &b, TreeBufs &T, const PassParams &p, int n, cudaStream
     const int maxb = sms * 8;
     const int L = 0;
     (void)L;
-    k_init_root<<<1, 1, 0, st>>>(b, n, p.boxsize);
+    ph::note_launch(), k_init_root<<<1, 1, 0, st>>>(b, n, p.boxsize);
     PH_CUDA_CHECK(cudaGetLastError());
 
     std::vector<int> lvl_begin, lvl_count, leaf_begin, leaf_count;
@@ -468,22 +468,22 @@ int build_tree(BuildBufs &b, TreeBufs &T, const PassParams &p, int n, cudaStream
         lvl_count.push_back(C);
         int D = d % 3;  // direct_local_start = 0 at one rank; axis cycles (src/fmm.c:99)
 
-        k_level_nch<<<grid_for(C, TB, maxb), TB, 0, st>>>(b, lb, C);
+        ph::note_launch(), k_level_nch<<<grid_for(C, TB, maxb), TB, 0, st>>>(b, lb, C);
         scan_exclusive_i32(b.tn_nch, b.tn_chunk_base, b.cnt + BC_LEVEL_COUNT, b.cap_nodes, b.cnt + BC_W,
                            b.scan_scratch, b.scan_scratch_elems, st);
         int wgrid = maxb;
-        k_chunk_sum<<<wgrid, TB, 0, st>>>(b, lb, C, D);
-        k_node_mean<<<grid_for(C * 32, TB, maxb), TB, 0, st>>>(b, lb, C, D);
-        k_chunk_count<<<wgrid, TB, 0, st>>>(b, lb, C, D);
-        k_node_split<<<grid_for(C * 32, TB, maxb), TB, 0, st>>>(b, lb, C, p.maxleaf);
+        ph::note_launch(), k_chunk_sum<<<wgrid, TB, 0, st>>>(b, lb, C, D);
+        ph::note_launch(), k_node_mean<<<grid_for(C * 32, TB, maxb), TB, 0, st>>>(b, lb, C, D);
+        ph::note_launch(), k_chunk_count<<<wgrid, TB, 0, st>>>(b, lb, C, D);
+        ph::note_launch(), k_node_split<<<grid_for(C * 32, TB, maxb), TB, 0, st>>>(b, lb, C, p.maxleaf);
         scan_exclusive_i32(b.tn_nodeflag, b.tn_nodebase, b.cnt + BC_LEVEL_COUNT, b.cap_nodes, b.cnt + BC_NEXT_NODES,
                            b.scan_scratch, b.scan_scratch_elems, st);
         scan_exclusive_i32(b.tn_leafflag, b.tn_leafbase, b.cnt + BC_LEVEL_COUNT, b.cap_nodes, b.cnt + BC_NEW_LEAVES,
                            b.scan_scratch, b.scan_scratch_elems, st);
-        k_make_children<<<grid_for(C, TB, maxb), TB, 0, st>>>(b, lb, C, p.maxleaf, D);
-        k_rank<<<wgrid, TB, 0, st>>>(b, lb, C, D);
-        k_swap<<<wgrid, TB, 0, st>>>(b, lb, C, D);
-        k_level_finish<<<1, 1, 0, st>>>(b);
+        ph::note_launch(), k_make_children<<<grid_for(C, TB, maxb), TB, 0, st>>>(b, lb, C, p.maxleaf, D);
+        ph::note_launch(), k_rank<<<wgrid, TB, 0, st>>>(b, lb, C, D);
+        ph::note_launch(), k_swap<<<wgrid, TB, 0, st>>>(b, lb, C, D);
+        ph::note_launch(), k_level_finish<<<1, 1, 0, st>>>(b);
         PH_CUDA_CHECK(cudaGetLastError());
         lb += C;
     }
@@ -492,11 +492,11 @@ int build_tree(BuildBufs &b, TreeBufs &T, const PassParams &p, int n, cudaStream
     int nlev = (int)lvl_begin.size();
     // subtree sizes bottom-up, numbers top-down
     for (int d = nlev - 1; d >= 0; d--)
-        k_subtree_counts<<<grid_for(lvl_count[d], TB, maxb), TB, 0, st>>>(b, lvl_begin[d], lvl_count[d]);
+        ph::note_launch(), k_subtree_counts<<<grid_for(lvl_count[d], TB, maxb), TB, 0, st>>>(b, lvl_begin[d], lvl_count[d]);
     for (int d = 0; d < nlev; d++)
-        k_number<<<grid_for(lvl_count[d], TB, maxb), TB, 0, st>>>(b, lvl_begin[d], lvl_count[d]);
-    k_scatter_nodes<<<grid_for(nnodes, TB, maxb), TB, 0, st>>>(b, T, nnodes, nleaves);
-    k_scatter_leaves<<<grid_for(nleaves, TB, maxb), TB, 0, st>>>(b, T, nleaves);
+        ph::note_launch(), k_number<<<grid_for(lvl_count[d], TB, maxb), TB, 0, st>>>(b, lvl_begin[d], lvl_count[d]);
+    ph::note_launch(), k_scatter_nodes<<<grid_for(nnodes, TB, maxb), TB, 0, st>>>(b, T, nnodes, nleaves);
+    ph::note_launch(), k_scatter_leaves<<<grid_for(nleaves, TB, maxb), TB, 0, st>>>(b, T, nleaves);
     // depth lists: depth d = nodes of level d + leaves created by level d-1
     int ndepth = nlev + 1;  // leaves can sit one level below the deepest nodes
     std::vector<int> doff(ndepth + 1, 0);
@@ -511,7 +511,7 @@ int build_tree(BuildBufs &b, TreeBufs &T, const PassParams &p, int n, cudaStream
         int lc = d < (int)leaf_count.size() ? leaf_count[d] : 0;
         int lbeg = d < (int)leaf_begin.size() ? leaf_begin[d] : 0;
         if (nc + lc == 0) continue;
-        k_depth_lists<<<grid_for(nc + lc, TB, maxb), TB, 0, st>>>(b, T, d, nbeg, nc, lbeg, lc, doff[d], nleaves);
+        ph::note_launch(), k_depth_lists<<<grid_for(nc + lc, TB, maxb), TB, 0, st>>>(b, T, d, nbeg, nc, lbeg, lc, doff[d], nleaves);
     }
     PH_CUDA_CHECK(cudaMemcpyAsync(T.depth_off, doff.data(), sizeof(int) * (ndepth + 1), cudaMemcpyHostToDevice, st));
     PH_CUDA_CHECK(cudaGetLastError());

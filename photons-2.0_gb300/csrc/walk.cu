@@ -331,9 +331,9 @@ int walk_lists(WalkBufs &w, const TreeBufs &t, const TreeInfo &info, const PassP
         if (A.list_end > A.list_begin) {
             int need = A.list_end - A.list_begin;
             int nb = (need * 32 + WALK_TB - 1) / WALK_TB;
-            k_walk_level<<<nb < blocks ? nb : blocks, WALK_TB, 0, st>>>(A);
+            ph::note_launch(), k_walk_level<<<nb < blocks ? nb : blocks, WALK_TB, 0, st>>>(A);
         }
-        k_walk_level_done<<<1, 1, 0, st>>>(w, d);
+        ph::note_launch(), k_walk_level_done<<<1, 1, 0, st>>>(w, d);
     }
     PH_CUDA_CHECK(cudaGetLastError());
     PH_CUDA_CHECK(cudaMemcpyAsync(stats.c, w.ctr, sizeof(stats.c), cudaMemcpyDeviceToHost, st));
