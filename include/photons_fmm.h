@@ -140,8 +140,10 @@ int photons_direct_sum(const photons_params *p, int n, const double *pos, int nt
 /* kernels launched by this library so far (all contexts) */
 unsigned long long photons_launch_count(void);
 
-/* FP32 FMA throughput probe: returns TFLOP/s measured over ~iters FMAs per thread */
+/* FP32 FMA throughput probes: TFLOP/s of FFMA chains, and of the paired
+   (float2) FFMA of sm_100+; ~iters x 128 FMAs per thread */
 double photons_fp32_fma_peak(int iters);
+double photons_fp32x2_fma_peak(int iters);
 
 #ifdef __cplusplus
 }

@@ -147,6 +147,7 @@ static int alloc_tree(photons_ctx *c, int n, int cap)
         PH_TRY(dalloc(w.pd_off, cu)); PH_TRY(dalloc(w.pd_cnt, cu));
         PH_TRY(dalloc(w.p2p_off, cu)); PH_TRY(dalloc(w.p2p_cnt, cu));
         PH_TRY(dalloc(w.m2l_off, cu)); PH_TRY(dalloc(w.m2l_cnt, cu));
+        PH_TRY(dalloc(t.chi, cu)); PH_TRY(dalloc(t.clo, cu)); PH_TRY(dalloc(t.w32, cu));
         PH_TRY(dalloc(c->M, (size_t)cu * PH_NMULTI));
         PH_TRY(dalloc(c->L, (size_t)cu * PH_NMULTI));
         c->cap_u = cu;
@@ -200,7 +201,7 @@ static void free_all(photons_ctx *c)
                     c->t.wz, c->t.wsum, c->t.split, c->t.depth_list, c->t.depth_off, c->w.pd_pool[0],
                     c->w.pd_pool[1], c->w.pd_off, c->w.pd_cnt, c->w.p2p_pool, c->w.p2p_off, c->w.p2p_cnt,
                     c->w.m2l_pool, c->w.m2l_off, c->w.m2l_cnt, c->w.scratch, c->w.ctr, c->pos4, c->ax, c->ay,
-                    c->az, c->M, c->L, c->io, c->work_counter};
+                    c->az, c->M, c->L, c->io, c->work_counter, c->t.chi, c->t.clo, c->t.w32};
     for (void *p : ptrs)
         if (p) cudaFree(p);
 }
@@ -276,6 +277,7 @@ int ph_stage_build(photons_ctx *c, const photons_params *p, int n, const double 
     info.nleaf_cap = info.nnode_cap = cap;
     PH_TRY(ph::build_tree(c->b, c->t, c->pp, n, st, info, nullptr));
     c->info = info;
+    PH_TRY(ph::launch_geom32(c->t, info.nleaf + info.nnode, st));
     PH_TRY(ph::launch_leaf_offsets(c->b, c->t, info.nleaf, c->pos4, st));
     PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_TREE], st));
     c->have_tree = true;
@@ -340,11 +342,17 @@ int ph_stage_p2p(photons_ctx *c, int precision, int zero)
     a.nleaf = c->info.nleaf;
     a.p2p_pool = c->w.p2p_pool; a.p2p_off = c->w.p2p_off; a.p2p_cnt = c->w.p2p_cnt;
     a.pos4 = c->pos4;
+    a.chi = c->t.chi;
+    a.clo = c->t.clo;
     a.px = c->b.x; a.py = c->b.y; a.pz = c->b.z;
     a.ax = c->ax; a.ay = c->ay; a.az = c->az;
     a.work_counter = c->work_counter;
     a.boxsize = c->pp.boxsize; a.eps = c->pp.eps; a.mass = c->pp.mass; a.rs = c->pp.rs;
     a.k = ph::make_split_consts(c->pp);
+    {
+        const char *v = getenv("PHOTONS_P2P_KERNEL");
+        a.variant = (v && !strcmp(v, "scalar")) ? 1 : 0;
+    }
     PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_P2P_BEGIN], st));
     PH_TRY(ph::launch_p2p(a, precision == PHOTONS_FP64, st));
     PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_P2P], st));

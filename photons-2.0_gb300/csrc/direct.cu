@@ -82,6 +82,25 @@ __global__ void k_fma_probe(float *out, int iters, float seed)
     if (s == 1234.5f) out[0] = s;  // keeps the chains live
 }
 
+__global__ void k_fma2_probe(float *out, int iters, float seed)
+{
+    float2 a0 = make_float2(seed + threadIdx.x, seed - threadIdx.x), a1 = make_float2(a0.x + 1.f, a0.y + 1.f),
+           a2 = make_float2(a0.x + 2.f, a0.y + 2.f), a3 = make_float2(a0.x + 3.f, a0.y + 3.f);
+    float2 a4 = make_float2(a0.x + 4.f, a0.y + 4.f), a5 = make_float2(a0.x + 5.f, a0.y + 5.f),
+           a6 = make_float2(a0.x + 6.f, a0.y + 6.f), a7 = make_float2(a0.x + 7.f, a0.y + 7.f);
+    const float2 m = make_float2(0.999999f, 0.999999f), c = make_float2(1e-7f, 1e-7f);
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            a0 = __ffma2_rn(a0, m, c); a1 = __ffma2_rn(a1, m, c); a2 = __ffma2_rn(a2, m, c); a3 = __ffma2_rn(a3, m, c);
+            a4 = __ffma2_rn(a4, m, c); a5 = __ffma2_rn(a5, m, c); a6 = __ffma2_rn(a6, m, c); a7 = __ffma2_rn(a7, m, c);
+        }
+    }
+    float s = a0.x + a1.x + a2.x + a3.x + a4.x + a5.x + a6.x + a7.x + a0.y + a1.y + a2.y + a3.y + a4.y + a5.y +
+              a6.y + a7.y;
+    if (s == 1234.5f) out[0] = s;
+}
+
 }  // namespace
 
 extern "C" int photons_direct_sum(const photons_params *p, int n, const double *pos, int nt, const int *targets,
@@ -164,7 +183,7 @@ extern "C" int photons_direct_sum(const photons_params *p, int n, const double *
     return rc;
 }
 
-extern "C" double photons_fp32_fma_peak(int iters)
+static double fma_probe(int iters, bool packed)
 {
     photons_gpu_clear_error();
     if (iters < 1) iters = 4096;
@@ -174,9 +193,11 @@ extern "C" double photons_fp32_fma_peak(int iters)
     cudaEvent_t a, b;
     cudaEventCreate(&a);
     cudaEventCreate(&b);
-    ph::note_launch(), k_fma_probe<<<blocks, threads>>>(d, iters / 8 + 1, 1.0f);  // warm-up
+    if (packed) ph::note_launch(), k_fma2_probe<<<blocks, threads>>>(d, iters / 8 + 1, 1.0f);  // warm-up
+    else ph::note_launch(), k_fma_probe<<<blocks, threads>>>(d, iters / 8 + 1, 1.0f);
     cudaEventRecord(a);
-    ph::note_launch(), k_fma_probe<<<blocks, threads>>>(d, iters, 1.0f);
+    if (packed) ph::note_launch(), k_fma2_probe<<<blocks, threads>>>(d, iters, 1.0f);
+    else ph::note_launch(), k_fma_probe<<<blocks, threads>>>(d, iters, 1.0f);
     cudaEventRecord(b);
     cudaEventSynchronize(b);
     float ms = 0.f;
@@ -185,6 +206,20 @@ extern "C" double photons_fp32_fma_peak(int iters)
     cudaEventDestroy(b);
     cudaFree(d);
     if (cudaGetLastError() != cudaSuccess || ms <= 0.f) return -1.0;
-    double flops = 2.0 * 8.0 * 16.0 * (double)iters * blocks * threads;
+    double flops = (packed ? 2.0 : 1.0) * 2.0 * 8.0 * 16.0 * (double)iters * blocks * threads;
     return flops / (ms * 1e-3) / 1e12;
+}
+
+extern "C" double photons_fp32_fma_peak(int iters)
+{
+    photons_gpu_clear_error();
+    if (iters < 1) iters = 4096;
+    return fma_probe(iters, false);
+}
+
+extern "C" double photons_fp32x2_fma_peak(int iters)
+{
+    photons_gpu_clear_error();
+    if (iters < 1) iters = 4096;
+    return fma_probe(iters, true);
 }

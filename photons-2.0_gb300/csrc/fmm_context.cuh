@@ -58,6 +58,7 @@ struct TreeBufs {
     double *cx = nullptr, *cy = nullptr, *cz = nullptr;
     double *wx = nullptr, *wy = nullptr, *wz = nullptr;
     double *wsum = nullptr, *split = nullptr;
+    float4 *chi = nullptr, *clo = nullptr, *w32 = nullptr;  // FP32 copies (centre hi/lo, widths + sum)
     // per-depth lists of unified ids
     int *depth_off = nullptr;   // [max_depth+2]
     int *depth_list = nullptr;  // [cap_u]
@@ -103,6 +104,7 @@ struct WalkStats {
     unsigned long long c[WC_N];
 };
 
+int launch_geom32(const TreeBufs &t, int nu, cudaStream_t st);
 // image_mask: bit 0 the local tree, bit k the k-th periodic image
 int walk_lists(WalkBufs &w, const TreeBufs &t, const TreeInfo &info, const PassParams &p, unsigned image_mask,
                cudaStream_t st, WalkStats &stats);

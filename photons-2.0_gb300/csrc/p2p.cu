@@ -195,6 +195,229 @@ __global__ void __launch_bounds__(P2P_TB) k_p2p_split(P2PArgs A)
 }
 
 // ---------------------------------------------------------------------
+// FP32 split-precision kernel, packed (the default).
+//
+// * Centre differences without FP64: every leaf centre is kept as an FP32
+//   pair hi + lo.  For an image shift of +-L along an axis the L is taken off
+//   whichever centre lies near the far face (target for +L, source for -L),
+//   where the subtraction is exact; then (hi_s - hi_t) + (lo_s - lo_t) is
+//   exact up to the final rounding.
+// * Staging: one lane per staged source (coalesced loads, conflict-free
+//   shared stores); the lane finds its list entry by a binary search over
+//   the 32 entries' prefix counts held in the warp.
+// * Lanes: a block of up to 64 targets is taken in at most two rounds of
+//   m = 32, 16, ..., 1 targets with 32/m source streams each; both rounds
+//   run over every staged batch, accumulating in registers.
+// * Arithmetic: two sources per lane per step with the paired FP32
+//   instructions of sm_100+; each stream's batch partial is added to its
+//   running sum with Kahan compensation.
+// ---------------------------------------------------------------------
+#define STAGE2 384  // staged sources per warp; 3 x 8 warps x 386 floats + reduction fit 48 KB
+
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+
+// one round's share of a staged batch: stream k takes source pairs k, k+G, ...
+__device__ __forceinline__ void p2p_round(const float2 *__restrict__ X2, const float2 *__restrict__ Y2,
+                                          const float2 *__restrict__ Z2, int npairs, int k, int G, float ox,
+                                          float oy, float oz, const SplitConsts &K, float &rx, float &ry, float &rz)
+{
+    const float2 nox = f2(-ox), noy = f2(-oy), noz = f2(-oz);
+    const float2 kq2 = f2(K.kq), pia2 = f2(K.pia), clin2 = f2(K.clin), one2 = f2(1.0f);
+    const float2 a0 = f2(K.a[0]), a1 = f2(K.a[1]), a2 = f2(K.a[2]), a3 = f2(K.a[3]), a4 = f2(K.a[4]),
+                 a5 = f2(K.a[5]);
+    float2 ax = f2(0.f), ay = f2(0.f), az = f2(0.f);
+#pragma unroll 2
+    for (int pp = k; pp < npairs; pp += G) {
+        const float2 dx = __fadd2_rn(X2[pp], nox);
+        const float2 dy = __fadd2_rn(Y2[pp], noy);
+        const float2 dz = __fadd2_rn(Z2[pp], noz);
+        float2 qq = __fmul2_rn(dx, dx);
+        qq = __ffma2_rn(dy, dy, qq);
+        qq = __ffma2_rn(dz, dz, qq);
+        qq.x = fmaxf(qq.x, K.eps2);
+        qq.y = fmaxf(qq.y, K.eps2);
+        const float2 rinv = make_float2(rsqrt_approx(qq.x), rsqrt_approx(qq.y));
+        const float2 r = __fmul2_rn(qq, rinv);
+        const float2 den = __ffma2_rn(pia2, r, one2);
+        const float2 tt = make_float2(rcp_approx(den.x), rcp_approx(den.y));
+        float2 P = __ffma2_rn(a5, tt, a4);
+        P = __ffma2_rn(P, tt, a3);
+        P = __ffma2_rn(P, tt, a2);
+        P = __ffma2_rn(P, tt, a1);
+        P = __ffma2_rn(P, tt, a0);
+        const float2 h = __ffma2_rn(tt, P, __fmul2_rn(clin2, r));
+        const float2 ea = __fmul2_rn(qq, kq2);
+        const float2 ex = make_float2(ex2_approx(ea.x), ex2_approx(ea.y));
+        const float2 rinv2 = __fmul2_rn(rinv, rinv);
+        const float2 f = __fmul2_rn(__fmul2_rn(ex, h), __fmul2_rn(rinv2, rinv));
+        ax = __ffma2_rn(dx, f, ax);
+        ay = __ffma2_rn(dy, f, ay);
+        az = __ffma2_rn(dz, f, az);
+    }
+    rx = ax.x + ax.y;
+    ry = ay.x + ay.y;
+    rz = az.x + az.y;
+}
+
+// centre difference (c_s + shift) - c_t per axis from hi/lo parts
+__device__ __forceinline__ float centre_diff(float hs, float ls, float ht, float lt, int o, float Lhi, float Llo)
+{
+    if (o < 0) { hs -= Lhi; ls -= Llo; }
+    else if (o > 0) { ht -= Lhi; lt -= Llo; }
+    return (hs - ht) + (ls - lt);
+}
+
+__global__ void __launch_bounds__(P2P_TB, 3) k_p2p_split_packed(P2PArgs A)
+{
+    __shared__ __align__(16) float s_x[P2P_WARPS][STAGE2 + 2];
+    __shared__ __align__(16) float s_y[P2P_WARPS][STAGE2 + 2];
+    __shared__ __align__(16) float s_z[P2P_WARPS][STAGE2 + 2];
+    __shared__ double s_red[P2P_WARPS][32][3];
+    const int lane = warp_lane();
+    const int wib = threadIdx.x >> 5;
+    float *sx = s_x[wib], *sy = s_y[wib], *sz = s_z[wib];
+    const float2 *X2 = reinterpret_cast<const float2 *>(sx);
+    const float2 *Y2 = reinterpret_cast<const float2 *>(sy);
+    const float2 *Z2 = reinterpret_cast<const float2 *>(sz);
+    const SplitConsts K = A.k;
+    const float Lhi = (float)A.boxsize, Llo = (float)(A.boxsize - (double)Lhi);
+
+    for (;;) {
+        int t;
+        if (lane == 0) t = atomicAdd(A.work_counter, 1);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= A.nleaf) break;
+        const int nt = A.npart[t], it = A.ipart[t];
+        if (nt == 0) continue;
+        const float4 cth = A.chi[t], ctl = A.clo[t];
+        const long long eoff = A.p2p_off[t];
+        const int ecnt = A.p2p_cnt[t];
+
+        for (int tb = 0; tb < nt; tb += 64) {
+            // rounds: m1 = largest power of two <= min(nb, 32); m2 covers the rest
+            const int nb = min(64, nt - tb);
+            const int lg1 = nb >= 32 ? 5 : 31 - __clz(nb);
+            const int m1 = 1 << lg1;
+            const int rest = nb - m1;
+            const int lg2 = rest <= 0 ? -1 : (rest >= 32 ? 5 : 32 - __clz(rest - 1));  // ceil(log2(rest))
+            const int m2 = lg2 < 0 ? 0 : (1 << lg2);
+            const int G1 = 32 >> lg1, q1 = lane & (m1 - 1), k1 = lane >> lg1;
+            const int G2 = m2 ? 32 >> lg2 : 1, q2 = m2 ? (lane & (m2 - 1)) : 0, k2 = m2 ? (lane >> lg2) : 0;
+            const float4 o1 = A.pos4[it + tb + q1];
+            // round-2 lanes beyond the block's last target reuse it; their sums are discarded
+            const float4 o2 = m2 ? A.pos4[it + tb + m1 + min(q2, rest - 1)] : make_float4(0.f, 0.f, 0.f, 0.f);
+            float s1x = 0.f, s1y = 0.f, s1z = 0.f, c1x = 0.f, c1y = 0.f, c1z = 0.f;
+            float s2x = 0.f, s2y = 0.f, s2z = 0.f, c2x = 0.f, c2y = 0.f, c2z = 0.f;
+
+            int e = 0;
+            while (e < ecnt) {
+                // lane i owns entry e+i: source leaf, size, centre offset
+                const int ne = min(32, ecnt - e);
+                int is = 0, ns = 0;
+                float d0 = 0.f, d1 = 0.f, d2 = 0.f;
+                if (lane < ne) {
+                    uint32_t en = A.p2p_pool[eoff + e + lane];
+                    int s = PH_ENTRY_ID(en), img = PH_ENTRY_IMG(en);
+                    is = A.ipart[s];
+                    ns = A.npart[s];
+                    const float4 csh = A.chi[s], csl = A.clo[s];
+                    int mi, mj, mk;
+                    image_offsets(img, mi, mj, mk);
+                    d0 = centre_diff(csh.x, csl.x, cth.x, ctl.x, mi, Lhi, Llo);
+                    d1 = centre_diff(csh.y, csl.y, cth.y, ctl.y, mj, Lhi, Llo);
+                    d2 = centre_diff(csh.z, csl.z, cth.z, ctl.z, mk, Lhi, Llo);
+                }
+                const int incl = warp_incl_scan(ns);
+                const unsigned fit = __ballot_sync(0xffffffffu, lane < ne && incl <= STAGE2);
+                const int nfit = __popc(fit);
+                if (nfit == 0) break;  // unreachable under the MAXLEAF bound; never spin
+                const int nstaged = __shfl_sync(0xffffffffu, incl, nfit - 1);
+                const int pre = incl - ns;
+                // cooperative staging: staged source idx -> its entry by binary search
+                for (int s0 = 0; s0 < nstaged; s0 += 32) {
+                    const int idx = s0 + lane;
+                    int lo = 0;
+#pragma unroll
+                    for (int step = 16; step >= 1; step >>= 1) {
+                        const int cand = lo + step;
+                        const int pc = __shfl_sync(0xffffffffu, pre, cand & 31);
+                        if (cand < nfit && pc <= idx) lo = cand;
+                    }
+                    const int eis = __shfl_sync(0xffffffffu, is, lo);
+                    const int epre = __shfl_sync(0xffffffffu, pre, lo);
+                    const float e0 = __shfl_sync(0xffffffffu, d0, lo);
+                    const float e1 = __shfl_sync(0xffffffffu, d1, lo);
+                    const float e2 = __shfl_sync(0xffffffffu, d2, lo);
+                    if (idx < nstaged) {
+                        const float4 o = A.pos4[eis + idx - epre];
+                        sx[idx] = o.x + e0;
+                        sy[idx] = o.y + e1;
+                        sz[idx] = o.z + e2;
+                    }
+                }
+                // an odd count gets one far-away source whose force is exactly 0
+                if (lane == 0 && (nstaged & 1)) {
+                    sx[nstaged] = 1e18f;
+                    sy[nstaged] = 1e18f;
+                    sz[nstaged] = 1e18f;
+                }
+                __syncwarp();
+                const int npairs = (nstaged + 1) >> 1;
+                float px, py, pz;
+                p2p_round(X2, Y2, Z2, npairs, k1, G1, o1.x, o1.y, o1.z, K, px, py, pz);
+                kahan_add(s1x, c1x, px);
+                kahan_add(s1y, c1y, py);
+                kahan_add(s1z, c1z, pz);
+                if (m2) {
+                    p2p_round(X2, Y2, Z2, npairs, k2, G2, o2.x, o2.y, o2.z, K, px, py, pz);
+                    kahan_add(s2x, c2x, px);
+                    kahan_add(s2y, c2y, py);
+                    kahan_add(s2z, c2z, pz);
+                }
+                __syncwarp();
+                e += nfit;
+            }
+            // combine the streams of each target in a fixed order
+            double *red = &s_red[wib][0][0];
+            red[3 * lane + 0] = (double)s1x - (double)c1x;
+            red[3 * lane + 1] = (double)s1y - (double)c1y;
+            red[3 * lane + 2] = (double)s1z - (double)c1z;
+            __syncwarp();
+            if (lane < m1) {
+                double b0 = 0.0, b1 = 0.0, b2 = 0.0;
+                for (int k = 0; k < G1; k++) {
+                    const int l = k * m1 + lane;
+                    b0 += red[3 * l]; b1 += red[3 * l + 1]; b2 += red[3 * l + 2];
+                }
+                const int ip = it + tb + lane;
+                A.ax[ip] += b0;
+                A.ay[ip] += b1;
+                A.az[ip] += b2;
+            }
+            __syncwarp();
+            if (m2) {
+                red[3 * lane + 0] = (double)s2x - (double)c2x;
+                red[3 * lane + 1] = (double)s2y - (double)c2y;
+                red[3 * lane + 2] = (double)s2z - (double)c2z;
+                __syncwarp();
+                if (lane < rest) {
+                    double b0 = 0.0, b1 = 0.0, b2 = 0.0;
+                    for (int k = 0; k < G2; k++) {
+                        const int l = k * m2 + lane;
+                        b0 += red[3 * l]; b1 += red[3 * l + 1]; b2 += red[3 * l + 2];
+                    }
+                    const int ip = it + tb + m1 + lane;
+                    A.ax[ip] += b0;
+                    A.ay[ip] += b1;
+                    A.az[ip] += b2;
+                }
+                __syncwarp();
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------
 // FP64 kernel: the reference's arithmetic
 // ---------------------------------------------------------------------
 struct Src64 {
@@ -344,7 +567,8 @@ int launch_p2p(const P2PArgs &a, int fp64, cudaStream_t st)
     PH_CUDA_CHECK(cudaMemsetAsync(a.work_counter, 0, sizeof(int), st));
     int blocks = device_sm_count() * (fp64 ? 4 : 4);
     if (fp64) ph::note_launch(), k_p2p_fp64<<<blocks, P2P_TB, 0, st>>>(a);
-    else ph::note_launch(), k_p2p_split<<<blocks, P2P_TB, 0, st>>>(a);
+    else if (a.variant == 1) ph::note_launch(), k_p2p_split<<<blocks, P2P_TB, 0, st>>>(a);
+    else ph::note_launch(), k_p2p_split_packed<<<blocks, P2P_TB, 0, st>>>(a);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }

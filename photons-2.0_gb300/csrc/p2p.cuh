@@ -21,12 +21,14 @@ struct P2PArgs {
     const int *p2p_cnt;
     // particles (tree order)
     const float4 *pos4;  // FP32 offsets from the leaf centre
+    const float4 *chi, *clo;  // leaf centres as FP32 hi + lo pairs
     const double *px, *py, *pz;
     // output (tree order); written, not accumulated
     double *ax, *ay, *az;
     int *work_counter;
     double boxsize, eps, mass, rs;
     SplitConsts k;
+    int variant;  // FP32: 0 packed (default), 1 scalar
 };
 
 SplitConsts make_split_consts(const PassParams &p);

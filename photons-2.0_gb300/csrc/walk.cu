@@ -36,6 +36,7 @@ namespace {
 struct Geo {
     const double *cx, *cy, *cz, *wx, *wy, *wz, *wsum;
     const int *son0, *son1, *npart, *parent;
+    const float4 *chi, *clo, *w32;  // FP32 copies: centre hi/lo, (width xyz, width sum)
 };
 
 // MAC of src/fmm.c:266-326 (LONGSHORT): 1 accept, 0 open, -1 drop
@@ -61,6 +62,50 @@ __device__ __forceinline__ int acceptance_fp64(double wi0, double wi1, double wi
     return (__dmul_rn(wmax, wmax) < __dmul_rn(theta2, dd2)) ? 1 : 0;
 }
 
+// (c_b + shift) - c_a along one axis from FP32 hi/lo centres: the box side
+// is taken off whichever centre lies near the far face, where it is exact
+__device__ __forceinline__ float centre_diff32(float hb, float lb, float ha, float la, int o, float Lhi, float Llo)
+{
+    if (o < 0) { hb -= Lhi; lb -= Llo; }
+    else if (o > 0) { ha -= Lhi; la -= Llo; }
+    return (hb - ha) + (lb - la);
+}
+
+// The MAC in FP32 with error margins.  Inputs: d = c_a - c_b' (relative
+// error ~1e-7 from the hi/lo difference), FP32 widths.  Every comparison of
+// the reference's sequence is decided only if the FP32 value clears its
+// threshold by a margin several times the worst-case FP32 error; otherwise
+// -2 is returned and the caller evaluates the exact FP64 MAC.
+__device__ __forceinline__ int acceptance_fp32(float wi0, float wi1, float wi2, float wj0, float wj1, float wj2,
+                                               float d0, float d1, float d2, float theta2, float c2)
+{
+    const float w0 = (wi0 + wj0) * 0.5f, w1 = (wi1 + wj1) * 0.5f, w2 = (wi2 + wj2) * 0.5f;
+    const float a0 = fabsf(d0), a1 = fabsf(d1), a2 = fabsf(d2);
+    const float u0 = a0 + w0, u1 = a1 + w1, u2 = a2 + w2;  // error scale of each gap
+    float g0 = a0 - w0, g1 = a1 - w1, g2 = a2 - w2;
+    g0 = g0 > 0.f ? g0 : 0.f;
+    g1 = g1 > 0.f ? g1 : 0.f;
+    g2 = g2 > 0.f ? g2 : 0.f;
+    const float S = g0 + g1 + g2;
+    const float eS = 2e-6f * (u0 + u1 + u2);
+    if (S < 1e-4f - eS) return 0;        // touching
+    if (S < 1e-4f + eS) return -2;
+    const float dm2 = g0 * g0 + g1 * g1 + g2 * g2;
+    const float edm = 4e-6f * (g0 * u0 + g1 * u1 + g2 * u2) + 1e-6f * (dm2 + c2);
+    if (dm2 >= c2 + edm) return -1;      // beyond the cutoff
+    if (dm2 > c2 - edm) return -2;
+    const float dd2 = d0 * d0 + d1 * d1 + d2 * d2;
+    const float edd = 2e-6f * (dd2 + c2);
+    if (dd2 > c2 + edd) return 0;
+    if (dd2 >= c2 - edd) return -2;
+    float wmax = fmaxf(w0, fmaxf(w1, w2)) * 2.f;
+    const float lhs = wmax * wmax, rhs = theta2 * dd2;
+    const float ew = 2e-6f * (lhs + rhs);
+    if (lhs < rhs - ew) return 1;
+    if (lhs > rhs + ew) return 0;
+    return -2;
+}
+
 struct WalkArgs {
     Geo g;
     WalkBufs w;
@@ -70,6 +115,7 @@ struct WalkArgs {
     int nroot;               // entries of the root's list: (root, img) for the selected images
     int root_img[PH_NIMG];
     double boxsize, theta2, c2, rcut, theta;
+    float Lhi, Llo, theta2f, c2f;
 };
 
 // sender-side pruning of an image node, src/remotes.c:97-158
@@ -121,6 +167,7 @@ __global__ void __launch_bounds__(WALK_TB) k_walk_level(WalkArgs A)
         const bool leaf_a = a < A.nleaf;
         const double ca0 = g.cx[a], ca1 = g.cy[a], ca2 = g.cz[a];
         const double wa0 = g.wx[a], wa1 = g.wy[a], wa2 = g.wz[a], wsa = g.wsum[a];
+        const float4 ah = g.chi[a], al = g.clo[a], aw = g.w32[a];
         const int na = g.npart[a];
         const int a0 = leaf_a ? -1 : g.son0[a], a1 = leaf_a ? -1 : g.son1[a];
         const int par = g.parent[a];
@@ -167,27 +214,35 @@ __global__ void __launch_bounds__(WALK_TB) k_walk_level(WalkArgs A)
                     if (img == 0) { c_p2p_loc++; c_pl += pr; }
                     else { c_p2p_img++; c_pi += pr; }
                 } else {
-                    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
                     int mi, mj, mk;
                     image_offsets(img, mi, mj, mk);
-                    s0 = mi * A.boxsize; s1 = mj * A.boxsize; s2 = mk * A.boxsize;
-                    // image node centre = local centre + shift (src/remotes.c:123-125)
-                    double cb0 = g.cx[b], cb1 = g.cy[b], cb2 = g.cz[b];
-                    if (img) { cb0 = __dadd_rn(cb0, s0); cb1 = __dadd_rn(cb1, s1); cb2 = __dadd_rn(cb2, s2); }
-                    int flag = acceptance_fp64(wa0, wa1, wa2, g.wx[b], g.wy[b], g.wz[b], __dsub_rn(ca0, cb0),
+                    const float4 bh = g.chi[b], bl = g.clo[b], bw = g.w32[b];
+                    const float e0 = centre_diff32(bh.x, bl.x, ah.x, al.x, mi, A.Lhi, A.Llo);
+                    const float e1 = centre_diff32(bh.y, bl.y, ah.y, al.y, mj, A.Lhi, A.Llo);
+                    const float e2 = centre_diff32(bh.z, bl.z, ah.z, al.z, mk, A.Lhi, A.Llo);
+                    int flag = acceptance_fp32(aw.x, aw.y, aw.z, bw.x, bw.y, bw.z, e0, e1, e2, A.theta2f, A.c2f);
+                    double s0 = mi * A.boxsize, s1 = mj * A.boxsize, s2 = mk * A.boxsize;
+                    if (flag == -2) {
+                        // image node centre = local centre + shift (src/remotes.c:123-125)
+                        double cb0 = g.cx[b], cb1 = g.cy[b], cb2 = g.cz[b];
+                        if (img) { cb0 = __dadd_rn(cb0, s0); cb1 = __dadd_rn(cb1, s1); cb2 = __dadd_rn(cb2, s2); }
+                        flag = acceptance_fp64(wa0, wa1, wa2, g.wx[b], g.wy[b], g.wz[b], __dsub_rn(ca0, cb0),
                                                __dsub_rn(ca1, cb1), __dsub_rn(ca2, cb2), A.theta2, A.c2);
+                    }
+                    // width-sum comparison of the open rule: FP32 decides unless the values tie
+                    const bool bigger_a = (aw.w != bw.w) ? (aw.w > bw.w) : (wsa > g.wsum[b]);
                     if (flag == -1) {
                         kind = OUT_NONE;
                     } else if (img == 0) {
                         if (flag == 1) kind = OUT_M2L;
                         else if (leaf_a) kind = OUT_OPEN;
                         else if (leaf_b) kind = OUT_PUSH;
-                        else kind = (wsa > g.wsum[b]) ? OUT_PUSH : OUT_OPEN;
+                        else kind = bigger_a ? OUT_PUSH : OUT_OPEN;
                     } else {
                         bool pruned = !leaf_b && image_pruned(A, b, s0, s1, s2);
                         if (leaf_a) kind = (flag == 1 || pruned) ? OUT_M2L : OUT_OPEN;
                         else if (flag == 1) kind = OUT_M2L;
-                        else kind = (leaf_b || pruned || wsa > g.wsum[b]) ? OUT_PUSH : OUT_OPEN;
+                        else kind = (leaf_b || pruned || bigger_a) ? OUT_PUSH : OUT_OPEN;
                     }
                     if (kind == OUT_M2L) {
                         if (img == 0) c_m2l_loc++;
@@ -300,7 +355,31 @@ __global__ void k_walk_level_done(WalkBufs W, int depth)
     }
 }
 
+// FP32 copies of the geometry for every unified id: centre as hi + lo,
+// widths and width sum rounded
+__global__ void k_geom32(const double *cx, const double *cy, const double *cz, const double *wx, const double *wy,
+                         const double *wz, const double *wsum, int nu, float4 *chi, float4 *clo, float4 *w32)
+{
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += gridDim.x * blockDim.x) {
+        double c0 = cx[u], c1 = cy[u], c2 = cz[u];
+        float h0 = (float)c0, h1 = (float)c1, h2 = (float)c2;
+        chi[u] = make_float4(h0, h1, h2, 0.f);
+        clo[u] = make_float4((float)(c0 - h0), (float)(c1 - h1), (float)(c2 - h2), 0.f);
+        w32[u] = make_float4((float)wx[u], (float)wy[u], (float)wz[u], (float)wsum[u]);
+    }
+}
+
 }  // namespace
+
+int launch_geom32(const TreeBufs &t, int nu, cudaStream_t st)
+{
+    int blocks = (nu + 255) / 256;
+    if (blocks > device_sm_count() * 8) blocks = device_sm_count() * 8;
+    if (blocks < 1) blocks = 1;
+    ph::note_launch(), k_geom32<<<blocks, 256, 0, st>>>(t.cx, t.cy, t.cz, t.wx, t.wy, t.wz, t.wsum, nu, t.chi, t.clo, t.w32);
+    PH_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
 
 int walk_lists(WalkBufs &w, const TreeBufs &t, const TreeInfo &info, const PassParams &p, unsigned image_mask,
                cudaStream_t st, WalkStats &stats)
@@ -311,6 +390,11 @@ int walk_lists(WalkBufs &w, const TreeBufs &t, const TreeInfo &info, const PassP
     A.g.cx = t.cx; A.g.cy = t.cy; A.g.cz = t.cz;
     A.g.wx = t.wx; A.g.wy = t.wy; A.g.wz = t.wz; A.g.wsum = t.wsum;
     A.g.son0 = t.son0; A.g.son1 = t.son1; A.g.npart = t.npart; A.g.parent = t.parent;
+    A.g.chi = t.chi; A.g.clo = t.clo; A.g.w32 = t.w32;
+    A.Lhi = (float)p.boxsize;
+    A.Llo = (float)(p.boxsize - (double)A.Lhi);
+    A.theta2f = (float)(p.theta * p.theta);
+    A.c2f = (float)(p.rcut * p.rcut);
     A.w = w;
     A.depth_list = t.depth_list;
     A.nleaf = info.nleaf;
