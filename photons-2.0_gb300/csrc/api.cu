@@ -147,13 +147,14 @@ static int alloc_tree(photons_ctx *c, int n, int cap)
         PH_TRY(dalloc(w.pd_off, cu)); PH_TRY(dalloc(w.pd_cnt, cu));
         PH_TRY(dalloc(w.p2p_off, cu)); PH_TRY(dalloc(w.p2p_cnt, cu));
         PH_TRY(dalloc(w.m2l_off, cu)); PH_TRY(dalloc(w.m2l_cnt, cu));
-        PH_TRY(dalloc(t.chi, cu)); PH_TRY(dalloc(t.clo, cu)); PH_TRY(dalloc(t.w32, cu));
+        PH_TRY(dalloc(t.chi, cu)); PH_TRY(dalloc(t.clo, cu)); PH_TRY(dalloc(t.w32, cu)); PH_TRY(dalloc(t.son2, cu));
         PH_TRY(dalloc(c->M, (size_t)cu * PH_NMULTI));
         PH_TRY(dalloc(c->L, (size_t)cu * PH_NMULTI));
         c->cap_u = cu;
     }
     if (chunks > b.cap_chunks) {
         PH_TRY(dalloc(b.ch_partial, chunks)); PH_TRY(dalloc(b.ch_cnt, chunks)); PH_TRY(dalloc(b.ch_small_base, chunks));
+        PH_TRY(dalloc(b.ch_node, chunks));
         b.cap_chunks = chunks;
         size_t need = ph::scan_scratch_elems(cap > chunks ? cap : chunks) + 8;
         if (need > b.scan_scratch_elems) {
@@ -177,7 +178,9 @@ static int alloc_walk(photons_ctx *c, long long p2p_cap, long long pd_cap, long 
         w.pd_cap = pd_cap;
     }
     if (m2l_cap > w.m2l_cap) { PH_TRY(dalloc(w.m2l_pool, m2l_cap)); w.m2l_cap = m2l_cap; }
-    int nwarps = ph::device_sm_count() * 2 * 8;
+    // resident 256-thread walk blocks per SM: 2 (no register spills) or 3
+    const char *wb = getenv("PHOTONS_WALK_BLOCKS");
+    int nwarps = ph::device_sm_count() * ((wb && atoi(wb) == 3) ? 3 : 2) * 8;
     if (stack_cap > w.stack_cap || stage_cap > w.stage_cap || nwarps != w.nwarps) {
         if (stack_cap < w.stack_cap) stack_cap = w.stack_cap;
         if (stage_cap < w.stage_cap) stage_cap = w.stage_cap;
@@ -196,12 +199,12 @@ static void free_all(photons_ctx *c)
                     b.tn_child0, b.tn_child1, b.tn_mode, b.tn_S, b.tn_box, b.tn_split, b.tn_nch, b.tn_chunk_base,
                     b.tn_nodeflag, b.tn_leafflag, b.tn_nodebase, b.tn_leafbase, b.tn_sub_nodes, b.tn_sub_leaves,
                     b.tn_pre, b.tn_lbase, b.tl_start, b.tl_len, b.tl_depth, b.tl_parent, b.tl_final, b.tl_box,
-                    b.ch_partial, b.ch_cnt, b.ch_small_base, b.cnt, b.scan_scratch, c->t.ipart, c->t.npart,
+                    b.ch_partial, b.ch_cnt, b.ch_small_base, b.ch_node, b.cnt, b.scan_scratch, c->t.ipart, c->t.npart,
                     c->t.depth, c->t.parent, c->t.son0, c->t.son1, c->t.cx, c->t.cy, c->t.cz, c->t.wx, c->t.wy,
                     c->t.wz, c->t.wsum, c->t.split, c->t.depth_list, c->t.depth_off, c->w.pd_pool[0],
                     c->w.pd_pool[1], c->w.pd_off, c->w.pd_cnt, c->w.p2p_pool, c->w.p2p_off, c->w.p2p_cnt,
                     c->w.m2l_pool, c->w.m2l_off, c->w.m2l_cnt, c->w.scratch, c->w.ctr, c->pos4, c->ax, c->ay,
-                    c->az, c->M, c->L, c->io, c->work_counter, c->t.chi, c->t.clo, c->t.w32};
+                    c->az, c->M, c->L, c->io, c->work_counter, c->t.chi, c->t.clo, c->t.w32, c->t.son2};
     for (void *p : ptrs)
         if (p) cudaFree(p);
 }

@@ -30,7 +30,7 @@ struct BuildBufs {
     double *tl_box = nullptr;  // [6][cap_leaves]
     // chunks
     double *ch_partial = nullptr;
-    int *ch_cnt = nullptr, *ch_small_base = nullptr;
+    int *ch_cnt = nullptr, *ch_small_base = nullptr, *ch_node = nullptr;
     // small device counters
     int *cnt = nullptr;  // see BuildCounter
     int *scan_scratch = nullptr;
@@ -59,6 +59,7 @@ struct TreeBufs {
     double *wx = nullptr, *wy = nullptr, *wz = nullptr;
     double *wsum = nullptr, *split = nullptr;
     float4 *chi = nullptr, *clo = nullptr, *w32 = nullptr;  // FP32 copies (centre hi/lo, widths + sum)
+    int2 *son2 = nullptr;                                    // (son0, son1)
     // per-depth lists of unified ids
     int *depth_off = nullptr;   // [max_depth+2]
     int *depth_list = nullptr;  // [cap_u]

@@ -87,6 +87,17 @@ __global__ void k_level_nch(BuildBufs b, int lb, int C)
         b.tn_nch[i] = (b.tn_len[lb + i] + CHUNK - 1) / CHUNK;
 }
 
+// chunk -> level-local node index, written once per level
+__global__ void k_chunk_map(BuildBufs b, int C)
+{
+    int lane = warp_lane();
+    int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = gw; i < C; i += nw) {
+        int c0 = b.tn_chunk_base[i], nc = b.tn_nch[i];
+        for (int k = lane; k < nc; k += 32) b.ch_node[c0 + k] = i;
+    }
+}
+
 __global__ void k_chunk_sum(BuildBufs b, int lb, int C, int D)
 {
     const double *coord = axis_ptr(b.x, b.y, b.z, D);
@@ -94,7 +105,7 @@ __global__ void k_chunk_sum(BuildBufs b, int lb, int C, int D)
     int lane = warp_lane();
     int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
     for (int w = gw; w < W; w += nw) {
-        int i = upper_bound_i32(b.tn_chunk_base, C, w) - 1;
+        int i = b.ch_node[w];
         int t = lb + i;
         int start = b.tn_start[t], len = b.tn_len[t];
         int s0 = (w - b.tn_chunk_base[i]) * CHUNK;
@@ -134,7 +145,7 @@ __global__ void k_chunk_count(BuildBufs b, int lb, int C, int D)
     int lane = warp_lane();
     int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
     for (int w = gw; w < W; w += nw) {
-        int i = upper_bound_i32(b.tn_chunk_base, C, w) - 1;
+        int i = b.ch_node[w];
         int t = lb + i;
         int start = b.tn_start[t], len = b.tn_len[t];
         double mean = b.tn_split[t];
@@ -266,7 +277,7 @@ __global__ void k_rank(BuildBufs b, int lb, int C, int D)
     unsigned lt = (1u << lane) - 1u;
     int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
     for (int w = gw; w < W; w += nw) {
-        int i = upper_bound_i32(b.tn_chunk_base, C, w) - 1;
+        int i = b.ch_node[w];
         int t = lb + i;
         if (b.tn_mode[t] != 0) continue;
         int start = b.tn_start[t], len = b.tn_len[t];
@@ -308,7 +319,7 @@ __global__ void k_swap(BuildBufs b, int lb, int C, int D)
     int lane = warp_lane();
     int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
     for (int w = gw; w < W; w += nw) {
-        int i = upper_bound_i32(b.tn_chunk_base, C, w) - 1;
+        int i = b.ch_node[w];
         int t = lb + i;
         int mode = b.tn_mode[t];
         int start = b.tn_start[t], len = b.tn_len[t];
@@ -472,6 +483,7 @@ int build_tree(BuildBufs &b, TreeBufs &T, const PassParams &p, int n, cudaStream
         scan_exclusive_i32(b.tn_nch, b.tn_chunk_base, b.cnt + BC_LEVEL_COUNT, b.cap_nodes, b.cnt + BC_W,
                            b.scan_scratch, b.scan_scratch_elems, st);
         int wgrid = maxb;
+        ph::note_launch(), k_chunk_map<<<grid_for(C * 32, TB, maxb), TB, 0, st>>>(b, C);
         ph::note_launch(), k_chunk_sum<<<wgrid, TB, 0, st>>>(b, lb, C, D);
         ph::note_launch(), k_node_mean<<<grid_for(C * 32, TB, maxb), TB, 0, st>>>(b, lb, C, D);
         ph::note_launch(), k_chunk_count<<<wgrid, TB, 0, st>>>(b, lb, C, D);

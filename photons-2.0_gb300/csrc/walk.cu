@@ -36,6 +36,7 @@ namespace {
 struct Geo {
     const double *cx, *cy, *cz, *wx, *wy, *wz, *wsum;
     const int *son0, *son1, *npart, *parent;
+    const int2 *son;                // (son0, son1) of nodes, for one load
     const float4 *chi, *clo, *w32;  // FP32 copies: centre hi/lo, (width xyz, width sum)
 };
 
@@ -144,7 +145,26 @@ __device__ __forceinline__ bool image_pruned(const WalkArgs &A, int b, double s0
 
 enum { OUT_NONE = 0, OUT_P2P = 1, OUT_M2L = 2, OUT_PUSH = 3, OUT_OPEN = 4, OUT_SELF_PUSH = 5 };
 
-__global__ void __launch_bounds__(WALK_TB) k_walk_level(WalkArgs A)
+// Per-warp stack and output staging: the first entries live in shared
+// memory, the rest in the warp's global scratch (same index space).
+#define WS_STACK 256
+#define WS_P2P 640
+#define WS_PD 448
+#define WS_M2L 128
+#define WS_TOTAL (WS_STACK + WS_P2P + WS_PD + WS_M2L)
+
+__device__ __forceinline__ void put2(uint32_t *s, int scap, uint32_t *g, int pos, uint32_t v)
+{
+    if (pos < scap) s[pos] = v;
+    else g[pos] = v;
+}
+__device__ __forceinline__ uint32_t get2(const uint32_t *s, int scap, const uint32_t *g, int pos)
+{
+    return pos < scap ? s[pos] : g[pos];
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(WALK_TB, MINB) k_walk_level(WalkArgs A)
 {
     const Geo &g = A.g;
     WalkBufs &W = A.w;
@@ -157,6 +177,11 @@ __global__ void __launch_bounds__(WALK_TB) k_walk_level(WalkArgs A)
     uint32_t *st_p2p = stack + W.stack_cap;
     uint32_t *st_m2l = st_p2p + W.stage_cap;
     uint32_t *st_pd = st_m2l + W.stage_cap;
+    __shared__ uint32_t s_buf[WALK_TB / 32][WS_TOTAL];
+    uint32_t *sh_stack = s_buf[threadIdx.x >> 5];
+    uint32_t *sh_p2p = sh_stack + WS_STACK;
+    uint32_t *sh_pd = sh_p2p + WS_P2P;
+    uint32_t *sh_m2l = sh_pd + WS_PD;
     const int parity = A.depth & 1;
     unsigned long long c_p2p_loc = 0, c_p2p_img = 0, c_m2l_loc = 0, c_m2l_img = 0, c_pl = 0, c_pi = 0;
     unsigned flags = 0;
@@ -182,111 +207,150 @@ __global__ void __launch_bounds__(WALK_TB) k_walk_level(WalkArgs A)
         int top = 0, in_pos = 0;
         int n_p2p = 0, n_m2l = 0, n_pd = 0;
         for (;;) {
+            // up to 64 entries per step, two per lane, stack first
             int k;
-            uint32_t e = 0;
+            uint32_t e[2] = {0u, 0u};
             if (top > 0) {
-                k = min(32, top);
+                k = min(64, top);
                 top -= k;
-                if (lane < k) e = stack[top + lane];
+                if (lane < k) e[0] = get2(sh_stack, WS_STACK, stack, top + lane);
+                if (lane + 32 < k) e[1] = get2(sh_stack, WS_STACK, stack, top + lane + 32);
             } else if (in_pos < n_in) {
-                k = min(32, n_in - in_pos);
-                if (lane < k) e = input ? input[in_pos + lane] : PH_ENTRY(a, A.root_img[in_pos + lane]);
+                k = min(64, n_in - in_pos);
+                if (input) {
+                    if (lane < k) e[0] = input[in_pos + lane];
+                    if (lane + 32 < k) e[1] = input[in_pos + lane + 32];
+                } else {
+                    if (lane < k) e[0] = PH_ENTRY(a, A.root_img[in_pos + lane]);
+                }
                 in_pos += k;
             } else {
                 break;
             }
             __syncwarp();
-            int kind = OUT_NONE;
-            int b = PH_ENTRY_ID(e), img = PH_ENTRY_IMG(e);
-            if (lane < k) {
-                const bool leaf_b = b < A.nleaf;
-                if (img == 0 && b == a) {
+            // load phase: everything both slots need, before any use
+            int b[2], img[2], need[2], npb[2];
+            float4 bh[2], bl[2], bw[2];
+#pragma unroll
+            for (int s = 0; s < 2; s++) {
+                const bool valid = lane + 32 * s < k;
+                b[s] = PH_ENTRY_ID(e[s]);
+                img[s] = PH_ENTRY_IMG(e[s]);
+                const bool leaf_b = b[s] < A.nleaf;
+                const bool self = img[s] == 0 && b[s] == a;
+                need[s] = valid && !self && !(leaf_a && leaf_b);
+                npb[s] = (valid && !self && leaf_a && leaf_b) ? g.npart[b[s]] : 0;
+                if (need[s]) {
+                    bh[s] = g.chi[b[s]];
+                    bl[s] = g.clo[b[s]];
+                    bw[s] = g.w32[b[s]];
+                }
+            }
+            int kind[2];
+#pragma unroll
+            for (int s = 0; s < 2; s++) {
+                kind[s] = OUT_NONE;
+                if (lane + 32 * s >= k) continue;
+                const int bb = b[s], im = img[s];
+                const bool leaf_b = bb < A.nleaf;
+                if (im == 0 && bb == a) {
                     if (leaf_a) {
-                        kind = OUT_P2P;
+                        kind[s] = OUT_P2P;
                         c_p2p_loc++;
                         c_pl += (unsigned long long)na * (na - 1);
                     } else {
-                        kind = OUT_SELF_PUSH;
+                        kind[s] = OUT_SELF_PUSH;
                     }
                 } else if (leaf_a && leaf_b) {
-                    kind = OUT_P2P;
-                    unsigned long long pr = (unsigned long long)na * g.npart[b];
-                    if (img == 0) { c_p2p_loc++; c_pl += pr; }
+                    kind[s] = OUT_P2P;
+                    const unsigned long long pr = (unsigned long long)na * npb[s];
+                    if (im == 0) { c_p2p_loc++; c_pl += pr; }
                     else { c_p2p_img++; c_pi += pr; }
                 } else {
                     int mi, mj, mk;
-                    image_offsets(img, mi, mj, mk);
-                    const float4 bh = g.chi[b], bl = g.clo[b], bw = g.w32[b];
-                    const float e0 = centre_diff32(bh.x, bl.x, ah.x, al.x, mi, A.Lhi, A.Llo);
-                    const float e1 = centre_diff32(bh.y, bl.y, ah.y, al.y, mj, A.Lhi, A.Llo);
-                    const float e2 = centre_diff32(bh.z, bl.z, ah.z, al.z, mk, A.Lhi, A.Llo);
-                    int flag = acceptance_fp32(aw.x, aw.y, aw.z, bw.x, bw.y, bw.z, e0, e1, e2, A.theta2f, A.c2f);
-                    double s0 = mi * A.boxsize, s1 = mj * A.boxsize, s2 = mk * A.boxsize;
+                    image_offsets(im, mi, mj, mk);
+                    const float e0 = centre_diff32(bh[s].x, bl[s].x, ah.x, al.x, mi, A.Lhi, A.Llo);
+                    const float e1 = centre_diff32(bh[s].y, bl[s].y, ah.y, al.y, mj, A.Lhi, A.Llo);
+                    const float e2 = centre_diff32(bh[s].z, bl[s].z, ah.z, al.z, mk, A.Lhi, A.Llo);
+                    int flag = acceptance_fp32(aw.x, aw.y, aw.z, bw[s].x, bw[s].y, bw[s].z, e0, e1, e2, A.theta2f,
+                                               A.c2f);
+                    const double s0 = mi * A.boxsize, s1 = mj * A.boxsize, s2 = mk * A.boxsize;
                     if (flag == -2) {
                         // image node centre = local centre + shift (src/remotes.c:123-125)
-                        double cb0 = g.cx[b], cb1 = g.cy[b], cb2 = g.cz[b];
-                        if (img) { cb0 = __dadd_rn(cb0, s0); cb1 = __dadd_rn(cb1, s1); cb2 = __dadd_rn(cb2, s2); }
-                        flag = acceptance_fp64(wa0, wa1, wa2, g.wx[b], g.wy[b], g.wz[b], __dsub_rn(ca0, cb0),
+                        double cb0 = g.cx[bb], cb1 = g.cy[bb], cb2 = g.cz[bb];
+                        if (im) { cb0 = __dadd_rn(cb0, s0); cb1 = __dadd_rn(cb1, s1); cb2 = __dadd_rn(cb2, s2); }
+                        flag = acceptance_fp64(wa0, wa1, wa2, g.wx[bb], g.wy[bb], g.wz[bb], __dsub_rn(ca0, cb0),
                                                __dsub_rn(ca1, cb1), __dsub_rn(ca2, cb2), A.theta2, A.c2);
                     }
                     // width-sum comparison of the open rule: FP32 decides unless the values tie
-                    const bool bigger_a = (aw.w != bw.w) ? (aw.w > bw.w) : (wsa > g.wsum[b]);
+                    const bool bigger_a = (aw.w != bw[s].w) ? (aw.w > bw[s].w) : (wsa > g.wsum[bb]);
+                    int kd;
                     if (flag == -1) {
-                        kind = OUT_NONE;
-                    } else if (img == 0) {
-                        if (flag == 1) kind = OUT_M2L;
-                        else if (leaf_a) kind = OUT_OPEN;
-                        else if (leaf_b) kind = OUT_PUSH;
-                        else kind = bigger_a ? OUT_PUSH : OUT_OPEN;
+                        kd = OUT_NONE;
+                    } else if (im == 0) {
+                        if (flag == 1) kd = OUT_M2L;
+                        else if (leaf_a) kd = OUT_OPEN;
+                        else if (leaf_b) kd = OUT_PUSH;
+                        else kd = bigger_a ? OUT_PUSH : OUT_OPEN;
                     } else {
-                        bool pruned = !leaf_b && image_pruned(A, b, s0, s1, s2);
-                        if (leaf_a) kind = (flag == 1 || pruned) ? OUT_M2L : OUT_OPEN;
-                        else if (flag == 1) kind = OUT_M2L;
-                        else kind = (leaf_b || pruned || bigger_a) ? OUT_PUSH : OUT_OPEN;
+                        const bool pruned = !leaf_b && image_pruned(A, bb, s0, s1, s2);
+                        if (leaf_a) kd = (flag == 1 || pruned) ? OUT_M2L : OUT_OPEN;
+                        else if (flag == 1) kd = OUT_M2L;
+                        else kd = (leaf_b || pruned || bigger_a) ? OUT_PUSH : OUT_OPEN;
                     }
-                    if (kind == OUT_M2L) {
-                        if (img == 0) c_m2l_loc++;
+                    if (kd == OUT_M2L) {
+                        if (im == 0) c_m2l_loc++;
                         else c_m2l_img++;
                     }
+                    kind[s] = kd;
                 }
             }
-            // compaction
-            unsigned mp = __ballot_sync(0xffffffffu, kind == OUT_P2P);
-            unsigned mm = __ballot_sync(0xffffffffu, kind == OUT_M2L);
-            int npush = (kind == OUT_PUSH) ? 1 : (kind == OUT_SELF_PUSH ? 2 : 0);
-            int nopen = (kind == OUT_OPEN) ? 2 : 0;
-            int push_incl = warp_incl_scan(npush);
-            int open_incl = warp_incl_scan(nopen);
-            int push_tot = shfl(push_incl, 31), open_tot = shfl(open_incl, 31);
-            if (kind == OUT_P2P) {
-                int pos = n_p2p + __popc(mp & lt);
-                if (pos < W.stage_cap) st_p2p[pos] = e;
-            } else if (kind == OUT_M2L) {
-                int pos = n_m2l + __popc(mm & lt);
-                if (pos < W.stage_cap) st_m2l[pos] = e;
-            } else if (kind == OUT_PUSH) {
-                int pos = n_pd + push_incl - 1;
-                if (pos < W.stage_cap) st_pd[pos] = e;
-            } else if (kind == OUT_SELF_PUSH) {
-                int pos = n_pd + push_incl - 2;
-                if (pos + 1 < W.stage_cap) {
-                    st_pd[pos] = PH_ENTRY(a0, 0);
-                    st_pd[pos + 1] = PH_ENTRY(a1, 0);
+            // children of opened sources, both slots
+            int2 ch[2];
+#pragma unroll
+            for (int s = 0; s < 2; s++)
+                if (kind[s] == OUT_OPEN) ch[s] = g.son[b[s]];
+            // compaction, slot 0 then slot 1
+#pragma unroll
+            for (int s = 0; s < 2; s++) {
+                const int kd = kind[s];
+                const unsigned mp = __ballot_sync(0xffffffffu, kd == OUT_P2P);
+                const unsigned mm = __ballot_sync(0xffffffffu, kd == OUT_M2L);
+                const int npush = (kd == OUT_PUSH) ? 1 : (kd == OUT_SELF_PUSH ? 2 : 0);
+                const int nopen = (kd == OUT_OPEN) ? 2 : 0;
+                const int push_incl = warp_incl_scan(npush);
+                const int open_incl = warp_incl_scan(nopen);
+                const int push_tot = shfl(push_incl, 31), open_tot = shfl(open_incl, 31);
+                if (kd == OUT_P2P) {
+                    const int pos = n_p2p + __popc(mp & lt);
+                    if (pos < W.stage_cap) put2(sh_p2p, WS_P2P, st_p2p, pos, e[s]);
+                } else if (kd == OUT_M2L) {
+                    const int pos = n_m2l + __popc(mm & lt);
+                    if (pos < W.stage_cap) put2(sh_m2l, WS_M2L, st_m2l, pos, e[s]);
+                } else if (kd == OUT_PUSH) {
+                    const int pos = n_pd + push_incl - 1;
+                    if (pos < W.stage_cap) put2(sh_pd, WS_PD, st_pd, pos, e[s]);
+                } else if (kd == OUT_SELF_PUSH) {
+                    const int pos = n_pd + push_incl - 2;
+                    if (pos + 1 < W.stage_cap) {
+                        put2(sh_pd, WS_PD, st_pd, pos, PH_ENTRY(a0, 0));
+                        put2(sh_pd, WS_PD, st_pd, pos + 1, PH_ENTRY(a1, 0));
+                    }
+                } else if (kd == OUT_OPEN) {
+                    const int pos = top + open_incl - 2;
+                    if (pos + 1 < W.stack_cap) {
+                        put2(sh_stack, WS_STACK, stack, pos, PH_ENTRY(ch[s].x, img[s]));
+                        put2(sh_stack, WS_STACK, stack, pos + 1, PH_ENTRY(ch[s].y, img[s]));
+                    }
                 }
-            } else if (kind == OUT_OPEN) {
-                int pos = top + open_incl - 2;
-                if (pos + 1 < W.stack_cap) {
-                    stack[pos] = PH_ENTRY(g.son0[b], img);
-                    stack[pos + 1] = PH_ENTRY(g.son1[b], img);
+                n_p2p += __popc(mp);
+                n_m2l += __popc(mm);
+                n_pd += push_tot;
+                top += open_tot;
+                if (top > W.stack_cap) {
+                    flags |= PH_FLAG_STACK_OVERFLOW;
+                    top = W.stack_cap;  // entries beyond were dropped; results are invalid
                 }
-            }
-            n_p2p += __popc(mp);
-            n_m2l += __popc(mm);
-            n_pd += push_tot;
-            top += open_tot;
-            if (top > W.stack_cap) {
-                flags |= PH_FLAG_STACK_OVERFLOW;
-                top = W.stack_cap;  // entries beyond were dropped; results are invalid
             }
             max_stack = max(max_stack, top);
             __syncwarp();
@@ -302,7 +366,8 @@ __global__ void __launch_bounds__(WALK_TB) k_walk_level(WalkArgs A)
             bool ok = off + n_p2p <= W.p2p_cap && n_p2p <= W.stage_cap;
             if (!ok) flags |= PH_FLAG_POOL_OVERFLOW;
             else
-                for (int i = lane; i < n_p2p; i += 32) W.p2p_pool[off + i] = st_p2p[i];
+#pragma unroll 4
+                for (int i = lane; i < n_p2p; i += 32) W.p2p_pool[off + i] = get2(sh_p2p, WS_P2P, st_p2p, i);
             if (lane == 0) { W.p2p_off[a] = ok ? off : 0; W.p2p_cnt[a] = ok ? n_p2p : 0; }
         } else {
             if (lane == 0) off = (long long)atomicAdd((unsigned long long *)&W.ctr[WC_PD_FILL0 + parity], (unsigned long long)n_pd);
@@ -310,7 +375,8 @@ __global__ void __launch_bounds__(WALK_TB) k_walk_level(WalkArgs A)
             bool ok = off + n_pd <= W.pd_cap && n_pd <= W.stage_cap;
             if (!ok) flags |= PH_FLAG_POOL_OVERFLOW;
             else
-                for (int i = lane; i < n_pd; i += 32) W.pd_pool[parity][off + i] = st_pd[i];
+#pragma unroll 4
+                for (int i = lane; i < n_pd; i += 32) W.pd_pool[parity][off + i] = get2(sh_pd, WS_PD, st_pd, i);
             if (lane == 0) { W.pd_off[a] = ok ? off : 0; W.pd_cnt[a] = ok ? n_pd : 0; }
         }
         if (lane == 0) off = (long long)atomicAdd((unsigned long long *)&W.ctr[WC_M2L_FILL], (unsigned long long)n_m2l);
@@ -319,7 +385,8 @@ __global__ void __launch_bounds__(WALK_TB) k_walk_level(WalkArgs A)
             bool ok = off + n_m2l <= W.m2l_cap && n_m2l <= W.stage_cap;
             if (!ok) flags |= PH_FLAG_POOL_OVERFLOW;
             else
-                for (int i = lane; i < n_m2l; i += 32) W.m2l_pool[off + i] = st_m2l[i];
+#pragma unroll 4
+                for (int i = lane; i < n_m2l; i += 32) W.m2l_pool[off + i] = get2(sh_m2l, WS_M2L, st_m2l, i);
             if (lane == 0) { W.m2l_off[a] = ok ? off : 0; W.m2l_cnt[a] = ok ? n_m2l : 0; }
         }
         __syncwarp();
@@ -358,9 +425,11 @@ __global__ void k_walk_level_done(WalkBufs W, int depth)
 // FP32 copies of the geometry for every unified id: centre as hi + lo,
 // widths and width sum rounded
 __global__ void k_geom32(const double *cx, const double *cy, const double *cz, const double *wx, const double *wy,
-                         const double *wz, const double *wsum, int nu, float4 *chi, float4 *clo, float4 *w32)
+                         const double *wz, const double *wsum, const int *son0, const int *son1, int nu, float4 *chi,
+                         float4 *clo, float4 *w32, int2 *son2)
 {
     for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += gridDim.x * blockDim.x) {
+        son2[u] = make_int2(son0[u], son1[u]);
         double c0 = cx[u], c1 = cy[u], c2 = cz[u];
         float h0 = (float)c0, h1 = (float)c1, h2 = (float)c2;
         chi[u] = make_float4(h0, h1, h2, 0.f);
@@ -376,7 +445,8 @@ int launch_geom32(const TreeBufs &t, int nu, cudaStream_t st)
     int blocks = (nu + 255) / 256;
     if (blocks > device_sm_count() * 8) blocks = device_sm_count() * 8;
     if (blocks < 1) blocks = 1;
-    ph::note_launch(), k_geom32<<<blocks, 256, 0, st>>>(t.cx, t.cy, t.cz, t.wx, t.wy, t.wz, t.wsum, nu, t.chi, t.clo, t.w32);
+    ph::note_launch(), k_geom32<<<blocks, 256, 0, st>>>(t.cx, t.cy, t.cz, t.wx, t.wy, t.wz, t.wsum, t.son0, t.son1, nu, t.chi,
+                                                    t.clo, t.w32, t.son2);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }
@@ -390,7 +460,7 @@ int walk_lists(WalkBufs &w, const TreeBufs &t, const TreeInfo &info, const PassP
     A.g.cx = t.cx; A.g.cy = t.cy; A.g.cz = t.cz;
     A.g.wx = t.wx; A.g.wy = t.wy; A.g.wz = t.wz; A.g.wsum = t.wsum;
     A.g.son0 = t.son0; A.g.son1 = t.son1; A.g.npart = t.npart; A.g.parent = t.parent;
-    A.g.chi = t.chi; A.g.clo = t.clo; A.g.w32 = t.w32;
+    A.g.chi = t.chi; A.g.clo = t.clo; A.g.w32 = t.w32; A.g.son = t.son2;
     A.Lhi = (float)p.boxsize;
     A.Llo = (float)(p.boxsize - (double)A.Lhi);
     A.theta2f = (float)(p.theta * p.theta);
@@ -415,7 +485,10 @@ int walk_lists(WalkBufs &w, const TreeBufs &t, const TreeInfo &info, const PassP
         if (A.list_end > A.list_begin) {
             int need = A.list_end - A.list_begin;
             int nb = (need * 32 + WALK_TB - 1) / WALK_TB;
-            ph::note_launch(), k_walk_level<<<nb < blocks ? nb : blocks, WALK_TB, 0, st>>>(A);
+            if (w.nwarps == device_sm_count() * 3 * 8)
+                ph::note_launch(), k_walk_level<3><<<nb < blocks ? nb : blocks, WALK_TB, 0, st>>>(A);
+            else
+                ph::note_launch(), k_walk_level<2><<<nb < blocks ? nb : blocks, WALK_TB, 0, st>>>(A);
         }
         ph::note_launch(), k_walk_level_done<<<1, 1, 0, st>>>(w, d);
     }
