@@ -44,7 +44,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--nside", type=int, default=256)
-    ap.add_argument("--maxleaf", type=int, default=32)
+    ap.add_argument("--maxleaf", type=int, default=0, help="0: pick by the autotuner (error <= 1e-4)")
+    ap.add_argument("--error-bound", type=float, default=1e-4)
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 GPU comparison pass")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     return ap.parse_args()
@@ -192,9 +193,15 @@ def main():
     import __graft_entry__ as g
 
     ph = g.load_package()
-    pos, p = workload(args.nside, args.maxleaf, seed_offset=rank)
+    pos, p = workload(args.nside, args.maxleaf or 16, seed_offset=rank)
     n = pos.shape[0]
     fp = ph.ForcePass(local)
+    tune = None
+    if not args.maxleaf:
+        best, table = ph.autotune_leaf(fp, pos, p, error_bound=args.error_bound)
+        p["maxleaf"] = best
+        tune = {"chosen_maxleaf": best, "error_bound_median": args.error_bound, "candidates": table,
+                "score": "fastest pass with median error vs the FP64 direct sum <= bound (2000-particle sample)"}
     stream = torch.cuda.current_stream()
     fp.set_stream(stream.cuda_stream)
     dpos = torch.from_numpy(pos).to("cuda")
@@ -323,6 +330,8 @@ def main():
         "pairs_per_particle": pairs / n,
     }
     line.update(extra)
+    if tune:
+        line["autotune"] = tune
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

@@ -302,3 +302,37 @@ class Reference:
 
     def deconstruct(self):
         self.lib.fmm_deconstruct()
+
+
+def autotune_leaf(fp, pos, p, candidates=(16, 24, 32, 48, 64), error_bound=1e-4, sample=2000, repeats=2,
+                  precision=FP32_SPLIT, seed=11):
+    """Pick MAXLEAF for this input: the fastest candidate whose median
+    relative force error against the FP64 direct sum (untruncated split
+    kernel within 2 rcut, `sample` random particles) is within
+    `error_bound`; if none qualifies, the most accurate one.
+
+    Returns (best_leaf, table) where table lists, per candidate, the pass
+    time (ms, CUDA events of the pass), pairs per particle and the median /
+    99th-percentile error."""
+    pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+    rng = np.random.default_rng(seed)
+    tgt = rng.choice(pos.shape[0], min(sample, pos.shape[0]), replace=False).astype(np.int32)
+    ref = direct_sum(pos, p, tgt)
+    nref = np.linalg.norm(ref, axis=1)
+    table = []
+    for leaf in candidates:
+        q = dict(p)
+        q["maxleaf"] = int(leaf)
+        ms = []
+        acc = None
+        for _ in range(repeats):
+            acc = fp.run(pos, q, precision=precision)
+            ms.append(fp.timings()["total"])
+        c = fp.counters()
+        err = np.linalg.norm(acc[tgt] - ref, axis=1) / np.maximum(nref, 1e-300)
+        table.append(dict(maxleaf=int(leaf), ms=float(min(ms)), median=float(np.median(err)),
+                          p99=float(np.percentile(err, 99)),
+                          pairs_per_particle=(c["pairs_local"] + c["pairs_image"]) / pos.shape[0]))
+    ok = [t for t in table if t["median"] <= error_bound]
+    best = min(ok, key=lambda t: t["ms"]) if ok else min(table, key=lambda t: t["median"])
+    return best["maxleaf"], table

@@ -244,7 +244,9 @@ int ph_validate(const photons_params *p, int n)
         return ph_set_error(PH_ERR_ARG, "invalid force parameters");
     if (p->precision != PHOTONS_FP32_SPLIT && p->precision != PHOTONS_FP64)
         return ph_set_error(PH_ERR_ARG, "unknown precision %d", p->precision);
-    if (n >= PH_MAX_UNIFIED / 2) return ph_set_error(PH_ERR_ARG, "N=%d exceeds the 2^26 particle limit", n);
+    // leaves + nodes are addressed with 27-bit ids in the lists: 2 x (2N/MAXLEAF) + 2 < 2^27
+    if (2.0 * (2.0 * n / p->maxleaf) + 2.0 >= (double)PH_MAX_UNIFIED)
+        return ph_set_error(PH_ERR_ARG, "N=%d with MAXLEAF=%d exceeds the 2^27 tree-id space", n, p->maxleaf);
     return 0;
 }
 
@@ -291,8 +293,8 @@ int ph_stage_walk(photons_ctx *c, unsigned mask)
 {
     if (!c->have_tree) return ph_set_error(PH_ERR_STATE, "no tree: run the build first");
     const int n = c->n;
-    long long p2p_cap = c->hint_p2p ? c->hint_p2p : (long long)n * 48 + 4096;
-    long long pd_cap = c->hint_pd ? c->hint_pd : (long long)n * 48 + 4096;
+    long long p2p_cap = c->hint_p2p ? c->hint_p2p : (long long)n * 32 + 4096;
+    long long pd_cap = c->hint_pd ? c->hint_pd : (long long)n * 16 + 4096;
     long long m2l_cap = c->hint_m2l ? c->hint_m2l : (long long)n * 2 + 4096;
     int stack_cap = 4096, stage_cap = 16384;
     for (int attempt = 0; attempt < 6; attempt++) {
