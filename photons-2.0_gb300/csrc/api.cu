@@ -150,6 +150,7 @@ static int alloc_tree(photons_ctx *c, int n, int cap)
         PH_TRY(dalloc(t.chi, cu)); PH_TRY(dalloc(t.clo, cu)); PH_TRY(dalloc(t.w32, cu)); PH_TRY(dalloc(t.son2, cu));
         PH_TRY(dalloc(c->M, (size_t)cu * PH_NMULTI));
         PH_TRY(dalloc(c->L, (size_t)cu * PH_NMULTI));
+        PH_TRY(dalloc(c->M32, (size_t)cu * PH_NMULTI));
         c->cap_u = cu;
     }
     if (chunks > b.cap_chunks) {
@@ -204,7 +205,7 @@ static void free_all(photons_ctx *c)
                     c->t.wz, c->t.wsum, c->t.split, c->t.depth_list, c->t.depth_off, c->w.pd_pool[0],
                     c->w.pd_pool[1], c->w.pd_off, c->w.pd_cnt, c->w.p2p_pool, c->w.p2p_off, c->w.p2p_cnt,
                     c->w.m2l_pool, c->w.m2l_off, c->w.m2l_cnt, c->w.scratch, c->w.ctr, c->pos4, c->ax, c->ay,
-                    c->az, c->M, c->L, c->io, c->work_counter, c->t.chi, c->t.clo, c->t.w32, c->t.son2};
+                    c->az, c->M, c->L, c->io, c->work_counter, c->t.chi, c->t.clo, c->t.w32, c->t.son2, c->M32};
     for (void *p : ptrs)
         if (p) cudaFree(p);
 }
@@ -378,6 +379,7 @@ static ph::MultipoleArgs multipole_args(photons_ctx *c)
     a.depth_off = c->info.depth_off.data();
     a.m2l_pool = c->w.m2l_pool; a.m2l_off = c->w.m2l_off; a.m2l_cnt = c->w.m2l_cnt;
     a.M = c->M; a.L = c->L;
+    a.chi = c->t.chi; a.clo = c->t.clo; a.pos4 = c->pos4;
     a.ax = c->ax; a.ay = c->ay; a.az = c->az;
     a.mass = c->pp.mass; a.rs = c->pp.rs; a.boxsize = c->pp.boxsize;
     return a;
@@ -393,15 +395,17 @@ int ph_stage_multipoles(photons_ctx *c)
     return 0;
 }
 
-int ph_stage_m2l(photons_ctx *c)
+int ph_stage_m2l(photons_ctx *c, int precision)
 {
     ph::MultipoleArgs a = multipole_args(c);
+    if (precision == PHOTONS_FP32_SPLIT) return ph::run_m2l_f32(a, c->M32, c->stream);
     return ph::run_m2l(a, c->stream);
 }
 
-int ph_stage_downward(photons_ctx *c)
+int ph_stage_downward(photons_ctx *c, int precision)
 {
     ph::MultipoleArgs a = multipole_args(c);
+    if (precision == PHOTONS_FP32_SPLIT) return ph::run_downward_f32(a, c->stream);
     return ph::run_downward(a, c->stream);
 }
 
@@ -476,8 +480,8 @@ extern "C" int photons_force_pass(photons_ctx *c, const photons_params *p, int n
     unsigned long long nm2l = c->ws.c[ph::WC_M2L_LOCAL] + c->ws.c[ph::WC_M2L_IMAGE];
     if (far && (nm2l > 0 || (p->flags & PHOTONS_F_MULTIPOLES))) {
         PH_TRY(ph_stage_multipoles(c));
-        PH_TRY(ph_stage_m2l(c));
-        PH_TRY(ph_stage_downward(c));
+        PH_TRY(ph_stage_m2l(c, p->precision));
+        PH_TRY(ph_stage_downward(c, p->precision));
     } else if (p->flags & PHOTONS_F_MULTIPOLES) {
         PH_TRY(ph_stage_multipoles(c));
     }

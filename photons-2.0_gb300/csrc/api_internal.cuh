@@ -35,6 +35,7 @@ struct photons_ctx {
     float4 *pos4 = nullptr;
     double *ax = nullptr, *ay = nullptr, *az = nullptr;
     double *M = nullptr, *L = nullptr;
+    float *M32 = nullptr;  // multipoles rounded to FP32 for the split M2L
     double *io = nullptr;  // 3*cap_n staging for host transfers and gathers
     int *work_counter = nullptr;
     int cap_n = 0, cap_u = 0;
@@ -60,8 +61,8 @@ int ph_stage_build(photons_ctx *c, const photons_params *p, int n, const double 
 int ph_stage_walk(photons_ctx *c, unsigned mask);
 int ph_stage_p2p(photons_ctx *c, int precision, int zero);
 int ph_stage_multipoles(photons_ctx *c);
-int ph_stage_m2l(photons_ctx *c);
-int ph_stage_downward(photons_ctx *c);
+int ph_stage_m2l(photons_ctx *c, int precision);
+int ph_stage_downward(photons_ctx *c, int precision);
 int ph_stage_output(photons_ctx *c, double *acc, int device_io, int tree_order);
 int ph_download_tree(photons_ctx *c, HostTree &h, bool with_expansions);
 

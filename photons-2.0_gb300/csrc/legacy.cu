@@ -218,8 +218,8 @@ static void interact(unsigned mask, bool downward)
     if (ph_stage_walk(c, mask)) fatal("walk");
     if (ph_stage_p2p(c, p.precision, 1)) fatal("p2p");
     unsigned long long nm2l = c->ws.c[ph::WC_M2L_LOCAL] + c->ws.c[ph::WC_M2L_IMAGE];
-    if (nm2l && ph_stage_m2l(c)) fatal("m2l");
-    if (downward && ph_stage_downward(c)) fatal("l2l/l2p");
+    if (nm2l && ph_stage_m2l(c, p.precision)) fatal("m2l");
+    if (downward && ph_stage_downward(c, p.precision)) fatal("l2l/l2p");
     if (ph_stage_output(c, g_stage.data(), 0, 1)) fatal("download");
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) { ph_set_error(PH_ERR_CUDA, "stream"); fatal("sync"); }
     for (int i = 0; i < NPART; i++)

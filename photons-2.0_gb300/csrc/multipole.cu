@@ -13,6 +13,7 @@
 
 #include "fmm_context.cuh"
 #include "multipole.cuh"
+#include "split_kernel_coeffs.h"
 
 #define MP_TB 128
 
@@ -260,6 +261,151 @@ __global__ void k_l2p(const double *px, const double *py, const double *pz, cons
     }
 }
 
+// ---------------- split-precision far field ----------------
+// M2L in FP32: centre differences from the FP32 hi/lo centres (the side
+// near the far face takes off the box length, so the subtraction is
+// exact), multipoles rounded to FP32, radial factors from
+// erfc(u) = exp(-u^2) t P(t) (the fit of fit_split_kernel.py), L
+// accumulated per target in FP32 and added to the FP64 expansion.
+__device__ __forceinline__ float rsqrt_f(float x) { float y; asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x)); return y; }
+__device__ __forceinline__ float rcp_f(float x) { float y; asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x)); return y; }
+__device__ __forceinline__ float ex2_f(float x) { float y; asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x)); return y; }
+
+struct FarConsts {
+    float a, pa, Lhi, Llo;
+    float c[SPLIT_NA];
+};
+
+__device__ __forceinline__ float cdiff(float ht, float lt, float hs, float ls, int o, float Lhi, float Llo)
+{
+    // (c_t) - (c_s + shift)
+    if (o > 0) { ht -= Lhi; lt -= Llo; }
+    else if (o < 0) { hs -= Lhi; ls -= Llo; }
+    return (ht - hs) + (lt - ls);
+}
+
+__device__ __forceinline__ void m2l_add_f32(float dx, float dy, float dz, const float *Ms, const FarConsts &F,
+                                            float *L)
+{
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    const float ir = rsqrt_f(r2);
+    const float r = r2 * ir;
+    const float a = F.a, a2 = a * a;
+    const float u = a * r;
+    const float E = ex2_f(-u * u * 1.44269504f);
+    const float t = rcp_f(fmaf(F.pa, r, 1.0f));
+    float P = F.c[SPLIT_NA - 1];
+#pragma unroll
+    for (int k = SPLIT_NA - 2; k >= 0; k--) P = fmaf(P, t, F.c[k]);
+    const float er = E * t * P;
+    const float ce = 1.12837917f * E;
+    const float ir2 = ir * ir;
+    float f[4];
+    f[0] = er * ir;
+    f[1] = -er * ir * ir2 - ce * a * ir2;
+    f[2] = 3.0f * er * ir * ir2 * ir2 + ce * (3.0f * a * ir2 * ir2 + 2.0f * a * a2 * ir2);
+    f[3] = -15.0f * er * ir * ir2 * ir2 * ir2 - ce * (15.0f * a * ir2 * ir2 * ir2 + 10.0f * a * a2 * ir2 * ir2 +
+                                                      4.0f * a * a2 * a2 * ir2);
+    const float x[3] = {dx, dy, dz};
+    float pw[3][4];
+#pragma unroll
+    for (int d = 0; d < 3; d++) { pw[d][0] = 1.0f; pw[d][1] = x[d]; pw[d][2] = x[d] * x[d]; pw[d][3] = x[d] * x[d] * x[d]; }
+    float D[PH_NMULTI];
+#pragma unroll
+    for (int g = 0; g < PH_NMULTI; g++) {
+        const int e0 = h_mi.e[g][0], e1 = h_mi.e[g][1], e2 = h_mi.e[g][2], k = h_mi.ord[g];
+        float v = f[k] * pw[0][e0] * pw[1][e1] * pw[2][e2];
+        if (k >= 2) {
+            if (e0 >= 2) v += f[k - 1] * (float)(e0 * (e0 - 1) / 2) * pw[0][e0 - 2] * pw[1][e1] * pw[2][e2];
+            if (e1 >= 2) v += f[k - 1] * (float)(e1 * (e1 - 1) / 2) * pw[0][e0] * pw[1][e1 - 2] * pw[2][e2];
+            if (e2 >= 2) v += f[k - 1] * (float)(e2 * (e2 - 1) / 2) * pw[0][e0] * pw[1][e1] * pw[2][e2 - 2];
+        }
+        D[g] = v;
+    }
+#pragma unroll
+    for (int b = 0; b < PH_NMULTI; b++) {
+        float acc = 0.0f;
+#pragma unroll
+        for (int aa = 0; aa < PH_NMULTI; aa++) {
+            if (h_mi.ord[aa] + h_mi.ord[b] > 3) continue;
+            acc = fmaf(Ms[aa], D[h_mi.idx[h_mi.e[aa][0] + h_mi.e[b][0]][h_mi.e[aa][1] + h_mi.e[b][1]]
+                                       [h_mi.e[aa][2] + h_mi.e[b][2]]], acc);
+        }
+        L[b] += acc;
+    }
+}
+
+__global__ void k_m_to_f32(const double *M, float *M32, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        M32[i] = (float)M[i];
+}
+
+__global__ void k_m2l_f32(int nunified, const uint32_t *pool, const long long *off, const int *cnt, const float4 *chi,
+                          const float4 *clo, const float *M32, double *Lout, FarConsts F)
+{
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nunified; u += gridDim.x * blockDim.x) {
+        const int n = cnt[u];
+        if (n == 0) continue;
+        float L[PH_NMULTI];
+#pragma unroll
+        for (int a = 0; a < PH_NMULTI; a++) L[a] = 0.0f;
+        const float4 th = chi[u], tl = clo[u];
+        const long long o = off[u];
+        for (int k = 0; k < n; k++) {
+            const uint32_t e = pool[o + k];
+            const int s = PH_ENTRY_ID(e), img = PH_ENTRY_IMG(e);
+            int mi, mj, mk;
+            image_offsets(img, mi, mj, mk);
+            const float4 sh = chi[s], sl = clo[s];
+            const float dx = cdiff(th.x, tl.x, sh.x, sl.x, mi, F.Lhi, F.Llo);
+            const float dy = cdiff(th.y, tl.y, sh.y, sl.y, mj, F.Lhi, F.Llo);
+            const float dz = cdiff(th.z, tl.z, sh.z, sl.z, mk, F.Lhi, F.Llo);
+            float Ms[PH_NMULTI];
+#pragma unroll
+            for (int a = 0; a < PH_NMULTI; a++) Ms[a] = M32[(size_t)s * PH_NMULTI + a];
+            m2l_add_f32(dx, dy, dz, Ms, F, L);
+        }
+#pragma unroll
+        for (int a = 0; a < PH_NMULTI; a++) Lout[(size_t)u * PH_NMULTI + a] += (double)L[a];
+    }
+}
+
+// L2P in FP32 on the leaf-centre offsets, added to the FP64 accelerations
+__global__ void k_l2p_f32(const float4 *pos4, const int *ipart, const int *npart, int nleaf, const double *L,
+                          double *ax, double *ay, double *az)
+{
+    const int lane = warp_lane();
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    for (int l = gw; l < nleaf; l += nw) {
+        const int ip = ipart[l], np = npart[l];
+        float Ll[PH_NMULTI];
+#pragma unroll
+        for (int a = 0; a < PH_NMULTI; a++) Ll[a] = (float)L[(size_t)l * PH_NMULTI + a];
+        for (int j = lane; j < np; j += 32) {
+            const float4 o = pos4[ip + j];
+            const float px[4] = {1.f, o.x, o.x * o.x, 0.f}, py[4] = {1.f, o.y, o.y * o.y, 0.f},
+                        pz[4] = {1.f, o.z, o.z * o.z, 0.f};
+            float F[3];
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                float acc = 0.0f;
+#pragma unroll
+                for (int g = 0; g < PH_NMULTI; g++) {
+                    if (h_mi.ord[g] > 2) continue;
+                    const int e0 = h_mi.e[g][0] + (i == 0), e1 = h_mi.e[g][1] + (i == 1), e2 = h_mi.e[g][2] + (i == 2);
+                    const float mono = px[h_mi.e[g][0]] * py[h_mi.e[g][1]] * pz[h_mi.e[g][2]] * (float)h_mi.invf[g];
+                    acc = fmaf(Ll[h_mi.idx[e0][e1][e2]], mono, acc);
+                }
+                F[i] = acc;
+            }
+            ax[ip + j] += F[0];
+            ay[ip + j] += F[1];
+            az[ip + j] += F[2];
+        }
+    }
+}
+
 inline int grid_for(long long n, int tpb)
 {
     long long g = (n + tpb - 1) / tpb;
@@ -288,6 +434,37 @@ int run_downward(const MultipoleArgs &a, cudaStream_t st)
     }
     ph::note_launch(), k_l2p<<<grid_for((long long)a.nleaf * 32, 256), 256, 0, st>>>(a.px, a.py, a.pz, a.ipart, a.npart, a.cx, a.cy,
                                                                   a.cz, a.nleaf, a.L, a.ax, a.ay, a.az);
+    PH_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
+int run_m2l_f32(const MultipoleArgs &a, float *M32, cudaStream_t st)
+{
+    const long long nm = (long long)a.nunified * PH_NMULTI;
+    ph::note_launch(), k_m_to_f32<<<grid_for(nm, 256), 256, 0, st>>>(a.M, M32, nm);
+    FarConsts F;
+    const double ia = 0.5 / a.rs;
+    F.a = (float)ia;
+    F.pa = (float)(SPLIT_P * ia);
+    F.Lhi = (float)a.boxsize;
+    F.Llo = (float)(a.boxsize - (double)F.Lhi);
+    for (int i = 0; i < SPLIT_NA; i++) F.c[i] = (float)SPLIT_A[i];
+    ph::note_launch(), k_m2l_f32<<<grid_for(a.nunified, MP_TB), MP_TB, 0, st>>>(a.nunified, a.m2l_pool, a.m2l_off, a.m2l_cnt,
+                                                                               a.chi, a.clo, M32, a.L, F);
+    PH_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
+int run_downward_f32(const MultipoleArgs &a, cudaStream_t st)
+{
+    for (int d = 1; d < a.ndepth; d++) {
+        int b = a.depth_off[d], e = a.depth_off[d + 1];
+        if (e > b)
+            ph::note_launch(), k_l2l_depth<<<grid_for(e - b, MP_TB), MP_TB, 0, st>>>(a.depth_list, b, e, a.parent, a.cx, a.cy,
+                                                                                  a.cz, a.L);
+    }
+    ph::note_launch(), k_l2p_f32<<<grid_for((long long)a.nleaf * 32, 256), 256, 0, st>>>(a.pos4, a.ipart, a.npart, a.nleaf,
+                                                                                       a.L, a.ax, a.ay, a.az);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }

@@ -16,6 +16,7 @@ struct MultipoleArgs {
     const long long *m2l_off;
     const int *m2l_cnt;
     double *M, *L;  // [nunified][20]
+    const float4 *chi, *clo, *pos4;  // FP32 centres (hi + lo) and leaf offsets, for the split far field
     double *ax, *ay, *az;
     double mass, rs, boxsize;
 };
@@ -24,6 +25,9 @@ struct MultipoleArgs {
 int run_m2l(const MultipoleArgs &a, cudaStream_t st);
 // L2L top-down, then L2P accumulated into ax/ay/az
 int run_downward(const MultipoleArgs &a, cudaStream_t st);
+// split precision: FP32 M2L (M rounded into M32) and FP32 L2P after FP64 L2L
+int run_m2l_f32(const MultipoleArgs &a, float *M32, cudaStream_t st);
+int run_downward_f32(const MultipoleArgs &a, cudaStream_t st);
 // P2M and M2M only (multipoles for callers that read them)
 int run_p2m_m2m(const MultipoleArgs &a, cudaStream_t st);
 // op: 0 m2l (in = M, inout = L, rs), 1 m2m (in = M, inout = M'), 2 l2l (in = L, inout = L')

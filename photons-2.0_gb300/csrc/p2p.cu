@@ -259,6 +259,60 @@ __device__ __forceinline__ void p2p_round(const float2 *__restrict__ X2, const f
     rz = az.x + az.y;
 }
 
+// two targets of equal stream layout in one sweep over the stage: each
+// source pair is loaded once and feeds two independent dependency chains
+__device__ __forceinline__ void p2p_round_dual(const float2 *__restrict__ X2, const float2 *__restrict__ Y2,
+                                               const float2 *__restrict__ Z2, int npairs, int k, int G, float4 oA,
+                                               float4 oB, const SplitConsts &K, float &rAx, float &rAy, float &rAz,
+                                               float &rBx, float &rBy, float &rBz)
+{
+    const float2 kq2 = f2(K.kq), pia2 = f2(K.pia), clin2 = f2(K.clin), one2 = f2(1.0f);
+    const float2 a0 = f2(K.a[0]), a1 = f2(K.a[1]), a2 = f2(K.a[2]), a3 = f2(K.a[3]), a4 = f2(K.a[4]),
+                 a5 = f2(K.a[5]);
+    const float2 nAx = f2(-oA.x), nAy = f2(-oA.y), nAz = f2(-oA.z);
+    const float2 nBx = f2(-oB.x), nBy = f2(-oB.y), nBz = f2(-oB.z);
+    float2 ax = f2(0.f), ay = f2(0.f), az = f2(0.f), bx = f2(0.f), by = f2(0.f), bz = f2(0.f);
+    for (int pp = k; pp < npairs; pp += G) {
+        const float2 X = X2[pp], Y = Y2[pp], Z = Z2[pp];
+#pragma unroll
+        for (int w = 0; w < 2; w++) {
+            const float2 dx = __fadd2_rn(X, w ? nBx : nAx);
+            const float2 dy = __fadd2_rn(Y, w ? nBy : nAy);
+            const float2 dz = __fadd2_rn(Z, w ? nBz : nAz);
+            float2 qq = __fmul2_rn(dx, dx);
+            qq = __ffma2_rn(dy, dy, qq);
+            qq = __ffma2_rn(dz, dz, qq);
+            qq.x = fmaxf(qq.x, K.eps2);
+            qq.y = fmaxf(qq.y, K.eps2);
+            const float2 rinv = make_float2(rsqrt_approx(qq.x), rsqrt_approx(qq.y));
+            const float2 r = __fmul2_rn(qq, rinv);
+            const float2 den = __ffma2_rn(pia2, r, one2);
+            const float2 tt = make_float2(rcp_approx(den.x), rcp_approx(den.y));
+            float2 P = __ffma2_rn(a5, tt, a4);
+            P = __ffma2_rn(P, tt, a3);
+            P = __ffma2_rn(P, tt, a2);
+            P = __ffma2_rn(P, tt, a1);
+            P = __ffma2_rn(P, tt, a0);
+            const float2 h = __ffma2_rn(tt, P, __fmul2_rn(clin2, r));
+            const float2 ea = __fmul2_rn(qq, kq2);
+            const float2 ex = make_float2(ex2_approx(ea.x), ex2_approx(ea.y));
+            const float2 rinv2 = __fmul2_rn(rinv, rinv);
+            const float2 f = __fmul2_rn(__fmul2_rn(ex, h), __fmul2_rn(rinv2, rinv));
+            if (w) {
+                bx = __ffma2_rn(dx, f, bx);
+                by = __ffma2_rn(dy, f, by);
+                bz = __ffma2_rn(dz, f, bz);
+            } else {
+                ax = __ffma2_rn(dx, f, ax);
+                ay = __ffma2_rn(dy, f, ay);
+                az = __ffma2_rn(dz, f, az);
+            }
+        }
+    }
+    rAx = ax.x + ax.y; rAy = ay.x + ay.y; rAz = az.x + az.y;
+    rBx = bx.x + bx.y; rBy = by.x + by.y; rBz = bz.x + bz.y;
+}
+
 // centre difference (c_s + shift) - c_t per axis from hi/lo parts
 __device__ __forceinline__ float centre_diff(float hs, float ls, float ht, float lt, int o, float Lhi, float Llo)
 {
@@ -364,6 +418,20 @@ __global__ void __launch_bounds__(P2P_TB, 3) k_p2p_split_packed(P2PArgs A)
                 __syncwarp();
                 const int npairs = (nstaged + 1) >> 1;
                 float px, py, pz;
+                if (m2 == m1) {
+                    // equal rounds (a block of 2m targets): one sweep for both
+                    float qx, qy, qz;
+                    p2p_round_dual(X2, Y2, Z2, npairs, k1, G1, o1, o2, K, px, py, pz, qx, qy, qz);
+                    kahan_add(s1x, c1x, px);
+                    kahan_add(s1y, c1y, py);
+                    kahan_add(s1z, c1z, pz);
+                    kahan_add(s2x, c2x, qx);
+                    kahan_add(s2y, c2y, qy);
+                    kahan_add(s2z, c2z, qz);
+                    __syncwarp();
+                    e += nfit;
+                    continue;
+                }
                 p2p_round(X2, Y2, Z2, npairs, k1, G1, o1.x, o1.y, o1.z, K, px, py, pz);
                 kahan_add(s1x, c1x, px);
                 kahan_add(s1y, c1y, py);

@@ -138,3 +138,16 @@ def test_too_few_particles_is_an_error(ph, fp):
     p = dict(boxsize=1.0, theta=0.5, rs=0.1, rcut=0.45, eps=0.01, mass=1.0, maxleaf=8)
     with pytest.raises(ph.PhotonsError, match="error 5"):
         fp.run(pos, p)
+
+
+@pytest.mark.parametrize("nside,maxleaf", [(32, 8), (40, 16)])
+def test_fp32_split_precision_clustered(ph, fp, ics, nside, maxleaf):
+    """Clustered input with many M2L tasks: the split far field (FP32 M2L
+    and L2P) stays within the precision budget of the FP64 pass."""
+    pos, p = ics.make("nfw128", nside=nside, maxleaf=maxleaf)
+    a64 = fp.run(pos, p, precision=ph.FP64)
+    assert fp.counters()["walk_m2l_count"] > 1000
+    a32 = fp.run(pos, p, precision=ph.FP32_SPLIT)
+    e = rel_err(a32, a64, p)
+    assert np.median(e) <= 2e-6, np.median(e)
+    assert np.percentile(e, 99) <= 2e-5, np.percentile(e, 99)
