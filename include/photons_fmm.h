@@ -137,6 +137,24 @@ int photons_op_batch(int op, int n, const double *d, const double *in, double *i
 int photons_direct_sum(const photons_params *p, int n, const double *pos, int nt, const int *targets,
                        double rmax, double *acc);
 
+/* The same FP64 direct sum, allocating nothing (no cudaMalloc, cudaFree or
+   allocating library call).  It has no counterpart in the reference.  It is
+   for callers that cannot allocate device memory mid-run: a run that has
+   budgeted all of HBM up front (particles, PM mesh, force-pass pools), where
+   a cudaMalloc between steps fails, or whose other streams must not be
+   stalled by the device-wide synchronisation of cudaMalloc/cudaFree.
+   pos[3n], targets[nt] and acc[3nt] are DEVICE pointers (host pointers are
+   rejected).  At most 262144 sources and 65536 targets; larger sizes return
+   error 1 with a message.  Scratch is one fixed array of about 10.8 MB per
+   device, held from the library's load until the process exits.  The first
+   call on a device looks up that array's address (with the device current);
+   make that first call before any stream capture.  All calls share the
+   array, so calls that overlap on the GPU (other streams or host threads)
+   race.  Runs on cuda_stream (NULL: the default stream) and returns after
+   that stream has finished the call's work. */
+int photons_direct_sum_noalloc(const photons_params *p, int n, const double *pos, int nt, const int *targets,
+                               double rmax, double *acc, void *cuda_stream);
+
 /* kernels launched by this library so far (all contexts) */
 unsigned long long photons_launch_count(void);
 

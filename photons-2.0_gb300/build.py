@@ -18,7 +18,7 @@ LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libphotons_fmm.so")
 INCLUDE = os.path.join(ROOT, "include")
 
-SOURCES = ["scan.cu", "tree.cu", "walk.cu", "p2p.cu", "multipole.cu", "api.cu", "legacy.cu", "direct.cu"]
+SOURCES = ["scan.cu", "tree.cu", "walk.cu", "p2p.cu", "multipole.cu", "api.cu", "legacy.cu", "direct.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=default",
          "-I" + INCLUDE, "-I" + CSRC, "-diag-suppress", "177"]
