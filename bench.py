@@ -314,7 +314,7 @@ def main():
                    "eps": p["eps"], "precision": "fp32-split (fp64 positions and centre differences)",
                    "l2": "inputs larger than L2 (positions %.0f MB), no flush" % (n * 24 / 1e6),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "roofline": {"bound": "fp32", "kernel": "k_p2p_split", "achieved": achieved, "peak": peak,
+        "roofline": {"bound": "fp32", "kernel": "k_p2p_split_packed", "achieved": achieved, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                      "peak_source": "FFMA probe measured in this run (MEASURED_PEAKS.json holds no FP32 figure)",
                      "work": "%d flops/pair x %d pairs per launch" % (FLOPS_PER_PAIR, pairs),

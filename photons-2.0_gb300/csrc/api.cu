@@ -106,6 +106,7 @@ static int alloc_particles(photons_ctx *c, int n)
     PH_TRY(dalloc(c->pos4, n));
     PH_TRY(dalloc(c->ax, n)); PH_TRY(dalloc(c->ay, n)); PH_TRY(dalloc(c->az, n));
     PH_TRY(dalloc(c->io, (size_t)3 * n));
+    c->epoch++;
     b.cap_n = n;
     c->cap_n = n;
     return 0;
@@ -128,6 +129,9 @@ static int alloc_tree(photons_ctx *c, int n, int cap)
         b.scan_scratch_elems = ph::scan_scratch_elems(cap > chunks ? cap : chunks) + 8;
         PH_TRY(dalloc(b.scan_scratch, b.scan_scratch_elems));
         PH_TRY(dalloc(b.cnt, ph::BC_NCOUNTERS));
+        PH_TRY(dalloc(b.lvl_begin, MAX_DEPTH_CAP + 2)); PH_TRY(dalloc(b.lvl_count, MAX_DEPTH_CAP + 2));
+        PH_TRY(dalloc(b.leaf_begin, MAX_DEPTH_CAP + 2)); PH_TRY(dalloc(b.leaf_count, MAX_DEPTH_CAP + 2));
+        c->epoch++;
         b.cap_nodes = cap;
         b.cap_leaves = cap;
         // unified tree
@@ -140,6 +144,7 @@ static int alloc_tree(photons_ctx *c, int n, int cap)
         PH_TRY(dalloc(t.wsum, cu)); PH_TRY(dalloc(t.split, cu));
         PH_TRY(dalloc(t.depth_list, cu));
         PH_TRY(dalloc(t.depth_off, MAX_DEPTH_CAP + 2));
+        PH_TRY(dalloc(t.depth_cnt, MAX_DEPTH_CAP + 2));
         t.max_depth_cap = MAX_DEPTH_CAP;
         t.cap_u = cu;
         // per-unified walk bookkeeping and expansions
@@ -156,11 +161,13 @@ static int alloc_tree(photons_ctx *c, int n, int cap)
     if (chunks > b.cap_chunks) {
         PH_TRY(dalloc(b.ch_partial, chunks)); PH_TRY(dalloc(b.ch_cnt, chunks)); PH_TRY(dalloc(b.ch_small_base, chunks));
         PH_TRY(dalloc(b.ch_node, chunks));
+        c->epoch++;
         b.cap_chunks = chunks;
         size_t need = ph::scan_scratch_elems(cap > chunks ? cap : chunks) + 8;
         if (need > b.scan_scratch_elems) {
             b.scan_scratch_elems = need;
             PH_TRY(dalloc(b.scan_scratch, need));
+            c->epoch++;
         }
     }
     return 0;
@@ -170,15 +177,16 @@ static int alloc_walk(photons_ctx *c, long long p2p_cap, long long pd_cap, long 
                       int stage_cap)
 {
     ph::WalkBufs &w = c->w;
-    if (!w.ctr) PH_TRY(dalloc(w.ctr, ph::WC_N));
-    if (!c->work_counter) PH_TRY(dalloc(c->work_counter, 4));
-    if (p2p_cap > w.p2p_cap) { PH_TRY(dalloc(w.p2p_pool, p2p_cap)); w.p2p_cap = p2p_cap; }
+    if (!w.ctr) { PH_TRY(dalloc(w.ctr, ph::WC_N)); c->epoch++; }
+    if (!c->work_counter) { PH_TRY(dalloc(c->work_counter, 4)); c->epoch++; }
+    if (p2p_cap > w.p2p_cap) { PH_TRY(dalloc(w.p2p_pool, p2p_cap)); w.p2p_cap = p2p_cap; c->epoch++; }
     if (pd_cap > w.pd_cap) {
         PH_TRY(dalloc(w.pd_pool[0], pd_cap));
         PH_TRY(dalloc(w.pd_pool[1], pd_cap));
         w.pd_cap = pd_cap;
+        c->epoch++;
     }
-    if (m2l_cap > w.m2l_cap) { PH_TRY(dalloc(w.m2l_pool, m2l_cap)); w.m2l_cap = m2l_cap; }
+    if (m2l_cap > w.m2l_cap) { PH_TRY(dalloc(w.m2l_pool, m2l_cap)); w.m2l_cap = m2l_cap; c->epoch++; }
     // resident 256-thread walk blocks per SM: 2 (no register spills) or 3
     const char *wb = getenv("PHOTONS_WALK_BLOCKS");
     int nwarps = ph::device_sm_count() * ((wb && atoi(wb) == 3) ? 3 : 2) * 8;
@@ -186,6 +194,7 @@ static int alloc_walk(photons_ctx *c, long long p2p_cap, long long pd_cap, long 
         if (stack_cap < w.stack_cap) stack_cap = w.stack_cap;
         if (stage_cap < w.stage_cap) stage_cap = w.stage_cap;
         PH_TRY(dalloc(w.scratch, (size_t)nwarps * (stack_cap + 3 * (size_t)stage_cap)));
+        c->epoch++;
         w.stack_cap = stack_cap;
         w.stage_cap = stage_cap;
         w.nwarps = nwarps;
@@ -205,7 +214,8 @@ static void free_all(photons_ctx *c)
                     c->t.wz, c->t.wsum, c->t.split, c->t.depth_list, c->t.depth_off, c->w.pd_pool[0],
                     c->w.pd_pool[1], c->w.pd_off, c->w.pd_cnt, c->w.p2p_pool, c->w.p2p_off, c->w.p2p_cnt,
                     c->w.m2l_pool, c->w.m2l_off, c->w.m2l_cnt, c->w.scratch, c->w.ctr, c->pos4, c->ax, c->ay,
-                    c->az, c->M, c->L, c->io, c->work_counter, c->t.chi, c->t.clo, c->t.w32, c->t.son2, c->M32};
+                    c->az, c->M, c->L, c->io, c->work_counter, c->t.chi, c->t.clo, c->t.w32, c->t.son2, c->M32,
+                    b.lvl_begin, b.lvl_count, b.leaf_begin, b.leaf_count, c->t.depth_cnt};
     for (void *p : ptrs)
         if (p) cudaFree(p);
 }
@@ -227,6 +237,13 @@ __global__ void k_gather_out(const int *perm, const double *ax, const double *ay
 }
 
 }  // namespace
+
+// FP32 P2P kernel: 0 packed pairs (default), 1 scalar (PHOTONS_P2P_KERNEL=scalar)
+static int p2p_variant()
+{
+    const char *v = getenv("PHOTONS_P2P_KERNEL");
+    return (v && !strcmp(v, "scalar")) ? 1 : 0;
+}
 
 // ------------------------------------------------------------------
 // stages
@@ -251,7 +268,29 @@ int ph_validate(const photons_params *p, int n)
     return 0;
 }
 
-int ph_stage_build(photons_ctx *c, const photons_params *p, int n, const double *pos, int device_io)
+// events inside a captured pass become event-record nodes of the graph
+static int ph_record(photons_ctx *c, int ev)
+{
+    PH_CUDA_CHECK(cudaEventRecordWithFlags(c->ev[ev], c->stream,
+                                           c->capturing ? cudaEventRecordExternal : cudaEventRecordDefault));
+    return 0;
+}
+
+// node levels to launch for a context's first pass: mean splits roughly
+// halve the count per level; clustered sets go deeper (PH_FLAG_DEPTH grows
+// it).  PHOTONS_TREE_LEVELS sets the starting count instead.
+static int estimate_levels(int n, int maxleaf)
+{
+    const char *e = getenv("PHOTONS_TREE_LEVELS");
+    if (e && atoi(e) > 0) return atoi(e) < MAX_DEPTH_CAP - 1 ? atoi(e) : MAX_DEPTH_CAP - 1;
+    int lv = 1;
+    while (lv < 60 && (double)n / std::ldexp(1.0, lv) > (double)maxleaf) lv++;
+    lv += 8;
+    return lv < MAX_DEPTH_CAP - 1 ? lv : MAX_DEPTH_CAP - 1;
+}
+
+// validation, capacities and parameters of a pass over n particles
+static int ph_prepare(photons_ctx *c, const photons_params *p, int n)
 {
     PH_TRY(ph_validate(p, n));
     int cap = (int)(2.0 * ((double)n) / ((double)p->maxleaf));  // src/fmm.c:203-209
@@ -269,65 +308,148 @@ int ph_stage_build(photons_ctx *c, const photons_params *p, int n, const double 
     c->pp.maxleaf = p->maxleaf;
     c->pp.images = 1;
     c->n = n;
+    c->info.nleaf_cap = c->info.nnode_cap = cap;
     c->have_tree = c->have_lists = c->have_multipoles = false;
+    return 0;
+}
+
+// tree build from device positions src (enqueue only)
+static int ph_enqueue_tree(photons_ctx *c, const double *src, int levels)
+{
+    cudaStream_t st = c->stream;
+    PH_TRY(ph::launch_init_particles(c->b, src, c->n, st));
+    PH_TRY(ph::build_tree(c->b, c->t, c->pp, c->n, levels, st));
+    PH_TRY(ph::launch_geom32(c->t, c->b.cnt, st));
+    PH_TRY(ph::launch_leaf_offsets(c->b, c->t, c->pos4, st));
+    c->ndepth = levels + 1;
+    return ph_record(c, EV_TREE);
+}
+
+// build flags after the stream has finished: capacity overflow is an error
+// of the reference's rule; PH_FLAG_DEPTH asks for more levels
+static int ph_check_build(photons_ctx *c, int flags, int levels, int *grow)
+{
+    *grow = 0;
+    if (flags & PH_FLAG_LEAF_CAPACITY)
+        return ph_set_error(PH_ERR_CAPACITY, "leaf capacity 2N/MAXLEAF=%d exceeded by the mean-split tree", c->b.rule_cap);
+    if (flags & PH_FLAG_NODE_CAPACITY)
+        return ph_set_error(PH_ERR_CAPACITY, "node capacity 2N/MAXLEAF=%d exceeded by the mean-split tree", c->b.rule_cap);
+    if (flags & PH_FLAG_DEPTH) {
+        if (levels >= MAX_DEPTH_CAP - 1) return ph_set_error(PH_ERR_DEPTH, "tree deeper than %d levels", MAX_DEPTH_CAP - 1);
+        *grow = levels * 2 < MAX_DEPTH_CAP - 1 ? levels * 2 : MAX_DEPTH_CAP - 1;
+    }
+    return 0;
+}
+
+static void ph_tree_info_from(photons_ctx *c, const int *h, int levels)
+{
+    c->info.nleaf = h[ph::BC_LEAVES];
+    c->info.nnode = h[ph::BC_NODES];
+    c->info.depth = h[ph::BC_DEPTH];
+    c->info.levels = h[ph::BC_NLEVELS];
+    c->info.flags = h[ph::BC_FLAGS];
+    // keep the launch count while it covers the tree with a small margin,
+    // so repeated passes over similar trees reuse one captured graph
+    const int lv = c->info.levels;
+    if (levels < lv + 1 || levels > lv + 6) c->hint_levels = lv + 3;
+    else c->hint_levels = levels;
+}
+
+int ph_stage_build(photons_ctx *c, const photons_params *p, int n, const double *pos, int device_io)
+{
+    PH_TRY(ph_prepare(c, p, n));
     cudaStream_t st = c->stream;
     const double *src = pos;
-    PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_START], st));
+    PH_TRY(ph_record(c, EV_START));
     if (!device_io) {
         PH_CUDA_CHECK(cudaMemcpyAsync(c->io, pos, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, st));
         src = c->io;
     }
-    PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_UPLOADED], st));
-    PH_TRY(ph::launch_init_particles(c->b, src, n, st));
-    ph::TreeInfo info;
-    info.nleaf_cap = info.nnode_cap = cap;
-    PH_TRY(ph::build_tree(c->b, c->t, c->pp, n, st, info, nullptr));
-    c->info = info;
-    PH_TRY(ph::launch_geom32(c->t, info.nleaf + info.nnode, st));
-    PH_TRY(ph::launch_leaf_offsets(c->b, c->t, info.nleaf, c->pos4, st));
-    PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_TREE], st));
+    PH_TRY(ph_record(c, EV_UPLOADED));
+    int levels = c->hint_levels ? c->hint_levels : estimate_levels(n, p->maxleaf);
+    for (;;) {
+        PH_TRY(ph_enqueue_tree(c, src, levels));
+        PH_CUDA_CHECK(cudaStreamSynchronize(st));
+        ph::TreeInfo info = c->info;
+        PH_TRY(ph::read_tree_info(c->b, c->t, levels, info));
+        int grow = 0;
+        PH_TRY(ph_check_build(c, info.flags, levels, &grow));
+        if (grow) { levels = grow; continue; }
+        c->info.depth_off = info.depth_off;
+        int h[ph::BC_NCOUNTERS] = {0};
+        h[ph::BC_LEAVES] = info.nleaf;
+        h[ph::BC_NODES] = info.nnode;
+        h[ph::BC_DEPTH] = info.depth;
+        h[ph::BC_NLEVELS] = info.levels;
+        h[ph::BC_FLAGS] = info.flags;
+        ph_tree_info_from(c, h, levels);
+        c->ndepth = info.depth + 1;
+        break;
+    }
     c->have_tree = true;
     return 0;
+}
+
+// list-pool sizes after an overflowed walk
+static void grow_walk_caps(photons_ctx *c, unsigned long long fl, long long &p2p_cap, long long &pd_cap,
+                           long long &m2l_cap, int &stack_cap, int &stage_cap)
+{
+    const unsigned long long *w = c->ws.c;
+    if (fl & PH_FLAG_POOL_OVERFLOW) {
+        long long need = (long long)w[ph::WC_P2P_FILL];
+        if (need > c->w.p2p_cap) p2p_cap = need + need / 8 + 4096;
+        need = (long long)w[ph::WC_PD_MAX];
+        long long cur = (long long)w[ph::WC_PD_FILL0];
+        if ((long long)w[ph::WC_PD_FILL1] > cur) cur = (long long)w[ph::WC_PD_FILL1];
+        if (cur > need) need = cur;
+        if (need > c->w.pd_cap) pd_cap = need + need / 8 + 4096;
+        need = (long long)w[ph::WC_M2L_FILL];
+        if (need > c->w.m2l_cap) m2l_cap = need + need / 8 + 4096;
+    }
+    if (fl & PH_FLAG_STACK_OVERFLOW) stack_cap = c->w.stack_cap * 4;
+    if (fl & PH_FLAG_STAGE_OVERFLOW) {
+        long long need = (long long)w[ph::WC_MAX_STAGE];
+        stage_cap = (int)(need > 2LL * c->w.stage_cap ? need + 1024 : 2LL * c->w.stage_cap);
+    }
+}
+
+static void walk_caps(photons_ctx *c, long long &p2p_cap, long long &pd_cap, long long &m2l_cap, int &stack_cap,
+                      int &stage_cap)
+{
+    const long long n = c->n;
+    p2p_cap = c->hint_p2p ? c->hint_p2p : n * 32 + 4096;
+    pd_cap = c->hint_pd ? c->hint_pd : n * 16 + 4096;
+    m2l_cap = c->hint_m2l ? c->hint_m2l : n * 2 + 4096;
+    stack_cap = c->w.stack_cap ? c->w.stack_cap : 4096;
+    stage_cap = c->w.stage_cap ? c->w.stage_cap : 16384;
+}
+
+static void keep_walk_hints(photons_ctx *c, long long p2p_cap, long long pd_cap, long long m2l_cap)
+{
+    c->hint_p2p = p2p_cap;
+    c->hint_pd = pd_cap;
+    c->hint_m2l = m2l_cap;
 }
 
 int ph_stage_walk(photons_ctx *c, unsigned mask)
 {
     if (!c->have_tree) return ph_set_error(PH_ERR_STATE, "no tree: run the build first");
-    const int n = c->n;
-    long long p2p_cap = c->hint_p2p ? c->hint_p2p : (long long)n * 32 + 4096;
-    long long pd_cap = c->hint_pd ? c->hint_pd : (long long)n * 16 + 4096;
-    long long m2l_cap = c->hint_m2l ? c->hint_m2l : (long long)n * 2 + 4096;
-    int stack_cap = 4096, stage_cap = 16384;
+    long long p2p_cap, pd_cap, m2l_cap;
+    int stack_cap, stage_cap;
+    walk_caps(c, p2p_cap, pd_cap, m2l_cap, stack_cap, stage_cap);
     for (int attempt = 0; attempt < 6; attempt++) {
         PH_TRY(alloc_walk(c, p2p_cap, pd_cap, m2l_cap, stack_cap, stage_cap));
-        PH_TRY(ph::walk_lists(c->w, c->t, c->info, c->pp, mask, c->stream, c->ws));
+        PH_TRY(ph::walk_lists(c->w, c->t, c->b.cnt, c->ndepth, c->pp, mask, c->stream));
+        PH_CUDA_CHECK(cudaMemcpyAsync(c->ws.c, c->w.ctr, sizeof(c->ws.c), cudaMemcpyDeviceToHost, c->stream));
+        PH_CUDA_CHECK(cudaStreamSynchronize(c->stream));
         unsigned long long fl = c->ws.c[ph::WC_FLAGS];
         if (!fl) {
             c->have_lists = true;
             c->mask = mask;
-            // keep the sizes as hints so a repeated pass allocates once
-            c->hint_p2p = p2p_cap;
-            c->hint_pd = pd_cap;
-            c->hint_m2l = m2l_cap;
-            PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_WALK], c->stream));
-            return 0;
+            keep_walk_hints(c, p2p_cap, pd_cap, m2l_cap);  // a repeated pass allocates once
+            return ph_record(c, EV_WALK);
         }
-        if (fl & PH_FLAG_POOL_OVERFLOW) {
-            long long need = (long long)c->ws.c[ph::WC_P2P_FILL];
-            if (need > c->w.p2p_cap) p2p_cap = need + need / 8 + 4096;
-            need = (long long)c->ws.c[ph::WC_PD_MAX];
-            long long cur = (long long)c->ws.c[ph::WC_PD_FILL0];
-            if ((long long)c->ws.c[ph::WC_PD_FILL1] > cur) cur = (long long)c->ws.c[ph::WC_PD_FILL1];
-            if (cur > need) need = cur;
-            if (need > c->w.pd_cap) pd_cap = need + need / 8 + 4096;
-            need = (long long)c->ws.c[ph::WC_M2L_FILL];
-            if (need > c->w.m2l_cap) m2l_cap = need + need / 8 + 4096;
-        }
-        if (fl & PH_FLAG_STACK_OVERFLOW) stack_cap = c->w.stack_cap * 4;
-        if (fl & PH_FLAG_STAGE_OVERFLOW) {
-            long long need = (long long)c->ws.c[ph::WC_MAX_STAGE];
-            stage_cap = (int)(need > 2LL * c->w.stage_cap ? need + 1024 : 2LL * c->w.stage_cap);
-        }
+        grow_walk_caps(c, fl, p2p_cap, pd_cap, m2l_cap, stack_cap, stage_cap);
     }
     return ph_set_error(PH_ERR_CAPACITY, "interaction lists did not fit after repeated growth");
 }
@@ -345,7 +467,8 @@ int ph_stage_p2p(photons_ctx *c, int precision, int zero)
     memset(&a, 0, sizeof a);
     a.ipart = c->t.ipart; a.npart = c->t.npart;
     a.cx = c->t.cx; a.cy = c->t.cy; a.cz = c->t.cz;
-    a.nleaf = c->info.nleaf;
+    a.tree_cnt = c->b.cnt;
+    a.walk_flags = c->w.ctr + ph::WC_FLAGS;
     a.p2p_pool = c->w.p2p_pool; a.p2p_off = c->w.p2p_off; a.p2p_cnt = c->w.p2p_cnt;
     a.pos4 = c->pos4;
     a.chi = c->t.chi;
@@ -355,14 +478,10 @@ int ph_stage_p2p(photons_ctx *c, int precision, int zero)
     a.work_counter = c->work_counter;
     a.boxsize = c->pp.boxsize; a.eps = c->pp.eps; a.mass = c->pp.mass; a.rs = c->pp.rs;
     a.k = ph::make_split_consts(c->pp);
-    {
-        const char *v = getenv("PHOTONS_P2P_KERNEL");
-        a.variant = (v && !strcmp(v, "scalar")) ? 1 : 0;
-    }
-    PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_P2P_BEGIN], st));
+    a.variant = p2p_variant();
+    PH_TRY(ph_record(c, EV_P2P_BEGIN));
     PH_TRY(ph::launch_p2p(a, precision == PHOTONS_FP64, st));
-    PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_P2P], st));
-    return 0;
+    return ph_record(c, EV_P2P);
 }
 
 static ph::MultipoleArgs multipole_args(photons_ctx *c)
@@ -372,11 +491,11 @@ static ph::MultipoleArgs multipole_args(photons_ctx *c)
     a.px = c->b.x; a.py = c->b.y; a.pz = c->b.z;
     a.ipart = c->t.ipart; a.npart = c->t.npart; a.son0 = c->t.son0; a.son1 = c->t.son1; a.parent = c->t.parent;
     a.cx = c->t.cx; a.cy = c->t.cy; a.cz = c->t.cz;
-    a.nleaf = c->info.nleaf;
-    a.nunified = c->info.nleaf + c->info.nnode;
-    a.ndepth = c->info.depth + 1;
+    a.tree_cnt = c->b.cnt;
+    a.walk_flags = c->w.ctr + ph::WC_FLAGS;
+    a.ndepth = c->ndepth;
     a.depth_list = c->t.depth_list;
-    a.depth_off = c->info.depth_off.data();
+    a.depth_off = c->t.depth_off;
     a.m2l_pool = c->w.m2l_pool; a.m2l_off = c->w.m2l_off; a.m2l_cnt = c->w.m2l_cnt;
     a.M = c->M; a.L = c->L;
     a.chi = c->t.chi; a.clo = c->t.clo; a.pos4 = c->pos4;
@@ -389,8 +508,6 @@ int ph_stage_multipoles(photons_ctx *c)
 {
     ph::MultipoleArgs a = multipole_args(c);
     PH_TRY(ph::run_p2m_m2m(a, c->stream));
-    size_t nu = (size_t)(c->info.nleaf + c->info.nnode);
-    PH_CUDA_CHECK(cudaMemsetAsync(c->L, 0, sizeof(double) * PH_NMULTI * nu, c->stream));
     c->have_multipoles = true;
     return 0;
 }
@@ -409,19 +526,149 @@ int ph_stage_downward(photons_ctx *c, int precision)
     return ph::run_downward(a, c->stream);
 }
 
+// accelerations from tree order into dst (input order unless tree_order)
+static int ph_enqueue_gather(photons_ctx *c, double *dst, int tree_order)
+{
+    int blocks = ph::device_sm_count() * 8;
+    ph::note_launch(), k_gather_out<<<blocks, 256, 0, c->stream>>>(c->b.perm, c->ax, c->ay, c->az, c->n, dst,
+                                                                    tree_order);
+    PH_CUDA_CHECK(cudaGetLastError());
+    return ph_record(c, EV_GATHERED);
+}
+
 int ph_stage_output(photons_ctx *c, double *acc, int device_io, int tree_order)
 {
-    cudaStream_t st = c->stream;
-    const int n = c->n;
-    double *dst = device_io ? acc : c->io;
-    int blocks = ph::device_sm_count() * 8;
-    ph::note_launch(), k_gather_out<<<blocks, 256, 0, st>>>(c->b.perm, c->ax, c->ay, c->az, n, dst, tree_order);
-    PH_CUDA_CHECK(cudaGetLastError());
-    PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_GATHERED], st));
+    PH_TRY(ph_enqueue_gather(c, device_io ? acc : c->io, tree_order));
     if (!device_io)
-        PH_CUDA_CHECK(cudaMemcpyAsync(acc, c->io, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost, st));
-    PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_END], st));
-    return 0;
+        PH_CUDA_CHECK(cudaMemcpyAsync(acc, c->io, sizeof(double) * 3 * (size_t)c->n, cudaMemcpyDeviceToHost,
+                                      c->stream));
+    return ph_record(c, EV_END);
+}
+
+// ------------------------------------------------------------------
+// the whole pass as one CUDA graph
+// ------------------------------------------------------------------
+static PassKey pass_key(photons_ctx *c, const photons_params *p, int n, const double *pos, double *acc, int dio,
+                        int levels, unsigned mask)
+{
+    PassKey k;
+    memset(&k, 0, sizeof k);
+    k.n = n; k.levels = levels; k.maxleaf = p->maxleaf; k.precision = p->precision; k.flags = p->flags;
+    k.dio = dio; k.variant = p2p_variant(); k.nwarps = c->w.nwarps; k.mask = mask;
+    k.boxsize = p->boxsize; k.theta = p->theta; k.rs = p->rs; k.rcut = p->rcut; k.eps = p->eps; k.mass = p->mass;
+    k.pos = dio ? (const void *)pos : nullptr;
+    k.acc = dio ? (const void *)acc : nullptr;
+    k.stream = c->stream;
+    k.epoch = c->epoch;
+    return k;
+}
+
+// device part of a pass: positions already in src, accelerations to dst
+static int ph_enqueue_pass(photons_ctx *c, const photons_params *p, const double *src, double *dst, int levels,
+                           unsigned mask)
+{
+    PH_TRY(ph_enqueue_tree(c, src, levels));
+    PH_TRY(ph::walk_lists(c->w, c->t, c->b.cnt, c->ndepth, c->pp, mask, c->stream));
+    PH_TRY(ph_record(c, EV_WALK));
+    PH_TRY(ph_stage_p2p(c, p->precision, 1));
+    const bool far = !(p->flags & PHOTONS_F_NO_FARFIELD);
+    if (far) {
+        PH_TRY(ph_stage_multipoles(c));
+        PH_TRY(ph_stage_m2l(c, p->precision));
+        PH_TRY(ph_stage_downward(c, p->precision));
+    } else if (p->flags & PHOTONS_F_MULTIPOLES) {
+        PH_TRY(ph_stage_multipoles(c));
+    }
+    PH_TRY(ph_record(c, EV_FAR));
+    return ph_enqueue_gather(c, dst, p->flags & PHOTONS_F_TREE_ORDER);
+}
+
+static void drop_graph(photons_ctx *c)
+{
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+    c->have_key = false;
+}
+
+static int capture_pass(photons_ctx *c, const photons_params *p, const double *src, double *dst, int levels,
+                        unsigned mask)
+{
+    drop_graph(c);
+    cudaStream_t st = c->stream;
+    PH_CUDA_CHECK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    c->capturing = true;
+    // kernels are counted when the graph runs, not when it is captured
+    const unsigned long long launches_before = ph::g_launches;
+    int rc = ph_enqueue_pass(c, p, src, dst, levels, mask);
+    c->graph_kernels = ph::g_launches - launches_before;
+    ph::g_launches = launches_before;
+    c->capturing = false;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (!rc && e != cudaSuccess) rc = ph_set_cuda_error(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+    if (!rc) {
+        e = cudaGraphInstantiate(&c->gexec, g, 0);
+        if (e != cudaSuccess) {
+            c->gexec = nullptr;
+            rc = ph_set_cuda_error(e, "cudaGraphInstantiate", __FILE__, __LINE__);
+        }
+    }
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return rc;
+}
+
+static int force_pass_graph(photons_ctx *c, const photons_params *p, int n, const double *pos, double *acc, int dio,
+                            unsigned mask)
+{
+    PH_TRY(ph_prepare(c, p, n));
+    cudaStream_t st = c->stream;
+    int levels = c->hint_levels ? c->hint_levels : estimate_levels(n, p->maxleaf);
+    long long p2p_cap, pd_cap, m2l_cap;
+    int stack_cap, stage_cap;
+    walk_caps(c, p2p_cap, pd_cap, m2l_cap, stack_cap, stage_cap);
+    const double *src = dio ? pos : c->io;
+    double *dst = dio ? acc : c->io;
+    for (int attempt = 0; attempt < 16; attempt++) {
+        PH_TRY(alloc_walk(c, p2p_cap, pd_cap, m2l_cap, stack_cap, stage_cap));
+        PassKey k = pass_key(c, p, n, pos, acc, dio, levels, mask);
+        if (!c->gexec || !c->have_key || memcmp(&k, &c->key, sizeof k) != 0) {
+            PH_TRY(capture_pass(c, p, src, dst, levels, mask));
+            c->key = k;
+            c->have_key = true;
+        }
+        PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_START], st));
+        if (!dio) PH_CUDA_CHECK(cudaMemcpyAsync(c->io, pos, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, st));
+        PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_UPLOADED], st));
+        PH_CUDA_CHECK(cudaGraphLaunch(c->gexec, st));
+        ph::g_launches += c->graph_kernels;
+        if (!dio) PH_CUDA_CHECK(cudaMemcpyAsync(acc, c->io, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost, st));
+        PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_END], st));
+        int h[ph::BC_NCOUNTERS];
+        PH_CUDA_CHECK(cudaMemcpyAsync(h, c->b.cnt, sizeof h, cudaMemcpyDeviceToHost, st));
+        PH_CUDA_CHECK(cudaMemcpyAsync(c->ws.c, c->w.ctr, sizeof(c->ws.c), cudaMemcpyDeviceToHost, st));
+        c->info.depth_off.resize(levels + 2);
+        PH_CUDA_CHECK(cudaMemcpyAsync(c->info.depth_off.data(), c->t.depth_off, sizeof(int) * (levels + 2),
+                                      cudaMemcpyDeviceToHost, st));
+        PH_CUDA_CHECK(cudaStreamSynchronize(st));
+        int grow = 0;
+        PH_TRY(ph_check_build(c, h[ph::BC_FLAGS], levels, &grow));
+        if (grow) { levels = grow; continue; }
+        ph_tree_info_from(c, h, levels);
+        c->have_tree = true;
+        unsigned long long fl = c->ws.c[ph::WC_FLAGS];
+        if (fl) {
+            grow_walk_caps(c, fl, p2p_cap, pd_cap, m2l_cap, stack_cap, stage_cap);
+            continue;
+        }
+        c->info.depth_off.resize(c->info.depth + 2);
+        c->have_lists = true;
+        c->mask = mask;
+        c->have_multipoles = !(p->flags & PHOTONS_F_NO_FARFIELD) || (p->flags & PHOTONS_F_MULTIPOLES);
+        keep_walk_hints(c, p2p_cap, pd_cap, m2l_cap);
+        return 0;
+    }
+    return ph_set_error(PH_ERR_CAPACITY, "force pass did not fit after repeated growth");
 }
 
 // ------------------------------------------------------------------
@@ -452,6 +699,7 @@ extern "C" void photons_destroy(photons_ctx *c)
     if (!c) return;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
     free_all(c);
     for (int i = 0; i < EV_COUNT; i++) cudaEventDestroy(c->ev[i]);
     cudaStreamDestroy(c->own_stream);
@@ -470,24 +718,31 @@ extern "C" int photons_force_pass(photons_ctx *c, const photons_params *p, int n
     photons_gpu_clear_error();
     if (!c) return ph_set_error(PH_ERR_ARG, "null context");
     if (!pos || !acc) return ph_set_error(PH_ERR_ARG, "null particle arrays");
+    if (!p) return ph_set_error(PH_ERR_ARG, "null parameters");
     cudaSetDevice(c->device);
-    const int dio = p && (p->flags & PHOTONS_F_DEVICE_IO);
-    PH_TRY(ph_stage_build(c, p, n, pos, dio));
-    unsigned mask = p->image_mask ? p->image_mask : ((1u << PH_NIMG) - 1u);
-    PH_TRY(ph_stage_walk(c, mask));
-    PH_TRY(ph_stage_p2p(c, p->precision, 1));
-    bool far = !(p->flags & PHOTONS_F_NO_FARFIELD);
-    unsigned long long nm2l = c->ws.c[ph::WC_M2L_LOCAL] + c->ws.c[ph::WC_M2L_IMAGE];
-    if (far && (nm2l > 0 || (p->flags & PHOTONS_F_MULTIPOLES))) {
-        PH_TRY(ph_stage_multipoles(c));
-        PH_TRY(ph_stage_m2l(c, p->precision));
-        PH_TRY(ph_stage_downward(c, p->precision));
-    } else if (p->flags & PHOTONS_F_MULTIPOLES) {
-        PH_TRY(ph_stage_multipoles(c));
+    const int dio = p->flags & PHOTONS_F_DEVICE_IO;
+    const unsigned mask = p->image_mask ? p->image_mask : ((1u << PH_NIMG) - 1u);
+    const char *g = getenv("PHOTONS_GRAPH");
+    if (!(g && !strcmp(g, "0"))) {
+        PH_TRY(force_pass_graph(c, p, n, pos, acc, dio, mask));
+    } else {
+        // stage by stage, with the host checking the build and the walk
+        PH_TRY(ph_stage_build(c, p, n, pos, dio));
+        PH_TRY(ph_stage_walk(c, mask));
+        PH_TRY(ph_stage_p2p(c, p->precision, 1));
+        const bool far = !(p->flags & PHOTONS_F_NO_FARFIELD);
+        const unsigned long long nm2l = c->ws.c[ph::WC_M2L_LOCAL] + c->ws.c[ph::WC_M2L_IMAGE];
+        if (far && (nm2l > 0 || (p->flags & PHOTONS_F_MULTIPOLES))) {
+            PH_TRY(ph_stage_multipoles(c));
+            PH_TRY(ph_stage_m2l(c, p->precision));
+            PH_TRY(ph_stage_downward(c, p->precision));
+        } else if (p->flags & PHOTONS_F_MULTIPOLES) {
+            PH_TRY(ph_stage_multipoles(c));
+        }
+        PH_TRY(ph_record(c, EV_FAR));
+        PH_TRY(ph_stage_output(c, acc, dio, p->flags & PHOTONS_F_TREE_ORDER));
+        PH_CUDA_CHECK(cudaStreamSynchronize(c->stream));
     }
-    PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_FAR], c->stream));
-    PH_TRY(ph_stage_output(c, acc, dio, p->flags & PHOTONS_F_TREE_ORDER));
-    PH_CUDA_CHECK(cudaStreamSynchronize(c->stream));
     c->last_flags = p->flags;
     c->precision = p->precision;
     return 0;

@@ -25,6 +25,17 @@ enum {
     EV_START = 0, EV_UPLOADED, EV_TREE, EV_WALK, EV_P2P_BEGIN, EV_P2P, EV_FAR, EV_GATHERED, EV_END, EV_COUNT
 };
 
+// Everything a captured pass bakes in; a pass with a different key is
+// captured anew.  Zero-filled before use so it compares with memcmp.
+struct PassKey {
+    int n, levels, maxleaf, precision, flags, dio, variant, nwarps;
+    unsigned mask;
+    double boxsize, theta, rs, rcut, eps, mass;
+    const void *pos, *acc;
+    cudaStream_t stream;
+    unsigned long long epoch;
+};
+
 struct photons_ctx {
     int device = 0;
     cudaStream_t own_stream = nullptr, stream = nullptr;
@@ -48,6 +59,14 @@ struct photons_ctx {
     int last_flags = 0, precision = 0;
     bool have_tree = false, have_lists = false, have_multipoles = false;
     long long hint_p2p = 0, hint_pd = 0, hint_m2l = 0;
+    int hint_levels = 0;  // node levels to launch (0: estimate from N)
+    int ndepth = 0;       // depths the walk and far field launch
+    unsigned long long epoch = 0;  // bumped by every device (re)allocation
+    // the captured pass
+    bool capturing = false, have_key = false;
+    cudaGraphExec_t gexec = nullptr;
+    unsigned long long graph_kernels = 0;  // kernel nodes of gexec
+    PassKey key{};
 };
 
 struct HostTree {

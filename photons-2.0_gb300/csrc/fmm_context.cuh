@@ -33,6 +33,8 @@ struct BuildBufs {
     int *ch_cnt = nullptr, *ch_small_base = nullptr, *ch_node = nullptr;
     // small device counters
     int *cnt = nullptr;  // see BuildCounter
+    int *lvl_begin = nullptr, *lvl_count = nullptr;    // per node level: first temp node, count
+    int *leaf_begin = nullptr, *leaf_count = nullptr;  // per depth: temp leaves created by the level above
     int *scan_scratch = nullptr;
     size_t scan_scratch_elems = 0;
     int cap_nodes = 0, cap_leaves = 0, cap_chunks = 0, cap_n = 0;
@@ -47,7 +49,11 @@ enum BuildCounter {
     BC_NEW_LEAVES = 3,    // leaf children created by the current level
     BC_LEAVES = 4,        // temp leaves so far
     BC_FLAGS = 5,
-    BC_NCOUNTERS = 8
+    BC_LEVEL_BEGIN = 6,   // first temp node of the current level
+    BC_NODES = 7,         // temp nodes in total (after the build)
+    BC_NLEVELS = 8,       // node levels built
+    BC_DEPTH = 9,         // deepest depth holding a node or leaf
+    BC_NCOUNTERS = 12
 };
 
 // Final tree in unified index space (leaves then nodes).
@@ -69,6 +75,7 @@ struct TreeBufs {
 
 struct TreeInfo {
     int nleaf = 0, nnode = 0, depth = 0;  // depth = deepest level index
+    int levels = 0, flags = 0;
     int nleaf_cap = 0, nnode_cap = 0;      // the reference's 2N/MAXLEAF capacity
     std::vector<int> depth_off;            // host copy of TreeBufs::depth_off
 };
@@ -105,12 +112,15 @@ struct WalkStats {
     unsigned long long c[WC_N];
 };
 
-int launch_geom32(const TreeBufs &t, int nu, cudaStream_t st);
-// image_mask: bit 0 the local tree, bit k the k-th periodic image
-int walk_lists(WalkBufs &w, const TreeBufs &t, const TreeInfo &info, const PassParams &p, unsigned image_mask,
-               cudaStream_t st, WalkStats &stats);
+// Everything below only enqueues work on st; tree sizes are read on the
+// device from tree_cnt (the build counters, BuildBufs::cnt).
+int launch_geom32(const TreeBufs &t, const int *tree_cnt, cudaStream_t st);
+// image_mask: bit 0 the local tree, bit k the k-th periodic image;
+// ndepth = depths to launch (at least the tree's deepest + 1)
+int walk_lists(WalkBufs &w, const TreeBufs &t, const int *tree_cnt, int ndepth, const PassParams &p,
+               unsigned image_mask, cudaStream_t st);
 
-int build_tree(BuildBufs &b, TreeBufs &t, const PassParams &p, int n, cudaStream_t st, TreeInfo &info,
-               double *t_ms_phase);
+int build_tree(BuildBufs &b, TreeBufs &t, const PassParams &p, int n, int levels, cudaStream_t st);
+int read_tree_info(const BuildBufs &b, const TreeBufs &t, int levels, TreeInfo &info);
 
 }  // namespace ph

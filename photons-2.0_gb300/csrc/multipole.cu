@@ -62,8 +62,9 @@ __device__ __forceinline__ void scaled_monomials(double dx, double dy, double dz
 
 // ---------------- P2M ----------------
 __global__ void k_p2m(const double *px, const double *py, const double *pz, const int *ipart, const int *npart,
-                      const double *cx, const double *cy, const double *cz, int nleaf, double mass, double *M)
+                      const double *cx, const double *cy, const double *cz, const int *tree_cnt, double mass, double *M)
 {
+    const int nleaf = tree_cnt[BC_LEAVES];
     for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < nleaf; l += gridDim.x * blockDim.x) {
         double acc[PH_NMULTI];
 #pragma unroll
@@ -100,9 +101,10 @@ __device__ __forceinline__ void m2m_add(double dx, double dy, double dz, const d
     }
 }
 
-__global__ void k_m2m_depth(const int *list, int begin, int end, int nleaf, const int *son0, const int *son1,
-                            const double *cx, const double *cy, const double *cz, double *M)
+__global__ void k_m2m_depth(const int *list, const int *depth_off, int d, const int *tree_cnt, const int *son0,
+                            const int *son1, const double *cx, const double *cy, const double *cz, double *M)
 {
+    const int begin = depth_off[d], end = depth_off[d + 1], nleaf = tree_cnt[BC_LEAVES];
     for (int i = begin + blockIdx.x * blockDim.x + threadIdx.x; i < end; i += gridDim.x * blockDim.x) {
         int u = list[i];
         if (u < nleaf) continue;
@@ -171,9 +173,11 @@ __device__ __forceinline__ void m2l_add(double dx, double dy, double dz, const d
     }
 }
 
-__global__ void k_m2l(int nunified, const uint32_t *pool, const long long *off, const int *cnt, const double *cx,
-                      const double *cy, const double *cz, const double *M, double *Lout, double rs, double boxsize)
+__global__ void k_m2l(const int *tree_cnt, const unsigned long long *walk_flags, const uint32_t *pool,
+                      const long long *off, const int *cnt, const double *cx, const double *cy, const double *cz,
+                      const double *M, double *Lout, double rs, double boxsize)
 {
+    const int nunified = *walk_flags ? 0 : tree_cnt[BC_LEAVES] + tree_cnt[BC_NODES];
     for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nunified; u += gridDim.x * blockDim.x) {
         int n = cnt[u];
         if (n == 0) continue;
@@ -202,9 +206,10 @@ __global__ void k_m2l(int nunified, const uint32_t *pool, const long long *off, 
 }
 
 // ---------------- L2L (one depth: each member adds its parent's expansion) ----------------
-__global__ void k_l2l_depth(const int *list, int begin, int end, const int *parent, const double *cx,
+__global__ void k_l2l_depth(const int *list, const int *depth_off, int d, const int *parent, const double *cx,
                             const double *cy, const double *cz, double *L)
 {
+    const int begin = depth_off[d], end = depth_off[d + 1];
     for (int i = begin + blockIdx.x * blockDim.x + threadIdx.x; i < end; i += gridDim.x * blockDim.x) {
         int u = list[i];
         int p = parent[u];
@@ -230,9 +235,10 @@ __global__ void k_l2l_depth(const int *list, int begin, int end, const int *pare
 
 // ---------------- L2P ----------------
 __global__ void k_l2p(const double *px, const double *py, const double *pz, const int *ipart, const int *npart,
-                      const double *cx, const double *cy, const double *cz, int nleaf, const double *L, double *ax,
-                      double *ay, double *az)
+                      const double *cx, const double *cy, const double *cz, const int *tree_cnt, const double *L,
+                      double *ax, double *ay, double *az)
 {
+    const int nleaf = tree_cnt[BC_LEAVES];
     int lane = warp_lane();
     int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
     for (int l = gw; l < nleaf; l += nw) {
@@ -335,15 +341,18 @@ __device__ __forceinline__ void m2l_add_f32(float dx, float dy, float dz, const 
     }
 }
 
-__global__ void k_m_to_f32(const double *M, float *M32, long long n)
+__global__ void k_m_to_f32(const double *M, float *M32, const int *tree_cnt)
 {
+    const long long n = (long long)(tree_cnt[BC_LEAVES] + tree_cnt[BC_NODES]) * PH_NMULTI;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
         M32[i] = (float)M[i];
 }
 
-__global__ void k_m2l_f32(int nunified, const uint32_t *pool, const long long *off, const int *cnt, const float4 *chi,
-                          const float4 *clo, const float *M32, double *Lout, FarConsts F)
+__global__ void k_m2l_f32(const int *tree_cnt, const unsigned long long *walk_flags, const uint32_t *pool,
+                          const long long *off, const int *cnt, const float4 *chi, const float4 *clo, const float *M32,
+                          double *Lout, FarConsts F)
 {
+    const int nunified = *walk_flags ? 0 : tree_cnt[BC_LEAVES] + tree_cnt[BC_NODES];
     for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nunified; u += gridDim.x * blockDim.x) {
         const int n = cnt[u];
         if (n == 0) continue;
@@ -372,9 +381,10 @@ __global__ void k_m2l_f32(int nunified, const uint32_t *pool, const long long *o
 }
 
 // L2P in FP32 on the leaf-centre offsets, added to the FP64 accelerations
-__global__ void k_l2p_f32(const float4 *pos4, const int *ipart, const int *npart, int nleaf, const double *L,
-                          double *ax, double *ay, double *az)
+__global__ void k_l2p_f32(const float4 *pos4, const int *ipart, const int *npart, const int *tree_cnt,
+                          const double *L, double *ax, double *ay, double *az)
 {
+    const int nleaf = tree_cnt[BC_LEAVES];
     const int lane = warp_lane();
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
     for (int l = gw; l < nleaf; l += nw) {
@@ -406,42 +416,54 @@ __global__ void k_l2p_f32(const float4 *pos4, const int *ipart, const int *npart
     }
 }
 
+// zero the local expansions of every unified id
+__global__ void k_zero_L(double *L, const int *tree_cnt)
+{
+    const long long n = (long long)(tree_cnt[BC_LEAVES] + tree_cnt[BC_NODES]) * PH_NMULTI;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        L[i] = 0.0;
+}
+
+inline int grid_cap() { return device_sm_count() * 16; }
+
 inline int grid_for(long long n, int tpb)
 {
     long long g = (n + tpb - 1) / tpb;
-    long long cap = (long long)device_sm_count() * 16;
     if (g < 1) g = 1;
-    return (int)(g < cap ? g : cap);
+    return (int)(g < grid_cap() ? g : grid_cap());
 }
 
 }  // namespace
 
+// All launches below read the tree sizes and depth slices on the device;
+// depths past the tree's deepest have empty slices.
 int run_m2l(const MultipoleArgs &a, cudaStream_t st)
 {
-    ph::note_launch(), k_m2l<<<grid_for(a.nunified, MP_TB), MP_TB, 0, st>>>(a.nunified, a.m2l_pool, a.m2l_off, a.m2l_cnt, a.cx, a.cy,
-                                                         a.cz, a.M, a.L, a.rs, a.boxsize);
+    ph::note_launch(), k_m2l<<<grid_cap(), MP_TB, 0, st>>>(a.tree_cnt, a.walk_flags, a.m2l_pool, a.m2l_off, a.m2l_cnt,
+                                                             a.cx, a.cy, a.cz, a.M, a.L, a.rs, a.boxsize);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }
 
+static void launch_l2l(const MultipoleArgs &a, cudaStream_t st)
+{
+    for (int d = 1; d < a.ndepth; d++)
+        ph::note_launch(), k_l2l_depth<<<grid_cap(), MP_TB, 0, st>>>(a.depth_list, a.depth_off, d, a.parent, a.cx, a.cy,
+                                                                       a.cz, a.L);
+}
+
 int run_downward(const MultipoleArgs &a, cudaStream_t st)
 {
-    for (int d = 1; d < a.ndepth; d++) {
-        int b = a.depth_off[d], e = a.depth_off[d + 1];
-        if (e > b)
-            ph::note_launch(), k_l2l_depth<<<grid_for(e - b, MP_TB), MP_TB, 0, st>>>(a.depth_list, b, e, a.parent, a.cx, a.cy, a.cz,
-                                                                  a.L);
-    }
-    ph::note_launch(), k_l2p<<<grid_for((long long)a.nleaf * 32, 256), 256, 0, st>>>(a.px, a.py, a.pz, a.ipart, a.npart, a.cx, a.cy,
-                                                                  a.cz, a.nleaf, a.L, a.ax, a.ay, a.az);
+    launch_l2l(a, st);
+    ph::note_launch(), k_l2p<<<grid_cap(), 256, 0, st>>>(a.px, a.py, a.pz, a.ipart, a.npart, a.cx, a.cy, a.cz,
+                                                           a.tree_cnt, a.L, a.ax, a.ay, a.az);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }
 
 int run_m2l_f32(const MultipoleArgs &a, float *M32, cudaStream_t st)
 {
-    const long long nm = (long long)a.nunified * PH_NMULTI;
-    ph::note_launch(), k_m_to_f32<<<grid_for(nm, 256), 256, 0, st>>>(a.M, M32, nm);
+    ph::note_launch(), k_m_to_f32<<<grid_cap(), 256, 0, st>>>(a.M, M32, a.tree_cnt);
     FarConsts F;
     const double ia = 0.5 / a.rs;
     F.a = (float)ia;
@@ -449,36 +471,29 @@ int run_m2l_f32(const MultipoleArgs &a, float *M32, cudaStream_t st)
     F.Lhi = (float)a.boxsize;
     F.Llo = (float)(a.boxsize - (double)F.Lhi);
     for (int i = 0; i < SPLIT_NA; i++) F.c[i] = (float)SPLIT_A[i];
-    ph::note_launch(), k_m2l_f32<<<grid_for(a.nunified, MP_TB), MP_TB, 0, st>>>(a.nunified, a.m2l_pool, a.m2l_off, a.m2l_cnt,
-                                                                               a.chi, a.clo, M32, a.L, F);
+    ph::note_launch(), k_m2l_f32<<<grid_cap(), MP_TB, 0, st>>>(a.tree_cnt, a.walk_flags, a.m2l_pool, a.m2l_off,
+                                                                 a.m2l_cnt, a.chi, a.clo, M32, a.L, F);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }
 
 int run_downward_f32(const MultipoleArgs &a, cudaStream_t st)
 {
-    for (int d = 1; d < a.ndepth; d++) {
-        int b = a.depth_off[d], e = a.depth_off[d + 1];
-        if (e > b)
-            ph::note_launch(), k_l2l_depth<<<grid_for(e - b, MP_TB), MP_TB, 0, st>>>(a.depth_list, b, e, a.parent, a.cx, a.cy,
-                                                                                  a.cz, a.L);
-    }
-    ph::note_launch(), k_l2p_f32<<<grid_for((long long)a.nleaf * 32, 256), 256, 0, st>>>(a.pos4, a.ipart, a.npart, a.nleaf,
-                                                                                       a.L, a.ax, a.ay, a.az);
+    launch_l2l(a, st);
+    ph::note_launch(), k_l2p_f32<<<grid_cap(), 256, 0, st>>>(a.pos4, a.ipart, a.npart, a.tree_cnt, a.L, a.ax, a.ay,
+                                                               a.az);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }
 
 int run_p2m_m2m(const MultipoleArgs &a, cudaStream_t st)
 {
-    ph::note_launch(), k_p2m<<<grid_for(a.nleaf, MP_TB), MP_TB, 0, st>>>(a.px, a.py, a.pz, a.ipart, a.npart, a.cx, a.cy, a.cz, a.nleaf,
-                                                       a.mass, a.M);
-    for (int d = a.ndepth - 1; d >= 0; d--) {
-        int b = a.depth_off[d], e = a.depth_off[d + 1];
-        if (e > b)
-            ph::note_launch(), k_m2m_depth<<<grid_for(e - b, MP_TB), MP_TB, 0, st>>>(a.depth_list, b, e, a.nleaf, a.son0, a.son1, a.cx,
-                                                                  a.cy, a.cz, a.M);
-    }
+    ph::note_launch(), k_p2m<<<grid_cap(), MP_TB, 0, st>>>(a.px, a.py, a.pz, a.ipart, a.npart, a.cx, a.cy, a.cz,
+                                                             a.tree_cnt, a.mass, a.M);
+    for (int d = a.ndepth - 1; d >= 0; d--)
+        ph::note_launch(), k_m2m_depth<<<grid_cap(), MP_TB, 0, st>>>(a.depth_list, a.depth_off, d, a.tree_cnt, a.son0,
+                                                                       a.son1, a.cx, a.cy, a.cz, a.M);
+    ph::note_launch(), k_zero_L<<<grid_cap(), 256, 0, st>>>(a.L, a.tree_cnt);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }

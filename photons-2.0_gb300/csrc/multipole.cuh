@@ -9,9 +9,11 @@ struct MultipoleArgs {
     const double *px, *py, *pz;
     const int *ipart, *npart, *son0, *son1, *parent;
     const double *cx, *cy, *cz;
-    int nleaf, nunified, ndepth;
+    const int *tree_cnt;                   // device build counters (BC_LEAVES, BC_NODES)
+    const unsigned long long *walk_flags;  // device walk flags; nonzero: lists incomplete, M2L does nothing
+    int ndepth;                            // depths to launch (at least the tree's deepest + 1)
     const int *depth_list;
-    const int *depth_off;  // host array [ndepth+1]
+    const int *depth_off;  // device [ndepth+1]
     const uint32_t *m2l_pool;
     const long long *m2l_off;
     const int *m2l_cnt;
@@ -28,7 +30,7 @@ int run_downward(const MultipoleArgs &a, cudaStream_t st);
 // split precision: FP32 M2L (M rounded into M32) and FP32 L2P after FP64 L2L
 int run_m2l_f32(const MultipoleArgs &a, float *M32, cudaStream_t st);
 int run_downward_f32(const MultipoleArgs &a, cudaStream_t st);
-// P2M and M2M only (multipoles for callers that read them)
+// P2M and M2M, and L zeroed for the M2L that follows
 int run_p2m_m2m(const MultipoleArgs &a, cudaStream_t st);
 // op: 0 m2l (in = M, inout = L, rs), 1 m2m (in = M, inout = M'), 2 l2l (in = L, inout = L')
 int launch_op_batch(int op, int n, const double *d, const double *in, double *inout, double rs, cudaStream_t st);

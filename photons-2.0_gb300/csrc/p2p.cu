@@ -76,6 +76,13 @@ __device__ __forceinline__ void leaf_shift(int img, double L, double &s0, double
 // ---------------------------------------------------------------------
 // FP32 split-precision kernel
 // ---------------------------------------------------------------------
+// target leaves of this pass; none if the walk overflowed a list pool
+// (its lists are then incomplete and the pass is repeated with larger pools)
+__device__ __forceinline__ int p2p_targets(const P2PArgs &A)
+{
+    return *A.walk_flags ? 0 : A.tree_cnt[BC_LEAVES];
+}
+
 __global__ void __launch_bounds__(P2P_TB) k_p2p_split(P2PArgs A)
 {
     __shared__ float4 s_src[P2P_WARPS][STAGE32];
@@ -85,11 +92,12 @@ __global__ void __launch_bounds__(P2P_TB) k_p2p_split(P2PArgs A)
     float4 *src = s_src[wib];
     const SplitConsts K = A.k;
 
+    const int nleaf = p2p_targets(A);
     for (;;) {
         int t;
         if (lane == 0) t = atomicAdd(A.work_counter, 1);
         t = __shfl_sync(0xffffffffu, t, 0);
-        if (t >= A.nleaf) break;
+        if (t >= nleaf) break;
         const int nt = A.npart[t], it = A.ipart[t];
         if (nt == 0) continue;
         const double ct0 = A.cx[t], ct1 = A.cy[t], ct2 = A.cz[t];
@@ -336,11 +344,12 @@ __global__ void __launch_bounds__(P2P_TB, 3) k_p2p_split_packed(P2PArgs A)
     const SplitConsts K = A.k;
     const float Lhi = (float)A.boxsize, Llo = (float)(A.boxsize - (double)Lhi);
 
+    const int nleaf = p2p_targets(A);
     for (;;) {
         int t;
         if (lane == 0) t = atomicAdd(A.work_counter, 1);
         t = __shfl_sync(0xffffffffu, t, 0);
-        if (t >= A.nleaf) break;
+        if (t >= nleaf) break;
         const int nt = A.npart[t], it = A.ipart[t];
         if (nt == 0) continue;
         const float4 cth = A.chi[t], ctl = A.clo[t];
@@ -505,11 +514,12 @@ __global__ void __launch_bounds__(P2P_TB) k_p2p_fp64(P2PArgs A)
     const double coeff = 2.0 / sqrt(M_PI);
     const double soft3 = mass / (eps * eps * eps);
 
+    const int nleaf = p2p_targets(A);
     for (;;) {
         int t;
         if (lane == 0) t = atomicAdd(A.work_counter, 1);
         t = __shfl_sync(0xffffffffu, t, 0);
-        if (t >= A.nleaf) break;
+        if (t >= nleaf) break;
         const int nt = A.npart[t], it = A.ipart[t];
         if (nt == 0) continue;
         const long long eoff = A.p2p_off[t];
@@ -594,9 +604,10 @@ __global__ void __launch_bounds__(P2P_TB) k_p2p_fp64(P2PArgs A)
 
 // FP32 offsets of every particle from its own leaf centre
 __global__ void k_leaf_offsets(const double *px, const double *py, const double *pz, const int *ipart,
-                               const int *npart, const double *cx, const double *cy, const double *cz, int nleaf,
-                               float4 *pos4)
+                               const int *npart, const double *cx, const double *cy, const double *cz,
+                               const int *tree_cnt, float4 *pos4)
 {
+    const int nleaf = tree_cnt[BC_LEAVES];
     int lane = warp_lane();
     int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
     for (int l = gw; l < nleaf; l += nw) {
@@ -622,10 +633,11 @@ SplitConsts make_split_consts(const PassParams &p)
     return k;
 }
 
-int launch_leaf_offsets(const BuildBufs &b, const TreeBufs &t, int nleaf, float4 *pos4, cudaStream_t st)
+int launch_leaf_offsets(const BuildBufs &b, const TreeBufs &t, float4 *pos4, cudaStream_t st)
 {
     int blocks = device_sm_count() * 8;
-    ph::note_launch(), k_leaf_offsets<<<blocks, 256, 0, st>>>(b.x, b.y, b.z, t.ipart, t.npart, t.cx, t.cy, t.cz, nleaf, pos4);
+    ph::note_launch(), k_leaf_offsets<<<blocks, 256, 0, st>>>(b.x, b.y, b.z, t.ipart, t.npart, t.cx, t.cy, t.cz, b.cnt,
+                                                              pos4);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }

@@ -14,7 +14,8 @@ struct P2PArgs {
     // tree (leaf part of the unified arrays)
     const int *ipart, *npart;
     const double *cx, *cy, *cz;
-    int nleaf;
+    const int *tree_cnt;                     // device build counters (leaves at BC_LEAVES)
+    const unsigned long long *walk_flags;    // device walk flags; nonzero: lists incomplete, no work
     // lists
     const uint32_t *p2p_pool;
     const long long *p2p_off;
@@ -32,7 +33,7 @@ struct P2PArgs {
 };
 
 SplitConsts make_split_consts(const PassParams &p);
-int launch_leaf_offsets(const BuildBufs &b, const TreeBufs &t, int nleaf, float4 *pos4, cudaStream_t st);
+int launch_leaf_offsets(const BuildBufs &b, const TreeBufs &t, float4 *pos4, cudaStream_t st);
 int launch_p2p(const P2PArgs &a, int fp64, cudaStream_t st);
 
 }  // namespace ph

@@ -67,6 +67,8 @@ __global__ void k_init_root(BuildBufs b, int n, double L)
         }
         for (int i = 0; i < BC_NCOUNTERS; i++) b.cnt[i] = 0;
         b.cnt[BC_LEVEL_COUNT] = 1;
+        b.leaf_begin[0] = 0;
+        b.leaf_count[0] = 0;
     }
 }
 
@@ -81,15 +83,17 @@ __global__ void k_init_particles(const double *__restrict__ pos, int n, BuildBuf
 }
 
 
-__global__ void k_level_nch(BuildBufs b, int lb, int C)
+__global__ void k_level_nch(BuildBufs b)
 {
+    const int lb = b.cnt[BC_LEVEL_BEGIN], C = b.cnt[BC_LEVEL_COUNT];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x)
         b.tn_nch[i] = (b.tn_len[lb + i] + CHUNK - 1) / CHUNK;
 }
 
 // chunk -> level-local node index, written once per level
-__global__ void k_chunk_map(BuildBufs b, int C)
+__global__ void k_chunk_map(BuildBufs b)
 {
+    const int C = b.cnt[BC_LEVEL_COUNT];
     int lane = warp_lane();
     int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
     for (int i = gw; i < C; i += nw) {
@@ -98,8 +102,9 @@ __global__ void k_chunk_map(BuildBufs b, int C)
     }
 }
 
-__global__ void k_chunk_sum(BuildBufs b, int lb, int C, int D)
+__global__ void k_chunk_sum(BuildBufs b, int D)
 {
+    const int lb = b.cnt[BC_LEVEL_BEGIN];
     const double *coord = axis_ptr(b.x, b.y, b.z, D);
     int W = b.cnt[BC_W];
     int lane = warp_lane();
@@ -117,8 +122,9 @@ __global__ void k_chunk_sum(BuildBufs b, int lb, int C, int D)
     }
 }
 
-__global__ void k_node_mean(BuildBufs b, int lb, int C, int D)
+__global__ void k_node_mean(BuildBufs b, int D)
 {
+    const int lb = b.cnt[BC_LEVEL_BEGIN], C = b.cnt[BC_LEVEL_COUNT];
     const double *coord = axis_ptr(b.x, b.y, b.z, D);
     int lane = warp_lane();
     int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
@@ -138,8 +144,9 @@ __global__ void k_node_mean(BuildBufs b, int lb, int C, int D)
     }
 }
 
-__global__ void k_chunk_count(BuildBufs b, int lb, int C, int D)
+__global__ void k_chunk_count(BuildBufs b, int D)
 {
+    const int lb = b.cnt[BC_LEVEL_BEGIN];
     const double *coord = axis_ptr(b.x, b.y, b.z, D);
     int W = b.cnt[BC_W];
     int lane = warp_lane();
@@ -159,8 +166,9 @@ __global__ void k_chunk_count(BuildBufs b, int lb, int C, int D)
 }
 
 // per node: prefix of chunk counts, partition sizes, child kinds
-__global__ void k_node_split(BuildBufs b, int lb, int C, int maxleaf)
+__global__ void k_node_split(BuildBufs b, int maxleaf)
 {
+    const int lb = b.cnt[BC_LEVEL_BEGIN], C = b.cnt[BC_LEVEL_COUNT];
     int lane = warp_lane();
     int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
     for (int i = gw; i < C; i += nw) {
@@ -193,8 +201,9 @@ __global__ void k_node_split(BuildBufs b, int lb, int C, int maxleaf)
     }
 }
 
-__global__ void k_make_children(BuildBufs b, int lb, int C, int maxleaf, int D)
+__global__ void k_make_children(BuildBufs b, int maxleaf, int D)
 {
+    const int lb = b.cnt[BC_LEVEL_BEGIN], C = b.cnt[BC_LEVEL_COUNT];
     int leaves_before = b.cnt[BC_LEAVES];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
         int t = lb + i;
@@ -255,11 +264,41 @@ __global__ void k_make_children(BuildBufs b, int lb, int C, int maxleaf, int D)
     }
 }
 
-__global__ void k_level_finish(BuildBufs b)
+// close level d: record its node range and the leaves it created, advance.
+// After a capacity overflow no further level is built.
+__global__ void k_level_finish(BuildBufs b, int d)
 {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const int C = b.cnt[BC_LEVEL_COUNT], lb = b.cnt[BC_LEVEL_BEGIN];
+        if (C == 0) return;
+        if (b.cnt[BC_FLAGS] & (PH_FLAG_LEAF_CAPACITY | PH_FLAG_NODE_CAPACITY)) {
+            b.cnt[BC_LEVEL_COUNT] = 0;
+            return;
+        }
+        b.lvl_begin[d] = lb;
+        b.lvl_count[d] = C;
+        b.leaf_begin[d + 1] = b.cnt[BC_LEAVES];
+        b.leaf_count[d + 1] = b.cnt[BC_NEW_LEAVES];
         b.cnt[BC_LEAVES] += b.cnt[BC_NEW_LEAVES];
+        b.cnt[BC_LEVEL_BEGIN] = lb + C;
         b.cnt[BC_LEVEL_COUNT] = b.cnt[BC_NEXT_NODES];
+        b.cnt[BC_NLEVELS] = d + 1;
+    }
+}
+
+// After the last launched level: totals, and PH_FLAG_DEPTH if nodes remain
+// unsplit.  A failed build (capacity or depth) reports an empty tree, so
+// every later stage of the pass has no work and reads nothing stale.
+__global__ void k_tree_totals(BuildBufs b)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        b.cnt[BC_NODES] = b.cnt[BC_LEVEL_BEGIN];
+        if (b.cnt[BC_LEVEL_COUNT] > 0) b.cnt[BC_FLAGS] |= PH_FLAG_DEPTH;
+        if (b.cnt[BC_FLAGS] & (PH_FLAG_LEAF_CAPACITY | PH_FLAG_NODE_CAPACITY | PH_FLAG_DEPTH)) {
+            b.cnt[BC_NODES] = 0;
+            b.cnt[BC_LEAVES] = 0;
+            b.cnt[BC_NLEVELS] = 0;
+        }
     }
 }
 
@@ -269,8 +308,9 @@ __global__ void k_level_finish(BuildBufs b)
 // the mean in the left region (p < S) records slot p-r (its rank among
 // particles above the mean).  Slot k pairs the k-th from the left with the
 // k-th from the right, which is the order src/fmm.c:60-72 swaps them in.
-__global__ void k_rank(BuildBufs b, int lb, int C, int D)
+__global__ void k_rank(BuildBufs b, int D)
 {
+    const int lb = b.cnt[BC_LEVEL_BEGIN];
     const double *coord = axis_ptr(b.x, b.y, b.z, D);
     int W = b.cnt[BC_W];
     int lane = warp_lane();
@@ -312,8 +352,9 @@ __device__ __forceinline__ void swap_particles(BuildBufs &b, int i, int j)
 
 // Each pair is exchanged by the thread of its left-region member only, so
 // the exchanges are disjoint.
-__global__ void k_swap(BuildBufs b, int lb, int C, int D)
+__global__ void k_swap(BuildBufs b, int D)
 {
+    const int lb = b.cnt[BC_LEVEL_BEGIN];
     const double *coord = axis_ptr(b.x, b.y, b.z, D);
     int W = b.cnt[BC_W];
     int lane = warp_lane();
@@ -339,8 +380,10 @@ __global__ void k_swap(BuildBufs b, int lb, int C, int D)
 }
 
 // ---------------- renumbering ----------------
-__global__ void k_subtree_counts(BuildBufs b, int lb, int C)
+__global__ void k_subtree_counts(BuildBufs b, int d)
 {
+    if (d >= b.cnt[BC_NLEVELS]) return;
+    const int lb = b.lvl_begin[d], C = b.lvl_count[d];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
         int t = lb + i;
         int sn = 1, sl = 0;
@@ -355,8 +398,10 @@ __global__ void k_subtree_counts(BuildBufs b, int lb, int C)
 }
 
 // preorder node numbers and depth-first leaf numbers, src/fmm.c:101-118
-__global__ void k_number(BuildBufs b, int lb, int C)
+__global__ void k_number(BuildBufs b, int d)
 {
+    if (d >= b.cnt[BC_NLEVELS]) return;
+    const int lb = b.lvl_begin[d], C = b.lvl_count[d];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
         int t = lb + i;
         if (t == 0) { b.tn_pre[0] = 0; b.tn_lbase[0] = 0; }
@@ -381,8 +426,9 @@ __device__ __forceinline__ void write_geom(TreeBufs &T, int u, const double *box
     T.wsum[u] = w0 + w1 + w2;
 }
 
-__global__ void k_scatter_nodes(BuildBufs b, TreeBufs T, int nnodes, int nleaves)
+__global__ void k_scatter_nodes(BuildBufs b, TreeBufs T)
 {
+    const int nnodes = b.cnt[BC_NODES], nleaves = b.cnt[BC_LEAVES];
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nnodes; t += gridDim.x * blockDim.x) {
         int u = nleaves + b.tn_pre[t];
         T.ipart[u] = b.tn_start[t];
@@ -398,8 +444,9 @@ __global__ void k_scatter_nodes(BuildBufs b, TreeBufs T, int nnodes, int nleaves
     }
 }
 
-__global__ void k_scatter_leaves(BuildBufs b, TreeBufs T, int nleaves)
+__global__ void k_scatter_leaves(BuildBufs b, TreeBufs T)
 {
+    const int nleaves = b.cnt[BC_LEAVES];
     for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < nleaves; l += gridDim.x * blockDim.x) {
         int u = b.tl_final[l];
         T.ipart[u] = b.tl_start[l];
@@ -414,23 +461,39 @@ __global__ void k_scatter_leaves(BuildBufs b, TreeBufs T, int nleaves)
 }
 
 // depth lists: depth d holds the level-d nodes (temp order) then the leaves
-// created by level d-1 (temp order)
-__global__ void k_depth_lists(BuildBufs b, TreeBufs T, int d, int node_b, int node_c, int leaf_b, int leaf_c,
-                              int off, int nleaves)
+// created by level d-1 (temp order); offsets by a one-thread prefix
+__global__ void k_depth_offsets(BuildBufs b, TreeBufs T, int ndepth)
 {
-    int tot = node_c + leaf_c;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += gridDim.x * blockDim.x) {
-        int u = (i < node_c) ? nleaves + b.tn_pre[node_b + i] : b.tl_final[leaf_b + (i - node_c)];
-        T.depth_list[off + i] = u;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        int off = 0;
+        const int nlev = b.cnt[BC_NLEVELS];
+        int deepest = 0;
+        for (int d = 0; d < ndepth; d++) {
+            T.depth_off[d] = off;
+            const int nc = d < nlev ? b.lvl_count[d] : 0;
+            const int lc = d <= nlev ? b.leaf_count[d] : 0;
+            T.depth_cnt[d] = nc + lc;
+            if (nc + lc) deepest = d;
+            off += nc + lc;
+        }
+        T.depth_off[ndepth] = off;
+        b.cnt[BC_DEPTH] = deepest;
     }
-    (void)d;
 }
 
-inline int grid_for(int n, int tpb, int maxblocks)
+__global__ void k_depth_lists(BuildBufs b, TreeBufs T)
 {
-    int g = (n + tpb - 1) / tpb;
-    if (g < 1) g = 1;
-    return g < maxblocks ? g : maxblocks;
+    const int d = blockIdx.y;
+    const int nlev = b.cnt[BC_NLEVELS], nleaves = b.cnt[BC_LEAVES];
+    const int node_c = d < nlev ? b.lvl_count[d] : 0;
+    const int node_b = d < nlev ? b.lvl_begin[d] : 0;
+    const int leaf_c = d <= nlev ? b.leaf_count[d] : 0, leaf_b = d <= nlev ? b.leaf_begin[d] : 0;
+    const int off = T.depth_off[d];
+    const int tot = node_c + leaf_c;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += gridDim.x * blockDim.x) {
+        const int u = (i < node_c) ? nleaves + b.tn_pre[node_b + i] : b.tl_final[leaf_b + (i - node_c)];
+        T.depth_list[off + i] = u;
+    }
 }
 
 }  // namespace
@@ -442,95 +505,63 @@ int launch_init_particles(BuildBufs &b, const double *pos, int n, cudaStream_t s
     return 0;
 }
 
-int build_tree(BuildBufs &b, TreeBufs &T, const PassParams &p, int n, cudaStream_t st, TreeInfo &info,
-               double *t_ms_phase)
+// Enqueue the whole build for at most `levels` node levels; no host sync.
+// Levels past the real depth exit at once.  If nodes remain after the last
+// level, PH_FLAG_DEPTH is raised in b.cnt[BC_FLAGS] (the caller grows
+// `levels` and builds again); capacity overflows raise their flags there too.
+// Depth lists cover depths 0..levels.
+int build_tree(BuildBufs &b, TreeBufs &T, const PassParams &p, int n, int levels, cudaStream_t st)
 {
-    (void)t_ms_phase;
-    const int sms = device_sm_count();
-    const int maxb = sms * 8;
-    const int L = 0;
-    (void)L;
+    const int maxb = device_sm_count() * 8;
+    if (levels < 1 || levels + 1 > T.max_depth_cap)
+        return ph_set_error(7, "tree deeper than %d levels", T.max_depth_cap - 1);
+    PH_CUDA_CHECK(cudaMemsetAsync(b.lvl_count, 0, sizeof(int) * (levels + 1), st));
+    PH_CUDA_CHECK(cudaMemsetAsync(b.leaf_count, 0, sizeof(int) * (levels + 2), st));
     ph::note_launch(), k_init_root<<<1, 1, 0, st>>>(b, n, p.boxsize);
-    PH_CUDA_CHECK(cudaGetLastError());
-
-    std::vector<int> lvl_begin, lvl_count, leaf_begin, leaf_count;
-    int lb = 0;
-    int leaves_total = 0;
-    int h[BC_NCOUNTERS];
-    for (int d = 0;; d++) {
-        PH_CUDA_CHECK(cudaMemcpyAsync(h, b.cnt, sizeof(h), cudaMemcpyDeviceToHost, st));
-        PH_CUDA_CHECK(cudaStreamSynchronize(st));
-        if (h[BC_FLAGS] & PH_FLAG_LEAF_CAPACITY)
-            return ph_set_error(4, "leaf capacity 2N/MAXLEAF=%d exceeded by the mean-split tree", b.rule_cap);
-        if (h[BC_FLAGS] & PH_FLAG_NODE_CAPACITY)
-            return ph_set_error(4, "node capacity 2N/MAXLEAF=%d exceeded by the mean-split tree", b.rule_cap);
-        int C = h[BC_LEVEL_COUNT];
-        if (d > 0) {
-            leaf_begin.push_back(leaves_total);
-            leaf_count.push_back(h[BC_LEAVES] - leaves_total);
-            leaves_total = h[BC_LEAVES];
-        } else {
-            leaf_begin.push_back(0);
-            leaf_count.push_back(0);
-        }
-        if (C == 0) break;
-        if (d >= T.max_depth_cap) return ph_set_error(7, "tree deeper than %d levels", T.max_depth_cap);
-        lvl_begin.push_back(lb);
-        lvl_count.push_back(C);
-        int D = d % 3;  // direct_local_start = 0 at one rank; axis cycles (src/fmm.c:99)
-
-        ph::note_launch(), k_level_nch<<<grid_for(C, TB, maxb), TB, 0, st>>>(b, lb, C);
+    for (int d = 0; d < levels; d++) {
+        const int D = d % 3;  // direct_local_start = 0 at one rank; axis cycles (src/fmm.c:99)
+        ph::note_launch(), k_level_nch<<<maxb, TB, 0, st>>>(b);
         scan_exclusive_i32(b.tn_nch, b.tn_chunk_base, b.cnt + BC_LEVEL_COUNT, b.cap_nodes, b.cnt + BC_W,
                            b.scan_scratch, b.scan_scratch_elems, st);
-        int wgrid = maxb;
-        ph::note_launch(), k_chunk_map<<<grid_for(C * 32, TB, maxb), TB, 0, st>>>(b, C);
-        ph::note_launch(), k_chunk_sum<<<wgrid, TB, 0, st>>>(b, lb, C, D);
-        ph::note_launch(), k_node_mean<<<grid_for(C * 32, TB, maxb), TB, 0, st>>>(b, lb, C, D);
-        ph::note_launch(), k_chunk_count<<<wgrid, TB, 0, st>>>(b, lb, C, D);
-        ph::note_launch(), k_node_split<<<grid_for(C * 32, TB, maxb), TB, 0, st>>>(b, lb, C, p.maxleaf);
+        ph::note_launch(), k_chunk_map<<<maxb, TB, 0, st>>>(b);
+        ph::note_launch(), k_chunk_sum<<<maxb, TB, 0, st>>>(b, D);
+        ph::note_launch(), k_node_mean<<<maxb, TB, 0, st>>>(b, D);
+        ph::note_launch(), k_chunk_count<<<maxb, TB, 0, st>>>(b, D);
+        ph::note_launch(), k_node_split<<<maxb, TB, 0, st>>>(b, p.maxleaf);
         scan_exclusive_i32(b.tn_nodeflag, b.tn_nodebase, b.cnt + BC_LEVEL_COUNT, b.cap_nodes, b.cnt + BC_NEXT_NODES,
                            b.scan_scratch, b.scan_scratch_elems, st);
         scan_exclusive_i32(b.tn_leafflag, b.tn_leafbase, b.cnt + BC_LEVEL_COUNT, b.cap_nodes, b.cnt + BC_NEW_LEAVES,
                            b.scan_scratch, b.scan_scratch_elems, st);
-        ph::note_launch(), k_make_children<<<grid_for(C, TB, maxb), TB, 0, st>>>(b, lb, C, p.maxleaf, D);
-        ph::note_launch(), k_rank<<<wgrid, TB, 0, st>>>(b, lb, C, D);
-        ph::note_launch(), k_swap<<<wgrid, TB, 0, st>>>(b, lb, C, D);
-        ph::note_launch(), k_level_finish<<<1, 1, 0, st>>>(b);
-        PH_CUDA_CHECK(cudaGetLastError());
-        lb += C;
+        ph::note_launch(), k_make_children<<<maxb, TB, 0, st>>>(b, p.maxleaf, D);
+        ph::note_launch(), k_rank<<<maxb, TB, 0, st>>>(b, D);
+        ph::note_launch(), k_swap<<<maxb, TB, 0, st>>>(b, D);
+        ph::note_launch(), k_level_finish<<<1, 1, 0, st>>>(b, d);
     }
-    int nnodes = lb;
-    int nleaves = leaves_total;
-    int nlev = (int)lvl_begin.size();
+    ph::note_launch(), k_tree_totals<<<1, 1, 0, st>>>(b);
     // subtree sizes bottom-up, numbers top-down
-    for (int d = nlev - 1; d >= 0; d--)
-        ph::note_launch(), k_subtree_counts<<<grid_for(lvl_count[d], TB, maxb), TB, 0, st>>>(b, lvl_begin[d], lvl_count[d]);
-    for (int d = 0; d < nlev; d++)
-        ph::note_launch(), k_number<<<grid_for(lvl_count[d], TB, maxb), TB, 0, st>>>(b, lvl_begin[d], lvl_count[d]);
-    ph::note_launch(), k_scatter_nodes<<<grid_for(nnodes, TB, maxb), TB, 0, st>>>(b, T, nnodes, nleaves);
-    ph::note_launch(), k_scatter_leaves<<<grid_for(nleaves, TB, maxb), TB, 0, st>>>(b, T, nleaves);
-    // depth lists: depth d = nodes of level d + leaves created by level d-1
-    int ndepth = nlev + 1;  // leaves can sit one level below the deepest nodes
-    std::vector<int> doff(ndepth + 1, 0);
-    for (int d = 0; d < ndepth; d++) {
-        int nc = d < nlev ? lvl_count[d] : 0;
-        int lc = d < (int)leaf_count.size() ? leaf_count[d] : 0;
-        doff[d + 1] = doff[d] + nc + lc;
-    }
-    for (int d = 0; d < ndepth; d++) {
-        int nc = d < nlev ? lvl_count[d] : 0;
-        int nbeg = d < nlev ? lvl_begin[d] : 0;
-        int lc = d < (int)leaf_count.size() ? leaf_count[d] : 0;
-        int lbeg = d < (int)leaf_begin.size() ? leaf_begin[d] : 0;
-        if (nc + lc == 0) continue;
-        ph::note_launch(), k_depth_lists<<<grid_for(nc + lc, TB, maxb), TB, 0, st>>>(b, T, d, nbeg, nc, lbeg, lc, doff[d], nleaves);
-    }
-    PH_CUDA_CHECK(cudaMemcpyAsync(T.depth_off, doff.data(), sizeof(int) * (ndepth + 1), cudaMemcpyHostToDevice, st));
+    for (int d = levels - 1; d >= 0; d--) ph::note_launch(), k_subtree_counts<<<maxb, TB, 0, st>>>(b, d);
+    for (int d = 0; d < levels; d++) ph::note_launch(), k_number<<<maxb, TB, 0, st>>>(b, d);
+    ph::note_launch(), k_scatter_nodes<<<maxb, TB, 0, st>>>(b, T);
+    ph::note_launch(), k_scatter_leaves<<<maxb, TB, 0, st>>>(b, T);
+    const int ndepth = levels + 1;  // leaves can sit one level below the deepest nodes
+    ph::note_launch(), k_depth_offsets<<<1, 1, 0, st>>>(b, T, ndepth);
+    ph::note_launch(), k_depth_lists<<<dim3(64, ndepth), TB, 0, st>>>(b, T);
     PH_CUDA_CHECK(cudaGetLastError());
-    info.nleaf = nleaves;
-    info.nnode = nnodes;
-    info.depth = ndepth - 1;
-    info.depth_off.assign(doff.begin(), doff.end());
+    return 0;
+}
+
+// host view of the finished build (after the stream has been synchronised)
+int read_tree_info(const BuildBufs &b, const TreeBufs &T, int levels, TreeInfo &info)
+{
+    int h[BC_NCOUNTERS];
+    PH_CUDA_CHECK(cudaMemcpy(h, b.cnt, sizeof(h), cudaMemcpyDeviceToHost));
+    info.nleaf = h[BC_LEAVES];
+    info.nnode = h[BC_NODES];
+    info.depth = h[BC_DEPTH];
+    info.levels = h[BC_NLEVELS];
+    info.flags = h[BC_FLAGS];
+    info.depth_off.resize(levels + 2);
+    PH_CUDA_CHECK(cudaMemcpy(info.depth_off.data(), T.depth_off, sizeof(int) * (levels + 2), cudaMemcpyDeviceToHost));
     return 0;
 }
 

@@ -111,8 +111,9 @@ struct WalkArgs {
     Geo g;
     WalkBufs w;
     const int *depth_list;
-    int list_begin, list_end;
-    int depth, nleaf, root;
+    const int *depth_off;  // device [depth+2]: this depth's slice of depth_list
+    const int *tree_cnt;   // device build counters: leaves at BC_LEAVES (the root is unified id nleaf)
+    int depth;
     int nroot;               // entries of the root's list: (root, img) for the selected images
     int root_img[PH_NIMG];
     double boxsize, theta2, c2, rcut, theta;
@@ -120,10 +121,9 @@ struct WalkArgs {
 };
 
 // sender-side pruning of an image node, src/remotes.c:97-158
-__device__ __forceinline__ bool image_pruned(const WalkArgs &A, int b, double s0, double s1, double s2)
+__device__ __forceinline__ bool image_pruned(const WalkArgs &A, int r, int b, double s0, double s1, double s2)
 {
     const Geo &g = A.g;
-    int r = A.root;
     double sx[3] = {s0, s1, s2};
     double rc[3] = {g.cx[r], g.cy[r], g.cz[r]}, rw[3] = {g.wx[r], g.wy[r], g.wz[r]};
     double bc[3] = {g.cx[b], g.cy[b], g.cz[b]}, bw[3] = {g.wx[b], g.wy[b], g.wz[b]};
@@ -183,13 +183,16 @@ __global__ void __launch_bounds__(WALK_TB, MINB) k_walk_level(WalkArgs A)
     uint32_t *sh_pd = sh_p2p + WS_P2P;
     uint32_t *sh_m2l = sh_pd + WS_PD;
     const int parity = A.depth & 1;
+    const int nleaf = A.tree_cnt[BC_LEAVES];
+    const int root = nleaf;  // node 0 in preorder
+    const int list_begin = A.depth_off[A.depth], list_end = A.depth_off[A.depth + 1];
     unsigned long long c_p2p_loc = 0, c_p2p_img = 0, c_m2l_loc = 0, c_m2l_img = 0, c_pl = 0, c_pi = 0;
     unsigned flags = 0;
     int max_stack = 0, max_stage = 0;
 
-    for (int ti = A.list_begin + gw; ti < A.list_end; ti += nw) {
+    for (int ti = list_begin + gw; ti < list_end; ti += nw) {
         const int a = A.depth_list[ti];
-        const bool leaf_a = a < A.nleaf;
+        const bool leaf_a = a < nleaf;
         const double ca0 = g.cx[a], ca1 = g.cy[a], ca2 = g.cz[a];
         const double wa0 = g.wx[a], wa1 = g.wy[a], wa2 = g.wz[a], wsa = g.wsum[a];
         const float4 ah = g.chi[a], al = g.clo[a], aw = g.w32[a];
@@ -236,7 +239,7 @@ __global__ void __launch_bounds__(WALK_TB, MINB) k_walk_level(WalkArgs A)
                 const bool valid = lane + 32 * s < k;
                 b[s] = PH_ENTRY_ID(e[s]);
                 img[s] = PH_ENTRY_IMG(e[s]);
-                const bool leaf_b = b[s] < A.nleaf;
+                const bool leaf_b = b[s] < nleaf;
                 const bool self = img[s] == 0 && b[s] == a;
                 need[s] = valid && !self && !(leaf_a && leaf_b);
                 npb[s] = (valid && !self && leaf_a && leaf_b) ? g.npart[b[s]] : 0;
@@ -252,7 +255,7 @@ __global__ void __launch_bounds__(WALK_TB, MINB) k_walk_level(WalkArgs A)
                 kind[s] = OUT_NONE;
                 if (lane + 32 * s >= k) continue;
                 const int bb = b[s], im = img[s];
-                const bool leaf_b = bb < A.nleaf;
+                const bool leaf_b = bb < nleaf;
                 if (im == 0 && bb == a) {
                     if (leaf_a) {
                         kind[s] = OUT_P2P;
@@ -293,7 +296,7 @@ __global__ void __launch_bounds__(WALK_TB, MINB) k_walk_level(WalkArgs A)
                         else if (leaf_b) kd = OUT_PUSH;
                         else kd = bigger_a ? OUT_PUSH : OUT_OPEN;
                     } else {
-                        const bool pruned = !leaf_b && image_pruned(A, bb, s0, s1, s2);
+                        const bool pruned = !leaf_b && image_pruned(A, root, bb, s0, s1, s2);
                         if (leaf_a) kd = (flag == 1 || pruned) ? OUT_M2L : OUT_OPEN;
                         else if (flag == 1) kd = OUT_M2L;
                         else kd = (leaf_b || pruned || bigger_a) ? OUT_PUSH : OUT_OPEN;
@@ -425,9 +428,10 @@ __global__ void k_walk_level_done(WalkBufs W, int depth)
 // FP32 copies of the geometry for every unified id: centre as hi + lo,
 // widths and width sum rounded
 __global__ void k_geom32(const double *cx, const double *cy, const double *cz, const double *wx, const double *wy,
-                         const double *wz, const double *wsum, const int *son0, const int *son1, int nu, float4 *chi,
+                         const double *wz, const double *wsum, const int *son0, const int *son1, const int *tree_cnt, float4 *chi,
                          float4 *clo, float4 *w32, int2 *son2)
 {
+    const int nu = tree_cnt[BC_LEAVES] + tree_cnt[BC_NODES];
     for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += gridDim.x * blockDim.x) {
         son2[u] = make_int2(son0[u], son1[u]);
         double c0 = cx[u], c1 = cy[u], c2 = cz[u];
@@ -440,19 +444,19 @@ __global__ void k_geom32(const double *cx, const double *cy, const double *cz, c
 
 }  // namespace
 
-int launch_geom32(const TreeBufs &t, int nu, cudaStream_t st)
+int launch_geom32(const TreeBufs &t, const int *tree_cnt, cudaStream_t st)
 {
-    int blocks = (nu + 255) / 256;
-    if (blocks > device_sm_count() * 8) blocks = device_sm_count() * 8;
-    if (blocks < 1) blocks = 1;
-    ph::note_launch(), k_geom32<<<blocks, 256, 0, st>>>(t.cx, t.cy, t.cz, t.wx, t.wy, t.wz, t.wsum, t.son0, t.son1, nu, t.chi,
-                                                    t.clo, t.w32, t.son2);
+    const int blocks = device_sm_count() * 8;
+    ph::note_launch(), k_geom32<<<blocks, 256, 0, st>>>(t.cx, t.cy, t.cz, t.wx, t.wy, t.wz, t.wsum, t.son0, t.son1, tree_cnt,
+                                                    t.chi, t.clo, t.w32, t.son2);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }
 
-int walk_lists(WalkBufs &w, const TreeBufs &t, const TreeInfo &info, const PassParams &p, unsigned image_mask,
-               cudaStream_t st, WalkStats &stats)
+// Enqueue the walk of depths 0..ndepth-1; depths past the tree's deepest
+// exit at once.  Counters and flags stay on the device (w.ctr).
+int walk_lists(WalkBufs &w, const TreeBufs &t, const int *tree_cnt, int ndepth, const PassParams &p,
+               unsigned image_mask, cudaStream_t st)
 {
     PH_CUDA_CHECK(cudaMemsetAsync(w.ctr, 0, sizeof(unsigned long long) * WC_N, st));
     WalkArgs A;
@@ -467,8 +471,8 @@ int walk_lists(WalkBufs &w, const TreeBufs &t, const TreeInfo &info, const PassP
     A.c2f = (float)(p.rcut * p.rcut);
     A.w = w;
     A.depth_list = t.depth_list;
-    A.nleaf = info.nleaf;
-    A.root = info.nleaf;  // node 0 in preorder
+    A.depth_off = t.depth_off;
+    A.tree_cnt = tree_cnt;
     A.nroot = 0;
     for (int img = 0; img < PH_NIMG; img++)
         if (image_mask & (1u << img)) A.root_img[A.nroot++] = img;
@@ -477,24 +481,16 @@ int walk_lists(WalkBufs &w, const TreeBufs &t, const TreeInfo &info, const PassP
     A.theta2 = p.theta * p.theta;
     A.rcut = p.rcut;
     A.c2 = p.rcut * p.rcut;
-    int blocks = (w.nwarps * 32 + WALK_TB - 1) / WALK_TB;
-    for (int d = 0; d <= info.depth; d++) {
+    const int blocks = (w.nwarps * 32 + WALK_TB - 1) / WALK_TB;
+    for (int d = 0; d < ndepth; d++) {
         A.depth = d;
-        A.list_begin = info.depth_off[d];
-        A.list_end = info.depth_off[d + 1];
-        if (A.list_end > A.list_begin) {
-            int need = A.list_end - A.list_begin;
-            int nb = (need * 32 + WALK_TB - 1) / WALK_TB;
-            if (w.nwarps == device_sm_count() * 3 * 8)
-                ph::note_launch(), k_walk_level<3><<<nb < blocks ? nb : blocks, WALK_TB, 0, st>>>(A);
-            else
-                ph::note_launch(), k_walk_level<2><<<nb < blocks ? nb : blocks, WALK_TB, 0, st>>>(A);
-        }
+        if (w.nwarps == device_sm_count() * 3 * 8)
+            ph::note_launch(), k_walk_level<3><<<blocks, WALK_TB, 0, st>>>(A);
+        else
+            ph::note_launch(), k_walk_level<2><<<blocks, WALK_TB, 0, st>>>(A);
         ph::note_launch(), k_walk_level_done<<<1, 1, 0, st>>>(w, d);
     }
     PH_CUDA_CHECK(cudaGetLastError());
-    PH_CUDA_CHECK(cudaMemcpyAsync(stats.c, w.ctr, sizeof(stats.c), cudaMemcpyDeviceToHost, st));
-    PH_CUDA_CHECK(cudaStreamSynchronize(st));
     return 0;
 }
 

@@ -123,6 +123,27 @@ def test_device_io_matches_host_io(ph, fp, ics):
     assert np.array_equal(dacc.cpu().numpy(), host)
 
 
+@pytest.mark.parametrize("precision", ["FP64", "FP32_SPLIT"])
+def test_graph_pass_matches_stage_pass(ph, ics, monkeypatch, precision):
+    """The captured-graph pass (default) and the stage-by-stage pass give
+    identical accelerations; so does a graph whose first capture launches
+    too few tree levels and is grown and re-captured."""
+    pos, p = ics.make("nfw128", nside=32, maxleaf=8)
+    prec = getattr(ph, precision)
+    graph = ph.ForcePass(0).run(pos, p, precision=prec)
+    monkeypatch.setenv("PHOTONS_GRAPH", "0")
+    stages = ph.ForcePass(0).run(pos, p, precision=prec)
+    monkeypatch.delenv("PHOTONS_GRAPH")
+    monkeypatch.setenv("PHOTONS_TREE_LEVELS", "2")
+    fp = ph.ForcePass(0)
+    grown = fp.run(pos, p, precision=prec)
+    again = fp.run(pos, p, precision=prec)
+    assert np.array_equal(graph, stages)
+    assert np.array_equal(graph, grown)
+    assert np.array_equal(graph, again)
+    assert fp.counters()["depth"] > 2
+
+
 def test_capacity_overflow_is_an_error(ph, fp):
     pos = np.full((100, 3), 3.0)
     p = dict(boxsize=10.0, theta=0.5, rs=1.0, rcut=4.5, eps=0.01, mass=1.0, maxleaf=8)
