@@ -478,6 +478,7 @@ int ph_stage_p2p(photons_ctx *c, int precision, int zero)
     a.work_counter = c->work_counter;
     a.boxsize = c->pp.boxsize; a.eps = c->pp.eps; a.mass = c->pp.mass; a.rs = c->pp.rs;
     a.k = ph::make_split_consts(c->pp);
+    a.acc_scale = c->pp.mass * ph::split_sig(c->pp) * ph::split_sig(c->pp);
     a.variant = p2p_variant();
     PH_TRY(ph_record(c, EV_P2P_BEGIN));
     PH_TRY(ph::launch_p2p(a, precision == PHOTONS_FP64, st));

@@ -223,6 +223,32 @@ __global__ void __launch_bounds__(P2P_TB) k_p2p_split(P2PArgs A)
 #define STAGE2 384  // staged sources per warp; 3 x 8 warps x 386 floats + reduction fit 48 KB
 
 __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float4 scaled(float4 o, float k) { return make_float4(o.x * k, o.y * k, o.z * k, 0.f); }
+
+// Pair factor in scaled coordinates x' = sig x, sig^2 = log2(e) / (4 rs^2),
+// so that exp(-u^2) = 2^(-|dx'|^2).  With t = 1 / (1 + p u) and r rinv = 1,
+//   m g(u) / r^3 dx = m sig^2 * ex rinv'^2 (t P(t) rinv' + c') dx',
+// c' = (2/sqrt(pi)) ia / sig; the constant m sig^2 is applied per target.
+// FP32-pipe work per pair: 3 dx + 3 |dx|^2 + 1 r + 1 den + 5 Horner + 2 for
+// t P rinv' + c' + 3 products + 3 accumulations = 21, plus rsqrt, rcp, ex2.
+__device__ __forceinline__ float2 pair_factor(float2 qq, const SplitConsts &K, float2 pia2, float2 one2, float2 c2,
+                                              float2 a0, float2 a1, float2 a2, float2 a3, float2 a4, float2 a5)
+{
+    qq.x = fmaxf(qq.x, K.e2s);
+    qq.y = fmaxf(qq.y, K.e2s);
+    const float2 rinv = make_float2(rsqrt_approx(qq.x), rsqrt_approx(qq.y));
+    const float2 r = __fmul2_rn(qq, rinv);
+    const float2 den = __ffma2_rn(pia2, r, one2);
+    const float2 tt = make_float2(rcp_approx(den.x), rcp_approx(den.y));
+    float2 P = __ffma2_rn(a5, tt, a4);
+    P = __ffma2_rn(P, tt, a3);
+    P = __ffma2_rn(P, tt, a2);
+    P = __ffma2_rn(P, tt, a1);
+    P = __ffma2_rn(P, tt, a0);
+    const float2 g1 = __ffma2_rn(__fmul2_rn(tt, rinv), P, c2);
+    const float2 ex = make_float2(ex2_approx(-qq.x), ex2_approx(-qq.y));
+    return __fmul2_rn(__fmul2_rn(ex, __fmul2_rn(rinv, rinv)), g1);
+}
 
 // one round's share of a staged batch: stream k takes source pairs k, k+G, ...
 __device__ __forceinline__ void p2p_round(const float2 *__restrict__ X2, const float2 *__restrict__ Y2,
@@ -230,9 +256,9 @@ __device__ __forceinline__ void p2p_round(const float2 *__restrict__ X2, const f
                                           float oy, float oz, const SplitConsts &K, float &rx, float &ry, float &rz)
 {
     const float2 nox = f2(-ox), noy = f2(-oy), noz = f2(-oz);
-    const float2 kq2 = f2(K.kq), pia2 = f2(K.pia), clin2 = f2(K.clin), one2 = f2(1.0f);
-    const float2 a0 = f2(K.a[0]), a1 = f2(K.a[1]), a2 = f2(K.a[2]), a3 = f2(K.a[3]), a4 = f2(K.a[4]),
-                 a5 = f2(K.a[5]);
+    const float2 pia2 = f2(K.pias), c2 = f2(K.cs), one2 = f2(1.0f);
+    const float2 a0 = f2(K.as[0]), a1 = f2(K.as[1]), a2 = f2(K.as[2]), a3 = f2(K.as[3]), a4 = f2(K.as[4]),
+                 a5 = f2(K.as[5]);
     float2 ax = f2(0.f), ay = f2(0.f), az = f2(0.f);
 #pragma unroll 2
     for (int pp = k; pp < npairs; pp += G) {
@@ -242,22 +268,7 @@ __device__ __forceinline__ void p2p_round(const float2 *__restrict__ X2, const f
         float2 qq = __fmul2_rn(dx, dx);
         qq = __ffma2_rn(dy, dy, qq);
         qq = __ffma2_rn(dz, dz, qq);
-        qq.x = fmaxf(qq.x, K.eps2);
-        qq.y = fmaxf(qq.y, K.eps2);
-        const float2 rinv = make_float2(rsqrt_approx(qq.x), rsqrt_approx(qq.y));
-        const float2 r = __fmul2_rn(qq, rinv);
-        const float2 den = __ffma2_rn(pia2, r, one2);
-        const float2 tt = make_float2(rcp_approx(den.x), rcp_approx(den.y));
-        float2 P = __ffma2_rn(a5, tt, a4);
-        P = __ffma2_rn(P, tt, a3);
-        P = __ffma2_rn(P, tt, a2);
-        P = __ffma2_rn(P, tt, a1);
-        P = __ffma2_rn(P, tt, a0);
-        const float2 h = __ffma2_rn(tt, P, __fmul2_rn(clin2, r));
-        const float2 ea = __fmul2_rn(qq, kq2);
-        const float2 ex = make_float2(ex2_approx(ea.x), ex2_approx(ea.y));
-        const float2 rinv2 = __fmul2_rn(rinv, rinv);
-        const float2 f = __fmul2_rn(__fmul2_rn(ex, h), __fmul2_rn(rinv2, rinv));
+        const float2 f = pair_factor(qq, K, pia2, one2, c2, a0, a1, a2, a3, a4, a5);
         ax = __ffma2_rn(dx, f, ax);
         ay = __ffma2_rn(dy, f, ay);
         az = __ffma2_rn(dz, f, az);
@@ -274,9 +285,9 @@ __device__ __forceinline__ void p2p_round_dual(const float2 *__restrict__ X2, co
                                                float4 oB, const SplitConsts &K, float &rAx, float &rAy, float &rAz,
                                                float &rBx, float &rBy, float &rBz)
 {
-    const float2 kq2 = f2(K.kq), pia2 = f2(K.pia), clin2 = f2(K.clin), one2 = f2(1.0f);
-    const float2 a0 = f2(K.a[0]), a1 = f2(K.a[1]), a2 = f2(K.a[2]), a3 = f2(K.a[3]), a4 = f2(K.a[4]),
-                 a5 = f2(K.a[5]);
+    const float2 pia2 = f2(K.pias), c2 = f2(K.cs), one2 = f2(1.0f);
+    const float2 a0 = f2(K.as[0]), a1 = f2(K.as[1]), a2 = f2(K.as[2]), a3 = f2(K.as[3]), a4 = f2(K.as[4]),
+                 a5 = f2(K.as[5]);
     const float2 nAx = f2(-oA.x), nAy = f2(-oA.y), nAz = f2(-oA.z);
     const float2 nBx = f2(-oB.x), nBy = f2(-oB.y), nBz = f2(-oB.z);
     float2 ax = f2(0.f), ay = f2(0.f), az = f2(0.f), bx = f2(0.f), by = f2(0.f), bz = f2(0.f);
@@ -290,22 +301,7 @@ __device__ __forceinline__ void p2p_round_dual(const float2 *__restrict__ X2, co
             float2 qq = __fmul2_rn(dx, dx);
             qq = __ffma2_rn(dy, dy, qq);
             qq = __ffma2_rn(dz, dz, qq);
-            qq.x = fmaxf(qq.x, K.eps2);
-            qq.y = fmaxf(qq.y, K.eps2);
-            const float2 rinv = make_float2(rsqrt_approx(qq.x), rsqrt_approx(qq.y));
-            const float2 r = __fmul2_rn(qq, rinv);
-            const float2 den = __ffma2_rn(pia2, r, one2);
-            const float2 tt = make_float2(rcp_approx(den.x), rcp_approx(den.y));
-            float2 P = __ffma2_rn(a5, tt, a4);
-            P = __ffma2_rn(P, tt, a3);
-            P = __ffma2_rn(P, tt, a2);
-            P = __ffma2_rn(P, tt, a1);
-            P = __ffma2_rn(P, tt, a0);
-            const float2 h = __ffma2_rn(tt, P, __fmul2_rn(clin2, r));
-            const float2 ea = __fmul2_rn(qq, kq2);
-            const float2 ex = make_float2(ex2_approx(ea.x), ex2_approx(ea.y));
-            const float2 rinv2 = __fmul2_rn(rinv, rinv);
-            const float2 f = __fmul2_rn(__fmul2_rn(ex, h), __fmul2_rn(rinv2, rinv));
+            const float2 f = pair_factor(qq, K, pia2, one2, c2, a0, a1, a2, a3, a4, a5);
             if (w) {
                 bx = __ffma2_rn(dx, f, bx);
                 by = __ffma2_rn(dy, f, by);
@@ -366,9 +362,10 @@ __global__ void __launch_bounds__(P2P_TB, 3) k_p2p_split_packed(P2PArgs A)
             const int m2 = lg2 < 0 ? 0 : (1 << lg2);
             const int G1 = 32 >> lg1, q1 = lane & (m1 - 1), k1 = lane >> lg1;
             const int G2 = m2 ? 32 >> lg2 : 1, q2 = m2 ? (lane & (m2 - 1)) : 0, k2 = m2 ? (lane >> lg2) : 0;
-            const float4 o1 = A.pos4[it + tb + q1];
+            const float4 o1 = scaled(A.pos4[it + tb + q1], K.sig);
             // round-2 lanes beyond the block's last target reuse it; their sums are discarded
-            const float4 o2 = m2 ? A.pos4[it + tb + m1 + min(q2, rest - 1)] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 o2 = m2 ? scaled(A.pos4[it + tb + m1 + min(q2, rest - 1)], K.sig)
+                                 : make_float4(0.f, 0.f, 0.f, 0.f);
             float s1x = 0.f, s1y = 0.f, s1z = 0.f, c1x = 0.f, c1y = 0.f, c1z = 0.f;
             float s2x = 0.f, s2y = 0.f, s2z = 0.f, c2x = 0.f, c2y = 0.f, c2z = 0.f;
 
@@ -386,9 +383,9 @@ __global__ void __launch_bounds__(P2P_TB, 3) k_p2p_split_packed(P2PArgs A)
                     const float4 csh = A.chi[s], csl = A.clo[s];
                     int mi, mj, mk;
                     image_offsets(img, mi, mj, mk);
-                    d0 = centre_diff(csh.x, csl.x, cth.x, ctl.x, mi, Lhi, Llo);
-                    d1 = centre_diff(csh.y, csl.y, cth.y, ctl.y, mj, Lhi, Llo);
-                    d2 = centre_diff(csh.z, csl.z, cth.z, ctl.z, mk, Lhi, Llo);
+                    d0 = centre_diff(csh.x, csl.x, cth.x, ctl.x, mi, Lhi, Llo) * K.sig;
+                    d1 = centre_diff(csh.y, csl.y, cth.y, ctl.y, mj, Lhi, Llo) * K.sig;
+                    d2 = centre_diff(csh.z, csl.z, cth.z, ctl.z, mk, Lhi, Llo) * K.sig;
                 }
                 const int incl = warp_incl_scan(ns);
                 const unsigned fit = __ballot_sync(0xffffffffu, lane < ne && incl <= STAGE2);
@@ -413,9 +410,9 @@ __global__ void __launch_bounds__(P2P_TB, 3) k_p2p_split_packed(P2PArgs A)
                     const float e2 = __shfl_sync(0xffffffffu, d2, lo);
                     if (idx < nstaged) {
                         const float4 o = A.pos4[eis + idx - epre];
-                        sx[idx] = o.x + e0;
-                        sy[idx] = o.y + e1;
-                        sz[idx] = o.z + e2;
+                        sx[idx] = fmaf(o.x, K.sig, e0);
+                        sy[idx] = fmaf(o.y, K.sig, e1);
+                        sz[idx] = fmaf(o.z, K.sig, e2);
                     }
                 }
                 // an odd count gets one far-away source whose force is exactly 0
@@ -467,9 +464,9 @@ __global__ void __launch_bounds__(P2P_TB, 3) k_p2p_split_packed(P2PArgs A)
                     b0 += red[3 * l]; b1 += red[3 * l + 1]; b2 += red[3 * l + 2];
                 }
                 const int ip = it + tb + lane;
-                A.ax[ip] += b0;
-                A.ay[ip] += b1;
-                A.az[ip] += b2;
+                A.ax[ip] += b0 * A.acc_scale;
+                A.ay[ip] += b1 * A.acc_scale;
+                A.az[ip] += b2 * A.acc_scale;
             }
             __syncwarp();
             if (m2) {
@@ -484,9 +481,9 @@ __global__ void __launch_bounds__(P2P_TB, 3) k_p2p_split_packed(P2PArgs A)
                         b0 += red[3 * l]; b1 += red[3 * l + 1]; b2 += red[3 * l + 2];
                     }
                     const int ip = it + tb + m1 + lane;
-                    A.ax[ip] += b0;
-                    A.ay[ip] += b1;
-                    A.az[ip] += b2;
+                    A.ax[ip] += b0 * A.acc_scale;
+                    A.ay[ip] += b1 * A.acc_scale;
+                    A.az[ip] += b2 * A.acc_scale;
                 }
                 __syncwarp();
             }
@@ -620,6 +617,13 @@ __global__ void k_leaf_offsets(const double *px, const double *py, const double 
 
 }  // namespace
 
+// coordinate scale of the packed kernel, rounded to FP32 first so that the
+// constants below match the scaling the kernel applies
+double split_sig(const PassParams &p)
+{
+    return (double)(float)(0.5 / p.rs * sqrt(1.4426950408889634));
+}
+
 SplitConsts make_split_consts(const PassParams &p)
 {
     SplitConsts k;
@@ -630,6 +634,14 @@ SplitConsts make_split_consts(const PassParams &p)
     for (int i = 0; i < SPLIT_NA; i++) k.a[i] = (float)(SPLIT_A[i] * p.mass);
     for (int i = SPLIT_NA; i < 8; i++) k.a[i] = 0.f;
     k.clin = (float)(p.mass * 2.0 / sqrt(M_PI) * ia);
+    // packed kernel: scaled coordinates, mass applied per target
+    const double sig = split_sig(p);
+    k.sig = (float)sig;
+    k.e2s = (float)(p.eps * p.eps * sig * sig);
+    k.pias = (float)(SPLIT_P * ia / sig);
+    k.cs = (float)(2.0 / sqrt(M_PI) * ia / sig);
+    for (int i = 0; i < SPLIT_NA; i++) k.as[i] = (float)SPLIT_A[i];
+    for (int i = SPLIT_NA; i < 8; i++) k.as[i] = 0.f;
     return k;
 }
 

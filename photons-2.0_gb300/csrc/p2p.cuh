@@ -6,8 +6,13 @@
 namespace ph {
 
 struct SplitConsts {
+    // scalar kernel: unscaled offsets, mass folded into a[] and clin
     float eps2, kq, pia, clin;
     float a[8];
+    // packed kernel: offsets scaled by sig (exp(-u^2) = 2^(-|dx'|^2)); the
+    // per-target sums are multiplied by P2PArgs::acc_scale = m sig^2
+    float sig, e2s, pias, cs;
+    float as[8];
 };
 
 struct P2PArgs {
@@ -28,11 +33,13 @@ struct P2PArgs {
     double *ax, *ay, *az;
     int *work_counter;
     double boxsize, eps, mass, rs;
+    double acc_scale;  // packed FP32 kernel: m sig^2
     SplitConsts k;
     int variant;  // FP32: 0 packed (default), 1 scalar
 };
 
 SplitConsts make_split_consts(const PassParams &p);
+double split_sig(const PassParams &p);
 int launch_leaf_offsets(const BuildBufs &b, const TreeBufs &t, float4 *pos4, cudaStream_t st);
 int launch_p2p(const P2PArgs &a, int fp64, cudaStream_t st);
 
