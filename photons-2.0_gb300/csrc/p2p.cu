@@ -34,6 +34,18 @@
 #define STAGE32 256  // staged sources per warp, FP32 variant
 #define STAGE64 128  // staged sources per warp, FP64 variant
 
+#ifndef P2P_MINB
+#define P2P_MINB 3  // resident blocks per SM the packed kernel is compiled for (80 registers)
+#endif
+#ifndef P2P_DUAL_UNROLL
+#define P2P_DUAL_UNROLL 2  // two source pairs per step of the dual sweep: four independent chains per lane
+#endif
+constexpr int kDualUnroll = P2P_DUAL_UNROLL;
+#ifndef P2P_ROUND_UNROLL
+#define P2P_ROUND_UNROLL 2
+#endif
+constexpr int kRoundUnroll = P2P_ROUND_UNROLL;
+
 namespace ph {
 namespace {
 
@@ -260,7 +272,7 @@ __device__ __forceinline__ void p2p_round(const float2 *__restrict__ X2, const f
     const float2 a0 = f2(K.as[0]), a1 = f2(K.as[1]), a2 = f2(K.as[2]), a3 = f2(K.as[3]), a4 = f2(K.as[4]),
                  a5 = f2(K.as[5]);
     float2 ax = f2(0.f), ay = f2(0.f), az = f2(0.f);
-#pragma unroll 2
+#pragma unroll kRoundUnroll
     for (int pp = k; pp < npairs; pp += G) {
         const float2 dx = __fadd2_rn(X2[pp], nox);
         const float2 dy = __fadd2_rn(Y2[pp], noy);
@@ -291,6 +303,7 @@ __device__ __forceinline__ void p2p_round_dual(const float2 *__restrict__ X2, co
     const float2 nAx = f2(-oA.x), nAy = f2(-oA.y), nAz = f2(-oA.z);
     const float2 nBx = f2(-oB.x), nBy = f2(-oB.y), nBz = f2(-oB.z);
     float2 ax = f2(0.f), ay = f2(0.f), az = f2(0.f), bx = f2(0.f), by = f2(0.f), bz = f2(0.f);
+#pragma unroll kDualUnroll
     for (int pp = k; pp < npairs; pp += G) {
         const float2 X = X2[pp], Y = Y2[pp], Z = Z2[pp];
 #pragma unroll
@@ -325,7 +338,7 @@ __device__ __forceinline__ float centre_diff(float hs, float ls, float ht, float
     return (hs - ht) + (ls - lt);
 }
 
-__global__ void __launch_bounds__(P2P_TB, 3) k_p2p_split_packed(P2PArgs A)
+__global__ void __launch_bounds__(P2P_TB, P2P_MINB) k_p2p_split_packed(P2PArgs A)
 {
     __shared__ __align__(16) float s_x[P2P_WARPS][STAGE2 + 2];
     __shared__ __align__(16) float s_y[P2P_WARPS][STAGE2 + 2];
