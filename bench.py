@@ -48,6 +48,10 @@ def parse():
     ap.add_argument("--error-bound", type=float, default=1e-4)
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 GPU comparison pass")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--workload", default="zeldovich256", choices=["zeldovich256", "zeldovich512", "nfw128"],
+                    help="zeldovich256: the headline (P(k)~k^-2, seed 3); zeldovich512: P(k)~k^-1.5, seed 5, "
+                         "L=1000 at 512^3; nfw128: 50%% uniform + 50%% in NFW halos, L=200 at 128^3")
+    ap.add_argument("--kdk", action="store_true", help="also time device-resident kick-drift-kick steps")
     return ap.parse_args()
 
 
@@ -58,12 +62,14 @@ def dist_env():
     return rank, world, local
 
 
-def workload(nside, maxleaf, seed_offset=0):
+def workload(nside, maxleaf, seed_offset=0, name="zeldovich256"):
     import __graft_entry__ as g
 
     g.load_package()
     from photons_gb300 import ics
 
+    if name != "zeldovich256":
+        return ics.make(name, nside=nside, maxleaf=maxleaf)
     L = 500.0 * nside / 256
     pos = ics.zeldovich(nside, L, -2.0, seed=3 + seed_offset)
     p = ics.force_params(pos.shape[0], L, nside, theta=0.5, maxleaf=maxleaf)
@@ -173,6 +179,55 @@ def run_reference_arm(args):
     print(json.dumps(line))
 
 
+def kdk_measure(ph, fp, torch, stream, dpos, dacc, n, p, steps):
+    """Device-resident kick-drift-kick steps at a = 0.5 -> 0.505 (the
+    reference's kick_loga / drift_loga factors, G = 43007.105732), and the
+    kick and drift kernels alone against the measured HBM copy bandwidth."""
+    om, ox, G = 0.3, 0.7, 43007.105732
+    la, lb = math.log(0.5), math.log(0.505)
+    dkh = 0.5 * ph.kick_loga(om, ox, la, lb) * G
+    dd = ph.drift_loga(om, ox, la, lb)
+    pos = dpos.clone()
+    acc = dacc.clone()
+    vel = torch.zeros_like(pos)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    fp.kdk_step_device(pos.data_ptr(), vel.data_ptr(), acc.data_ptr(), n, p, dkh, dd, precision=ph.FP32_SPLIT)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        fp.kdk_step_device(pos.data_ptr(), vel.data_ptr(), acc.data_ptr(), n, p, dkh, dd, precision=ph.FP32_SPLIT)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    step_ms = e0.elapsed_time(e1) / steps
+    s = stream.cuda_stream
+    reps = 10
+    e0.record(stream)
+    for _ in range(reps):
+        ph.kick(n, vel.data_ptr(), acc.data_ptr(), 1e-9, s)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    kick_ms = e0.elapsed_time(e1) / reps
+    e0.record(stream)
+    for _ in range(reps):
+        ph.drift(n, pos.data_ptr(), vel.data_ptr(), 1e-9, p["boxsize"], s)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    drift_ms = e0.elapsed_time(e1) / reps
+    bytes_each = 3 * n * 24  # read two arrays, write one, 3n doubles
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    hbm = peaks.get("hbm_gbs")
+    out = {"step_ms": step_ms, "a": [0.5, 0.505], "dkh": dkh, "dd": dd,
+           "kick_ms": kick_ms, "drift_ms": drift_ms,
+           "kick_gbs": bytes_each / (kick_ms * 1e-3) / 1e9, "drift_gbs": bytes_each / (drift_ms * 1e-3) / 1e9,
+           "bytes_per_kernel": bytes_each}
+    if hbm:
+        out["kick_frac_of_measured_hbm"] = out["kick_gbs"] / hbm
+        out["drift_frac_of_measured_hbm"] = out["drift_gbs"] / hbm
+    return out
+
+
 def rel_err(a, b):
     return np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-300)
 
@@ -193,8 +248,10 @@ def main():
     import __graft_entry__ as g
 
     ph = g.load_package()
-    pos, p = workload(args.nside, args.maxleaf or 16, seed_offset=rank)
+    pos, p = workload(args.nside, args.maxleaf or 16, seed_offset=rank, name=args.workload)
     n = pos.shape[0]
+    torch.cuda.synchronize()
+    free0, total_hbm = torch.cuda.mem_get_info()
     fp = ph.ForcePass(local)
     tune = None
     if not args.maxleaf:
@@ -213,6 +270,8 @@ def main():
 
     for _ in range(max(3, args.warmup)):
         step()
+    torch.cuda.synchronize()
+    hbm_used = free0 - torch.cuda.mem_get_info()[0]
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -277,6 +336,14 @@ def main():
         traffic = float(m.group(1)) if m else None
 
     extra = {}
+    kdk = kdk_measure(ph, fp, torch, stream, dpos, dacc, n, p, args.steps) if args.kdk else None
+    rng = np.random.default_rng(7)
+    tgt = rng.choice(n, min(n, 10000), replace=False).astype(np.int32)
+    ds = ph.direct_sum(pos, p, tgt)
+    a32 = rel_err(acc32[tgt], ds)
+    extra["errors"] = {"algorithmic_vs_direct_sum_10k": {
+        "fp32_median": float(np.median(a32)), "fp32_p99": float(np.percentile(a32, 99)),
+        "direct_sum": "FP64 GPU, untruncated erfc kernel, all sources within 2 rcut, minimum image"}}
     if not args.no_fp64:
         fp.run_device(dpos.data_ptr(), dacc.data_ptr(), n, p, precision=ph.FP64)
         torch.cuda.synchronize()
@@ -288,10 +355,6 @@ def main():
         torch.cuda.synchronize()
         ms64 = e0.elapsed_time(e1)
         e = rel_err(acc32, acc64)
-        rng = np.random.default_rng(7)
-        tgt = rng.choice(n, 10000, replace=False).astype(np.int32)
-        ds = ph.direct_sum(pos, p, tgt)
-        a32 = rel_err(acc32[tgt], ds)
         a64 = rel_err(acc64[tgt], ds)
         extra["fp64_gpu"] = {"value": n / (ms64 * 1e-3), "ms_per_pass": ms64, "p2p_ms": t64["p2p"],
                              "speedup_fp32_over_fp64": ms64 / ms}
@@ -309,7 +372,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "zeldovich256", "n": n, "boxsize": p["boxsize"], "mesh": args.nside,
+        "config": {"workload": args.workload, "n": n, "boxsize": p["boxsize"], "mesh": args.nside,
                    "maxleaf": p["maxleaf"], "theta": p["theta"], "rs": p["rs"], "rcut": p["rcut"],
                    "eps": p["eps"], "precision": "fp32-split (fp64 positions and centre differences)",
                    "l2": "inputs larger than L2 (positions %.0f MB), no flush" % (n * 24 / 1e6),
@@ -328,7 +391,12 @@ def main():
         "counters": {k: counters[k] for k in ("idxP2P", "idxM2L", "walk_m2l_count", "p2p_count_remote", "nleaf",
                                               "nnode", "pairs_local", "pairs_image", "depth")},
         "pairs_per_particle": pairs / n,
+        "hbm": {"device_bytes_used": int(hbm_used), "device_bytes_total": int(total_hbm),
+                "what": "device memory taken by the pass context and the resident position/acceleration "
+                        "buffers after warm-up (cudaMemGetInfo difference)"},
     }
+    if kdk:
+        line["kdk"] = kdk
     line.update(extra)
     if tune:
         line["autotune"] = tune

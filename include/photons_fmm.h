@@ -155,6 +155,26 @@ int photons_direct_sum(const photons_params *p, int n, const double *pos, int nt
 int photons_direct_sum_noalloc(const photons_params *p, int n, const double *pos, int nt, const int *targets,
                                double rmax, double *acc, void *cuda_stream);
 
+/* ---- kick-drift-kick integration on device arrays (src/photoNs.c:141-196,
+   257-268).  Products and sums are rounded separately, as in the reference's
+   loops, so a step matches it bit for bit given the same accelerations. ---- */
+/* the reference's kick and drift factors: Simpson's rule over 128 intervals
+   of log a (src/initial.c:639-683); omega_m, omega_x stand for its OmegaM0
+   and OmegaX0 globals.  Host functions. */
+double photons_kick_loga(double omega_m, double omega_x, double loga_i, double loga_f);
+double photons_drift_loga(double omega_m, double omega_x, double loga_i, double loga_f);
+/* vel[3n] += acc[3n] * dkh (src/photoNs.c:164-174); device arrays, 16-byte
+   aligned; enqueued on cuda_stream (NULL: default stream) */
+int photons_kick(int n, double *vel, const double *acc, double dkh, void *cuda_stream);
+/* pos[3n] += vel[3n] * dd, each coordinate then wrapped into [0, boxsize)
+   as src/photoNs.c:176-196 does; enqueued on cuda_stream */
+int photons_drift(int n, double *pos, const double *vel, double dd, double boxsize, void *cuda_stream);
+/* one step on device arrays: kick with acc, drift, force pass into acc (the
+   short-range force; PHOTONS_F_DEVICE_IO implied), kick with the new acc.
+   dkh = kick factor x G / 2, dd = drift factor.  Returns after the step. */
+int photons_kdk_step(photons_ctx *ctx, const photons_params *p, int n, double *pos, double *vel, double *acc,
+                     double dkh, double dd);
+
 /* kernels launched by this library so far (all contexts) */
 unsigned long long photons_launch_count(void);
 

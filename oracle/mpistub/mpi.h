@@ -45,6 +45,7 @@ int MPI_Comm_rank(MPI_Comm c, int *rank);
 int MPI_Comm_dup(MPI_Comm c, MPI_Comm *out);
 int MPI_Type_contiguous(int count, MPI_Datatype old, MPI_Datatype *out);
 int MPI_Type_commit(MPI_Datatype *t);
+int MPI_Type_free(MPI_Datatype *t);
 int MPI_Barrier(MPI_Comm c);
 int MPI_Abort(MPI_Comm c, int code);
 int MPI_Isend(const void *buf, int count, MPI_Datatype t, int dest, int tag, MPI_Comm c, MPI_Request *req);

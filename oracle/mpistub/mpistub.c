@@ -19,6 +19,7 @@ int MPI_Comm_rank(MPI_Comm c, int *rank) { (void)c; *rank = 0; return 0; }
 int MPI_Comm_dup(MPI_Comm c, MPI_Comm *out) { *out = c; return 0; }
 int MPI_Type_contiguous(int count, MPI_Datatype old, MPI_Datatype *out) { *out = (MPI_Datatype)count * old; return 0; }
 int MPI_Type_commit(MPI_Datatype *t) { (void)t; return 0; }
+int MPI_Type_free(MPI_Datatype *t) { (void)t; return 0; }
 int MPI_Barrier(MPI_Comm c) { (void)c; return 0; }
 int MPI_Abort(MPI_Comm c, int code) { (void)c; fprintf(stderr, "MPI_Abort(%d)\n", code); exit(code); }
 

@@ -93,7 +93,9 @@ class RefOracle(_Base):
     def __init__(self):
         if not ref_available():
             raise FileNotFoundError(REF_SO)
-        lib = C.CDLL(REF_SO)
+        # The GPU library defines the same FMM entry points and globals; bind
+        # the reference's calls to its own definitions whatever was loaded first.
+        lib = C.CDLL(REF_SO, mode=os.RTLD_LOCAL | getattr(os, "RTLD_DEEPBIND", 0))
         lib.ref_run.restype = C.c_double
         lib.ref_run.argtypes = [C.c_int, _dp, C.c_double, C.c_int, C.c_double, C.c_double,
                                 C.c_double, C.c_double, C.c_double, C.c_int, _dp, _dp, _dp, _lp]
@@ -107,7 +109,16 @@ class RefOracle(_Base):
         lib.ref_l2l.argtypes = [C.c_double] * 3 + [_dp, _dp]
         lib.ref_acceptance.restype = C.c_int
         lib.ref_acceptance.argtypes = [_dp, _dp, _dp, C.c_double, C.c_double]
+        for name in ("ref_kick_loga", "ref_drift_loga"):
+            getattr(lib, name).restype = C.c_double
+            getattr(lib, name).argtypes = [C.c_double] * 4
         self.lib = lib
+
+    def kick_loga(self, om, ox, la, lb):
+        return self.lib.ref_kick_loga(om, ox, la, lb)
+
+    def drift_loga(self, om, ox, la, lb):
+        return self.lib.ref_drift_loga(om, ox, la, lb)
 
     def run(self, pos, p, capture=True, tree=True):
         pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
@@ -177,6 +188,11 @@ class PortOracle(_Base):
         lib.po_acceptance.argtypes = [_dp, _dp, _dp, C.c_double, C.c_double]
         lib.po_direct_sum.restype = C.c_int
         lib.po_direct_sum.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, _ip, C.c_double, _dp]
+        for name in ("po_kick_loga", "po_drift_loga"):
+            getattr(lib, name).restype = C.c_double
+            getattr(lib, name).argtypes = [C.c_double] * 4
+        lib.po_kick.argtypes = [C.c_longlong, _dp, _dp, C.c_double]
+        lib.po_drift.argtypes = [C.c_longlong, _dp, _dp, C.c_double, C.c_double]
         self.lib = lib
         self.state = C.c_void_p(lib.po_create())
 
@@ -234,6 +250,24 @@ class PortOracle(_Base):
         shim.po_copy_leaves = lambda *a: self.lib.po_copy_leaves(self.state, *a)
         shim.po_copy_nodes = lambda *a: self.lib.po_copy_nodes(self.state, *a)
         return self._tree(shim, "po_", counters)
+
+    def kick_loga(self, om, ox, la, lb):
+        return self.lib.po_kick_loga(om, ox, la, lb)
+
+    def drift_loga(self, om, ox, la, lb):
+        return self.lib.po_drift_loga(om, ox, la, lb)
+
+    def kick(self, vel, acc, dkh):
+        """vel += acc dkh in place (float64 arrays of equal size)."""
+        assert vel.dtype == np.float64 and vel.flags.c_contiguous
+        acc = np.ascontiguousarray(acc, np.float64)
+        self.lib.po_kick(vel.size, _ptr(vel), _ptr(acc), dkh)
+
+    def drift(self, pos, vel, dd, L):
+        """pos += vel dd in place, wrapped into [0, L)."""
+        assert pos.dtype == np.float64 and pos.flags.c_contiguous
+        vel = np.ascontiguousarray(vel, np.float64)
+        self.lib.po_drift(pos.size, _ptr(pos), _ptr(vel), dd, L)
 
     def direct_sum(self, pos, p, targets, rmax=None, nthreads=1):
         pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)

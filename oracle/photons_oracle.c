@@ -1014,3 +1014,55 @@ int po_direct_sum(const po_params *p, int n, const double *pos, int nt, const in
     free(next);
     return PO_OK;
 }
+
+/* ------------------------------------------------------------------ */
+/* time integration                                                     */
+/* ------------------------------------------------------------------ */
+
+/* Simpson's rule with 128 intervals in log a of z^zpow / h, h = 0.1 sqrt(Om z^3
+   + OL), z = 1/a; weights 1, 4, 2, 4, ..., 4, 1 accumulated in index order
+   (src/initial.c:639-683, whose kick uses zpow 1 and drift zpow 2). */
+static double po_loga_simpson(double om, double ox, double la, double lb, int zpow)
+{
+    const int nb = 128;
+    double dl = (lb - la) / nb;
+    double z = 1.0 / exp(la);
+    double h = 0.1 * sqrt(om * z * z * z + ox);
+    double acc = zpow == 1 ? dl * z / h : dl * z * z / h;
+    for (int k = 1; k < nb; k++) {
+        z = 1.0 / (exp(la + dl * k));
+        h = 0.1 * sqrt(om * z * z * z + ox);
+        acc += zpow == 1 ? 2.0 * (1 + k % 2) * dl * z / h : 2.0 * (1 + k % 2) * dl * z * z / h;
+    }
+    z = 1.0 / exp(lb);
+    h = 0.1 * sqrt(om * z * z * z + ox);
+    acc += zpow == 1 ? dl * z / h : dl * z * z / h;
+    return acc / 3.0;
+}
+
+double po_kick_loga(double omega_m, double omega_x, double loga_i, double loga_f)
+{
+    return po_loga_simpson(omega_m, omega_x, loga_i, loga_f, 1);
+}
+
+double po_drift_loga(double omega_m, double omega_x, double loga_i, double loga_f)
+{
+    return po_loga_simpson(omega_m, omega_x, loga_i, loga_f, 2);
+}
+
+/* src/photoNs.c:164-174: one velocity update per coordinate */
+void po_kick(long long m, double *vel, const double *acc, double dkh)
+{
+    for (long long i = 0; i < m; i++) vel[i] += acc[i] * dkh;
+}
+
+/* src/photoNs.c:176-196: move, then bring each coordinate back into [0, L) */
+void po_drift(long long m, double *pos, const double *vel, double dd, double L)
+{
+    for (long long i = 0; i < m; i++) {
+        double x = pos[i] + vel[i] * dd;
+        while (x < 0.0) x += L;
+        while (x >= L) x -= L;
+        pos[i] = x;
+    }
+}

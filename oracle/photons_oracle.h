@@ -73,6 +73,14 @@ int po_acceptance(const double wi[3], const double wj[3], const double dist[3], 
 int po_direct_sum(const po_params *p, int n, const double *pos, int nt, const int *targets,
                   double rmax, double *acc_out);
 
+/* time integration (src/photoNs.c:141-196, 257-268; src/initial.c:639-683):
+   the kick and drift factors over [loga_i, loga_f], and the kick / drift
+   updates of m = 3n coordinates (drift wraps into [0, L)) */
+double po_kick_loga(double omega_m, double omega_x, double loga_i, double loga_f);
+double po_drift_loga(double omega_m, double omega_x, double loga_i, double loga_f);
+void po_kick(long long m, double *vel, const double *acc, double dkh);
+void po_drift(long long m, double *pos, const double *vel, double dd, double L);
+
 #ifdef __cplusplus
 }
 #endif

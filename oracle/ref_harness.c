@@ -257,3 +257,24 @@ int ref_acceptance(double *wi, double *wj, double *dist, double theta, double rc
     open_angle = theta; cutoffRadius = rcut;
     return acceptance(wi, wj, dist);
 }
+
+/* The reference's time integrals (src/initial.c:639-683) read OmegaM0 and
+   OmegaX0; initial.c and snapshot.c are compiled in only for them.  The
+   2DECOMP&FFT call of initialize_nbody is never reached here. */
+double kick_loga(double loga_i, double loga_f);
+double drift_loga(double loga_i, double loga_f);
+void get_local_size_(void) {}
+
+double ref_kick_loga(double omega_m, double omega_x, double loga_i, double loga_f)
+{
+    OmegaM0 = omega_m;
+    OmegaX0 = omega_x;
+    return kick_loga(loga_i, loga_f);
+}
+
+double ref_drift_loga(double omega_m, double omega_x, double loga_i, double loga_f)
+{
+    OmegaM0 = omega_m;
+    OmegaX0 = omega_x;
+    return drift_loga(loga_i, loga_f);
+}

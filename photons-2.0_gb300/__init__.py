@@ -101,6 +101,13 @@ def load_library():
     lib.acceptance.restype = C.c_int
     lib.acceptance.argtypes = [_dp, _dp, _dp]
     lib.fmm_remote.argtypes = [C.c_int, _dp]
+    for name in ("photons_kick_loga", "photons_drift_loga"):
+        getattr(lib, name).restype = C.c_double
+        getattr(lib, name).argtypes = [C.c_double] * 4
+    lib.photons_kick.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]
+    lib.photons_drift.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_void_p]
+    lib.photons_kdk_step.argtypes = [C.c_void_p, C.POINTER(Params), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.c_double, C.c_double]
     _lib = lib
     return lib
 
@@ -160,6 +167,14 @@ class ForcePass:
         """Device pointers (e.g. torch tensors' data_ptr()), AoS (n,3) float64."""
         prm = make_params(p, precision, image_mask, flags | F_DEVICE_IO)
         _check(self.lib.photons_force_pass(self.h, C.byref(prm), int(n), C.c_void_p(pos_ptr), C.c_void_p(acc_ptr)))
+        self.n = n
+
+    def kdk_step_device(self, pos_ptr, vel_ptr, acc_ptr, n, p, dkh, dd, precision=FP32_SPLIT, image_mask=0, flags=0):
+        """One kick-drift-kick step on device arrays (n,3) float64: vel += acc dkh,
+        pos += vel dd (wrapped), acc = forces at the new positions, vel += acc dkh."""
+        prm = make_params(p, precision, image_mask, flags | F_DEVICE_IO)
+        _check(self.lib.photons_kdk_step(self.h, C.byref(prm), int(n), C.c_void_p(pos_ptr), C.c_void_p(vel_ptr),
+                                         C.c_void_p(acc_ptr), float(dkh), float(dd)))
         self.n = n
 
     def counters(self):
@@ -237,6 +252,28 @@ def direct_sum(pos, p, targets, rmax=None):
     _check(lib.photons_direct_sum(C.byref(prm), pos.shape[0], _p(pos), targets.size, _p(targets, _ip),
                                   float(rmax), _p(out)))
     return out
+
+
+def kick_loga(omega_m, omega_x, loga_i, loga_f):
+    """The reference's kick factor over [loga_i, loga_f] (src/initial.c:639-660)."""
+    return load_library().photons_kick_loga(float(omega_m), float(omega_x), float(loga_i), float(loga_f))
+
+
+def drift_loga(omega_m, omega_x, loga_i, loga_f):
+    """The reference's drift factor over [loga_i, loga_f] (src/initial.c:662-683)."""
+    return load_library().photons_drift_loga(float(omega_m), float(omega_x), float(loga_i), float(loga_f))
+
+
+def kick(n, vel_ptr, acc_ptr, dkh, stream_ptr=0):
+    """vel += acc dkh on device arrays (n,3) float64 (asynchronous on the stream)."""
+    _check(load_library().photons_kick(int(n), C.c_void_p(vel_ptr), C.c_void_p(acc_ptr), float(dkh),
+                                       C.c_void_p(stream_ptr)))
+
+
+def drift(n, pos_ptr, vel_ptr, dd, boxsize, stream_ptr=0):
+    """pos += vel dd, wrapped into [0, boxsize), on device arrays (asynchronous)."""
+    _check(load_library().photons_drift(int(n), C.c_void_p(pos_ptr), C.c_void_p(vel_ptr), float(dd),
+                                        float(boxsize), C.c_void_p(stream_ptr)))
 
 
 def fp32_fma_peak(iters=4096):

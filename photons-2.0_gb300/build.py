@@ -18,9 +18,12 @@ LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libphotons_fmm.so")
 INCLUDE = os.path.join(ROOT, "include")
 
-SOURCES = ["scan.cu", "tree.cu", "walk.cu", "p2p.cu", "multipole.cu", "api.cu", "legacy.cu", "direct.cu", "noalloc.cu"]
+SOURCES = ["scan.cu", "tree.cu", "walk.cu", "p2p.cu", "multipole.cu", "api.cu", "legacy.cu", "direct.cu", "noalloc.cu", "integrate.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code is not contracted into FMAs (the host operators and integrals
+# follow the reference's separately rounded arithmetic on every host CPU)
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=default",
+         "-Xcompiler", "-ffp-contract=off",
          "-I" + INCLUDE, "-I" + CSRC, "-diag-suppress", "177"]
 
 

@@ -88,11 +88,6 @@ static void dfree(T *&p)
     p = nullptr;
 }
 
-#define PH_TRY(x)               \
-    do {                        \
-        int rc__ = (x);         \
-        if (rc__) return rc__;  \
-    } while (0)
 
 #define CHUNK_ELEMS 1024
 #define MAX_DEPTH_CAP 2048
@@ -417,8 +412,11 @@ static void walk_caps(photons_ctx *c, long long &p2p_cap, long long &pd_cap, lon
                       int &stage_cap)
 {
     const long long n = c->n;
-    p2p_cap = c->hint_p2p ? c->hint_p2p : n * 32 + 4096;
-    pd_cap = c->hint_pd ? c->hint_pd : n * 16 + 4096;
+    // first-pass guesses: entries per particle fall as leaves grow (about
+    // 130 list entries per target leaf at leaf 16-64); an overflow grows them
+    const long long per = c->pp.maxleaf > 16 ? c->pp.maxleaf : 16;
+    p2p_cap = c->hint_p2p ? c->hint_p2p : n * 32 * 16 / per + 4096;
+    pd_cap = c->hint_pd ? c->hint_pd : n * 16 * 16 / per + 4096;
     m2l_cap = c->hint_m2l ? c->hint_m2l : n * 2 + 4096;
     stack_cap = c->w.stack_cap ? c->w.stack_cap : 4096;
     stage_cap = c->w.stage_cap ? c->w.stage_cap : 16384;

@@ -69,6 +69,13 @@ struct photons_ctx {
     PassKey key{};
 };
 
+// return a nonzero status code from the enclosing function
+#define PH_TRY(x)               \
+    do {                        \
+        int rc__ = (x);         \
+        if (rc__) return rc__;  \
+    } while (0)
+
 struct HostTree {
     int nleaf = 0, nnode = 0;
     std::vector<int> ipart, npart, son0, son1, parent;

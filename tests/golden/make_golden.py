@@ -90,5 +90,25 @@ def main():
             name, pos.shape[0], c["idxP2P"], c["idxM2L"], c["n_p2p_ext"], c["n_m2l_ext"], os.path.getsize(path) / 1024))
 
 
+def time_integrals():
+    """The reference's kick_loga / drift_loga (src/initial.c:639-683) over a
+    spread of steps and cosmologies -> time/loga_integrals.npz."""
+    ref = oracle.RefOracle()
+    rng = np.random.default_rng(21)
+    rows = []
+    for om in (0.3, 0.25, 1.0):
+        ox = 1.0 - om
+        for _ in range(8):
+            a0 = float(np.exp(rng.uniform(np.log(0.01), np.log(0.9))))
+            a1 = a0 * float(np.exp(rng.uniform(1e-3, 0.2)))
+            la, lb = np.log(a0), np.log(a1)
+            rows.append([om, ox, la, lb, ref.kick_loga(om, ox, la, lb), ref.drift_loga(om, ox, la, lb)])
+    os.makedirs(os.path.join(HERE, "time"), exist_ok=True)
+    path = os.path.join(HERE, "time", "loga_integrals.npz")
+    np.savez_compressed(path, rows=np.array(rows))
+    print("time/loga_integrals  %d rows" % len(rows))
+
+
 if __name__ == "__main__":
     main()
+    time_integrals()

@@ -1,0 +1,121 @@
+"""Kick-drift-kick integration (src/photoNs.c:141-196, 257-268;
+src/initial.c:639-683): the time integrals on the host, the kick and drift
+kernels and one device-resident step.
+
+CPU tests pin the oracle's restatement of kick_loga / drift_loga, and the
+library's host copy, to the reference (compiled in place when present, else
+the committed golden values).  GPU tests compare the kernels and the step
+with the oracle's kick / drift loops and a host-composed step, bit for bit.
+"""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+
+def _golden_rows():
+    return np.load(os.path.join(GOLDEN, "time", "loga_integrals.npz"))["rows"]
+
+
+def test_loga_integrals_golden(port, ph):
+    for om, ox, la, lb, kick, drift in _golden_rows():
+        assert port.kick_loga(om, ox, la, lb) == kick
+        assert port.drift_loga(om, ox, la, lb) == drift
+        assert ph.kick_loga(om, ox, la, lb) == kick
+        assert ph.drift_loga(om, ox, la, lb) == drift
+
+
+def test_loga_integrals_match_reference(port, oracle_mod):
+    try:
+        ref = oracle_mod.RefOracle()
+    except FileNotFoundError:
+        pytest.skip("reference build not present")
+    rng = np.random.default_rng(5)
+    for _ in range(20):
+        om = float(rng.uniform(0.1, 1.0))
+        a0 = float(np.exp(rng.uniform(math.log(0.005), math.log(1.0))))
+        la, lb = math.log(a0), math.log(a0) + float(rng.uniform(1e-4, 0.3))
+        assert port.kick_loga(om, 1 - om, la, lb) == ref.kick_loga(om, 1 - om, la, lb)
+        assert port.drift_loga(om, 1 - om, la, lb) == ref.drift_loga(om, 1 - om, la, lb)
+
+
+def test_loga_integrals_match_quadrature(port):
+    """Independent check of the integrands: the Simpson sums over 128
+    intervals agree to 1e-9 with adaptive quadrature of the integrals over
+    log a of z/h (kick) and z^2/h (drift), h = 0.1 sqrt(Om z^3 + OL)."""
+    scipy_integrate = pytest.importorskip("scipy.integrate")
+    om, ox = 0.3, 0.7
+    la, lb = math.log(0.5), math.log(0.6)
+
+    def h(l):
+        z = math.exp(-l)
+        return 0.1 * math.sqrt(om * z ** 3 + ox)
+
+    kick = scipy_integrate.quad(lambda l: math.exp(-l) / h(l), la, lb, epsabs=0, epsrel=1e-13)[0]
+    drift = scipy_integrate.quad(lambda l: math.exp(-2 * l) / h(l), la, lb, epsabs=0, epsrel=1e-13)[0]
+    assert abs(port.kick_loga(om, ox, la, lb) / kick - 1) < 1e-9
+    assert abs(port.drift_loga(om, ox, la, lb) / drift - 1) < 1e-9
+
+
+def test_oracle_drift_wraps_like_the_reference(port):
+    L = 10.0
+    pos = np.array([0.1, 9.9, 5.0, 0.0, 9.999999999999998, 3.0])
+    vel = np.array([-1.0, 1.0, 26.0, -1e-300, 0.0, -33.0])
+    port.drift(pos, vel, 0.5, L)
+    assert np.all((pos >= 0) & (pos < L))
+    assert pos[0] == -0.4 + L and pos[2] == (5.0 + 13.0) - L
+
+
+@pytest.mark.gpu
+def test_kick_drift_kernels_match_oracle(ph, port):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(9)
+    n = 100003  # odd coordinate count exercises the tail
+    L = 37.5
+    pos = rng.random((n, 3)) * L
+    pos[:100] = rng.choice([0.0, L * (1 - 1e-16), 1e-12, L - 1e-12], size=(100, 3))
+    vel = rng.standard_normal((n, 3)) * 3.0
+    vel[:50] *= 40.0  # several box lengths per step
+    acc = rng.standard_normal((n, 3))
+    dkh, dd = 0.0173, 0.91
+    dpos, dvel, dacc = (torch.from_numpy(a.copy()).cuda() for a in (pos, vel, acc))
+    ph.kick(n, dvel.data_ptr(), dacc.data_ptr(), dkh)
+    ph.drift(n, dpos.data_ptr(), dvel.data_ptr(), dd, L)
+    torch.cuda.synchronize()
+    port.kick(vel, acc, dkh)
+    port.drift(pos, vel, dd, L)
+    assert np.array_equal(dvel.cpu().numpy(), vel)
+    assert np.array_equal(dpos.cpu().numpy(), pos)
+    assert pos.min() >= 0 and pos.max() < L
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["FP64", "FP32_SPLIT"])
+def test_kdk_step_matches_host_composition(ph, port, ics, precision):
+    """photons_kdk_step == kick (oracle) + drift (oracle) + force pass + kick."""
+    torch = pytest.importorskip("torch")
+    pos, p = ics.make("zeldovich512", nside=24, maxleaf=16)
+    rng = np.random.default_rng(3)
+    vel = rng.standard_normal(pos.shape) * 0.5
+    prec = getattr(ph, precision)
+    om, ox = 0.3, 0.7
+    la, lb = math.log(0.5), math.log(0.505)
+    G = 43007.105732
+    dkh = 0.5 * ph.kick_loga(om, ox, la, lb) * G
+    dd = ph.drift_loga(om, ox, la, lb)
+    fp = ph.ForcePass(0)
+    acc0 = fp.run(pos, p, precision=prec)
+    dpos, dvel, dacc = (torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (pos, vel, acc0))
+    torch.cuda.synchronize()
+    fp.kdk_step_device(dpos.data_ptr(), dvel.data_ptr(), dacc.data_ptr(), pos.shape[0], p, dkh, dd, precision=prec)
+    hp, hv = pos.copy(), vel.copy()
+    port.kick(hv, acc0, dkh)
+    port.drift(hp, hv, dd, p["boxsize"])
+    acc1 = fp.run(hp, p, precision=prec)
+    port.kick(hv, acc1, dkh)
+    assert np.array_equal(dpos.cpu().numpy(), hp)
+    assert np.array_equal(dacc.cpu().numpy(), acc1)
+    assert np.array_equal(dvel.cpu().numpy(), hv)
