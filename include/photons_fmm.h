@@ -104,6 +104,17 @@ int photons_set_stream(photons_ctx *ctx, void *cuda_stream);
    Host or device pointers per PHOTONS_F_DEVICE_IO. */
 int photons_force_pass(photons_ctx *ctx, const photons_params *p, int n, const double *pos, double *acc);
 
+/* One pass over nbox independent periodic boxes in one launch per operator:
+   box b holds counts[b] particles, stored after those of boxes 0..b-1 in
+   pos[3 sum(counts)] (acc likewise).  params[b] gives each box's side, rs,
+   rcut, softening and mass; theta, maxleaf, precision, image_mask and flags
+   must be the same in every entry.  Each box is its own tree and periodic
+   domain (one root per box; images shift by that box's side), so the
+   result equals nbox separate passes.  No counterpart in the reference,
+   which evaluates one domain per rank. */
+int photons_force_pass_boxes(photons_ctx *ctx, int nbox, const photons_params *params, const int *counts,
+                             const double *pos, double *acc);
+
 /* counters[32] after a pass: idxP2P, idxM2L, walk_m2l_count, p2p_count_remote,
    NLEAF, NNODE, nleaf, nnode, first_leaf, first_node, direct_local_start,
    n_p2p, n_m2l, n_p2p_ext, n_m2l_ext, n_images, local pairs, image pairs,

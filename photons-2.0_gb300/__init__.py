@@ -78,6 +78,7 @@ def load_library():
     lib.photons_destroy.argtypes = [C.c_void_p]
     lib.photons_set_stream.argtypes = [C.c_void_p, C.c_void_p]
     lib.photons_force_pass.argtypes = [C.c_void_p, C.POINTER(Params), C.c_int, C.c_void_p, C.c_void_p]
+    lib.photons_force_pass_boxes.argtypes = [C.c_void_p, C.c_int, C.POINTER(Params), _ip, C.c_void_p, C.c_void_p]
     lib.photons_get_counters.argtypes = [C.c_void_p, _lp, C.c_int]
     lib.photons_get_timings.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.c_int]
     lib.photons_get_perm.argtypes = [C.c_void_p, _ip]
@@ -162,6 +163,22 @@ class ForcePass:
         _check(self.lib.photons_force_pass(self.h, C.byref(prm), n, pos.ctypes.data, acc.ctypes.data))
         self.n = n
         return acc
+
+    def run_boxes(self, boxes, precision=FP32_SPLIT, image_mask=0, flags=0):
+        """Independent periodic boxes in one pass: boxes = [(pos (n_b,3), params_b), ...]
+        -> list of acc (n_b,3).  theta and maxleaf are taken from the first box."""
+        nb = len(boxes)
+        counts = np.array([b[0].shape[0] for b in boxes], np.int32)
+        pos = np.ascontiguousarray(np.concatenate([np.asarray(b[0], np.float64).reshape(-1, 3) for b in boxes]))
+        acc = np.empty_like(pos)
+        p0 = boxes[0][1]
+        prm = (Params * nb)()
+        for i, (_, p) in enumerate(boxes):
+            q = dict(p, theta=p0["theta"], maxleaf=p0["maxleaf"])
+            prm[i] = make_params(q, precision, image_mask, flags & ~F_DEVICE_IO)
+        _check(self.lib.photons_force_pass_boxes(self.h, nb, prm, _p(counts, _ip), pos.ctypes.data, acc.ctypes.data))
+        self.n = pos.shape[0]
+        return np.split(acc, np.cumsum(counts)[:-1])
 
     def run_device(self, pos_ptr, acc_ptr, n, p, precision=FP32_SPLIT, image_mask=0, flags=0):
         """Device pointers (e.g. torch tensors' data_ptr()), AoS (n,3) float64."""

@@ -8,11 +8,14 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
+#include <cstdint>
 #include <cstring>
 #include <vector>
 
 #include "photons_fmm.h"
 #include "api_internal.cuh"
+#include "p2p.cuh"
+#include "split_kernel_coeffs.h"
 
 // ------------------------------------------------------------------
 // errors
@@ -121,6 +124,7 @@ static int alloc_tree(photons_ctx *c, int n, int cap)
         PH_TRY(dalloc(b.tn_pre, cap)); PH_TRY(dalloc(b.tn_lbase, cap));
         PH_TRY(dalloc(b.tl_start, cap)); PH_TRY(dalloc(b.tl_len, cap)); PH_TRY(dalloc(b.tl_depth, cap));
         PH_TRY(dalloc(b.tl_parent, cap)); PH_TRY(dalloc(b.tl_final, cap)); PH_TRY(dalloc(b.tl_box, (size_t)6 * cap));
+        PH_TRY(dalloc(b.tn_boxid, cap)); PH_TRY(dalloc(b.tl_boxid, cap));
         b.scan_scratch_elems = ph::scan_scratch_elems(cap > chunks ? cap : chunks) + 8;
         PH_TRY(dalloc(b.scan_scratch, b.scan_scratch_elems));
         PH_TRY(dalloc(b.cnt, ph::BC_NCOUNTERS));
@@ -148,6 +152,7 @@ static int alloc_tree(photons_ctx *c, int n, int cap)
         PH_TRY(dalloc(w.p2p_off, cu)); PH_TRY(dalloc(w.p2p_cnt, cu));
         PH_TRY(dalloc(w.m2l_off, cu)); PH_TRY(dalloc(w.m2l_cnt, cu));
         PH_TRY(dalloc(t.chi, cu)); PH_TRY(dalloc(t.clo, cu)); PH_TRY(dalloc(t.w32, cu)); PH_TRY(dalloc(t.son2, cu));
+        PH_TRY(dalloc(t.boxid, cu));
         PH_TRY(dalloc(c->M, (size_t)cu * PH_NMULTI));
         PH_TRY(dalloc(c->L, (size_t)cu * PH_NMULTI));
         PH_TRY(dalloc(c->M32, (size_t)cu * PH_NMULTI));
@@ -210,7 +215,8 @@ static void free_all(photons_ctx *c)
                     c->w.pd_pool[1], c->w.pd_off, c->w.pd_cnt, c->w.p2p_pool, c->w.p2p_off, c->w.p2p_cnt,
                     c->w.m2l_pool, c->w.m2l_off, c->w.m2l_cnt, c->w.scratch, c->w.ctr, c->pos4, c->ax, c->ay,
                     c->az, c->M, c->L, c->io, c->work_counter, c->t.chi, c->t.clo, c->t.w32, c->t.son2, c->M32,
-                    b.lvl_begin, b.lvl_count, b.leaf_begin, b.leaf_count, c->t.depth_cnt};
+                    b.lvl_begin, b.lvl_count, b.leaf_begin, b.leaf_count, c->t.depth_cnt, b.tn_boxid, b.tl_boxid,
+                    c->t.boxid, b.boxes};
     for (void *p : ptrs)
         if (p) cudaFree(p);
 }
@@ -285,15 +291,83 @@ static int estimate_levels(int n, int maxleaf)
 }
 
 // validation, capacities and parameters of a pass over n particles
-static int ph_prepare(photons_ctx *c, const photons_params *p, int n)
+// the reference's 2N/MAXLEAF node and leaf capacity of one box (src/fmm.c:203-209)
+static int box_cap(int n, int maxleaf)
 {
-    PH_TRY(ph_validate(p, n));
-    int cap = (int)(2.0 * ((double)n) / ((double)p->maxleaf));  // src/fmm.c:203-209
+    int cap = (int)(2.0 * ((double)n) / ((double)maxleaf));
     if (cap > n) cap = n + 1;
     if (cap < 1) cap = 1;
-    PH_TRY(alloc_particles(c, n));
-    PH_TRY(alloc_tree(c, n, cap));
-    c->b.rule_cap = cap;
+    return cap;
+}
+
+// the per-box constants every kernel reads (host side of BoxParams)
+static BoxParams box_params(const photons_params *p, int first, int count)
+{
+    BoxParams B;
+    memset(&B, 0, sizeof B);
+    B.boxsize = p->boxsize;
+    B.rs = p->rs;
+    B.rcut = p->rcut;
+    B.eps = p->eps;
+    B.mass = p->mass;
+    B.rcut2 = p->rcut * p->rcut;
+    B.Lhi = (float)p->boxsize;
+    B.Llo = (float)(p->boxsize - (double)B.Lhi);
+    B.c2f = (float)(p->rcut * p->rcut);
+    PassParams pp{};
+    pp.boxsize = p->boxsize; pp.theta = p->theta; pp.rs = p->rs; pp.rcut = p->rcut; pp.eps = p->eps;
+    pp.mass = p->mass; pp.maxleaf = p->maxleaf;
+    const ph::SplitConsts k = ph::make_split_consts(pp);
+    B.sig = k.sig;
+    B.e2s = k.e2s;
+    B.pias = k.pias;
+    B.cs = k.cs;
+    const double sig = ph::split_sig(pp);
+    B.acc_scale = p->mass * sig * sig;
+    const double ia = 0.5 / p->rs;
+    B.far_a = (float)ia;
+    B.far_pa = (float)(SPLIT_P * ia);
+    B.first = first;
+    B.count = count;
+    B.root = -1;
+    return B;
+}
+
+// Validation, capacities, the box table and the pass-wide parameters of a
+// pass over nbox boxes (counts[b] particles each, concatenated).  Boxes may
+// differ in side, rs, rcut, softening and mass; theta, MAXLEAF, precision,
+// image mask and flags are those of the pass.
+static int ph_prepare_boxes(photons_ctx *c, int nbox, const photons_params *p, const int *counts)
+{
+    if (nbox < 1 || !p || !counts) return ph_set_error(PH_ERR_ARG, "bad box list");
+    long long n = 0, cap = 0;
+    for (int b = 0; b < nbox; b++) {
+        if (p[b].theta != p[0].theta || p[b].maxleaf != p[0].maxleaf || p[b].precision != p[0].precision ||
+            p[b].image_mask != p[0].image_mask || p[b].flags != p[0].flags)
+            return ph_set_error(PH_ERR_ARG, "box %d: theta, MAXLEAF, precision, image mask and flags must match "
+                                            "those of box 0", b);
+        PH_TRY(ph_validate(&p[b], counts[b]));
+        n += counts[b];
+        cap += box_cap(counts[b], p[b].maxleaf);
+    }
+    if (n > INT32_MAX / 3) return ph_set_error(PH_ERR_ARG, "%lld particles in one pass exceed the supported count", n);
+    photons_params all = p[0];
+    PH_TRY(ph_validate(&all, (int)n));  // the 27-bit id space over all boxes
+    PH_TRY(alloc_particles(c, (int)n));
+    PH_TRY(alloc_tree(c, (int)n, (int)cap));
+    if (nbox > c->cap_box) {
+        PH_TRY(dalloc(c->b.boxes, nbox));
+        c->cap_box = nbox;
+        c->epoch++;
+    }
+    c->h_boxes.resize(nbox);
+    int first = 0;
+    for (int b = 0; b < nbox; b++) {
+        c->h_boxes[b] = box_params(&p[b], first, counts[b]);
+        first += counts[b];
+    }
+    c->b.nbox = nbox;
+    c->b.rule_cap = (int)cap;
     c->pp.boxsize = p->boxsize;
     c->pp.theta = p->theta;
     c->pp.rs = p->rs;
@@ -302,9 +376,22 @@ static int ph_prepare(photons_ctx *c, const photons_params *p, int n)
     c->pp.mass = p->mass;
     c->pp.maxleaf = p->maxleaf;
     c->pp.images = 1;
-    c->n = n;
-    c->info.nleaf_cap = c->info.nnode_cap = cap;
+    c->n = (int)n;
+    c->info.nleaf_cap = c->info.nnode_cap = (int)cap;
     c->have_tree = c->have_lists = c->have_multipoles = false;
+    return 0;
+}
+
+static int ph_prepare(photons_ctx *c, const photons_params *p, int n)
+{
+    return ph_prepare_boxes(c, 1, p, &n);
+}
+
+// the box table for this pass (before the build; the build writes the roots)
+static int ph_upload_boxes(photons_ctx *c)
+{
+    PH_CUDA_CHECK(cudaMemcpyAsync(c->b.boxes, c->h_boxes.data(), sizeof(BoxParams) * c->h_boxes.size(),
+                                  cudaMemcpyHostToDevice, c->stream));
     return 0;
 }
 
@@ -313,7 +400,7 @@ static int ph_enqueue_tree(photons_ctx *c, const double *src, int levels)
 {
     cudaStream_t st = c->stream;
     PH_TRY(ph::launch_init_particles(c->b, src, c->n, st));
-    PH_TRY(ph::build_tree(c->b, c->t, c->pp, c->n, levels, st));
+    PH_TRY(ph::build_tree(c->b, c->t, c->pp, levels, st));
     PH_TRY(ph::launch_geom32(c->t, c->b.cnt, st));
     PH_TRY(ph::launch_leaf_offsets(c->b, c->t, c->pos4, st));
     c->ndepth = levels + 1;
@@ -350,10 +437,13 @@ static void ph_tree_info_from(photons_ctx *c, const int *h, int levels)
     else c->hint_levels = levels;
 }
 
-int ph_stage_build(photons_ctx *c, const photons_params *p, int n, const double *pos, int device_io)
+static int ph_stage_build_boxes(photons_ctx *c, int nbox, const photons_params *p, const int *counts,
+                                const double *pos, int device_io)
 {
-    PH_TRY(ph_prepare(c, p, n));
+    PH_TRY(ph_prepare_boxes(c, nbox, p, counts));
+    const int n = c->n;
     cudaStream_t st = c->stream;
+    PH_TRY(ph_upload_boxes(c));
     const double *src = pos;
     PH_TRY(ph_record(c, EV_START));
     if (!device_io) {
@@ -383,6 +473,11 @@ int ph_stage_build(photons_ctx *c, const photons_params *p, int n, const double 
     }
     c->have_tree = true;
     return 0;
+}
+
+int ph_stage_build(photons_ctx *c, const photons_params *p, int n, const double *pos, int device_io)
+{
+    return ph_stage_build_boxes(c, 1, p, &n, pos, device_io);
 }
 
 // list-pool sizes after an overflowed walk
@@ -437,7 +532,7 @@ int ph_stage_walk(photons_ctx *c, unsigned mask)
     walk_caps(c, p2p_cap, pd_cap, m2l_cap, stack_cap, stage_cap);
     for (int attempt = 0; attempt < 6; attempt++) {
         PH_TRY(alloc_walk(c, p2p_cap, pd_cap, m2l_cap, stack_cap, stage_cap));
-        PH_TRY(ph::walk_lists(c->w, c->t, c->b.cnt, c->ndepth, c->pp, mask, c->stream));
+        PH_TRY(ph::walk_lists(c->w, c->t, c->b.cnt, c->b.boxes, c->ndepth, c->pp, mask, c->stream));
         PH_CUDA_CHECK(cudaMemcpyAsync(c->ws.c, c->w.ctr, sizeof(c->ws.c), cudaMemcpyDeviceToHost, c->stream));
         PH_CUDA_CHECK(cudaStreamSynchronize(c->stream));
         unsigned long long fl = c->ws.c[ph::WC_FLAGS];
@@ -467,6 +562,9 @@ int ph_stage_p2p(photons_ctx *c, int precision, int zero)
     a.cx = c->t.cx; a.cy = c->t.cy; a.cz = c->t.cz;
     a.tree_cnt = c->b.cnt;
     a.walk_flags = c->w.ctr + ph::WC_FLAGS;
+    a.boxid = c->t.boxid;
+    a.boxes = c->b.boxes;
+    a.nbox = c->b.nbox;
     a.p2p_pool = c->w.p2p_pool; a.p2p_off = c->w.p2p_off; a.p2p_cnt = c->w.p2p_cnt;
     a.pos4 = c->pos4;
     a.chi = c->t.chi;
@@ -476,7 +574,6 @@ int ph_stage_p2p(photons_ctx *c, int precision, int zero)
     a.work_counter = c->work_counter;
     a.boxsize = c->pp.boxsize; a.eps = c->pp.eps; a.mass = c->pp.mass; a.rs = c->pp.rs;
     a.k = ph::make_split_consts(c->pp);
-    a.acc_scale = c->pp.mass * ph::split_sig(c->pp) * ph::split_sig(c->pp);
     a.variant = p2p_variant();
     PH_TRY(ph_record(c, EV_P2P_BEGIN));
     PH_TRY(ph::launch_p2p(a, precision == PHOTONS_FP64, st));
@@ -499,7 +596,8 @@ static ph::MultipoleArgs multipole_args(photons_ctx *c)
     a.M = c->M; a.L = c->L;
     a.chi = c->t.chi; a.clo = c->t.clo; a.pos4 = c->pos4;
     a.ax = c->ax; a.ay = c->ay; a.az = c->az;
-    a.mass = c->pp.mass; a.rs = c->pp.rs; a.boxsize = c->pp.boxsize;
+    a.boxid = c->t.boxid;
+    a.boxes = c->b.boxes;
     return a;
 }
 
@@ -552,7 +650,7 @@ static PassKey pass_key(photons_ctx *c, const photons_params *p, int n, const do
 {
     PassKey k;
     memset(&k, 0, sizeof k);
-    k.n = n; k.levels = levels; k.maxleaf = p->maxleaf; k.precision = p->precision; k.flags = p->flags;
+    k.n = n; k.nbox = c->b.nbox; k.levels = levels; k.maxleaf = p->maxleaf; k.precision = p->precision; k.flags = p->flags;
     k.dio = dio; k.variant = p2p_variant(); k.nwarps = c->w.nwarps; k.mask = mask;
     k.boxsize = p->boxsize; k.theta = p->theta; k.rs = p->rs; k.rcut = p->rcut; k.eps = p->eps; k.mass = p->mass;
     k.pos = dio ? (const void *)pos : nullptr;
@@ -567,7 +665,7 @@ static int ph_enqueue_pass(photons_ctx *c, const photons_params *p, const double
                            unsigned mask)
 {
     PH_TRY(ph_enqueue_tree(c, src, levels));
-    PH_TRY(ph::walk_lists(c->w, c->t, c->b.cnt, c->ndepth, c->pp, mask, c->stream));
+    PH_TRY(ph::walk_lists(c->w, c->t, c->b.cnt, c->b.boxes, c->ndepth, c->pp, mask, c->stream));
     PH_TRY(ph_record(c, EV_WALK));
     PH_TRY(ph_stage_p2p(c, p->precision, 1));
     const bool far = !(p->flags & PHOTONS_F_NO_FARFIELD);
@@ -617,10 +715,13 @@ static int capture_pass(photons_ctx *c, const photons_params *p, const double *s
     return rc;
 }
 
-static int force_pass_graph(photons_ctx *c, const photons_params *p, int n, const double *pos, double *acc, int dio,
-                            unsigned mask)
+// The per-box constants live in the device box table, uploaded before each
+// launch, so a captured graph serves any boxes with the same count and sizes.
+static int force_pass_graph(photons_ctx *c, int nbox, const photons_params *p, const int *counts, const double *pos,
+                            double *acc, int dio, unsigned mask)
 {
-    PH_TRY(ph_prepare(c, p, n));
+    PH_TRY(ph_prepare_boxes(c, nbox, p, counts));
+    const int n = c->n;
     cudaStream_t st = c->stream;
     int levels = c->hint_levels ? c->hint_levels : estimate_levels(n, p->maxleaf);
     long long p2p_cap, pd_cap, m2l_cap;
@@ -637,6 +738,7 @@ static int force_pass_graph(photons_ctx *c, const photons_params *p, int n, cons
             c->have_key = true;
         }
         PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_START], st));
+        PH_TRY(ph_upload_boxes(c));
         if (!dio) PH_CUDA_CHECK(cudaMemcpyAsync(c->io, pos, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, st));
         PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_UPLOADED], st));
         PH_CUDA_CHECK(cudaGraphLaunch(c->gexec, st));
@@ -712,21 +814,22 @@ extern "C" int photons_set_stream(photons_ctx *c, void *stream)
     return 0;
 }
 
-extern "C" int photons_force_pass(photons_ctx *c, const photons_params *p, int n, const double *pos, double *acc)
+static int force_pass_boxes(photons_ctx *c, int nbox, const photons_params *p, const int *counts, const double *pos,
+                            double *acc)
 {
     photons_gpu_clear_error();
     if (!c) return ph_set_error(PH_ERR_ARG, "null context");
     if (!pos || !acc) return ph_set_error(PH_ERR_ARG, "null particle arrays");
-    if (!p) return ph_set_error(PH_ERR_ARG, "null parameters");
+    if (!p || !counts || nbox < 1) return ph_set_error(PH_ERR_ARG, "null parameters");
     cudaSetDevice(c->device);
     const int dio = p->flags & PHOTONS_F_DEVICE_IO;
     const unsigned mask = p->image_mask ? p->image_mask : ((1u << PH_NIMG) - 1u);
     const char *g = getenv("PHOTONS_GRAPH");
     if (!(g && !strcmp(g, "0"))) {
-        PH_TRY(force_pass_graph(c, p, n, pos, acc, dio, mask));
+        PH_TRY(force_pass_graph(c, nbox, p, counts, pos, acc, dio, mask));
     } else {
         // stage by stage, with the host checking the build and the walk
-        PH_TRY(ph_stage_build(c, p, n, pos, dio));
+        PH_TRY(ph_stage_build_boxes(c, nbox, p, counts, pos, dio));
         PH_TRY(ph_stage_walk(c, mask));
         PH_TRY(ph_stage_p2p(c, p->precision, 1));
         const bool far = !(p->flags & PHOTONS_F_NO_FARFIELD);
@@ -745,6 +848,17 @@ extern "C" int photons_force_pass(photons_ctx *c, const photons_params *p, int n
     c->last_flags = p->flags;
     c->precision = p->precision;
     return 0;
+}
+
+extern "C" int photons_force_pass(photons_ctx *c, const photons_params *p, int n, const double *pos, double *acc)
+{
+    return force_pass_boxes(c, 1, p, &n, pos, acc);
+}
+
+extern "C" int photons_force_pass_boxes(photons_ctx *c, int nbox, const photons_params *params, const int *counts,
+                                        const double *pos, double *acc)
+{
+    return force_pass_boxes(c, nbox, params, counts, pos, acc);
 }
 
 extern "C" int photons_get_counters(photons_ctx *c, long long *out, int n)

@@ -28,7 +28,7 @@ enum {
 // Everything a captured pass bakes in; a pass with a different key is
 // captured anew.  Zero-filled before use so it compares with memcmp.
 struct PassKey {
-    int n, levels, maxleaf, precision, flags, dio, variant, nwarps;
+    int n, nbox, levels, maxleaf, precision, flags, dio, variant, nwarps;
     unsigned mask;
     double boxsize, theta, rs, rcut, eps, mass;
     const void *pos, *acc;
@@ -60,6 +60,8 @@ struct photons_ctx {
     bool have_tree = false, have_lists = false, have_multipoles = false;
     long long hint_p2p = 0, hint_pd = 0, hint_m2l = 0;
     int hint_levels = 0;  // node levels to launch (0: estimate from N)
+    std::vector<BoxParams> h_boxes;  // this pass's box table (host copy)
+    int cap_box = 0;
     int ndepth = 0;       // depths the walk and far field launch
     unsigned long long epoch = 0;  // bumped by every device (re)allocation
     // the captured pass

@@ -40,6 +40,10 @@ struct BuildBufs {
     int cap_nodes = 0, cap_leaves = 0, cap_chunks = 0, cap_n = 0;
     int rule_cap = 0;  // this pass's 2N/MAXLEAF capacity (src/fmm.c:203-209), <= cap_nodes
     int *level_begin_h = nullptr;  // host copy, per level
+    // boxes: temp node / leaf -> box, and the per-box table
+    int *tn_boxid = nullptr, *tl_boxid = nullptr;
+    BoxParams *boxes = nullptr;
+    int nbox = 1;
 };
 
 enum BuildCounter {
@@ -65,6 +69,7 @@ struct TreeBufs {
     double *wx = nullptr, *wy = nullptr, *wz = nullptr;
     double *wsum = nullptr, *split = nullptr;
     float4 *chi = nullptr, *clo = nullptr, *w32 = nullptr;  // FP32 copies (centre hi/lo, widths + sum)
+    int *boxid = nullptr;                                    // box of each unified id
     int2 *son2 = nullptr;                                    // (son0, son1)
     // per-depth lists of unified ids
     int *depth_off = nullptr;   // [max_depth+2]
@@ -117,10 +122,10 @@ struct WalkStats {
 int launch_geom32(const TreeBufs &t, const int *tree_cnt, cudaStream_t st);
 // image_mask: bit 0 the local tree, bit k the k-th periodic image;
 // ndepth = depths to launch (at least the tree's deepest + 1)
-int walk_lists(WalkBufs &w, const TreeBufs &t, const int *tree_cnt, int ndepth, const PassParams &p,
-               unsigned image_mask, cudaStream_t st);
+int walk_lists(WalkBufs &w, const TreeBufs &t, const int *tree_cnt, const BoxParams *boxes, int ndepth,
+               const PassParams &p, unsigned image_mask, cudaStream_t st);
 
-int build_tree(BuildBufs &b, TreeBufs &t, const PassParams &p, int n, int levels, cudaStream_t st);
+int build_tree(BuildBufs &b, TreeBufs &t, const PassParams &p, int levels, cudaStream_t st);
 int read_tree_info(const BuildBufs &b, const TreeBufs &t, int levels, TreeInfo &info);
 
 }  // namespace ph

@@ -40,6 +40,21 @@ struct PassParams {
     int images;  // unused by the kernels; the walk takes an image mask
 };
 
+// One periodic box of a pass.  A pass covers one box or many independent
+// boxes (their particles concatenated, one tree root each); every kernel
+// reads the constants of the box its target belongs to from this table.
+struct BoxParams {
+    double boxsize, rs, rcut, eps, mass;
+    double rcut2;       // rcut^2
+    double acc_scale;   // packed FP32 P2P: m sig^2
+    float Lhi, Llo;     // box side as an FP32 pair
+    float c2f;          // rcut^2 in FP32 (walk filter)
+    float sig, e2s, pias, cs;  // packed FP32 P2P: coordinate scale, eps'^2, p ia / sig, (2/sqrt(pi)) ia / sig
+    float far_a, far_pa;       // FP32 M2L: ia = 1/(2 rs) and p ia
+    int first, count;   // particle range in the concatenated input
+    int root;           // unified id of the box's root node (written by the build)
+};
+
 // ------------------------------------------------------------------
 // device helpers
 // ------------------------------------------------------------------

@@ -62,7 +62,8 @@ __device__ __forceinline__ void scaled_monomials(double dx, double dy, double dz
 
 // ---------------- P2M ----------------
 __global__ void k_p2m(const double *px, const double *py, const double *pz, const int *ipart, const int *npart,
-                      const double *cx, const double *cy, const double *cz, const int *tree_cnt, double mass, double *M)
+                      const double *cx, const double *cy, const double *cz, const int *tree_cnt, const int *boxid,
+                      const BoxParams *boxes, double *M)
 {
     const int nleaf = tree_cnt[BC_LEAVES];
     for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < nleaf; l += gridDim.x * blockDim.x) {
@@ -71,6 +72,7 @@ __global__ void k_p2m(const double *px, const double *py, const double *pz, cons
         for (int i = 0; i < PH_NMULTI; i++) acc[i] = 0.0;
         double c0 = cx[l], c1 = cy[l], c2 = cz[l];
         int ip = ipart[l], np = npart[l];
+        const double mass = boxes[boxid[l]].mass;
         for (int p = ip; p < ip + np; p++) {
             double mono[PH_NMULTI];
             scaled_monomials(-(px[p] - c0), -(py[p] - c1), -(pz[p] - c2), mono);
@@ -175,7 +177,7 @@ __device__ __forceinline__ void m2l_add(double dx, double dy, double dz, const d
 
 __global__ void k_m2l(const int *tree_cnt, const unsigned long long *walk_flags, const uint32_t *pool,
                       const long long *off, const int *cnt, const double *cx, const double *cy, const double *cz,
-                      const double *M, double *Lout, double rs, double boxsize)
+                      const double *M, double *Lout, const int *boxid, const BoxParams *boxes)
 {
     const int nunified = *walk_flags ? 0 : tree_cnt[BC_LEAVES] + tree_cnt[BC_NODES];
     for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nunified; u += gridDim.x * blockDim.x) {
@@ -185,6 +187,8 @@ __global__ void k_m2l(const int *tree_cnt, const unsigned long long *walk_flags,
 #pragma unroll
         for (int a = 0; a < PH_NMULTI; a++) L[a] = Lout[(size_t)u * PH_NMULTI + a];
         double c0 = cx[u], c1 = cy[u], c2 = cz[u];
+        const BoxParams &B = boxes[boxid[u]];
+        const double rs = B.rs, boxsize = B.boxsize;
         long long o = off[u];
         for (int k = 0; k < n; k++) {
             uint32_t e = pool[o + k];
@@ -350,7 +354,7 @@ __global__ void k_m_to_f32(const double *M, float *M32, const int *tree_cnt)
 
 __global__ void k_m2l_f32(const int *tree_cnt, const unsigned long long *walk_flags, const uint32_t *pool,
                           const long long *off, const int *cnt, const float4 *chi, const float4 *clo, const float *M32,
-                          double *Lout, FarConsts F)
+                          double *Lout, const int *boxid, const BoxParams *boxes, FarConsts F)
 {
     const int nunified = *walk_flags ? 0 : tree_cnt[BC_LEAVES] + tree_cnt[BC_NODES];
     for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nunified; u += gridDim.x * blockDim.x) {
@@ -360,6 +364,11 @@ __global__ void k_m2l_f32(const int *tree_cnt, const unsigned long long *walk_fl
 #pragma unroll
         for (int a = 0; a < PH_NMULTI; a++) L[a] = 0.0f;
         const float4 th = chi[u], tl = clo[u];
+        const BoxParams &B = boxes[boxid[u]];
+        F.a = B.far_a;
+        F.pa = B.far_pa;
+        F.Lhi = B.Lhi;
+        F.Llo = B.Llo;
         const long long o = off[u];
         for (int k = 0; k < n; k++) {
             const uint32_t e = pool[o + k];
@@ -440,7 +449,7 @@ inline int grid_for(long long n, int tpb)
 int run_m2l(const MultipoleArgs &a, cudaStream_t st)
 {
     ph::note_launch(), k_m2l<<<grid_cap(), MP_TB, 0, st>>>(a.tree_cnt, a.walk_flags, a.m2l_pool, a.m2l_off, a.m2l_cnt,
-                                                             a.cx, a.cy, a.cz, a.M, a.L, a.rs, a.boxsize);
+                                                             a.cx, a.cy, a.cz, a.M, a.L, a.boxid, a.boxes);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }
@@ -464,15 +473,11 @@ int run_downward(const MultipoleArgs &a, cudaStream_t st)
 int run_m2l_f32(const MultipoleArgs &a, float *M32, cudaStream_t st)
 {
     ph::note_launch(), k_m_to_f32<<<grid_cap(), 256, 0, st>>>(a.M, M32, a.tree_cnt);
-    FarConsts F;
-    const double ia = 0.5 / a.rs;
-    F.a = (float)ia;
-    F.pa = (float)(SPLIT_P * ia);
-    F.Lhi = (float)a.boxsize;
-    F.Llo = (float)(a.boxsize - (double)F.Lhi);
+    FarConsts F;  // per-box fields are filled per target from the box table
+    F.a = F.pa = F.Lhi = F.Llo = 0.f;
     for (int i = 0; i < SPLIT_NA; i++) F.c[i] = (float)SPLIT_A[i];
     ph::note_launch(), k_m2l_f32<<<grid_cap(), MP_TB, 0, st>>>(a.tree_cnt, a.walk_flags, a.m2l_pool, a.m2l_off,
-                                                                 a.m2l_cnt, a.chi, a.clo, M32, a.L, F);
+                                                                 a.m2l_cnt, a.chi, a.clo, M32, a.L, a.boxid, a.boxes, F);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }
@@ -489,7 +494,7 @@ int run_downward_f32(const MultipoleArgs &a, cudaStream_t st)
 int run_p2m_m2m(const MultipoleArgs &a, cudaStream_t st)
 {
     ph::note_launch(), k_p2m<<<grid_cap(), MP_TB, 0, st>>>(a.px, a.py, a.pz, a.ipart, a.npart, a.cx, a.cy, a.cz,
-                                                             a.tree_cnt, a.mass, a.M);
+                                                             a.tree_cnt, a.boxid, a.boxes, a.M);
     for (int d = a.ndepth - 1; d >= 0; d--)
         ph::note_launch(), k_m2m_depth<<<grid_cap(), MP_TB, 0, st>>>(a.depth_list, a.depth_off, d, a.tree_cnt, a.son0,
                                                                        a.son1, a.cx, a.cy, a.cz, a.M);

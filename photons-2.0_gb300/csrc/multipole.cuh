@@ -20,7 +20,8 @@ struct MultipoleArgs {
     double *M, *L;  // [nunified][20]
     const float4 *chi, *clo, *pos4;  // FP32 centres (hi + lo) and leaf offsets, for the split far field
     double *ax, *ay, *az;
-    double mass, rs, boxsize;
+    const int *boxid;         // box of each unified id
+    const BoxParams *boxes;   // per box: mass (P2M), rs and side (M2L)
 };
 
 // M2L of every list, accumulated into L

@@ -350,8 +350,7 @@ __global__ void __launch_bounds__(P2P_TB, P2P_MINB) k_p2p_split_packed(P2PArgs A
     const float2 *X2 = reinterpret_cast<const float2 *>(sx);
     const float2 *Y2 = reinterpret_cast<const float2 *>(sy);
     const float2 *Z2 = reinterpret_cast<const float2 *>(sz);
-    const SplitConsts K = A.k;
-    const float Lhi = (float)A.boxsize, Llo = (float)(A.boxsize - (double)Lhi);
+    SplitConsts K = A.k;  // polynomial coefficients; the rest per target box below
 
     const int nleaf = p2p_targets(A);
     for (;;) {
@@ -361,6 +360,13 @@ __global__ void __launch_bounds__(P2P_TB, P2P_MINB) k_p2p_split_packed(P2PArgs A
         if (t >= nleaf) break;
         const int nt = A.npart[t], it = A.ipart[t];
         if (nt == 0) continue;
+        const BoxParams &B = A.boxes[A.boxid[t]];
+        K.sig = B.sig;
+        K.e2s = B.e2s;
+        K.pias = B.pias;
+        K.cs = B.cs;
+        const float Lhi = B.Lhi, Llo = B.Llo;
+        const double acc_scale = B.acc_scale;
         const float4 cth = A.chi[t], ctl = A.clo[t];
         const long long eoff = A.p2p_off[t];
         const int ecnt = A.p2p_cnt[t];
@@ -477,9 +483,9 @@ __global__ void __launch_bounds__(P2P_TB, P2P_MINB) k_p2p_split_packed(P2PArgs A
                     b0 += red[3 * l]; b1 += red[3 * l + 1]; b2 += red[3 * l + 2];
                 }
                 const int ip = it + tb + lane;
-                A.ax[ip] += b0 * A.acc_scale;
-                A.ay[ip] += b1 * A.acc_scale;
-                A.az[ip] += b2 * A.acc_scale;
+                A.ax[ip] += b0 * acc_scale;
+                A.ay[ip] += b1 * acc_scale;
+                A.az[ip] += b2 * acc_scale;
             }
             __syncwarp();
             if (m2) {
@@ -494,9 +500,9 @@ __global__ void __launch_bounds__(P2P_TB, P2P_MINB) k_p2p_split_packed(P2PArgs A
                         b0 += red[3 * l]; b1 += red[3 * l + 1]; b2 += red[3 * l + 2];
                     }
                     const int ip = it + tb + m1 + lane;
-                    A.ax[ip] += b0 * A.acc_scale;
-                    A.ay[ip] += b1 * A.acc_scale;
-                    A.az[ip] += b2 * A.acc_scale;
+                    A.ax[ip] += b0 * acc_scale;
+                    A.ay[ip] += b1 * acc_scale;
+                    A.az[ip] += b2 * acc_scale;
                 }
                 __syncwarp();
             }
@@ -520,9 +526,7 @@ __global__ void __launch_bounds__(P2P_TB) k_p2p_fp64(P2PArgs A)
     const int lane = warp_lane();
     const int wib = threadIdx.x >> 5;
     Src64 *src = s_src[wib];
-    const double eps = A.eps, mass = A.mass, rs = A.rs;
     const double coeff = 2.0 / sqrt(M_PI);
-    const double soft3 = mass / (eps * eps * eps);
 
     const int nleaf = p2p_targets(A);
     for (;;) {
@@ -532,6 +536,9 @@ __global__ void __launch_bounds__(P2P_TB) k_p2p_fp64(P2PArgs A)
         if (t >= nleaf) break;
         const int nt = A.npart[t], it = A.ipart[t];
         if (nt == 0) continue;
+        const BoxParams &B = A.boxes[A.boxid[t]];
+        const double eps = B.eps, mass = B.mass, rs = B.rs, boxL = B.boxsize;
+        const double soft3 = mass / (eps * eps * eps);
         const long long eoff = A.p2p_off[t];
         const int ecnt = A.p2p_cnt[t];
         for (int r0 = 0; r0 < nt; r0 += 32) {
@@ -562,7 +569,7 @@ __global__ void __launch_bounds__(P2P_TB) k_p2p_fp64(P2PArgs A)
                 int base = incl - ns;
                 if (lane < nfit) {
                     double h0 = 0.0, h1 = 0.0, h2 = 0.0;
-                    if (img) leaf_shift(img, A.boxsize, h0, h1, h2);
+                    if (img) leaf_shift(img, boxL, h0, h1, h2);
                     for (int j = 0; j < ns; j++) {
                         Src64 sj;
                         sj.x = A.px[is + j] + h0;
@@ -669,6 +676,8 @@ int launch_leaf_offsets(const BuildBufs &b, const TreeBufs &t, float4 *pos4, cud
 
 int launch_p2p(const P2PArgs &a, int fp64, cudaStream_t st)
 {
+    if (!fp64 && a.variant == 1 && a.nbox != 1)
+        return ph_set_error(8, "the scalar FP32 P2P kernel runs one box per pass");
     PH_CUDA_CHECK(cudaMemsetAsync(a.work_counter, 0, sizeof(int), st));
     int blocks = device_sm_count() * (fp64 ? 4 : 4);
     if (fp64) ph::note_launch(), k_p2p_fp64<<<blocks, P2P_TB, 0, st>>>(a);

@@ -32,9 +32,11 @@ struct P2PArgs {
     // output (tree order); written, not accumulated
     double *ax, *ay, *az;
     int *work_counter;
-    double boxsize, eps, mass, rs;
-    double acc_scale;  // packed FP32 kernel: m sig^2
-    SplitConsts k;
+    double boxsize, eps, mass, rs;  // scalar FP32 kernel (one box)
+    const int *boxid;               // box of each unified id
+    const BoxParams *boxes;         // per-box constants (packed FP32 and FP64 kernels)
+    int nbox;
+    SplitConsts k;                  // scalar kernel: all fields; packed: the polynomial coefficients
     int variant;  // FP32: 0 packed (default), 1 scalar
 };
 

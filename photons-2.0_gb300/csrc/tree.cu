@@ -51,22 +51,27 @@ __device__ __forceinline__ const double *axis_ptr(const double *x, const double 
     return D == 0 ? x : (D == 1 ? y : z);
 }
 
-__global__ void k_init_root(BuildBufs b, int n, double L)
+// one root per box: its particle range and the box [0, L]^3 as
+// src/fmm.c:194-197 derives the root from the domain box (centre 0.5*(L+0),
+// width L-0, src/toptree.c:150-159)
+__global__ void k_init_roots(BuildBufs b)
 {
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        b.tn_start[0] = 0;
-        b.tn_len[0] = n;
-        b.tn_depth[0] = 0;
-        b.tn_parent[0] = -1;
-        // root box as src/fmm.c:194-197 derives it from the domain box
-        // (centre 0.5*(L+0), width L-0, src/toptree.c:150-159)
-        double c = 0.5 * (L + 0.0), w = L - 0.0;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < b.nbox; t += gridDim.x * blockDim.x) {
+        const BoxParams &B = b.boxes[t];
+        b.tn_start[t] = B.first;
+        b.tn_len[t] = B.count;
+        b.tn_depth[t] = 0;
+        b.tn_parent[t] = -1;
+        b.tn_boxid[t] = t;
+        const double c = 0.5 * (B.boxsize + 0.0), w = B.boxsize - 0.0;
         for (int d = 0; d < 3; d++) {
-            b.tn_box[d * b.cap_nodes] = c - 0.5 * w;
-            b.tn_box[(3 + d) * b.cap_nodes] = c + 0.5 * w;
+            b.tn_box[d * b.cap_nodes + t] = c - 0.5 * w;
+            b.tn_box[(3 + d) * b.cap_nodes + t] = c + 0.5 * w;
         }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
         for (int i = 0; i < BC_NCOUNTERS; i++) b.cnt[i] = 0;
-        b.cnt[BC_LEVEL_COUNT] = 1;
+        b.cnt[BC_LEVEL_COUNT] = b.nbox;
         b.leaf_begin[0] = 0;
         b.leaf_count[0] = 0;
     }
@@ -233,6 +238,7 @@ __global__ void k_make_children(BuildBufs b, int maxleaf, int D)
                     b.tl_len[lid] = sizes[c];
                     b.tl_depth[lid] = depth + 1;
                     b.tl_parent[lid] = t;
+                    b.tl_boxid[lid] = b.tn_boxid[t];
                     for (int d = 0; d < 3; d++) {
                         b.tl_box[d * b.cap_leaves + lid] = clo[d];
                         b.tl_box[(3 + d) * b.cap_leaves + lid] = chi[d];
@@ -249,6 +255,7 @@ __global__ void k_make_children(BuildBufs b, int maxleaf, int D)
                     b.tn_len[nid] = sizes[c];
                     b.tn_depth[nid] = depth + 1;
                     b.tn_parent[nid] = t;
+                    b.tn_boxid[nid] = b.tn_boxid[t];
                     for (int d = 0; d < 3; d++) {
                         b.tn_box[d * b.cap_nodes + nid] = clo[d];
                         b.tn_box[(3 + d) * b.cap_nodes + nid] = chi[d];
@@ -397,6 +404,21 @@ __global__ void k_subtree_counts(BuildBufs b, int d)
     }
 }
 
+// the boxes' trees follow one another in box order: root r starts after the
+// nodes and leaves of roots 0..r-1
+__global__ void k_root_bases(BuildBufs b)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0 && b.cnt[BC_NLEVELS] > 0) {
+        int nodes = 0, leaves = 0;
+        for (int r = 0; r < b.nbox; r++) {
+            b.tn_pre[r] = nodes;
+            b.tn_lbase[r] = leaves;
+            nodes += b.tn_sub_nodes[r];
+            leaves += b.tn_sub_leaves[r];
+        }
+    }
+}
+
 // preorder node numbers and depth-first leaf numbers, src/fmm.c:101-118
 __global__ void k_number(BuildBufs b, int d)
 {
@@ -404,7 +426,6 @@ __global__ void k_number(BuildBufs b, int d)
     const int lb = b.lvl_begin[d], C = b.lvl_count[d];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
         int t = lb + i;
-        if (t == 0) { b.tn_pre[0] = 0; b.tn_lbase[0] = 0; }
         int pre = b.tn_pre[t], lbase = b.tn_lbase[t];
         int c0 = b.tn_child0[t], c1 = b.tn_child1[t];
         int off_nodes, off_leaves;
@@ -440,6 +461,8 @@ __global__ void k_scatter_nodes(BuildBufs b, TreeBufs T)
         T.son0[u] = PH_IS_LEAF_CODE(c0) ? b.tl_final[~c0] : nleaves + b.tn_pre[c0];
         T.son1[u] = PH_IS_LEAF_CODE(c1) ? b.tl_final[~c1] : nleaves + b.tn_pre[c1];
         T.split[u] = b.tn_split[t];
+        T.boxid[u] = b.tn_boxid[t];
+        if (t < b.nbox) b.boxes[t].root = u;
         write_geom(T, u, b.tn_box, b.cap_nodes, t);
     }
 }
@@ -456,6 +479,7 @@ __global__ void k_scatter_leaves(BuildBufs b, TreeBufs T)
         T.son0[u] = -1;
         T.son1[u] = -1;
         T.split[u] = 0.0;
+        T.boxid[u] = b.tl_boxid[l];
         write_geom(T, u, b.tl_box, b.cap_leaves, l);
     }
 }
@@ -510,14 +534,14 @@ int launch_init_particles(BuildBufs &b, const double *pos, int n, cudaStream_t s
 // level, PH_FLAG_DEPTH is raised in b.cnt[BC_FLAGS] (the caller grows
 // `levels` and builds again); capacity overflows raise their flags there too.
 // Depth lists cover depths 0..levels.
-int build_tree(BuildBufs &b, TreeBufs &T, const PassParams &p, int n, int levels, cudaStream_t st)
+int build_tree(BuildBufs &b, TreeBufs &T, const PassParams &p, int levels, cudaStream_t st)
 {
     const int maxb = device_sm_count() * 8;
     if (levels < 1 || levels + 1 > T.max_depth_cap)
         return ph_set_error(7, "tree deeper than %d levels", T.max_depth_cap - 1);
     PH_CUDA_CHECK(cudaMemsetAsync(b.lvl_count, 0, sizeof(int) * (levels + 1), st));
     PH_CUDA_CHECK(cudaMemsetAsync(b.leaf_count, 0, sizeof(int) * (levels + 2), st));
-    ph::note_launch(), k_init_root<<<1, 1, 0, st>>>(b, n, p.boxsize);
+    ph::note_launch(), k_init_roots<<<(b.nbox + TB - 1) / TB, TB, 0, st>>>(b);
     for (int d = 0; d < levels; d++) {
         const int D = d % 3;  // direct_local_start = 0 at one rank; axis cycles (src/fmm.c:99)
         ph::note_launch(), k_level_nch<<<maxb, TB, 0, st>>>(b);
@@ -540,6 +564,7 @@ int build_tree(BuildBufs &b, TreeBufs &T, const PassParams &p, int n, int levels
     ph::note_launch(), k_tree_totals<<<1, 1, 0, st>>>(b);
     // subtree sizes bottom-up, numbers top-down
     for (int d = levels - 1; d >= 0; d--) ph::note_launch(), k_subtree_counts<<<maxb, TB, 0, st>>>(b, d);
+    ph::note_launch(), k_root_bases<<<1, 1, 0, st>>>(b);
     for (int d = 0; d < levels; d++) ph::note_launch(), k_number<<<maxb, TB, 0, st>>>(b, d);
     ph::note_launch(), k_scatter_nodes<<<maxb, TB, 0, st>>>(b, T);
     ph::note_launch(), k_scatter_leaves<<<maxb, TB, 0, st>>>(b, T);

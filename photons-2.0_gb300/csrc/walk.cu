@@ -116,12 +116,15 @@ struct WalkArgs {
     int depth;
     int nroot;               // entries of the root's list: (root, img) for the selected images
     int root_img[PH_NIMG];
-    double boxsize, theta2, c2, rcut, theta;
-    float Lhi, Llo, theta2f, c2f;
+    const int *boxid;        // box of each unified id
+    const BoxParams *boxes;  // per box: side, rcut, root
+    double theta2, theta;
+    float theta2f;
 };
 
 // sender-side pruning of an image node, src/remotes.c:97-158
-__device__ __forceinline__ bool image_pruned(const WalkArgs &A, int r, int b, double s0, double s1, double s2)
+__device__ __forceinline__ bool image_pruned(const WalkArgs &A, int r, double rcut, int b, double s0, double s1,
+                                             double s2)
 {
     const Geo &g = A.g;
     double sx[3] = {s0, s1, s2};
@@ -139,7 +142,7 @@ __device__ __forceinline__ bool image_pruned(const WalkArgs &A, int r, int b, do
     double wmax = bw[0];
     if (wmax < bw[1]) wmax = bw[1];
     if (wmax < bw[2]) wmax = bw[2];
-    if (dr >= A.rcut) return true;
+    if (dr >= rcut) return true;
     return wmax < __dmul_rn(__dmul_rn(0.95, A.theta), dr);
 }
 
@@ -184,7 +187,6 @@ __global__ void __launch_bounds__(WALK_TB, MINB) k_walk_level(WalkArgs A)
     uint32_t *sh_m2l = sh_pd + WS_PD;
     const int parity = A.depth & 1;
     const int nleaf = A.tree_cnt[BC_LEAVES];
-    const int root = nleaf;  // node 0 in preorder
     const int list_begin = A.depth_off[A.depth], list_end = A.depth_off[A.depth + 1];
     unsigned long long c_p2p_loc = 0, c_p2p_img = 0, c_m2l_loc = 0, c_m2l_img = 0, c_pl = 0, c_pi = 0;
     unsigned flags = 0;
@@ -193,6 +195,12 @@ __global__ void __launch_bounds__(WALK_TB, MINB) k_walk_level(WalkArgs A)
     for (int ti = list_begin + gw; ti < list_end; ti += nw) {
         const int a = A.depth_list[ti];
         const bool leaf_a = a < nleaf;
+        // the target's box: its root (the receiving domain of the image
+        // pruning), side and cutoff
+        const BoxParams &B = A.boxes[A.boxid[a]];
+        const int root = B.root;
+        const double boxL = B.boxsize, rcut = B.rcut, c2 = B.rcut2;
+        const float Lhi = B.Lhi, Llo = B.Llo, c2f = B.c2f;
         const double ca0 = g.cx[a], ca1 = g.cy[a], ca2 = g.cz[a];
         const double wa0 = g.wx[a], wa1 = g.wy[a], wa2 = g.wz[a], wsa = g.wsum[a];
         const float4 ah = g.chi[a], al = g.clo[a], aw = g.w32[a];
@@ -272,18 +280,18 @@ __global__ void __launch_bounds__(WALK_TB, MINB) k_walk_level(WalkArgs A)
                 } else {
                     int mi, mj, mk;
                     image_offsets(im, mi, mj, mk);
-                    const float e0 = centre_diff32(bh[s].x, bl[s].x, ah.x, al.x, mi, A.Lhi, A.Llo);
-                    const float e1 = centre_diff32(bh[s].y, bl[s].y, ah.y, al.y, mj, A.Lhi, A.Llo);
-                    const float e2 = centre_diff32(bh[s].z, bl[s].z, ah.z, al.z, mk, A.Lhi, A.Llo);
+                    const float e0 = centre_diff32(bh[s].x, bl[s].x, ah.x, al.x, mi, Lhi, Llo);
+                    const float e1 = centre_diff32(bh[s].y, bl[s].y, ah.y, al.y, mj, Lhi, Llo);
+                    const float e2 = centre_diff32(bh[s].z, bl[s].z, ah.z, al.z, mk, Lhi, Llo);
                     int flag = acceptance_fp32(aw.x, aw.y, aw.z, bw[s].x, bw[s].y, bw[s].z, e0, e1, e2, A.theta2f,
-                                               A.c2f);
-                    const double s0 = mi * A.boxsize, s1 = mj * A.boxsize, s2 = mk * A.boxsize;
+                                               c2f);
+                    const double s0 = mi * boxL, s1 = mj * boxL, s2 = mk * boxL;
                     if (flag == -2) {
                         // image node centre = local centre + shift (src/remotes.c:123-125)
                         double cb0 = g.cx[bb], cb1 = g.cy[bb], cb2 = g.cz[bb];
                         if (im) { cb0 = __dadd_rn(cb0, s0); cb1 = __dadd_rn(cb1, s1); cb2 = __dadd_rn(cb2, s2); }
                         flag = acceptance_fp64(wa0, wa1, wa2, g.wx[bb], g.wy[bb], g.wz[bb], __dsub_rn(ca0, cb0),
-                                               __dsub_rn(ca1, cb1), __dsub_rn(ca2, cb2), A.theta2, A.c2);
+                                               __dsub_rn(ca1, cb1), __dsub_rn(ca2, cb2), A.theta2, c2);
                     }
                     // width-sum comparison of the open rule: FP32 decides unless the values tie
                     const bool bigger_a = (aw.w != bw[s].w) ? (aw.w > bw[s].w) : (wsa > g.wsum[bb]);
@@ -296,7 +304,7 @@ __global__ void __launch_bounds__(WALK_TB, MINB) k_walk_level(WalkArgs A)
                         else if (leaf_b) kd = OUT_PUSH;
                         else kd = bigger_a ? OUT_PUSH : OUT_OPEN;
                     } else {
-                        const bool pruned = !leaf_b && image_pruned(A, root, bb, s0, s1, s2);
+                        const bool pruned = !leaf_b && image_pruned(A, root, rcut, bb, s0, s1, s2);
                         if (leaf_a) kd = (flag == 1 || pruned) ? OUT_M2L : OUT_OPEN;
                         else if (flag == 1) kd = OUT_M2L;
                         else kd = (leaf_b || pruned || bigger_a) ? OUT_PUSH : OUT_OPEN;
@@ -455,8 +463,8 @@ int launch_geom32(const TreeBufs &t, const int *tree_cnt, cudaStream_t st)
 
 // Enqueue the walk of depths 0..ndepth-1; depths past the tree's deepest
 // exit at once.  Counters and flags stay on the device (w.ctr).
-int walk_lists(WalkBufs &w, const TreeBufs &t, const int *tree_cnt, int ndepth, const PassParams &p,
-               unsigned image_mask, cudaStream_t st)
+int walk_lists(WalkBufs &w, const TreeBufs &t, const int *tree_cnt, const BoxParams *boxes, int ndepth,
+               const PassParams &p, unsigned image_mask, cudaStream_t st)
 {
     PH_CUDA_CHECK(cudaMemsetAsync(w.ctr, 0, sizeof(unsigned long long) * WC_N, st));
     WalkArgs A;
@@ -465,10 +473,9 @@ int walk_lists(WalkBufs &w, const TreeBufs &t, const int *tree_cnt, int ndepth, 
     A.g.wx = t.wx; A.g.wy = t.wy; A.g.wz = t.wz; A.g.wsum = t.wsum;
     A.g.son0 = t.son0; A.g.son1 = t.son1; A.g.npart = t.npart; A.g.parent = t.parent;
     A.g.chi = t.chi; A.g.clo = t.clo; A.g.w32 = t.w32; A.g.son = t.son2;
-    A.Lhi = (float)p.boxsize;
-    A.Llo = (float)(p.boxsize - (double)A.Lhi);
     A.theta2f = (float)(p.theta * p.theta);
-    A.c2f = (float)(p.rcut * p.rcut);
+    A.boxid = t.boxid;
+    A.boxes = boxes;
     A.w = w;
     A.depth_list = t.depth_list;
     A.depth_off = t.depth_off;
@@ -476,11 +483,8 @@ int walk_lists(WalkBufs &w, const TreeBufs &t, const int *tree_cnt, int ndepth, 
     A.nroot = 0;
     for (int img = 0; img < PH_NIMG; img++)
         if (image_mask & (1u << img)) A.root_img[A.nroot++] = img;
-    A.boxsize = p.boxsize;
     A.theta = p.theta;
     A.theta2 = p.theta * p.theta;
-    A.rcut = p.rcut;
-    A.c2 = p.rcut * p.rcut;
     const int blocks = (w.nwarps * 32 + WALK_TB - 1) / WALK_TB;
     for (int d = 0; d < ndepth; d++) {
         A.depth = d;
