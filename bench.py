@@ -48,9 +48,11 @@ def parse():
     ap.add_argument("--error-bound", type=float, default=1e-4)
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 GPU comparison pass")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
-    ap.add_argument("--workload", default="zeldovich256", choices=["zeldovich256", "zeldovich512", "nfw128"],
+    ap.add_argument("--workload", default="zeldovich256",
+                    choices=["zeldovich256", "zeldovich512", "nfw128", "boxes256"],
                     help="zeldovich256: the headline (P(k)~k^-2, seed 3); zeldovich512: P(k)~k^-1.5, seed 5, "
-                         "L=1000 at 512^3; nfw128: 50%% uniform + 50%% in NFW halos, L=200 at 128^3")
+                         "L=1000 at 512^3; nfw128: 50%% uniform + 50%% in NFW halos, L=200 at 128^3; "
+                         "boxes256: 256 independent Plummer + uniform boxes of 16^3-64^3 particles in one pass")
     ap.add_argument("--kdk", action="store_true", help="also time device-resident kick-drift-kick steps")
     return ap.parse_args()
 
@@ -228,6 +230,142 @@ def kdk_measure(ph, fp, torch, stream, dpos, dacc, n, p, steps):
     return out
 
 
+def run_boxes_bench(args):
+    """Many independent periodic boxes (70% Plummer a = 0.05 L_b + 30% uniform,
+    N_b log-uniform in [16^3, 64^3], L_b in [20, 100], seed 4) in one batched
+    pass, against looping over the boxes one pass at a time (FP32 and FP64)."""
+    import ctypes as C
+    import torch
+    import __graft_entry__ as g
+
+    ph = g.load_package()
+    from photons_gb300 import ics
+
+    torch.cuda.set_device(0)
+    leaf = args.maxleaf or 32
+    boxes = [(pos, dict(p, maxleaf=leaf)) for pos, p in ics.plummer_boxes(nbox=256, seed=4)]
+    counts = np.array([b[0].shape[0] for b in boxes], np.int32)
+    offs = np.concatenate([[0], np.cumsum(counts)])
+    n = int(offs[-1])
+    pos = np.ascontiguousarray(np.concatenate([b[0] for b in boxes]))
+    fp = ph.ForcePass(0)
+    stream = torch.cuda.current_stream()
+    fp.set_stream(stream.cuda_stream)
+    dpos = torch.from_numpy(pos).cuda()
+    dacc = torch.empty_like(dpos)
+    lib = fp.lib
+
+    def params(prec):
+        arr = (ph.Params * len(boxes))()
+        for i, (_, p) in enumerate(boxes):
+            arr[i] = ph.make_params(p, prec, 0, ph.F_DEVICE_IO)
+        return arr
+
+    p32, p64 = params(ph.FP32_SPLIT), params(ph.FP64)
+    cptr = counts.ctypes.data_as(C.POINTER(C.c_int))
+
+    def batched(prm):
+        rc = lib.photons_force_pass_boxes(fp.h, len(boxes), prm, cptr, C.c_void_p(dpos.data_ptr()),
+                                          C.c_void_p(dacc.data_ptr()))
+        if rc:
+            raise RuntimeError(lib.photons_gpu_error().decode())
+
+    # the loop gives each box its own context, so each keeps its captured pass
+    ctxs = [ph.ForcePass(0) for _ in boxes]
+    for cx in ctxs:
+        cx.set_stream(stream.cuda_stream)
+
+    def loop(prec):
+        for i, (_, p) in enumerate(boxes):
+            ctxs[i].run_device(dpos.data_ptr() + 24 * int(offs[i]), dacc.data_ptr() + 24 * int(offs[i]),
+                               int(counts[i]), p, precision=prec)
+
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, reps):
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    for _ in range(max(3, args.warmup)):
+        batched(p32)
+    sampler = ClockSampler(0)
+    sampler.start()
+    launches0 = lib.photons_launch_count()
+    ms = timed(lambda: batched(p32), args.steps)
+    launches = lib.photons_launch_count() - launches0
+    clocks = sampler.stop()
+    t = fp.timings()
+    c = fp.counters()
+    pairs = c["pairs_local"] + c["pairs_image"]
+    acc32 = dacc.cpu().numpy()
+    loop(ph.FP32_SPLIT)
+    ms_loop32 = timed(lambda: loop(ph.FP32_SPLIT), 1)
+    batched(p64)
+    ms64 = timed(lambda: batched(p64), 1)
+    acc64 = dacc.cpu().numpy()
+    loop(ph.FP64)
+    ms_loop64 = timed(lambda: loop(ph.FP64), 1)
+    # errors: FP32 vs FP64 everywhere, and both vs the direct sum on ~40 particles per box
+    e = rel_err(acc32, acc64)
+    rng = np.random.default_rng(7)
+    a32, a64 = [], []
+    for i, (bp, p) in enumerate(boxes):
+        tg = rng.choice(counts[i], min(40, counts[i]), replace=False).astype(np.int32)
+        ds = ph.direct_sum(bp, p, tg)
+        a32.append(rel_err(acc32[offs[i] + tg], ds))
+        a64.append(rel_err(acc64[offs[i] + tg], ds))
+    a32, a64 = np.concatenate(a32), np.concatenate(a64)
+    # end to end: host arrays through the batched C-ABI call
+    hpos = torch.from_numpy(pos).pin_memory()
+    hacc = torch.empty_like(hpos).pin_memory()
+    hp32 = (ph.Params * len(boxes))()
+    for i, (_, p) in enumerate(boxes):
+        hp32[i] = ph.make_params(p, ph.FP32_SPLIT, 0, 0)
+
+    def e2e():
+        rc = lib.photons_force_pass_boxes(fp.h, len(boxes), hp32, cptr, C.c_void_p(hpos.data_ptr()),
+                                          C.c_void_p(hacc.data_ptr()))
+        if rc:
+            raise RuntimeError(lib.photons_gpu_error().decode())
+
+    e2e()
+    t0 = time.time()
+    for _ in range(3):
+        e2e()
+    e2e_ms = (time.time() - t0) * 1e3 / 3
+    peak = ph.fp32_fma_peak(8192)
+    achieved = FLOPS_PER_PAIR * pairs / (t["p2p"] * 1e-3) / 1e12
+    line = {
+        "metric": "particle-forces/s, 256 independent boxes in one batched pass", "value": n / (ms * 1e-3),
+        "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "boxes256", "n": n, "nbox": len(boxes), "maxleaf": leaf,
+                   "n_box_min": int(counts.min()), "n_box_max": int(counts.max()),
+                   "precision": "fp32-split", "l2": "inputs larger than L2 (positions %.0f MB)" % (n * 24 / 1e6)},
+        "roofline": {"bound": "fp32", "kernel": "k_p2p_split_packed", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak, "p2p_ms": t["p2p"]},
+        "e2e": {"value": n / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": n * 24, "d2h_bytes_per_step": n * 24,
+                "ms_per_step": e2e_ms},
+        "gpu_launches": int(launches), "clocks": clocks,
+        "phases_ms": t,
+        "boxes": {"batched_fp32_ms": ms, "loop_fp32_ms": ms_loop32, "batched_fp64_ms": ms64,
+                  "loop_fp64_ms": ms_loop64, "speedup_batched_fp32_vs_loop_fp64": ms_loop64 / ms,
+                  "speedup_batched_vs_loop_fp32": ms_loop32 / ms},
+        "errors": {"precision_fp32_vs_fp64gpu": {"median": float(np.median(e)), "p99": float(np.percentile(e, 99))},
+                   "algorithmic_vs_direct_sum": {"fp32_median": float(np.median(a32)),
+                                                 "fp32_p99": float(np.percentile(a32, 99)),
+                                                 "fp64_median": float(np.median(a64)),
+                                                 "sample": "%d particles, 40 per box" % a32.size}},
+    }
+    print(json.dumps(line))
+
+
 def rel_err(a, b):
     return np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-300)
 
@@ -236,6 +374,9 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference_arm(args)
+        return
+    if args.workload == "boxes256":
+        run_boxes_bench(args)
         return
     rank, world, local = dist_env()
     import torch
