@@ -470,7 +470,7 @@ def main():
     t_p2p = float(np.mean(p2p_ms))
     achieved = FLOPS_PER_PAIR * pairs / (t_p2p * 1e-3) / 1e12
     traffic = None
-    tp = os.path.join(ROOT, "profiles", "k_p2p_split_zeldovich160.md")
+    tp = os.path.join(ROOT, "profiles", "k_p2p_split_packed_zeldovich160.md")
     if os.path.exists(tp) and args.nside == 256:
         import re
         m = re.search(r"dram_bytes_per_launch_scaled_to_256:\s*([0-9.eE+]+)", open(tp).read())

@@ -178,6 +178,7 @@ static int alloc_walk(photons_ctx *c, long long p2p_cap, long long pd_cap, long 
 {
     ph::WalkBufs &w = c->w;
     if (!w.ctr) { PH_TRY(dalloc(w.ctr, ph::WC_N)); c->epoch++; }
+    if (!c->far_gate) { PH_TRY(dalloc(c->far_gate, 2)); c->epoch++; }
     if (!c->work_counter) { PH_TRY(dalloc(c->work_counter, 4)); c->epoch++; }
     if (p2p_cap > w.p2p_cap) { PH_TRY(dalloc(w.p2p_pool, p2p_cap)); w.p2p_cap = p2p_cap; c->epoch++; }
     if (pd_cap > w.pd_cap) {
@@ -216,7 +217,7 @@ static void free_all(photons_ctx *c)
                     c->w.m2l_pool, c->w.m2l_off, c->w.m2l_cnt, c->w.scratch, c->w.ctr, c->pos4, c->ax, c->ay,
                     c->az, c->M, c->L, c->io, c->work_counter, c->t.chi, c->t.clo, c->t.w32, c->t.son2, c->M32,
                     b.lvl_begin, b.lvl_count, b.leaf_begin, b.leaf_count, c->t.depth_cnt, b.tn_boxid, b.tl_boxid,
-                    c->t.boxid, b.boxes};
+                    c->t.boxid, b.boxes, c->far_gate};
     for (void *p : ptrs)
         if (p) cudaFree(p);
 }
@@ -598,6 +599,8 @@ static ph::MultipoleArgs multipole_args(photons_ctx *c)
     a.ax = c->ax; a.ay = c->ay; a.az = c->az;
     a.boxid = c->t.boxid;
     a.boxes = c->b.boxes;
+    a.gate_m = c->capturing ? c->far_gate : nullptr;
+    a.gate_l = c->capturing ? c->far_gate + 1 : nullptr;
     return a;
 }
 
@@ -669,6 +672,10 @@ static int ph_enqueue_pass(photons_ctx *c, const photons_params *p, const double
     PH_TRY(ph_record(c, EV_WALK));
     PH_TRY(ph_stage_p2p(c, p->precision, 1));
     const bool far = !(p->flags & PHOTONS_F_NO_FARFIELD);
+    // the far field runs only if the walk made an M2L task (decided on the
+    // device); multipoles also when the caller keeps them
+    if (far || (p->flags & PHOTONS_F_MULTIPOLES))
+        PH_TRY(ph::launch_far_gate(c->w.ctr, (p->flags & PHOTONS_F_MULTIPOLES) ? 1 : 0, c->far_gate, c->stream));
     if (far) {
         PH_TRY(ph_stage_multipoles(c));
         PH_TRY(ph_stage_m2l(c, p->precision));
@@ -765,7 +772,8 @@ static int force_pass_graph(photons_ctx *c, int nbox, const photons_params *p, c
         c->info.depth_off.resize(c->info.depth + 2);
         c->have_lists = true;
         c->mask = mask;
-        c->have_multipoles = !(p->flags & PHOTONS_F_NO_FARFIELD) || (p->flags & PHOTONS_F_MULTIPOLES);
+        const bool any_m2l = c->ws.c[ph::WC_M2L_LOCAL] + c->ws.c[ph::WC_M2L_IMAGE] > 0;
+        c->have_multipoles = (!(p->flags & PHOTONS_F_NO_FARFIELD) && any_m2l) || (p->flags & PHOTONS_F_MULTIPOLES);
         keep_walk_hints(c, p2p_cap, pd_cap, m2l_cap);
         return 0;
     }

@@ -49,6 +49,7 @@ struct photons_ctx {
     float *M32 = nullptr;  // multipoles rounded to FP32 for the split M2L
     double *io = nullptr;  // 3*cap_n staging for host transfers and gathers
     int *work_counter = nullptr;
+    int *far_gate = nullptr;  // [2] far-field switches of the captured pass
     int cap_n = 0, cap_u = 0;
     // last pass
     PassParams pp{};

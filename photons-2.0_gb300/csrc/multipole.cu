@@ -63,8 +63,9 @@ __device__ __forceinline__ void scaled_monomials(double dx, double dy, double dz
 // ---------------- P2M ----------------
 __global__ void k_p2m(const double *px, const double *py, const double *pz, const int *ipart, const int *npart,
                       const double *cx, const double *cy, const double *cz, const int *tree_cnt, const int *boxid,
-                      const BoxParams *boxes, double *M)
+                      const BoxParams *boxes, double *M, const int *gate)
 {
+    if (gate && !*gate) return;
     const int nleaf = tree_cnt[BC_LEAVES];
     for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < nleaf; l += gridDim.x * blockDim.x) {
         double acc[PH_NMULTI];
@@ -104,8 +105,10 @@ __device__ __forceinline__ void m2m_add(double dx, double dy, double dz, const d
 }
 
 __global__ void k_m2m_depth(const int *list, const int *depth_off, int d, const int *tree_cnt, const int *son0,
-                            const int *son1, const double *cx, const double *cy, const double *cz, double *M)
+                            const int *son1, const double *cx, const double *cy, const double *cz, double *M,
+                            const int *gate)
 {
+    if (gate && !*gate) return;
     const int begin = depth_off[d], end = depth_off[d + 1], nleaf = tree_cnt[BC_LEAVES];
     for (int i = begin + blockIdx.x * blockDim.x + threadIdx.x; i < end; i += gridDim.x * blockDim.x) {
         int u = list[i];
@@ -211,8 +214,9 @@ __global__ void k_m2l(const int *tree_cnt, const unsigned long long *walk_flags,
 
 // ---------------- L2L (one depth: each member adds its parent's expansion) ----------------
 __global__ void k_l2l_depth(const int *list, const int *depth_off, int d, const int *parent, const double *cx,
-                            const double *cy, const double *cz, double *L)
+                            const double *cy, const double *cz, double *L, const int *gate)
 {
+    if (gate && !*gate) return;
     const int begin = depth_off[d], end = depth_off[d + 1];
     for (int i = begin + blockIdx.x * blockDim.x + threadIdx.x; i < end; i += gridDim.x * blockDim.x) {
         int u = list[i];
@@ -240,8 +244,9 @@ __global__ void k_l2l_depth(const int *list, const int *depth_off, int d, const 
 // ---------------- L2P ----------------
 __global__ void k_l2p(const double *px, const double *py, const double *pz, const int *ipart, const int *npart,
                       const double *cx, const double *cy, const double *cz, const int *tree_cnt, const double *L,
-                      double *ax, double *ay, double *az)
+                      double *ax, double *ay, double *az, const int *gate)
 {
+    if (gate && !*gate) return;
     const int nleaf = tree_cnt[BC_LEAVES];
     int lane = warp_lane();
     int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
@@ -345,8 +350,9 @@ __device__ __forceinline__ void m2l_add_f32(float dx, float dy, float dz, const 
     }
 }
 
-__global__ void k_m_to_f32(const double *M, float *M32, const int *tree_cnt)
+__global__ void k_m_to_f32(const double *M, float *M32, const int *tree_cnt, const int *gate)
 {
+    if (gate && !*gate) return;
     const long long n = (long long)(tree_cnt[BC_LEAVES] + tree_cnt[BC_NODES]) * PH_NMULTI;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
         M32[i] = (float)M[i];
@@ -391,8 +397,9 @@ __global__ void k_m2l_f32(const int *tree_cnt, const unsigned long long *walk_fl
 
 // L2P in FP32 on the leaf-centre offsets, added to the FP64 accelerations
 __global__ void k_l2p_f32(const float4 *pos4, const int *ipart, const int *npart, const int *tree_cnt,
-                          const double *L, double *ax, double *ay, double *az)
+                          const double *L, double *ax, double *ay, double *az, const int *gate)
 {
+    if (gate && !*gate) return;
     const int nleaf = tree_cnt[BC_LEAVES];
     const int lane = warp_lane();
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
@@ -426,11 +433,23 @@ __global__ void k_l2p_f32(const float4 *pos4, const int *ipart, const int *npart
 }
 
 // zero the local expansions of every unified id
-__global__ void k_zero_L(double *L, const int *tree_cnt)
+__global__ void k_zero_L(double *L, const int *tree_cnt, const int *gate)
 {
+    if (gate && !*gate) return;
     const long long n = (long long)(tree_cnt[BC_LEAVES] + tree_cnt[BC_NODES]) * PH_NMULTI;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
         L[i] = 0.0;
+}
+
+// far-field switches of a captured pass: gate[0] multipoles (M2L work or
+// kept multipoles), gate[1] M2L / L2L / L2P (any M2L task)
+__global__ void k_far_gate(const unsigned long long *walk_ctr, int keep_multipoles, int *gate)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const bool m2l = walk_ctr[WC_M2L_LOCAL] + walk_ctr[WC_M2L_IMAGE] > 0;
+        gate[0] = m2l || keep_multipoles;
+        gate[1] = m2l;
+    }
 }
 
 inline int grid_cap() { return device_sm_count() * 16; }
@@ -458,21 +477,21 @@ static void launch_l2l(const MultipoleArgs &a, cudaStream_t st)
 {
     for (int d = 1; d < a.ndepth; d++)
         ph::note_launch(), k_l2l_depth<<<grid_cap(), MP_TB, 0, st>>>(a.depth_list, a.depth_off, d, a.parent, a.cx, a.cy,
-                                                                       a.cz, a.L);
+                                                                       a.cz, a.L, a.gate_l);
 }
 
 int run_downward(const MultipoleArgs &a, cudaStream_t st)
 {
     launch_l2l(a, st);
     ph::note_launch(), k_l2p<<<grid_cap(), 256, 0, st>>>(a.px, a.py, a.pz, a.ipart, a.npart, a.cx, a.cy, a.cz,
-                                                           a.tree_cnt, a.L, a.ax, a.ay, a.az);
+                                                           a.tree_cnt, a.L, a.ax, a.ay, a.az, a.gate_l);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }
 
 int run_m2l_f32(const MultipoleArgs &a, float *M32, cudaStream_t st)
 {
-    ph::note_launch(), k_m_to_f32<<<grid_cap(), 256, 0, st>>>(a.M, M32, a.tree_cnt);
+    ph::note_launch(), k_m_to_f32<<<grid_cap(), 256, 0, st>>>(a.M, M32, a.tree_cnt, a.gate_l);
     FarConsts F;  // per-box fields are filled per target from the box table
     F.a = F.pa = F.Lhi = F.Llo = 0.f;
     for (int i = 0; i < SPLIT_NA; i++) F.c[i] = (float)SPLIT_A[i];
@@ -486,7 +505,7 @@ int run_downward_f32(const MultipoleArgs &a, cudaStream_t st)
 {
     launch_l2l(a, st);
     ph::note_launch(), k_l2p_f32<<<grid_cap(), 256, 0, st>>>(a.pos4, a.ipart, a.npart, a.tree_cnt, a.L, a.ax, a.ay,
-                                                               a.az);
+                                                               a.az, a.gate_l);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }
@@ -494,11 +513,18 @@ int run_downward_f32(const MultipoleArgs &a, cudaStream_t st)
 int run_p2m_m2m(const MultipoleArgs &a, cudaStream_t st)
 {
     ph::note_launch(), k_p2m<<<grid_cap(), MP_TB, 0, st>>>(a.px, a.py, a.pz, a.ipart, a.npart, a.cx, a.cy, a.cz,
-                                                             a.tree_cnt, a.boxid, a.boxes, a.M);
+                                                             a.tree_cnt, a.boxid, a.boxes, a.M, a.gate_m);
     for (int d = a.ndepth - 1; d >= 0; d--)
         ph::note_launch(), k_m2m_depth<<<grid_cap(), MP_TB, 0, st>>>(a.depth_list, a.depth_off, d, a.tree_cnt, a.son0,
-                                                                       a.son1, a.cx, a.cy, a.cz, a.M);
-    ph::note_launch(), k_zero_L<<<grid_cap(), 256, 0, st>>>(a.L, a.tree_cnt);
+                                                                       a.son1, a.cx, a.cy, a.cz, a.M, a.gate_m);
+    ph::note_launch(), k_zero_L<<<grid_cap(), 256, 0, st>>>(a.L, a.tree_cnt, a.gate_m);
+    PH_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
+int launch_far_gate(const unsigned long long *walk_ctr, int keep_multipoles, int *gate, cudaStream_t st)
+{
+    ph::note_launch(), k_far_gate<<<1, 1, 0, st>>>(walk_ctr, keep_multipoles, gate);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }

@@ -22,6 +22,9 @@ struct MultipoleArgs {
     double *ax, *ay, *az;
     const int *boxid;         // box of each unified id
     const BoxParams *boxes;   // per box: mass (P2M), rs and side (M2L)
+    // device switches (null: always run): gate_m for P2M/M2M, gate_l for
+    // M2L/L2L/L2P; set by launch_far_gate from the walk's M2L count
+    const int *gate_m, *gate_l;
 };
 
 // M2L of every list, accumulated into L
@@ -33,6 +36,8 @@ int run_m2l_f32(const MultipoleArgs &a, float *M32, cudaStream_t st);
 int run_downward_f32(const MultipoleArgs &a, cudaStream_t st);
 // P2M and M2M, and L zeroed for the M2L that follows
 int run_p2m_m2m(const MultipoleArgs &a, cudaStream_t st);
+// the far-field switches of a captured pass (gate[2], see MultipoleArgs)
+int launch_far_gate(const unsigned long long *walk_ctr, int keep_multipoles, int *gate, cudaStream_t st);
 // op: 0 m2l (in = M, inout = L, rs), 1 m2m (in = M, inout = M'), 2 l2l (in = L, inout = L')
 int launch_op_batch(int op, int n, const double *d, const double *in, double *inout, double rs, cudaStream_t st);
 
