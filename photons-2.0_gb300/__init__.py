@@ -366,8 +366,8 @@ def autotune_leaf(fp, pos, p, candidates=(16, 24, 32, 48, 64), error_bound=1e-4,
     `error_bound`; if none qualifies, the most accurate one.
 
     Returns (best_leaf, table) where table lists, per candidate, the pass
-    time (ms, CUDA events of the pass), pairs per particle and the median /
-    99th-percentile error."""
+    time on the device (ms, CUDA events: tree, walk, P2P, far field, gather),
+    pairs per particle and the median / 99th-percentile error."""
     pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
     rng = np.random.default_rng(seed)
     tgt = rng.choice(pos.shape[0], min(sample, pos.shape[0]), replace=False).astype(np.int32)
@@ -381,7 +381,8 @@ def autotune_leaf(fp, pos, p, candidates=(16, 24, 32, 48, 64), error_bound=1e-4,
         acc = None
         for _ in range(repeats):
             acc = fp.run(pos, q, precision=precision)
-            ms.append(fp.timings()["total"])
+            t = fp.timings()
+            ms.append(t["total"] - t["upload"] - t["download"])  # the device part of the pass
         c = fp.counters()
         err = np.linalg.norm(acc[tgt] - ref, axis=1) / np.maximum(nref, 1e-300)
         table.append(dict(maxleaf=int(leaf), ms=float(min(ms)), median=float(np.median(err)),
