@@ -186,6 +186,28 @@ int photons_drift(int n, double *pos, const double *vel, double dd, double boxsi
 int photons_kdk_step(photons_ctx *ctx, const photons_params *p, int n, double *pos, double *vel, double *acc,
                      double dkh, double dd);
 
+/* ---- Gadget-2 snapshots (the reference's SnapFormat 2, src/snapshot.c:5-22,
+   64-293, 397-549): header block, FP32 position and velocity blocks.  Host
+   functions. ---- */
+typedef struct photons_gadget_header {
+    int npart[6];
+    double mass[6];
+    double time, redshift;
+    int flag_sfr, flag_feedback;
+    int npart_total[6];
+    int flag_cooling, num_files;
+    double boxsize, omega0, omega_lambda, hubble;
+} photons_gadget_header;
+int photons_gadget_read_header(const char *path, photons_gadget_header *h);
+/* particles [first, first+count) of the file (species in order) as FP64:
+   pos[3 count]; vel[3 count] (may be NULL) multiplied by (1/(1+z))^1.5 as
+   src/snapshot.c:163-181 does */
+int photons_gadget_read(const char *path, long long first, long long count, double *pos, double *vel);
+/* one file of n particles (positions and velocities rounded to FP32,
+   velocities divided by (1/(1+z))^1.5 as src/snapshot.c:470-481) */
+int photons_gadget_write(const char *path, const photons_gadget_header *h, long long n, const double *pos,
+                         const double *vel);
+
 /* kernels launched by this library so far (all contexts) */
 unsigned long long photons_launch_count(void);
 

@@ -21,6 +21,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_SO = os.path.join(HERE, "_ref", "libphotons_ref.so")
+REFROOT = os.environ.get("PHOTONS_REFERENCE", "/root/reference")  # the reference tree, where present
 PORT_SO = os.path.join(HERE, "_build", "libphotons_oracle.so")
 
 NMULTI = 20
@@ -113,6 +114,20 @@ class RefOracle(_Base):
             getattr(lib, name).restype = C.c_double
             getattr(lib, name).argtypes = [C.c_double] * 4
         self.lib = lib
+
+    def gadget(self, path):
+        """(header values, pos, vel) read by the reference's own Gadget-2 readers."""
+        lib = self.lib
+        lib.ref_gadget_header.argtypes = [C.c_char_p, _dp]
+        lib.ref_gadget_read.argtypes = [C.c_char_p, C.c_int, _dp, _dp]
+        h = np.zeros(7)
+        lib.ref_gadget_header(path.encode(), _ptr(h))
+        n = int(h[1])
+        pos = np.empty((n, 3))
+        vel = np.empty((n, 3))
+        lib.ref_gadget_read(path.encode(), n, _ptr(pos), _ptr(vel))
+        keys = ("boxsize", "npart_total", "mass", "omega0", "omega_lambda", "hubble", "redshift")
+        return dict(zip(keys, h.tolist())), pos, vel
 
     def kick_loga(self, om, ox, la, lb):
         return self.lib.ref_kick_loga(om, ox, la, lb)

@@ -278,3 +278,34 @@ double ref_drift_loga(double omega_m, double omega_x, double loga_i, double loga
     OmegaX0 = omega_x;
     return drift_loga(loga_i, loga_f);
 }
+
+/* Gadget-2 snapshots through the reference's own readers
+   (src/snapshot.c:64-118, 209-293): header values and particles [0, n). */
+void read_GadgetHeader(const char filename[]);
+void read_Particle_Gadget2(char filename[], int n_start, int n_count);
+
+void ref_gadget_header(const char *path, double *out)
+{
+    read_GadgetHeader(path);
+    out[0] = BOXSIZE;
+    out[1] = (double)NPART_TOTAL;
+    out[2] = MASSPART;
+    out[3] = OmegaM0;
+    out[4] = OmegaX0;
+    out[5] = Hubble0;
+    out[6] = InitialTime;
+}
+
+void ref_gadget_read(const char *path, int n, double *pos, double *vel)
+{
+    Body *saved = part;
+    part = (Body *)calloc((size_t)n, sizeof(Body));
+    read_Particle_Gadget2((char *)path, 0, n);
+    for (int i = 0; i < n; i++)
+        for (int d = 0; d < 3; d++) {
+            pos[3 * i + d] = part[i].pos[d];
+            vel[3 * i + d] = part[i].vel[d];
+        }
+    free(part);
+    part = saved;
+}

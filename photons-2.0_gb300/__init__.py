@@ -271,6 +271,47 @@ def direct_sum(pos, p, targets, rmax=None):
     return out
 
 
+class GadgetHeader(C.Structure):
+    _fields_ = [("npart", C.c_int * 6), ("mass", C.c_double * 6), ("time", C.c_double), ("redshift", C.c_double),
+                ("flag_sfr", C.c_int), ("flag_feedback", C.c_int), ("npart_total", C.c_int * 6),
+                ("flag_cooling", C.c_int), ("num_files", C.c_int), ("boxsize", C.c_double), ("omega0", C.c_double),
+                ("omega_lambda", C.c_double), ("hubble", C.c_double)]
+
+
+def gadget_read(path, first=0, count=None):
+    """Gadget-2 snapshot -> (header dict, pos (n,3), vel (n,3)); velocities
+    scaled by (1/(1+z))^1.5 as the reference reads them."""
+    lib = load_library()
+    lib.photons_gadget_read_header.argtypes = [C.c_char_p, C.POINTER(GadgetHeader)]
+    lib.photons_gadget_read.argtypes = [C.c_char_p, C.c_longlong, C.c_longlong, C.c_void_p, C.c_void_p]
+    h = GadgetHeader()
+    _check(lib.photons_gadget_read_header(str(path).encode(), C.byref(h)))
+    n = sum(h.npart) - first if count is None else count
+    pos = np.empty((n, 3))
+    vel = np.empty((n, 3))
+    _check(lib.photons_gadget_read(str(path).encode(), first, n, pos.ctypes.data, vel.ctypes.data))
+    hd = {f: (list(getattr(h, f)) if f in ("npart", "mass", "npart_total") else getattr(h, f)) for f, _ in h._fields_}
+    return hd, pos, vel
+
+
+def gadget_write(path, header, pos, vel):
+    """Write one Gadget-2 file (header dict as gadget_read returns)."""
+    lib = load_library()
+    lib.photons_gadget_write.argtypes = [C.c_char_p, C.POINTER(GadgetHeader), C.c_longlong, C.c_void_p, C.c_void_p]
+    h = GadgetHeader()
+    for f, _ in h._fields_:
+        v = header.get(f, 0)
+        if f in ("npart", "mass", "npart_total"):
+            arr = getattr(h, f)
+            for i, x in enumerate(v if v else [0] * 6):
+                arr[i] = x
+        else:
+            setattr(h, f, v)
+    pos = np.ascontiguousarray(pos, np.float64)
+    vel = np.ascontiguousarray(vel, np.float64)
+    _check(lib.photons_gadget_write(str(path).encode(), C.byref(h), pos.shape[0], pos.ctypes.data, vel.ctypes.data))
+
+
 def kick_loga(omega_m, omega_x, loga_i, loga_f):
     """The reference's kick factor over [loga_i, loga_f] (src/initial.c:639-660)."""
     return load_library().photons_kick_loga(float(omega_m), float(omega_x), float(loga_i), float(loga_f))

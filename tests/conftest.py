@@ -54,6 +54,8 @@ def golden_names():
 def load_golden(name):
     z = np.load(os.path.join(GOLDEN, name + ".npz"))
     d = {k: z[k] for k in z.files}
+    for k in ("pos_in", "pos_tree"):  # stored as FP32 where the input itself is FP32 (exact)
+        d[k] = d[k].astype(np.float64)
     pr = d["params"]
     d["p"] = dict(boxsize=pr[0], theta=pr[1], rs=pr[2], rcut=pr[3], eps=pr[4], mass=pr[5], maxleaf=int(pr[6]))
     return d

@@ -2,7 +2,7 @@
 own FMM sources (compiled in place into oracle/_ref/libphotons_ref.so by
 oracle/Makefile, with the one-rank MPI stand-in) on small seeded inputs.
 
-    make -C oracle ref && python tests/golden/make_golden.py
+    make -C oracle ref && python tests/golden/make_golden.py [names]
 
 Each fixture holds the input positions and force parameters, and the
 reference's outputs: the tree-ordered positions (its in-place permutation),
@@ -60,12 +60,26 @@ def cases():
     pos = rng.random((300, 3)) * 20.0
     p = ics.force_params(300, 20.0, 40, theta=0.5, maxleaf=1)
     out.append(("random300_leaf1", pos, p, True))
+    # the reference's demo initial conditions (z = 49 LCDM, 32^3 particles)
+    # read by its own Gadget-2 reader, with its demo run's parameters
+    # (demo/lcdm_g2.run: OPENANGLE 0.4, MaxPackage 8, NumMeshSide 32) and its
+    # derived force parameters (src/initial.c:316-337)
+    demo = os.path.join(oracle.REFROOT, "demo", "ic_lcdm.gdt2")
+    if os.path.exists(demo):
+        hd, pos, _ = oracle.RefOracle().gadget(demo)
+        L = hd["boxsize"]
+        rs = 1.25 * L / 32
+        p = dict(boxsize=L, theta=0.4, rs=rs, rcut=4.5 * rs, eps=0.03 * L / pow(float(pos.shape[0]), 0.3333333),
+                 mass=hd["mass"], maxleaf=8)
+        out.append(("demo_lcdm_leaf8", pos, p, False))
     return out
 
 
-def main():
+def main(only=None):
     ref = oracle.RefOracle()
     for name, pos, p, full in cases():
+        if only and name not in only:
+            continue
         r = ref.run(pos, p, capture=True, tree=True)
         d = {
             "pos_in": pos, "pos_tree": r["pos"], "acc_task": r["acc_task"], "acc": r["acc"],
@@ -83,6 +97,13 @@ def main():
             d["ntarget_" + kind] = np.bincount(t - t.min(), minlength=1).astype(np.int32) if t.size else np.zeros(0, np.int32)
             if full:
                 d["list_" + kind] = np.stack([t, s, im]).astype(np.int32)
+        if name.startswith("demo"):
+            # positions are FP32 in the snapshot, so FP32 storage is exact;
+            # the fmm_task-only accelerations are left out to keep it small
+            d["pos_in"] = d["pos_in"].astype(np.float32)
+            d["pos_tree"] = d["pos_tree"].astype(np.float32)
+            assert np.array_equal(d["pos_in"].astype(np.float64), pos)
+            del d["acc_task"]
         path = os.path.join(HERE, name + ".npz")
         np.savez_compressed(path, **d)
         c = r["counters"]
@@ -110,5 +131,8 @@ def time_integrals():
 
 
 if __name__ == "__main__":
-    main()
-    time_integrals()
+    # python make_golden.py [fixture names]  (default: all)
+    names = sys.argv[1:]
+    main(names or None)
+    if not names or "time" in names:
+        time_integrals()

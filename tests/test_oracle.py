@@ -37,7 +37,8 @@ def test_port_matches_golden(port, name):
             # full lists, in the reference's order
             assert np.array_equal(np.stack([t, s, im]), g["list_" + kind]), kind
     # without M2L the sums run in the reference's order: identical bits
-    assert np.array_equal(r["acc_task"], g["acc_task"])
+    if "acc_task" in g:
+        assert np.array_equal(r["acc_task"], g["acc_task"])
     if g["counters"][2] == 0:
         assert np.array_equal(r["acc"], g["acc"])
     else:
