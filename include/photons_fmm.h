@@ -186,6 +186,15 @@ int photons_drift(int n, double *pos, const double *vel, double dd, double boxsi
 int photons_kdk_step(photons_ctx *ctx, const photons_params *p, int n, double *pos, double *vel, double *acc,
                      double dkh, double dd);
 
+/* ---- PM long-range force (src/partmesh.c:18-800 at one rank, the
+   convolution of src/conv.f90:128-247): CIC deposit of the particle mass on
+   an nside^3 periodic mesh, FFT, the long-range Green's function
+   exp(-k^2 rs^2)/k^2 with the CIC window deconvolved, inverse FFT, 4-point
+   gradient and CIC interpolation: acc_pm[3n] (G-free, like the short-range
+   acc).  Uses boxsize, rs and mass of p; host or device pointers per
+   PHOTONS_F_DEVICE_IO.  Returns after the work is done. ---- */
+int photons_pm_force(photons_ctx *ctx, const photons_params *p, int nside, int n, const double *pos, double *acc_pm);
+
 /* ---- Gadget-2 snapshots (the reference's SnapFormat 2, src/snapshot.c:5-22,
    64-293, 397-549): header block, FP32 position and velocity blocks.  Host
    functions. ---- */

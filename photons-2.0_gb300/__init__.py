@@ -107,6 +107,7 @@ def load_library():
         getattr(lib, name).argtypes = [C.c_double] * 4
     lib.photons_kick.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]
     lib.photons_drift.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_void_p]
+    lib.photons_pm_force.argtypes = [C.c_void_p, C.POINTER(Params), C.c_int, C.c_int, C.c_void_p, C.c_void_p]
     lib.photons_kdk_step.argtypes = [C.c_void_p, C.POINTER(Params), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.c_double, C.c_double]
     _lib = lib
@@ -193,6 +194,15 @@ class ForcePass:
         _check(self.lib.photons_kdk_step(self.h, C.byref(prm), int(n), C.c_void_p(pos_ptr), C.c_void_p(vel_ptr),
                                          C.c_void_p(acc_ptr), float(dkh), float(dd)))
         self.n = n
+
+    def pm_force(self, pos, p, nside):
+        """PM long-range acceleration (n,3) on an nside^3 mesh (host arrays)."""
+        pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+        acc = np.empty_like(pos)
+        prm = make_params(p, FP64, 0, 0)
+        _check(self.lib.photons_pm_force(self.h, C.byref(prm), int(nside), pos.shape[0], pos.ctypes.data,
+                                         acc.ctypes.data))
+        return acc
 
     def counters(self):
         v = np.zeros(32, np.int64)

@@ -18,7 +18,7 @@ LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libphotons_fmm.so")
 INCLUDE = os.path.join(ROOT, "include")
 
-SOURCES = ["scan.cu", "tree.cu", "walk.cu", "p2p.cu", "multipole.cu", "api.cu", "legacy.cu", "direct.cu", "noalloc.cu", "integrate.cu", "snapshot.cu"]
+SOURCES = ["scan.cu", "tree.cu", "walk.cu", "p2p.cu", "multipole.cu", "api.cu", "legacy.cu", "direct.cu", "noalloc.cu", "integrate.cu", "snapshot.cu", "pm.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code is not contracted into FMAs (the host operators and integrals
 # follow the reference's separately rounded arithmetic on every host CPU)
@@ -67,7 +67,7 @@ def build(force=False, verbose=False):
             if err.strip():
                 print(err)
     if force or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-lcufft"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stdout + r.stderr))

@@ -809,6 +809,8 @@ extern "C" void photons_destroy(photons_ctx *c)
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    ph_pm_release(c);
+    cudaFree(c->pm_io);
     free_all(c);
     for (int i = 0; i < EV_COUNT; i++) cudaEventDestroy(c->ev[i]);
     cudaStreamDestroy(c->own_stream);

@@ -7,6 +7,8 @@
 #include "fmm_context.cuh"
 #include "multipole.cuh"
 #include "p2p.cuh"
+#include <cufft.h>
+
 #include "photons_fmm.h"
 
 enum {
@@ -50,6 +52,11 @@ struct photons_ctx {
     double *io = nullptr;  // 3*cap_n staging for host transfers and gathers
     int *work_counter = nullptr;
     int *far_gate = nullptr;  // [2] far-field switches of the captured pass
+    // PM mesh (pm.cu): density / potential, half spectrum, gradient grids, FFT plans
+    int pm_n = 0, pm_cap_io = 0;
+    double *pm_rho = nullptr, *pm_grad = nullptr, *pm_io = nullptr;
+    cufftDoubleComplex *pm_rk = nullptr;
+    cufftHandle pm_plan_r2c = 0, pm_plan_c2r = 0;
     int cap_n = 0, cap_u = 0;
     // last pass
     PassParams pp{};
@@ -94,6 +101,8 @@ int ph_stage_m2l(photons_ctx *c, int precision);
 int ph_stage_downward(photons_ctx *c, int precision);
 int ph_stage_output(photons_ctx *c, double *acc, int device_io, int tree_order);
 int ph_download_tree(photons_ctx *c, HostTree &h, bool with_expansions);
+int ph_pm_enqueue(photons_ctx *c, const photons_params *p, int nside, int n, const double *pos, double *acc_pm);
+void ph_pm_release(photons_ctx *c);
 
 namespace ph {
 int launch_init_particles(BuildBufs &b, const double *pos, int n, cudaStream_t st);
