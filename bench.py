@@ -216,11 +216,40 @@ def kdk_measure(ph, fp, torch, stream, dpos, dacc, n, p, steps):
     e1.record(stream)
     torch.cuda.synchronize()
     drift_ms = e0.elapsed_time(e1) / reps
+    # PM long-range force on the configuration's mesh, and the step with both halves
+    import ctypes as C
+    nside = int(round(p["boxsize"] / (p["rs"] / 1.25)))
+    acc_pm = torch.zeros_like(pos)
+    prm = ph.make_params(p, ph.FP64, 0, ph.F_DEVICE_IO)
+
+    def pm():
+        rc = fp.lib.photons_pm_force(fp.h, C.byref(prm), nside, n, C.c_void_p(pos.data_ptr()),
+                                     C.c_void_p(acc_pm.data_ptr()))
+        if rc:
+            raise RuntimeError(fp.lib.photons_gpu_error().decode())
+
+    pm()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        pm()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    pm_ms = e0.elapsed_time(e1) / reps
+    fp.kdk_step_pm_device(pos.data_ptr(), vel.data_ptr(), acc.data_ptr(), acc_pm.data_ptr(), n, p, nside, dkh, dd)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        fp.kdk_step_pm_device(pos.data_ptr(), vel.data_ptr(), acc.data_ptr(), acc_pm.data_ptr(), n, p, nside, dkh, dd)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    step_pm_ms = e0.elapsed_time(e1) / steps
     bytes_each = 3 * n * 24  # read two arrays, write one, 3n doubles
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     hbm = peaks.get("hbm_gbs")
-    out = {"step_ms": step_ms, "a": [0.5, 0.505], "dkh": dkh, "dd": dd,
+    out = {"step_ms": step_ms, "step_with_pm_ms": step_pm_ms, "pm_ms": pm_ms, "pm_mesh": nside,
+           "a": [0.5, 0.505], "dkh": dkh, "dd": dd,
            "kick_ms": kick_ms, "drift_ms": drift_ms,
            "kick_gbs": bytes_each / (kick_ms * 1e-3) / 1e9, "drift_gbs": bytes_each / (drift_ms * 1e-3) / 1e9,
            "bytes_per_kernel": bytes_each}

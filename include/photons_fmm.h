@@ -217,6 +217,13 @@ int photons_gadget_read(const char *path, long long first, long long count, doub
 int photons_gadget_write(const char *path, const photons_gadget_header *h, long long n, const double *pos,
                          const double *vel);
 
+/* the reference's whole step with both halves of the force, on device
+   arrays: kick with acc_pm then acc, drift and wrap, short-range pass into
+   acc and PM (nside^3 mesh) into acc_pm, kick with acc then acc_pm
+   (src/photoNs.c:158-196, 229-268) */
+int photons_kdk_step_pm(photons_ctx *ctx, const photons_params *p, int nside, int n, double *pos, double *vel,
+                        double *acc, double *acc_pm, double dkh, double dd);
+
 /* kernels launched by this library so far (all contexts) */
 unsigned long long photons_launch_count(void);
 

@@ -108,6 +108,8 @@ def load_library():
     lib.photons_kick.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]
     lib.photons_drift.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_void_p]
     lib.photons_pm_force.argtypes = [C.c_void_p, C.POINTER(Params), C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+    lib.photons_kdk_step_pm.argtypes = [C.c_void_p, C.POINTER(Params), C.c_int, C.c_int] + [C.c_void_p] * 4 + \
+        [C.c_double, C.c_double]
     lib.photons_kdk_step.argtypes = [C.c_void_p, C.POINTER(Params), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.c_double, C.c_double]
     _lib = lib
@@ -193,6 +195,15 @@ class ForcePass:
         prm = make_params(p, precision, image_mask, flags | F_DEVICE_IO)
         _check(self.lib.photons_kdk_step(self.h, C.byref(prm), int(n), C.c_void_p(pos_ptr), C.c_void_p(vel_ptr),
                                          C.c_void_p(acc_ptr), float(dkh), float(dd)))
+        self.n = n
+
+    def kdk_step_pm_device(self, pos_ptr, vel_ptr, acc_ptr, acc_pm_ptr, n, p, nside, dkh, dd, precision=FP32_SPLIT,
+                           flags=0):
+        """The reference's step with both force halves on device arrays (n,3) float64."""
+        prm = make_params(p, precision, 0, flags | F_DEVICE_IO)
+        _check(self.lib.photons_kdk_step_pm(self.h, C.byref(prm), int(nside), int(n), C.c_void_p(pos_ptr),
+                                            C.c_void_p(vel_ptr), C.c_void_p(acc_ptr), C.c_void_p(acc_pm_ptr),
+                                            float(dkh), float(dd)))
         self.n = n
 
     def pm_force(self, pos, p, nside):

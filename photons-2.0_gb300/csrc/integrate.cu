@@ -147,3 +147,27 @@ extern "C" int photons_kdk_step(photons_ctx *c, const photons_params *p, int n, 
     PH_CUDA_CHECK(cudaStreamSynchronize(st));
     return 0;
 }
+
+extern "C" int photons_kdk_step_pm(photons_ctx *c, const photons_params *p, int nside, int n, double *pos,
+                                   double *vel, double *acc, double *acc_pm, double dkh, double dd)
+{
+    photons_gpu_clear_error();
+    if (!c || !p || !acc_pm) return ph_set_error(PH_ERR_ARG, "null argument");
+    cudaSetDevice(c->device);
+    cudaStream_t st = c->stream;
+    // src/photoNs.c:158-196: PM kick, short-range kick, drift and wrap
+    PH_TRY(enqueue_kick(n, vel, acc_pm, dkh, st));
+    PH_TRY(enqueue_kick(n, vel, acc, dkh, st));
+    PH_TRY(enqueue_drift(n, pos, vel, dd, p->boxsize, st));
+    // forces at the new positions: the short-range pass and the PM mesh
+    photons_params q = *p;
+    q.flags |= PHOTONS_F_DEVICE_IO;
+    q.flags &= ~PHOTONS_F_TREE_ORDER;
+    PH_TRY(photons_force_pass(c, &q, n, pos, acc));
+    PH_TRY(ph_pm_enqueue(c, &q, nside, n, pos, acc_pm));
+    // src/photoNs.c:257-268: short-range kick, then PM kick
+    PH_TRY(enqueue_kick(n, vel, acc, dkh, st));
+    PH_TRY(enqueue_kick(n, vel, acc_pm, dkh, st));
+    PH_CUDA_CHECK(cudaStreamSynchronize(st));
+    return 0;
+}

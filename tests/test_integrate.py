@@ -119,3 +119,38 @@ def test_kdk_step_matches_host_composition(ph, port, ics, precision):
     assert np.array_equal(dpos.cpu().numpy(), hp)
     assert np.array_equal(dacc.cpu().numpy(), acc1)
     assert np.array_equal(dvel.cpu().numpy(), hv)
+
+
+@pytest.mark.gpu
+def test_kdk_step_with_pm_matches_host_composition(ph, port, ics):
+    """The full step with both halves of the force, against the oracle's
+    kicks and drift around separately computed short-range and PM forces."""
+    torch = pytest.importorskip("torch")
+    pos, p = ics.make("zeldovich512", nside=24, maxleaf=16)
+    rng = np.random.default_rng(5)
+    vel = rng.standard_normal(pos.shape) * 0.5
+    nside = 24
+    la, lb = math.log(0.5), math.log(0.505)
+    dkh = 0.5 * ph.kick_loga(0.3, 0.7, la, lb) * 43007.105732
+    dd = ph.drift_loga(0.3, 0.7, la, lb)
+    fp = ph.ForcePass(0)
+    acc0 = fp.run(pos, p, precision=ph.FP64)
+    pm0 = fp.pm_force(pos, p, nside)
+    dpos, dvel, dacc, dpm = (torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (pos, vel, acc0, pm0))
+    torch.cuda.synchronize()
+    fp.kdk_step_pm_device(dpos.data_ptr(), dvel.data_ptr(), dacc.data_ptr(), dpm.data_ptr(), pos.shape[0], p, nside,
+                          dkh, dd, precision=ph.FP64)
+    hp, hv = pos.copy(), vel.copy()
+    port.kick(hv, pm0, dkh)
+    port.kick(hv, acc0, dkh)
+    port.drift(hp, hv, dd, p["boxsize"])
+    acc1 = fp.run(hp, p, precision=ph.FP64)
+    pm1 = fp.pm_force(hp, p, nside)
+    assert np.array_equal(dpos.cpu().numpy(), hp)
+    assert np.array_equal(dacc.cpu().numpy(), acc1)
+    # the PM deposit adds with atomics: its last bits vary between runs
+    gpm = dpm.cpu().numpy()
+    assert np.abs(gpm - pm1).max() <= 1e-12 * np.abs(pm1).max()
+    port.kick(hv, acc1, dkh)
+    port.kick(hv, gpm, dkh)
+    assert np.array_equal(dvel.cpu().numpy(), hv)
