@@ -153,6 +153,11 @@ static int alloc_tree(photons_ctx *c, int n, int cap)
         PH_TRY(dalloc(w.m2l_off, cu)); PH_TRY(dalloc(w.m2l_cnt, cu));
         PH_TRY(dalloc(t.chi, cu)); PH_TRY(dalloc(t.clo, cu)); PH_TRY(dalloc(t.w32, cu)); PH_TRY(dalloc(t.son2, cu));
         PH_TRY(dalloc(t.boxid, cu));
+        PH_TRY(dalloc(c->mu_sorted, cu)); PH_TRY(dalloc(c->mu_nrecv, cu));
+        PH_TRY(dalloc(c->mu_size, cu)); PH_TRY(dalloc(c->mu_rbase, cu));
+        PH_TRY(dalloc(c->mu_scan, ph::scan_scratch_elems(cu) + 8));
+        if (!c->mu_total) { PH_TRY(dalloc(c->mu_total, 1)); PH_TRY(dalloc(c->mu_over, 1)); }
+        c->mu_cap_leaves = cu;
         PH_TRY(dalloc(c->M, (size_t)cu * PH_NMULTI));
         PH_TRY(dalloc(c->L, (size_t)cu * PH_NMULTI));
         PH_TRY(dalloc(c->M32, (size_t)cu * PH_NMULTI));
@@ -180,7 +185,13 @@ static int alloc_walk(photons_ctx *c, long long p2p_cap, long long pd_cap, long 
     if (!w.ctr) { PH_TRY(dalloc(w.ctr, ph::WC_N)); c->epoch++; }
     if (!c->far_gate) { PH_TRY(dalloc(c->far_gate, 2)); c->epoch++; }
     if (!c->work_counter) { PH_TRY(dalloc(c->work_counter, 4)); c->epoch++; }
-    if (p2p_cap > w.p2p_cap) { PH_TRY(dalloc(w.p2p_pool, p2p_cap)); w.p2p_cap = p2p_cap; c->epoch++; }
+    if (p2p_cap > w.p2p_cap) {
+        PH_TRY(dalloc(w.p2p_pool, p2p_cap));
+        PH_TRY(dalloc(c->mu_slot, p2p_cap));
+        w.p2p_cap = p2p_cap;
+        c->mu_slot_cap = p2p_cap;
+        c->epoch++;
+    }
     if (pd_cap > w.pd_cap) {
         PH_TRY(dalloc(w.pd_pool[0], pd_cap));
         PH_TRY(dalloc(w.pd_pool[1], pd_cap));
@@ -217,7 +228,8 @@ static void free_all(photons_ctx *c)
                     c->w.m2l_pool, c->w.m2l_off, c->w.m2l_cnt, c->w.scratch, c->w.ctr, c->pos4, c->ax, c->ay,
                     c->az, c->M, c->L, c->io, c->work_counter, c->t.chi, c->t.clo, c->t.w32, c->t.son2, c->M32,
                     b.lvl_begin, b.lvl_count, b.leaf_begin, b.leaf_count, c->t.depth_cnt, b.tn_boxid, b.tl_boxid,
-                    c->t.boxid, b.boxes, c->far_gate};
+                    c->t.boxid, b.boxes, c->far_gate, c->mu_sorted, c->mu_nrecv, c->mu_slot, c->mu_over,
+                    c->mu_size, c->mu_rbase, c->mu_total, c->mu_scan, c->mu_buf};
     for (void *p : ptrs)
         if (p) cudaFree(p);
 }
@@ -240,11 +252,39 @@ __global__ void k_gather_out(const int *perm, const double *ax, const double *ay
 
 }  // namespace
 
-// FP32 P2P kernel: 0 packed pairs (default), 1 scalar (PHOTONS_P2P_KERNEL=scalar)
+// FP32 P2P kernel: 2 mutual pairs (default for MAXLEAF <= 64), 0 packed
+// one-way pairs, 1 scalar (PHOTONS_P2P_KERNEL=mutual|packed|scalar)
 static int p2p_variant()
 {
     const char *v = getenv("PHOTONS_P2P_KERNEL");
-    return (v && !strcmp(v, "scalar")) ? 1 : 0;
+    if (v && !strcmp(v, "scalar")) return 1;
+    if (v && !strcmp(v, "packed")) return 0;
+    return 2;
+}
+
+// the reaction buffer of the mutual kernel (floats); grown from the last
+// pass's need, which the device reports when it did not fit
+// A reaction buffer that was too small made the pass evaluate every pair
+// one way (correct, but not the mutual kernel's rounding); size it and
+// report that the pass should be repeated, so results never depend on
+// whether an earlier pass had already grown the buffer.
+static bool mutual_feedback(photons_ctx *c, int over, long long need)
+{
+    if (!over || need <= c->mu_buf_cap) return false;
+    c->hint_mubuf = need + need / 16 + 4096;
+    return true;
+}
+
+static int alloc_mutual(photons_ctx *c)
+{
+    // first guess: about half of a leaf's ~130-250 list entries received, 3 floats per particle
+    long long want = c->hint_mubuf ? c->hint_mubuf : (long long)c->n * 256 + 4096;
+    if (want > c->mu_buf_cap) {
+        PH_TRY(dalloc(c->mu_buf, (size_t)want));
+        c->mu_buf_cap = want;
+        c->epoch++;
+    }
+    return 0;
 }
 
 // ------------------------------------------------------------------
@@ -551,6 +591,9 @@ int ph_stage_walk(photons_ctx *c, unsigned mask)
 int ph_stage_p2p(photons_ctx *c, int precision, int zero)
 {
     cudaStream_t st = c->stream;
+    PH_TRY(alloc_mutual(c));
+    PH_CUDA_CHECK(cudaMemsetAsync(c->mu_over, 0, sizeof(int), st));
+    PH_CUDA_CHECK(cudaMemsetAsync(c->mu_total, 0, sizeof(long long), st));
     const int n = c->n;
     if (zero) {
         PH_CUDA_CHECK(cudaMemsetAsync(c->ax, 0, sizeof(double) * n, st));
@@ -577,7 +620,17 @@ int ph_stage_p2p(photons_ctx *c, int precision, int zero)
     a.k = ph::make_split_consts(c->pp);
     a.variant = p2p_variant();
     PH_TRY(ph_record(c, EV_P2P_BEGIN));
-    PH_TRY(ph::launch_p2p(a, precision == PHOTONS_FP64, st));
+    if (precision != PHOTONS_FP64 && a.variant == 2 && c->pp.maxleaf <= 64) {
+        ph::MutualBufs m;
+        m.pool = c->w.p2p_pool;
+        m.sorted = c->mu_sorted; m.nrecv = c->mu_nrecv; m.size = c->mu_size; m.rbase = c->mu_rbase;
+        m.total = c->mu_total; m.scan_scratch = c->mu_scan; m.slot = c->mu_slot; m.over = c->mu_over;
+        m.buf = c->mu_buf; m.buf_cap = c->mu_buf_cap; m.cap_leaves = c->mu_cap_leaves;
+        PH_TRY(ph::launch_p2p_mutual(a, m, st));
+    } else {
+        if (a.variant == 2) a.variant = 0;
+        PH_TRY(ph::launch_p2p(a, precision == PHOTONS_FP64, st));
+    }
     return ph_record(c, EV_P2P);
 }
 
@@ -738,6 +791,7 @@ static int force_pass_graph(photons_ctx *c, int nbox, const photons_params *p, c
     double *dst = dio ? acc : c->io;
     for (int attempt = 0; attempt < 16; attempt++) {
         PH_TRY(alloc_walk(c, p2p_cap, pd_cap, m2l_cap, stack_cap, stage_cap));
+        PH_TRY(alloc_mutual(c));
         PassKey k = pass_key(c, p, n, pos, acc, dio, levels, mask);
         if (!c->gexec || !c->have_key || memcmp(&k, &c->key, sizeof k) != 0) {
             PH_TRY(capture_pass(c, p, src, dst, levels, mask));
@@ -758,7 +812,12 @@ static int force_pass_graph(photons_ctx *c, int nbox, const photons_params *p, c
         c->info.depth_off.resize(levels + 2);
         PH_CUDA_CHECK(cudaMemcpyAsync(c->info.depth_off.data(), c->t.depth_off, sizeof(int) * (levels + 2),
                                       cudaMemcpyDeviceToHost, st));
+        long long mu_need = 0;
+        int mu_over = 0;
+        PH_CUDA_CHECK(cudaMemcpyAsync(&mu_need, c->mu_total, sizeof mu_need, cudaMemcpyDeviceToHost, st));
+        PH_CUDA_CHECK(cudaMemcpyAsync(&mu_over, c->mu_over, sizeof mu_over, cudaMemcpyDeviceToHost, st));
         PH_CUDA_CHECK(cudaStreamSynchronize(st));
+        const bool mu_grow = mutual_feedback(c, mu_over, mu_need);
         int grow = 0;
         PH_TRY(ph_check_build(c, h[ph::BC_FLAGS], levels, &grow));
         if (grow) { levels = grow; continue; }
@@ -769,6 +828,7 @@ static int force_pass_graph(photons_ctx *c, int nbox, const photons_params *p, c
             grow_walk_caps(c, fl, p2p_cap, pd_cap, m2l_cap, stack_cap, stage_cap);
             continue;
         }
+        if (mu_grow) continue;
         c->info.depth_off.resize(c->info.depth + 2);
         c->have_lists = true;
         c->mask = mask;
@@ -838,22 +898,30 @@ static int force_pass_boxes(photons_ctx *c, int nbox, const photons_params *p, c
     if (!(g && !strcmp(g, "0"))) {
         PH_TRY(force_pass_graph(c, nbox, p, counts, pos, acc, dio, mask));
     } else {
-        // stage by stage, with the host checking the build and the walk
-        PH_TRY(ph_stage_build_boxes(c, nbox, p, counts, pos, dio));
-        PH_TRY(ph_stage_walk(c, mask));
-        PH_TRY(ph_stage_p2p(c, p->precision, 1));
-        const bool far = !(p->flags & PHOTONS_F_NO_FARFIELD);
-        const unsigned long long nm2l = c->ws.c[ph::WC_M2L_LOCAL] + c->ws.c[ph::WC_M2L_IMAGE];
-        if (far && (nm2l > 0 || (p->flags & PHOTONS_F_MULTIPOLES))) {
-            PH_TRY(ph_stage_multipoles(c));
-            PH_TRY(ph_stage_m2l(c, p->precision));
-            PH_TRY(ph_stage_downward(c, p->precision));
-        } else if (p->flags & PHOTONS_F_MULTIPOLES) {
-            PH_TRY(ph_stage_multipoles(c));
+        // stage by stage, with the host checking the build and the walk; a second
+        // attempt only when the mutual kernel's reaction buffer had to grow
+        for (int attempt = 0; attempt < 2; attempt++) {
+            PH_TRY(ph_stage_build_boxes(c, nbox, p, counts, pos, dio));
+            PH_TRY(ph_stage_walk(c, mask));
+            PH_TRY(ph_stage_p2p(c, p->precision, 1));
+            const bool far = !(p->flags & PHOTONS_F_NO_FARFIELD);
+            const unsigned long long nm2l = c->ws.c[ph::WC_M2L_LOCAL] + c->ws.c[ph::WC_M2L_IMAGE];
+            if (far && (nm2l > 0 || (p->flags & PHOTONS_F_MULTIPOLES))) {
+                PH_TRY(ph_stage_multipoles(c));
+                PH_TRY(ph_stage_m2l(c, p->precision));
+                PH_TRY(ph_stage_downward(c, p->precision));
+            } else if (p->flags & PHOTONS_F_MULTIPOLES) {
+                PH_TRY(ph_stage_multipoles(c));
+            }
+            PH_TRY(ph_record(c, EV_FAR));
+            PH_TRY(ph_stage_output(c, acc, dio, p->flags & PHOTONS_F_TREE_ORDER));
+            PH_CUDA_CHECK(cudaStreamSynchronize(c->stream));
+            long long mu_need = 0;
+            int mu_over = 0;
+            PH_CUDA_CHECK(cudaMemcpy(&mu_need, c->mu_total, sizeof mu_need, cudaMemcpyDeviceToHost));
+            PH_CUDA_CHECK(cudaMemcpy(&mu_over, c->mu_over, sizeof mu_over, cudaMemcpyDeviceToHost));
+            if (!mutual_feedback(c, mu_over, mu_need)) break;
         }
-        PH_TRY(ph_record(c, EV_FAR));
-        PH_TRY(ph_stage_output(c, acc, dio, p->flags & PHOTONS_F_TREE_ORDER));
-        PH_CUDA_CHECK(cudaStreamSynchronize(c->stream));
     }
     c->last_flags = p->flags;
     c->precision = p->precision;

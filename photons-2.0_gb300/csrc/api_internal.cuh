@@ -52,6 +52,12 @@ struct photons_ctx {
     double *io = nullptr;  // 3*cap_n staging for host transfers and gathers
     int *work_counter = nullptr;
     int *far_gate = nullptr;  // [2] far-field switches of the captured pass
+    // mutual P2P (p2p.cu): per-leaf pairing data, per-entry slots, reaction buffer
+    int *mu_sorted = nullptr, *mu_nrecv = nullptr, *mu_slot = nullptr, *mu_over = nullptr;
+    long long *mu_size = nullptr, *mu_rbase = nullptr, *mu_total = nullptr, *mu_scan = nullptr;
+    float *mu_buf = nullptr;
+    long long mu_buf_cap = 0, mu_slot_cap = 0, hint_mubuf = 0;
+    int mu_cap_leaves = 0;
     // PM mesh (pm.cu): density / potential, half spectrum, gradient grids, FFT plans
     int pm_n = 0, pm_cap_io = 0;
     double *pm_rho = nullptr, *pm_grad = nullptr, *pm_io = nullptr;

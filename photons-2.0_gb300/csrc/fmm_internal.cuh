@@ -120,6 +120,9 @@ inline void note_launch() { g_launches++; }
 void scan_exclusive_i32(const int *in, int *out, const int *n_ptr, int cap, int *total, int *scratch,
                         size_t scratch_elems, cudaStream_t st);
 size_t scan_scratch_elems(int cap);
+// the same over 64-bit values; scratch holds scan_scratch_elems(cap) values
+void scan_exclusive_i64(const long long *in, long long *out, const int *n_ptr, int cap, long long *total,
+                        long long *scratch, cudaStream_t st);
 
 }  // namespace ph
 

@@ -635,6 +635,322 @@ __global__ void k_leaf_offsets(const double *px, const double *py, const double 
     }
 }
 
+
+// ---------------------------------------------------------------------
+// FP32 split-precision P2P with mutual pairs.
+//
+// The local P2P lists are symmetric (leaf B is in A's list exactly when A is
+// in B's), so each such pair is evaluated once: the leaf with the lower id
+// (the owner) computes the forces on its own particles and the equal and
+// opposite reactions on the other leaf's particles, which it stores in a
+// slot of a reaction buffer; a second kernel adds each leaf's received
+// reactions in list order.  Self pairs, image pairs and any entry whose
+// partner entry is missing are evaluated one way, as before.  Results are
+// deterministic.
+//
+// Pairing: every target's list is sorted by raw entry value (local sources
+// first, by id); a local entry (A, B) is mutual when both lists are sorted
+// and B's list holds A; its slot is A's rank q in B's list.  B's received
+// entries are then the leading entries of its list (ids below B), so slot
+// q of B lives at rbase[B] + q nB 3 floats.
+//
+// Lanes: 8 target groups x 4 source groups; a lane holds 8 targets (as four
+// pairs of the paired FP32 instructions) and takes 8 sources of each batch
+// of 32, so reactions are summed over 8 target groups through shared memory
+// and target sums over 4 source groups at the end (FP64, fixed order).
+// ---------------------------------------------------------------------
+#define MU_TB 128
+#define MU_WARPS (MU_TB / 32)
+#ifndef MU_MINB
+#define MU_MINB 4  // resident blocks of MU_TB per SM the mutual kernel is compiled for (126 registers)
+#endif
+#ifndef MU_UNROLL
+#define MU_UNROLL 1
+#endif
+constexpr int kMuUnroll = MU_UNROLL;
+#define MU_SORT_MAX 1024  // longer lists stay unsorted and are evaluated one way
+
+__global__ void __launch_bounds__(256) k_mu_sort(const int *tree_cnt, const unsigned long long *walk_flags,
+                                                  uint32_t *pool, const long long *off, const int *cnt,
+                                                  const int *npart, int *sorted, int *nrecv, long long *size)
+{
+    __shared__ uint32_t s_buf[8][MU_SORT_MAX];
+    const int lane = warp_lane(), wib = threadIdx.x >> 5;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    const int nleaf = *walk_flags ? 0 : tree_cnt[BC_LEAVES];
+    uint32_t *buf = s_buf[wib];
+    for (int t = gw; t < nleaf; t += nw) {
+        const int L = cnt[t];
+        uint32_t *lst = pool + off[t];
+        const int ok = L <= MU_SORT_MAX;
+        int below = 0;
+        if (ok && L > 1) {
+            int P = 2;
+            while (P < L) P <<= 1;
+            for (int i = lane; i < P; i += 32) buf[i] = i < L ? lst[i] : 0xffffffffu;
+            for (int k = 2; k <= P; k <<= 1)
+                for (int j = k >> 1; j > 0; j >>= 1) {
+                    __syncwarp();
+                    for (int i = lane; i < P; i += 32) {
+                        const int ixj = i ^ j;
+                        if (ixj > i) {
+                            const uint32_t a = buf[i], b = buf[ixj];
+                            if ((a > b) == ((i & k) == 0)) {
+                                buf[i] = b;
+                                buf[ixj] = a;
+                            }
+                        }
+                    }
+                }
+            __syncwarp();
+            for (int i = lane; i < L; i += 32) {
+                lst[i] = buf[i];
+                below += buf[i] < (uint32_t)t;
+            }
+            __syncwarp();
+        } else if (ok) {
+            for (int i = lane; i < L; i += 32) below += lst[i] < (uint32_t)t;
+        }
+        below = __reduce_add_sync(0xffffffffu, below);
+        if (lane == 0) {
+            sorted[t] = ok;
+            nrecv[t] = ok ? below : 0;
+            size[t] = ok ? (long long)below * npart[t] * 3 : 0;
+        }
+    }
+}
+
+// position of value v in the sorted list lst[0, L), or -1
+__device__ __forceinline__ int mu_find(const uint32_t *lst, int L, uint32_t v)
+{
+    int lo = 0, hi = L;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (lst[mid] < v) lo = mid + 1;
+        else hi = mid;
+    }
+    return (lo < L && lst[lo] == v) ? lo : -1;
+}
+
+// slot per entry: q >= 0 owned mutual (the owner's rank in the partner's
+// list), -2 received mutual, -1 evaluated one way
+__global__ void k_mu_slots(const int *tree_cnt, const unsigned long long *walk_flags, const uint32_t *pool,
+                           const long long *off, const int *cnt, const int *sorted, const long long *total,
+                           long long cap, int *slot, int *over)
+{
+    const int lane = warp_lane();
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    const int nleaf = *walk_flags ? 0 : tree_cnt[BC_LEAVES];
+    const bool fits = *total <= cap;
+    if (gw == 0 && lane == 0) *over = fits ? 0 : 1;
+    for (int t = gw; t < nleaf; t += nw) {
+        const long long o = off[t];
+        const int L = cnt[t];
+        const bool st = sorted[t] && fits;
+        for (int e = lane; e < L; e += 32) {
+            const uint32_t v = pool[o + e];
+            const int b = PH_ENTRY_ID(v);
+            int r = -1;
+            if (st && PH_ENTRY_IMG(v) == 0 && b != t && sorted[b]) {
+                const int q = mu_find(pool + off[b], cnt[b], (uint32_t)t);
+                if (q >= 0) r = t < b ? q : -2;
+            }
+            slot[o + e] = r;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(MU_TB, MU_MINB) k_p2p_mutual(P2PArgs A, const int *slot, const long long *rbase,
+                                                           float *rbuf)
+{
+    // shared layouts avoid bank conflicts: sources padded by one float4 per
+    // group of 8 (the four source groups read distinct banks), reactions
+    // [source][component][target group] with a 25-word source stride, running
+    // sums [value][lane]
+    __shared__ __align__(16) float4 s_src[MU_WARPS][72];
+    __shared__ float s_red[MU_WARPS][32 * 25];
+    __shared__ float s_acc[MU_WARPS][48][32];  // Kahan sum and compensation of 8 targets x 3, per lane
+    const int lane = warp_lane(), wib = threadIdx.x >> 5;
+    const int tg = lane >> 2, sg = lane & 3;
+    float4 *src = s_src[wib];
+    float *red = s_red[wib];
+    SplitConsts K = A.k;
+    const float far = 1e18f;
+
+    const int nleaf = p2p_targets(A);
+    for (;;) {
+        int t;
+        if (lane == 0) t = atomicAdd(A.work_counter, 1);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= nleaf) break;
+        const int nt = A.npart[t], it = A.ipart[t];
+        if (nt == 0) continue;
+        const BoxParams &B = A.boxes[A.boxid[t]];
+        K.sig = B.sig;
+        K.e2s = B.e2s;
+        K.pias = B.pias;
+        K.cs = B.cs;
+        const float Lhi = B.Lhi, Llo = B.Llo;
+        const float2 pia2 = f2(K.pias), c2 = f2(K.cs), one2 = f2(1.0f);
+        const float2 a0 = f2(K.as[0]), a1 = f2(K.as[1]), a2 = f2(K.as[2]), a3 = f2(K.as[3]), a4 = f2(K.as[4]),
+                     a5 = f2(K.as[5]);
+        const float4 cth = A.chi[t], ctl = A.clo[t];
+        // this lane's 8 targets as four pairs, negated for dx = s - x
+        float2 nx[4], ny[4], nz[4];
+#pragma unroll
+        for (int p = 0; p < 4; p++) {
+            const int q0 = tg * 8 + 2 * p, q1 = q0 + 1;
+            const float4 o0 = q0 < nt ? scaled(A.pos4[it + q0], K.sig) : make_float4(far, far, far, 0.f);
+            const float4 o1 = q1 < nt ? scaled(A.pos4[it + q1], K.sig) : make_float4(far, far, far, 0.f);
+            nx[p] = make_float2(-o0.x, -o1.x);
+            ny[p] = make_float2(-o0.y, -o1.y);
+            nz[p] = make_float2(-o0.z, -o1.z);
+        }
+#pragma unroll
+        for (int k = 0; k < 48; k++) s_acc[wib][k][lane] = 0.f;
+        const long long eoff = A.p2p_off[t];
+        const int ecnt = A.p2p_cnt[t];
+        for (int e = 0; e < ecnt; e++) {
+            const int sl = slot[eoff + e];
+            if (sl == -2) continue;  // received: the owner writes it
+            const uint32_t en = A.p2p_pool[eoff + e];
+            const int s = PH_ENTRY_ID(en), img = PH_ENTRY_IMG(en);
+            const int is = A.ipart[s], ns = A.npart[s];
+            const float4 csh = A.chi[s], csl = A.clo[s];
+            int mi, mj, mk;
+            image_offsets(img, mi, mj, mk);
+            const float d0 = centre_diff(csh.x, csl.x, cth.x, ctl.x, mi, Lhi, Llo) * K.sig;
+            const float d1 = centre_diff(csh.y, csl.y, cth.y, ctl.y, mj, Lhi, Llo) * K.sig;
+            const float d2 = centre_diff(csh.z, csl.z, cth.z, ctl.z, mk, Lhi, Llo) * K.sig;
+            // stage the source leaf (scaled, relative to the target centre); padding is far away
+            for (int j = lane; j < 64; j += 32) {
+                float4 v = make_float4(far, far, far, 0.f);
+                if (j < ns) {
+                    const float4 o = A.pos4[is + j];
+                    v = make_float4(fmaf(o.x, K.sig, d0), fmaf(o.y, K.sig, d1), fmaf(o.z, K.sig, d2), 0.f);
+                }
+                src[j + (j >> 3)] = v;
+            }
+            __syncwarp();
+            const bool owned = sl >= 0;
+            float2 ax[4], ay[4], az[4];
+#pragma unroll
+            for (int p = 0; p < 4; p++) ax[p] = ay[p] = az[p] = f2(0.f);
+            for (int c0 = 0; c0 < ns; c0 += 32) {
+#pragma unroll kMuUnroll
+                for (int r = 0; r < 8; r++) {
+                    const float4 S = src[(c0 >> 3) * 9 + sg * 9 + r];
+                    const float2 sx = f2(S.x), sy = f2(S.y), sz = f2(S.z);
+                    float2 rx = f2(0.f), ry = f2(0.f), rz = f2(0.f);
+#pragma unroll
+                    for (int p = 0; p < 4; p++) {
+                        const float2 dx = __fadd2_rn(sx, nx[p]);
+                        const float2 dy = __fadd2_rn(sy, ny[p]);
+                        const float2 dz = __fadd2_rn(sz, nz[p]);
+                        float2 qq = __fmul2_rn(dx, dx);
+                        qq = __ffma2_rn(dy, dy, qq);
+                        qq = __ffma2_rn(dz, dz, qq);
+                        const float2 f = pair_factor(qq, K, pia2, one2, c2, a0, a1, a2, a3, a4, a5);
+                        ax[p] = __ffma2_rn(dx, f, ax[p]);
+                        ay[p] = __ffma2_rn(dy, f, ay[p]);
+                        az[p] = __ffma2_rn(dz, f, az[p]);
+                        if (owned) {
+                            rx = __ffma2_rn(dx, f, rx);
+                            ry = __ffma2_rn(dy, f, ry);
+                            rz = __ffma2_rn(dz, f, rz);
+                        }
+                    }
+                    if (owned) {
+                        float *rr = red + (sg * 8 + r) * 25 + tg;
+                        rr[0] = rx.x + rx.y;
+                        rr[8] = ry.x + ry.y;
+                        rr[16] = rz.x + rz.y;
+                    }
+                }
+                if (owned) {
+                    // reactions of the batch's 32 sources: minus the sum over the 8 target groups
+                    __syncwarp();
+                    float *out = rbuf + rbase[s] + (long long)sl * ns * 3 + (long long)c0 * 3;
+                    for (int k = lane; k < 96; k += 32) {
+                        const int j = k / 3, cmp = k - 3 * j;
+                        float v = 0.f;
+                        const float *rr = red + j * 25 + cmp * 8;
+#pragma unroll
+                        for (int g = 0; g < 8; g++) v += rr[g];
+                        if (c0 + j < ns) out[k] = -v;
+                    }
+                    __syncwarp();
+                }
+            }
+            // the entry's partial sums join the running sums with Kahan
+            // compensation (FP32: GB300's FP64 rate is 1/64 of FP32)
+#pragma unroll
+            for (int p = 0; p < 4; p++) {
+                const float v[6] = {ax[p].x, ay[p].x, az[p].x, ax[p].y, ay[p].y, az[p].y};
+#pragma unroll
+                for (int k = 0; k < 6; k++) kahan_add(s_acc[wib][6 * p + k][lane], s_acc[wib][24 + 6 * p + k][lane], v[k]);
+            }
+            __syncwarp();
+        }
+        __syncwarp();
+        // targets: each lane takes two of the 64, summing its 4 source groups in order
+        {
+            const double scale = B.acc_scale;
+            for (int tq = lane; tq < nt; tq += 32) {
+                const int tgq = tq >> 3, q = tq & 7;
+                float v[3], cmp[3];
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    v[d] = 0.f;
+                    cmp[d] = 0.f;
+#pragma unroll
+                    for (int g = 0; g < 4; g++) {
+                        const int l = tgq * 4 + g;
+                        kahan_add(v[d], cmp[d], s_acc[wib][3 * q + d][l]);
+                        kahan_add(v[d], cmp[d], -s_acc[wib][24 + 3 * q + d][l]);
+                    }
+                }
+                A.ax[it + tq] += ((double)v[0] - (double)cmp[0]) * scale;
+                A.ay[it + tq] += ((double)v[1] - (double)cmp[1]) * scale;
+                A.az[it + tq] += ((double)v[2] - (double)cmp[2]) * scale;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// each leaf adds the reactions its owners left in its slots, in list order
+__global__ void k_mu_gather(P2PArgs A, const int *slot, const int *nrecv, const long long *rbase, const float *rbuf)
+{
+    const int lane = warp_lane();
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    const int nleaf = p2p_targets(A);
+    for (int t = gw; t < nleaf; t += nw) {
+        const int nt = A.npart[t], it = A.ipart[t], nr = nrecv[t];
+        if (nr == 0 || nt == 0) continue;
+        const long long eoff = A.p2p_off[t];
+        const double scale = A.boxes[A.boxid[t]].acc_scale;
+        for (int j0 = 0; j0 < nt; j0 += 32) {
+            const int j = j0 + lane;
+            float v0 = 0.f, v1 = 0.f, v2 = 0.f, c0 = 0.f, c1 = 0.f, c2 = 0.f;
+            for (int r = 0; r < nr; r++) {
+                if (slot[eoff + r] != -2) continue;
+                if (j < nt) {
+                    const float *in = rbuf + rbase[t] + ((long long)r * nt + j) * 3;
+                    kahan_add(v0, c0, in[0]);
+                    kahan_add(v1, c1, in[1]);
+                    kahan_add(v2, c2, in[2]);
+                }
+            }
+            if (j < nt) {
+                A.ax[it + j] += ((double)v0 - (double)c0) * scale;
+                A.ay[it + j] += ((double)v1 - (double)c1) * scale;
+                A.az[it + j] += ((double)v2 - (double)c2) * scale;
+            }
+        }
+    }
+}
+
 }  // namespace
 
 // coordinate scale of the packed kernel, rounded to FP32 first so that the
@@ -670,6 +986,21 @@ int launch_leaf_offsets(const BuildBufs &b, const TreeBufs &t, float4 *pos4, cud
     int blocks = device_sm_count() * 8;
     ph::note_launch(), k_leaf_offsets<<<blocks, 256, 0, st>>>(b.x, b.y, b.z, t.ipart, t.npart, t.cx, t.cy, t.cz, b.cnt,
                                                               pos4);
+    PH_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
+int launch_p2p_mutual(const P2PArgs &a, const MutualBufs &m, cudaStream_t st)
+{
+    PH_CUDA_CHECK(cudaMemsetAsync(a.work_counter, 0, sizeof(int), st));
+    const int sms = device_sm_count();
+    ph::note_launch(), k_mu_sort<<<sms * 4, 256, 0, st>>>(a.tree_cnt, a.walk_flags, m.pool, a.p2p_off, a.p2p_cnt,
+                                                           a.npart, m.sorted, m.nrecv, m.size);
+    scan_exclusive_i64(m.size, m.rbase, a.tree_cnt + BC_LEAVES, m.cap_leaves, m.total, m.scan_scratch, st);
+    ph::note_launch(), k_mu_slots<<<sms * 8, 256, 0, st>>>(a.tree_cnt, a.walk_flags, m.pool, a.p2p_off, a.p2p_cnt,
+                                                            m.sorted, m.total, m.buf_cap, m.slot, m.over);
+    ph::note_launch(), k_p2p_mutual<<<sms * MU_MINB, MU_TB, 0, st>>>(a, m.slot, m.rbase, m.buf);
+    ph::note_launch(), k_mu_gather<<<sms * 8, 256, 0, st>>>(a, m.slot, m.nrecv, m.rbase, m.buf);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }

@@ -40,7 +40,24 @@ struct P2PArgs {
     int variant;  // FP32: 0 packed (default), 1 scalar
 };
 
+// buffers of the mutual FP32 kernel (see launch_p2p_mutual)
+struct MutualBufs {
+    uint32_t *pool;          // the P2P pool, each target's list sorted in place
+    int *sorted, *nrecv;     // per leaf: list sorted; received (lower-id) entries
+    long long *size, *rbase; // per leaf: reaction floats owed to it, and their offset
+    long long *total;        // device: floats needed
+    long long *scan_scratch;
+    int *slot;               // per pool entry: owner rank, -2 received, -1 one way
+    int *over;               // device: 1 if the reaction buffer was too small (all one way)
+    float *buf;              // reactions
+    long long buf_cap;       // floats
+    int cap_leaves;
+};
+
 SplitConsts make_split_consts(const PassParams &p);
+// FP32 P2P with mutual pairs (MAXLEAF <= 64): sorts the lists, pairs the
+// entries, evaluates, adds the received reactions
+int launch_p2p_mutual(const P2PArgs &a, const MutualBufs &m, cudaStream_t st);
 double split_sig(const PassParams &p);
 int launch_leaf_offsets(const BuildBufs &b, const TreeBufs &t, float4 *pos4, cudaStream_t st);
 int launch_p2p(const P2PArgs &a, int fp64, cudaStream_t st);

@@ -13,79 +13,95 @@
 
 namespace {
 
-__device__ __forceinline__ int block_excl_scan(int v, int *smem_warp, int &total)
+template <typename T>
+__device__ __forceinline__ T warp_incl_scan_t(T v)
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        T t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T block_excl_scan(T v, T *smem_warp, T &total)
 {
     int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    int incl = warp_incl_scan(v);
+    T incl = warp_incl_scan_t(v);
     if (lane == 31) smem_warp[wid] = incl;
     __syncthreads();
     if (wid == 0) {
-        int w = (lane < SCAN_THREADS / 32) ? smem_warp[lane] : 0;
-        int wi = warp_incl_scan(w);
+        T w = (lane < SCAN_THREADS / 32) ? smem_warp[lane] : T(0);
+        T wi = warp_incl_scan_t(w);
         if (lane < SCAN_THREADS / 32) smem_warp[lane] = wi - w;
         if (lane == SCAN_THREADS / 32 - 1) smem_warp[SCAN_THREADS / 32] = wi;
     }
     __syncthreads();
-    int r = incl - v + smem_warp[wid];
+    T r = incl - v + smem_warp[wid];
     total = smem_warp[SCAN_THREADS / 32];
     __syncthreads();
     return r;
 }
 
-__global__ void k_tile_sums(const int *__restrict__ in, const int *n_ptr, int *__restrict__ tile_sum)
+template <typename T>
+__global__ void k_tile_sums(const T *__restrict__ in, const int *n_ptr, T *__restrict__ tile_sum)
 {
-    __shared__ int sw[SCAN_THREADS / 32 + 1];
+    __shared__ T sw[SCAN_THREADS / 32 + 1];
     int n = *n_ptr;
     int ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         int base = t * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
-        int s = 0;
+        T s = 0;
 #pragma unroll
         for (int i = 0; i < SCAN_ITEMS; i++) {
             int idx = base + i;
-            s += (idx < n) ? in[idx] : 0;
+            s += (idx < n) ? in[idx] : T(0);
         }
-        int total;
+        T total;
         block_excl_scan(s, sw, total);
         if (threadIdx.x == 0) tile_sum[t] = total;
     }
 }
 
-__global__ void k_scan_tile_sums(int *tile_sum, const int *n_ptr, int *total_out)
+template <typename T>
+__global__ void k_scan_tile_sums(T *tile_sum, const int *n_ptr, T *total_out)
 {
-    __shared__ int sw[SCAN_THREADS / 32 + 1];
+    __shared__ T sw[SCAN_THREADS / 32 + 1];
     int n = *n_ptr;
     int ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
-    int carry = 0;
+    T carry = 0;
     for (int base = 0; base < ntiles; base += SCAN_THREADS) {
         int idx = base + threadIdx.x;
-        int v = (idx < ntiles) ? tile_sum[idx] : 0;
-        int total;
-        int ex = block_excl_scan(v, sw, total);
+        T v = (idx < ntiles) ? tile_sum[idx] : T(0);
+        T total;
+        T ex = block_excl_scan(v, sw, total);
         if (idx < ntiles) tile_sum[idx] = ex + carry;
         carry += total;
     }
     if (threadIdx.x == 0 && total_out) *total_out = carry;
 }
 
-__global__ void k_tile_scan(const int *__restrict__ in, int *__restrict__ out, const int *n_ptr,
-                            const int *__restrict__ tile_off)
+template <typename T>
+__global__ void k_tile_scan(const T *__restrict__ in, T *__restrict__ out, const int *n_ptr,
+                            const T *__restrict__ tile_off)
 {
-    __shared__ int sw[SCAN_THREADS / 32 + 1];
+    __shared__ T sw[SCAN_THREADS / 32 + 1];
     int n = *n_ptr;
     int ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         int base = t * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
-        int v[SCAN_ITEMS];
-        int s = 0;
+        T v[SCAN_ITEMS];
+        T s = 0;
 #pragma unroll
         for (int i = 0; i < SCAN_ITEMS; i++) {
             int idx = base + i;
-            v[i] = (idx < n) ? in[idx] : 0;
+            v[i] = (idx < n) ? in[idx] : T(0);
             s += v[i];
         }
-        int total;
-        int ex = block_excl_scan(s, sw, total) + tile_off[t];
+        T total;
+        T ex = block_excl_scan(s, sw, total) + tile_off[t];
 #pragma unroll
         for (int i = 0; i < SCAN_ITEMS; i++) {
             int idx = base + i;
@@ -93,6 +109,16 @@ __global__ void k_tile_scan(const int *__restrict__ in, int *__restrict__ out, c
             ex += v[i];
         }
     }
+}
+
+template <typename T>
+void scan_exclusive(const T *in, T *out, const int *n_ptr, int cap, T *total, T *scratch, cudaStream_t st)
+{
+    int ntiles_cap = (cap + SCAN_TILE - 1) / SCAN_TILE;
+    int grid = ntiles_cap < 4 * ph::device_sm_count() ? (ntiles_cap > 0 ? ntiles_cap : 1) : 4 * ph::device_sm_count();
+    ph::note_launch(), k_tile_sums<T><<<grid, SCAN_THREADS, 0, st>>>(in, n_ptr, scratch);
+    ph::note_launch(), k_scan_tile_sums<T><<<1, SCAN_THREADS, 0, st>>>(scratch, n_ptr, total);
+    ph::note_launch(), k_tile_scan<T><<<grid, SCAN_THREADS, 0, st>>>(in, out, n_ptr, scratch);
 }
 
 }  // namespace
@@ -105,11 +131,13 @@ void scan_exclusive_i32(const int *in, int *out, const int *n_ptr, int cap, int 
                         size_t scratch_elems, cudaStream_t st)
 {
     (void)scratch_elems;
-    int ntiles_cap = (cap + SCAN_TILE - 1) / SCAN_TILE;
-    int grid = ntiles_cap < 4 * device_sm_count() ? (ntiles_cap > 0 ? ntiles_cap : 1) : 4 * device_sm_count();
-    ph::note_launch(), k_tile_sums<<<grid, SCAN_THREADS, 0, st>>>(in, n_ptr, scratch);
-    ph::note_launch(), k_scan_tile_sums<<<1, SCAN_THREADS, 0, st>>>(scratch, n_ptr, total);
-    ph::note_launch(), k_tile_scan<<<grid, SCAN_THREADS, 0, st>>>(in, out, n_ptr, scratch);
+    scan_exclusive<int>(in, out, n_ptr, cap, total, scratch, st);
+}
+
+void scan_exclusive_i64(const long long *in, long long *out, const int *n_ptr, int cap, long long *total,
+                        long long *scratch, cudaStream_t st)
+{
+    scan_exclusive<long long>(in, out, n_ptr, cap, total, scratch, st);
 }
 
 }  // namespace ph

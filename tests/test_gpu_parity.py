@@ -152,6 +152,25 @@ def test_graph_pass_matches_stage_pass(ph, ics, monkeypatch, precision):
     assert fp.counters()["depth"] > 2
 
 
+@pytest.mark.parametrize("workload,nside,maxleaf", [("grid32", 32, 16), ("nfw128", 32, 8), ("zeldovich256", 32, 64)])
+def test_mutual_pairs_match_one_way(ph, ics, monkeypatch, workload, nside, maxleaf):
+    """The FP32 kernel that evaluates each local leaf pair once (reactions
+    through a buffer) against the one-way kernel and the FP64 pass: the
+    same forces to FP32 rounding, deterministic from pass to pass."""
+    pos, p = ics.make(workload, nside=nside, maxleaf=maxleaf)
+    fp = ph.ForcePass(0)
+    a64 = fp.run(pos, p, precision=ph.FP64)
+    mutual = fp.run(pos, p, precision=ph.FP32_SPLIT)
+    again = fp.run(pos, p, precision=ph.FP32_SPLIT)
+    monkeypatch.setenv("PHOTONS_P2P_KERNEL", "packed")
+    one_way = ph.ForcePass(0).run(pos, p, precision=ph.FP32_SPLIT)
+    assert np.array_equal(mutual, again)
+    e_mu, e_ow = rel_err(mutual, a64, p), rel_err(one_way, a64, p)
+    assert np.median(e_mu) <= 1.5 * np.median(e_ow) + 1e-7, (np.median(e_mu), np.median(e_ow))
+    assert np.percentile(e_mu, 99) <= 2e-5
+    assert np.median(rel_err(mutual, one_way, p)) <= 5e-6
+
+
 def test_capacity_overflow_is_an_error(ph, fp):
     pos = np.full((100, 3), 3.0)
     p = dict(boxsize=10.0, theta=0.5, rs=1.0, rcut=4.5, eps=0.01, mass=1.0, maxleaf=8)
