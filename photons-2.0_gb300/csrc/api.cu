@@ -252,8 +252,8 @@ __global__ void k_gather_out(const int *perm, const double *ax, const double *ay
 
 }  // namespace
 
-// FP32 P2P kernel: 2 mutual pairs (default for MAXLEAF <= 64), 0 packed
-// one-way pairs, 1 scalar (PHOTONS_P2P_KERNEL=mutual|packed|scalar)
+// FP32 P2P kernel: 2 mutual pairs (the default; used for MAXLEAF 48-64),
+// 0 packed one-way pairs, 1 scalar (PHOTONS_P2P_KERNEL=mutual|packed|scalar)
 static int p2p_variant()
 {
     const char *v = getenv("PHOTONS_P2P_KERNEL");
@@ -277,8 +277,10 @@ static bool mutual_feedback(photons_ctx *c, int over, long long need)
 
 static int alloc_mutual(photons_ctx *c)
 {
-    // first guess: about half of a leaf's ~130-250 list entries received, 3 floats per particle
-    long long want = c->hint_mubuf ? c->hint_mubuf : (long long)c->n * 256 + 4096;
+    // first guess: about half of a leaf's ~110-250 list entries received, 3
+    // floats per particle and entry (256^3 leaf 64 needs ~170 per particle);
+    // a pass that needs more repeats once with the measured size
+    long long want = c->hint_mubuf ? c->hint_mubuf : (long long)c->n * 176 + 4096;
     if (want > c->mu_buf_cap) {
         PH_TRY(dalloc(c->mu_buf, (size_t)want));
         c->mu_buf_cap = want;
@@ -620,7 +622,9 @@ int ph_stage_p2p(photons_ctx *c, int precision, int zero)
     a.k = ph::make_split_consts(c->pp);
     a.variant = p2p_variant();
     PH_TRY(ph_record(c, EV_P2P_BEGIN));
-    if (precision != PHOTONS_FP64 && a.variant == 2 && c->pp.maxleaf <= 64) {
+    // mutual pairs pay off from leaf size 48 (256^3: 71 vs 91 ms at leaf 64, a
+    // tie at 32); below that the per-entry work outweighs the halved pairs
+    if (precision != PHOTONS_FP64 && a.variant == 2 && c->pp.maxleaf >= 48 && c->pp.maxleaf <= 64) {
         ph::MutualBufs m;
         m.pool = c->w.p2p_pool;
         m.sorted = c->mu_sorted; m.nrecv = c->mu_nrecv; m.size = c->mu_size; m.rbase = c->mu_rbase;

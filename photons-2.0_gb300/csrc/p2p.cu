@@ -760,22 +760,156 @@ __global__ void k_mu_slots(const int *tree_cnt, const unsigned long long *walk_f
     }
 }
 
-__global__ void __launch_bounds__(MU_TB, MU_MINB) k_p2p_mutual(P2PArgs A, const int *slot, const long long *rbase,
-                                                           float *rbuf)
+// one target leaf with T targets per lane (8: leaves of up to 64
+// particles, 4: up to 32), eight target groups x four source groups
+template <int T>
+__device__ __forceinline__ void mu_target(const P2PArgs &A, const int *slot, const long long *rbase, float *rbuf, int t,
+                                          int nt, int it, const SplitConsts &K, float Lhi, float Llo, float4 *src,
+                                          float *red, float *accw, int lane)
 {
-    // shared layouts avoid bank conflicts: sources padded by one float4 per
-    // group of 8 (the four source groups read distinct banks), reactions
-    // [source][component][target group] with a 25-word source stride, running
-    // sums [value][lane]
-    __shared__ __align__(16) float4 s_src[MU_WARPS][72];
-    __shared__ float s_red[MU_WARPS][32 * 25];
-    __shared__ float s_acc[MU_WARPS][48][32];  // Kahan sum and compensation of 8 targets x 3, per lane
-    const int lane = warp_lane(), wib = threadIdx.x >> 5;
+    constexpr int TP = T / 2;  // target pairs per lane
     const int tg = lane >> 2, sg = lane & 3;
-    float4 *src = s_src[wib];
-    float *red = s_red[wib];
-    SplitConsts K = A.k;
     const float far = 1e18f;
+    const float2 pia2 = f2(K.pias), c2 = f2(K.cs), one2 = f2(1.0f);
+    const float2 a0 = f2(K.as[0]), a1 = f2(K.as[1]), a2 = f2(K.as[2]), a3 = f2(K.as[3]), a4 = f2(K.as[4]),
+                 a5 = f2(K.as[5]);
+    const float4 cth = A.chi[t], ctl = A.clo[t];
+    // this lane's targets as pairs, negated for dx = s - x
+    float2 nx[TP], ny[TP], nz[TP];
+#pragma unroll
+    for (int p = 0; p < TP; p++) {
+        const int q0 = tg * T + 2 * p, q1 = q0 + 1;
+        const float4 o0 = q0 < nt ? scaled(A.pos4[it + q0], K.sig) : make_float4(far, far, far, 0.f);
+        const float4 o1 = q1 < nt ? scaled(A.pos4[it + q1], K.sig) : make_float4(far, far, far, 0.f);
+        nx[p] = make_float2(-o0.x, -o1.x);
+        ny[p] = make_float2(-o0.y, -o1.y);
+        nz[p] = make_float2(-o0.z, -o1.z);
+    }
+#pragma unroll
+    for (int k = 0; k < 6 * T; k++) accw[k * 32 + lane] = 0.f;
+    const long long eoff = A.p2p_off[t];
+    const int ecnt = A.p2p_cnt[t];
+    for (int e = 0; e < ecnt; e++) {
+        const int sl = slot[eoff + e];
+        if (sl == -2) continue;  // received: the owner writes it
+        const uint32_t en = A.p2p_pool[eoff + e];
+        const int s = PH_ENTRY_ID(en), img = PH_ENTRY_IMG(en);
+        const int is = A.ipart[s], ns = A.npart[s];
+        const float4 csh = A.chi[s], csl = A.clo[s];
+        int mi, mj, mk;
+        image_offsets(img, mi, mj, mk);
+        const float d0 = centre_diff(csh.x, csl.x, cth.x, ctl.x, mi, Lhi, Llo) * K.sig;
+        const float d1 = centre_diff(csh.y, csl.y, cth.y, ctl.y, mj, Lhi, Llo) * K.sig;
+        const float d2 = centre_diff(csh.z, csl.z, cth.z, ctl.z, mk, Lhi, Llo) * K.sig;
+        // stage the source leaf (scaled, relative to the target centre); padding is far away
+        for (int j = lane; j < 64; j += 32) {
+            float4 v = make_float4(far, far, far, 0.f);
+            if (j < ns) {
+                const float4 o = A.pos4[is + j];
+                v = make_float4(fmaf(o.x, K.sig, d0), fmaf(o.y, K.sig, d1), fmaf(o.z, K.sig, d2), 0.f);
+            }
+            src[j] = v;
+        }
+        __syncwarp();
+        const bool owned = sl >= 0;
+        float2 ax[TP], ay[TP], az[TP];
+#pragma unroll
+        for (int p = 0; p < TP; p++) ax[p] = ay[p] = az[p] = f2(0.f);
+        for (int c0 = 0; c0 < ns; c0 += 32) {
+            // the batch's sources spread evenly over the four source groups
+            const int nr = min(8, (ns - c0 + 3) >> 2);
+#pragma unroll kMuUnroll
+            for (int r = 0; r < nr; r++) {
+                const float4 S = src[c0 + 4 * r + sg];
+                const float2 sx = f2(S.x), sy = f2(S.y), sz = f2(S.z);
+                float2 rx = f2(0.f), ry = f2(0.f), rz = f2(0.f);
+#pragma unroll
+                for (int p = 0; p < TP; p++) {
+                    const float2 dx = __fadd2_rn(sx, nx[p]);
+                    const float2 dy = __fadd2_rn(sy, ny[p]);
+                    const float2 dz = __fadd2_rn(sz, nz[p]);
+                    float2 qq = __fmul2_rn(dx, dx);
+                    qq = __ffma2_rn(dy, dy, qq);
+                    qq = __ffma2_rn(dz, dz, qq);
+                    const float2 f = pair_factor(qq, K, pia2, one2, c2, a0, a1, a2, a3, a4, a5);
+                    ax[p] = __ffma2_rn(dx, f, ax[p]);
+                    ay[p] = __ffma2_rn(dy, f, ay[p]);
+                    az[p] = __ffma2_rn(dz, f, az[p]);
+                    if (owned) {
+                        rx = __ffma2_rn(dx, f, rx);
+                        ry = __ffma2_rn(dy, f, ry);
+                        rz = __ffma2_rn(dz, f, rz);
+                    }
+                }
+                if (owned) {
+                    float *rr = red + (4 * r + sg) * 40 + tg;
+                    rr[0] = rx.x + rx.y;
+                    rr[8] = ry.x + ry.y;
+                    rr[16] = rz.x + rz.y;
+                }
+            }
+            if (owned) {
+                // reactions of the batch's sources: minus the sum over the 8 target groups
+                __syncwarp();
+                float *out = rbuf + rbase[s] + (long long)sl * ns * 3 + (long long)c0 * 3;
+                for (int k = lane; k < 96; k += 32) {
+                    const int j = k / 3, cmp = k - 3 * j;
+                    if (c0 + j < ns) {
+                        const float4 *rr = reinterpret_cast<const float4 *>(red + j * 40 + cmp * 8);
+                        const float4 u = rr[0], w = rr[1];
+                        out[k] = -((((u.x + u.y) + (u.z + u.w)) + ((w.x + w.y) + (w.z + w.w))));
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        // the entry's partial sums join the running sums with Kahan
+        // compensation (FP32: GB300's FP64 rate is 1/64 of FP32)
+#pragma unroll
+        for (int p = 0; p < TP; p++) {
+            const float v[6] = {ax[p].x, ay[p].x, az[p].x, ax[p].y, ay[p].y, az[p].y};
+#pragma unroll
+            for (int k = 0; k < 6; k++)
+                kahan_add(accw[(6 * p + k) * 32 + lane], accw[(3 * T + 6 * p + k) * 32 + lane], v[k]);
+        }
+        __syncwarp();
+    }
+    __syncwarp();
+    // targets: each lane takes one or two, summing its 4 source groups in order
+    const double scale = A.boxes[A.boxid[t]].acc_scale;
+    for (int tq = lane; tq < nt; tq += 32) {
+        const int tgq = tq / T, q = tq - tgq * T;
+        float v[3], cmp[3];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            v[d] = 0.f;
+            cmp[d] = 0.f;
+#pragma unroll
+            for (int g = 0; g < 4; g++) {
+                const int l = tgq * 4 + g;
+                kahan_add(v[d], cmp[d], accw[(3 * q + d) * 32 + l]);
+                kahan_add(v[d], cmp[d], -accw[(3 * T + 3 * q + d) * 32 + l]);
+            }
+        }
+        A.ax[it + tq] += ((double)v[0] - (double)cmp[0]) * scale;
+        A.ay[it + tq] += ((double)v[1] - (double)cmp[1]) * scale;
+        A.az[it + tq] += ((double)v[2] - (double)cmp[2]) * scale;
+    }
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(MU_TB, MU_MINB) k_p2p_mutual(P2PArgs A, const int *slot, const long long *rbase,
+                                                               float *rbuf)
+{
+    // shared layouts avoid bank conflicts: a batch's source k (of 32) is
+    // read by source group k % 4, so the four groups read adjacent float4s;
+    // reactions [source][component][target group] with a 40-word source
+    // stride; running sums [value][lane]
+    __shared__ __align__(16) float4 s_src[MU_WARPS][64];
+    __shared__ __align__(16) float s_red[MU_WARPS][32 * 40];
+    __shared__ float s_acc[MU_WARPS][48 * 32];  // Kahan sum and compensation of up to 8 targets x 3, per lane
+    const int lane = warp_lane(), wib = threadIdx.x >> 5;
+    SplitConsts K = A.k;
 
     const int nleaf = p2p_targets(A);
     for (;;) {
@@ -790,132 +924,10 @@ __global__ void __launch_bounds__(MU_TB, MU_MINB) k_p2p_mutual(P2PArgs A, const 
         K.e2s = B.e2s;
         K.pias = B.pias;
         K.cs = B.cs;
-        const float Lhi = B.Lhi, Llo = B.Llo;
-        const float2 pia2 = f2(K.pias), c2 = f2(K.cs), one2 = f2(1.0f);
-        const float2 a0 = f2(K.as[0]), a1 = f2(K.as[1]), a2 = f2(K.as[2]), a3 = f2(K.as[3]), a4 = f2(K.as[4]),
-                     a5 = f2(K.as[5]);
-        const float4 cth = A.chi[t], ctl = A.clo[t];
-        // this lane's 8 targets as four pairs, negated for dx = s - x
-        float2 nx[4], ny[4], nz[4];
-#pragma unroll
-        for (int p = 0; p < 4; p++) {
-            const int q0 = tg * 8 + 2 * p, q1 = q0 + 1;
-            const float4 o0 = q0 < nt ? scaled(A.pos4[it + q0], K.sig) : make_float4(far, far, far, 0.f);
-            const float4 o1 = q1 < nt ? scaled(A.pos4[it + q1], K.sig) : make_float4(far, far, far, 0.f);
-            nx[p] = make_float2(-o0.x, -o1.x);
-            ny[p] = make_float2(-o0.y, -o1.y);
-            nz[p] = make_float2(-o0.z, -o1.z);
-        }
-#pragma unroll
-        for (int k = 0; k < 48; k++) s_acc[wib][k][lane] = 0.f;
-        const long long eoff = A.p2p_off[t];
-        const int ecnt = A.p2p_cnt[t];
-        for (int e = 0; e < ecnt; e++) {
-            const int sl = slot[eoff + e];
-            if (sl == -2) continue;  // received: the owner writes it
-            const uint32_t en = A.p2p_pool[eoff + e];
-            const int s = PH_ENTRY_ID(en), img = PH_ENTRY_IMG(en);
-            const int is = A.ipart[s], ns = A.npart[s];
-            const float4 csh = A.chi[s], csl = A.clo[s];
-            int mi, mj, mk;
-            image_offsets(img, mi, mj, mk);
-            const float d0 = centre_diff(csh.x, csl.x, cth.x, ctl.x, mi, Lhi, Llo) * K.sig;
-            const float d1 = centre_diff(csh.y, csl.y, cth.y, ctl.y, mj, Lhi, Llo) * K.sig;
-            const float d2 = centre_diff(csh.z, csl.z, cth.z, ctl.z, mk, Lhi, Llo) * K.sig;
-            // stage the source leaf (scaled, relative to the target centre); padding is far away
-            for (int j = lane; j < 64; j += 32) {
-                float4 v = make_float4(far, far, far, 0.f);
-                if (j < ns) {
-                    const float4 o = A.pos4[is + j];
-                    v = make_float4(fmaf(o.x, K.sig, d0), fmaf(o.y, K.sig, d1), fmaf(o.z, K.sig, d2), 0.f);
-                }
-                src[j + (j >> 3)] = v;
-            }
-            __syncwarp();
-            const bool owned = sl >= 0;
-            float2 ax[4], ay[4], az[4];
-#pragma unroll
-            for (int p = 0; p < 4; p++) ax[p] = ay[p] = az[p] = f2(0.f);
-            for (int c0 = 0; c0 < ns; c0 += 32) {
-#pragma unroll kMuUnroll
-                for (int r = 0; r < 8; r++) {
-                    const float4 S = src[(c0 >> 3) * 9 + sg * 9 + r];
-                    const float2 sx = f2(S.x), sy = f2(S.y), sz = f2(S.z);
-                    float2 rx = f2(0.f), ry = f2(0.f), rz = f2(0.f);
-#pragma unroll
-                    for (int p = 0; p < 4; p++) {
-                        const float2 dx = __fadd2_rn(sx, nx[p]);
-                        const float2 dy = __fadd2_rn(sy, ny[p]);
-                        const float2 dz = __fadd2_rn(sz, nz[p]);
-                        float2 qq = __fmul2_rn(dx, dx);
-                        qq = __ffma2_rn(dy, dy, qq);
-                        qq = __ffma2_rn(dz, dz, qq);
-                        const float2 f = pair_factor(qq, K, pia2, one2, c2, a0, a1, a2, a3, a4, a5);
-                        ax[p] = __ffma2_rn(dx, f, ax[p]);
-                        ay[p] = __ffma2_rn(dy, f, ay[p]);
-                        az[p] = __ffma2_rn(dz, f, az[p]);
-                        if (owned) {
-                            rx = __ffma2_rn(dx, f, rx);
-                            ry = __ffma2_rn(dy, f, ry);
-                            rz = __ffma2_rn(dz, f, rz);
-                        }
-                    }
-                    if (owned) {
-                        float *rr = red + (sg * 8 + r) * 25 + tg;
-                        rr[0] = rx.x + rx.y;
-                        rr[8] = ry.x + ry.y;
-                        rr[16] = rz.x + rz.y;
-                    }
-                }
-                if (owned) {
-                    // reactions of the batch's 32 sources: minus the sum over the 8 target groups
-                    __syncwarp();
-                    float *out = rbuf + rbase[s] + (long long)sl * ns * 3 + (long long)c0 * 3;
-                    for (int k = lane; k < 96; k += 32) {
-                        const int j = k / 3, cmp = k - 3 * j;
-                        float v = 0.f;
-                        const float *rr = red + j * 25 + cmp * 8;
-#pragma unroll
-                        for (int g = 0; g < 8; g++) v += rr[g];
-                        if (c0 + j < ns) out[k] = -v;
-                    }
-                    __syncwarp();
-                }
-            }
-            // the entry's partial sums join the running sums with Kahan
-            // compensation (FP32: GB300's FP64 rate is 1/64 of FP32)
-#pragma unroll
-            for (int p = 0; p < 4; p++) {
-                const float v[6] = {ax[p].x, ay[p].x, az[p].x, ax[p].y, ay[p].y, az[p].y};
-#pragma unroll
-                for (int k = 0; k < 6; k++) kahan_add(s_acc[wib][6 * p + k][lane], s_acc[wib][24 + 6 * p + k][lane], v[k]);
-            }
-            __syncwarp();
-        }
-        __syncwarp();
-        // targets: each lane takes two of the 64, summing its 4 source groups in order
-        {
-            const double scale = B.acc_scale;
-            for (int tq = lane; tq < nt; tq += 32) {
-                const int tgq = tq >> 3, q = tq & 7;
-                float v[3], cmp[3];
-#pragma unroll
-                for (int d = 0; d < 3; d++) {
-                    v[d] = 0.f;
-                    cmp[d] = 0.f;
-#pragma unroll
-                    for (int g = 0; g < 4; g++) {
-                        const int l = tgq * 4 + g;
-                        kahan_add(v[d], cmp[d], s_acc[wib][3 * q + d][l]);
-                        kahan_add(v[d], cmp[d], -s_acc[wib][24 + 3 * q + d][l]);
-                    }
-                }
-                A.ax[it + tq] += ((double)v[0] - (double)cmp[0]) * scale;
-                A.ay[it + tq] += ((double)v[1] - (double)cmp[1]) * scale;
-                A.az[it + tq] += ((double)v[2] - (double)cmp[2]) * scale;
-            }
-        }
-        __syncwarp();
+        if (nt > 32)
+            mu_target<8>(A, slot, rbase, rbuf, t, nt, it, K, B.Lhi, B.Llo, s_src[wib], s_red[wib], s_acc[wib], lane);
+        else
+            mu_target<4>(A, slot, rbase, rbuf, t, nt, it, K, B.Lhi, B.Llo, s_src[wib], s_red[wib], s_acc[wib], lane);
     }
 }
 
@@ -930,16 +942,27 @@ __global__ void k_mu_gather(P2PArgs A, const int *slot, const int *nrecv, const 
         if (nr == 0 || nt == 0) continue;
         const long long eoff = A.p2p_off[t];
         const double scale = A.boxes[A.boxid[t]].acc_scale;
+        const float *base = rbuf + rbase[t];
         for (int j0 = 0; j0 < nt; j0 += 32) {
             const int j = j0 + lane;
             float v0 = 0.f, v1 = 0.f, v2 = 0.f, c0 = 0.f, c1 = 0.f, c2 = 0.f;
-            for (int r = 0; r < nr; r++) {
-                if (slot[eoff + r] != -2) continue;
-                if (j < nt) {
-                    const float *in = rbuf + rbase[t] + ((long long)r * nt + j) * 3;
-                    kahan_add(v0, c0, in[0]);
-                    kahan_add(v1, c1, in[1]);
-                    kahan_add(v2, c2, in[2]);
+            for (int r0 = 0; r0 < nr; r0 += 4) {
+                // four slots' loads in flight, then added in slot order
+                float in[4][3];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const int r = r0 + k;
+                    const bool use = r < nr && j < nt && slot[eoff + r] == -2;
+                    const float *q = base + ((long long)r * nt + j) * 3;
+                    in[k][0] = use ? q[0] : 0.f;
+                    in[k][1] = use ? q[1] : 0.f;
+                    in[k][2] = use ? q[2] : 0.f;
+                }
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    kahan_add(v0, c0, in[k][0]);
+                    kahan_add(v1, c1, in[k][1]);
+                    kahan_add(v2, c2, in[k][2]);
                 }
             }
             if (j < nt) {

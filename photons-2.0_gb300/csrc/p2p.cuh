@@ -55,8 +55,8 @@ struct MutualBufs {
 };
 
 SplitConsts make_split_consts(const PassParams &p);
-// FP32 P2P with mutual pairs (MAXLEAF <= 64): sorts the lists, pairs the
-// entries, evaluates, adds the received reactions
+// FP32 P2P with mutual pairs (MAXLEAF <= 64; chosen for 48-64): sorts the
+// lists, pairs the entries, evaluates, adds the received reactions
 int launch_p2p_mutual(const P2PArgs &a, const MutualBufs &m, cudaStream_t st);
 double split_sig(const PassParams &p);
 int launch_leaf_offsets(const BuildBufs &b, const TreeBufs &t, float4 *pos4, cudaStream_t st);

@@ -152,7 +152,7 @@ def test_graph_pass_matches_stage_pass(ph, ics, monkeypatch, precision):
     assert fp.counters()["depth"] > 2
 
 
-@pytest.mark.parametrize("workload,nside,maxleaf", [("grid32", 32, 16), ("nfw128", 32, 8), ("zeldovich256", 32, 64)])
+@pytest.mark.parametrize("workload,nside,maxleaf", [("grid32", 32, 48), ("nfw128", 32, 64), ("zeldovich256", 32, 64)])
 def test_mutual_pairs_match_one_way(ph, ics, monkeypatch, workload, nside, maxleaf):
     """The FP32 kernel that evaluates each local leaf pair once (reactions
     through a buffer) against the one-way kernel and the FP64 pass: the
