@@ -668,6 +668,9 @@ __global__ void k_leaf_offsets(const double *px, const double *py, const double 
 #define MU_UNROLL 1
 #endif
 constexpr int kMuUnroll = MU_UNROLL;
+#ifndef MU_FLUSH
+#define MU_FLUSH 4  // evaluated entries per compensated flush of the partial sums
+#endif
 #define MU_SORT_MAX 1024  // longer lists stay unsorted and are evaluated one way
 
 __global__ void __launch_bounds__(256) k_mu_sort(const int *tree_cnt, const unsigned long long *walk_flags,
@@ -789,6 +792,12 @@ __device__ __forceinline__ void mu_target(const P2PArgs &A, const int *slot, con
     for (int k = 0; k < 6 * T; k++) accw[k * 32 + lane] = 0.f;
     const long long eoff = A.p2p_off[t];
     const int ecnt = A.p2p_cnt[t];
+    // partial sums run over up to MU_FLUSH evaluated entries (at most 64 terms
+    // per lane) before they join the compensated running sums
+    float2 ax[TP], ay[TP], az[TP];
+#pragma unroll
+    for (int p = 0; p < TP; p++) ax[p] = ay[p] = az[p] = f2(0.f);
+    int pending = 0;
     for (int e = 0; e < ecnt; e++) {
         const int sl = slot[eoff + e];
         if (sl == -2) continue;  // received: the owner writes it
@@ -812,9 +821,6 @@ __device__ __forceinline__ void mu_target(const P2PArgs &A, const int *slot, con
         }
         __syncwarp();
         const bool owned = sl >= 0;
-        float2 ax[TP], ay[TP], az[TP];
-#pragma unroll
-        for (int p = 0; p < TP; p++) ax[p] = ay[p] = az[p] = f2(0.f);
         for (int c0 = 0; c0 < ns; c0 += 32) {
             // the batch's sources spread evenly over the four source groups
             const int nr = min(8, (ns - c0 + 3) >> 2);
@@ -863,16 +869,27 @@ __device__ __forceinline__ void mu_target(const P2PArgs &A, const int *slot, con
                 __syncwarp();
             }
         }
-        // the entry's partial sums join the running sums with Kahan
-        // compensation (FP32: GB300's FP64 rate is 1/64 of FP32)
+        // every MU_FLUSH entries the partial sums join the running sums with
+        // Kahan compensation (FP32: GB300's FP64 rate is 1/64 of FP32)
+        if (++pending == MU_FLUSH) {
+            pending = 0;
 #pragma unroll
-        for (int p = 0; p < TP; p++) {
-            const float v[6] = {ax[p].x, ay[p].x, az[p].x, ax[p].y, ay[p].y, az[p].y};
+            for (int p = 0; p < TP; p++) {
+                const float v[6] = {ax[p].x, ay[p].x, az[p].x, ax[p].y, ay[p].y, az[p].y};
 #pragma unroll
-            for (int k = 0; k < 6; k++)
-                kahan_add(accw[(6 * p + k) * 32 + lane], accw[(3 * T + 6 * p + k) * 32 + lane], v[k]);
+                for (int k = 0; k < 6; k++)
+                    kahan_add(accw[(6 * p + k) * 32 + lane], accw[(3 * T + 6 * p + k) * 32 + lane], v[k]);
+                ax[p] = ay[p] = az[p] = f2(0.f);
+            }
         }
         __syncwarp();
+    }
+#pragma unroll
+    for (int p = 0; p < TP; p++) {
+        const float v[6] = {ax[p].x, ay[p].x, az[p].x, ax[p].y, ay[p].y, az[p].y};
+#pragma unroll
+        for (int k = 0; k < 6; k++)
+            kahan_add(accw[(6 * p + k) * 32 + lane], accw[(3 * T + 6 * p + k) * 32 + lane], v[k]);
     }
     __syncwarp();
     // targets: each lane takes one or two, summing its 4 source groups in order
