@@ -153,7 +153,7 @@ static int alloc_tree(photons_ctx *c, int n, int cap)
         PH_TRY(dalloc(w.m2l_off, cu)); PH_TRY(dalloc(w.m2l_cnt, cu));
         PH_TRY(dalloc(t.chi, cu)); PH_TRY(dalloc(t.clo, cu)); PH_TRY(dalloc(t.w32, cu)); PH_TRY(dalloc(t.son2, cu));
         PH_TRY(dalloc(t.boxid, cu));
-        PH_TRY(dalloc(c->mu_sorted, cu)); PH_TRY(dalloc(c->mu_nrecv, cu));
+        PH_TRY(dalloc(c->mu_sorted, cu)); PH_TRY(dalloc(c->mu_nrecv, cu)); PH_TRY(dalloc(c->mu_nev, cu));
         PH_TRY(dalloc(c->mu_size, cu)); PH_TRY(dalloc(c->mu_rbase, cu));
         PH_TRY(dalloc(c->mu_scan, ph::scan_scratch_elems(cu) + 8));
         if (!c->mu_total) { PH_TRY(dalloc(c->mu_total, 1)); PH_TRY(dalloc(c->mu_over, 1)); }
@@ -188,6 +188,7 @@ static int alloc_walk(photons_ctx *c, long long p2p_cap, long long pd_cap, long 
     if (p2p_cap > w.p2p_cap) {
         PH_TRY(dalloc(w.p2p_pool, p2p_cap));
         PH_TRY(dalloc(c->mu_slot, p2p_cap));
+        PH_TRY(dalloc(c->mu_ev, p2p_cap));
         w.p2p_cap = p2p_cap;
         c->mu_slot_cap = p2p_cap;
         c->epoch++;
@@ -229,7 +230,7 @@ static void free_all(photons_ctx *c)
                     c->az, c->M, c->L, c->io, c->work_counter, c->t.chi, c->t.clo, c->t.w32, c->t.son2, c->M32,
                     b.lvl_begin, b.lvl_count, b.leaf_begin, b.leaf_count, c->t.depth_cnt, b.tn_boxid, b.tl_boxid,
                     c->t.boxid, b.boxes, c->far_gate, c->mu_sorted, c->mu_nrecv, c->mu_slot, c->mu_over,
-                    c->mu_size, c->mu_rbase, c->mu_total, c->mu_scan, c->mu_buf};
+                    c->mu_size, c->mu_rbase, c->mu_total, c->mu_scan, c->mu_buf, c->mu_ev, c->mu_nev};
     for (void *p : ptrs)
         if (p) cudaFree(p);
 }
@@ -629,6 +630,7 @@ int ph_stage_p2p(photons_ctx *c, int precision, int zero)
         m.pool = c->w.p2p_pool;
         m.sorted = c->mu_sorted; m.nrecv = c->mu_nrecv; m.size = c->mu_size; m.rbase = c->mu_rbase;
         m.total = c->mu_total; m.scan_scratch = c->mu_scan; m.slot = c->mu_slot; m.over = c->mu_over;
+        m.ev = c->mu_ev; m.nev = c->mu_nev;
         m.buf = c->mu_buf; m.buf_cap = c->mu_buf_cap; m.cap_leaves = c->mu_cap_leaves;
         PH_TRY(ph::launch_p2p_mutual(a, m, st));
     } else {

@@ -55,6 +55,8 @@ struct photons_ctx {
     // mutual P2P (p2p.cu): per-leaf pairing data, per-entry slots, reaction buffer
     int *mu_sorted = nullptr, *mu_nrecv = nullptr, *mu_slot = nullptr, *mu_over = nullptr;
     long long *mu_size = nullptr, *mu_rbase = nullptr, *mu_total = nullptr, *mu_scan = nullptr;
+    int *mu_nev = nullptr;
+    int2 *mu_ev = nullptr;
     float *mu_buf = nullptr;
     long long mu_buf_cap = 0, mu_slot_cap = 0, hint_mubuf = 0;
     int mu_cap_leaves = 0;

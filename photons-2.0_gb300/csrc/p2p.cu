@@ -652,12 +652,13 @@ __global__ void k_leaf_offsets(const double *px, const double *py, const double 
 // first, by id); a local entry (A, B) is mutual when both lists are sorted
 // and B's list holds A; its slot is A's rank q in B's list.  B's received
 // entries are then the leading entries of its list (ids below B), so slot
-// q of B lives at rbase[B] + q nB 3 floats.
+// q of B lives at rbase[B] + 3 q nB floats, x then y then z of B's nB
+// particles.
 //
 // Lanes: 8 target groups x 4 source groups; a lane holds 8 targets (as four
 // pairs of the paired FP32 instructions) and takes 8 sources of each batch
 // of 32, so reactions are summed over 8 target groups through shared memory
-// and target sums over 4 source groups at the end (FP64, fixed order).
+// and target sums over 4 source groups at the end (fixed order).
 // ---------------------------------------------------------------------
 #define MU_TB 128
 #define MU_WARPS (MU_TB / 32)
@@ -736,39 +737,96 @@ __device__ __forceinline__ int mu_find(const uint32_t *lst, int L, uint32_t v)
 }
 
 // slot per entry: q >= 0 owned mutual (the owner's rank in the partner's
-// list), -2 received mutual, -1 evaluated one way
+// list), -2 received mutual, -1 evaluated one way; the entries a target
+// evaluates (all but the received) are also packed in list order into
+// ev[off + k] = (entry, slot), nev[t] of them
 __global__ void k_mu_slots(const int *tree_cnt, const unsigned long long *walk_flags, const uint32_t *pool,
                            const long long *off, const int *cnt, const int *sorted, const long long *total,
-                           long long cap, int *slot, int *over)
+                           long long cap, int *slot, int2 *ev, int *nev, int *over)
 {
     const int lane = warp_lane();
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
     const int nleaf = *walk_flags ? 0 : tree_cnt[BC_LEAVES];
     const bool fits = *total <= cap;
     if (gw == 0 && lane == 0) *over = fits ? 0 : 1;
+    const unsigned below = (1u << lane) - 1u;
     for (int t = gw; t < nleaf; t += nw) {
         const long long o = off[t];
         const int L = cnt[t];
         const bool st = sorted[t] && fits;
-        for (int e = lane; e < L; e += 32) {
-            const uint32_t v = pool[o + e];
-            const int b = PH_ENTRY_ID(v);
-            int r = -1;
-            if (st && PH_ENTRY_IMG(v) == 0 && b != t && sorted[b]) {
-                const int q = mu_find(pool + off[b], cnt[b], (uint32_t)t);
-                if (q >= 0) r = t < b ? q : -2;
+        int kept = 0;
+        for (int e0 = 0; e0 < L; e0 += 32) {
+            const int e = e0 + lane;
+            uint32_t v = 0;
+            int r = -2;
+            if (e < L) {
+                v = pool[o + e];
+                const int b = PH_ENTRY_ID(v);
+                r = -1;
+                if (st && PH_ENTRY_IMG(v) == 0 && b != t && sorted[b]) {
+                    const int q = mu_find(pool + off[b], cnt[b], (uint32_t)t);
+                    if (q >= 0) r = t < b ? q : -2;
+                }
+                slot[o + e] = r;
             }
-            slot[o + e] = r;
+            const unsigned keep = __ballot_sync(0xffffffffu, r != -2);
+            if (r != -2) ev[o + kept + __popc(keep & below)] = make_int2((int)v, r);
+            kept += __popc(keep);
         }
+        if (lane == 0) nev[t] = kept;
+    }
+}
+
+// one evaluated entry as the warp sees it: centre difference (source -
+// target, scaled), source range, and where its reactions go
+struct MuEntry {
+    float d0, d1, d2;
+    int is, ns, owned;
+    long long out;  // float offset of the pair's slot in the reaction buffer
+};
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+// copy an entry's raw source offsets (leaf-centre relative) into a stage
+__device__ __forceinline__ void mu_issue(const float4 *__restrict__ pos4, const MuEntry &E, float4 *buf, int lane)
+{
+    if (lane < E.ns) cp_async16(buf + lane, pos4 + E.is + lane);
+    if (lane + 32 < E.ns) cp_async16(buf + lane + 32, pos4 + E.is + lane + 32);
+}
+
+// once a lane's own copies have landed: scale and shift them in place
+// (relative to the target centre); padding is far away
+__device__ __forceinline__ void mu_place(const MuEntry &E, float4 *buf, float sig, int lane)
+{
+    const float far = 1e18f;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int j = lane + 32 * h;
+        float4 v = make_float4(far, far, far, 0.f);
+        if (j < E.ns) {
+            const float4 o = buf[j];
+            v = make_float4(fmaf(o.x, sig, E.d0), fmaf(o.y, sig, E.d1), fmaf(o.z, sig, E.d2), 0.f);
+        }
+        buf[j] = v;
     }
 }
 
 // one target leaf with T targets per lane (8: leaves of up to 64
-// particles, 4: up to 32), eight target groups x four source groups
+// particles, 4: up to 32), eight target groups x four source groups.
+// Entries come in batches of 32: each lane loads one entry's metadata into
+// shared memory, then the warp walks the batch with the next entry's
+// sources in flight (cp.async into the second stage) while it evaluates
+// the current one.
 template <int T>
-__device__ __forceinline__ void mu_target(const P2PArgs &A, const int *slot, const long long *rbase, float *rbuf, int t,
-                                          int nt, int it, const SplitConsts &K, float Lhi, float Llo, float4 *src,
-                                          float *red, float *accw, int lane)
+__device__ __forceinline__ void mu_target(const P2PArgs &A, const int2 *ev, int ne, const long long *rbase,
+                                          float *rbuf, int t, int nt, int it, const SplitConsts &K, float Lhi,
+                                          float Llo, float4 *src, MuEntry *meta, float *red, float *accw, int lane)
 {
     constexpr int TP = T / 2;  // target pairs per lane
     const int tg = lane >> 2, sg = lane & 3;
@@ -790,99 +848,109 @@ __device__ __forceinline__ void mu_target(const P2PArgs &A, const int *slot, con
     }
 #pragma unroll
     for (int k = 0; k < 6 * T; k++) accw[k * 32 + lane] = 0.f;
-    const long long eoff = A.p2p_off[t];
-    const int ecnt = A.p2p_cnt[t];
     // partial sums run over up to MU_FLUSH evaluated entries (at most 64 terms
     // per lane) before they join the compensated running sums
     float2 ax[TP], ay[TP], az[TP];
 #pragma unroll
     for (int p = 0; p < TP; p++) ax[p] = ay[p] = az[p] = f2(0.f);
     int pending = 0;
-    for (int e = 0; e < ecnt; e++) {
-        const int sl = slot[eoff + e];
-        if (sl == -2) continue;  // received: the owner writes it
-        const uint32_t en = A.p2p_pool[eoff + e];
-        const int s = PH_ENTRY_ID(en), img = PH_ENTRY_IMG(en);
-        const int is = A.ipart[s], ns = A.npart[s];
-        const float4 csh = A.chi[s], csl = A.clo[s];
-        int mi, mj, mk;
-        image_offsets(img, mi, mj, mk);
-        const float d0 = centre_diff(csh.x, csl.x, cth.x, ctl.x, mi, Lhi, Llo) * K.sig;
-        const float d1 = centre_diff(csh.y, csl.y, cth.y, ctl.y, mj, Lhi, Llo) * K.sig;
-        const float d2 = centre_diff(csh.z, csl.z, cth.z, ctl.z, mk, Lhi, Llo) * K.sig;
-        // stage the source leaf (scaled, relative to the target centre); padding is far away
-        for (int j = lane; j < 64; j += 32) {
-            float4 v = make_float4(far, far, far, 0.f);
-            if (j < ns) {
-                const float4 o = A.pos4[is + j];
-                v = make_float4(fmaf(o.x, K.sig, d0), fmaf(o.y, K.sig, d1), fmaf(o.z, K.sig, d2), 0.f);
-            }
-            src[j] = v;
+    for (int k0 = 0; k0 < ne; k0 += 32) {
+        const int kmax = min(32, ne - k0);
+        if (lane < kmax) {
+            const int2 en = ev[k0 + lane];
+            const int s = PH_ENTRY_ID((uint32_t)en.x), img = PH_ENTRY_IMG((uint32_t)en.x);
+            const float4 csh = A.chi[s], csl = A.clo[s];
+            int mi, mj, mk;
+            image_offsets(img, mi, mj, mk);
+            MuEntry m;
+            m.d0 = centre_diff(csh.x, csl.x, cth.x, ctl.x, mi, Lhi, Llo) * K.sig;
+            m.d1 = centre_diff(csh.y, csl.y, cth.y, ctl.y, mj, Lhi, Llo) * K.sig;
+            m.d2 = centre_diff(csh.z, csl.z, cth.z, ctl.z, mk, Lhi, Llo) * K.sig;
+            m.is = A.ipart[s];
+            m.ns = A.npart[s];
+            m.owned = en.y >= 0;
+            m.out = en.y >= 0 ? rbase[s] + (long long)en.y * m.ns * 3 : 0;
+            meta[lane] = m;
         }
         __syncwarp();
-        const bool owned = sl >= 0;
-        for (int c0 = 0; c0 < ns; c0 += 32) {
-            // the batch's sources spread evenly over the four source groups
-            const int nr = min(8, (ns - c0 + 3) >> 2);
+        int cur = 0;
+        mu_issue(A.pos4, meta[0], src, lane);
+        cp_async_commit();
+        for (int kk = 0; kk < kmax; kk++) {
+            const MuEntry E = meta[kk];
+            float4 *stage = src + 64 * cur;
+            if (kk + 1 < kmax) mu_issue(A.pos4, meta[kk + 1], src + 64 * (cur ^ 1), lane);
+            cp_async_commit();
+            cp_async_wait_prev();
+            mu_place(E, stage, K.sig, lane);
+            __syncwarp();
+            const int ns = E.ns;
+            const bool owned = E.owned;
+            for (int c0 = 0; c0 < ns; c0 += 32) {
+                // the batch's sources spread evenly over the four source groups
+                const int nr = min(8, (ns - c0 + 3) >> 2);
 #pragma unroll kMuUnroll
-            for (int r = 0; r < nr; r++) {
-                const float4 S = src[c0 + 4 * r + sg];
-                const float2 sx = f2(S.x), sy = f2(S.y), sz = f2(S.z);
-                float2 rx = f2(0.f), ry = f2(0.f), rz = f2(0.f);
+                for (int r = 0; r < nr; r++) {
+                    const float4 S = stage[c0 + 4 * r + sg];
+                    const float2 sx = f2(S.x), sy = f2(S.y), sz = f2(S.z);
+                    float2 rx = f2(0.f), ry = f2(0.f), rz = f2(0.f);
 #pragma unroll
-                for (int p = 0; p < TP; p++) {
-                    const float2 dx = __fadd2_rn(sx, nx[p]);
-                    const float2 dy = __fadd2_rn(sy, ny[p]);
-                    const float2 dz = __fadd2_rn(sz, nz[p]);
-                    float2 qq = __fmul2_rn(dx, dx);
-                    qq = __ffma2_rn(dy, dy, qq);
-                    qq = __ffma2_rn(dz, dz, qq);
-                    const float2 f = pair_factor(qq, K, pia2, one2, c2, a0, a1, a2, a3, a4, a5);
-                    ax[p] = __ffma2_rn(dx, f, ax[p]);
-                    ay[p] = __ffma2_rn(dy, f, ay[p]);
-                    az[p] = __ffma2_rn(dz, f, az[p]);
+                    for (int p = 0; p < TP; p++) {
+                        const float2 dx = __fadd2_rn(sx, nx[p]);
+                        const float2 dy = __fadd2_rn(sy, ny[p]);
+                        const float2 dz = __fadd2_rn(sz, nz[p]);
+                        float2 qq = __fmul2_rn(dx, dx);
+                        qq = __ffma2_rn(dy, dy, qq);
+                        qq = __ffma2_rn(dz, dz, qq);
+                        const float2 f = pair_factor(qq, K, pia2, one2, c2, a0, a1, a2, a3, a4, a5);
+                        ax[p] = __ffma2_rn(dx, f, ax[p]);
+                        ay[p] = __ffma2_rn(dy, f, ay[p]);
+                        az[p] = __ffma2_rn(dz, f, az[p]);
+                        if (owned) {
+                            rx = __ffma2_rn(dx, f, rx);
+                            ry = __ffma2_rn(dy, f, ry);
+                            rz = __ffma2_rn(dz, f, rz);
+                        }
+                    }
                     if (owned) {
-                        rx = __ffma2_rn(dx, f, rx);
-                        ry = __ffma2_rn(dy, f, ry);
-                        rz = __ffma2_rn(dz, f, rz);
+                        float *rr = red + (4 * r + sg) * 24 + tg;
+                        rr[0] = rx.x + rx.y;
+                        rr[8] = ry.x + ry.y;
+                        rr[16] = rz.x + rz.y;
                     }
                 }
                 if (owned) {
-                    float *rr = red + (4 * r + sg) * 40 + tg;
-                    rr[0] = rx.x + rx.y;
-                    rr[8] = ry.x + ry.y;
-                    rr[16] = rz.x + rz.y;
-                }
-            }
-            if (owned) {
-                // reactions of the batch's sources: minus the sum over the 8 target groups
-                __syncwarp();
-                float *out = rbuf + rbase[s] + (long long)sl * ns * 3 + (long long)c0 * 3;
-                for (int k = lane; k < 96; k += 32) {
-                    const int j = k / 3, cmp = k - 3 * j;
-                    if (c0 + j < ns) {
-                        const float4 *rr = reinterpret_cast<const float4 *>(red + j * 40 + cmp * 8);
-                        const float4 u = rr[0], w = rr[1];
-                        out[k] = -((((u.x + u.y) + (u.z + u.w)) + ((w.x + w.y) + (w.z + w.w))));
+                    // reactions of the batch's sources: minus the sum over the 8 target groups
+                    __syncwarp();
+                    // slot layout [component][source particle]
+                    if (c0 + lane < ns) {
+                        float *out = rbuf + E.out + c0 + lane;
+#pragma unroll
+                        for (int cmp = 0; cmp < 3; cmp++) {
+                            const float4 *rr = reinterpret_cast<const float4 *>(red + lane * 24 + cmp * 8);
+                            const float4 u = rr[0], w = rr[1];
+                            out[cmp * ns] = -((((u.x + u.y) + (u.z + u.w)) + ((w.x + w.y) + (w.z + w.w))));
+                        }
                     }
+                    __syncwarp();
                 }
-                __syncwarp();
             }
-        }
-        // every MU_FLUSH entries the partial sums join the running sums with
-        // Kahan compensation (FP32: GB300's FP64 rate is 1/64 of FP32)
-        if (++pending == MU_FLUSH) {
-            pending = 0;
+            // every MU_FLUSH entries the partial sums join the running sums with
+            // Kahan compensation (FP32: GB300's FP64 rate is 1/64 of FP32)
+            if (++pending == MU_FLUSH) {
+                pending = 0;
 #pragma unroll
-            for (int p = 0; p < TP; p++) {
-                const float v[6] = {ax[p].x, ay[p].x, az[p].x, ax[p].y, ay[p].y, az[p].y};
+                for (int p = 0; p < TP; p++) {
+                    const float v[6] = {ax[p].x, ay[p].x, az[p].x, ax[p].y, ay[p].y, az[p].y};
 #pragma unroll
-                for (int k = 0; k < 6; k++)
-                    kahan_add(accw[(6 * p + k) * 32 + lane], accw[(3 * T + 6 * p + k) * 32 + lane], v[k]);
-                ax[p] = ay[p] = az[p] = f2(0.f);
+                    for (int k = 0; k < 6; k++)
+                        kahan_add(accw[(6 * p + k) * 32 + lane], accw[(3 * T + 6 * p + k) * 32 + lane], v[k]);
+                    ax[p] = ay[p] = az[p] = f2(0.f);
+                }
             }
+            __syncwarp();
+            cur ^= 1;
         }
-        __syncwarp();
     }
 #pragma unroll
     for (int p = 0; p < TP; p++) {
@@ -915,15 +983,17 @@ __device__ __forceinline__ void mu_target(const P2PArgs &A, const int *slot, con
     __syncwarp();
 }
 
-__global__ void __launch_bounds__(MU_TB, MU_MINB) k_p2p_mutual(P2PArgs A, const int *slot, const long long *rbase,
-                                                               float *rbuf)
+__global__ void __launch_bounds__(MU_TB, MU_MINB) k_p2p_mutual(P2PArgs A, const int2 *ev, const int *nev,
+                                                               const long long *rbase, float *rbuf)
 {
     // shared layouts avoid bank conflicts: a batch's source k (of 32) is
     // read by source group k % 4, so the four groups read adjacent float4s;
-    // reactions [source][component][target group] with a 40-word source
-    // stride; running sums [value][lane]
-    __shared__ __align__(16) float4 s_src[MU_WARPS][64];
-    __shared__ __align__(16) float s_red[MU_WARPS][32 * 40];
+    // reactions [source][component][target group] with a 24-word source
+    // stride; running sums [value][lane].  12 KB per warp: four blocks of
+    // four warps fill an SM's 228 KB.
+    __shared__ __align__(16) float4 s_src[MU_WARPS][2 * 64];  // two stages
+    __shared__ __align__(16) MuEntry s_meta[MU_WARPS][32];
+    __shared__ __align__(16) float s_red[MU_WARPS][32 * 24];
     __shared__ float s_acc[MU_WARPS][48 * 32];  // Kahan sum and compensation of up to 8 targets x 3, per lane
     const int lane = warp_lane(), wib = threadIdx.x >> 5;
     SplitConsts K = A.k;
@@ -941,14 +1011,21 @@ __global__ void __launch_bounds__(MU_TB, MU_MINB) k_p2p_mutual(P2PArgs A, const 
         K.e2s = B.e2s;
         K.pias = B.pias;
         K.cs = B.cs;
+        const int2 *evt = ev + A.p2p_off[t];
+        const int ne = nev[t];
         if (nt > 32)
-            mu_target<8>(A, slot, rbase, rbuf, t, nt, it, K, B.Lhi, B.Llo, s_src[wib], s_red[wib], s_acc[wib], lane);
+            mu_target<8>(A, evt, ne, rbase, rbuf, t, nt, it, K, B.Lhi, B.Llo, s_src[wib], s_meta[wib], s_red[wib],
+                         s_acc[wib], lane);
         else
-            mu_target<4>(A, slot, rbase, rbuf, t, nt, it, K, B.Lhi, B.Llo, s_src[wib], s_red[wib], s_acc[wib], lane);
+            mu_target<4>(A, evt, ne, rbase, rbuf, t, nt, it, K, B.Lhi, B.Llo, s_src[wib], s_meta[wib], s_red[wib],
+                         s_acc[wib], lane);
     }
 }
 
-// each leaf adds the reactions its owners left in its slots, in list order
+// each leaf adds the reactions its owners left in its slots, in list order.
+// Slot r of leaf t holds [3][nt] floats at rbase[t] + 3 r nt; which slots
+// were written (slot == -2) is read once per 32 as a warp mask, and eight
+// slots' loads are in flight at a time.
 __global__ void k_mu_gather(P2PArgs A, const int *slot, const int *nrecv, const long long *rbase, const float *rbuf)
 {
     const int lane = warp_lane();
@@ -959,27 +1036,31 @@ __global__ void k_mu_gather(P2PArgs A, const int *slot, const int *nrecv, const 
         if (nr == 0 || nt == 0) continue;
         const long long eoff = A.p2p_off[t];
         const double scale = A.boxes[A.boxid[t]].acc_scale;
-        const float *base = rbuf + rbase[t];
+        const long long stride = 3LL * nt;
         for (int j0 = 0; j0 < nt; j0 += 32) {
             const int j = j0 + lane;
+            const float *base = rbuf + rbase[t] + j;
             float v0 = 0.f, v1 = 0.f, v2 = 0.f, c0 = 0.f, c1 = 0.f, c2 = 0.f;
-            for (int r0 = 0; r0 < nr; r0 += 4) {
-                // four slots' loads in flight, then added in slot order
-                float in[4][3];
+            for (int r0 = 0; r0 < nr; r0 += 32) {
+                const unsigned got = __ballot_sync(0xffffffffu, r0 + lane < nr && slot[eoff + r0 + lane] == -2);
+                for (int k0 = 0; k0 < 32 && (got >> k0); k0 += 8) {
+                    float in[8][3];
 #pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    const int r = r0 + k;
-                    const bool use = r < nr && j < nt && slot[eoff + r] == -2;
-                    const float *q = base + ((long long)r * nt + j) * 3;
-                    in[k][0] = use ? q[0] : 0.f;
-                    in[k][1] = use ? q[1] : 0.f;
-                    in[k][2] = use ? q[2] : 0.f;
-                }
+                    for (int k = 0; k < 8; k++) {
+                        const bool use = j < nt && ((got >> (k0 + k)) & 1u);
+                        const float *q = base + (r0 + k0 + k) * stride;
+                        in[k][0] = use ? q[0] : 0.f;
+                        in[k][1] = use ? q[nt] : 0.f;
+                        in[k][2] = use ? q[2 * nt] : 0.f;
+                    }
 #pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    kahan_add(v0, c0, in[k][0]);
-                    kahan_add(v1, c1, in[k][1]);
-                    kahan_add(v2, c2, in[k][2]);
+                    for (int k = 0; k < 8; k++) {
+                        if ((got >> (k0 + k)) & 1u) {
+                            kahan_add(v0, c0, in[k][0]);
+                            kahan_add(v1, c1, in[k][1]);
+                            kahan_add(v2, c2, in[k][2]);
+                        }
+                    }
                 }
             }
             if (j < nt) {
@@ -1038,8 +1119,9 @@ int launch_p2p_mutual(const P2PArgs &a, const MutualBufs &m, cudaStream_t st)
                                                            a.npart, m.sorted, m.nrecv, m.size);
     scan_exclusive_i64(m.size, m.rbase, a.tree_cnt + BC_LEAVES, m.cap_leaves, m.total, m.scan_scratch, st);
     ph::note_launch(), k_mu_slots<<<sms * 8, 256, 0, st>>>(a.tree_cnt, a.walk_flags, m.pool, a.p2p_off, a.p2p_cnt,
-                                                            m.sorted, m.total, m.buf_cap, m.slot, m.over);
-    ph::note_launch(), k_p2p_mutual<<<sms * MU_MINB, MU_TB, 0, st>>>(a, m.slot, m.rbase, m.buf);
+                                                            m.sorted, m.total, m.buf_cap, m.slot, m.ev, m.nev,
+                                                            m.over);
+    ph::note_launch(), k_p2p_mutual<<<sms * MU_MINB, MU_TB, 0, st>>>(a, m.ev, m.nev, m.rbase, m.buf);
     ph::note_launch(), k_mu_gather<<<sms * 8, 256, 0, st>>>(a, m.slot, m.nrecv, m.rbase, m.buf);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;

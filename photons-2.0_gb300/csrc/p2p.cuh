@@ -52,6 +52,8 @@ struct MutualBufs {
     float *buf;              // reactions
     long long buf_cap;       // floats
     int cap_leaves;
+    int2 *ev;                // per pool offset: the entries a target evaluates, packed in list order
+    int *nev;                // per leaf: their number
 };
 
 SplitConsts make_split_consts(const PassParams &p);
