@@ -505,7 +505,8 @@ def main():
     t_p2p = float(np.mean(p2p_ms))
     achieved = FLOPS_PER_PAIR * pairs / (t_p2p * 1e-3) / 1e12
     traffic = None
-    tp = os.path.join(ROOT, "profiles", "k_p2p_split_packed_zeldovich160.md")
+    tp = os.path.join(ROOT, "profiles", {"k_p2p_mutual": "k_p2p_mutual_zeldovich128.md",
+                                         "k_p2p_split_packed": "k_p2p_split_packed_zeldovich160.md"}[kernel])
     if os.path.exists(tp) and args.nside == 256:
         import re
         m = re.search(r"dram_bytes_per_launch_scaled_to_256:\s*([0-9.eE+]+)", open(tp).read())

@@ -187,10 +187,7 @@ static int alloc_walk(photons_ctx *c, long long p2p_cap, long long pd_cap, long 
     if (!c->work_counter) { PH_TRY(dalloc(c->work_counter, 4)); c->epoch++; }
     if (p2p_cap > w.p2p_cap) {
         PH_TRY(dalloc(w.p2p_pool, p2p_cap));
-        PH_TRY(dalloc(c->mu_slot, p2p_cap));
-        PH_TRY(dalloc(c->mu_ev, p2p_cap));
         w.p2p_cap = p2p_cap;
-        c->mu_slot_cap = p2p_cap;
         c->epoch++;
     }
     if (pd_cap > w.pd_cap) {
@@ -276,12 +273,39 @@ static bool mutual_feedback(photons_ctx *c, int over, long long need)
     return true;
 }
 
-static int alloc_mutual(photons_ctx *c)
+// mutual pairs pay off from leaf size 48 (256^3: 71 vs 91 ms at leaf 64, a
+// tie at 32); below that the per-entry work outweighs the halved pairs
+static bool uses_mutual(const photons_ctx *c, int precision)
 {
+    return precision != PHOTONS_FP64 && p2p_variant() == 2 && c->pp.maxleaf >= 48 && c->pp.maxleaf <= 64 &&
+           !c->mu_off;
+}
+
+// buffers of the mutual kernel, only for passes that run it: per-entry
+// slots and packed entries (the P2P pool's capacity) and the reaction slots
+static int alloc_mutual(photons_ctx *c, int precision)
+{
+    if (!uses_mutual(c, precision)) return 0;
     // first guess: about half of a leaf's ~110-250 list entries received, 3
     // floats per particle and entry (256^3 leaf 64 needs ~170 per particle);
     // a pass that needs more repeats once with the measured size
     long long want = c->hint_mubuf ? c->hint_mubuf : (long long)c->n * 176 + 4096;
+    // the reaction slots take ~700 bytes per particle: where they would not
+    // leave 1 GB of the device free, this context evaluates every pair one way
+    size_t grow = 0, free_b = 0, total_b = 0;
+    if (c->w.p2p_cap > c->mu_slot_cap) grow += (size_t)(c->w.p2p_cap - c->mu_slot_cap) * (sizeof(int) + sizeof(int2));
+    if (want > c->mu_buf_cap) grow += (size_t)(want - c->mu_buf_cap) * sizeof(float);
+    if (grow && cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && grow + ((size_t)1 << 30) > free_b) {
+        c->mu_off = true;
+        c->epoch++;
+        return 0;
+    }
+    if (c->w.p2p_cap > c->mu_slot_cap) {
+        PH_TRY(dalloc(c->mu_slot, (size_t)c->w.p2p_cap));
+        PH_TRY(dalloc(c->mu_ev, (size_t)c->w.p2p_cap));
+        c->mu_slot_cap = c->w.p2p_cap;
+        c->epoch++;
+    }
     if (want > c->mu_buf_cap) {
         PH_TRY(dalloc(c->mu_buf, (size_t)want));
         c->mu_buf_cap = want;
@@ -594,7 +618,7 @@ int ph_stage_walk(photons_ctx *c, unsigned mask)
 int ph_stage_p2p(photons_ctx *c, int precision, int zero)
 {
     cudaStream_t st = c->stream;
-    PH_TRY(alloc_mutual(c));
+    PH_TRY(alloc_mutual(c, precision));
     PH_CUDA_CHECK(cudaMemsetAsync(c->mu_over, 0, sizeof(int), st));
     PH_CUDA_CHECK(cudaMemsetAsync(c->mu_total, 0, sizeof(long long), st));
     const int n = c->n;
@@ -623,9 +647,7 @@ int ph_stage_p2p(photons_ctx *c, int precision, int zero)
     a.k = ph::make_split_consts(c->pp);
     a.variant = p2p_variant();
     PH_TRY(ph_record(c, EV_P2P_BEGIN));
-    // mutual pairs pay off from leaf size 48 (256^3: 71 vs 91 ms at leaf 64, a
-    // tie at 32); below that the per-entry work outweighs the halved pairs
-    if (precision != PHOTONS_FP64 && a.variant == 2 && c->pp.maxleaf >= 48 && c->pp.maxleaf <= 64) {
+    if (uses_mutual(c, precision)) {
         ph::MutualBufs m;
         m.pool = c->w.p2p_pool;
         m.sorted = c->mu_sorted; m.nrecv = c->mu_nrecv; m.size = c->mu_size; m.rbase = c->mu_rbase;
@@ -797,7 +819,7 @@ static int force_pass_graph(photons_ctx *c, int nbox, const photons_params *p, c
     double *dst = dio ? acc : c->io;
     for (int attempt = 0; attempt < 16; attempt++) {
         PH_TRY(alloc_walk(c, p2p_cap, pd_cap, m2l_cap, stack_cap, stage_cap));
-        PH_TRY(alloc_mutual(c));
+        PH_TRY(alloc_mutual(c, p->precision));
         PassKey k = pass_key(c, p, n, pos, acc, dio, levels, mask);
         if (!c->gexec || !c->have_key || memcmp(&k, &c->key, sizeof k) != 0) {
             PH_TRY(capture_pass(c, p, src, dst, levels, mask));

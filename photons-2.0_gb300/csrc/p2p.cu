@@ -673,6 +673,9 @@ constexpr int kMuUnroll = MU_UNROLL;
 #define MU_FLUSH 4  // evaluated entries per compensated flush of the partial sums
 #endif
 #define MU_SORT_MAX 1024  // longer lists stay unsorted and are evaluated one way
+#ifndef MU_BATCH
+#define MU_BATCH 32  // sources per reaction reduction (32 or 16)
+#endif
 
 __global__ void __launch_bounds__(256) k_mu_sort(const int *tree_cnt, const unsigned long long *walk_flags,
                                                   uint32_t *pool, const long long *off, const int *cnt,
@@ -886,9 +889,9 @@ __device__ __forceinline__ void mu_target(const P2PArgs &A, const int2 *ev, int 
             __syncwarp();
             const int ns = E.ns;
             const bool owned = E.owned;
-            for (int c0 = 0; c0 < ns; c0 += 32) {
+            for (int c0 = 0; c0 < ns; c0 += MU_BATCH) {
                 // the batch's sources spread evenly over the four source groups
-                const int nr = min(8, (ns - c0 + 3) >> 2);
+                const int nr = min(MU_BATCH / 4, (ns - c0 + 3) >> 2);
 #pragma unroll kMuUnroll
                 for (int r = 0; r < nr; r++) {
                     const float4 S = stage[c0 + 4 * r + sg];
@@ -923,7 +926,7 @@ __device__ __forceinline__ void mu_target(const P2PArgs &A, const int2 *ev, int 
                     // reactions of the batch's sources: minus the sum over the 8 target groups
                     __syncwarp();
                     // slot layout [component][source particle]
-                    if (c0 + lane < ns) {
+                    if (lane < MU_BATCH && c0 + lane < ns) {
                         float *out = rbuf + E.out + c0 + lane;
 #pragma unroll
                         for (int cmp = 0; cmp < 3; cmp++) {
@@ -993,7 +996,7 @@ __global__ void __launch_bounds__(MU_TB, MU_MINB) k_p2p_mutual(P2PArgs A, const 
     // four warps fill an SM's 228 KB.
     __shared__ __align__(16) float4 s_src[MU_WARPS][2 * 64];  // two stages
     __shared__ __align__(16) MuEntry s_meta[MU_WARPS][32];
-    __shared__ __align__(16) float s_red[MU_WARPS][32 * 24];
+    __shared__ __align__(16) float s_red[MU_WARPS][MU_BATCH * 24];
     __shared__ float s_acc[MU_WARPS][48 * 32];  // Kahan sum and compensation of up to 8 targets x 3, per lane
     const int lane = warp_lane(), wib = threadIdx.x >> 5;
     SplitConsts K = A.k;
