@@ -262,6 +262,65 @@ __device__ __forceinline__ float2 pair_factor(float2 qq, const SplitConsts &K, f
     return __fmul2_rn(__fmul2_rn(ex, __fmul2_rn(rinv, rinv)), g1);
 }
 
+// IL target pairs of one source, evaluated stage by stage so that the IL
+// dependency chains interleave; accumulates into the target sums and the
+// source's reaction sums
+template <int IL>
+__device__ __forceinline__ void mu_pairs(float2 sx, float2 sy, float2 sz, const float2 *nx, const float2 *ny,
+                                         const float2 *nz, float2 *ax, float2 *ay, float2 *az, float2 &rx,
+                                         float2 &ry, float2 &rz, bool owned, const SplitConsts &K, float2 pia2,
+                                         float2 one2, float2 c2, float2 a0, float2 a1, float2 a2, float2 a3,
+                                         float2 a4, float2 a5)
+{
+    float2 dx[IL], dy[IL], dz[IL], qq[IL], rinv[IL], tt[IL], P[IL], ex[IL];
+#pragma unroll
+    for (int k = 0; k < IL; k++) {
+        dx[k] = __fadd2_rn(sx, nx[k]);
+        dy[k] = __fadd2_rn(sy, ny[k]);
+        dz[k] = __fadd2_rn(sz, nz[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < IL; k++) {
+        qq[k] = __fmul2_rn(dx[k], dx[k]);
+        qq[k] = __ffma2_rn(dy[k], dy[k], qq[k]);
+        qq[k] = __ffma2_rn(dz[k], dz[k], qq[k]);
+        qq[k].x = fmaxf(qq[k].x, K.e2s);
+        qq[k].y = fmaxf(qq[k].y, K.e2s);
+    }
+#pragma unroll
+    for (int k = 0; k < IL; k++) rinv[k] = make_float2(rsqrt_approx(qq[k].x), rsqrt_approx(qq[k].y));
+#pragma unroll
+    for (int k = 0; k < IL; k++) {
+        const float2 den = __ffma2_rn(pia2, __fmul2_rn(qq[k], rinv[k]), one2);
+        tt[k] = make_float2(rcp_approx(den.x), rcp_approx(den.y));
+    }
+#pragma unroll
+    for (int k = 0; k < IL; k++) ex[k] = make_float2(ex2_approx(-qq[k].x), ex2_approx(-qq[k].y));
+#pragma unroll
+    for (int k = 0; k < IL; k++) P[k] = __ffma2_rn(a5, tt[k], a4);
+#pragma unroll
+    for (int k = 0; k < IL; k++) P[k] = __ffma2_rn(P[k], tt[k], a3);
+#pragma unroll
+    for (int k = 0; k < IL; k++) P[k] = __ffma2_rn(P[k], tt[k], a2);
+#pragma unroll
+    for (int k = 0; k < IL; k++) P[k] = __ffma2_rn(P[k], tt[k], a1);
+#pragma unroll
+    for (int k = 0; k < IL; k++) P[k] = __ffma2_rn(P[k], tt[k], a0);
+#pragma unroll
+    for (int k = 0; k < IL; k++) {
+        const float2 g1 = __ffma2_rn(__fmul2_rn(tt[k], rinv[k]), P[k], c2);
+        const float2 f = __fmul2_rn(__fmul2_rn(ex[k], __fmul2_rn(rinv[k], rinv[k])), g1);
+        ax[k] = __ffma2_rn(dx[k], f, ax[k]);
+        ay[k] = __ffma2_rn(dy[k], f, ay[k]);
+        az[k] = __ffma2_rn(dz[k], f, az[k]);
+        if (owned) {
+            rx = __ffma2_rn(dx[k], f, rx);
+            ry = __ffma2_rn(dy[k], f, ry);
+            rz = __ffma2_rn(dz[k], f, rz);
+        }
+    }
+}
+
 // one round's share of a staged batch: stream k takes source pairs k, k+G, ...
 __device__ __forceinline__ void p2p_round(const float2 *__restrict__ X2, const float2 *__restrict__ Y2,
                                           const float2 *__restrict__ Z2, int npairs, int k, int G, float ox,
@@ -663,7 +722,7 @@ __global__ void k_leaf_offsets(const double *px, const double *py, const double 
 #define MU_TB 128
 #define MU_WARPS (MU_TB / 32)
 #ifndef MU_MINB
-#define MU_MINB 4  // resident blocks of MU_TB per SM the mutual kernel is compiled for (126 registers)
+#define MU_MINB 3  // resident blocks of MU_TB per SM the mutual kernel is compiled for (158 registers)
 #endif
 #ifndef MU_UNROLL
 #define MU_UNROLL 1
@@ -673,6 +732,9 @@ constexpr int kMuUnroll = MU_UNROLL;
 #define MU_FLUSH 4  // evaluated entries per compensated flush of the partial sums
 #endif
 #define MU_SORT_MAX 1024  // longer lists stay unsorted and are evaluated one way
+#ifndef MU_IL
+#define MU_IL 2  // target pairs evaluated stage by stage together (1, 2 or 4)
+#endif
 #ifndef MU_BATCH
 #define MU_BATCH 32  // sources per reaction reduction (32 or 16)
 #endif
@@ -897,6 +959,15 @@ __device__ __forceinline__ void mu_target(const P2PArgs &A, const int2 *ev, int 
                     const float4 S = stage[c0 + 4 * r + sg];
                     const float2 sx = f2(S.x), sy = f2(S.y), sz = f2(S.z);
                     float2 rx = f2(0.f), ry = f2(0.f), rz = f2(0.f);
+#if MU_IL > 1
+                    // never more chains than this lane's TP target pairs
+                    constexpr int IL = MU_IL < TP ? MU_IL : TP;
+                    static_assert(TP % IL == 0, "target pairs in whole interleave groups");
+#pragma unroll
+                    for (int p = 0; p < TP; p += IL)
+                        mu_pairs<IL>(sx, sy, sz, nx + p, ny + p, nz + p, ax + p, ay + p, az + p, rx, ry, rz, owned, K,
+                                     pia2, one2, c2, a0, a1, a2, a3, a4, a5);
+#else
 #pragma unroll
                     for (int p = 0; p < TP; p++) {
                         const float2 dx = __fadd2_rn(sx, nx[p]);
@@ -915,6 +986,7 @@ __device__ __forceinline__ void mu_target(const P2PArgs &A, const int2 *ev, int 
                             rz = __ffma2_rn(dz, f, rz);
                         }
                     }
+#endif
                     if (owned) {
                         float *rr = red + (4 * r + sg) * 24 + tg;
                         rr[0] = rx.x + rx.y;
@@ -992,8 +1064,7 @@ __global__ void __launch_bounds__(MU_TB, MU_MINB) k_p2p_mutual(P2PArgs A, const 
     // shared layouts avoid bank conflicts: a batch's source k (of 32) is
     // read by source group k % 4, so the four groups read adjacent float4s;
     // reactions [source][component][target group] with a 24-word source
-    // stride; running sums [value][lane].  12 KB per warp: four blocks of
-    // four warps fill an SM's 228 KB.
+    // stride; running sums [value][lane].  12 KB per warp.
     __shared__ __align__(16) float4 s_src[MU_WARPS][2 * 64];  // two stages
     __shared__ __align__(16) MuEntry s_meta[MU_WARPS][32];
     __shared__ __align__(16) float s_red[MU_WARPS][MU_BATCH * 24];
