@@ -845,7 +845,6 @@ static int force_pass_graph(photons_ctx *c, int nbox, const photons_params *p, c
         PH_CUDA_CHECK(cudaMemcpyAsync(&mu_need, c->mu_total, sizeof mu_need, cudaMemcpyDeviceToHost, st));
         PH_CUDA_CHECK(cudaMemcpyAsync(&mu_over, c->mu_over, sizeof mu_over, cudaMemcpyDeviceToHost, st));
         PH_CUDA_CHECK(cudaStreamSynchronize(st));
-        const bool mu_grow = mutual_feedback(c, mu_over, mu_need);
         int grow = 0;
         PH_TRY(ph_check_build(c, h[ph::BC_FLAGS], levels, &grow));
         if (grow) { levels = grow; continue; }
@@ -856,7 +855,8 @@ static int force_pass_graph(photons_ctx *c, int nbox, const photons_params *p, c
             grow_walk_caps(c, fl, p2p_cap, pd_cap, m2l_cap, stack_cap, stage_cap);
             continue;
         }
-        if (mu_grow) continue;
+        // the reaction total means something only once tree and lists are complete
+        if (mutual_feedback(c, mu_over, mu_need)) continue;
         c->info.depth_off.resize(c->info.depth + 2);
         c->have_lists = true;
         c->mask = mask;

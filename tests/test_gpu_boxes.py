@@ -39,6 +39,20 @@ def test_boxes_match_separate_passes(ph, ics, precision):
         assert cb[k] == sums[k], k
 
 
+@pytest.mark.parametrize("maxleaf", [48, 64])
+def test_boxes_mutual_pairs_match_separate_passes(ph, ics, maxleaf):
+    """From leaf 48 the FP32 pass evaluates each symmetric leaf pair once
+    (reactions through per-pair slots).  Pairing never crosses boxes and
+    keeps each box's leaf order, so the batched pass still equals the
+    separate passes bit for bit."""
+    boxes = [(pos, dict(p, maxleaf=maxleaf, theta=0.5))
+             for pos, p in ics.plummer_boxes(nbox=4, seed=6, nmin=24 ** 3, nmax=32 ** 3)]
+    got = ph.ForcePass(0).run_boxes(boxes, precision=ph.FP32_SPLIT)
+    one = ph.ForcePass(0)
+    for (pos, p), g in zip(boxes, got):
+        assert np.array_equal(g, one.run(pos, p, precision=ph.FP32_SPLIT))
+
+
 def test_boxes_graph_and_stage_paths_agree(ph, ics, monkeypatch):
     boxes = _boxes(ics, nbox=4)
     a = ph.ForcePass(0).run_boxes(boxes, precision=ph.FP32_SPLIT)
