@@ -652,7 +652,7 @@ int ph_stage_p2p(photons_ctx *c, int precision, int zero)
         m.pool = c->w.p2p_pool;
         m.sorted = c->mu_sorted; m.nrecv = c->mu_nrecv; m.size = c->mu_size; m.rbase = c->mu_rbase;
         m.total = c->mu_total; m.scan_scratch = c->mu_scan; m.slot = c->mu_slot; m.over = c->mu_over;
-        m.ev = c->mu_ev; m.nev = c->mu_nev;
+        m.ev = c->mu_ev; m.nev = c->mu_nev; m.maxleaf = c->pp.maxleaf;
         m.buf = c->mu_buf; m.buf_cap = c->mu_buf_cap; m.cap_leaves = c->mu_cap_leaves;
         PH_TRY(ph::launch_p2p_mutual(a, m, st));
     } else {

@@ -721,9 +721,6 @@ __global__ void k_leaf_offsets(const double *px, const double *py, const double 
 // ---------------------------------------------------------------------
 #define MU_TB 128
 #define MU_WARPS (MU_TB / 32)
-#ifndef MU_MINB
-#define MU_MINB 3  // resident blocks of MU_TB per SM the mutual kernel is compiled for (158 registers)
-#endif
 #ifndef MU_UNROLL
 #define MU_UNROLL 1
 #endif
@@ -732,9 +729,15 @@ constexpr int kMuUnroll = MU_UNROLL;
 #define MU_FLUSH 4  // evaluated entries per compensated flush of the partial sums
 #endif
 #define MU_SORT_MAX 1024  // longer lists stay unsorted and are evaluated one way
-#ifndef MU_IL
-#define MU_IL 2  // target pairs evaluated stage by stage together (1, 2 or 4)
-#endif
+// Two builds of the kernel, chosen by MAXLEAF: for leaves of up to 64
+// (mostly 8 targets per lane) 3 resident blocks per SM (158 registers) with
+// two target pairs evaluated stage by stage together; below 60, 4 blocks
+// (126 registers) and one pair at a time (256^3: 65.3 vs 66.4 ms at leaf 64,
+// 55.5 vs 59.6 ms at leaf 48)
+#define MU_WIDE_MINB 3
+#define MU_WIDE_IL 2
+#define MU_NARROW_MINB 4
+#define MU_NARROW_IL 1
 #ifndef MU_BATCH
 #define MU_BATCH 32  // sources per reaction reduction (32 or 16)
 #endif
@@ -888,7 +891,7 @@ __device__ __forceinline__ void mu_place(const MuEntry &E, float4 *buf, float si
 // shared memory, then the warp walks the batch with the next entry's
 // sources in flight (cp.async into the second stage) while it evaluates
 // the current one.
-template <int T>
+template <int T, int ILR>
 __device__ __forceinline__ void mu_target(const P2PArgs &A, const int2 *ev, int ne, const long long *rbase,
                                           float *rbuf, int t, int nt, int it, const SplitConsts &K, float Lhi,
                                           float Llo, float4 *src, MuEntry *meta, float *red, float *accw, int lane)
@@ -959,34 +962,34 @@ __device__ __forceinline__ void mu_target(const P2PArgs &A, const int2 *ev, int 
                     const float4 S = stage[c0 + 4 * r + sg];
                     const float2 sx = f2(S.x), sy = f2(S.y), sz = f2(S.z);
                     float2 rx = f2(0.f), ry = f2(0.f), rz = f2(0.f);
-#if MU_IL > 1
                     // never more chains than this lane's TP target pairs
-                    constexpr int IL = MU_IL < TP ? MU_IL : TP;
+                    constexpr int IL = ILR < TP ? ILR : TP;
                     static_assert(TP % IL == 0, "target pairs in whole interleave groups");
+                    if constexpr (IL > 1) {
 #pragma unroll
-                    for (int p = 0; p < TP; p += IL)
-                        mu_pairs<IL>(sx, sy, sz, nx + p, ny + p, nz + p, ax + p, ay + p, az + p, rx, ry, rz, owned, K,
-                                     pia2, one2, c2, a0, a1, a2, a3, a4, a5);
-#else
+                        for (int p = 0; p < TP; p += IL)
+                            mu_pairs<IL>(sx, sy, sz, nx + p, ny + p, nz + p, ax + p, ay + p, az + p, rx, ry, rz,
+                                         owned, K, pia2, one2, c2, a0, a1, a2, a3, a4, a5);
+                    } else {
 #pragma unroll
-                    for (int p = 0; p < TP; p++) {
-                        const float2 dx = __fadd2_rn(sx, nx[p]);
-                        const float2 dy = __fadd2_rn(sy, ny[p]);
-                        const float2 dz = __fadd2_rn(sz, nz[p]);
-                        float2 qq = __fmul2_rn(dx, dx);
-                        qq = __ffma2_rn(dy, dy, qq);
-                        qq = __ffma2_rn(dz, dz, qq);
-                        const float2 f = pair_factor(qq, K, pia2, one2, c2, a0, a1, a2, a3, a4, a5);
-                        ax[p] = __ffma2_rn(dx, f, ax[p]);
-                        ay[p] = __ffma2_rn(dy, f, ay[p]);
-                        az[p] = __ffma2_rn(dz, f, az[p]);
-                        if (owned) {
-                            rx = __ffma2_rn(dx, f, rx);
-                            ry = __ffma2_rn(dy, f, ry);
-                            rz = __ffma2_rn(dz, f, rz);
+                        for (int p = 0; p < TP; p++) {
+                            const float2 dx = __fadd2_rn(sx, nx[p]);
+                            const float2 dy = __fadd2_rn(sy, ny[p]);
+                            const float2 dz = __fadd2_rn(sz, nz[p]);
+                            float2 qq = __fmul2_rn(dx, dx);
+                            qq = __ffma2_rn(dy, dy, qq);
+                            qq = __ffma2_rn(dz, dz, qq);
+                            const float2 f = pair_factor(qq, K, pia2, one2, c2, a0, a1, a2, a3, a4, a5);
+                            ax[p] = __ffma2_rn(dx, f, ax[p]);
+                            ay[p] = __ffma2_rn(dy, f, ay[p]);
+                            az[p] = __ffma2_rn(dz, f, az[p]);
+                            if (owned) {
+                                rx = __ffma2_rn(dx, f, rx);
+                                ry = __ffma2_rn(dy, f, ry);
+                                rz = __ffma2_rn(dz, f, rz);
+                            }
                         }
                     }
-#endif
                     if (owned) {
                         float *rr = red + (4 * r + sg) * 24 + tg;
                         rr[0] = rx.x + rx.y;
@@ -1058,8 +1061,9 @@ __device__ __forceinline__ void mu_target(const P2PArgs &A, const int2 *ev, int 
     __syncwarp();
 }
 
-__global__ void __launch_bounds__(MU_TB, MU_MINB) k_p2p_mutual(P2PArgs A, const int2 *ev, const int *nev,
-                                                               const long long *rbase, float *rbuf)
+template <int MINB, int ILR>
+__global__ void __launch_bounds__(MU_TB, MINB) k_p2p_mutual(P2PArgs A, const int2 *ev, const int *nev,
+                                                            const long long *rbase, float *rbuf)
 {
     // shared layouts avoid bank conflicts: a batch's source k (of 32) is
     // read by source group k % 4, so the four groups read adjacent float4s;
@@ -1088,10 +1092,10 @@ __global__ void __launch_bounds__(MU_TB, MU_MINB) k_p2p_mutual(P2PArgs A, const 
         const int2 *evt = ev + A.p2p_off[t];
         const int ne = nev[t];
         if (nt > 32)
-            mu_target<8>(A, evt, ne, rbase, rbuf, t, nt, it, K, B.Lhi, B.Llo, s_src[wib], s_meta[wib], s_red[wib],
+            mu_target<8, ILR>(A, evt, ne, rbase, rbuf, t, nt, it, K, B.Lhi, B.Llo, s_src[wib], s_meta[wib], s_red[wib],
                          s_acc[wib], lane);
         else
-            mu_target<4>(A, evt, ne, rbase, rbuf, t, nt, it, K, B.Lhi, B.Llo, s_src[wib], s_meta[wib], s_red[wib],
+            mu_target<4, ILR>(A, evt, ne, rbase, rbuf, t, nt, it, K, B.Lhi, B.Llo, s_src[wib], s_meta[wib], s_red[wib],
                          s_acc[wib], lane);
     }
 }
@@ -1195,7 +1199,12 @@ int launch_p2p_mutual(const P2PArgs &a, const MutualBufs &m, cudaStream_t st)
     ph::note_launch(), k_mu_slots<<<sms * 8, 256, 0, st>>>(a.tree_cnt, a.walk_flags, m.pool, a.p2p_off, a.p2p_cnt,
                                                             m.sorted, m.total, m.buf_cap, m.slot, m.ev, m.nev,
                                                             m.over);
-    ph::note_launch(), k_p2p_mutual<<<sms * MU_MINB, MU_TB, 0, st>>>(a, m.ev, m.nev, m.rbase, m.buf);
+    if (m.maxleaf >= 60)
+        ph::note_launch(), k_p2p_mutual<MU_WIDE_MINB, MU_WIDE_IL>
+            <<<sms * MU_WIDE_MINB, MU_TB, 0, st>>>(a, m.ev, m.nev, m.rbase, m.buf);
+    else
+        ph::note_launch(), k_p2p_mutual<MU_NARROW_MINB, MU_NARROW_IL>
+            <<<sms * MU_NARROW_MINB, MU_TB, 0, st>>>(a, m.ev, m.nev, m.rbase, m.buf);
     ph::note_launch(), k_mu_gather<<<sms * 8, 256, 0, st>>>(a, m.slot, m.nrecv, m.rbase, m.buf);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;

@@ -54,6 +54,7 @@ struct MutualBufs {
     int cap_leaves;
     int2 *ev;                // per pool offset: the entries a target evaluates, packed in list order
     int *nev;                // per leaf: their number
+    int maxleaf;             // selects the kernel build
 };
 
 SplitConsts make_split_consts(const PassParams &p);
