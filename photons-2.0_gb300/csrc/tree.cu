@@ -127,25 +127,38 @@ __global__ void k_chunk_sum(BuildBufs b, int D)
     }
 }
 
+// Node means.  A node of one chunk (most nodes of the deep levels) takes
+// one thread: 0.0 + its chunk sum, the value the warp reduction below gives
+// for a single nonzero term.  Larger nodes take a warp each: lane-strided
+// sums of the chunk sums, then the warp reduction (fixed order).
 __global__ void k_node_mean(BuildBufs b, int D)
 {
     const int lb = b.cnt[BC_LEVEL_BEGIN], C = b.cnt[BC_LEVEL_COUNT];
     const double *coord = axis_ptr(b.x, b.y, b.z, D);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
+        if (b.tn_nch[i] != 1) continue;
+        const int t = lb + i;
+        const int len = b.tn_len[t];
+        if (len == 2) {
+            const int start = b.tn_start[t];
+            b.tn_split[t] = 0.5 * (coord[start] + coord[start + 1]);
+        } else {
+            double s = 0.0;
+            s += b.ch_partial[b.tn_chunk_base[i]];
+            b.tn_split[t] = s / (double)len;
+        }
+    }
     int lane = warp_lane();
     int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
     for (int i = gw; i < C; i += nw) {
-        int t = lb + i;
-        int len = b.tn_len[t];
-        if (len == 2) {
-            int start = b.tn_start[t];
-            if (lane == 0) b.tn_split[t] = 0.5 * (coord[start] + coord[start + 1]);
-            continue;
-        }
-        int c0 = b.tn_chunk_base[i], nc = b.tn_nch[i];
+        const int nc = b.tn_nch[i];
+        if (nc == 1) continue;
+        const int t = lb + i;
+        const int c0 = b.tn_chunk_base[i];
         double s = 0.0;
         for (int k = lane; k < nc; k += 32) s += b.ch_partial[c0 + k];
         s = warp_sum_d(s);
-        if (lane == 0) b.tn_split[t] = s / (double)len;
+        if (lane == 0) b.tn_split[t] = s / (double)b.tn_len[t];
     }
 }
 
@@ -170,39 +183,56 @@ __global__ void k_chunk_count(BuildBufs b, int D)
     }
 }
 
-// per node: prefix of chunk counts, partition sizes, child kinds
+// per node: the child kinds and sizes from the count of particles not above
+// the mean
+__device__ __forceinline__ void node_split_finish(BuildBufs &b, int i, int t, int len, int S, int maxleaf)
+{
+    int mode, left;
+    if (len == 2) { mode = 2; left = 1; }
+    else if (S == len) { mode = 1; left = len - 1; }
+    else { mode = 0; left = S; }
+    b.tn_S[t] = S;
+    b.tn_mode[t] = mode;
+    int right = len - left;
+    // child sizes are stashed in child codes until the children exist
+    b.tn_child0[t] = left;
+    b.tn_child1[t] = right;
+    b.tn_nodeflag[i] = (left > maxleaf) + (right > maxleaf);
+    b.tn_leafflag[i] = (left <= maxleaf) + (right <= maxleaf);
+}
+
+// per node: prefix of chunk counts, partition sizes, child kinds.  A node
+// of one chunk takes one thread; a larger node a warp, each lane summing a
+// contiguous block of chunk counts (the prefix is exact integer
+// arithmetic, so the blocking does not change it).
 __global__ void k_node_split(BuildBufs b, int maxleaf)
 {
     const int lb = b.cnt[BC_LEVEL_BEGIN], C = b.cnt[BC_LEVEL_COUNT];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
+        if (b.tn_nch[i] != 1) continue;
+        const int t = lb + i, c0 = b.tn_chunk_base[i];
+        b.ch_small_base[c0] = 0;
+        node_split_finish(b, i, t, b.tn_len[t], b.ch_cnt[c0], maxleaf);
+    }
     int lane = warp_lane();
     int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
     for (int i = gw; i < C; i += nw) {
-        int t = lb + i;
-        int len = b.tn_len[t];
-        int c0 = b.tn_chunk_base[i], nc = b.tn_nch[i];
-        int carry = 0;
-        for (int k0 = 0; k0 < nc; k0 += 32) {
-            int k = k0 + lane;
-            int v = (k < nc) ? b.ch_cnt[c0 + k] : 0;
-            int incl = warp_incl_scan(v);
-            if (k < nc) b.ch_small_base[c0 + k] = carry + incl - v;
-            carry += shfl(incl, 31);
+        const int nc = b.tn_nch[i];
+        if (nc == 1) continue;
+        const int t = lb + i, c0 = b.tn_chunk_base[i];
+        const int per = (nc + 31) / 32;
+        const int kb = min(nc, lane * per), ke = min(nc, kb + per);
+        int own = 0;
+#pragma unroll 8
+        for (int k = kb; k < ke; k++) own += b.ch_cnt[c0 + k];
+        const int incl = warp_incl_scan(own);
+        int run = incl - own;
+        for (int k = kb; k < ke; k++) {
+            b.ch_small_base[c0 + k] = run;
+            run += b.ch_cnt[c0 + k];
         }
-        if (lane == 0) {
-            int S = carry;
-            int mode, left;
-            if (len == 2) { mode = 2; left = 1; }
-            else if (S == len) { mode = 1; left = len - 1; }
-            else { mode = 0; left = S; }
-            b.tn_S[t] = S;
-            b.tn_mode[t] = mode;
-            int right = len - left;
-            // child sizes are stashed in child codes until the children exist
-            b.tn_child0[t] = left;
-            b.tn_child1[t] = right;
-            b.tn_nodeflag[i] = (left > maxleaf) + (right > maxleaf);
-            b.tn_leafflag[i] = (left <= maxleaf) + (right <= maxleaf);
-        }
+        const int S = shfl(incl, 31);
+        if (lane == 0) node_split_finish(b, i, t, b.tn_len[t], S, maxleaf);
     }
 }
 
