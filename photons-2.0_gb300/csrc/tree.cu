@@ -3,7 +3,9 @@
 // Restates src/fmm.c:30-264 (bksort_inplace, build_kdtree, center_kdtree,
 // build_localtree) as a level-synchronous build: every node of one depth
 // is split in the same set of launches.  Per level:
-//   1. each node's particle range is cut into chunks of CHUNK particles;
+//   1. each node's particle range is cut into chunks of CHUNK particles
+//      (a node of at most one chunk is split by one warp in k_narrow_split,
+//      which does steps 2-3 for it in one kernel);
 //   2. chunk sums of the split coordinate (axis = depth mod 3) and a
 //      fixed-order reduction give the node's mean;
 //   3. the reference's two-ended swap partition (src/fmm.c:58-72) is
@@ -91,8 +93,10 @@ __global__ void k_init_particles(const double *__restrict__ pos, int n, BuildBuf
 __global__ void k_level_nch(BuildBufs b)
 {
     const int lb = b.cnt[BC_LEVEL_BEGIN], C = b.cnt[BC_LEVEL_COUNT];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x)
-        b.tn_nch[i] = (b.tn_len[lb + i] + CHUNK - 1) / CHUNK;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
+        const int len = b.tn_len[lb + i];
+        b.tn_nch[i] = len <= CHUNK ? 0 : (len + CHUNK - 1) / CHUNK;  // one chunk or less: k_narrow_split
+    }
 }
 
 // chunk -> level-local node index, written once per level
@@ -127,32 +131,16 @@ __global__ void k_chunk_sum(BuildBufs b, int D)
     }
 }
 
-// Node means.  A node of one chunk (most nodes of the deep levels) takes
-// one thread: 0.0 + its chunk sum, the value the warp reduction below gives
-// for a single nonzero term.  Larger nodes take a warp each: lane-strided
-// sums of the chunk sums, then the warp reduction (fixed order).
+// Node means of the nodes of more than one chunk, a warp each:
+// lane-strided sums of the chunk sums, then the warp reduction (fixed order)
 __global__ void k_node_mean(BuildBufs b, int D)
 {
     const int lb = b.cnt[BC_LEVEL_BEGIN], C = b.cnt[BC_LEVEL_COUNT];
-    const double *coord = axis_ptr(b.x, b.y, b.z, D);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
-        if (b.tn_nch[i] != 1) continue;
-        const int t = lb + i;
-        const int len = b.tn_len[t];
-        if (len == 2) {
-            const int start = b.tn_start[t];
-            b.tn_split[t] = 0.5 * (coord[start] + coord[start + 1]);
-        } else {
-            double s = 0.0;
-            s += b.ch_partial[b.tn_chunk_base[i]];
-            b.tn_split[t] = s / (double)len;
-        }
-    }
     int lane = warp_lane();
     int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
     for (int i = gw; i < C; i += nw) {
         const int nc = b.tn_nch[i];
-        if (nc == 1) continue;
+        if (nc == 0) continue;
         const int t = lb + i;
         const int c0 = b.tn_chunk_base[i];
         double s = 0.0;
@@ -201,24 +189,18 @@ __device__ __forceinline__ void node_split_finish(BuildBufs &b, int i, int t, in
     b.tn_leafflag[i] = (left <= maxleaf) + (right <= maxleaf);
 }
 
-// per node: prefix of chunk counts, partition sizes, child kinds.  A node
-// of one chunk takes one thread; a larger node a warp, each lane summing a
-// contiguous block of chunk counts (the prefix is exact integer
-// arithmetic, so the blocking does not change it).
+// per node of more than one chunk, a warp each: prefix of chunk counts,
+// partition sizes, child kinds.  Each lane sums a contiguous block of chunk
+// counts (the prefix is exact integer arithmetic, so the blocking does not
+// change it).
 __global__ void k_node_split(BuildBufs b, int maxleaf)
 {
     const int lb = b.cnt[BC_LEVEL_BEGIN], C = b.cnt[BC_LEVEL_COUNT];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
-        if (b.tn_nch[i] != 1) continue;
-        const int t = lb + i, c0 = b.tn_chunk_base[i];
-        b.ch_small_base[c0] = 0;
-        node_split_finish(b, i, t, b.tn_len[t], b.ch_cnt[c0], maxleaf);
-    }
     int lane = warp_lane();
     int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
     for (int i = gw; i < C; i += nw) {
         const int nc = b.tn_nch[i];
-        if (nc == 1) continue;
+        if (nc == 0) continue;
         const int t = lb + i, c0 = b.tn_chunk_base[i];
         const int per = (nc + 31) / 32;
         const int kb = min(nc, lane * per), ke = min(nc, kb + per);
@@ -385,6 +367,69 @@ __device__ __forceinline__ void swap_particles(BuildBufs &b, int i, int j)
     t = b.y[i]; b.y[i] = b.y[j]; b.y[j] = t;
     t = b.z[i]; b.z[i] = b.z[j]; b.z[j] = t;
     int q = b.perm[i]; b.perm[i] = b.perm[j]; b.perm[j] = q;
+}
+
+// Nodes of at most one chunk, a warp each, in one kernel while the node's
+// data is in cache: the sum, mean, count, child kinds, ranks and swaps that
+// k_chunk_sum, k_node_mean, k_chunk_count, k_node_split, k_rank and k_swap
+// give a node of one chunk, with the same lane order and reductions (the
+// chunk sum is lane 0's butterfly result; the mean adds it to 0.0 first, as
+// the one-term reduction of k_node_mean does).
+__global__ void k_narrow_split(BuildBufs b, int D, int maxleaf)
+{
+    const int lb = b.cnt[BC_LEVEL_BEGIN], C = b.cnt[BC_LEVEL_COUNT];
+    const double *coord = axis_ptr(b.x, b.y, b.z, D);
+    const int lane = warp_lane();
+    const unsigned lt = (1u << lane) - 1u;
+    int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = gw; i < C; i += nw) {
+        if (b.tn_nch[i] != 0) continue;
+        const int t = lb + i;
+        const int start = b.tn_start[t], len = b.tn_len[t];
+        const double *cd = coord + start;
+        double mean;
+        if (len == 2) {
+            mean = 0.5 * (cd[0] + cd[1]);
+        } else {
+            double s = 0.0;
+            for (int k = lane; k < len; k += 32) s += cd[k];
+            s = __shfl_sync(0xffffffffu, warp_sum_d(s), 0);
+            double m = 0.0;
+            m += s;
+            mean = m / (double)len;
+        }
+        int c = 0;
+        for (int k = lane; k < len; k += 32) c += !(cd[k] > mean);
+        const int S = __reduce_add_sync(0xffffffffu, c);
+        if (lane == 0) {
+            b.tn_split[t] = mean;
+            node_split_finish(b, i, t, len, S, maxleaf);
+        }
+        if (len == 2) {
+            if (lane == 0 && cd[0] > cd[1]) swap_particles(b, start, start + 1);
+            continue;
+        }
+        if (S == len) continue;  // nothing above the mean: the last particle goes up, no swaps
+        int run = 0;
+        for (int k0 = 0; k0 < len; k0 += 32) {
+            const int p = k0 + lane;
+            const bool in = p < len;
+            const bool small = in && !(cd[p] > mean);
+            const unsigned m = __ballot_sync(0xffffffffu, small);
+            const int r = run + __popc(m & lt);
+            if (in) {
+                if (p < S) b.bigslot[start + p] = small ? -1 : (p - r);
+                else if (small) b.smallpos[start + (S - 1 - r)] = p;
+            }
+            run += __popc(m);
+        }
+        __syncwarp();
+        for (int p = lane; p < S; p += 32) {
+            const int k = b.bigslot[start + p];
+            if (k >= 0) swap_particles(b, start + p, start + b.smallpos[start + k]);
+        }
+        __syncwarp();
+    }
 }
 
 // Each pair is exchanged by the thread of its left-region member only, so
@@ -575,6 +620,7 @@ int build_tree(BuildBufs &b, TreeBufs &T, const PassParams &p, int levels, cudaS
     for (int d = 0; d < levels; d++) {
         const int D = d % 3;  // direct_local_start = 0 at one rank; axis cycles (src/fmm.c:99)
         ph::note_launch(), k_level_nch<<<maxb, TB, 0, st>>>(b);
+        ph::note_launch(), k_narrow_split<<<maxb, TB, 0, st>>>(b, D, p.maxleaf);
         scan_exclusive_i32(b.tn_nch, b.tn_chunk_base, b.cnt + BC_LEVEL_COUNT, b.cap_nodes, b.cnt + BC_W,
                            b.scan_scratch, b.scan_scratch_elems, st);
         ph::note_launch(), k_chunk_map<<<maxb, TB, 0, st>>>(b);
