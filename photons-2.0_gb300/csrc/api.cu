@@ -273,12 +273,18 @@ static bool mutual_feedback(photons_ctx *c, int over, long long need)
     return true;
 }
 
-// mutual pairs pay off from leaf size 48 (256^3: 71 vs 91 ms at leaf 64, a
-// tie at 32); below that the per-entry work outweighs the halved pairs
+// Mutual pairs from leaf size 48.  At leaf 32 they win on near-uniform
+// input (256^3 Zel'dovich: 55 vs 69 ms) but lose on halos (128^3 NFW: 47 vs
+// 30 ms: leaves of 22 particles fill 32 target slots, and 65 % of the
+// entries sit in lists longer than the sort handles, evaluated one way);
+// below 32 they lose everywhere
+#ifndef MU_MIN_LEAF
+#define MU_MIN_LEAF 48
+#endif
 static bool uses_mutual(const photons_ctx *c, int precision)
 {
-    return precision != PHOTONS_FP64 && p2p_variant() == 2 && c->pp.maxleaf >= 48 && c->pp.maxleaf <= 64 &&
-           !c->mu_off;
+    return precision != PHOTONS_FP64 && p2p_variant() == 2 && c->pp.maxleaf >= MU_MIN_LEAF &&
+           c->pp.maxleaf <= 64 && !c->mu_off;
 }
 
 // buffers of the mutual kernel, only for passes that run it: per-entry
