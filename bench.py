@@ -34,7 +34,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "particle-forces/s at 256^3 clustered: FP32-split vs FP64 GPU at rel err <=1e-4"
 UNIT = "particle-forces/s"
-FLOPS_PER_PAIR = 36  # fixed work unit per pair interaction
+# fixed work unit per pair interaction of the reference's pair set (the
+# conventional count for a softened, erfc-truncated pair force); the P2P
+# roofline is this times the pairs, over the P2P phase time
+FLOPS_PER_PAIR = 36
 
 
 def parse():
@@ -62,6 +65,29 @@ def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def max_over_ranks(ms, dist, device="cpu"):
+    """The slowest rank's time: a step of the whole job ends when every
+    rank's step has ended (replicas: each rank runs its own box)."""
+    if not dist:
+        return ms
+    import torch
+
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def broadcast_from_rank0(v, dist, device="cpu"):
+    """Rank 0's integer on every rank (the leaf size all replicas run)."""
+    if not dist:
+        return v
+    import torch
+
+    t = torch.tensor([int(v)], dtype=torch.int64, device=device)
+    dist.broadcast(t, 0)
+    return int(t.item())
 
 
 def workload(nside, maxleaf, seed_offset=0, name="zeldovich256"):
@@ -426,6 +452,7 @@ def main():
     tune = None
     if not args.maxleaf:
         best, table = ph.autotune_leaf(fp, pos, p, error_bound=args.error_bound)
+        best = broadcast_from_rank0(best, dist, "cuda")  # every replica runs rank 0's choice
         p["maxleaf"] = best
         tune = {"chosen_maxleaf": best, "error_bound_median": args.error_bound, "candidates": table,
                 "score": "fastest pass with median error vs the FP64 direct sum <= bound (2000-particle sample)"}
@@ -464,11 +491,7 @@ def main():
         dist.barrier()
     launches = ph.load_library().photons_launch_count() - launches0
     clocks = sampler.stop() if sampler else None
-    ms = e0.elapsed_time(e1) / args.steps
-    if dist:
-        tt = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, dist, "cuda")
     counters = fp.counters()
     pairs = counters["pairs_local"] + counters["pairs_image"]
     value = n * world / (ms * 1e-3)
@@ -479,6 +502,9 @@ def main():
     hp, ha = hpos.numpy(), hacc.numpy()
     fp.run(hp, p, precision=ph.FP32_SPLIT, out=ha)
     torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
     e0.record(stream)
     t0 = time.time()
     esteps = max(1, min(args.steps, 5))
@@ -486,7 +512,9 @@ def main():
         fp.run(hp, p, precision=ph.FP32_SPLIT, out=ha)
     e1.record(stream)
     torch.cuda.synchronize()
-    e2e_ms = max(e0.elapsed_time(e1), (time.time() - t0) * 1e3) / esteps
+    if dist:
+        dist.barrier()
+    e2e_ms = max_over_ranks(max(e0.elapsed_time(e1), (time.time() - t0) * 1e3) / esteps, dist, "cuda")
     acc32 = ha.copy()
 
     if rank != 0:
@@ -563,8 +591,8 @@ def main():
                      "evaluated_frac": FLOPS_PER_PAIR * evaluated / (t_p2p * 1e-3) / 1e12 / peak,
                      "p2p_ms": t_p2p},
         "cpu_baseline": cpu,
-        "e2e": {"value": n / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": n * 24,
-                "d2h_bytes_per_step": n * 24, "ms_per_step": e2e_ms},
+        "e2e": {"value": n * world / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": n * 24 * world,
+                "d2h_bytes_per_step": n * 24 * world, "ms_per_step": e2e_ms},
         "gpu_launches": int(launches),
         "clocks": clocks,
         "phases_ms": tmean,
