@@ -64,6 +64,8 @@ struct photons_ctx {
     // PM mesh (pm.cu): density / potential, half spectrum, gradient grids, FFT plans
     int pm_n = 0, pm_cap_io = 0;
     double *pm_rho = nullptr, *pm_grad = nullptr, *pm_io = nullptr;
+    double *pm_green = nullptr;                        // Green's function of the half spectrum
+    double pm_green_pref = 0.0, pm_green_ismth2 = 0.0;  // the constants it was computed for
     cufftDoubleComplex *pm_rk = nullptr;
     cufftHandle pm_plan_r2c = 0, pm_plan_c2r = 0;
     int cap_n = 0, cap_u = 0;

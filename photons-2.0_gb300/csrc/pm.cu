@@ -92,8 +92,9 @@ __device__ __forceinline__ double pm_sinc(int q, int N)
     return __ddiv_rn(sin(f), f);
 }
 
-// the half spectrum [N][N][N/2+1] times the Green's function
-__global__ void k_pm_green(cufftDoubleComplex *rk, int N, double pref, double ismth2)
+// the Green's function on the half spectrum [N][N][N/2+1]; it depends only
+// on the mesh size, L and rs, so a context computes it once per set
+__global__ void k_pm_green_table(double *G, int N, double pref, double ismth2)
 {
     const int nz = N / 2 + 1, nhalf = N / 2;
     const size_t m = (size_t)N * N * nz;
@@ -113,6 +114,15 @@ __global__ void k_pm_green(cufftDoubleComplex *rk, int N, double pref, double is
             gf = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(gf, ff), ff), ff), ff);
             gf = __ddiv_rn(gf, k2);
         }
+        G[t] = gf;
+    }
+}
+
+// the half spectrum times the Green's function
+__global__ void k_pm_green(cufftDoubleComplex *rk, const double *__restrict__ G, size_t m)
+{
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < m; t += (size_t)gridDim.x * blockDim.x) {
+        const double gf = G[t];
         rk[t].x = __dmul_rn(rk[t].x, gf);
         rk[t].y = __dmul_rn(rk[t].y, gf);
     }
@@ -120,45 +130,57 @@ __global__ void k_pm_green(cufftDoubleComplex *rk, int N, double pref, double is
 
 // 4-point derivative along each axis (src/partmesh.c:524-531):
 // f1 invx (psi+1 - psi-1) - f2 invx (psi+2 - psi-2), f1 = 4/3, f2 = 1/6, invx = N / (2 L)
-__global__ void k_pm_gradient(const double *__restrict__ psi, int N, double invx, double *gx, double *gy, double *gz)
+// (x, y, z, 0) per cell, one 32-byte record, so that the interpolation's
+// eight corners are eight sector loads
+__global__ void k_pm_gradient(const double *__restrict__ psi, int N, double invx, double4 *g4)
 {
     const double f1 = 4.0 / 3.0, f2 = 1.0 / 6.0;
     const double c1 = __dmul_rn(f1, invx), c2 = __dmul_rn(f2, invx);
     const size_t m = (size_t)N * N * N;
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < m; t += (size_t)gridDim.x * blockDim.x) {
         const int i = (int)(t / ((size_t)N * N)), j = (int)((t / N) % N), k = (int)(t % N);
-        double d;
+        double d, gx, gy, gz;
         d = __dmul_rn(c1, __dsub_rn(psi[cell(wrap(i + 1, N), j, k, N)], psi[cell(wrap(i - 1, N), j, k, N)]));
-        gx[t] = __dsub_rn(d, __dmul_rn(c2, __dsub_rn(psi[cell(wrap(i + 2, N), j, k, N)], psi[cell(wrap(i - 2, N), j, k, N)])));
+        gx = __dsub_rn(d, __dmul_rn(c2, __dsub_rn(psi[cell(wrap(i + 2, N), j, k, N)], psi[cell(wrap(i - 2, N), j, k, N)])));
         d = __dmul_rn(c1, __dsub_rn(psi[cell(i, wrap(j + 1, N), k, N)], psi[cell(i, wrap(j - 1, N), k, N)]));
-        gy[t] = __dsub_rn(d, __dmul_rn(c2, __dsub_rn(psi[cell(i, wrap(j + 2, N), k, N)], psi[cell(i, wrap(j - 2, N), k, N)])));
+        gy = __dsub_rn(d, __dmul_rn(c2, __dsub_rn(psi[cell(i, wrap(j + 2, N), k, N)], psi[cell(i, wrap(j - 2, N), k, N)])));
         d = __dmul_rn(c1, __dsub_rn(psi[cell(i, j, wrap(k + 1, N), N)], psi[cell(i, j, wrap(k - 1, N), N)]));
-        gz[t] = __dsub_rn(d, __dmul_rn(c2, __dsub_rn(psi[cell(i, j, wrap(k + 2, N), N)], psi[cell(i, j, wrap(k - 2, N), N)])));
+        gz = __dsub_rn(d, __dmul_rn(c2, __dsub_rn(psi[cell(i, j, wrap(k + 2, N), N)], psi[cell(i, j, wrap(k - 2, N), N)])));
+        g4[t] = make_double4(gx, gy, gz, 0.0);
     }
 }
 
-// sum of the eight weighted cell values, in the reference's order
-__device__ __forceinline__ double interp(const double *g, const Cic &s, int N)
+// one corner's weighted gradient added to the three running sums
+__device__ __forceinline__ void corner(double3 &a, double w, const double4 &g, bool first)
 {
-    double a = __dmul_rn(w3(s.win, s.wjn, s.wkn), g[cell(s.i, s.j, s.k, N)]);
-    a = __dadd_rn(a, __dmul_rn(w3(s.wi, s.wjn, s.wkn), g[cell(s.ii, s.j, s.k, N)]));
-    a = __dadd_rn(a, __dmul_rn(w3(s.win, s.wj, s.wkn), g[cell(s.i, s.jj, s.k, N)]));
-    a = __dadd_rn(a, __dmul_rn(w3(s.wi, s.wj, s.wkn), g[cell(s.ii, s.jj, s.k, N)]));
-    a = __dadd_rn(a, __dmul_rn(w3(s.win, s.wjn, s.wk), g[cell(s.i, s.j, s.kk, N)]));
-    a = __dadd_rn(a, __dmul_rn(w3(s.wi, s.wjn, s.wk), g[cell(s.ii, s.j, s.kk, N)]));
-    a = __dadd_rn(a, __dmul_rn(w3(s.win, s.wj, s.wk), g[cell(s.i, s.jj, s.kk, N)]));
-    a = __dadd_rn(a, __dmul_rn(w3(s.wi, s.wj, s.wk), g[cell(s.ii, s.jj, s.kk, N)]));
-    return a;
+    if (first) {
+        a = make_double3(__dmul_rn(w, g.x), __dmul_rn(w, g.y), __dmul_rn(w, g.z));
+    } else {
+        a.x = __dadd_rn(a.x, __dmul_rn(w, g.x));
+        a.y = __dadd_rn(a.y, __dmul_rn(w, g.y));
+        a.z = __dadd_rn(a.z, __dmul_rn(w, g.z));
+    }
 }
 
+// the eight weighted cell values summed in the reference's order, for the
+// three components at once
 __global__ void k_pm_interp(const double *__restrict__ pos, int n, int N, double norm, double delta,
-                            const double *gx, const double *gy, const double *gz, double *acc)
+                            const double4 *__restrict__ g4, double *acc)
 {
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         const Cic s = cic(pos, p, norm, delta, N);
-        acc[3 * (size_t)p] = interp(gx, s, N);
-        acc[3 * (size_t)p + 1] = interp(gy, s, N);
-        acc[3 * (size_t)p + 2] = interp(gz, s, N);
+        double3 a;
+        corner(a, w3(s.win, s.wjn, s.wkn), g4[cell(s.i, s.j, s.k, N)], true);
+        corner(a, w3(s.wi, s.wjn, s.wkn), g4[cell(s.ii, s.j, s.k, N)], false);
+        corner(a, w3(s.win, s.wj, s.wkn), g4[cell(s.i, s.jj, s.k, N)], false);
+        corner(a, w3(s.wi, s.wj, s.wkn), g4[cell(s.ii, s.jj, s.k, N)], false);
+        corner(a, w3(s.win, s.wjn, s.wk), g4[cell(s.i, s.j, s.kk, N)], false);
+        corner(a, w3(s.wi, s.wjn, s.wk), g4[cell(s.ii, s.j, s.kk, N)], false);
+        corner(a, w3(s.win, s.wj, s.wk), g4[cell(s.i, s.jj, s.kk, N)], false);
+        corner(a, w3(s.wi, s.wj, s.wk), g4[cell(s.ii, s.jj, s.kk, N)], false);
+        acc[3 * (size_t)p] = a.x;
+        acc[3 * (size_t)p + 1] = a.y;
+        acc[3 * (size_t)p + 2] = a.z;
     }
 }
 
@@ -176,13 +198,15 @@ int ph_pm_prepare(photons_ctx *c, int N)
     if (c->pm_plan_r2c) cufftDestroy(c->pm_plan_r2c);
     if (c->pm_plan_c2r) cufftDestroy(c->pm_plan_c2r);
     c->pm_plan_r2c = c->pm_plan_c2r = 0;
-    cudaFree(c->pm_rho); cudaFree(c->pm_rk); cudaFree(c->pm_grad);
-    c->pm_rho = nullptr; c->pm_rk = nullptr; c->pm_grad = nullptr;
+    cudaFree(c->pm_rho); cudaFree(c->pm_rk); cudaFree(c->pm_grad); cudaFree(c->pm_green);
+    c->pm_rho = nullptr; c->pm_rk = nullptr; c->pm_grad = nullptr; c->pm_green = nullptr;
     c->pm_n = 0;
+    c->pm_green_pref = c->pm_green_ismth2 = 0.0;
     const size_t m = (size_t)N * N * N, mk = (size_t)N * N * (N / 2 + 1);
     cudaError_t e = cudaMalloc(&c->pm_rho, sizeof(double) * m);
     if (e == cudaSuccess) e = cudaMalloc(&c->pm_rk, sizeof(cufftDoubleComplex) * mk);
-    if (e == cudaSuccess) e = cudaMalloc(&c->pm_grad, 3 * sizeof(double) * m);
+    if (e == cudaSuccess) e = cudaMalloc(&c->pm_grad, 4 * sizeof(double) * m);
+    if (e == cudaSuccess) e = cudaMalloc(&c->pm_green, sizeof(double) * mk);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return ph_set_error(PH_ERR_NOMEM, "PM mesh of %d^3 cells does not fit", N);
@@ -199,10 +223,11 @@ void ph_pm_release(photons_ctx *c)
 {
     if (c->pm_plan_r2c) cufftDestroy(c->pm_plan_r2c);
     if (c->pm_plan_c2r) cufftDestroy(c->pm_plan_c2r);
-    cudaFree(c->pm_rho); cudaFree(c->pm_rk); cudaFree(c->pm_grad);
+    cudaFree(c->pm_rho); cudaFree(c->pm_rk); cudaFree(c->pm_grad); cudaFree(c->pm_green);
     c->pm_plan_r2c = c->pm_plan_c2r = 0;
-    c->pm_rho = nullptr; c->pm_rk = nullptr; c->pm_grad = nullptr;
+    c->pm_rho = nullptr; c->pm_rk = nullptr; c->pm_grad = nullptr; c->pm_green = nullptr;
     c->pm_n = 0;
+    c->pm_green_pref = c->pm_green_ismth2 = 0.0;
 }
 
 // enqueue the PM force on device positions pos[3n] into acc_pm[3n]
@@ -227,14 +252,18 @@ int ph_pm_enqueue(photons_ctx *c, const photons_params *p, int N, int n, const d
     double ismth2 = 2 * PM_PI * p->rs / L;
     ismth2 = ismth2 * ismth2;
     const double pref = L * L / (PM_PI * (double)N * (double)N * (double)N);
-    ph::note_launch(), k_pm_green<<<blocks, 256, 0, st>>>(c->pm_rk, N, pref, ismth2);
-    (void)mk;
+    if (c->pm_green_pref != pref || c->pm_green_ismth2 != ismth2) {
+        ph::note_launch(), k_pm_green_table<<<blocks, 256, 0, st>>>(c->pm_green, N, pref, ismth2);
+        c->pm_green_pref = pref;
+        c->pm_green_ismth2 = ismth2;
+    }
+    ph::note_launch(), k_pm_green<<<blocks, 256, 0, st>>>(c->pm_rk, c->pm_green, mk);
     r = cufftExecZ2D(c->pm_plan_c2r, c->pm_rk, c->pm_rho);
     if (r != CUFFT_SUCCESS) return cufft_error(r, "cufftExecZ2D");
     const double invx = 0.5 * N / L;  // src/partmesh.c:458
-    double *gx = c->pm_grad, *gy = gx + m, *gz = gy + m;
-    ph::note_launch(), k_pm_gradient<<<blocks, 256, 0, st>>>(c->pm_rho, N, invx, gx, gy, gz);
-    ph::note_launch(), k_pm_interp<<<blocks, 256, 0, st>>>(pos, n, N, norm, delta, gx, gy, gz, acc_pm);
+    double4 *g4 = reinterpret_cast<double4 *>(c->pm_grad);
+    ph::note_launch(), k_pm_gradient<<<blocks, 256, 0, st>>>(c->pm_rho, N, invx, g4);
+    ph::note_launch(), k_pm_interp<<<blocks, 256, 0, st>>>(pos, n, N, norm, delta, g4, acc_pm);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }
