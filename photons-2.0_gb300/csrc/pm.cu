@@ -10,8 +10,9 @@
 //   3. a 4-point finite-difference gradient of psi per mesh cell
 //      (src/partmesh.c:524-735) and its CIC interpolation to the particles:
 //      acc_pm = grad psi (src/partmesh.c:574-587).
-// The mesh arithmetic is FP64 with every product and sum rounded on its own,
-// in the reference's order; the constant pi is the reference's 3.1415926.
+// The mesh arithmetic is FP64 in the reference's order, every product and
+// sum rounded on its own except the interpolation sums (fused multiply-adds);
+// the constant pi is the reference's 3.1415926.
 // The deposit adds with FP64 atomics, so its summation order (and the last
 // bits of the density) varies from run to run.
 #include <cufft.h>
@@ -60,21 +61,24 @@ __device__ __forceinline__ Cic cic(const double *pos, int p, double norm, double
 
 __device__ __forceinline__ size_t cell(int i, int j, int k, int N) { return ((size_t)i * N + j) * N + k; }
 
-__device__ __forceinline__ double w3(double a, double b, double c) { return __dmul_rn(__dmul_rn(a, b), c); }
 
 __global__ void k_pm_deposit(const double *__restrict__ pos, int n, int N, double norm, double delta, double mass,
                              double *rho)
 {
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         const Cic s = cic(pos, p, norm, delta, N);
-        atomicAdd(rho + cell(s.i, s.j, s.k, N), __dmul_rn(w3(mass, s.win, s.wjn), s.wkn));
-        atomicAdd(rho + cell(s.ii, s.j, s.k, N), __dmul_rn(w3(mass, s.wi, s.wjn), s.wkn));
-        atomicAdd(rho + cell(s.i, s.jj, s.k, N), __dmul_rn(w3(mass, s.win, s.wj), s.wkn));
-        atomicAdd(rho + cell(s.i, s.j, s.kk, N), __dmul_rn(w3(mass, s.win, s.wjn), s.wk));
-        atomicAdd(rho + cell(s.ii, s.jj, s.k, N), __dmul_rn(w3(mass, s.wi, s.wj), s.wkn));
-        atomicAdd(rho + cell(s.ii, s.j, s.kk, N), __dmul_rn(w3(mass, s.wi, s.wjn), s.wk));
-        atomicAdd(rho + cell(s.i, s.jj, s.kk, N), __dmul_rn(w3(mass, s.win, s.wj), s.wk));
-        atomicAdd(rho + cell(s.ii, s.jj, s.kk, N), __dmul_rn(w3(mass, s.wi, s.wj), s.wk));
+        // ((m wx) wy) wz with the shared leading products formed once
+        const double mn = __dmul_rn(mass, s.win), mi = __dmul_rn(mass, s.wi);
+        const double nn = __dmul_rn(mn, s.wjn), in = __dmul_rn(mi, s.wjn);
+        const double nj = __dmul_rn(mn, s.wj), ij = __dmul_rn(mi, s.wj);
+        atomicAdd(rho + cell(s.i, s.j, s.k, N), __dmul_rn(nn, s.wkn));
+        atomicAdd(rho + cell(s.ii, s.j, s.k, N), __dmul_rn(in, s.wkn));
+        atomicAdd(rho + cell(s.i, s.jj, s.k, N), __dmul_rn(nj, s.wkn));
+        atomicAdd(rho + cell(s.i, s.j, s.kk, N), __dmul_rn(nn, s.wk));
+        atomicAdd(rho + cell(s.ii, s.jj, s.k, N), __dmul_rn(ij, s.wkn));
+        atomicAdd(rho + cell(s.ii, s.j, s.kk, N), __dmul_rn(in, s.wk));
+        atomicAdd(rho + cell(s.i, s.jj, s.kk, N), __dmul_rn(nj, s.wk));
+        atomicAdd(rho + cell(s.ii, s.jj, s.kk, N), __dmul_rn(ij, s.wk));
     }
 }
 
@@ -150,15 +154,17 @@ __global__ void k_pm_gradient(const double *__restrict__ psi, int N, double invx
     }
 }
 
-// one corner's weighted gradient added to the three running sums
+// one corner's weighted gradient added to the three running sums.  The
+// adds are fused multiply-adds (one rounding instead of two): the kernel is
+// bound by GB300's FP64 pipe, and this halves its work in the sums.
 __device__ __forceinline__ void corner(double3 &a, double w, const double4 &g, bool first)
 {
     if (first) {
         a = make_double3(__dmul_rn(w, g.x), __dmul_rn(w, g.y), __dmul_rn(w, g.z));
     } else {
-        a.x = __dadd_rn(a.x, __dmul_rn(w, g.x));
-        a.y = __dadd_rn(a.y, __dmul_rn(w, g.y));
-        a.z = __dadd_rn(a.z, __dmul_rn(w, g.z));
+        a.x = __fma_rn(w, g.x, a.x);
+        a.y = __fma_rn(w, g.y, a.y);
+        a.z = __fma_rn(w, g.z, a.z);
     }
 }
 
@@ -169,15 +175,18 @@ __global__ void k_pm_interp(const double *__restrict__ pos, int n, int N, double
 {
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         const Cic s = cic(pos, p, norm, delta, N);
+        // (wx wy) wz with the four leading products formed once
+        const double nn = __dmul_rn(s.win, s.wjn), in = __dmul_rn(s.wi, s.wjn);
+        const double nj = __dmul_rn(s.win, s.wj), ij = __dmul_rn(s.wi, s.wj);
         double3 a;
-        corner(a, w3(s.win, s.wjn, s.wkn), g4[cell(s.i, s.j, s.k, N)], true);
-        corner(a, w3(s.wi, s.wjn, s.wkn), g4[cell(s.ii, s.j, s.k, N)], false);
-        corner(a, w3(s.win, s.wj, s.wkn), g4[cell(s.i, s.jj, s.k, N)], false);
-        corner(a, w3(s.wi, s.wj, s.wkn), g4[cell(s.ii, s.jj, s.k, N)], false);
-        corner(a, w3(s.win, s.wjn, s.wk), g4[cell(s.i, s.j, s.kk, N)], false);
-        corner(a, w3(s.wi, s.wjn, s.wk), g4[cell(s.ii, s.j, s.kk, N)], false);
-        corner(a, w3(s.win, s.wj, s.wk), g4[cell(s.i, s.jj, s.kk, N)], false);
-        corner(a, w3(s.wi, s.wj, s.wk), g4[cell(s.ii, s.jj, s.kk, N)], false);
+        corner(a, __dmul_rn(nn, s.wkn), g4[cell(s.i, s.j, s.k, N)], true);
+        corner(a, __dmul_rn(in, s.wkn), g4[cell(s.ii, s.j, s.k, N)], false);
+        corner(a, __dmul_rn(nj, s.wkn), g4[cell(s.i, s.jj, s.k, N)], false);
+        corner(a, __dmul_rn(ij, s.wkn), g4[cell(s.ii, s.jj, s.k, N)], false);
+        corner(a, __dmul_rn(nn, s.wk), g4[cell(s.i, s.j, s.kk, N)], false);
+        corner(a, __dmul_rn(in, s.wk), g4[cell(s.ii, s.j, s.kk, N)], false);
+        corner(a, __dmul_rn(nj, s.wk), g4[cell(s.i, s.jj, s.kk, N)], false);
+        corner(a, __dmul_rn(ij, s.wk), g4[cell(s.ii, s.jj, s.kk, N)], false);
         acc[3 * (size_t)p] = a.x;
         acc[3 * (size_t)p + 1] = a.y;
         acc[3 * (size_t)p + 2] = a.z;
