@@ -207,7 +207,7 @@ def run_reference_arm(args):
     print(json.dumps(line))
 
 
-def kdk_measure(ph, fp, torch, stream, dpos, dacc, n, p, steps):
+def kdk_measure(ph, fp, torch, stream, dpos, dacc, n, p, steps, pflags=0):
     """Device-resident kick-drift-kick steps at a = 0.5 -> 0.505 (the
     reference's kick_loga / drift_loga factors, G = 43007.105732), and the
     kick and drift kernels alone against the measured HBM copy bandwidth."""
@@ -220,11 +220,13 @@ def kdk_measure(ph, fp, torch, stream, dpos, dacc, n, p, steps):
     vel = torch.zeros_like(pos)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    fp.kdk_step_device(pos.data_ptr(), vel.data_ptr(), acc.data_ptr(), n, p, dkh, dd, precision=ph.FP32_SPLIT)
+    fp.kdk_step_device(pos.data_ptr(), vel.data_ptr(), acc.data_ptr(), n, p, dkh, dd, precision=ph.FP32_SPLIT,
+                       flags=pflags)
     torch.cuda.synchronize()
     e0.record(stream)
     for _ in range(steps):
-        fp.kdk_step_device(pos.data_ptr(), vel.data_ptr(), acc.data_ptr(), n, p, dkh, dd, precision=ph.FP32_SPLIT)
+        fp.kdk_step_device(pos.data_ptr(), vel.data_ptr(), acc.data_ptr(), n, p, dkh, dd, precision=ph.FP32_SPLIT,
+                           flags=pflags)
     e1.record(stream)
     torch.cuda.synchronize()
     step_ms = e0.elapsed_time(e1) / steps
@@ -262,11 +264,13 @@ def kdk_measure(ph, fp, torch, stream, dpos, dacc, n, p, steps):
     e1.record(stream)
     torch.cuda.synchronize()
     pm_ms = e0.elapsed_time(e1) / reps
-    fp.kdk_step_pm_device(pos.data_ptr(), vel.data_ptr(), acc.data_ptr(), acc_pm.data_ptr(), n, p, nside, dkh, dd)
+    fp.kdk_step_pm_device(pos.data_ptr(), vel.data_ptr(), acc.data_ptr(), acc_pm.data_ptr(), n, p, nside, dkh, dd,
+                          flags=pflags)
     torch.cuda.synchronize()
     e0.record(stream)
     for _ in range(steps):
-        fp.kdk_step_pm_device(pos.data_ptr(), vel.data_ptr(), acc.data_ptr(), acc_pm.data_ptr(), n, p, nside, dkh, dd)
+        fp.kdk_step_pm_device(pos.data_ptr(), vel.data_ptr(), acc.data_ptr(), acc_pm.data_ptr(), n, p, nside, dkh, dd,
+                              flags=pflags)
     e1.record(stream)
     torch.cuda.synchronize()
     step_pm_ms = e0.elapsed_time(e1) / steps
@@ -450,11 +454,14 @@ def main():
     free0, total_hbm = torch.cuda.mem_get_info()
     fp = ph.ForcePass(local)
     tune = None
+    pflags = 0  # PHOTONS_F_ONE_WAY where the autotuner found the one-way P2P kernel faster
     if not args.maxleaf:
-        best, table = ph.autotune_leaf(fp, pos, p, error_bound=args.error_bound)
+        best, table, pflags = ph.autotune_leaf(fp, pos, p, error_bound=args.error_bound)
         best = broadcast_from_rank0(best, dist, "cuda")  # every replica runs rank 0's choice
+        pflags = broadcast_from_rank0(pflags, dist, "cuda")
         p["maxleaf"] = best
-        tune = {"chosen_maxleaf": best, "error_bound_median": args.error_bound, "candidates": table,
+        tune = {"chosen_maxleaf": best, "chosen_kernel": "one-way" if (pflags or best < 48) else "mutual",
+                "error_bound_median": args.error_bound, "candidates": table,
                 "score": "fastest pass with median error vs the FP64 direct sum <= bound (2000-particle sample)"}
     stream = torch.cuda.current_stream()
     fp.set_stream(stream.cuda_stream)
@@ -463,7 +470,7 @@ def main():
     torch.cuda.synchronize()
 
     def step():
-        fp.run_device(dpos.data_ptr(), dacc.data_ptr(), n, p, precision=ph.FP32_SPLIT)
+        fp.run_device(dpos.data_ptr(), dacc.data_ptr(), n, p, precision=ph.FP32_SPLIT, flags=pflags)
 
     for _ in range(max(3, args.warmup)):
         step()
@@ -500,7 +507,7 @@ def main():
     hpos = torch.from_numpy(pos).pin_memory()
     hacc = torch.empty_like(hpos).pin_memory()
     hp, ha = hpos.numpy(), hacc.numpy()
-    fp.run(hp, p, precision=ph.FP32_SPLIT, out=ha)
+    fp.run(hp, p, precision=ph.FP32_SPLIT, flags=pflags, out=ha)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -509,7 +516,7 @@ def main():
     t0 = time.time()
     esteps = max(1, min(args.steps, 5))
     for _ in range(esteps):
-        fp.run(hp, p, precision=ph.FP32_SPLIT, out=ha)
+        fp.run(hp, p, precision=ph.FP32_SPLIT, flags=pflags, out=ha)
     e1.record(stream)
     torch.cuda.synchronize()
     if dist:
@@ -526,7 +533,7 @@ def main():
     # mutual kernel evaluates each local leaf pair once for both leaves, so
     # the pairs it evaluates are about half the reference's pair set (self pairs,
     # about 1 %, are counted at half here although they are evaluated in full)
-    mutual = p["maxleaf"] >= 48 and os.environ.get("PHOTONS_P2P_KERNEL", "mutual") == "mutual"
+    mutual = p["maxleaf"] >= 48 and not pflags and os.environ.get("PHOTONS_P2P_KERNEL", "mutual") == "mutual"
     kernel = "k_p2p_mutual" if mutual else "k_p2p_split_packed"
     evaluated = (counters["pairs_local"] // 2 + counters["pairs_image"]) if mutual else pairs
     peak = ph.fp32_fma_peak(8192)
@@ -541,7 +548,7 @@ def main():
         traffic = float(m.group(1)) if m else None
 
     extra = {}
-    kdk = kdk_measure(ph, fp, torch, stream, dpos, dacc, n, p, args.steps) if args.kdk else None
+    kdk = kdk_measure(ph, fp, torch, stream, dpos, dacc, n, p, args.steps, pflags) if args.kdk else None
     rng = np.random.default_rng(7)
     tgt = rng.choice(n, min(n, 10000), replace=False).astype(np.int32)
     ds = ph.direct_sum(pos, p, tgt)

@@ -92,6 +92,7 @@ typedef struct photons_params {
 #define PHOTONS_F_NO_FARFIELD 4     /* skip P2M/M2M/M2L/L2L/L2P */
 #define PHOTONS_F_MULTIPOLES 8      /* compute P2M/M2M even when no M2L task exists */
 #define PHOTONS_F_KEEP_LISTS 16     /* keep lists for photons_list_* */
+#define PHOTONS_F_ONE_WAY 32        /* FP32: every pair one way (no mutual pairs, no reaction slots) */
 
 typedef struct photons_ctx photons_ctx;
 

@@ -277,14 +277,16 @@ static bool mutual_feedback(photons_ctx *c, int over, long long need)
 // input (256^3 Zel'dovich: 55 vs 69 ms) but lose on halos (128^3 NFW: 47 vs
 // 30 ms: leaves of 22 particles fill 32 target slots, and 65 % of the
 // entries sit in lists longer than the sort handles, evaluated one way);
-// below 32 they lose everywhere
+// below 32 they lose everywhere.  On halo-dominated input the one-way
+// kernel can win at 48-64 too (128^3 NFW leaf 48: 35 against 39 ms);
+// PHOTONS_F_ONE_WAY selects it, and the leaf-size autotuner times both.
 #ifndef MU_MIN_LEAF
 #define MU_MIN_LEAF 48
 #endif
 static bool uses_mutual(const photons_ctx *c, int precision)
 {
     return precision != PHOTONS_FP64 && p2p_variant() == 2 && c->pp.maxleaf >= MU_MIN_LEAF &&
-           c->pp.maxleaf <= 64 && !c->mu_off;
+           c->pp.maxleaf <= 64 && !c->mu_off && !(c->pass_flags & PHOTONS_F_ONE_WAY);
 }
 
 // buffers of the mutual kernel, only for passes that run it: per-entry
@@ -450,6 +452,7 @@ static int ph_prepare_boxes(photons_ctx *c, int nbox, const photons_params *p, c
     c->pp.mass = p->mass;
     c->pp.maxleaf = p->maxleaf;
     c->pp.images = 1;
+    c->pass_flags = p->flags;
     c->n = (int)n;
     c->info.nleaf_cap = c->info.nnode_cap = (int)cap;
     c->have_tree = c->have_lists = c->have_multipoles = false;

@@ -60,6 +60,7 @@ struct photons_ctx {
     float *mu_buf = nullptr;
     long long mu_buf_cap = 0, mu_slot_cap = 0, hint_mubuf = 0;
     bool mu_off = false;  // the reaction slots did not fit: every pair one way
+    int pass_flags = 0;   // PHOTONS_F_* of the pass being prepared
     int mu_cap_leaves = 0;
     // PM mesh (pm.cu): density / potential, half spectrum, gradient grids, FFT plans
     int pm_n = 0, pm_cap_io = 0;

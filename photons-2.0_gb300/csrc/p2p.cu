@@ -728,7 +728,10 @@ constexpr int kMuUnroll = MU_UNROLL;
 #ifndef MU_FLUSH
 #define MU_FLUSH 4  // evaluated entries per compensated flush of the partial sums
 #endif
-#define MU_SORT_MAX 1024  // longer lists stay unsorted and are evaluated one way
+// Longer lists stay unsorted and are evaluated one way.  (Sorting lists of
+// up to 8192 entries with a block each, so that halo leaves pair too, made
+// 128^3 NFW at leaf 48 slower: 46.6 against 39.4 ms.)
+#define MU_SORT_MAX 1024
 // Two builds of the kernel, chosen by MAXLEAF: for leaves of up to 64
 // (mostly 8 targets per lane) 3 resident blocks per SM (158 registers) with
 // two target pairs evaluated stage by stage together; below 60, 4 blocks
@@ -963,7 +966,7 @@ __device__ __forceinline__ void mu_target(const P2PArgs &A, const int2 *ev, int 
                     const float2 sx = f2(S.x), sy = f2(S.y), sz = f2(S.z);
                     float2 rx = f2(0.f), ry = f2(0.f), rz = f2(0.f);
                     // never more chains than this lane's TP target pairs
-                    constexpr int IL = ILR < TP ? ILR : TP;
+                    constexpr int IL = (ILR < TP && TP % ILR == 0) ? ILR : (TP % ILR == 0 ? TP : 1);
                     static_assert(TP % IL == 0, "target pairs in whole interleave groups");
                     if constexpr (IL > 1) {
 #pragma unroll
@@ -1061,7 +1064,7 @@ __device__ __forceinline__ void mu_target(const P2PArgs &A, const int2 *ev, int 
     __syncwarp();
 }
 
-template <int MINB, int ILR>
+template <int MINB, int ILR, bool T6>
 __global__ void __launch_bounds__(MU_TB, MINB) k_p2p_mutual(P2PArgs A, const int2 *ev, const int *nev,
                                                             const long long *rbase, float *rbuf)
 {
@@ -1091,8 +1094,14 @@ __global__ void __launch_bounds__(MU_TB, MINB) k_p2p_mutual(P2PArgs A, const int
         K.cs = B.cs;
         const int2 *evt = ev + A.p2p_off[t];
         const int ne = nev[t];
-        if (nt > 32)
+        // the narrow build gives leaves of 33-48 particles 6 targets per lane
+        // (48 slots; 128^3 NFW at leaf 48: 39.4 against 47.4 ms with 64);
+        // in the wide build the extra path cost 1.3 % at 256^3 leaf 64
+        if (nt > 48 || (nt > 32 && !T6))
             mu_target<8, ILR>(A, evt, ne, rbase, rbuf, t, nt, it, K, B.Lhi, B.Llo, s_src[wib], s_meta[wib], s_red[wib],
+                         s_acc[wib], lane);
+        else if (nt > 32)
+            mu_target<6, ILR>(A, evt, ne, rbase, rbuf, t, nt, it, K, B.Lhi, B.Llo, s_src[wib], s_meta[wib], s_red[wib],
                          s_acc[wib], lane);
         else
             mu_target<4, ILR>(A, evt, ne, rbase, rbuf, t, nt, it, K, B.Lhi, B.Llo, s_src[wib], s_meta[wib], s_red[wib],
@@ -1200,10 +1209,10 @@ int launch_p2p_mutual(const P2PArgs &a, const MutualBufs &m, cudaStream_t st)
                                                             m.sorted, m.total, m.buf_cap, m.slot, m.ev, m.nev,
                                                             m.over);
     if (m.maxleaf >= 60)
-        ph::note_launch(), k_p2p_mutual<MU_WIDE_MINB, MU_WIDE_IL>
+        ph::note_launch(), k_p2p_mutual<MU_WIDE_MINB, MU_WIDE_IL, false>
             <<<sms * MU_WIDE_MINB, MU_TB, 0, st>>>(a, m.ev, m.nev, m.rbase, m.buf);
     else
-        ph::note_launch(), k_p2p_mutual<MU_NARROW_MINB, MU_NARROW_IL>
+        ph::note_launch(), k_p2p_mutual<MU_NARROW_MINB, MU_NARROW_IL, true>
             <<<sms * MU_NARROW_MINB, MU_TB, 0, st>>>(a, m.ev, m.nev, m.rbase, m.buf);
     ph::note_launch(), k_mu_gather<<<sms * 8, 256, 0, st>>>(a, m.slot, m.nrecv, m.rbase, m.buf);
     PH_CUDA_CHECK(cudaGetLastError());

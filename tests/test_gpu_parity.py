@@ -182,6 +182,31 @@ def test_mutual_pairs_graph_and_stage_paths_agree(ph, ics, monkeypatch):
     assert np.array_equal(graph, stages)
 
 
+def test_one_way_flag_selects_the_one_way_kernel(ph, ics, monkeypatch):
+    """PHOTONS_F_ONE_WAY at leaf 64 runs the one-way kernel: the same
+    accelerations, bit for bit, as forcing it through the environment."""
+    pos, p = ics.make("zeldovich256", nside=32, maxleaf=64)
+    flagged = ph.ForcePass(0).run(pos, p, precision=ph.FP32_SPLIT, flags=ph.F_ONE_WAY)
+    mutual = ph.ForcePass(0).run(pos, p, precision=ph.FP32_SPLIT)
+    monkeypatch.setenv("PHOTONS_P2P_KERNEL", "packed")
+    packed = ph.ForcePass(0).run(pos, p, precision=ph.FP32_SPLIT)
+    assert np.array_equal(flagged, packed)
+    assert not np.array_equal(flagged, mutual)  # the default at leaf 64 is the mutual kernel
+    assert np.median(rel_err(flagged, mutual, p)) <= 5e-6
+
+
+def test_autotuner_times_both_kernels_from_leaf_48(ph, ics):
+    pos, p = ics.make("nfw128", nside=32, maxleaf=16)
+    fp = ph.ForcePass(0)
+    best, table, flags = ph.autotune_leaf(fp, pos, p, candidates=(32, 48), sample=500, repeats=1)
+    assert sorted((r["maxleaf"], r["kernel"]) for r in table) == [(32, "one-way"), (48, "mutual"), (48, "one-way")]
+    chosen = [r for r in table if r["maxleaf"] == best and r["flags"] == flags]
+    assert len(chosen) == 1
+    ok = [r for r in table if r["median"] <= 1e-4]
+    if ok:
+        assert chosen[0]["ms"] == min(r["ms"] for r in ok)
+
+
 def test_capacity_overflow_is_an_error(ph, fp):
     pos = np.full((100, 3), 3.0)
     p = dict(boxsize=10.0, theta=0.5, rs=1.0, rcut=4.5, eps=0.01, mass=1.0, maxleaf=8)
