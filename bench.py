@@ -530,12 +530,13 @@ def main():
         return
 
     # roofline of the dominant kernel (P2P, FP32 pipe).  From leaf 48 the
-    # mutual kernel evaluates each local leaf pair once for both leaves, so
-    # the pairs it evaluates are about half the reference's pair set (self pairs,
-    # about 1 %, are counted at half here although they are evaluated in full)
+    # mutual kernel evaluates each symmetric leaf pair (local or image) once
+    # for both leaves, so the pairs it evaluates are about half the
+    # reference's pair set (self pairs, about 1 %, are counted at half here
+    # although they are evaluated in full)
     mutual = p["maxleaf"] >= 48 and not pflags and os.environ.get("PHOTONS_P2P_KERNEL", "mutual") == "mutual"
     kernel = "k_p2p_mutual" if mutual else "k_p2p_split_packed"
-    evaluated = (counters["pairs_local"] // 2 + counters["pairs_image"]) if mutual else pairs
+    evaluated = pairs // 2 if mutual else pairs
     peak = ph.fp32_fma_peak(8192)
     t_p2p = float(np.mean(p2p_ms))
     achieved = FLOPS_PER_PAIR * pairs / (t_p2p * 1e-3) / 1e12

@@ -227,7 +227,7 @@ static void free_all(photons_ctx *c)
                     c->az, c->M, c->L, c->io, c->work_counter, c->t.chi, c->t.clo, c->t.w32, c->t.son2, c->M32,
                     b.lvl_begin, b.lvl_count, b.leaf_begin, b.leaf_count, c->t.depth_cnt, b.tn_boxid, b.tl_boxid,
                     c->t.boxid, b.boxes, c->far_gate, c->mu_sorted, c->mu_nrecv, c->mu_slot, c->mu_over,
-                    c->mu_size, c->mu_rbase, c->mu_total, c->mu_scan, c->mu_buf, c->mu_ev, c->mu_nev};
+                    c->mu_size, c->mu_rbase, c->mu_total, c->mu_scan, c->mu_buf, c->mu_ev, c->mu_nev, c->mu_pq};
     for (void *p : ptrs)
         if (p) cudaFree(p);
 }
@@ -295,13 +295,13 @@ static int alloc_mutual(photons_ctx *c, int precision)
 {
     if (!uses_mutual(c, precision)) return 0;
     // first guess: about half of a leaf's ~110-250 list entries received, 3
-    // floats per particle and entry (256^3 leaf 64 needs ~170 per particle);
+    // floats per particle and entry (256^3 leaf 64 needs ~180 per particle);
     // a pass that needs more repeats once with the measured size
-    long long want = c->hint_mubuf ? c->hint_mubuf : (long long)c->n * 176 + 4096;
+    long long want = c->hint_mubuf ? c->hint_mubuf : (long long)c->n * 192 + 4096;
     // the reaction slots take ~700 bytes per particle: where they would not
     // leave 1 GB of the device free, this context evaluates every pair one way
     size_t grow = 0, free_b = 0, total_b = 0;
-    if (c->w.p2p_cap > c->mu_slot_cap) grow += (size_t)(c->w.p2p_cap - c->mu_slot_cap) * (sizeof(int) + sizeof(int2));
+    if (c->w.p2p_cap > c->mu_slot_cap) grow += (size_t)(c->w.p2p_cap - c->mu_slot_cap) * (2 * sizeof(int) + sizeof(int2));
     if (want > c->mu_buf_cap) grow += (size_t)(want - c->mu_buf_cap) * sizeof(float);
     if (grow && cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && grow + ((size_t)1 << 30) > free_b) {
         c->mu_off = true;
@@ -311,6 +311,7 @@ static int alloc_mutual(photons_ctx *c, int precision)
     if (c->w.p2p_cap > c->mu_slot_cap) {
         PH_TRY(dalloc(c->mu_slot, (size_t)c->w.p2p_cap));
         PH_TRY(dalloc(c->mu_ev, (size_t)c->w.p2p_cap));
+        PH_TRY(dalloc(c->mu_pq, (size_t)c->w.p2p_cap));
         c->mu_slot_cap = c->w.p2p_cap;
         c->epoch++;
     }
@@ -661,7 +662,7 @@ int ph_stage_p2p(photons_ctx *c, int precision, int zero)
         m.pool = c->w.p2p_pool;
         m.sorted = c->mu_sorted; m.nrecv = c->mu_nrecv; m.size = c->mu_size; m.rbase = c->mu_rbase;
         m.total = c->mu_total; m.scan_scratch = c->mu_scan; m.slot = c->mu_slot; m.over = c->mu_over;
-        m.ev = c->mu_ev; m.nev = c->mu_nev; m.maxleaf = c->pp.maxleaf;
+        m.ev = c->mu_ev; m.nev = c->mu_nev; m.maxleaf = c->pp.maxleaf; m.pq = c->mu_pq;
         m.buf = c->mu_buf; m.buf_cap = c->mu_buf_cap; m.cap_leaves = c->mu_cap_leaves;
         PH_TRY(ph::launch_p2p_mutual(a, m, st));
     } else {

@@ -56,6 +56,7 @@ struct photons_ctx {
     int *mu_sorted = nullptr, *mu_nrecv = nullptr, *mu_slot = nullptr, *mu_over = nullptr;
     long long *mu_size = nullptr, *mu_rbase = nullptr, *mu_total = nullptr, *mu_scan = nullptr;
     int *mu_nev = nullptr;
+    int *mu_pq = nullptr;
     int2 *mu_ev = nullptr;
     float *mu_buf = nullptr;
     long long mu_buf_cap = 0, mu_slot_cap = 0, hint_mubuf = 0;

@@ -698,22 +698,23 @@ __global__ void k_leaf_offsets(const double *px, const double *py, const double 
 // ---------------------------------------------------------------------
 // FP32 split-precision P2P with mutual pairs.
 //
-// The local P2P lists are symmetric (leaf B is in A's list exactly when A is
-// in B's), so each such pair is evaluated once: the leaf with the lower id
-// (the owner) computes the forces on its own particles and the equal and
-// opposite reactions on the other leaf's particles, which it stores in a
-// slot of a reaction buffer; a second kernel adds each leaf's received
-// reactions in list order.  Self pairs, image pairs and any entry whose
-// partner entry is missing are evaluated one way, as before.  Results are
+// The P2P lists are symmetric: leaf B, shifted by the image offset s, is in
+// A's list exactly when A shifted by -s is in B's (s = 0 for local pairs;
+// A = B for a leaf and its own periodic image).  So each such pair is
+// evaluated once.  The owner is the entry with the smaller (leaf id, image)
+// key.  It computes the forces on its own particles and the equal and
+// opposite reactions on the other leaf's particles, and stores those in a
+// slot of a reaction buffer.  A second kernel adds each leaf's received
+// reactions in list order.  Self pairs and entries whose partner is missing
+// (or whose list is too long to sort) are evaluated one way.  Results are
 // deterministic.
 //
-// Pairing: every target's list is sorted by raw entry value (local sources
-// first, by id); a local entry (A, B) is mutual when both lists are sorted
-// and B's list holds A; its slot is A's rank q in B's list.  B's received
-// entries are then the leading entries of its list (ids below B), so slot
-// q of B lives at rbase[B] + 3 q nB floats, x then y then z of B's nB
-// particles.
-//
+// Pairing: every target's list is sorted by raw entry value.  Entry (B, s)
+// of A is paired when both lists are sorted and B's list holds (A, -s),
+// found by binary search.  The received entries of B are numbered in list
+// order.  B's k-th received slot lives at rbase[B] + 3 k nB floats: x, then
+// y, then z of B's nB particles.
+
 // Lanes: 8 target groups x 4 source groups; a lane holds 8 targets (as four
 // pairs of the paired FP32 instructions) and takes 8 sources of each batch
 // of 32, so reactions are summed over 8 target groups through shared memory
@@ -746,8 +747,7 @@ constexpr int kMuUnroll = MU_UNROLL;
 #endif
 
 __global__ void __launch_bounds__(256) k_mu_sort(const int *tree_cnt, const unsigned long long *walk_flags,
-                                                  uint32_t *pool, const long long *off, const int *cnt,
-                                                  const int *npart, int *sorted, int *nrecv, long long *size)
+                                                  uint32_t *pool, const long long *off, const int *cnt, int *sorted)
 {
     __shared__ uint32_t s_buf[8][MU_SORT_MAX];
     const int lane = warp_lane(), wib = threadIdx.x >> 5;
@@ -758,7 +758,6 @@ __global__ void __launch_bounds__(256) k_mu_sort(const int *tree_cnt, const unsi
         const int L = cnt[t];
         uint32_t *lst = pool + off[t];
         const int ok = L <= MU_SORT_MAX;
-        int below = 0;
         if (ok && L > 1) {
             int P = 2;
             while (P < L) P <<= 1;
@@ -778,20 +777,10 @@ __global__ void __launch_bounds__(256) k_mu_sort(const int *tree_cnt, const unsi
                     }
                 }
             __syncwarp();
-            for (int i = lane; i < L; i += 32) {
-                lst[i] = buf[i];
-                below += buf[i] < (uint32_t)t;
-            }
+            for (int i = lane; i < L; i += 32) lst[i] = buf[i];
             __syncwarp();
-        } else if (ok) {
-            for (int i = lane; i < L; i += 32) below += lst[i] < (uint32_t)t;
         }
-        below = __reduce_add_sync(0xffffffffu, below);
-        if (lane == 0) {
-            sorted[t] = ok;
-            nrecv[t] = ok ? below : 0;
-            size[t] = ok ? (long long)below * npart[t] * 3 : 0;
-        }
+        if (lane == 0) sorted[t] = ok;
     }
 }
 
@@ -807,13 +796,71 @@ __device__ __forceinline__ int mu_find(const uint32_t *lst, int L, uint32_t v)
     return (lo < L && lst[lo] == v) ? lo : -1;
 }
 
-// slot per entry: q >= 0 owned mutual (the owner's rank in the partner's
-// list), -2 received mutual, -1 evaluated one way; the entries a target
-// evaluates (all but the received) are also packed in list order into
-// ev[off + k] = (entry, slot), nev[t] of them
+// the image with the opposite shift (the partner of an image entry)
+__device__ __forceinline__ int img_neg(int img)
+{
+    if (img == 0) return 0;
+    const int c = img <= 13 ? img - 1 : img;  // index among the 27 cells (13 = no shift)
+    const int cn = 26 - c;
+    return cn <= 12 ? cn + 1 : cn;
+}
+
+// Pairing, per target t and list entry (b, img), b's list searched for the
+// partner entry (t, -img).  Found: the entry with the smaller (id, image)
+// key owns the pair, the other receives it.  Received entries are numbered
+// in list order (their slots in t's reaction area); owned entries record the
+// partner's position.  slot[e]: -1 one way, -2 received, -3 owned; pq[e]:
+// the received rank, or the partner's position in b's list.
+__global__ void k_mu_pair(const int *tree_cnt, const unsigned long long *walk_flags, const uint32_t *pool,
+                          const long long *off, const int *cnt, const int *npart, const int *sorted, int *slot,
+                          int *pq, int *nrecv, long long *size)
+{
+    const int lane = warp_lane();
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    const int nleaf = *walk_flags ? 0 : tree_cnt[BC_LEAVES];
+    const unsigned below = (1u << lane) - 1u;
+    for (int t = gw; t < nleaf; t += nw) {
+        const long long o = off[t];
+        const int L = cnt[t];
+        const bool st = sorted[t];
+        int recv = 0;
+        for (int e0 = 0; e0 < L; e0 += 32) {
+            const int e = e0 + lane;
+            int kind = -1, q = -1;
+            if (e < L) {
+                const uint32_t v = pool[o + e];
+                const int b = PH_ENTRY_ID(v), img = PH_ENTRY_IMG(v), nimg = img_neg(img);
+                if (st && sorted[b] && !(img == 0 && b == t)) {
+                    q = mu_find(pool + off[b], cnt[b], PH_ENTRY(t, nimg));
+                    if (q >= 0) {
+                        const unsigned long long mine = ((unsigned long long)t << 5) | (unsigned)img;
+                        const unsigned long long theirs = ((unsigned long long)b << 5) | (unsigned)nimg;
+                        kind = mine < theirs ? -3 : -2;
+                    }
+                }
+            }
+            const unsigned got = __ballot_sync(0xffffffffu, kind == -2);
+            if (e < L) {
+                slot[o + e] = kind;
+                pq[o + e] = kind == -2 ? recv + __popc(got & below) : (kind == -3 ? q : -1);
+            }
+            recv += __popc(got);
+        }
+        if (lane == 0) {
+            nrecv[t] = recv;
+            size[t] = (long long)recv * npart[t] * 3;
+        }
+    }
+}
+
+// Final slots once the reaction offsets are known: owned entries take the
+// partner's received rank; with the reaction buffer too small every entry
+// is evaluated one way.  The entries a target evaluates (all but the
+// received) are packed in list order into ev[off + k] = (entry, slot),
+// nev[t] of them.
 __global__ void k_mu_slots(const int *tree_cnt, const unsigned long long *walk_flags, const uint32_t *pool,
-                           const long long *off, const int *cnt, const int *sorted, const long long *total,
-                           long long cap, int *slot, int2 *ev, int *nev, int *over)
+                           const long long *off, const int *cnt, const long long *total, long long cap,
+                           const int *pq, int *slot, int2 *ev, int *nev, int *over)
 {
     const int lane = warp_lane();
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
@@ -824,7 +871,6 @@ __global__ void k_mu_slots(const int *tree_cnt, const unsigned long long *walk_f
     for (int t = gw; t < nleaf; t += nw) {
         const long long o = off[t];
         const int L = cnt[t];
-        const bool st = sorted[t] && fits;
         int kept = 0;
         for (int e0 = 0; e0 < L; e0 += 32) {
             const int e = e0 + lane;
@@ -832,16 +878,13 @@ __global__ void k_mu_slots(const int *tree_cnt, const unsigned long long *walk_f
             int r = -2;
             if (e < L) {
                 v = pool[o + e];
-                const int b = PH_ENTRY_ID(v);
-                r = -1;
-                if (st && PH_ENTRY_IMG(v) == 0 && b != t && sorted[b]) {
-                    const int q = mu_find(pool + off[b], cnt[b], (uint32_t)t);
-                    if (q >= 0) r = t < b ? q : -2;
-                }
+                r = slot[o + e];
+                if (!fits) r = -1;
+                else if (r == -3) r = pq[off[PH_ENTRY_ID(v)] + pq[o + e]];
                 slot[o + e] = r;
             }
-            const unsigned keep = __ballot_sync(0xffffffffu, r != -2);
-            if (r != -2) ev[o + kept + __popc(keep & below)] = make_int2((int)v, r);
+            const unsigned keep = __ballot_sync(0xffffffffu, e < L && r != -2);
+            if (e < L && r != -2) ev[o + kept + __popc(keep & below)] = make_int2((int)v, r);
             kept += __popc(keep);
         }
         if (lane == 0) nev[t] = kept;
@@ -1110,9 +1153,10 @@ __global__ void __launch_bounds__(MU_TB, MINB) k_p2p_mutual(P2PArgs A, const int
 }
 
 // each leaf adds the reactions its owners left in its slots, in list order.
-// Slot r of leaf t holds [3][nt] floats at rbase[t] + 3 r nt; which slots
-// were written (slot == -2) is read once per 32 as a warp mask, and eight
-// slots' loads are in flight at a time.
+// The k-th received entry of leaf t (slot == -2, counted in list order)
+// holds [3][nt] floats at rbase[t] + 3 k nt; which entries are received is
+// read once per 32 as a warp mask, and eight slots' loads are in flight at
+// a time.
 __global__ void k_mu_gather(P2PArgs A, const int *slot, const int *nrecv, const long long *rbase, const float *rbuf)
 {
     const int lane = warp_lane();
@@ -1122,32 +1166,40 @@ __global__ void k_mu_gather(P2PArgs A, const int *slot, const int *nrecv, const 
         const int nt = A.npart[t], it = A.ipart[t], nr = nrecv[t];
         if (nr == 0 || nt == 0) continue;
         const long long eoff = A.p2p_off[t];
+        const int L = A.p2p_cnt[t];
         const double scale = A.boxes[A.boxid[t]].acc_scale;
         const long long stride = 3LL * nt;
         for (int j0 = 0; j0 < nt; j0 += 32) {
             const int j = j0 + lane;
             const float *base = rbuf + rbase[t] + j;
             float v0 = 0.f, v1 = 0.f, v2 = 0.f, c0 = 0.f, c1 = 0.f, c2 = 0.f;
-            for (int r0 = 0; r0 < nr; r0 += 32) {
-                const unsigned got = __ballot_sync(0xffffffffu, r0 + lane < nr && slot[eoff + r0 + lane] == -2);
-                for (int k0 = 0; k0 < 32 && (got >> k0); k0 += 8) {
+            int k = 0;  // received entries before this chunk
+            for (int e0 = 0; e0 < L && k < nr; e0 += 32) {
+                unsigned got = __ballot_sync(0xffffffffu, e0 + lane < L && slot[eoff + e0 + lane] == -2);
+                while (got) {
+                    // up to eight received slots: loads first, then the adds in order
                     float in[8][3];
+                    int cntk = 0;
 #pragma unroll
-                    for (int k = 0; k < 8; k++) {
-                        const bool use = j < nt && ((got >> (k0 + k)) & 1u);
-                        const float *q = base + (r0 + k0 + k) * stride;
-                        in[k][0] = use ? q[0] : 0.f;
-                        in[k][1] = use ? q[nt] : 0.f;
-                        in[k][2] = use ? q[2 * nt] : 0.f;
+                    for (int q = 0; q < 8; q++) {
+                        const bool use = got != 0;
+                        if (use) got &= got - 1;
+                        cntk += use;
+                        const bool ld = use && j < nt;
+                        const float *src = base + (long long)(k + q) * stride;
+                        in[q][0] = ld ? src[0] : 0.f;
+                        in[q][1] = ld ? src[nt] : 0.f;
+                        in[q][2] = ld ? src[2 * nt] : 0.f;
                     }
 #pragma unroll
-                    for (int k = 0; k < 8; k++) {
-                        if ((got >> (k0 + k)) & 1u) {
-                            kahan_add(v0, c0, in[k][0]);
-                            kahan_add(v1, c1, in[k][1]);
-                            kahan_add(v2, c2, in[k][2]);
+                    for (int q = 0; q < 8; q++) {
+                        if (q < cntk) {
+                            kahan_add(v0, c0, in[q][0]);
+                            kahan_add(v1, c1, in[q][1]);
+                            kahan_add(v2, c2, in[q][2]);
                         }
                     }
+                    k += cntk;
                 }
             }
             if (j < nt) {
@@ -1203,11 +1255,12 @@ int launch_p2p_mutual(const P2PArgs &a, const MutualBufs &m, cudaStream_t st)
     PH_CUDA_CHECK(cudaMemsetAsync(a.work_counter, 0, sizeof(int), st));
     const int sms = device_sm_count();
     ph::note_launch(), k_mu_sort<<<sms * 4, 256, 0, st>>>(a.tree_cnt, a.walk_flags, m.pool, a.p2p_off, a.p2p_cnt,
-                                                           a.npart, m.sorted, m.nrecv, m.size);
+                                                           m.sorted);
+    ph::note_launch(), k_mu_pair<<<sms * 8, 256, 0, st>>>(a.tree_cnt, a.walk_flags, m.pool, a.p2p_off, a.p2p_cnt,
+                                                           a.npart, m.sorted, m.slot, m.pq, m.nrecv, m.size);
     scan_exclusive_i64(m.size, m.rbase, a.tree_cnt + BC_LEAVES, m.cap_leaves, m.total, m.scan_scratch, st);
     ph::note_launch(), k_mu_slots<<<sms * 8, 256, 0, st>>>(a.tree_cnt, a.walk_flags, m.pool, a.p2p_off, a.p2p_cnt,
-                                                            m.sorted, m.total, m.buf_cap, m.slot, m.ev, m.nev,
-                                                            m.over);
+                                                            m.total, m.buf_cap, m.pq, m.slot, m.ev, m.nev, m.over);
     if (m.maxleaf >= 60)
         ph::note_launch(), k_p2p_mutual<MU_WIDE_MINB, MU_WIDE_IL, false>
             <<<sms * MU_WIDE_MINB, MU_TB, 0, st>>>(a, m.ev, m.nev, m.rbase, m.buf);

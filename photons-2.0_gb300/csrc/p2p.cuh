@@ -55,6 +55,7 @@ struct MutualBufs {
     int2 *ev;                // per pool offset: the entries a target evaluates, packed in list order
     int *nev;                // per leaf: their number
     int maxleaf;             // selects the kernel build
+    int *pq;                 // per pool entry: received rank, or the owned pair's partner position
 };
 
 SplitConsts make_split_consts(const PassParams &p);
