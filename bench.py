@@ -507,7 +507,8 @@ def main():
     hpos = torch.from_numpy(pos).pin_memory()
     hacc = torch.empty_like(hpos).pin_memory()
     hp, ha = hpos.numpy(), hacc.numpy()
-    fp.run(hp, p, precision=ph.FP32_SPLIT, flags=pflags, out=ha)
+    for _ in range(2):  # the host-buffer pass is captured as its own graph on first use
+        fp.run(hp, p, precision=ph.FP32_SPLIT, flags=pflags, out=ha)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
