@@ -712,8 +712,8 @@ __global__ void k_leaf_offsets(const double *px, const double *py, const double 
 // Pairing: every target's list is sorted by raw entry value.  Entry (B, s)
 // of A is paired when both lists are sorted and B's list holds (A, -s),
 // found by binary search.  The received entries of B are numbered in list
-// order.  B's k-th received slot lives at rbase[B] + 3 k nB floats: x, then
-// y, then z of B's nB particles.
+// order.  B's k-th received slot lives at rbase[B] + 3 k r floats: x, then
+// y, then z of B's nB particles, each row r = nB rounded up to 32 floats.
 
 // Lanes: 8 target groups x 4 source groups; a lane holds 8 targets (as four
 // pairs of the paired FP32 instructions) and takes 8 sources of each batch
@@ -796,6 +796,10 @@ __device__ __forceinline__ int mu_find(const uint32_t *lst, int L, uint32_t v)
     return (lo < L && lst[lo] == v) ? lo : -1;
 }
 
+// floats per component row of a reaction slot: n rounded up to 32, so that
+// every row starts on a 128-byte line
+__host__ __device__ __forceinline__ int mu_row(int n) { return (n + 31) & ~31; }
+
 // the image with the opposite shift (the partner of an image entry)
 __device__ __forceinline__ int img_neg(int img)
 {
@@ -848,7 +852,7 @@ __global__ void k_mu_pair(const int *tree_cnt, const unsigned long long *walk_fl
         }
         if (lane == 0) {
             nrecv[t] = recv;
-            size[t] = (long long)recv * npart[t] * 3;
+            size[t] = (long long)recv * mu_row(npart[t]) * 3;
         }
     }
 }
@@ -983,7 +987,7 @@ __device__ __forceinline__ void mu_target(const P2PArgs &A, const int2 *ev, int 
             m.is = A.ipart[s];
             m.ns = A.npart[s];
             m.owned = en.y >= 0;
-            m.out = en.y >= 0 ? rbase[s] + (long long)en.y * m.ns * 3 : 0;
+            m.out = en.y >= 0 ? rbase[s] + (long long)en.y * mu_row(m.ns) * 3 : 0;
             meta[lane] = m;
         }
         __syncwarp();
@@ -1053,7 +1057,7 @@ __device__ __forceinline__ void mu_target(const P2PArgs &A, const int2 *ev, int 
                         for (int cmp = 0; cmp < 3; cmp++) {
                             const float4 *rr = reinterpret_cast<const float4 *>(red + lane * 24 + cmp * 8);
                             const float4 u = rr[0], w = rr[1];
-                            out[cmp * ns] = -((((u.x + u.y) + (u.z + u.w)) + ((w.x + w.y) + (w.z + w.w))));
+                            out[cmp * mu_row(ns)] = -((((u.x + u.y) + (u.z + u.w)) + ((w.x + w.y) + (w.z + w.w))));
                         }
                     }
                     __syncwarp();
@@ -1154,9 +1158,9 @@ __global__ void __launch_bounds__(MU_TB, MINB) k_p2p_mutual(P2PArgs A, const int
 
 // each leaf adds the reactions its owners left in its slots, in list order.
 // The k-th received entry of leaf t (slot == -2, counted in list order)
-// holds [3][nt] floats at rbase[t] + 3 k nt; which entries are received is
-// read once per 32 as a warp mask, and eight slots' loads are in flight at
-// a time.
+// holds [3][r] floats at rbase[t] + 3 k r (r = nt rounded up to 32).  Which
+// entries are received is read once per 32 as a warp mask, and eight
+// slots' loads are in flight at a time.
 __global__ void k_mu_gather(P2PArgs A, const int *slot, const int *nrecv, const long long *rbase, const float *rbuf)
 {
     const int lane = warp_lane();
@@ -1168,7 +1172,8 @@ __global__ void k_mu_gather(P2PArgs A, const int *slot, const int *nrecv, const 
         const long long eoff = A.p2p_off[t];
         const int L = A.p2p_cnt[t];
         const double scale = A.boxes[A.boxid[t]].acc_scale;
-        const long long stride = 3LL * nt;
+        const int rl = mu_row(nt);
+        const long long stride = 3LL * rl;
         for (int j0 = 0; j0 < nt; j0 += 32) {
             const int j = j0 + lane;
             const float *base = rbuf + rbase[t] + j;
@@ -1188,8 +1193,8 @@ __global__ void k_mu_gather(P2PArgs A, const int *slot, const int *nrecv, const 
                         const bool ld = use && j < nt;
                         const float *src = base + (long long)(k + q) * stride;
                         in[q][0] = ld ? src[0] : 0.f;
-                        in[q][1] = ld ? src[nt] : 0.f;
-                        in[q][2] = ld ? src[2 * nt] : 0.f;
+                        in[q][1] = ld ? src[rl] : 0.f;
+                        in[q][2] = ld ? src[2 * rl] : 0.f;
                     }
 #pragma unroll
                     for (int q = 0; q < 8; q++) {
