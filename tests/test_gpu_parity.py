@@ -152,11 +152,16 @@ def test_graph_pass_matches_stage_pass(ph, ics, monkeypatch, precision):
     assert fp.counters()["depth"] > 2
 
 
-@pytest.mark.parametrize("workload,nside,maxleaf", [("grid32", 32, 48), ("nfw128", 32, 64), ("zeldovich256", 32, 64)])
+@pytest.mark.parametrize("workload,nside,maxleaf", [("grid32", 32, 48), ("nfw128", 32, 64), ("zeldovich256", 32, 64),
+                                                    ("nfw128", 40, 48), ("zeldovich256", 32, 60),
+                                                    ("zeldovich256", 24, 56)])
 def test_mutual_pairs_match_one_way(ph, ics, monkeypatch, workload, nside, maxleaf):
-    """The FP32 kernel that evaluates each local leaf pair once (reactions
-    through a buffer) against the one-way kernel and the FP64 pass: the
-    same forces to FP32 rounding, deterministic from pass to pass."""
+    """The FP32 kernel that evaluates each symmetric leaf pair (local or
+    periodic image) once, reactions through a buffer, against the one-way
+    kernel and the FP64 pass: the same forces to FP32 rounding,
+    deterministic from pass to pass.  Covers both builds (leaf 60+ and
+    below), the 48-slot tile (halo leaves of 33-48 particles) and lists
+    too long to pair."""
     pos, p = ics.make(workload, nside=nside, maxleaf=maxleaf)
     fp = ph.ForcePass(0)
     a64 = fp.run(pos, p, precision=ph.FP64)
