@@ -460,11 +460,6 @@ static int ph_prepare_boxes(photons_ctx *c, int nbox, const photons_params *p, c
     return 0;
 }
 
-static int ph_prepare(photons_ctx *c, const photons_params *p, int n)
-{
-    return ph_prepare_boxes(c, 1, p, &n);
-}
-
 // the box table for this pass (before the build; the build writes the roots)
 static int ph_upload_boxes(photons_ctx *c)
 {

@@ -136,7 +136,7 @@ __global__ void k_pm_green(cufftDoubleComplex *rk, const double *__restrict__ G,
 // f1 invx (psi+1 - psi-1) - f2 invx (psi+2 - psi-2), f1 = 4/3, f2 = 1/6, invx = N / (2 L)
 // (x, y, z, 0) per cell, one 32-byte record, so that the interpolation's
 // eight corners are eight sector loads
-__global__ void k_pm_gradient(const double *__restrict__ psi, int N, double invx, double4 *g4)
+__global__ void k_pm_gradient(const double *__restrict__ psi, int N, double invx, double4_32a *g4)
 {
     const double f1 = 4.0 / 3.0, f2 = 1.0 / 6.0;
     const double c1 = __dmul_rn(f1, invx), c2 = __dmul_rn(f2, invx);
@@ -150,14 +150,14 @@ __global__ void k_pm_gradient(const double *__restrict__ psi, int N, double invx
         gy = __dsub_rn(d, __dmul_rn(c2, __dsub_rn(psi[cell(i, wrap(j + 2, N), k, N)], psi[cell(i, wrap(j - 2, N), k, N)])));
         d = __dmul_rn(c1, __dsub_rn(psi[cell(i, j, wrap(k + 1, N), N)], psi[cell(i, j, wrap(k - 1, N), N)]));
         gz = __dsub_rn(d, __dmul_rn(c2, __dsub_rn(psi[cell(i, j, wrap(k + 2, N), N)], psi[cell(i, j, wrap(k - 2, N), N)])));
-        g4[t] = make_double4(gx, gy, gz, 0.0);
+        g4[t] = make_double4_32a(gx, gy, gz, 0.0);
     }
 }
 
 // one corner's weighted gradient added to the three running sums.  The
 // adds are fused multiply-adds (one rounding instead of two): the kernel is
 // bound by GB300's FP64 pipe, and this halves its work in the sums.
-__device__ __forceinline__ void corner(double3 &a, double w, const double4 &g, bool first)
+__device__ __forceinline__ void corner(double3 &a, double w, const double4_32a &g, bool first)
 {
     if (first) {
         a = make_double3(__dmul_rn(w, g.x), __dmul_rn(w, g.y), __dmul_rn(w, g.z));
@@ -171,7 +171,7 @@ __device__ __forceinline__ void corner(double3 &a, double w, const double4 &g, b
 // the eight weighted cell values summed in the reference's order, for the
 // three components at once
 __global__ void k_pm_interp(const double *__restrict__ pos, int n, int N, double norm, double delta,
-                            const double4 *__restrict__ g4, double *acc)
+                            const double4_32a *__restrict__ g4, double *acc)
 {
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         const Cic s = cic(pos, p, norm, delta, N);
@@ -270,7 +270,7 @@ int ph_pm_enqueue(photons_ctx *c, const photons_params *p, int N, int n, const d
     r = cufftExecZ2D(c->pm_plan_c2r, c->pm_rk, c->pm_rho);
     if (r != CUFFT_SUCCESS) return cufft_error(r, "cufftExecZ2D");
     const double invx = 0.5 * N / L;  // src/partmesh.c:458
-    double4 *g4 = reinterpret_cast<double4 *>(c->pm_grad);
+    double4_32a *g4 = reinterpret_cast<double4_32a *>(c->pm_grad);
     ph::note_launch(), k_pm_gradient<<<blocks, 256, 0, st>>>(c->pm_rho, N, invx, g4);
     ph::note_launch(), k_pm_interp<<<blocks, 256, 0, st>>>(pos, n, N, norm, delta, g4, acc_pm);
     PH_CUDA_CHECK(cudaGetLastError());

@@ -37,17 +37,6 @@
 namespace ph {
 namespace {
 
-__device__ __forceinline__ int upper_bound_i32(const int *a, int n, int v)
-{
-    int lo = 0, hi = n;
-    while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if (a[mid] <= v) lo = mid + 1;
-        else hi = mid;
-    }
-    return lo;
-}
-
 __device__ __forceinline__ const double *axis_ptr(const double *x, const double *y, const double *z, int D)
 {
     return D == 0 ? x : (D == 1 ? y : z);

@@ -467,8 +467,7 @@ int walk_lists(WalkBufs &w, const TreeBufs &t, const int *tree_cnt, const BoxPar
                const PassParams &p, unsigned image_mask, cudaStream_t st)
 {
     PH_CUDA_CHECK(cudaMemsetAsync(w.ctr, 0, sizeof(unsigned long long) * WC_N, st));
-    WalkArgs A;
-    memset(&A, 0, sizeof A);
+    WalkArgs A{};
     A.g.cx = t.cx; A.g.cy = t.cy; A.g.cz = t.cz;
     A.g.wx = t.wx; A.g.wy = t.wy; A.g.wz = t.wz; A.g.wsum = t.wsum;
     A.g.son0 = t.son0; A.g.son1 = t.son1; A.g.npart = t.npart; A.g.parent = t.parent;
