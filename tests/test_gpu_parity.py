@@ -212,6 +212,26 @@ def test_autotuner_times_both_kernels_from_leaf_48(ph, ics):
         assert chosen[0]["ms"] == min(r["ms"] for r in ok)
 
 
+def test_context_release_returns_device_memory(ph, ics):
+    """Contexts that ran passes of both precisions (tree, lists, reaction
+    slots, captured graphs) give their device memory back on release."""
+    torch = pytest.importorskip("torch")
+    pos, p = ics.make("zeldovich256", nside=32, maxleaf=64)
+    torch.cuda.synchronize()
+    f = ph.ForcePass(0)  # a first context pays the library's one-time setup
+    f.run(pos, p, precision=ph.FP32_SPLIT)
+    f.close()
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        f = ph.ForcePass(0)
+        f.run(pos, p, precision=ph.FP32_SPLIT)
+        f.run(pos, p, precision=ph.FP64)
+        f.close()
+    torch.cuda.synchronize()
+    assert free0 - torch.cuda.mem_get_info()[0] < (64 << 20)
+
+
 def test_capacity_overflow_is_an_error(ph, fp):
     pos = np.full((100, 3), 3.0)
     p = dict(boxsize=10.0, theta=0.5, rs=1.0, rcut=4.5, eps=0.01, mass=1.0, maxleaf=8)
