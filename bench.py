@@ -274,11 +274,37 @@ def kdk_measure(ph, fp, torch, stream, dpos, dacc, n, p, steps, pflags=0):
     e1.record(stream)
     torch.cuda.synchronize()
     step_pm_ms = e0.elapsed_time(e1) / steps
+    # the same steps keeping the state in tree order (the reference's part[]
+    # ordering): each build starts from the previous step's tree order
+    opos, ovel, oacc, opm = pos.clone(), vel.clone(), acc.clone(), acc_pm.clone()
+    oids = torch.arange(n, dtype=torch.int64, device=pos.device)
+
+    def ordered(with_pm):
+        fp.kdk_step_ordered_device(opos.data_ptr(), ovel.data_ptr(), oacc.data_ptr(), oids.data_ptr(), n, p, dkh, dd,
+                                   precision=ph.FP32_SPLIT, flags=pflags, nside=nside if with_pm else 0,
+                                   acc_pm_ptr=opm.data_ptr())
+
+    ordered(False)
+    ordered(False)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        ordered(False)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    step_ordered_ms = e0.elapsed_time(e1) / steps
+    e0.record(stream)
+    for _ in range(steps):
+        ordered(True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    step_ordered_pm_ms = e0.elapsed_time(e1) / steps
     bytes_each = 3 * n * 24  # read two arrays, write one, 3n doubles
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     hbm = peaks.get("hbm_gbs")
     out = {"step_ms": step_ms, "step_with_pm_ms": step_pm_ms, "pm_ms": pm_ms, "pm_mesh": nside,
+           "step_tree_order_ms": step_ordered_ms, "step_tree_order_with_pm_ms": step_ordered_pm_ms,
            "a": [0.5, 0.505], "dkh": dkh, "dd": dd,
            "kick_ms": kick_ms, "drift_ms": drift_ms,
            "kick_gbs": bytes_each / (kick_ms * 1e-3) / 1e9, "drift_gbs": bytes_each / (drift_ms * 1e-3) / 1e9,

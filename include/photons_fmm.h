@@ -225,6 +225,17 @@ int photons_gadget_write(const char *path, const photons_gadget_header *h, long 
 int photons_kdk_step_pm(photons_ctx *ctx, const photons_params *p, int nside, int n, double *pos, double *vel,
                         double *acc, double *acc_pm, double dkh, double dd);
 
+/* the two steps above with the particle state kept in tree order, as the
+   reference's driver keeps part[] (src/fmm.c:30-78): after the short-range
+   pass pos, vel and ids (optional, may be NULL; the caller's particle
+   identities) are permuted into the pass's tree order and acc (and acc_pm)
+   come back in it, so the next step's build starts from nearly sorted
+   particles.  No counterpart function in the reference; device arrays. */
+int photons_kdk_step_ordered(photons_ctx *ctx, const photons_params *p, int n, double *pos, double *vel, double *acc,
+                             long long *ids, double dkh, double dd);
+int photons_kdk_step_pm_ordered(photons_ctx *ctx, const photons_params *p, int nside, int n, double *pos,
+                                double *vel, double *acc, double *acc_pm, long long *ids, double dkh, double dd);
+
 /* kernels launched by this library so far (all contexts) */
 unsigned long long photons_launch_count(void);
 

@@ -113,6 +113,10 @@ def load_library():
         [C.c_double, C.c_double]
     lib.photons_kdk_step.argtypes = [C.c_void_p, C.POINTER(Params), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.c_double, C.c_double]
+    lib.photons_kdk_step_ordered.argtypes = [C.c_void_p, C.POINTER(Params), C.c_int] + [C.c_void_p] * 4 + \
+        [C.c_double, C.c_double]
+    lib.photons_kdk_step_pm_ordered.argtypes = [C.c_void_p, C.POINTER(Params), C.c_int, C.c_int] + \
+        [C.c_void_p] * 5 + [C.c_double, C.c_double]
     _lib = lib
     return lib
 
@@ -205,6 +209,23 @@ class ForcePass:
         _check(self.lib.photons_kdk_step_pm(self.h, C.byref(prm), int(nside), int(n), C.c_void_p(pos_ptr),
                                             C.c_void_p(vel_ptr), C.c_void_p(acc_ptr), C.c_void_p(acc_pm_ptr),
                                             float(dkh), float(dd)))
+        self.n = n
+
+    def kdk_step_ordered_device(self, pos_ptr, vel_ptr, acc_ptr, ids_ptr, n, p, dkh, dd, precision=FP32_SPLIT,
+                                flags=0, nside=0, acc_pm_ptr=0):
+        """The KDK step (with the PM half when nside > 0) keeping pos, vel,
+        acc (acc_pm) and ids (int64, may be 0) in the order of the pass's
+        tree, as the reference keeps part[]; device arrays."""
+        prm = make_params(p, precision, 0, flags | F_DEVICE_IO)
+        if nside:
+            _check(self.lib.photons_kdk_step_pm_ordered(self.h, C.byref(prm), int(nside), int(n), C.c_void_p(pos_ptr),
+                                                        C.c_void_p(vel_ptr), C.c_void_p(acc_ptr),
+                                                        C.c_void_p(acc_pm_ptr), C.c_void_p(ids_ptr or None),
+                                                        float(dkh), float(dd)))
+        else:
+            _check(self.lib.photons_kdk_step_ordered(self.h, C.byref(prm), int(n), C.c_void_p(pos_ptr),
+                                                     C.c_void_p(vel_ptr), C.c_void_p(acc_ptr),
+                                                     C.c_void_p(ids_ptr or None), float(dkh), float(dd)))
         self.n = n
 
     def pm_force(self, pos, p, nside):

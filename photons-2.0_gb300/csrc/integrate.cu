@@ -108,6 +108,50 @@ int enqueue_drift(int n, double *pos, const double *vel, double dd, double L, cu
 
 }  // namespace
 
+namespace {
+
+// positions in tree order from the build's FP64 copies (the same values)
+__global__ void k_pos_from_tree(const double *__restrict__ x, const double *__restrict__ y,
+                                const double *__restrict__ z, int n, double *pos)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        pos[3 * (size_t)i] = x[i];
+        pos[3 * (size_t)i + 1] = y[i];
+        pos[3 * (size_t)i + 2] = z[i];
+    }
+}
+
+// out[i] = in[perm[i]], for records of w 8-byte words
+__global__ void k_permute(const int *__restrict__ perm, const long long *__restrict__ in, int n, int w,
+                          long long *__restrict__ out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const size_t s = (size_t)perm[i] * w, d = (size_t)i * w;
+        for (int k = 0; k < w; k++) out[d + k] = in[s + k];
+    }
+}
+
+// after a pass with PHOTONS_F_TREE_ORDER: positions, velocities and ids
+// (optional) into the pass's tree order, as the reference keeps part[]
+// (src/fmm.c:30-78 permutes whole Body records); acc is already in it
+int reorder_state(photons_ctx *c, int n, double *pos, double *vel, long long *ids, cudaStream_t st)
+{
+    const int blocks = ph::device_sm_count() * 8;
+    ph::note_launch(), k_pos_from_tree<<<blocks, 256, 0, st>>>(c->b.x, c->b.y, c->b.z, n, pos);
+    long long *scratch = reinterpret_cast<long long *>(c->io);  // 3n words, free between passes
+    ph::note_launch(), k_permute<<<blocks, 256, 0, st>>>(c->b.perm, reinterpret_cast<const long long *>(vel), n, 3,
+                                                      scratch);
+    PH_CUDA_CHECK(cudaMemcpyAsync(vel, scratch, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToDevice, st));
+    if (ids) {
+        ph::note_launch(), k_permute<<<blocks, 256, 0, st>>>(c->b.perm, ids, n, 1, scratch);
+        PH_CUDA_CHECK(cudaMemcpyAsync(ids, scratch, sizeof(long long) * (size_t)n, cudaMemcpyDeviceToDevice, st));
+    }
+    PH_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
+}  // namespace
+
 extern "C" double photons_kick_loga(double omega_m, double omega_x, double loga_i, double loga_f)
 {
     return loga_integral(omega_m, omega_x, loga_i, loga_f, 1);
@@ -166,6 +210,52 @@ extern "C" int photons_kdk_step_pm(photons_ctx *c, const photons_params *p, int 
     PH_TRY(photons_force_pass(c, &q, n, pos, acc));
     PH_TRY(ph_pm_enqueue(c, &q, nside, n, pos, acc_pm));
     // src/photoNs.c:257-268: short-range kick, then PM kick
+    PH_TRY(enqueue_kick(n, vel, acc, dkh, st));
+    PH_TRY(enqueue_kick(n, vel, acc_pm, dkh, st));
+    PH_CUDA_CHECK(cudaStreamSynchronize(st));
+    return 0;
+}
+
+// The same steps with the state kept in the order of the last pass's tree:
+// after the short-range pass, pos, vel (and ids, if given) are permuted
+// into tree order and acc comes back in it, so every array stays in one
+// order and the next build starts from nearly sorted particles, as the
+// reference's driver does with part[].  The caller follows particles by ids.
+extern "C" int photons_kdk_step_ordered(photons_ctx *c, const photons_params *p, int n, double *pos, double *vel,
+                                        double *acc, long long *ids, double dkh, double dd)
+{
+    photons_gpu_clear_error();
+    if (!c || !p) return ph_set_error(PH_ERR_ARG, "null argument");
+    cudaSetDevice(c->device);
+    cudaStream_t st = c->stream;
+    PH_TRY(enqueue_kick(n, vel, acc, dkh, st));
+    PH_TRY(enqueue_drift(n, pos, vel, dd, p->boxsize, st));
+    photons_params q = *p;
+    q.flags |= PHOTONS_F_DEVICE_IO | PHOTONS_F_TREE_ORDER;
+    PH_TRY(photons_force_pass(c, &q, n, pos, acc));
+    PH_TRY(reorder_state(c, n, pos, vel, ids, st));
+    PH_TRY(enqueue_kick(n, vel, acc, dkh, st));
+    PH_CUDA_CHECK(cudaStreamSynchronize(st));
+    return 0;
+}
+
+extern "C" int photons_kdk_step_pm_ordered(photons_ctx *c, const photons_params *p, int nside, int n, double *pos,
+                                           double *vel, double *acc, double *acc_pm, long long *ids, double dkh,
+                                           double dd)
+{
+    photons_gpu_clear_error();
+    if (!c || !p || !acc_pm) return ph_set_error(PH_ERR_ARG, "null argument");
+    cudaSetDevice(c->device);
+    cudaStream_t st = c->stream;
+    PH_TRY(enqueue_kick(n, vel, acc_pm, dkh, st));
+    PH_TRY(enqueue_kick(n, vel, acc, dkh, st));
+    PH_TRY(enqueue_drift(n, pos, vel, dd, p->boxsize, st));
+    photons_params q = *p;
+    q.flags |= PHOTONS_F_DEVICE_IO | PHOTONS_F_TREE_ORDER;
+    PH_TRY(photons_force_pass(c, &q, n, pos, acc));
+    PH_TRY(reorder_state(c, n, pos, vel, ids, st));
+    // the PM force at the reordered positions comes out in the same order
+    PH_TRY(ph_pm_enqueue(c, &q, nside, n, pos, acc_pm));
     PH_TRY(enqueue_kick(n, vel, acc, dkh, st));
     PH_TRY(enqueue_kick(n, vel, acc_pm, dkh, st));
     PH_CUDA_CHECK(cudaStreamSynchronize(st));

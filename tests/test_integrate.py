@@ -154,3 +154,77 @@ def test_kdk_step_with_pm_matches_host_composition(ph, port, ics):
     port.kick(hv, acc1, dkh)
     port.kick(hv, gpm, dkh)
     assert np.array_equal(dvel.cpu().numpy(), hv)
+
+
+def _kdk_factors(ph):
+    la, lb = math.log(0.5), math.log(0.505)
+    return 0.5 * ph.kick_loga(0.3, 0.7, la, lb) * 43007.105732, ph.drift_loga(0.3, 0.7, la, lb)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("maxleaf", [16, 64])
+def test_ordered_kdk_step_is_the_step_in_tree_order(ph, ics, maxleaf):
+    """photons_kdk_step_ordered leaves pos, vel, acc and ids in the pass's
+    tree order: after one step from the same state they are the plain
+    step's arrays permuted by ids, bit for bit; over further steps (each
+    build starting from the previous tree order) the trajectories agree to
+    the FP32 rounding of the force."""
+    torch = pytest.importorskip("torch")
+    pos, p = ics.make("zeldovich512", nside=24, maxleaf=maxleaf)
+    n = pos.shape[0]
+    vel = np.random.default_rng(7).standard_normal(pos.shape) * 0.5
+    dkh, dd = _kdk_factors(ph)
+    fa, fb = ph.ForcePass(0), ph.ForcePass(0)
+    acc0 = fa.run(pos, p, precision=ph.FP32_SPLIT)
+    plain = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (pos, vel, acc0)]
+    ordered = [t.clone() for t in plain]
+    ids = torch.arange(n, dtype=torch.int64, device="cuda")
+    torch.cuda.synchronize()
+    for step in range(3):
+        fa.kdk_step_device(*(t.data_ptr() for t in plain), n, p, dkh, dd, precision=ph.FP32_SPLIT)
+        fb.kdk_step_ordered_device(*(t.data_ptr() for t in ordered), ids.data_ptr(), n, p, dkh, dd,
+                                   precision=ph.FP32_SPLIT)
+        torch.cuda.synchronize()
+        idx = ids.cpu().numpy()
+        assert np.array_equal(np.sort(idx), np.arange(n))
+        got = [t.cpu().numpy() for t in ordered]
+        want = [t.cpu().numpy()[idx] for t in plain]
+        if step == 0:
+            for g, w in zip(got, want):
+                assert np.array_equal(g, w)
+        else:
+            L = p["boxsize"]
+            dpos = np.abs(got[0] - want[0])
+            dpos = np.minimum(dpos, L - dpos)  # periodic
+            assert dpos.max() <= 1e-9 * L
+            e = np.linalg.norm(got[2] - want[2], axis=1) / np.linalg.norm(want[2], axis=1)
+            assert np.median(e) <= 1e-5
+
+
+@pytest.mark.gpu
+def test_ordered_kdk_step_with_pm(ph, ics):
+    torch = pytest.importorskip("torch")
+    pos, p = ics.make("zeldovich512", nside=24, maxleaf=64)
+    n, nside = pos.shape[0], 24
+    vel = np.random.default_rng(9).standard_normal(pos.shape) * 0.5
+    dkh, dd = _kdk_factors(ph)
+    fa, fb = ph.ForcePass(0), ph.ForcePass(0)
+    acc0 = fa.run(pos, p, precision=ph.FP32_SPLIT)
+    pm0 = fa.pm_force(pos, p, nside)
+    plain = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (pos, vel, acc0, pm0)]
+    ordered = [t.clone() for t in plain]
+    ids = torch.arange(n, dtype=torch.int64, device="cuda")
+    torch.cuda.synchronize()
+    fa.kdk_step_pm_device(*(t.data_ptr() for t in plain), n, p, nside, dkh, dd, precision=ph.FP32_SPLIT)
+    fb.kdk_step_ordered_device(ordered[0].data_ptr(), ordered[1].data_ptr(), ordered[2].data_ptr(), ids.data_ptr(),
+                               n, p, dkh, dd, precision=ph.FP32_SPLIT, nside=nside,
+                               acc_pm_ptr=ordered[3].data_ptr())
+    torch.cuda.synchronize()
+    idx = ids.cpu().numpy()
+    got = [t.cpu().numpy() for t in ordered]
+    want = [t.cpu().numpy()[idx] for t in plain]
+    assert np.array_equal(got[0], want[0])
+    assert np.array_equal(got[2], want[2])
+    # the PM deposit adds with atomics: its last bits vary between runs
+    assert np.abs(got[3] - want[3]).max() <= 1e-12 * np.abs(want[3]).max()
+    assert np.abs(got[1] - want[1]).max() <= 1e-12 * np.abs(want[1]).max()
