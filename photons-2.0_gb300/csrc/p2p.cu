@@ -20,9 +20,12 @@
 // lane's partial sum over one staged batch is added to its running sum with
 // Kahan compensation.
 //
-// FP64 variant: the reference's arithmetic (sqrt, division, erfc, exp) on
-// absolute FP64 positions, image positions formed as pos + shift like the
-// exported bodies of src/remotes.c:83-89, self pair skipped by index.
+// FP64 variant: the reference's pair force in FP64 on absolute positions,
+// image positions formed as pos + shift like the exported bodies of
+// src/remotes.c:83-89, self pair skipped by index.  1/r comes from rsqrt and
+// erfc(u) + (2/sqrt(pi)) u exp(-u^2) from exp(-u^2) (erfcx(u) + ...), one
+// exponential, which is fewer FP64 operations than the reference's sqrt,
+// division, erfc and exp and agrees with them to ~1e-15 relative.
 #include <cmath>
 
 #include "fmm_context.cuh"
@@ -36,6 +39,9 @@
 
 #ifndef P2P_MINB
 #define P2P_MINB 3  // resident blocks per SM the packed kernel is compiled for (80 registers)
+#endif
+#ifndef P2P_FP64_FAST
+#define P2P_FP64_FAST 1  // 0: sqrt, division, erfc and exp as written in the reference
 #endif
 #ifndef P2P_DUAL_UNROLL
 #define P2P_DUAL_UNROLL 2  // two source pairs per step of the dual sweep: four independent chains per lane
@@ -598,6 +604,7 @@ __global__ void __launch_bounds__(P2P_TB) k_p2p_fp64(P2PArgs A)
         const BoxParams &B = A.boxes[A.boxid[t]];
         const double eps = B.eps, mass = B.mass, rs = B.rs, boxL = B.boxsize;
         const double soft3 = mass / (eps * eps * eps);
+        const double hrs = 0.5 / rs;  // u = r / (2 rs)
         const long long eoff = A.p2p_off[t];
         const int ecnt = A.p2p_cnt[t];
         for (int r0 = 0; r0 < nt; r0 += 32) {
@@ -645,10 +652,22 @@ __global__ void __launch_bounds__(P2P_TB) k_p2p_fp64(P2PArgs A)
                         Src64 sj = src[j];
                         if (sj.idx == ip) continue;
                         double dx = sj.x - px, dy = sj.y - py, dz = sj.z - pz;
+#if P2P_FP64_FAST
+                        // the same quantities with fewer FP64 operations (GB300's FP64
+                        // rate is 1/64 of FP32): 1/r from rsqrt, and erfc(u) + c u
+                        // exp(-u^2) as exp(-u^2) (erfcx(u) + c u), one exponential
+                        const double r2 = dx * dx + dy * dy + dz * dz;
+                        const double rinv = rsqrt(r2);
+                        const double dr = r2 * rinv;
+                        double ir3 = (dr < eps) ? soft3 : mass * (rinv * rinv * rinv);
+                        const double drs = dr * hrs;
+                        ir3 *= exp(-drs * drs) * (erfcx(drs) + coeff * drs);
+#else
                         double dr = sqrt(dx * dx + dy * dy + dz * dz);
                         double ir3 = (dr < eps) ? soft3 : mass / (dr * dr * dr);
                         double drs = 0.5 * dr / rs;
                         ir3 *= (erfc(drs) + coeff * drs * exp(-drs * drs));
+#endif
                         ax += dx * ir3;
                         ay += dy * ir3;
                         az += dz * ir3;
