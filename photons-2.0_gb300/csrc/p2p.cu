@@ -48,7 +48,7 @@
 #endif
 constexpr int kDualUnroll = P2P_DUAL_UNROLL;
 #ifndef P2P_ROUND_UNROLL
-#define P2P_ROUND_UNROLL 2
+#define P2P_ROUND_UNROLL 4  // source pairs per step of a single round (leaves of up to 32 in one-way passes)
 #endif
 constexpr int kRoundUnroll = P2P_ROUND_UNROLL;
 
