@@ -174,7 +174,6 @@ __global__ void __launch_bounds__(WALK_TB, MINB) k_walk_level(WalkArgs A)
     const int lane = warp_lane();
     const unsigned lt = (1u << lane) - 1u;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
     if (gw >= W.nwarps) return;
     uint32_t *stack = W.scratch + (size_t)gw * (W.stack_cap + 3 * W.stage_cap);
     uint32_t *st_p2p = stack + W.stack_cap;
@@ -192,7 +191,13 @@ __global__ void __launch_bounds__(WALK_TB, MINB) k_walk_level(WalkArgs A)
     unsigned flags = 0;
     int max_stack = 0, max_stage = 0;
 
-    for (int ti = list_begin + gw; ti < list_end; ti += nw) {
+    // targets are handed out one at a time (their lists differ in length by
+    // more than tenfold on clustered input); each is expanded by one warp
+    for (;;) {
+        unsigned long long tk = 0;
+        if (lane == 0) tk = atomicAdd(&W.ctr[WC_WORK], 1ULL);
+        const long long ti = list_begin + (long long)__shfl_sync(0xffffffffu, tk, 0);
+        if (ti >= list_end) break;
         const int a = A.depth_list[ti];
         const bool leaf_a = a < nleaf;
         // the target's box: its root (the receiving domain of the image
@@ -430,6 +435,7 @@ __global__ void k_walk_level_done(WalkBufs W, int depth)
         unsigned long long f = W.ctr[WC_PD_FILL0 + (depth & 1)];
         if (f > W.ctr[WC_PD_MAX]) W.ctr[WC_PD_MAX] = f;
         W.ctr[WC_PD_FILL0 + ((depth + 1) & 1)] = 0;
+        W.ctr[WC_WORK] = 0;
     }
 }
 
