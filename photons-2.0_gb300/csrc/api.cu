@@ -685,6 +685,7 @@ static ph::MultipoleArgs multipole_args(photons_ctx *c)
     a.ax = c->ax; a.ay = c->ay; a.az = c->az;
     a.boxid = c->t.boxid;
     a.boxes = c->b.boxes;
+    a.work = c->work_counter + 1;
     a.gate_m = c->capturing ? c->far_gate : nullptr;
     a.gate_l = c->capturing ? c->far_gate + 1 : nullptr;
     return a;

@@ -358,12 +358,21 @@ __global__ void k_m_to_f32(const double *M, float *M32, const int *tree_cnt, con
         M32[i] = (float)M[i];
 }
 
+// one warp per target (lists differ in length by orders of magnitude on
+// clustered input; targets are handed out one at a time): lanes take the
+// entries k = lane, lane + 32, ...; their partial expansions are combined
+// by a fixed butterfly (lane 0's result) and added to the FP64 L
 __global__ void k_m2l_f32(const int *tree_cnt, const unsigned long long *walk_flags, const uint32_t *pool,
                           const long long *off, const int *cnt, const float4 *chi, const float4 *clo, const float *M32,
-                          double *Lout, const int *boxid, const BoxParams *boxes, FarConsts F)
+                          double *Lout, const int *boxid, const BoxParams *boxes, FarConsts F, int *work)
 {
     const int nunified = *walk_flags ? 0 : tree_cnt[BC_LEAVES] + tree_cnt[BC_NODES];
-    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nunified; u += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int u = 0;
+        if (lane == 0) u = atomicAdd(work, 1);
+        u = __shfl_sync(0xffffffffu, u, 0);
+        if (u >= nunified) break;
         const int n = cnt[u];
         if (n == 0) continue;
         float L[PH_NMULTI];
@@ -376,7 +385,7 @@ __global__ void k_m2l_f32(const int *tree_cnt, const unsigned long long *walk_fl
         F.Lhi = B.Lhi;
         F.Llo = B.Llo;
         const long long o = off[u];
-        for (int k = 0; k < n; k++) {
+        for (int k = lane; k < n; k += 32) {
             const uint32_t e = pool[o + k];
             const int s = PH_ENTRY_ID(e), img = PH_ENTRY_IMG(e);
             int mi, mj, mk;
@@ -391,7 +400,16 @@ __global__ void k_m2l_f32(const int *tree_cnt, const unsigned long long *walk_fl
             m2l_add_f32(dx, dy, dz, Ms, F, L);
         }
 #pragma unroll
-        for (int a = 0; a < PH_NMULTI; a++) Lout[(size_t)u * PH_NMULTI + a] += (double)L[a];
+        for (int a = 0; a < PH_NMULTI; a++) {
+            float v = L[a];
+#pragma unroll
+            for (int w = 16; w > 0; w >>= 1) v += __shfl_xor_sync(0xffffffffu, v, w);
+            L[a] = v;
+        }
+        if (lane == 0) {
+#pragma unroll
+            for (int a = 0; a < PH_NMULTI; a++) Lout[(size_t)u * PH_NMULTI + a] += (double)L[a];
+        }
     }
 }
 
@@ -495,8 +513,10 @@ int run_m2l_f32(const MultipoleArgs &a, float *M32, cudaStream_t st)
     FarConsts F;  // per-box fields are filled per target from the box table
     F.a = F.pa = F.Lhi = F.Llo = 0.f;
     for (int i = 0; i < SPLIT_NA; i++) F.c[i] = (float)SPLIT_A[i];
+    PH_CUDA_CHECK(cudaMemsetAsync(a.work, 0, sizeof(int), st));
     ph::note_launch(), k_m2l_f32<<<grid_cap(), MP_TB, 0, st>>>(a.tree_cnt, a.walk_flags, a.m2l_pool, a.m2l_off,
-                                                                 a.m2l_cnt, a.chi, a.clo, M32, a.L, a.boxid, a.boxes, F);
+                                                                 a.m2l_cnt, a.chi, a.clo, M32, a.L, a.boxid, a.boxes, F,
+                                                                 a.work);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }

@@ -25,6 +25,7 @@ struct MultipoleArgs {
     // device switches (null: always run): gate_m for P2M/M2M, gate_l for
     // M2L/L2L/L2P; set by launch_far_gate from the walk's M2L count
     const int *gate_m, *gate_l;
+    int *work;  // device counter of the split M2L's targets
 };
 
 // M2L of every list, accumulated into L
