@@ -95,10 +95,16 @@ static void dfree(T *&p)
 #define CHUNK_ELEMS 1024
 #define MAX_DEPTH_CAP 2048
 
+// Each grow below first marks its capacity empty and bumps the epoch, then
+// sets the capacity only after every allocation succeeded: a failed
+// cudaMalloc leaves null buffers that the next pass reallocates, never a
+// recorded capacity over a freed buffer (or a captured graph that uses one).
 static int alloc_particles(photons_ctx *c, int n)
 {
     if (n <= c->cap_n) return 0;
     ph::BuildBufs &b = c->b;
+    c->cap_n = b.cap_n = 0;
+    c->epoch++;
     PH_TRY(dalloc(b.x, n)); PH_TRY(dalloc(b.y, n)); PH_TRY(dalloc(b.z, n));
     PH_TRY(dalloc(b.perm, n)); PH_TRY(dalloc(b.smallpos, n)); PH_TRY(dalloc(b.bigslot, n));
     PH_TRY(dalloc(c->pos4, n));
@@ -115,6 +121,10 @@ static int alloc_tree(photons_ctx *c, int n, int cap)
     int chunks = n / CHUNK_ELEMS + cap + 2;
     ph::BuildBufs &b = c->b;
     if (cap > b.cap_nodes) {
+        b.cap_nodes = b.cap_leaves = 0;
+        c->t.cap_u = c->cap_u = c->mu_cap_leaves = 0;
+        b.scan_scratch_elems = 0;
+        c->epoch++;
         PH_TRY(dalloc(b.tn_start, cap)); PH_TRY(dalloc(b.tn_len, cap)); PH_TRY(dalloc(b.tn_depth, cap));
         PH_TRY(dalloc(b.tn_parent, cap)); PH_TRY(dalloc(b.tn_child0, cap)); PH_TRY(dalloc(b.tn_child1, cap));
         PH_TRY(dalloc(b.tn_mode, cap)); PH_TRY(dalloc(b.tn_S, cap)); PH_TRY(dalloc(b.tn_box, (size_t)6 * cap));
@@ -125,8 +135,9 @@ static int alloc_tree(photons_ctx *c, int n, int cap)
         PH_TRY(dalloc(b.tl_start, cap)); PH_TRY(dalloc(b.tl_len, cap)); PH_TRY(dalloc(b.tl_depth, cap));
         PH_TRY(dalloc(b.tl_parent, cap)); PH_TRY(dalloc(b.tl_final, cap)); PH_TRY(dalloc(b.tl_box, (size_t)6 * cap));
         PH_TRY(dalloc(b.tn_boxid, cap)); PH_TRY(dalloc(b.tl_boxid, cap));
-        b.scan_scratch_elems = ph::scan_scratch_elems(cap > chunks ? cap : chunks) + 8;
-        PH_TRY(dalloc(b.scan_scratch, b.scan_scratch_elems));
+        const size_t scratch = ph::scan_scratch_elems(cap > chunks ? cap : chunks) + 8;
+        PH_TRY(dalloc(b.scan_scratch, scratch));
+        b.scan_scratch_elems = scratch;
         PH_TRY(dalloc(b.cnt, ph::BC_NCOUNTERS));
         PH_TRY(dalloc(b.lvl_begin, MAX_DEPTH_CAP + 2)); PH_TRY(dalloc(b.lvl_count, MAX_DEPTH_CAP + 2));
         PH_TRY(dalloc(b.leaf_begin, MAX_DEPTH_CAP + 2)); PH_TRY(dalloc(b.leaf_count, MAX_DEPTH_CAP + 2));
@@ -156,7 +167,7 @@ static int alloc_tree(photons_ctx *c, int n, int cap)
         PH_TRY(dalloc(c->mu_sorted, cu)); PH_TRY(dalloc(c->mu_nrecv, cu)); PH_TRY(dalloc(c->mu_nev, cu));
         PH_TRY(dalloc(c->mu_size, cu)); PH_TRY(dalloc(c->mu_rbase, cu));
         PH_TRY(dalloc(c->mu_scan, ph::scan_scratch_elems(cu) + 8));
-        if (!c->mu_total) { PH_TRY(dalloc(c->mu_total, 1)); PH_TRY(dalloc(c->mu_over, 1)); }
+        if (!c->mu_total || !c->mu_over) { PH_TRY(dalloc(c->mu_total, 1)); PH_TRY(dalloc(c->mu_over, 1)); }
         c->mu_cap_leaves = cu;
         PH_TRY(dalloc(c->M, (size_t)cu * PH_NMULTI));
         PH_TRY(dalloc(c->L, (size_t)cu * PH_NMULTI));
@@ -164,15 +175,17 @@ static int alloc_tree(photons_ctx *c, int n, int cap)
         c->cap_u = cu;
     }
     if (chunks > b.cap_chunks) {
+        b.cap_chunks = 0;
+        c->epoch++;
         PH_TRY(dalloc(b.ch_partial, chunks)); PH_TRY(dalloc(b.ch_cnt, chunks)); PH_TRY(dalloc(b.ch_small_base, chunks));
         PH_TRY(dalloc(b.ch_node, chunks));
         c->epoch++;
         b.cap_chunks = chunks;
         size_t need = ph::scan_scratch_elems(cap > chunks ? cap : chunks) + 8;
         if (need > b.scan_scratch_elems) {
-            b.scan_scratch_elems = need;
+            b.scan_scratch_elems = 0;
             PH_TRY(dalloc(b.scan_scratch, need));
-            c->epoch++;
+            b.scan_scratch_elems = need;
         }
     }
     return 0;
@@ -186,23 +199,34 @@ static int alloc_walk(photons_ctx *c, long long p2p_cap, long long pd_cap, long 
     if (!c->far_gate) { PH_TRY(dalloc(c->far_gate, 2)); c->epoch++; }
     if (!c->work_counter) { PH_TRY(dalloc(c->work_counter, 4)); c->epoch++; }
     if (p2p_cap > w.p2p_cap) {
+        w.p2p_cap = 0;
+        c->epoch++;
         PH_TRY(dalloc(w.p2p_pool, p2p_cap));
         w.p2p_cap = p2p_cap;
         c->epoch++;
     }
     if (pd_cap > w.pd_cap) {
+        w.pd_cap = 0;
+        c->epoch++;
         PH_TRY(dalloc(w.pd_pool[0], pd_cap));
         PH_TRY(dalloc(w.pd_pool[1], pd_cap));
         w.pd_cap = pd_cap;
         c->epoch++;
     }
-    if (m2l_cap > w.m2l_cap) { PH_TRY(dalloc(w.m2l_pool, m2l_cap)); w.m2l_cap = m2l_cap; c->epoch++; }
+    if (m2l_cap > w.m2l_cap) {
+        w.m2l_cap = 0;
+        c->epoch++;
+        PH_TRY(dalloc(w.m2l_pool, m2l_cap));
+        w.m2l_cap = m2l_cap;
+    }
     // resident 256-thread walk blocks per SM: 2 (no register spills) or 3
     const char *wb = getenv("PHOTONS_WALK_BLOCKS");
     int nwarps = ph::device_sm_count() * ((wb && atoi(wb) == 3) ? 3 : 2) * 8;
     if (stack_cap > w.stack_cap || stage_cap > w.stage_cap || nwarps != w.nwarps) {
         if (stack_cap < w.stack_cap) stack_cap = w.stack_cap;
         if (stage_cap < w.stage_cap) stage_cap = w.stage_cap;
+        w.stack_cap = w.stage_cap = w.nwarps = 0;
+        c->epoch++;
         PH_TRY(dalloc(w.scratch, (size_t)nwarps * (stack_cap + 3 * (size_t)stage_cap)));
         c->epoch++;
         w.stack_cap = stack_cap;
@@ -309,6 +333,8 @@ static int alloc_mutual(photons_ctx *c, int precision)
         return 0;
     }
     if (c->w.p2p_cap > c->mu_slot_cap) {
+        c->mu_slot_cap = 0;
+        c->epoch++;
         PH_TRY(dalloc(c->mu_slot, (size_t)c->w.p2p_cap));
         PH_TRY(dalloc(c->mu_ev, (size_t)c->w.p2p_cap));
         PH_TRY(dalloc(c->mu_pq, (size_t)c->w.p2p_cap));
@@ -316,6 +342,8 @@ static int alloc_mutual(photons_ctx *c, int precision)
         c->epoch++;
     }
     if (want > c->mu_buf_cap) {
+        c->mu_buf_cap = 0;
+        c->epoch++;
         PH_TRY(dalloc(c->mu_buf, (size_t)want));
         c->mu_buf_cap = want;
         c->epoch++;
@@ -433,6 +461,8 @@ static int ph_prepare_boxes(photons_ctx *c, int nbox, const photons_params *p, c
     PH_TRY(alloc_particles(c, (int)n));
     PH_TRY(alloc_tree(c, (int)n, (int)cap));
     if (nbox > c->cap_box) {
+        c->cap_box = 0;
+        c->epoch++;
         PH_TRY(dalloc(c->b.boxes, nbox));
         c->cap_box = nbox;
         c->epoch++;
@@ -1164,6 +1194,7 @@ extern "C" int photons_list_copy(photons_ctx *c, int kind, int *target, int *sou
     std::vector<int> t, s, im;
     long long n = 0;
     PH_TRY(collect_lists(c, kind, &t, &s, &im, &n));
+    if (n && (!target || !source || !image)) return ph_set_error(PH_ERR_ARG, "null list arrays");
     if (n) {
         memcpy(target, t.data(), sizeof(int) * n);
         memcpy(source, s.data(), sizeof(int) * n);
@@ -1184,12 +1215,13 @@ extern "C" int photons_op_batch(int op, int n, const double *d, const double *in
         dfree(dd); dfree(di); dfree(dio);
         return rc;
     }
-    cudaMemcpy(dd, d, sizeof(double) * 3 * n, cudaMemcpyHostToDevice);
-    cudaMemcpy(di, in, sizeof(double) * PH_NMULTI * n, cudaMemcpyHostToDevice);
-    cudaMemcpy(dio, inout, sizeof(double) * PH_NMULTI * n, cudaMemcpyHostToDevice);
-    rc = ph::launch_op_batch(op, n, dd, di, dio, rs, 0);
+    cudaError_t e = cudaMemcpy(dd, d, sizeof(double) * 3 * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(di, in, sizeof(double) * PH_NMULTI * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dio, inout, sizeof(double) * PH_NMULTI * n, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) rc = ph_set_cuda_error(e, "cudaMemcpy", __FILE__, __LINE__);
+    if (!rc) rc = ph::launch_op_batch(op, n, dd, di, dio, rs, 0);
     if (!rc) {
-        cudaError_t e = cudaMemcpy(inout, dio, sizeof(double) * PH_NMULTI * n, cudaMemcpyDeviceToHost);
+        e = cudaMemcpy(inout, dio, sizeof(double) * PH_NMULTI * n, cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) rc = ph_set_cuda_error(e, "cudaMemcpy", __FILE__, __LINE__);
     }
     dfree(dd); dfree(di); dfree(dio);
