@@ -1180,7 +1180,8 @@ __global__ void __launch_bounds__(MU_TB, MINB) k_p2p_mutual(P2PArgs A, const int
 // holds [3][r] floats at rbase[t] + 3 k r (r = nt rounded up to 32).  Which
 // entries are received is read once per 32 as a warp mask, and eight
 // slots' loads are in flight at a time.
-__global__ void k_mu_gather(P2PArgs A, const int *slot, const int *nrecv, const long long *rbase, const float *rbuf)
+// 3 resident blocks of 256 threads per SM (80 registers); launched as one wave
+__global__ void __launch_bounds__(256, 3) k_mu_gather(P2PArgs A, const int *slot, const int *nrecv, const long long *rbase, const float *rbuf)
 {
     const int lane = warp_lane();
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
@@ -1193,6 +1194,61 @@ __global__ void k_mu_gather(P2PArgs A, const int *slot, const int *nrecv, const 
         const double scale = A.boxes[A.boxid[t]].acc_scale;
         const int rl = mu_row(nt);
         const long long stride = 3LL * rl;
+        if (rl == 64) {
+            // 33-64 particles: lane takes particles 2 lane and 2 lane + 1, one
+            // float2 per component row, so one sweep of the list serves the
+            // whole leaf with twice the bytes in flight per load.  Rows are
+            // padded to 64 floats (in bounds for every lane) and every
+            // particle's sum runs over the same slots in the same order as
+            // below.  rbase and the rows are multiples of 32 floats: float2
+            // aligned.
+            const float2 *base = reinterpret_cast<const float2 *>(rbuf + rbase[t]) + lane;
+            const long long stride2 = stride / 2;
+            float2 v0 = make_float2(0.f, 0.f), v1 = v0, v2 = v0, c0 = v0, c1 = v0, c2 = v0;
+            int k = 0;
+            for (int e0 = 0; e0 < L && k < nr; e0 += 32) {
+                unsigned got = __ballot_sync(0xffffffffu, e0 + lane < L && slot[eoff + e0 + lane] == -2);
+                while (got) {
+                    float2 in[8][3];
+                    int cntk = 0;
+#pragma unroll
+                    for (int q = 0; q < 8; q++) {
+                        const bool use = got != 0;
+                        if (use) got &= got - 1;
+                        cntk += use;
+                        const float2 *src = base + (long long)(k + q) * stride2;
+                        const float2 z = make_float2(0.f, 0.f);
+                        in[q][0] = use ? src[0] : z;
+                        in[q][1] = use ? src[32] : z;
+                        in[q][2] = use ? src[64] : z;
+                    }
+#pragma unroll
+                    for (int q = 0; q < 8; q++) {
+                        if (q < cntk) {
+                            kahan_add(v0.x, c0.x, in[q][0].x);
+                            kahan_add(v0.y, c0.y, in[q][0].y);
+                            kahan_add(v1.x, c1.x, in[q][1].x);
+                            kahan_add(v1.y, c1.y, in[q][1].y);
+                            kahan_add(v2.x, c2.x, in[q][2].x);
+                            kahan_add(v2.y, c2.y, in[q][2].y);
+                        }
+                    }
+                    k += cntk;
+                }
+            }
+            const int j = 2 * lane;
+            if (j < nt) {
+                A.ax[it + j] += ((double)v0.x - (double)c0.x) * scale;
+                A.ay[it + j] += ((double)v1.x - (double)c1.x) * scale;
+                A.az[it + j] += ((double)v2.x - (double)c2.x) * scale;
+            }
+            if (j + 1 < nt) {
+                A.ax[it + j + 1] += ((double)v0.y - (double)c0.y) * scale;
+                A.ay[it + j + 1] += ((double)v1.y - (double)c1.y) * scale;
+                A.az[it + j + 1] += ((double)v2.y - (double)c2.y) * scale;
+            }
+            continue;
+        }
         for (int j0 = 0; j0 < nt; j0 += 32) {
             const int j = j0 + lane;
             const float *base = rbuf + rbase[t] + j;
@@ -1291,7 +1347,7 @@ int launch_p2p_mutual(const P2PArgs &a, const MutualBufs &m, cudaStream_t st)
     else
         ph::note_launch(), k_p2p_mutual<MU_NARROW_MINB, MU_NARROW_IL, true>
             <<<sms * MU_NARROW_MINB, MU_TB, 0, st>>>(a, m.ev, m.nev, m.rbase, m.buf);
-    ph::note_launch(), k_mu_gather<<<sms * 8, 256, 0, st>>>(a, m.slot, m.nrecv, m.rbase, m.buf);
+    ph::note_launch(), k_mu_gather<<<sms * 3, 256, 0, st>>>(a, m.slot, m.nrecv, m.rbase, m.buf);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }
