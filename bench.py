@@ -38,6 +38,10 @@ UNIT = "particle-forces/s"
 # conventional count for a softened, erfc-truncated pair force); the P2P
 # roofline is this times the pairs, over the P2P phase time
 FLOPS_PER_PAIR = 36
+# MAXLEAF the GPU arm's autotuner picks for each workload on GB300 (the
+# fastest leaf within the 1e-4 median error bound); the CPU baselines run
+# the same leaf so that both arms compute the same lists at the same error
+CHOSEN_LEAF = {"zeldovich256": 64, "zeldovich512": 64, "nfw128": 24, "grid32": 16}
 
 
 def parse():
@@ -152,9 +156,10 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_baseline(nthreads=None, target_s=10.0):
+def cpu_baseline(nthreads=None, target_s=10.0, maxleaf=64, name="zeldovich256"):
     """The oracle's CPU restatement of the pass, all host threads, on a bounded
-    sample of the same workload (same density and clustering, smaller box)."""
+    sample of the same workload (same density, clustering and MAXLEAF,
+    smaller box)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
 
@@ -163,15 +168,15 @@ def cpu_baseline(nthreads=None, target_s=10.0):
     nthreads = nthreads or os.cpu_count() or 1
     nside = 48
     while True:
-        pos, p = workload(nside, 16)
+        pos, p = workload(nside, maxleaf, name=name)
         r = port.run(pos, p, capture=False, tree=False, nthreads=nthreads)
         secs = r["seconds"]
         if secs * 2.5 > target_s or nside >= 96:
             break
         nside = min(96, int(nside * (target_s / max(secs, 1e-3)) ** (1 / 3.0) * 0.9) // 8 * 8 or nside + 16)
     return {"value": pos.shape[0] / secs, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": "one full pass of the same workload at %d^3 (L=%.1f, leaf 16, reference rules) "
-                      "on the host: %.2f s" % (nside, p["boxsize"], secs)}
+            "sample": "one full pass of the same workload at %d^3 (L=%.1f, leaf %d, reference rules) "
+                      "on the host: %.2f s" % (nside, p["boxsize"], maxleaf, secs)}
 
 
 def run_reference_arm(args):
@@ -185,7 +190,9 @@ def run_reference_arm(args):
     port = oracle.PortOracle(build=False)
     nthreads = os.cpu_count() or 1
     nside = 64
-    pos, p = workload(nside, 16)
+    name = args.workload if args.workload in CHOSEN_LEAF else "zeldovich256"
+    leaf = args.maxleaf or CHOSEN_LEAF[name]
+    pos, p = workload(nside, leaf, name=name)
     for _ in range(max(0, args.warmup)):
         port.run(pos, p, capture=False, tree=False, nthreads=nthreads)
     t = []
@@ -197,8 +204,8 @@ def run_reference_arm(args):
     line = {"metric": METRIC, "impl": "reference", "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": secs * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "zeldovich256 sample at %d^3 (same density/clustering), leaf 16" % nside,
-                       "n": int(pos.shape[0]), "boxsize": p["boxsize"], "theta": 0.5},
+            "config": {"workload": "%s sample at %d^3 (same density/clustering)" % (name, nside),
+                       "n": int(pos.shape[0]), "boxsize": p["boxsize"], "maxleaf": leaf, "theta": 0.5},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
                              "sample": "each step one full pass at %d^3 on %d host threads (the reference's "
                                        "algorithm restated in C; the reference sources are not on this host)"
@@ -605,7 +612,7 @@ def main():
                 "fp32_median": float(np.median(a32)), "fp32_p99": float(np.percentile(a32, 99)),
                 "fp64_median": float(np.median(a64)), "fp64_p99": float(np.percentile(a64, 99)),
                 "direct_sum": "FP64 GPU, untruncated erfc kernel, all sources within 2 rcut, minimum image"}}
-    cpu = None if args.no_cpu else cpu_baseline()
+    cpu = None if args.no_cpu else cpu_baseline(maxleaf=p["maxleaf"], name=args.workload)
 
     tmean = {k: float(np.mean([t[k] for t in phase])) for k in phase[0]}
     line = {
