@@ -3,8 +3,9 @@ INFRASTRUCTURE ONLY: tests/ use it to check the GPU PM (photons_pm_force).
 
 Follows src/partmesh.c (one rank: CIC deposit :86-180, the 4-point gradient
 :524-735, CIC interpolation :574-587) and the convolution of
-src/conv.f90:128-247 (Green's function :171-227, pi = 3.1415926 as the
-Fortran declares it).  numpy float64 arithmetic rounds every operation on
+src/conv.f90:128-247 (Green's function :171-227, with its pi: the Fortran
+declares `real*8, parameter :: M_PI = 3.1415926`, a default-kind, i.e.
+single-precision, literal, so pi is 3.1415926 rounded to FP32).  numpy float64 arithmetic rounds every operation on
 its own, in the reference's order; the FFT is numpy's, so results differ
 from the reference's 2DECOMP&FFT (and from cuFFT) in the last bits.  The
 reference's PM needs 2DECOMP&FFT (Fortran), which does not build here:
@@ -15,7 +16,7 @@ from __future__ import annotations
 
 import numpy as np
 
-PM_PI = 3.1415926
+PM_PI = float(np.float32(3.1415926))  # 3.141592502593994
 
 
 def _axis(x, norm, delta, N):

@@ -12,7 +12,9 @@
 //      acc_pm = grad psi (src/partmesh.c:574-587).
 // The mesh arithmetic is FP64 in the reference's order, every product and
 // sum rounded on its own except the interpolation sums (fused multiply-adds);
-// the constant pi is the reference's 3.1415926.
+// the constant pi is the reference's: conv.f90 declares
+// `real*8, parameter :: M_PI = 3.1415926`, a default (single-precision)
+// real literal, so its value is 3.1415926 rounded to FP32 (3.141592502593994).
 // The deposit adds with FP64 atomics, so its summation order (and the last
 // bits of the density) varies from run to run.
 #include <cufft.h>
@@ -23,7 +25,7 @@
 
 namespace {
 
-constexpr double PM_PI = 3.1415926;  // conv.f90 declares M_PI = 3.1415926
+constexpr double PM_PI = (double)3.1415926f;  // src/conv.f90:171
 
 struct Cic {
     int i, j, k, ii, jj, kk;
