@@ -129,6 +129,15 @@ class RefOracle(_Base):
         keys = ("boxsize", "npart_total", "mass", "omega0", "omega_lambda", "hubble", "redshift")
         return dict(zip(keys, h.tolist())), pos, vel
 
+    def pm_force(self, pos, boxsize, nside, rs, mass):
+        """acc_pm (n, 3) of the reference's own PM (src/partmesh.c, one rank),
+        with the Fortran convolution replaced by oracle/pm_conv.c."""
+        pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+        out = np.empty_like(pos)
+        self.lib.ref_pm_force.argtypes = [C.c_int, _dp, C.c_double, C.c_int, C.c_double, C.c_double, _dp]
+        self.lib.ref_pm_force(pos.shape[0], _ptr(pos), float(boxsize), int(nside), float(rs), float(mass), _ptr(out))
+        return out
+
     def kick_loga(self, om, ox, la, lb):
         return self.lib.ref_kick_loga(om, ox, la, lb)
 

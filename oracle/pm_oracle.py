@@ -8,9 +8,12 @@ declares `real*8, parameter :: M_PI = 3.1415926`, a default-kind, i.e.
 single-precision, literal, so pi is 3.1415926 rounded to FP32).  numpy float64 arithmetic rounds every operation on
 its own, in the reference's order; the FFT is numpy's, so results differ
 from the reference's 2DECOMP&FFT (and from cuFFT) in the last bits.  The
-reference's PM needs 2DECOMP&FFT (Fortran), which does not build here:
-parity unpinned against a reference binary; pinned by this restatement and
-by the physics test (PM + short-range force = Newtonian force).
+reference's PM needs 2DECOMP&FFT (Fortran), which does not build here, so
+the pin is partial: src/partmesh.c itself is compiled in place
+(oracle/Makefile) with the Fortran convolution replaced by a C stand-in
+(oracle/pm_conv.c), and this restatement matches it to 3e-15 of the largest
+force (tests/golden/pm/, made by tests/golden/make_golden.py).  The
+convolution's Green's function is a restatement on both sides.
 """
 from __future__ import annotations
 

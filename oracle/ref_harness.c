@@ -309,3 +309,44 @@ void ref_gadget_read(const char *path, int n, double *pos, double *vel)
     free(part);
     part = saved;
 }
+
+/*
+ * The reference's PM at one rank: src/partmesh.c:18-795 (partmesh_thread,
+ * the branch its Makefile builds with -DPMTHREAD -DMYALLTOALLV) on the
+ * reference's globals, with the pencil decomposition of one rank and an
+ * nside^3 mesh set up as src/initial.c:453-493 would (local start 0, end
+ * nside - 1 as get_local_size returns them, size nside), and the Fortran
+ * convolution replaced by oracle/pm_conv.c.  acc_pm[3n] out.
+ */
+void partmesh_thread(void);
+extern MPI_Comm PM_COMM_WORLD;  /* inc/photoNs.h:311-313, declared under PMTHREAD */
+void ref_pm_force(int npart, const double *pos, double boxsize, int nside, double rs, double mass, double *acc_pm)
+{
+    static int msize0, msize1;
+    Body *saved = part;
+    int saved_n = NPART;
+    part = (Body *)calloc((size_t)npart, sizeof(Body));
+    for (int n = 0; n < npart; n++)
+        for (int d = 0; d < 3; d++) part[n].pos[d] = pos[3 * n + d];
+    MPI_Type_contiguous(sizeof(MKey), MPI_CHAR, &strMKey);
+    PM_COMM_WORLD = MPI_COMM_WORLD;
+    PROC_SIZE = 1; PROC_RANK = 0;
+    NPART = npart; BOXSIZE = boxsize; NSIDE = nside; splitRadius = rs; MASSPART = mass;
+    vproc[0] = vproc[1] = 1;
+    pside[0] = pside[1] = nside;
+    for (int d = 0; d < 3; d++) {
+        local_xstart[d] = 0;
+        local_xend[d] = nside - 1;
+        local_xsize[d] = nside;
+    }
+    data_length = (long)nside * nside * nside;
+    msize0 = msize1 = nside - 1;  /* MPI_Allgather of local_xend[1], local_xend[2] over one rank */
+    MSIZE0 = &msize0;
+    MSIZE1 = &msize1;
+    partmesh_thread();
+    for (int n = 0; n < npart; n++)
+        for (int d = 0; d < 3; d++) acc_pm[3 * n + d] = part[n].acc_pm[d];
+    free(part);
+    part = saved;
+    NPART = saved_n;
+}

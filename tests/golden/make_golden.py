@@ -8,6 +8,9 @@ Each fixture holds the input positions and force parameters, and the
 reference's outputs: the tree-ordered positions (its in-place permutation),
 the accelerations after fmm_task and after fmm_ext, the counters, the tree
 and a digest of every interaction list (full lists for the small cases).
+time/ holds the reference's kick and drift factors; pm/ the reference's PM
+accelerations (src/partmesh.c, with the Fortran convolution of
+src/conv.f90 replaced by oracle/pm_conv.c, which needs no 2DECOMP&FFT).
 """
 from __future__ import annotations
 
@@ -130,9 +133,35 @@ def time_integrals():
     print("time/loga_integrals  %d rows" % len(rows))
 
 
+def pm_cases():
+    """(name, pos, boxsize, nside, rs, mass): a clump in a uniform box, and a
+    perturbed grid on a mesh finer than its particle spacing."""
+    rng = np.random.default_rng(3)
+    L = 50.0
+    pos = rng.random((1500, 3)) * L
+    pos[:500] = (0.3 * L + rng.normal(scale=0.02 * L, size=(500, 3))) % L
+    yield "pm_clump16", pos, L, 16, 1.25 * L / 16, 0.7
+    g, p = ics.make("grid32", nside=12)
+    yield "pm_grid12_mesh24", g, p["boxsize"], 24, 1.25 * p["boxsize"] / 24, p["mass"]
+
+
+def pm_fixtures():
+    """The reference's own PM (src/partmesh.c at one rank, the Fortran
+    convolution replaced by oracle/pm_conv.c) -> pm/<name>.npz."""
+    ref = oracle.RefOracle()
+    os.makedirs(os.path.join(HERE, "pm"), exist_ok=True)
+    for name, pos, L, N, rs, m in pm_cases():
+        acc = ref.pm_force(pos, L, N, rs, m)
+        path = os.path.join(HERE, "pm", name + ".npz")
+        np.savez_compressed(path, pos=pos, acc_pm=acc, params=np.array([L, N, rs, m]))
+        print("pm/%-16s N=%5d mesh %d  %6.1f KB" % (name, pos.shape[0], N, os.path.getsize(path) / 1024))
+
+
 if __name__ == "__main__":
-    # python make_golden.py [fixture names]  (default: all)
+    # python make_golden.py [fixture names | time | pm]  (default: all)
     names = sys.argv[1:]
     main(names or None)
     if not names or "time" in names:
         time_integrals()
+    if not names or "pm" in names:
+        pm_fixtures()
