@@ -61,6 +61,19 @@ int acceptance(double wi[3], double wj[3], double dist[3]);
    (src/remotes.c:684-751); at one rank idx must be 0 */
 void fmm_remote(int idx, double shift[3]);
 
+/* inc/partmesh.h:16-17, 22 -- the PM long-range force at one rank, on the
+   GPU (src/partmesh.c:18-795 in the -DPMTHREAD build, :800-1582 without):
+   part[].acc_pm from part[].pos on an NSIDE^3 mesh with splitRadius,
+   BOXSIZE and MASSPART.  pm_thread is the entry of the driver's PM thread
+   (src/partmesh.c:11-16, src/photoNs.c:104); the PM uses a GPU context of
+   its own, so it runs beside the FMM calls of the driver's main thread. */
+void partmesh_thread(void);
+void partmesh(void);
+void *pm_thread(void *arg);
+/* src/conv.f90:3-23, called as decomp_2d_init by src/initial.c:226, 468: the
+   pencil of one rank is the whole mesh (0-based start and end) */
+void get_local_size_(int *global_size, int *vproc, int *local_start, int *local_end, int *local_size);
+
 /* ------------------------------------------------------------------ */
 /* 2. extensions                                                       */
 /* ------------------------------------------------------------------ */

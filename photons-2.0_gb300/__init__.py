@@ -97,9 +97,12 @@ def load_library():
     lib.photons_fp32_fma_peak.argtypes = [C.c_int]
     lib.photons_gpu_error.restype = C.c_char_p
     lib.photons_gpu_status.restype = C.c_int
-    for name in ("fmm_construct", "fmm_prepare", "fmm_task", "fmm_ext", "fmm_deconstruct", "build_localtree"):
+    for name in ("fmm_construct", "fmm_prepare", "fmm_task", "fmm_ext", "fmm_deconstruct", "build_localtree",
+                 "partmesh_thread", "partmesh"):
         getattr(lib, name).restype = None
         getattr(lib, name).argtypes = []
+    lib.pm_thread.restype = C.c_void_p
+    lib.pm_thread.argtypes = [C.c_void_p]
     lib.acceptance.restype = C.c_int
     lib.acceptance.argtypes = [_dp, _dp, _dp]
     lib.fmm_remote.argtypes = [C.c_int, _dp]
@@ -422,15 +425,31 @@ class Reference:
         for name in ("idxP2P", "idxM2L", "walk_m2l_count", "p2p_count_remote"):
             self._set(C.c_ulong, name, 0)
 
-    def force_pass(self):
-        """The driver sequence of src/photoNs.c:97-116 (without PM)."""
+    def force_pass(self, pm_nside=0):
+        """The driver sequence of src/photoNs.c:97-116.  With pm_nside, the PM
+        runs as the driver runs it: pm_thread on a second thread from after
+        fmm_prepare until before fmm_ext, beside fmm_task (PMTHREAD)."""
+        import threading
         lib = self.lib
         lib.fmm_construct()
         lib.fmm_prepare()
+        pm = None
+        if pm_nside:
+            self._set(C.c_int, "NSIDE", int(pm_nside))
+            pm = threading.Thread(target=lib.pm_thread, args=(None,))
+            pm.start()
         lib.fmm_task()
+        if pm:
+            pm.join()
         acc_task = self._part["acc"].copy()
         lib.fmm_ext()
         return acc_task
+
+    def pm(self, nside):
+        """partmesh_thread() on the current part[]: acc_pm (n, 3)."""
+        self._set(C.c_int, "NSIDE", int(nside))
+        self.lib.partmesh_thread()
+        return self._part["acc_pm"].copy()
 
     def part(self):
         return self._part

@@ -48,6 +48,8 @@ REF_INT64 idxP2P = 0, idxM2L = 0, walk_m2l_count = 0, p2p_count_remote = 0, m2l_
 double dtime_p2p = 0, dtime_m2l = 0, dtime_fmm = 0, dtime_task = 0, dtime_ext = 0, dtime_prep = 0,
        dtime_fmm_remote = 0;
 double DTIME_THIS_DOMAIN = 0.0;
+int NSIDE = 0;          // PM mesh side (inc/photoNs.h:58)
+double dtime_pm = 0.0;  // inc/photoNs.h:107
 }
 
 static photons_ctx *g_ctx = nullptr;
@@ -498,4 +500,73 @@ extern "C" int acceptance(double wi[3], double wj[3], double dist[3])
     volatile double lhs = wmax * wmax, th2 = open_angle * open_angle;
     volatile double rhs = th2 * dd2;
     return lhs < rhs ? 1 : 0;
+}
+
+// ------------------------------------------------------------------
+// the reference's PM entry points (inc/partmesh.h:16-21), on the GPU
+// ------------------------------------------------------------------
+// The reference driver runs pm_thread on a second host thread while the
+// FMM runs (src/photoNs.c:104, 237), so the PM keeps a context (stream,
+// mesh buffers, FFT plans) of its own and shares nothing with the FMM's.
+static photons_ctx *g_pm_ctx = nullptr;
+static std::vector<double> g_pm_stage;
+
+// src/partmesh.c:18-795 (the -DPMTHREAD build) and :800-1582: part[].acc_pm
+// from part[].pos on an NSIDE^3 mesh with splitRadius, BOXSIZE and
+// MASSPART, at one rank (photons_pm_force: CIC deposit, the convolution of
+// src/conv.f90:128-247, 4-point gradient, CIC interpolation)
+extern "C" void partmesh_thread(void)
+{
+    photons_gpu_clear_error();
+    if (PROC_SIZE != 1) {
+        ph_set_error(PH_ERR_UNSUPPORTED, "PROC_SIZE=%d: only the single-GPU, single-rank PM is provided", PROC_SIZE);
+        fatal("partmesh");
+    }
+    const double t0 = wall();
+    if (!part || NPART < 1) { ph_set_error(PH_ERR_ARG, "no particles"); fatal("partmesh"); }
+    if (!g_pm_ctx) {
+        g_pm_ctx = photons_create(0);
+        if (!g_pm_ctx) fatal("partmesh");
+    }
+    photons_params p;
+    memset(&p, 0, sizeof p);
+    p.boxsize = BOXSIZE;
+    p.rs = splitRadius;
+    p.mass = MASSPART;
+    p.precision = PHOTONS_FP64;
+    const size_t n = (size_t)NPART;
+    g_pm_stage.resize(6 * n);
+    double *pos = g_pm_stage.data(), *acc = pos + 3 * n;
+    for (size_t i = 0; i < n; i++)
+        for (int d = 0; d < 3; d++) pos[3 * i + d] = part[i].pos[d];
+    if (photons_pm_force(g_pm_ctx, &p, NSIDE, NPART, pos, acc)) fatal("partmesh");
+    for (size_t i = 0; i < n; i++)
+        for (int d = 0; d < 3; d++) part[i].acc_pm[d] = acc[3 * i + d];
+    dtime_pm = wall() - t0;
+}
+
+// src/partmesh.c:800 (the build without PMTHREAD)
+extern "C" void partmesh(void) { partmesh_thread(); }
+
+// src/partmesh.c:11-16: the thread entry src/photoNs.c:104 starts
+extern "C" void *pm_thread(void *arg)
+{
+    (void)arg;
+    partmesh_thread();
+    return nullptr;
+}
+
+// src/conv.f90:3-23, called as decomp_2d_init by src/initial.c:226, 468:
+// the pencil of one rank is the whole mesh (0-based start and end)
+extern "C" void get_local_size_(int *global_size, int *vproc, int *local_start, int *local_end, int *local_size)
+{
+    if (vproc && vproc[0] * vproc[1] != 1) {
+        ph_set_error(PH_ERR_UNSUPPORTED, "vproc %d x %d: only one rank is provided", vproc[0], vproc[1]);
+        fatal("get_local_size");
+    }
+    for (int d = 0; d < 3; d++) {
+        local_start[d] = 0;
+        local_end[d] = global_size[d] - 1;
+        local_size[d] = global_size[d];
+    }
 }

@@ -13,7 +13,7 @@ REFERENCE_GLOBALS = [
     "part", "btree", "leaf", "toptree", "open_angle", "first_node", "last_node", "first_leaf", "last_leaf",
     "MAXLEAF", "PROC_RANK", "PROC_SIZE", "BOXSIZE", "NPART", "NLEAF", "NNODE", "NPART_TOTAL", "MASSPART",
     "SoftenScale", "cutoffRadius", "splitRadius", "first_domain", "last_domain", "this_domain", "mostleft",
-    "direct_local_start", "idxP2P", "idxM2L", "walk_m2l_count", "p2p_count_remote",
+    "direct_local_start", "idxP2P", "idxM2L", "walk_m2l_count", "p2p_count_remote", "NSIDE",
 ]
 
 
@@ -27,7 +27,8 @@ def declared_functions():
 def test_header_declares_reference_entry_points():
     names = declared_functions()
     for ref in ("fmm_construct", "fmm_prepare", "fmm_task", "fmm_ext", "fmm_deconstruct", "build_localtree",
-                "p2m", "m2m", "m2l", "l2l", "l2p", "walk_m2m", "walk_l2l", "acceptance", "fmm_remote"):
+                "p2m", "m2m", "m2l", "l2l", "l2p", "walk_m2m", "walk_l2l", "acceptance", "fmm_remote",
+                "partmesh_thread", "partmesh", "pm_thread", "get_local_size_"):
         assert ref in names
 
 

@@ -39,6 +39,43 @@ def test_driver_sequence_matches_reference(ph, name):
     ref.deconstruct()
 
 
+def _pm_golden():
+    import glob
+    import os
+    from conftest import GOLDEN
+    return sorted(glob.glob(os.path.join(GOLDEN, "pm", "*.npz")))
+
+
+@pytest.mark.parametrize("path", _pm_golden(), ids=lambda p: p.rsplit("/", 1)[-1][:-4])
+def test_partmesh_matches_reference_pm(ph, path):
+    """partmesh_thread() on the reference's globals against the reference's
+    own partmesh.c outputs (cuFFT against a direct DFT: last bits)."""
+    z = np.load(path)
+    L, N, rs, m = z["params"]
+    ref = ph.Reference()
+    ref.setup(z["pos"], dict(boxsize=L, theta=0.5, rs=rs, rcut=4.5 * rs, eps=0.0, mass=m, maxleaf=16))
+    got = ref.pm(int(N))
+    want = z["acc_pm"]
+    assert np.abs(got - want).max() <= 1e-10 * np.abs(want).max()
+
+
+def test_driver_sequence_with_pm_thread(ph):
+    """The driver's step with the PM on its own thread beside fmm_task: the
+    FMM result is unchanged and acc_pm is the PM of the tree-ordered part[]."""
+    import pm_oracle
+    g = load_golden("grid16_leaf16")
+    ref = ph.Reference()
+    ref.setup(g["pos_in"], g["p"])
+    nside = 16
+    ref.force_pass(pm_nside=nside)
+    part = ref.part()
+    assert rel_err(part["acc"], g["acc"], g["p"]).max() <= 1e-10
+    p = g["p"]
+    want = pm_oracle.pm_force(part["pos"], p["boxsize"], nside, p["rs"], p["mass"])
+    assert np.abs(part["acc_pm"] - want).max() <= 1e-10 * np.abs(want).max()
+    ref.deconstruct()
+
+
 def test_operators_match_oracle(ph, port):
     rng = np.random.default_rng(2)
     n = 64
