@@ -38,6 +38,12 @@ UNIT = "particle-forces/s"
 # conventional count for a softened, erfc-truncated pair force); the P2P
 # roofline is this times the pairs, over the P2P phase time
 FLOPS_PER_PAIR = 36
+# DRAM traffic of one launch of the dominant kernel at 256^3 leaf 64 (bytes
+# read + written): ncu dram__bytes_read.sum + dram__bytes_write.sum of one
+# launch on the 128^3 workload of the same density, scaled by the particle
+# count (x8; traffic grows in proportion).  The capture command and figures
+# are kept with the kernel's profile summary.
+TRAFFIC_PER_LAUNCH_256 = {"k_p2p_mutual": 13.05e9, "k_p2p_split_packed": 1.27e9}
 # MAXLEAF the GPU arm's autotuner picks for each workload on GB300 (the
 # fastest leaf within the 1e-4 median error bound); the CPU baselines run
 # the same leaf so that both arms compute the same lists at the same error
@@ -55,6 +61,8 @@ def parse():
     ap.add_argument("--error-bound", type=float, default=1e-4)
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 GPU comparison pass")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the parity leg (tree, lists, counters and FP64 forces against the oracle)")
     ap.add_argument("--workload", default="zeldovich256",
                     choices=["zeldovich256", "zeldovich512", "nfw128", "boxes256"],
                     help="zeldovich256: the headline (P(k)~k^-2, seed 3); zeldovich512: P(k)~k^-1.5, seed 5, "
@@ -179,7 +187,31 @@ def cpu_baseline(nthreads=None, target_s=10.0, maxleaf=64, name="zeldovich256"):
                       "on the host: %.2f s" % (nside, p["boxsize"], maxleaf, secs)}
 
 
+def workload_config(args, p, n):
+    """The workload description both arms print (identical keys and values)."""
+    return {"workload": args.workload, "n": int(n), "boxsize": p["boxsize"], "mesh": args.nside,
+            "maxleaf": int(p["maxleaf"]), "theta": p["theta"], "rs": p["rs"], "rcut": p["rcut"], "eps": p["eps"],
+            "l2": "inputs larger than L2 (positions %.0f MB), no flush" % (n * 24 / 1e6)}
+
+
+def tree_blocks(perm, k, rng, nblocks=8):
+    """k particles (input indices) in nblocks runs of consecutive tree
+    positions: whole leaves of spatially compact regions, drawn at random."""
+    n = perm.size
+    per = max(1, k // nblocks)
+    starts = rng.choice(max(1, n - per), nblocks, replace=False)
+    return np.unique(np.concatenate([perm[s0:s0 + per] for s0 in starts])).astype(np.int32)
+
+
 def run_reference_arm(args):
+    """The reference's algorithm (the oracle's C restatement, pinned bit for
+    bit to the reference's own fmm.c/operator.c/remotes.c) on the host cores,
+    on the same workload and leaf size as the GPU arm.  Setup: the tree
+    build, multipoles and dual-tree walks of the whole input, timed once.
+    Each step: the forces (P2P, M2L, L2L, L2P) of a sample of the particles
+    (runs of whole leaves at random places in tree order), timed; the step's
+    time adds the setup's share for the sample (setup x sample / N), so the
+    rate is particles per second of the whole pass."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
@@ -189,29 +221,97 @@ def run_reference_arm(args):
     oracle.build_port()
     port = oracle.PortOracle(build=False)
     nthreads = os.cpu_count() or 1
-    nside = 64
     name = args.workload if args.workload in CHOSEN_LEAF else "zeldovich256"
     leaf = args.maxleaf or CHOSEN_LEAF[name]
-    pos, p = workload(nside, leaf, name=name)
+    pos, p = workload(args.nside, leaf, name=name)
+    n = pos.shape[0]
+    rng = np.random.default_rng(5)
+    probe = rng.choice(n, 4096, replace=False).astype(np.int32)
+    r = port.run_sample(pos, p, probe, nthreads=nthreads, perm=True)
+    perm = r["perm"]
+    setup_s = r["times"]["tree"] + r["times"]["multipoles"] + r["times"]["walk"]
+    # size the sample to about 2 s of force work per step
+    k = 16384
+    _, secs = port.forces_sample(tree_blocks(perm, k, rng))
+    k = int(min(n, max(4096, k * 2.0 / max(secs, 1e-3))))
     for _ in range(max(0, args.warmup)):
-        port.run(pos, p, capture=False, tree=False, nthreads=nthreads)
-    t = []
+        port.forces_sample(tree_blocks(perm, k, rng))
+    t, ks = [], []
     for _ in range(max(1, args.steps)):
-        r = port.run(pos, p, capture=False, tree=False, nthreads=nthreads)
-        t.append(r["seconds"])
-    secs = float(np.mean(t))
-    v = pos.shape[0] / secs
+        tg = tree_blocks(perm, k, rng)
+        _, secs = port.forces_sample(tg)
+        t.append(secs + setup_s * tg.size / n)
+        ks.append(tg.size)
+    secs = float(np.sum(t))
+    v = float(np.sum(ks)) / secs
+    c = r["counters"]
+    pairs = c["pairs_local"] + c["pairs_image"]
     line = {"metric": METRIC, "impl": "reference", "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": secs * 1e3, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": secs * 1e3 / len(t), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "%s sample at %d^3 (same density/clustering)" % (name, nside),
-                       "n": int(pos.shape[0]), "boxsize": p["boxsize"], "maxleaf": leaf, "theta": 0.5},
+            "config": workload_config(args, p, n),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
-                             "sample": "each step one full pass at %d^3 on %d host threads (the reference's "
-                                       "algorithm restated in C; the reference sources are not on this host)"
-                                       % (nside, nthreads)},
-            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                             "sample": "setup once: tree, multipoles and walks of all %d particles on %d host "
+                                       "threads (%.2f s); each step: forces of %d particles (8 runs of whole "
+                                       "leaves in tree order) plus the setup's share for them; the reference's "
+                                       "algorithm restated in C and pinned bit-exact to its sources (which are "
+                                       "not on this host)" % (n, nthreads, setup_s, k)},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "setup_s": r["times"], "sample_particles_per_step": k,
+            "counters": {kk: c[kk] for kk in ("idxP2P", "idxM2L", "walk_m2l_count", "p2p_count_remote", "nleaf",
+                                              "nnode", "n_p2p_ext", "n_m2l_ext", "pairs_local", "pairs_image")},
+            "pairs_per_particle": pairs / n}
     print(json.dumps(line))
+
+
+def list_digest(t, s, im):
+    """SHA-256 of a list's (target, source, image) entries as a sorted multiset."""
+    import hashlib
+
+    key = (t.astype(np.int64) << 34) | (s.astype(np.int64) << 5) | im.astype(np.int64)
+    key.sort()
+    return hashlib.sha256(key.tobytes()).hexdigest()
+
+
+PARITY_COUNTERS = ("nleaf", "nnode", "idxP2P", "idxM2L", "walk_m2l_count", "p2p_count_remote", "n_p2p_ext",
+                   "n_m2l_ext", "pairs_local", "pairs_image")
+
+
+def parity_leg(fp, pos, p, tgt, acc64_tgt, acc32_tgt, nthreads):
+    """The GPU pass against the oracle's restatement (pinned bit for bit to
+    the reference's sources) on the same input and leaf size, outside the
+    timed region: tree and walk counters, the tree-order permutation, every
+    interaction list as a multiset, and the FP64 accelerations of the target
+    subset (relative bar 1e-10).  fp holds the last FP64 pass (lists kept)."""
+    import hashlib
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    t0 = time.time()
+    port = oracle.PortOracle()
+    r = port.run_sample(pos, p, tgt, nthreads=nthreads, lists=True, perm=True)
+    gc = fp.counters()
+    oc = r["counters"]
+    counts = {k: [int(gc[k]), int(oc[k])] for k in PARITY_COUNTERS}
+    gperm = fp.perm()
+    lists = {}
+    glists = fp.lists()
+    for kind, (t, s, im) in r["lists"].items():
+        lists[kind] = list_digest(*glists[kind]) == list_digest(t, s, im)
+    a_ref = r["acc"]
+    nref = np.maximum(np.linalg.norm(a_ref, axis=1), 1e-300)
+    e64 = np.linalg.norm(acc64_tgt - a_ref, axis=1) / nref
+    e32 = np.linalg.norm(acc32_tgt - a_ref, axis=1) / nref
+    return {"oracle": "the C restatement of the reference's pass (oracle/photons_oracle.c), bit-identical to the "
+                      "reference's compiled sources on the golden inputs; %d host threads" % nthreads,
+            "counts_equal": all(a == b for a, b in counts.values()), "counters_gpu_oracle": counts,
+            "perm_equal": bool(np.array_equal(gperm, r["perm"])),
+            "perm_sha256": hashlib.sha256(np.ascontiguousarray(gperm, np.int32).tobytes()).hexdigest(),
+            "lists_equal": lists,
+            "fp64_max_rel": float(e64.max()), "fp64_bar": 1e-10, "fp64_ok": bool(e64.max() <= 1e-10),
+            "fp32_vs_oracle_median": float(np.median(e32)), "fp32_vs_oracle_p99": float(np.percentile(e32, 99)),
+            "targets": int(tgt.size), "oracle_times_s": r["times"], "seconds": time.time() - t0}
 
 
 def kdk_measure(ph, fp, torch, stream, dpos, dacc, n, p, steps, pflags=0):
@@ -549,13 +649,20 @@ def main():
     e0.record(stream)
     t0 = time.time()
     esteps = max(1, min(args.steps, 5))
+    e2e_parts = []
     for _ in range(esteps):
+        t1 = time.perf_counter()
         fp.run(hp, p, precision=ph.FP32_SPLIT, flags=pflags, out=ha)
+        wall_ms = (time.perf_counter() - t1) * 1e3
+        t = fp.timings()  # CUDA events of this pass: copy in, device part, copy out
+        e2e_parts.append((t["upload"], t["total"] - t["upload"] - t["download"], t["download"], t["total"], wall_ms))
     e1.record(stream)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     e2e_ms = max_over_ranks(max(e0.elapsed_time(e1), (time.time() - t0) * 1e3) / esteps, dist, "cuda")
+    e2e_split = dict(zip(("h2d_ms", "device_ms", "d2h_ms", "events_total_ms", "host_call_ms"),
+                         (float(np.median([q[i] for q in e2e_parts])) for i in range(5))))
     acc32 = ha.copy()
 
     if rank != 0:
@@ -574,14 +681,7 @@ def main():
     peak = ph.fp32_fma_peak(8192)
     t_p2p = float(np.mean(p2p_ms))
     achieved = FLOPS_PER_PAIR * pairs / (t_p2p * 1e-3) / 1e12
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", {"k_p2p_mutual": "k_p2p_mutual_zeldovich128.md",
-                                         "k_p2p_split_packed": "k_p2p_split_packed_zeldovich160.md"}[kernel])
-    if os.path.exists(tp) and args.nside == 256:
-        import re
-        m = re.search(r"dram_bytes_per_launch_scaled_to_256:\s*([0-9.eE+]+)", open(tp).read())
-        traffic = float(m.group(1)) if m else None
-
+    traffic = TRAFFIC_PER_LAUNCH_256.get(kernel) if (args.nside == 256 and args.workload == "zeldovich256") else None
     extra = {}
     kdk = kdk_measure(ph, fp, torch, stream, dpos, dacc, n, p, args.steps, pflags) if args.kdk else None
     rng = np.random.default_rng(7)
@@ -597,10 +697,12 @@ def main():
         t64 = fp.timings()
         acc64 = np.empty_like(pos)
         e0.record(stream)
-        fp.run(pos, p, precision=ph.FP64, out=acc64)
+        fp.run(pos, p, precision=ph.FP64, out=acc64, flags=ph.F_KEEP_LISTS)
         e1.record(stream)
         torch.cuda.synchronize()
         ms64 = e0.elapsed_time(e1)
+        if not args.no_parity:
+            extra["parity"] = parity_leg(fp, pos, p, tgt, acc64[tgt], acc32[tgt], os.cpu_count() or 1)
         e = rel_err(acc32, acc64)
         a64 = rel_err(acc64[tgt], ds)
         extra["fp64_gpu"] = {"value": n / (ms64 * 1e-3), "ms_per_pass": ms64, "p2p_ms": t64["p2p"],
@@ -619,11 +721,9 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": args.workload, "n": n, "boxsize": p["boxsize"], "mesh": args.nside,
-                   "maxleaf": p["maxleaf"], "theta": p["theta"], "rs": p["rs"], "rcut": p["rcut"],
-                   "eps": p["eps"], "precision": "fp32-split (fp64 positions and centre differences)",
-                   "l2": "inputs larger than L2 (positions %.0f MB), no flush" % (n * 24 / 1e6),
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": workload_config(args, p, n),
+        "precision": "fp32-split (fp64 positions and centre differences)",
+        "parallelism": "replicas" if world > 1 else "single GPU",
         "roofline": {"bound": "fp32", "kernel": kernel, "achieved": achieved, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                      "peak_source": "FFMA probe measured in this run (MEASURED_PEAKS.json holds no FP32 figure)",
@@ -637,7 +737,8 @@ def main():
                               "is a lower bound for the kernel alone"},
         "cpu_baseline": cpu,
         "e2e": {"value": n * world / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": n * 24 * world,
-                "d2h_bytes_per_step": n * 24 * world, "ms_per_step": e2e_ms},
+                "d2h_bytes_per_step": n * 24 * world, "ms_per_step": e2e_ms, "split_median": e2e_split,
+                "path": "photons_force_pass with pinned host buffers (copies on the pass stream)"},
         "gpu_launches": int(launches),
         "clocks": clocks,
         "phases_ms": tmean,

@@ -168,15 +168,19 @@ int photons_direct_sum(const photons_params *p, int n, const double *pos, int nt
    budgeted all of HBM up front (particles, PM mesh, force-pass pools), where
    a cudaMalloc between steps fails, or whose other streams must not be
    stalled by the device-wide synchronisation of cudaMalloc/cudaFree.
-   pos[3n], targets[nt] and acc[3nt] are DEVICE pointers (host pointers are
-   rejected).  At most 262144 sources and 65536 targets; larger sizes return
-   error 1 with a message.  Scratch is one fixed array of about 10.8 MB per
-   device, held from the library's load until the process exits.  The first
-   call on a device looks up that array's address (with the device current);
-   make that first call before any stream capture.  All calls share the
-   array, so calls that overlap on the GPU (other streams or host threads)
-   race.  Runs on cuda_stream (NULL: the default stream) and returns after
-   that stream has finished the call's work. */
+   pos[3n], targets[nt] and acc[3nt] are DEVICE pointers on the current
+   device (host pointers and other devices' buffers are rejected).  At most
+   262144 sources and 65536 targets; larger sizes return error 1 with a
+   message.  Scratch is one fixed array of about 10.8 MB per device.  The
+   library's device code is loaded lazily, so that array is placed in device
+   memory by the first call on a device, which also looks up its address
+   (with the device current; again after the device's context is replaced):
+   make that first call before HBM is budgeted and before any stream
+   capture.  A call with nt = 0 does only this set-up (a warm-up; nothing is
+   launched).  From then on the array stays until the process exits.  All
+   calls share it, so calls that overlap on the GPU (other streams or host
+   threads) race.  Runs on cuda_stream (NULL: the default stream) and
+   returns after that stream has finished the call's work. */
 int photons_direct_sum_noalloc(const photons_params *p, int n, const double *pos, int nt, const int *targets,
                                double rmax, double *acc, void *cuda_stream);
 

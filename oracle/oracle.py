@@ -198,6 +198,11 @@ class PortOracle(_Base):
         lib.po_run.argtypes = [C.c_void_p, C.c_void_p, C.c_int, _dp, _dp]
         lib.po_counters.argtypes = [C.c_void_p, _lp]
         lib.po_particles.argtypes = [C.c_void_p, _dp, _dp, _dp, _ip]
+        lib.po_run_sample.restype = C.c_int
+        lib.po_run_sample.argtypes = [C.c_void_p, C.c_void_p, C.c_int, _dp, C.c_int, _ip, _dp, _dp]
+        lib.po_pairs.argtypes = [C.c_void_p, _lp, _lp]
+        lib.po_forces_sample.restype = C.c_int
+        lib.po_forces_sample.argtypes = [C.c_void_p, C.c_int, _ip, _dp, _dp]
         lib.po_list_size.restype = C.c_long
         lib.po_list_size.argtypes = [C.c_void_p, C.c_int]
         lib.po_list_copy.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _ip]
@@ -266,6 +271,56 @@ class PortOracle(_Base):
         if tree:
             r["tree"] = self._tree_port(counters)
         return r
+
+    def run_sample(self, pos, p, targets, nthreads=1, images=True, lists=False, perm=False):
+        """The pass with forces only for ``targets`` (input indices): complete
+        tree, walks and counters; the targets' accelerations equal the full
+        pass's.  Returns acc (len(targets), 3), counters (with pairs_local,
+        pairs_image), times {tree, multipoles, walk, forces} in seconds and,
+        on request, the lists (reference index space) and the permutation."""
+        pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+        targets = np.ascontiguousarray(targets, np.int32)
+        n = pos.shape[0]
+        prm = self._params(p, nthreads, True, images)
+        acc = np.empty((targets.size, 3))
+        t = np.zeros(4)
+        rc = self.lib.po_run_sample(self.state, C.byref(prm), n, _ptr(pos), targets.size, _ptr(targets, _ip),
+                                    _ptr(acc), _ptr(t))
+        if rc != 0:
+            raise RuntimeError(f"oracle sampled pass failed with code {rc}")
+        cnt = np.zeros(16, np.int64)
+        self.lib.po_counters(self.state, _ptr(cnt, _lp))
+        counters = dict(zip(COUNTER_NAMES, (int(c) for c in cnt)))
+        a, b = C.c_longlong(0), C.c_longlong(0)
+        self.lib.po_pairs(self.state, C.byref(a), C.byref(b))
+        counters["pairs_local"], counters["pairs_image"] = a.value, b.value
+        r = PassResult(acc=acc, counters=counters,
+                       times=dict(zip(("tree", "multipoles", "walk", "forces"), t.tolist())))
+        if perm:
+            pm = np.empty(n, np.int32)
+            self.lib.po_particles(self.state, None, None, None, _ptr(pm, _ip))
+            r["perm"] = pm
+        if lists:
+            out = {}
+            for name, k in LIST_KINDS.items():
+                m = self.lib.po_list_size(self.state, k)
+                tt = np.empty(m, np.int32); ss = np.empty(m, np.int32); im = np.empty(m, np.int32)
+                if m:
+                    self.lib.po_list_copy(self.state, k, _ptr(tt, _ip), _ptr(ss, _ip), _ptr(im, _ip))
+                out[name] = (tt, ss, im)
+            r["lists"] = out
+        return r
+
+    def forces_sample(self, targets):
+        """Forces for another target set on the last pass's tree and lists:
+        (acc (len(targets), 3), seconds)."""
+        targets = np.ascontiguousarray(targets, np.int32)
+        acc = np.empty((targets.size, 3))
+        secs = C.c_double(0.0)
+        rc = self.lib.po_forces_sample(self.state, targets.size, _ptr(targets, _ip), _ptr(acc), C.byref(secs))
+        if rc != 0:
+            raise RuntimeError(f"oracle sampled forces failed with code {rc}")
+        return acc, secs.value
 
     def _tree_port(self, counters):
         class Shim:

@@ -257,11 +257,27 @@ struct po_state {
     o_list list[4];
     long long walk_m2l_count, p2p_count_remote;
     int err;
-    /* per-image pruning: son[] of the exported copy (-1 when pruned) */
-    double shift[3];
-    int image;
     int capture;
+    /* sampled pass: forces only for these particles (tree order) and the
+       leaves / nodes that hold them; NULL = every particle */
+    unsigned char *part_on, *leaf_on, *node_on;
 };
+
+/* One dual-tree traversal's output.  Walks are split into independent
+   sub-walks (subtrees of the recursion) that run on separate threads and
+   are concatenated in the order a sequential traversal would emit them. */
+typedef struct { int kind, a, b; } o_item;   /* kind 0-3: list entry (t, s); 4: deferred sub-walk (im, jm) */
+typedef struct {
+    po_state *s;
+    int image;              /* 0 local, 1..26 periodic image */
+    double shift[3];
+    o_list list[4];
+    long long m2l;          /* contribution to walk_m2l_count */
+    int err;
+    int defer_depth;        /* >0: stop at this recursion depth and record the pair as an item */
+    o_item *items;
+    long nitems, capitems;
+} o_walker;
 
 po_state *po_create(void)
 {
@@ -273,7 +289,9 @@ static void free_run(po_state *s)
 {
     free(s->pos); free(s->perm); free(s->acc); free(s->acc_task);
     free(s->leaf); free(s->node);
+    free(s->part_on); free(s->leaf_on); free(s->node_on);
     s->pos = 0; s->perm = 0; s->acc = 0; s->acc_task = 0; s->leaf = 0; s->node = 0;
+    s->part_on = 0; s->leaf_on = 0; s->node_on = 0;
 }
 
 void po_destroy(po_state *s)
@@ -287,7 +305,7 @@ void po_destroy(po_state *s)
 static int list_push(o_list *l, int t, int src, int img)
 {
     if (l->n == l->cap) {
-        long cap = l->cap ? 2 * l->cap : 1 << 16;
+        long cap = l->cap ? 2 * l->cap : 1 << 10;
         int *a = realloc(l->t, sizeof(int) * cap), *b, *c;
         if (!a) return -1;
         l->t = a;
@@ -446,6 +464,8 @@ static void downward(po_state *s, int id)
     o_node *nd = NODE(s, id);
     for (int c = 0; c < 2; c++) {
         int ch = nd->son[c];
+        if (s->leaf_on && !(IS_LEAF(s, ch) ? s->leaf_on[ch - s->first_leaf] : s->node_on[ch - s->first_node]))
+            continue;
         if (!IS_LEAF(s, ch)) {
             o_node *cn = NODE(s, ch);
             po_l2l(cn->center[0] - nd->center[0], cn->center[1] - nd->center[1], cn->center[2] - nd->center[2],
@@ -472,11 +492,36 @@ static const double *geom_width(po_state *s, int id)
 }
 static double wsum(const double *w) { return w[0] + w[1] + w[2]; }
 
-static void emit(po_state *s, int kind, int t, int src)
+static int push_item(o_walker *w, int kind, int a, int b)
 {
-    if (s->err) return;
-    if (kind == PO_LIST_M2L || kind == PO_LIST_M2L_EXT) s->walk_m2l_count++;
-    if (list_push(&s->list[kind], t, src, s->image) != 0) s->err = PO_ERR_NOMEM;
+    if (w->nitems == w->capitems) {
+        long cap = w->capitems ? 2 * w->capitems : 256;
+        o_item *it = realloc(w->items, sizeof(o_item) * cap);
+        if (!it) return -1;
+        w->items = it;
+        w->capitems = cap;
+    }
+    w->items[w->nitems].kind = kind;
+    w->items[w->nitems].a = a;
+    w->items[w->nitems].b = b;
+    w->nitems++;
+    return 0;
+}
+
+static void emit(o_walker *w, int kind, int t, int src)
+{
+    if (w->err) return;
+    if (kind == PO_LIST_M2L || kind == PO_LIST_M2L_EXT) w->m2l++;
+    int rc = w->defer_depth ? push_item(w, kind, t, src) : list_push(&w->list[kind], t, src, w->image);
+    if (rc != 0) w->err = PO_ERR_NOMEM;
+}
+
+/* in a splitting walk, the pair (im, jm) at the split depth becomes a sub-walk */
+static int deferred(o_walker *w, int depth, int im, int jm)
+{
+    if (!w->defer_depth || depth < w->defer_depth) return 0;
+    if (push_item(w, 4, im, jm) != 0) w->err = PO_ERR_NOMEM;
+    return 1;
 }
 
 /*
@@ -486,39 +531,41 @@ static void emit(po_state *s, int kind, int t, int src)
  * accepted pair is an M2L task.  Node pairs that must be opened open the
  * side with the larger width sum (the source side on ties).
  */
-static void walk_local(po_state *s, int im, int jm)
+static void walk_local(o_walker *w, int im, int jm, int depth)
 {
-    if (s->err || im < 0 || jm < 0) return;
+    po_state *s = w->s;
+    if (w->err || im < 0 || jm < 0) return;
+    if (deferred(w, depth, im, jm)) return;
     int il = IS_LEAF(s, im), jl = IS_LEAF(s, jm);
     if (im == jm) {
-        if (il) { emit(s, PO_LIST_P2P, im, jm); return; }
+        if (il) { emit(w, PO_LIST_P2P, im, jm); return; }
         o_node *a = NODE(s, im);
-        walk_local(s, a->son[0], a->son[0]);
-        walk_local(s, a->son[0], a->son[1]);
-        walk_local(s, a->son[1], a->son[0]);
-        walk_local(s, a->son[1], a->son[1]);
+        walk_local(w, a->son[0], a->son[0], depth + 1);
+        walk_local(w, a->son[0], a->son[1], depth + 1);
+        walk_local(w, a->son[1], a->son[0], depth + 1);
+        walk_local(w, a->son[1], a->son[1], depth + 1);
         return;
     }
-    if (il && jl) { emit(s, PO_LIST_P2P, im, jm); return; }
+    if (il && jl) { emit(w, PO_LIST_P2P, im, jm); return; }
     const double *ci = geom_center(s, im), *cj = geom_center(s, jm);
     double dist[3] = {ci[0] - cj[0], ci[1] - cj[1], ci[2] - cj[2]};
     /* the reference passes the leaf's width first in mixed pairs */
     int flag = jl ? po_acceptance(geom_width(s, jm), geom_width(s, im), dist, s->p.theta, s->p.rcut)
                   : po_acceptance(geom_width(s, im), geom_width(s, jm), dist, s->p.theta, s->p.rcut);
     if (flag == -1) return;
-    if (flag == 1) { emit(s, PO_LIST_M2L, im, jm); return; }
+    if (flag == 1) { emit(w, PO_LIST_M2L, im, jm); return; }
     int open_target;
     if (il) open_target = 0;
     else if (jl) open_target = 1;
     else open_target = wsum(NODE(s, im)->width) > wsum(NODE(s, jm)->width);
     if (open_target) {
         o_node *a = NODE(s, im);
-        walk_local(s, a->son[0], jm);
-        walk_local(s, a->son[1], jm);
+        walk_local(w, a->son[0], jm, depth + 1);
+        walk_local(w, a->son[1], jm, depth + 1);
     } else {
         o_node *b = NODE(s, jm);
-        walk_local(s, im, b->son[0]);
-        walk_local(s, im, b->son[1]);
+        walk_local(w, im, b->son[0], depth + 1);
+        walk_local(w, im, b->son[1], depth + 1);
     }
 }
 
@@ -533,13 +580,14 @@ static void walk_local(po_state *s, int im, int jm)
  * the local domain (toptree[0] after connect_local_toptree, i.e. the root
  * box).
  */
-static int image_pruned(po_state *s, int id)
+static int image_pruned(o_walker *w, int id)
 {
+    po_state *s = w->s;
     o_node *nd = NODE(s, id);
     o_node *root = NODE(s, s->first_node);
     double dr = 0.0;
     for (int d = 0; d < 3; d++) {
-        double g = root->center[d] - nd->center[d] - s->shift[d];
+        double g = root->center[d] - nd->center[d] - w->shift[d];
         if (g < 0.0) g = -g;
         g -= (root->width[d] + nd->width[d]) * 0.5;
         if (g > 0.0) dr += g * g;
@@ -555,35 +603,37 @@ static int image_pruned(po_state *s, int id)
 /* src/remotes.c:213-372 (P2P) and 405-552 (M2L), one traversal.  The
    received node is a leaf iff it holds <= MAXLEAF particles; pruned
    received nodes are interacted by M2L unless dropped. */
-static void walk_image(po_state *s, int im, int jm)
+static void walk_image(o_walker *w, int im, int jm, int depth)
 {
-    if (s->err) return;
+    po_state *s = w->s;
+    if (w->err) return;
+    if (deferred(w, depth, im, jm)) return;
     int il = IS_LEAF(s, im);
     int jl = IS_LEAF(s, jm);
-    if (il && jl) { emit(s, PO_LIST_P2P_EXT, im, jm); return; }
+    if (il && jl) { emit(w, PO_LIST_P2P_EXT, im, jm); return; }
     const double *ci = geom_center(s, im), *cj = geom_center(s, jm);
-    double cjs[3] = {cj[0] + s->shift[0], cj[1] + s->shift[1], cj[2] + s->shift[2]};
+    double cjs[3] = {cj[0] + w->shift[0], cj[1] + w->shift[1], cj[2] + w->shift[2]};
     double dist[3] = {ci[0] - cjs[0], ci[1] - cjs[1], ci[2] - cjs[2]};
     int flag = po_acceptance(geom_width(s, im), geom_width(s, jm), dist, s->p.theta, s->p.rcut);
     if (flag == -1) return;
-    int pruned = jl ? 0 : image_pruned(s, jm);
+    int pruned = jl ? 0 : image_pruned(w, jm);
     if (il) {
-        if (flag == 1 || pruned) { emit(s, PO_LIST_M2L_EXT, im, jm); return; }
+        if (flag == 1 || pruned) { emit(w, PO_LIST_M2L_EXT, im, jm); return; }
         o_node *b = NODE(s, jm);
-        walk_image(s, im, b->son[0]);
-        walk_image(s, im, b->son[1]);
+        walk_image(w, im, b->son[0], depth + 1);
+        walk_image(w, im, b->son[1], depth + 1);
         return;
     }
-    if (flag == 1) { emit(s, PO_LIST_M2L_EXT, im, jm); return; }
+    if (flag == 1) { emit(w, PO_LIST_M2L_EXT, im, jm); return; }
     int open_target = jl || pruned || wsum(NODE(s, im)->width) > wsum(NODE(s, jm)->width);
     if (open_target) {
         o_node *a = NODE(s, im);
-        walk_image(s, a->son[0], jm);
-        walk_image(s, a->son[1], jm);
+        walk_image(w, a->son[0], jm, depth + 1);
+        walk_image(w, a->son[1], jm, depth + 1);
     } else {
         o_node *b = NODE(s, jm);
-        walk_image(s, im, b->son[0]);
-        walk_image(s, im, b->son[1]);
+        walk_image(w, im, b->son[0], depth + 1);
+        walk_image(w, im, b->son[1], depth + 1);
     }
 }
 
@@ -646,6 +696,7 @@ static void p2p_target(p2p_job *J, int lf_index)
         if (!J->ext) {
             for (int q = 0; q < T->npart; q++) {
                 int ip = T->ipart + q;
+                if (s->part_on && !s->part_on[ip]) continue;
                 double a[3] = {0, 0, 0};
                 for (int jp = S->ipart; jp < S->ipart + S->npart; jp++) {
                     if (jp == ip) continue;
@@ -663,11 +714,13 @@ static void p2p_target(p2p_job *J, int lf_index)
                         if (mi == 0 && mj == 0 && mk == 0) continue;
                         if (++c == img) { sh[0] = mi * p->boxsize; sh[1] = mj * p->boxsize; sh[2] = mk * p->boxsize; }
                     }
-            for (int ip = T->ipart; ip < T->ipart + T->npart; ip++)
+            for (int ip = T->ipart; ip < T->ipart + T->npart; ip++) {
+                if (s->part_on && !s->part_on[ip]) continue;
                 for (int jp = S->ipart; jp < S->ipart + S->npart; jp++) {
                     double pj[3] = {s->pos[3 * jp] + sh[0], s->pos[3 * jp + 1] + sh[1], s->pos[3 * jp + 2] + sh[2]};
                     pair_force(pj, s->pos + 3 * ip, p, coeff, s->acc + 3 * ip);
                 }
+            }
         }
     }
 }
@@ -682,7 +735,8 @@ static void *p2p_worker(void *arg)
         pthread_mutex_unlock(&J->mu);
         if (i >= J->s->nleaf) break;
         int e = i + 16 < J->s->nleaf ? i + 16 : J->s->nleaf;
-        for (; i < e; i++) p2p_target(J, i);
+        for (; i < e; i++)
+            if (!J->s->leaf_on || J->s->leaf_on[i]) p2p_target(J, i);
     }
     return 0;
 }
@@ -725,6 +779,8 @@ static void run_m2l(po_state *s, const o_list *l)
 {
     for (long e = 0; e < l->n; e++) {
         int im = l->t[e], jm = l->s[e];
+        if (s->leaf_on && !(IS_LEAF(s, im) ? s->leaf_on[im - s->first_leaf] : s->node_on[im - s->first_node]))
+            continue;
         double sh[3] = {0, 0, 0};
         if (l->img[e]) image_shift(&s->p, l->img[e], sh);
         const double *cj = geom_center(s, jm);
@@ -746,12 +802,200 @@ static double wall(void)
     return tv.tv_sec + 1e-6 * tv.tv_usec;
 }
 
+/* ------------------------------------------------------------------ */
+/* walks on several threads, lists in the sequential order             */
+/* ------------------------------------------------------------------ */
+typedef struct {
+    po_state *s;
+    o_walker *sub;          /* one walker per deferred sub-walk */
+    long nsub;
+    long next;
+    pthread_mutex_t mu;
+} walk_job;
+
+static void walk_run(o_walker *w, int im, int jm)
+{
+    if (w->image) walk_image(w, im, jm, 0);
+    else walk_local(w, im, jm, 0);
+}
+
+static void *walk_worker(void *arg)
+{
+    walk_job *J = arg;
+    for (;;) {
+        pthread_mutex_lock(&J->mu);
+        long i = J->next++;
+        pthread_mutex_unlock(&J->mu);
+        if (i >= J->nsub) break;
+        o_walker *w = &J->sub[i];
+        walk_run(w, w->items[0].a, w->items[0].b);
+    }
+    return 0;
+}
+
+static void walker_free(o_walker *w)
+{
+    for (int k = 0; k < 4; k++) { free(w->list[k].t); free(w->list[k].s); free(w->list[k].img); }
+    free(w->items);
+}
+
+static int list_append(o_list *dst, const o_list *src)
+{
+    for (long i = 0; i < src->n; i++)
+        if (list_push(dst, src->t[i], src->s[i], src->img[i]) != 0) return -1;
+    return 0;
+}
+
+/* The local walk (image 0) and then the 26 image walks, each as the
+   reference runs it (fmm_task, then fmm_ext's loop over images).  Each walk
+   is first expanded sequentially down to a fixed recursion depth; the
+   pairs met there are walked on the worker threads into lists of their
+   own, which are then concatenated in the order the sequential traversal
+   would have emitted them, so the lists are identical to a one-thread
+   walk's. */
+static int run_walks(po_state *s, int images)
+{
+    int nimg = images ? NIMG : 1;
+    o_walker top[NIMG];
+    memset(top, 0, sizeof top);
+    long nsub = 0;
+    int rc = PO_OK;
+    for (int img = 0; img < nimg; img++) {
+        top[img].s = s;
+        top[img].image = img;
+        if (img) image_shift(&s->p, img, top[img].shift);
+        top[img].defer_depth = 12;
+        walk_run(&top[img], s->first_node, s->first_node);
+        if (top[img].err) rc = top[img].err;
+        for (long i = 0; i < top[img].nitems; i++) nsub += top[img].items[i].kind == 4;
+    }
+    walk_job J;
+    memset(&J, 0, sizeof J);
+    J.s = s;
+    J.sub = calloc((size_t)(nsub ? nsub : 1), sizeof(o_walker));
+    if (!J.sub) rc = PO_ERR_NOMEM;
+    if (rc == PO_OK) {
+        long k = 0;
+        for (int img = 0; img < nimg; img++)
+            for (long i = 0; i < top[img].nitems; i++) {
+                if (top[img].items[i].kind != 4) continue;
+                o_walker *w = &J.sub[k++];
+                w->s = s;
+                w->image = img;
+                memcpy(w->shift, top[img].shift, sizeof w->shift);
+                if (push_item(w, 4, top[img].items[i].a, top[img].items[i].b) != 0) rc = PO_ERR_NOMEM;
+            }
+        J.nsub = nsub;
+    }
+    if (rc == PO_OK) {
+        pthread_mutex_init(&J.mu, 0);
+        int nt = s->p.nthreads > 1 ? s->p.nthreads : 1;
+        if (nt == 1) {
+            walk_worker(&J);
+        } else {
+            pthread_t *th = malloc(sizeof(pthread_t) * nt);
+            for (int i = 0; i < nt; i++) pthread_create(&th[i], 0, walk_worker, &J);
+            for (int i = 0; i < nt; i++) pthread_join(th[i], 0);
+            free(th);
+        }
+        pthread_mutex_destroy(&J.mu);
+        /* concatenate in traversal order */
+        long k = 0;
+        for (int img = 0; img < nimg && rc == PO_OK; img++) {
+            s->walk_m2l_count += top[img].m2l;
+            for (long i = 0; i < top[img].nitems && rc == PO_OK; i++) {
+                o_item *it = &top[img].items[i];
+                if (it->kind != 4) {
+                    if (list_push(&s->list[it->kind], it->a, it->b, img) != 0) rc = PO_ERR_NOMEM;
+                    continue;
+                }
+                o_walker *w = &J.sub[k++];
+                if (w->err) { rc = w->err; break; }
+                s->walk_m2l_count += w->m2l;
+                for (int kind = 0; kind < 4; kind++)
+                    if (list_append(&s->list[kind], &w->list[kind]) != 0) rc = PO_ERR_NOMEM;
+            }
+        }
+    }
+    for (long i = 0; i < nsub && J.sub; i++) walker_free(&J.sub[i]);
+    free(J.sub);
+    for (int img = 0; img < nimg; img++) walker_free(&top[img]);
+    return rc;
+}
+
+/* marks the nodes whose subtree holds a marked leaf */
+static int mark_nodes(po_state *s, int id)
+{
+    if (IS_LEAF(s, id)) return s->leaf_on[id - s->first_leaf];
+    o_node *nd = NODE(s, id);
+    int a = mark_nodes(s, nd->son[0]);
+    int b = mark_nodes(s, nd->son[1]);
+    s->node_on[id - s->first_node] = (unsigned char)(a || b);
+    return a || b;
+}
+
+/* The force phases of the pass on the tree and lists at hand: local P2P
+   and M2L (fmm_task), image P2P and M2L (fmm_ext), L2L and L2P.  With
+   targets (input indices), only those particles, their leaves and the
+   leaves' ancestors are formed, after their accelerations and local
+   expansions are cleared, so the same tree can serve several samples. */
+static int forces(po_state *s, int nt, const int *targets)
+{
+    int n = s->n;
+    if (targets) {
+        free(s->part_on); free(s->leaf_on); free(s->node_on);
+        s->part_on = calloc((size_t)n, 1);
+        s->leaf_on = calloc((size_t)s->nleaf, 1);
+        s->node_on = calloc((size_t)s->nnode, 1);
+        int *where = malloc(sizeof(int) * (size_t)n);
+        if (!s->part_on || !s->leaf_on || !s->node_on || !where) { free(where); return PO_ERR_NOMEM; }
+        for (int i = 0; i < n; i++) where[s->perm[i]] = i;
+        for (int k = 0; k < nt; k++) {
+            if (targets[k] < 0 || targets[k] >= n) { free(where); return PO_ERR_ARG; }
+            int q = where[targets[k]];
+            s->part_on[q] = 1;
+            for (int d = 0; d < 3; d++) s->acc[3 * (size_t)q + d] = 0.0;
+        }
+        free(where);
+        for (int i = 0; i < s->nleaf; i++) {
+            o_leaf *lf = &s->leaf[i];
+            for (int q = lf->ipart; q < lf->ipart + lf->npart; q++)
+                if (s->part_on[q]) { s->leaf_on[i] = 1; break; }
+            if (s->leaf_on[i]) memset(lf->L, 0, sizeof lf->L);
+        }
+        mark_nodes(s, s->first_node);
+        for (int i = 0; i < s->nnode; i++)
+            if (s->node_on[i]) memset(s->node[i].L, 0, sizeof s->node[i].L);
+    }
+    int rc = run_p2p(s, &s->list[PO_LIST_P2P], 0);
+    if (rc) return rc;
+    run_m2l(s, &s->list[PO_LIST_M2L]);
+    if (s->acc_task) memcpy(s->acc_task, s->acc, sizeof(double) * 3 * (size_t)n);
+    if (s->p.images) {
+        rc = run_p2p(s, &s->list[PO_LIST_P2P_EXT], 1);
+        if (rc) return rc;
+        run_m2l(s, &s->list[PO_LIST_M2L_EXT]);
+    }
+    downward(s, s->first_node);
+    for (int i = 0; i < s->nleaf; i++) {
+        if (s->leaf_on && !s->leaf_on[i]) continue;
+        o_leaf *lf = &s->leaf[i];
+        po_l2p(lf->npart, s->pos + 3 * lf->ipart, lf->center, lf->L, s->acc + 3 * lf->ipart);
+    }
+    return PO_OK;
+}
+
 /* the whole pass: src/fmm.c:329-360 (construct), 719-770 (prepare),
-   909-984 (task), 987-1075 (ext) at one rank */
-int po_run(po_state *s, const po_params *p, int n, const double *pos_in, double *seconds)
+   909-984 (task), 987-1075 (ext) at one rank.  With targets, the tree,
+   walks, counters and multipoles are complete, but forces are formed only
+   for the listed particles (P2P into them, M2L into their leaves and
+   ancestors, L2L down those paths, L2P on them), in the same operation
+   order as the full pass, so their accelerations are identical to it. */
+static int run_pass(po_state *s, const po_params *p, int n, const double *pos_in, int nt, const int *targets,
+                    double *times)
 {
     init_tables();
-    if (!s || !p || n < 1 || p->maxleaf < 1) return PO_ERR_ARG;
+    if (!s || !p || n < 1 || p->maxleaf < 1 || nt < 0) return PO_ERR_ARG;
     if (n <= p->maxleaf) return PO_ERR_SMALL;
     free_run(s);
     for (int k = 0; k < 4; k++) s->list[k].n = 0;
@@ -764,14 +1008,14 @@ int po_run(po_state *s, const po_params *p, int n, const double *pos_in, double 
     s->pos = malloc(sizeof(double) * 3 * (size_t)n);
     s->perm = malloc(sizeof(int) * (size_t)n);
     s->acc = calloc(3 * (size_t)n, sizeof(double));
-    s->acc_task = calloc(3 * (size_t)n, sizeof(double));
+    s->acc_task = targets ? NULL : calloc(3 * (size_t)n, sizeof(double));
     /* capacity rule of src/fmm.c:203-209 */
     int cap = (int)(2.0 * ((double)n) / ((double)p->maxleaf));
     if (cap > n) cap = n + 1;
     s->nleaf_cap = s->nnode_cap = cap;
     s->leaf = calloc((size_t)cap, sizeof(o_leaf));
     s->node = calloc((size_t)cap, sizeof(o_node));
-    if (!s->pos || !s->perm || !s->acc || !s->acc_task || !s->leaf || !s->node) return PO_ERR_NOMEM;
+    if (!s->pos || !s->perm || !s->acc || (!targets && !s->acc_task) || !s->leaf || !s->node) return PO_ERR_NOMEM;
     for (int i = 0; i < cap; i++) s->node[i].son[0] = s->node[i].son[1] = -1;
     memcpy(s->pos, pos_in, sizeof(double) * 3 * (size_t)n);
     for (int i = 0; i < n; i++) s->perm[i] = i;
@@ -786,44 +1030,86 @@ int po_run(po_state *s, const po_params *p, int n, const double *pos_in, double 
     s->nnode = last_node - s->first_node + 1;
     double lo[3] = {0, 0, 0}, hi[3] = {p->boxsize, p->boxsize, p->boxsize};
     geometry(s, 0, s->first_node, lo, hi);
+    double t1 = wall();
     for (int i = 0; i < s->nleaf; i++) {
         o_leaf *lf = &s->leaf[i];
         po_p2m(lf->npart, s->pos + 3 * lf->ipart, p->mass, lf->center, lf->M);
     }
     upward(s, s->first_node);
-
-    s->image = 0;
-    walk_local(s, s->first_node, s->first_node);
-    if (s->err) return s->err;
-    int rc = run_p2p(s, &s->list[PO_LIST_P2P], 0);
+    double t2 = wall();
+    int rc = run_walks(s, p->images);
     if (rc) return rc;
-    run_m2l(s, &s->list[PO_LIST_M2L]);
-    memcpy(s->acc_task, s->acc, sizeof(double) * 3 * (size_t)n);
+    o_list *pe = &s->list[PO_LIST_P2P_EXT];
+    for (long e = 0; e < pe->n; e++)
+        s->p2p_count_remote += (long long)LEAF(s, pe->t[e])->npart * LEAF(s, pe->s[e])->npart;
+    double t3 = wall();
 
-    if (p->images) {
-        long start_p2p = s->list[PO_LIST_P2P_EXT].n;
-        long start_m2l = s->list[PO_LIST_M2L_EXT].n;
-        for (int img = 1; img < NIMG; img++) {
-            s->image = img;
-            image_shift(p, img, s->shift);
-            walk_image(s, s->first_node, s->first_node);
-            if (s->err) return s->err;
-        }
-        (void)start_p2p; (void)start_m2l;
-        o_list *pe = &s->list[PO_LIST_P2P_EXT];
-        for (long e = 0; e < pe->n; e++)
-            s->p2p_count_remote += (long long)LEAF(s, pe->t[e])->npart * LEAF(s, pe->s[e])->npart;
-        rc = run_p2p(s, pe, 1);
-        if (rc) return rc;
-        run_m2l(s, &s->list[PO_LIST_M2L_EXT]);
+    rc = forces(s, nt, targets);
+    if (rc) return rc;
+    double t4 = wall();
+    if (times) {
+        times[0] = t1 - t0;   /* tree build and geometry */
+        times[1] = t2 - t1;   /* P2M, M2M */
+        times[2] = t3 - t2;   /* local and image walks */
+        times[3] = t4 - t3;   /* forces (all particles, or the listed ones) */
     }
-    downward(s, s->first_node);
-    for (int i = 0; i < s->nleaf; i++) {
-        o_leaf *lf = &s->leaf[i];
-        po_l2p(lf->npart, s->pos + 3 * lf->ipart, lf->center, lf->L, s->acc + 3 * lf->ipart);
-    }
-    if (seconds) *seconds = wall() - t0;
     return PO_OK;
+}
+
+int po_run(po_state *s, const po_params *p, int n, const double *pos_in, double *seconds)
+{
+    double t[4];
+    int rc = run_pass(s, p, n, pos_in, 0, NULL, t);
+    if (rc == PO_OK && seconds) *seconds = t[0] + t[1] + t[2] + t[3];
+    return rc;
+}
+
+static int gather_targets(po_state *s, int nt, const int *targets, double *acc_out)
+{
+    int n = s->n;
+    int *where = malloc(sizeof(int) * (size_t)n);
+    if (!where) return PO_ERR_NOMEM;
+    for (int i = 0; i < n; i++) where[s->perm[i]] = i;
+    for (int k = 0; k < nt; k++)
+        for (int d = 0; d < 3; d++) acc_out[3 * k + d] = s->acc[3 * (size_t)where[targets[k]] + d];
+    free(where);
+    return PO_OK;
+}
+
+int po_run_sample(po_state *s, const po_params *p, int n, const double *pos_in, int nt, const int *targets,
+                  double *acc_out, double *times)
+{
+    if (!targets || !acc_out) return PO_ERR_ARG;
+    int rc = run_pass(s, p, n, pos_in, nt, targets, times);
+    if (rc != PO_OK) return rc;
+    return gather_targets(s, nt, targets, acc_out);
+}
+
+int po_forces_sample(po_state *s, int nt, const int *targets, double *acc_out, double *seconds)
+{
+    if (!s || !s->leaf || !targets || !acc_out || nt < 0) return PO_ERR_ARG;
+    double t0 = wall();
+    int rc = forces(s, nt, targets);
+    if (rc != PO_OK) return rc;
+    if (seconds) *seconds = wall() - t0;
+    return gather_targets(s, nt, targets, acc_out);
+}
+
+/* pairs of the local and image P2P lists as the reference evaluates them:
+   n_t n_s per task, minus the self pairs of a leaf with itself (local);
+   n_t n_s per image task */
+void po_pairs(const po_state *s, long long *pairs_local, long long *pairs_image)
+{
+    long long a = 0, b = 0;
+    const o_list *l = &s->list[PO_LIST_P2P];
+    for (long e = 0; e < l->n; e++) {
+        long long nt = LEAF(s, l->t[e])->npart, ns = LEAF(s, l->s[e])->npart;
+        a += l->t[e] == l->s[e] ? nt * (nt - 1) : nt * ns;
+    }
+    l = &s->list[PO_LIST_P2P_EXT];
+    for (long e = 0; e < l->n; e++) b += (long long)LEAF(s, l->t[e])->npart * LEAF(s, l->s[e])->npart;
+    *pairs_local = a;
+    *pairs_image = b;
 }
 
 void po_counters(const po_state *s, long long *c)

@@ -48,6 +48,19 @@ void po_destroy(po_state *s);
 /* One force pass.  Returns PO_OK or an error code; *seconds = wall time. */
 int po_run(po_state *s, const po_params *p, int n, const double *pos_in, double *seconds);
 
+/* The same pass with forces formed only for the particles targets[0..nt)
+   (input indices): tree, walks, counters and multipoles are complete; the
+   targets' accelerations are identical to the full pass's.  acc_out: nt*3;
+   times[4]: tree build, multipoles, walks, sampled forces (seconds). */
+int po_run_sample(po_state *s, const po_params *p, int n, const double *pos_in, int nt, const int *targets,
+                  double *acc_out, double *times);
+/* forces for another set of targets on the tree and lists of the last
+   po_run_sample (or po_run), without rebuilding them; *seconds = wall time */
+int po_forces_sample(po_state *s, int nt, const int *targets, double *acc_out, double *seconds);
+/* pairs of the last pass's local and image P2P lists as the reference
+   evaluates them (n_t n_s per task, minus a leaf's self pairs) */
+void po_pairs(const po_state *s, long long *pairs_local, long long *pairs_image);
+
 /* counters[16]: idxP2P, idxM2L, walk_m2l_count, p2p_count_remote, NLEAF, NNODE,
    nleaf, nnode, first_leaf, first_node, direct_local_start(0), n_p2p, n_m2l,
    n_p2p_ext, n_m2l_ext, n_images, in the reference's index space. */

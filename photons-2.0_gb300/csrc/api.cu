@@ -41,7 +41,7 @@ int ph_set_cuda_error(cudaError_t e, const char *what, const char *file, int lin
 }
 
 extern "C" int photons_gpu_status(void) { return g_status; }
-extern "C" unsigned long long photons_launch_count(void) { return ph::g_launches; }
+extern "C" unsigned long long photons_launch_count(void) { return ph::g_launches.load(std::memory_order_relaxed); }
 extern "C" const char *photons_gpu_error(void) { return g_msg; }
 extern "C" void photons_gpu_clear_error(void)
 {
@@ -50,7 +50,8 @@ extern "C" void photons_gpu_clear_error(void)
 }
 
 namespace ph {
-unsigned long long g_launches = 0;
+std::atomic<unsigned long long> g_launches{0};
+thread_local unsigned long long *t_capture_tally = nullptr;
 
 int device_sm_count()
 {
@@ -819,10 +820,11 @@ static int capture_pass(photons_ctx *c, const photons_params *p, const double *s
     PH_CUDA_CHECK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     c->capturing = true;
     // kernels are counted when the graph runs, not when it is captured
-    const unsigned long long launches_before = ph::g_launches;
+    unsigned long long tally = 0;
+    ph::t_capture_tally = &tally;
     int rc = ph_enqueue_pass(c, p, src, dst, levels, mask);
-    c->graph_kernels = ph::g_launches - launches_before;
-    ph::g_launches = launches_before;
+    ph::t_capture_tally = nullptr;
+    c->graph_kernels = tally;
     c->capturing = false;
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(st, &g);

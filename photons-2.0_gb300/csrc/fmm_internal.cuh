@@ -8,6 +8,7 @@
 // The reference's own index space (leaves from N, nodes from N+NLEAF,
 // src/fmm.c:211-212) is used only at the C-ABI boundary.
 #pragma once
+#include <atomic>
 
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -112,8 +113,17 @@ namespace ph {
 int device_sm_count();
 
 // number of kernels this library has launched (reported by photons_launch_count)
-extern unsigned long long g_launches;
-inline void note_launch() { g_launches++; }
+// kernels launched by this library (photons_launch_count).  Host threads
+// (the PM thread beside the force pass) add to it concurrently; a thread
+// that is capturing a graph counts into its own tally instead, and the
+// graph's kernels are added each time the graph is launched.
+extern std::atomic<unsigned long long> g_launches;
+extern thread_local unsigned long long *t_capture_tally;
+inline void note_launch()
+{
+    if (t_capture_tally) ++*t_capture_tally;
+    else g_launches.fetch_add(1, std::memory_order_relaxed);
+}
 
 // exclusive scan of n int32 values (n read on the device from n_ptr, at most
 // cap elements); writes total to *total (device) if total != nullptr.

@@ -18,8 +18,14 @@
 // Host code must not pass g_direct_scratch itself to a kernel: on the host
 // that name is a stand-in, not a device address.  The first call on each
 // device looks the address up with cudaGetSymbolAddress while that device is
-// current and keeps it; that first call should come before any stream
-// capture.
+// current and keeps it for that device's CUDA context (a new context, e.g.
+// after cudaDeviceReset, is looked up again); that first call should come
+// before any stream capture.  The library's device code is loaded lazily, so
+// the array itself is placed in device memory by that first lookup: a caller
+// that budgets all of HBM makes one warm-up call first (nt = 0 does only
+// the set-up and launches nothing).
+#include <cuda.h>
+
 #include <cmath>
 #include <mutex>
 
@@ -225,8 +231,30 @@ __global__ void k_na_direct(unsigned char *s, int ncell, double cellw, int nt, d
 
 std::mutex g_na_mutex;
 unsigned char *g_na_ptr[NA_MAX_DEVICES];  // device address of g_direct_scratch, per device
+CUcontext g_na_ctx[NA_MAX_DEVICES];       // the context that address belongs to
 
-// device address of the scratch on the current device (looked up once)
+// the current thread's CUDA context, through the runtime's driver entry
+// point (the library does not link the driver library itself)
+CUcontext na_current_context()
+{
+    typedef CUresult (*GetCurrent)(CUcontext *);
+    static GetCurrent fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (GetCurrent)f;
+        cudaGetLastError();
+    });
+    CUcontext ctx = nullptr;
+    if (fn) fn(&ctx);
+    return ctx;
+}
+
+// device address of the scratch on the current device, looked up once per
+// device and context
 int na_scratch(unsigned char **out)
 {
     int dev = -1;
@@ -235,25 +263,29 @@ int na_scratch(unsigned char **out)
     if (dev < 0 || dev >= NA_MAX_DEVICES)
         return ph_set_error(PH_ERR_UNSUPPORTED, "device %d beyond the %d devices the no-allocation scratch tracks", dev,
                             NA_MAX_DEVICES);
+    const CUcontext ctx = na_current_context();  // null before the runtime has set up this thread's context
     std::lock_guard<std::mutex> lock(g_na_mutex);
-    if (!g_na_ptr[dev]) {
+    if (!g_na_ptr[dev] || !ctx || ctx != g_na_ctx[dev]) {
         void *ptr = nullptr;
         e = cudaGetSymbolAddress(&ptr, g_direct_scratch);
         if (e != cudaSuccess) return ph_set_cuda_error(e, "cudaGetSymbolAddress(no-allocation scratch)", __FILE__, __LINE__);
         g_na_ptr[dev] = (unsigned char *)ptr;
+        g_na_ctx[dev] = na_current_context();
     }
     *out = g_na_ptr[dev];
     return 0;
 }
 
-bool na_device_pointer(const void *ptr)
+// device memory (or managed memory) that the current device can use directly
+bool na_device_pointer(const void *ptr, int dev)
 {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    if (a.type == cudaMemoryTypeManaged) return true;
+    return a.type == cudaMemoryTypeDevice && a.device == dev;
 }
 
 }  // namespace
@@ -268,11 +300,14 @@ extern "C" int photons_direct_sum_noalloc(const photons_params *p, int n, const 
         return ph_set_error(PH_ERR_ARG, "no-allocation direct sum: %d sources exceed the maximum %d", n, NA_MAX_SOURCES);
     if (nt > NA_MAX_TARGETS)
         return ph_set_error(PH_ERR_ARG, "no-allocation direct sum: %d targets exceed the maximum %d", nt, NA_MAX_TARGETS);
-    if (nt == 0) return 0;
-    if (!na_device_pointer(pos) || !na_device_pointer(targets) || !na_device_pointer(acc))
-        return ph_set_error(PH_ERR_ARG, "no-allocation direct sum: pos, targets and acc must be device pointers");
     unsigned char *s = nullptr;
-    if (int rc = na_scratch(&s)) return rc;
+    if (int rc = na_scratch(&s)) return rc;  // with nt = 0 the call is the warm-up: set-up only
+    if (nt == 0) return 0;
+    int dev = -1;
+    cudaGetDevice(&dev);
+    if (!na_device_pointer(pos, dev) || !na_device_pointer(targets, dev) || !na_device_pointer(acc, dev))
+        return ph_set_error(PH_ERR_ARG, "no-allocation direct sum: pos, targets and acc must be device pointers "
+                                        "on the current device (%d)", dev);
 
     const double L = p->boxsize;
     int ncell = (int)(L / rmax);

@@ -260,3 +260,42 @@ def test_fp32_split_precision_clustered(ph, fp, ics, nside, maxleaf):
     e = rel_err(a32, a64, p)
     assert np.median(e) <= 2e-6, np.median(e)
     assert np.percentile(e, 99) <= 2e-5, np.percentile(e, 99)
+
+
+def _full_size_parity(ph, fp, port, pos, p, precision, tol, nsub=10000):
+    """The GPU pass against the oracle at a workload's full size: counters,
+    the tree-order permutation, every list as a multiset, and the forces on
+    a random subset of particles (the oracle forms only those)."""
+    import os
+    n = pos.shape[0]
+    tg = np.random.default_rng(17).choice(n, nsub, replace=False).astype(np.int32)
+    r = port.run_sample(pos, p, tg, nthreads=os.cpu_count() or 4, lists=True, perm=True)
+    acc = fp.run(pos, p, precision=precision, flags=ph.F_KEEP_LISTS)
+    c = fp.counters()
+    for k in ("nleaf", "nnode", "idxP2P", "idxM2L", "walk_m2l_count", "p2p_count_remote", "n_p2p_ext", "n_m2l_ext",
+              "pairs_local", "pairs_image"):
+        assert c[k] == r["counters"][k], k
+    assert np.array_equal(fp.perm(), r["perm"])
+    gl = fp.lists()
+    for kind, (t, s, im) in r["lists"].items():
+        assert digest(*gl[kind]) == digest(t, s, im), kind
+    e = rel_err(acc[tg], r["acc"], p)
+    assert e.max() <= tol, e.max()
+    return e
+
+
+@pytest.mark.parametrize("maxleaf", [16, 24])
+def test_c1_nfw128_full_size_matches_oracle(ph, fp, ics, port, maxleaf):
+    """128^3 particles, 50 % in 64 NFW halos (local and image M2L occur): the
+    reference's leaf 16 and the autotuned leaf 24, FP64 within 1e-10."""
+    pos, p = ics.make("nfw128", maxleaf=maxleaf)
+    _full_size_parity(ph, fp, port, pos, p, ph.FP64, FP64_TOL)
+
+
+def test_c2_zeldovich256_full_size_lists_match_oracle(ph, fp, ics, port):
+    """The headline input, 256^3 at leaf 64: tree, permutation, counters and
+    lists identical to the oracle's; the FP32 split forces on 10^4 particles
+    within the split-precision bar of the oracle's FP64 ones."""
+    pos, p = ics.make("zeldovich256", maxleaf=64)
+    e = _full_size_parity(ph, fp, port, pos, p, ph.FP32_SPLIT, 1e-3)
+    assert np.median(e) <= 2e-6, np.median(e)

@@ -144,3 +144,50 @@ def test_direct_sum_small(port):
         f = p["mass"] * (erfc(u) + 2 / np.sqrt(np.pi) * u * np.exp(-u * u)) / np.maximum(rr, p["eps"]) ** 3
         want = (d[m] * f[:, None]).sum(0)
         assert np.allclose(got[k], want, rtol=1e-12, atol=1e-15)
+
+
+@pytest.mark.parametrize("name,nside,maxleaf", [("grid32", 16, 16), ("nfw128", 24, 8)])
+def test_port_walks_on_threads_keep_the_sequential_lists(port, ics, name, nside, maxleaf):
+    """The walks run as sub-walks on several threads and are concatenated in
+    traversal order: the lists equal the one-thread walk's, in order."""
+    pos, p = ics.make(name, nside=nside, maxleaf=maxleaf)
+    a = port.run(pos, p, capture=True, tree=False, nthreads=1)
+    b = port.run(pos, p, capture=True, tree=False, nthreads=6)
+    assert a["counters"] == b["counters"]
+    for kind in a["lists"]:
+        assert all(np.array_equal(x, y) for x, y in zip(a["lists"][kind], b["lists"][kind])), kind
+    assert np.array_equal(a["acc"], b["acc"])
+
+
+@pytest.mark.parametrize("name,nside,maxleaf", [("zeldovich256", 20, 64), ("nfw128", 24, 8)])
+def test_port_sampled_pass_equals_full_pass(port, ics, name, nside, maxleaf):
+    """Forces for a target subset only (the parity leg at full size): the
+    subset's accelerations, counters and permutation are the full pass's,
+    bit for bit, also when the tree is reused for another subset; the pair
+    counts are the reference's pair set."""
+    pos, p = ics.make(name, nside=nside, maxleaf=maxleaf)
+    n = pos.shape[0]
+    full = port.run(pos, p, capture=True, tree=True, nthreads=4)
+    acc = np.empty_like(full["acc"])
+    acc[full["perm"]] = full["acc"]
+    rng = np.random.default_rng(3)
+    tg = rng.choice(n, 300, replace=False).astype(np.int32)
+    r = port.run_sample(pos, p, tg, nthreads=4, lists=True, perm=True)
+    assert np.array_equal(r["acc"], acc[tg])
+    assert np.array_equal(r["perm"], full["perm"])
+    for k, v in full["counters"].items():
+        assert r["counters"][k] == v, k
+    for kind in full["lists"]:
+        assert all(np.array_equal(x, y) for x, y in zip(full["lists"][kind], r["lists"][kind])), kind
+    # the reference's pair set: n_t n_s per task less a leaf's self pairs, plus image pairs
+    tr = full["tree"]
+    first = full["counters"]["first_leaf"]
+    t, s, _ = full["lists"]["p2p"]
+    nt, ns = tr["leaf_npart"][t - first].astype(np.int64), tr["leaf_npart"][s - first].astype(np.int64)
+    assert r["counters"]["pairs_local"] == int(np.where(t == s, nt * (nt - 1), nt * ns).sum())
+    assert r["counters"]["pairs_image"] == full["counters"]["p2p_count_remote"]
+    tg2 = rng.choice(n, 200, replace=False).astype(np.int32)
+    a2, secs = port.forces_sample(tg2)
+    assert np.array_equal(a2, acc[tg2]) and secs >= 0
+    a3, _ = port.forces_sample(tg)
+    assert np.array_equal(a3, acc[tg])

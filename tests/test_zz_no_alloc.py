@@ -69,6 +69,29 @@ def test_noalloc_matches_direct_sum_two_calls(ph, ics, noalloc):
         assert rel_err(got, want, p, pos.shape[0]).max() <= TOL, f"call {k + 1}"
 
 
+def test_noalloc_allocates_nothing_after_warm_up(ph, ics, noalloc):
+    """After the warm-up call (nt = 0: set-up only) a call leaves the
+    device's free memory unchanged, i.e. it allocated nothing."""
+    torch = pytest.importorskip("torch")
+    pos, p = ics.make("nfw128", nside=32)
+    dpos = torch.from_numpy(np.ascontiguousarray(pos, np.float64)).cuda()
+    dtargets = torch.arange(0, pos.shape[0], 97, dtype=torch.int32, device="cuda")
+    dacc = torch.empty((dtargets.shape[0], 3), dtype=torch.float64, device="cuda")
+    rc, msg = _call(noalloc, ph, p, dpos, dtargets, dacc, p["rcut"], nt=0)
+    assert rc == 0, msg
+    rc, msg = _call(noalloc, ph, p, dpos, dtargets, dacc, p["rcut"])  # first real call after the set-up
+    assert rc == 0, msg
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    stats0 = torch.cuda.memory_stats().get("allocation.all.allocated", 0)
+    for _ in range(3):
+        rc, msg = _call(noalloc, ph, p, dpos, dtargets, dacc, p["rcut"])
+        assert rc == 0, msg
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert torch.cuda.memory_stats().get("allocation.all.allocated", 0) == stats0
+
+
 def test_noalloc_rejects_bad_input(ph, ics, noalloc):
     torch = pytest.importorskip("torch")
     pos, p = ics.make("grid32", nside=8)
