@@ -587,15 +587,22 @@ def main():
     free0, total_hbm = torch.cuda.mem_get_info()
     fp = ph.ForcePass(local)
     tune = None
-    pflags = 0  # PHOTONS_F_ONE_WAY where the autotuner found the one-way P2P kernel faster
+    pflags = 0  # the autotuner's kernel choice: PHOTONS_F_ONE_WAY, or the mutual kernel's build (shape bits)
     if not args.maxleaf:
         best, table, pflags = ph.autotune_leaf(fp, pos, p, error_bound=args.error_bound)
         best = broadcast_from_rank0(best, dist, "cuda")  # every replica runs rank 0's choice
         pflags = broadcast_from_rank0(pflags, dist, "cuda")
         p["maxleaf"] = best
-        tune = {"chosen_maxleaf": best, "chosen_kernel": "one-way" if (pflags or best < 48) else "mutual",
+        one_way = bool(pflags & ph.F_ONE_WAY) or best < 48
+        tune = {"chosen_maxleaf": best,
+                "chosen_kernel": "one-way" if one_way else "mutual shape %d" % ((pflags >> 8) & 15),
+                "chosen_flags": pflags,
                 "error_bound_median": args.error_bound, "candidates": table,
                 "score": "fastest pass with median error vs the FP64 direct sum <= bound (2000-particle sample)"}
+        # the candidates' smaller leaves grew the context's list pools: time the
+        # chosen configuration in a fresh context sized for it alone
+        fp.close()
+        fp = ph.ForcePass(local)
     stream = torch.cuda.current_stream()
     fp.set_stream(stream.cuda_stream)
     dpos = torch.from_numpy(pos).to("cuda")
@@ -675,7 +682,8 @@ def main():
     # for both leaves, so the pairs it evaluates are about half the
     # reference's pair set (self pairs, about 1 %, are counted at half here
     # although they are evaluated in full)
-    mutual = p["maxleaf"] >= 48 and not pflags and os.environ.get("PHOTONS_P2P_KERNEL", "mutual") == "mutual"
+    mutual = p["maxleaf"] >= 48 and not (pflags & ph.F_ONE_WAY) and \
+        os.environ.get("PHOTONS_P2P_KERNEL", "mutual") == "mutual"
     kernel = "k_p2p_mutual" if mutual else "k_p2p_split_packed"
     evaluated = pairs // 2 if mutual else pairs
     peak = ph.fp32_fma_peak(8192)

@@ -61,6 +61,17 @@ int acceptance(double wi[3], double wj[3], double dist[3]);
    (src/remotes.c:684-751); at one rank idx must be 0 */
 void fmm_remote(int idx, double shift[3]);
 
+/* inc/kernels.h:4-8 -- one local P2P task on the GPU in FP64: the particles
+   of leaf inode from those of leaf jnode (reference leaf ids, after
+   fmm_prepare), added to part[].acc as src/fmm.c:823-868 adds a task.  The
+   reference declares these but never defines them.  p2p_kernel evaluates
+   the pair force as src/fmm.c:834-852 writes it; p2p_kernel_rinvsqrt the
+   same force with 1/r from the reciprocal square root and one exponential;
+   p2p_kernel_inleaf a leaf with itself (jnode == inode), self pairs skipped. */
+void p2p_kernel(int inode, int jnode);
+void p2p_kernel_rinvsqrt(int inode, int jnode);
+void p2p_kernel_inleaf(int inode, int jnode);
+
 /* inc/partmesh.h:16-17, 22 -- the PM long-range force at one rank, on the
    GPU (src/partmesh.c:18-795 in the -DPMTHREAD build, :800-1582 without):
    part[].acc_pm from part[].pos on an NSIDE^3 mesh with splitRadius,
@@ -106,6 +117,13 @@ typedef struct photons_params {
 #define PHOTONS_F_MULTIPOLES 8      /* compute P2M/M2M even when no M2L task exists */
 #define PHOTONS_F_KEEP_LISTS 16     /* keep lists for photons_list_* */
 #define PHOTONS_F_ONE_WAY 32        /* FP32: every pair one way (no mutual pairs, no reaction slots) */
+/* FP32 mutual P2P kernel build (bits 8-11): 0 chosen by MAXLEAF; 1 three
+   blocks per SM, two dependency chains; 2 four blocks, one chain, 6-target
+   path; 3 three blocks, one chain; 4 four blocks, two chains.  The builds
+   give identical forces; the autotuner times them. */
+#define PHOTONS_F_P2P_SHAPE(s) ((s) << 8)
+#define PHOTONS_F_SHAPE_OF(f) (((f) >> 8) & 15)
+#define PHOTONS_P2P_SHAPES 5
 
 typedef struct photons_ctx photons_ctx;
 

@@ -32,6 +32,12 @@ F_NO_FARFIELD = 4
 F_MULTIPOLES = 8
 F_KEEP_LISTS = 16
 F_ONE_WAY = 32
+P2P_SHAPES = 5
+
+
+def F_P2P_SHAPE(shape):
+    """Flag bits naming the FP32 mutual P2P kernel build (0: chosen by MAXLEAF)."""
+    return int(shape) << 8
 
 NMULTI = 20
 LIST_KINDS = {"p2p": 0, "m2l": 1, "p2p_ext": 2, "m2l_ext": 3}
@@ -462,43 +468,60 @@ class Reference:
 
 
 def autotune_leaf(fp, pos, p, candidates=(16, 24, 32, 48, 64), error_bound=1e-4, sample=2000, repeats=2,
-                  precision=FP32_SPLIT, seed=11):
-    """Pick MAXLEAF (and, at leaf sizes 48-64, the FP32 P2P kernel) for this
-    input: the fastest candidate whose median relative force error against
-    the FP64 direct sum (untruncated split kernel within 2 rcut, `sample`
-    random particles) is within `error_bound`; if none qualifies, the most
-    accurate one.  From leaf 48 the pass evaluates each symmetric leaf pair
-    once by default; halo-dominated inputs can run faster one way
-    (F_ONE_WAY), so both are timed there.  The two give the same forces to
-    FP32 rounding.
+                  precision=FP32_SPLIT, seed=11, shapes=True):
+    """Pick MAXLEAF and the FP32 P2P kernel for this input.
+
+    Leaf size: the fastest candidate whose median relative force error
+    against the FP64 direct sum (untruncated split kernel within 2 rcut,
+    `sample` random particles) is within `error_bound`; if none qualifies,
+    the most accurate one.  From leaf 48 the pass evaluates each symmetric
+    leaf pair once by default; halo-dominated inputs can run faster one way
+    (F_ONE_WAY), so both are timed there.  Kernel shape (with `shapes`): at
+    the chosen leaf size, when the mutual kernel won, each of its builds
+    (resident blocks per SM, interleaved dependency chains, the 6-target
+    path; F_P2P_SHAPE) is timed and the fastest kept.  All of these give the
+    same forces to FP32 rounding.
 
     Returns (best_leaf, table, flags): table lists, per candidate, the pass
     time on the device (ms, CUDA events: tree, walk, P2P, far field,
-    gather), pairs per particle, the median / 99th-percentile error and the
-    kernel; flags is 0 or F_ONE_WAY for the chosen candidate."""
+    gather), pairs per particle, the median / 99th-percentile error, the
+    kernel and its flags; flags are those of the chosen candidate."""
     pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
     rng = np.random.default_rng(seed)
     tgt = rng.choice(pos.shape[0], min(sample, pos.shape[0]), replace=False).astype(np.int32)
     ref = direct_sum(pos, p, tgt)
     nref = np.linalg.norm(ref, axis=1)
     table = []
-    for leaf in candidates:
+
+    def trial(leaf, flags, kernel):
         q = dict(p)
         q["maxleaf"] = int(leaf)
-        kernels = [0, F_ONE_WAY] if (precision == FP32_SPLIT and 48 <= leaf <= 64) else [0]
-        for flags in kernels:
-            ms = []
-            acc = None
-            for _ in range(repeats):
-                acc = fp.run(pos, q, precision=precision, flags=flags)
-                t = fp.timings()
-                ms.append(t["total"] - t["upload"] - t["download"])  # the device part of the pass
-            c = fp.counters()
-            err = np.linalg.norm(acc[tgt] - ref, axis=1) / np.maximum(nref, 1e-300)
-            table.append(dict(maxleaf=int(leaf), ms=float(min(ms)), median=float(np.median(err)),
-                              p99=float(np.percentile(err, 99)),
-                              pairs_per_particle=(c["pairs_local"] + c["pairs_image"]) / pos.shape[0],
-                              kernel="one-way" if (flags or len(kernels) == 1) else "mutual", flags=flags))
+        ms = []
+        acc = None
+        for _ in range(repeats):
+            acc = fp.run(pos, q, precision=precision, flags=flags)
+            t = fp.timings()
+            ms.append(t["total"] - t["upload"] - t["download"])  # the device part of the pass
+        c = fp.counters()
+        err = np.linalg.norm(acc[tgt] - ref, axis=1) / np.maximum(nref, 1e-300)
+        row = dict(maxleaf=int(leaf), ms=float(min(ms)), median=float(np.median(err)),
+                   p99=float(np.percentile(err, 99)),
+                   pairs_per_particle=(c["pairs_local"] + c["pairs_image"]) / pos.shape[0], kernel=kernel,
+                   flags=int(flags))
+        table.append(row)
+        return row
+
+    for leaf in candidates:
+        mutual = precision == FP32_SPLIT and 48 <= leaf <= 64
+        trial(leaf, 0, "mutual" if mutual else "one-way")
+        if mutual:
+            trial(leaf, F_ONE_WAY, "one-way")
     ok = [t for t in table if t["median"] <= error_bound]
     best = min(ok, key=lambda t: t["ms"]) if ok else min(table, key=lambda t: t["median"])
+    if shapes and precision == FP32_SPLIT and best["kernel"] == "mutual":
+        leaf = best["maxleaf"]
+        for flags, kernel in [(F_P2P_SHAPE(sh), "mutual shape %d" % sh) for sh in range(1, P2P_SHAPES)]:
+            row = trial(leaf, flags, kernel)
+            if row["ms"] < best["ms"] and row["median"] <= max(error_bound, best["median"]):
+                best = row
     return best["maxleaf"], table, best["flags"]

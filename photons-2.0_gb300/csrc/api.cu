@@ -369,6 +369,8 @@ int ph_validate(const photons_params *p, int n)
         return ph_set_error(PH_ERR_ARG, "invalid force parameters");
     if (p->precision != PHOTONS_FP32_SPLIT && p->precision != PHOTONS_FP64)
         return ph_set_error(PH_ERR_ARG, "unknown precision %d", p->precision);
+    if (PHOTONS_F_SHAPE_OF(p->flags) >= PHOTONS_P2P_SHAPES)
+        return ph_set_error(PH_ERR_ARG, "unknown P2P kernel shape %d", PHOTONS_F_SHAPE_OF(p->flags));
     // leaves + nodes are addressed with 27-bit ids in the lists: 2 x (2N/MAXLEAF) + 2 < 2^27
     if (2.0 * (2.0 * n / p->maxleaf) + 2.0 >= (double)PH_MAX_UNIFIED)
         return ph_set_error(PH_ERR_ARG, "N=%d with MAXLEAF=%d exceeds the 2^27 tree-id space", n, p->maxleaf);
@@ -682,6 +684,7 @@ int ph_stage_p2p(photons_ctx *c, int precision, int zero)
     a.boxsize = c->pp.boxsize; a.eps = c->pp.eps; a.mass = c->pp.mass; a.rs = c->pp.rs;
     a.k = ph::make_split_consts(c->pp);
     a.variant = p2p_variant();
+    a.shape = PHOTONS_F_SHAPE_OF(c->pass_flags);
     PH_TRY(ph_record(c, EV_P2P_BEGIN));
     if (uses_mutual(c, precision)) {
         ph::MutualBufs m;

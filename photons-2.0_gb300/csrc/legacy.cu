@@ -290,6 +290,80 @@ extern "C" void fmm_remote(int idx, double shift[3])
     p2p_count_remote += c->ws.c[ph::WC_PAIRS_IMAGE];
 }
 
+// ------------------------------------------------------------------
+// inc/kernels.h:4-8: one local P2P task, leaf inode's particles from leaf
+// jnode's (reference leaf ids, after fmm_prepare), on the GPU in FP64 and
+// added to part[].acc as src/fmm.c:823-868 adds a task.  The reference
+// declares these three but never defines them; here
+//   p2p_kernel           the pair force as src/fmm.c:834-852 writes it
+//                        (sqrt, division, erfc, exp)
+//   p2p_kernel_rinvsqrt  the same force with 1/r from the reciprocal
+//                        square root and one exponential (the FP64 pass's form)
+//   p2p_kernel_inleaf    a leaf with itself (jnode must equal inode), self
+//                        pairs skipped
+// ------------------------------------------------------------------
+static double *g_pair_dev = nullptr;  // [targets | sources | out], 3 doubles per particle each
+static int g_pair_cap = 0;
+static std::vector<double> g_pair_host;
+
+static void leaf_pair(int inode, int jnode, int exact, const char *who)
+{
+    photons_gpu_clear_error();
+    if (!leaf || !part) { ph_set_error(PH_ERR_STATE, "%s: fmm_prepare has not run", who); fatal(who); }
+    if (inode < first_leaf || inode >= last_leaf || jnode < first_leaf || jnode >= last_leaf) {
+        ph_set_error(PH_ERR_ARG, "%s(%d, %d): leaf ids must lie in [%d, %d)", who, inode, jnode, first_leaf, last_leaf);
+        fatal(who);
+    }
+    photons_ctx *c = ctx();
+    const Pack &T = leaf[inode], &S = leaf[jnode];
+    const int cap = T.npart > S.npart ? T.npart : S.npart;
+    if (cap > g_pair_cap) {
+        cudaFree(g_pair_dev);
+        g_pair_dev = nullptr;
+        g_pair_cap = 0;
+        if (cudaMalloc(&g_pair_dev, sizeof(double) * 9 * (size_t)cap) != cudaSuccess) {
+            cudaGetLastError();
+            ph_set_error(PH_ERR_NOMEM, "%s: device buffer", who);
+            fatal(who);
+        }
+        g_pair_cap = cap;
+    }
+    g_pair_host.resize((size_t)3 * (T.npart + S.npart));
+    for (int q = 0; q < T.npart; q++)
+        for (int d = 0; d < 3; d++) g_pair_host[3 * (size_t)q + d] = part[T.ipart + q].pos[d];
+    for (int q = 0; q < S.npart; q++)
+        for (int d = 0; d < 3; d++) g_pair_host[3 * (size_t)(T.npart + q) + d] = part[S.ipart + q].pos[d];
+    double *dt = g_pair_dev, *ds = g_pair_dev + 3 * (size_t)cap, *dout = g_pair_dev + 6 * (size_t)cap;
+    cudaStream_t st = c->stream;
+    cudaError_t e = cudaMemcpyAsync(dt, g_pair_host.data(), sizeof(double) * 3 * T.npart, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ds, g_pair_host.data() + 3 * (size_t)T.npart, sizeof(double) * 3 * S.npart,
+                            cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) { ph_set_cuda_error(e, "cudaMemcpyAsync", __FILE__, __LINE__); fatal(who); }
+    if (ph::launch_leaf_pair_fp64(dt, T.npart, T.ipart, ds, S.npart, S.ipart, SoftenScale, MASSPART, splitRadius, exact,
+                                  dout, st))
+        fatal(who);
+    e = cudaMemcpyAsync(g_pair_host.data(), dout, sizeof(double) * 3 * T.npart, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) { ph_set_cuda_error(e, "leaf pair", __FILE__, __LINE__); fatal(who); }
+    for (int q = 0; q < T.npart; q++)
+        for (int d = 0; d < 3; d++) part[T.ipart + q].acc[d] += g_pair_host[3 * (size_t)q + d];
+}
+
+extern "C" void p2p_kernel(int inode, int jnode) { leaf_pair(inode, jnode, 1, "p2p_kernel"); }
+
+extern "C" void p2p_kernel_rinvsqrt(int inode, int jnode) { leaf_pair(inode, jnode, 0, "p2p_kernel_rinvsqrt"); }
+
+extern "C" void p2p_kernel_inleaf(int inode, int jnode)
+{
+    if (inode != jnode) {
+        photons_gpu_clear_error();
+        ph_set_error(PH_ERR_ARG, "p2p_kernel_inleaf(%d, %d): a leaf with itself takes equal ids", inode, jnode);
+        fatal("p2p_kernel_inleaf");
+    }
+    leaf_pair(inode, inode, 1, "p2p_kernel_inleaf");
+}
+
 // src/fmm.c:1077-1087
 extern "C" void fmm_deconstruct(void)
 {

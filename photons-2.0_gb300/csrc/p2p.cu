@@ -757,10 +757,6 @@ constexpr int kMuUnroll = MU_UNROLL;
 // two target pairs evaluated stage by stage together; below 60, 4 blocks
 // (126 registers) and one pair at a time (256^3: 65.3 vs 66.4 ms at leaf 64,
 // 55.5 vs 59.6 ms at leaf 48)
-#define MU_WIDE_MINB 3
-#define MU_WIDE_IL 2
-#define MU_NARROW_MINB 4
-#define MU_NARROW_IL 1
 #ifndef MU_BATCH
 #define MU_BATCH 32  // sources per reaction reduction (32 or 16)
 #endif
@@ -1291,6 +1287,47 @@ __global__ void __launch_bounds__(256, 3) k_mu_gather(P2PArgs A, const int *slot
     }
 }
 
+// One leaf pair in FP64, the entry points of inc/kernels.h: forces on the
+// nt targets at tpos (particle indices tfirst..) from the ns sources at spos
+// (indices sfirst..), a source skipped where its index is the target's (a
+// leaf with itself), summed per target in source order as
+// src/fmm.c:823-855 sums a task.  exact: sqrt, division, erfc and exp as the
+// reference writes them; otherwise 1/r from rsqrt and one exponential with
+// erfcx (the FP64 pass's form).  out[3 q + d] = the target's sum.
+__global__ void k_leaf_pair_fp64(const double *tpos, int nt, int tfirst, const double *spos, int ns, int sfirst,
+                                 double eps, double mass, double rs, int exact, double *out)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nt) return;
+    const double px = tpos[3 * q], py = tpos[3 * q + 1], pz = tpos[3 * q + 2];
+    const double coeff = 2.0 / sqrt(M_PI), soft3 = mass / (eps * eps * eps), hrs = 0.5 / rs;
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    for (int j = 0; j < ns; j++) {
+        if (sfirst + j == tfirst + q) continue;
+        const double dx = spos[3 * j] - px, dy = spos[3 * j + 1] - py, dz = spos[3 * j + 2] - pz;
+        double ir3;
+        if (exact) {
+            const double dr = sqrt(dx * dx + dy * dy + dz * dz);
+            ir3 = (dr < eps) ? soft3 : mass / (dr * dr * dr);
+            const double drs = 0.5 * dr / rs;
+            ir3 *= (erfc(drs) + coeff * drs * exp(-drs * drs));
+        } else {
+            const double r2 = dx * dx + dy * dy + dz * dz;
+            const double rinv = rsqrt(r2);
+            const double dr = r2 * rinv;
+            ir3 = (dr < eps) ? soft3 : mass * (rinv * rinv * rinv);
+            const double drs = dr * hrs;
+            ir3 *= exp(-drs * drs) * (erfcx(drs) + coeff * drs);
+        }
+        ax += dx * ir3;
+        ay += dy * ir3;
+        az += dz * ir3;
+    }
+    out[3 * q] = ax;
+    out[3 * q + 1] = ay;
+    out[3 * q + 2] = az;
+}
+
 }  // namespace
 
 // coordinate scale of the packed kernel, rounded to FP32 first so that the
@@ -1341,13 +1378,36 @@ int launch_p2p_mutual(const P2PArgs &a, const MutualBufs &m, cudaStream_t st)
     scan_exclusive_i64(m.size, m.rbase, a.tree_cnt + BC_LEAVES, m.cap_leaves, m.total, m.scan_scratch, st);
     ph::note_launch(), k_mu_slots<<<sms * 8, 256, 0, st>>>(a.tree_cnt, a.walk_flags, m.pool, a.p2p_off, a.p2p_cnt,
                                                             m.total, m.buf_cap, m.pq, m.slot, m.ev, m.nev, m.over);
-    if (m.maxleaf >= 60)
-        ph::note_launch(), k_p2p_mutual<MU_WIDE_MINB, MU_WIDE_IL, false>
-            <<<sms * MU_WIDE_MINB, MU_TB, 0, st>>>(a, m.ev, m.nev, m.rbase, m.buf);
-    else
-        ph::note_launch(), k_p2p_mutual<MU_NARROW_MINB, MU_NARROW_IL, true>
-            <<<sms * MU_NARROW_MINB, MU_TB, 0, st>>>(a, m.ev, m.nev, m.rbase, m.buf);
+    // the build: shape 0 picks by MAXLEAF (three blocks per SM with two
+    // chains from leaf 60, else four blocks with one chain and the 6-target
+    // path); 1-4 name a build for the autotuner (PHOTONS_F_P2P_SHAPE)
+    int shape = a.shape;
+    if (shape == 0) shape = m.maxleaf >= 60 ? 1 : 2;
+    switch (shape) {
+    case 1:
+        ph::note_launch(), k_p2p_mutual<3, 2, false><<<sms * 3, MU_TB, 0, st>>>(a, m.ev, m.nev, m.rbase, m.buf);
+        break;
+    case 2:
+        ph::note_launch(), k_p2p_mutual<4, 1, true><<<sms * 4, MU_TB, 0, st>>>(a, m.ev, m.nev, m.rbase, m.buf);
+        break;
+    case 3:
+        ph::note_launch(), k_p2p_mutual<3, 1, false><<<sms * 3, MU_TB, 0, st>>>(a, m.ev, m.nev, m.rbase, m.buf);
+        break;
+    default:
+        ph::note_launch(), k_p2p_mutual<4, 2, true><<<sms * 4, MU_TB, 0, st>>>(a, m.ev, m.nev, m.rbase, m.buf);
+        break;
+    }
     ph::note_launch(), k_mu_gather<<<sms * 3, 256, 0, st>>>(a, m.slot, m.nrecv, m.rbase, m.buf);
+    PH_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
+int launch_leaf_pair_fp64(const double *tpos, int nt, int tfirst, const double *spos, int ns, int sfirst, double eps,
+                          double mass, double rs, int exact, double *out, cudaStream_t st)
+{
+    if (nt <= 0) return 0;
+    ph::note_launch(), k_leaf_pair_fp64<<<(nt + 63) / 64, 64, 0, st>>>(tpos, nt, tfirst, spos, ns, sfirst, eps, mass, rs,
+                                                                      exact, out);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }

@@ -38,6 +38,7 @@ struct P2PArgs {
     int nbox;
     SplitConsts k;                  // scalar kernel: all fields; packed: the polynomial coefficients
     int variant;  // FP32: 0 packed (default), 1 scalar
+    int shape;    // mutual kernel build (0: by MAXLEAF; see launch_p2p_mutual)
 };
 
 // buffers of the mutual FP32 kernel (see launch_p2p_mutual)
@@ -65,5 +66,9 @@ int launch_p2p_mutual(const P2PArgs &a, const MutualBufs &m, cudaStream_t st);
 double split_sig(const PassParams &p);
 int launch_leaf_offsets(const BuildBufs &b, const TreeBufs &t, float4 *pos4, cudaStream_t st);
 int launch_p2p(const P2PArgs &a, int fp64, cudaStream_t st);
+// one leaf pair in FP64 (inc/kernels.h): out[3 nt] = forces on tpos[3 nt]
+// (indices tfirst..) from spos[3 ns] (indices sfirst..), equal indices skipped
+int launch_leaf_pair_fp64(const double *tpos, int nt, int tfirst, const double *spos, int ns, int sfirst, double eps,
+                          double mass, double rs, int exact, double *out, cudaStream_t st);
 
 }  // namespace ph

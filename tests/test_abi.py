@@ -28,7 +28,8 @@ def test_header_declares_reference_entry_points():
     names = declared_functions()
     for ref in ("fmm_construct", "fmm_prepare", "fmm_task", "fmm_ext", "fmm_deconstruct", "build_localtree",
                 "p2m", "m2m", "m2l", "l2l", "l2p", "walk_m2m", "walk_l2l", "acceptance", "fmm_remote",
-                "partmesh_thread", "partmesh", "pm_thread", "get_local_size_"):
+                "partmesh_thread", "partmesh", "pm_thread", "get_local_size_", "p2p_kernel", "p2p_kernel_inleaf",
+                "p2p_kernel_rinvsqrt"):
         assert ref in names
 
 

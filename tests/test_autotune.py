@@ -50,7 +50,8 @@ def test_fastest_within_bound_and_both_kernels_timed(ph, setup):
     ms = {(16, 0): 9.0, (32, 0): 7.0, (48, 0): 6.0, (48, ow): 6.5, (64, 0): 5.0, (64, ow): 5.5}
     err = {(16, 0): 5e-4, (32, 0): 9e-5, (48, 0): 6e-5, (48, ow): 6e-5, (64, 0): 2e-5, (64, ow): 2e-5}
     fp = StandInPass(truth, ms, err)
-    best, table, flags = ph.autotune_leaf(fp, pos, p, candidates=(16, 32, 48, 64), sample=200, repeats=2)
+    best, table, flags = ph.autotune_leaf(fp, pos, p, candidates=(16, 32, 48, 64), sample=200, repeats=2,
+                                          shapes=False)
     assert (best, flags) == (64, 0)
     # every candidate ran `repeats` times; leaf 48 and 64 once per kernel
     keys = [k for k, _ in fp.runs]
@@ -74,7 +75,7 @@ def test_one_way_kernel_chosen_where_faster(ph, setup):
     ms = {(32, 0): 7.0, (48, 0): 6.0, (48, ow): 4.0}
     err = {(32, 0): 3e-5, (48, 0): 2e-5, (48, ow): 2e-5}
     best, table, flags = ph.autotune_leaf(StandInPass(truth, ms, err), pos, p, candidates=(32, 48), sample=100,
-                                          repeats=1)
+                                          repeats=1, shapes=False)
     assert (best, flags) == (48, ow)
 
 
@@ -83,7 +84,7 @@ def test_slow_accurate_candidate_loses_to_a_fast_one_within_bound(ph, setup):
     ms = {(16, 0): 3.0, (24, 0): 8.0}
     err = {(16, 0): 9e-5, (24, 0): 1e-6}
     best, _, flags = ph.autotune_leaf(StandInPass(truth, ms, err), pos, p, candidates=(16, 24), sample=100,
-                                      repeats=1)
+                                      repeats=1, shapes=False)
     assert (best, flags) == (16, 0)
 
 
@@ -92,7 +93,7 @@ def test_most_accurate_when_none_within_bound(ph, setup):
     ms = {(16, 0): 1.0, (24, 0): 2.0, (32, 0): 3.0}
     err = {(16, 0): 9e-3, (24, 0): 4e-4, (32, 0): 6e-4}
     best, table, flags = ph.autotune_leaf(StandInPass(truth, ms, err), pos, p, candidates=(16, 24, 32),
-                                          error_bound=1e-4, sample=100, repeats=1)
+                                          error_bound=1e-4, sample=100, repeats=1, shapes=False)
     assert (best, flags) == (24, 0)
     assert len(table) == 3
 
@@ -108,3 +109,25 @@ def test_fp64_times_one_kernel_per_leaf(ph, setup):
     assert [k for k, _ in fp.runs] == [(48, 0), (64, 0)]
     assert all(prec == ph.FP64 for _, prec in fp.runs)
     assert all(r["kernel"] == "one-way" for r in table)
+
+
+def test_kernel_builds_timed_at_the_chosen_leaf(ph, setup):
+    """With shapes on, a mutual-kernel choice is re-timed in every build of
+    that kernel and the fastest within the bound wins; a one-way choice is
+    not re-timed."""
+    pos, truth, p = setup
+    ow = ph.F_ONE_WAY
+    ms = {(32, 0): 9.0, (64, 0): 5.0, (64, ow): 7.0}
+    err = {(32, 0): 9e-5, (64, 0): 2e-5, (64, ow): 2e-5}
+    for sh in range(1, ph.P2P_SHAPES):
+        ms[(64, ph.F_P2P_SHAPE(sh))] = 5.0 + 0.1 * sh
+        err[(64, ph.F_P2P_SHAPE(sh))] = 2e-5
+    ms[(64, ph.F_P2P_SHAPE(3))] = 4.2
+    fp = StandInPass(truth, ms, err)
+    best, table, flags = ph.autotune_leaf(fp, pos, p, candidates=(32, 64), sample=100, repeats=1)
+    assert (best, flags) == (64, ph.F_P2P_SHAPE(3))
+    assert {k for k, _ in fp.runs} == set(ms)
+    ms2 = {(32, 0): 3.0}
+    fp = StandInPass(truth, ms2, {(32, 0): 9e-5})
+    best, _, flags = ph.autotune_leaf(fp, pos, p, candidates=(32,), sample=100, repeats=1)
+    assert (best, flags) == (32, 0) and [k for k, _ in fp.runs] == [(32, 0)]

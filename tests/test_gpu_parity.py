@@ -176,6 +176,30 @@ def test_mutual_pairs_match_one_way(ph, ics, monkeypatch, workload, nside, maxle
     assert np.median(rel_err(mutual, one_way, p)) <= 5e-6
 
 
+@pytest.mark.parametrize("workload,nside,maxleaf", [("zeldovich256", 32, 64), ("nfw128", 40, 48)])
+def test_every_p2p_build_gives_the_same_forces(ph, ics, workload, nside, maxleaf):
+    """The mutual kernel's builds that the autotuner chooses between
+    (resident blocks per SM, interleaved dependency chains, the 6-target
+    path): each is deterministic, within the split-precision bar of the FP64
+    pass, and agrees with the others to FP32 rounding; an unknown build is
+    an error."""
+    pos, p = ics.make(workload, nside=nside, maxleaf=maxleaf)
+    fp = ph.ForcePass(0)
+    a64 = fp.run(pos, p, precision=ph.FP64)
+    base = None
+    for shape in range(ph.P2P_SHAPES):
+        flags = ph.F_P2P_SHAPE(shape)
+        a = fp.run(pos, p, precision=ph.FP32_SPLIT, flags=flags)
+        assert np.array_equal(a, fp.run(pos, p, precision=ph.FP32_SPLIT, flags=flags))
+        e = rel_err(a, a64, p)
+        assert np.median(e) <= 2e-6 and np.percentile(e, 99) <= 2e-5, (shape, np.median(e))
+        base = a if base is None else base
+        assert np.median(rel_err(a, base, p)) <= 1e-6, shape
+    with pytest.raises(ph.PhotonsError, match="shape"):
+        fp.run(pos, p, precision=ph.FP32_SPLIT, flags=ph.F_P2P_SHAPE(ph.P2P_SHAPES))
+    fp.close()
+
+
 def test_mutual_pairs_graph_and_stage_paths_agree(ph, ics, monkeypatch):
     """The mutual kernel inside the captured graph and launched stage by
     stage (where the reaction buffer is sized between the stages) agree

@@ -105,3 +105,76 @@ def test_direct_sum_matches_oracle(ph, port, ics):
 def test_fp32_fma_probe_runs(ph):
     v = ph.fp32_fma_peak(2048)
     assert 1.0 < v < 1000.0
+
+
+IMAGE_SHIFTS = [(mi, mj, mk) for mi in (-1, 0, 1) for mj in (-1, 0, 1) for mk in (-1, 0, 1) if (mi, mj, mk) != (0, 0, 0)]
+
+
+@pytest.mark.parametrize("name", ["grid16_leaf16", "nfw16_leaf8"])
+def test_fmm_remote_per_image_then_host_downward(ph, name):
+    """fmm_ext's own sequence spelled out through the exported entry points
+    (src/fmm.c:1028-1070): after fmm_task, fmm_remote(0, shift) for the 26
+    image shifts, then the host walk_l2l from the root and l2p of every
+    leaf.  The accelerations and counters equal the reference's pass (the
+    nfw16 fixture has local and image M2L, so the host downward pass carries
+    the GPU's local expansions)."""
+    import ctypes as C
+    g = load_golden(name)
+    p = g["p"]
+    ref = ph.Reference()
+    ref.setup(g["pos_in"], p)
+    lib = ref.lib
+    lib.walk_l2l.argtypes = [C.c_int]
+    lib.l2p.argtypes = [C.c_int]
+    lib.fmm_construct()
+    lib.fmm_prepare()
+    lib.fmm_task()
+    part = ref.part()
+    assert rel_err(part["acc"].copy(), g["acc_task"], p).max() <= 1e-10
+    for s in IMAGE_SHIFTS:
+        shift = (C.c_double * 3)(*(float(v) * p["boxsize"] for v in s))
+        lib.fmm_remote(0, shift)
+    first_node = C.c_int.in_dll(lib, "first_node").value
+    first_leaf, last_leaf = C.c_int.in_dll(lib, "first_leaf").value, C.c_int.in_dll(lib, "last_leaf").value
+    lib.walk_l2l(first_node)
+    for n in range(first_leaf, last_leaf):
+        lib.l2p(n)
+    assert rel_err(part["acc"], g["acc"], p).max() <= 1e-10
+    c = ref.counters()
+    assert [c[k] for k in ("idxP2P", "idxM2L", "walk_m2l_count", "p2p_count_remote")] == list(g["counters"][:4])
+    ref.deconstruct()
+
+
+@pytest.mark.parametrize("entry", ["p2p_kernel", "p2p_kernel_rinvsqrt"])
+def test_kernels_h_leaf_pairs_sum_to_the_local_task_phase(ph, entry):
+    """The inc/kernels.h entry points, one call per task of the reference's
+    own local P2P list (in its order; a leaf with itself through
+    p2p_kernel_inleaf), after fmm_prepare: part[].acc equals the
+    reference's accelerations after fmm_task (no M2L in this fixture)."""
+    g = load_golden("grid16_leaf16")
+    p = g["p"]
+    ref = ph.Reference()
+    ref.setup(g["pos_in"], p)
+    lib = ref.lib
+    for name in ("p2p_kernel", "p2p_kernel_rinvsqrt", "p2p_kernel_inleaf"):
+        getattr(lib, name).argtypes = [C_int(), C_int()]
+        getattr(lib, name).restype = None
+    lib.fmm_construct()
+    lib.fmm_prepare()
+    part = ref.part()
+    part["acc"] = 0.0
+    fn = getattr(lib, entry)
+    t, s, _ = g["list_p2p"]
+    for a, b in zip(t.tolist(), s.tolist()):
+        if a == b and entry == "p2p_kernel":
+            lib.p2p_kernel_inleaf(a, b)
+        else:
+            fn(a, b)
+    assert ph.load_library().photons_gpu_status() == 0
+    assert rel_err(part["acc"], g["acc_task"], p).max() <= 1e-10
+    ref.deconstruct()
+
+
+def C_int():
+    import ctypes
+    return ctypes.c_int
