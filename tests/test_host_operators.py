@@ -23,13 +23,21 @@ TOL = 1e-13
 _dp = C.POINTER(C.c_double)
 
 
+SAVED = [(C.c_void_p, "part"), (C.c_void_p, "btree"), (C.c_void_p, "leaf"), (C.c_int, "first_leaf"),
+         (C.c_int, "first_node"), (C.c_int, "last_leaf"), (C.c_int, "last_node"), (C.c_double, "MASSPART"),
+         (C.c_double, "splitRadius"), (C.c_double, "cutoffRadius"), (C.c_double, "open_angle")]
+
+
 @pytest.fixture(scope="module")
 def libs(ph, oracle_mod):
+    """Both libraries, with the globals these tests point at their own
+    arrays restored afterwards (the reference frees its tree through them)."""
     if not oracle_mod.ref_available():
         pytest.skip("reference oracle not built here")
     assert NODE.itemsize == 392 and PACK.itemsize == 376 and BODY.itemsize == 96
     ours = C.CDLL(ph.library_path(), mode=os.RTLD_LOCAL)
     ref = oracle_mod.RefOracle().lib
+    saved = [[(t, n, t.in_dll(lib, n).value) for t, n in SAVED] for lib in (ours, ref)]
     for lib in (ours, ref):
         for name in ("m2m", "m2l", "l2l"):
             getattr(lib, name).argtypes = [C.c_double] * 3 + [_dp, _dp]
@@ -40,7 +48,10 @@ def libs(ph, oracle_mod):
         lib.walk_l2l.argtypes = [C.c_int]
         lib.acceptance.argtypes = [_dp, _dp, _dp]
         lib.acceptance.restype = C.c_int
-    return ours, ref
+    yield ours, ref
+    for lib, vals in zip((ours, ref), saved):
+        for t, n, v in vals:
+            t.in_dll(lib, n).value = v
 
 
 def _set(lib, ctype, name, v):
