@@ -201,6 +201,14 @@ class PortOracle(_Base):
         lib.po_run_sample.restype = C.c_int
         lib.po_run_sample.argtypes = [C.c_void_p, C.c_void_p, C.c_int, _dp, C.c_int, _ip, _dp, _dp]
         lib.po_pairs.argtypes = [C.c_void_p, _lp, _lp]
+        lib.po_run_domains.restype = C.c_int
+        lib.po_run_domains.argtypes = [C.c_int, C.c_void_p, C.c_int, _dp, C.c_int, _dp, _lp, _ip]
+        lib.po_domains.restype = C.c_int
+        lib.po_domains.argtypes = [C.c_int, C.c_double, _dp, _ip, _dp]
+        lib.po_prepare_domain.restype = C.c_int
+        lib.po_prepare_domain.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp, C.c_int, C.c_int, _dp]
+        lib.po_export.restype = C.c_int
+        lib.po_export.argtypes = [C.c_void_p, _dp, _dp, _dp, _ip, _ip, C.c_int, C.c_int, C.c_void_p, _dp]
         lib.po_forces_sample.restype = C.c_int
         lib.po_forces_sample.argtypes = [C.c_void_p, C.c_int, _ip, _dp, _dp]
         lib.po_list_size.restype = C.c_long
@@ -310,6 +318,65 @@ class PortOracle(_Base):
                 out[name] = (tt, ss, im)
             r["lists"] = out
         return r
+
+    def domains(self, nrank, boxsize):
+        """The reference's first domain decomposition: (box (P, 2, 3) lo/hi,
+        first split axis (P,), split planes (P-1,) in heap order)."""
+        box = np.empty((nrank, 2, 3))
+        axis = np.empty(nrank, np.int32)
+        split = np.empty(max(nrank - 1, 1))
+        rc = self.lib.po_domains(nrank, float(boxsize), _ptr(box), _ptr(axis, _ip), _ptr(split))
+        if rc != 0:
+            raise RuntimeError(f"oracle domains failed with code {rc}")
+        return box, axis, split[:nrank - 1]
+
+    def run_domains(self, pos, p, nrank, nthreads=1, explicit_self=False):
+        """One pass over `nrank` ranks emulated here: acc (n, 3) input
+        order, per-rank counters, each particle's rank."""
+        pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+        n = pos.shape[0]
+        prm = self._params(p, nthreads, True, True)
+        acc = np.empty_like(pos)
+        cnt = np.zeros((nrank, 16), np.int64)
+        rank = np.empty(n, np.int32)
+        rc = self.lib.po_run_domains(nrank, C.byref(prm), n, _ptr(pos), int(explicit_self), _ptr(acc),
+                                     _ptr(cnt, _lp), _ptr(rank, _ip))
+        if rc != 0:
+            raise RuntimeError(f"oracle domain pass failed with code {rc}")
+        return acc, [dict(zip(COUNTER_NAMES, (int(c) for c in row))) for row in cnt], rank
+
+    def prepare_domain(self, pos, p, lo, hi, axis, nthreads=1):
+        """fmm_prepare of one rank: its tree over the domain box (lo, hi)."""
+        pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+        prm = self._params(p, nthreads, True, True)
+        lo = np.ascontiguousarray(lo, np.float64)
+        hi = np.ascontiguousarray(hi, np.float64)
+        rc = self.lib.po_prepare_domain(self.state, C.byref(prm), _ptr(lo), _ptr(hi), int(axis), pos.shape[0],
+                                        _ptr(pos))
+        if rc != 0:
+            raise RuntimeError(f"oracle domain prepare failed with code {rc}")
+
+    def export(self, recv_lo, recv_hi, shift):
+        """The prepared tree shifted and pruned for the receiving domain
+        (its top-tree box recv_lo..recv_hi): nodes (structured: npart, son,
+        width, center, M), bodies (n, 3)."""
+        lo = np.asarray(recv_lo, np.float64)
+        hi = np.asarray(recv_hi, np.float64)
+        tc, tw = 0.5 * (hi + lo), hi - lo                  # the receiver's top-tree box
+        rlo, rhi = tc - 0.5 * tw, tc + 0.5 * tw             # its root's bounds
+        rc_, rw = np.ascontiguousarray(0.5 * (rhi + rlo)), np.ascontiguousarray(rhi - rlo)
+        sh = np.ascontiguousarray(shift, np.float64)
+        nn, nb = C.c_int(0), C.c_int(0)
+        self.lib.po_export(self.state, _ptr(rc_), _ptr(rw), _ptr(sh), C.byref(nn), C.byref(nb), 0, 0, None, None)
+        dt = np.dtype([("npart", "i4"), ("son", "i4", 2), ("width", "f8", 3), ("center", "f8", 3),
+                       ("M", "f8", NMULTI)], align=True)
+        nodes = np.zeros(nn.value, dt)
+        bodies = np.zeros((nb.value, 3))
+        rc = self.lib.po_export(self.state, _ptr(rc_), _ptr(rw), _ptr(sh), C.byref(nn), C.byref(nb), nodes.size,
+                                nb.value, nodes.ctypes.data, _ptr(bodies))
+        if rc != 0:
+            raise RuntimeError(f"oracle export failed with code {rc}")
+        return nodes, bodies
 
     def forces_sample(self, targets):
         """Forces for another target set on the last pass's tree and lists:

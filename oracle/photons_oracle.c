@@ -260,8 +260,23 @@ struct po_state {
     int capture;
     /* sampled pass: forces only for these particles (tree order) and the
        leaves / nodes that hold them; NULL = every particle */
-    unsigned char *part_on, *leaf_on, *node_on;
+    unsigned char *part_on, *leaf_on, *node_on;    /* the domain this tree covers (src/fmm.c:189-197): the root's box and
+       the first split axis (direct_local_start); the whole periodic box and
+       axis 0 at one rank */
+    int domain_set;
+    double dom_lo[3], dom_hi[3];
+    int axis0;
+    /* trees received from other ranks (or from this one, shifted), walked
+       as P2P/M2L "ext" lists with image tags PO_IMG_RECEIVED + k */
+    struct o_rtree *rt;
+    int nrt;
 };
+
+/* an exported (pruned, shifted) tree: src/remotes.c:60-169, the layout of
+   RemoteNode (inc/photoNs.h:177-183); bodies as x, y, z */
+typedef struct { int npart, son[2]; double width[3], center[3], M[NM]; } o_rnode;
+typedef struct o_rtree { int nnode, nbody; o_rnode *node; double *body; } o_rtree;
+#define PO_IMG_RECEIVED 100
 
 /* One dual-tree traversal's output.  Walks are split into independent
    sub-walks (subtrees of the recursion) that run on separate threads and
@@ -637,6 +652,117 @@ static void walk_image(o_walker *w, int im, int jm, int depth)
     }
 }
 
+/* The walk against a received tree (src/remotes.c:213-372 and 405-552,
+   one traversal): source jm indexes the received RemoteNode array; a node
+   is a leaf iff it holds <= MAXLEAF particles, and a node sent without its
+   children (son = -1, pruned by the sender) is interacted by M2L unless
+   dropped.  Entries carry the received tree's image tag. */
+static void walk_received(o_walker *w, const o_rtree *rt, int im, int jm, int depth)
+{
+    po_state *s = w->s;
+    if (w->err) return;
+    if (deferred(w, depth, im, jm)) return;
+    const o_rnode *J = &rt->node[jm];
+    int il = IS_LEAF(s, im);
+    int jl = J->npart <= s->p.maxleaf;
+    if (il && jl) { emit(w, PO_LIST_P2P_EXT, im, jm); return; }
+    const double *ci = geom_center(s, im);
+    double dist[3] = {ci[0] - J->center[0], ci[1] - J->center[1], ci[2] - J->center[2]};
+    int flag = po_acceptance(geom_width(s, im), J->width, dist, s->p.theta, s->p.rcut);
+    if (flag == -1) return;
+    int pruned = !jl && (J->son[0] < 0 || J->son[1] < 0);
+    if (il) {
+        if (flag == 1 || pruned) { emit(w, PO_LIST_M2L_EXT, im, jm); return; }
+        walk_received(w, rt, im, J->son[0], depth + 1);
+        walk_received(w, rt, im, J->son[1], depth + 1);
+        return;
+    }
+    if (flag == 1) { emit(w, PO_LIST_M2L_EXT, im, jm); return; }
+    int open_target = jl || pruned || wsum(NODE(s, im)->width) > wsum(J->width);
+    if (open_target) {
+        o_node *a = NODE(s, im);
+        walk_received(w, rt, a->son[0], jm, depth + 1);
+        walk_received(w, rt, a->son[1], jm, depth + 1);
+    } else {
+        walk_received(w, rt, im, J->son[0], depth + 1);
+        walk_received(w, rt, im, J->son[1], depth + 1);
+    }
+}
+
+/* The exported copy of a local tree (src/remotes.c:60-169): the tree
+   shifted by `sh`, in depth-first preorder, an internal node's children
+   left out when its shifted box lies at least rcut from the receiving
+   domain's box (centre rc, width rw) or its largest width is below
+   0.95 theta times that distance; leaves ship their bodies (shifted). */
+static int export_node(const po_state *s, int id, const double rc[3], const double rw[3], const double sh[3],
+                       o_rtree *out)
+{
+    int me = out->nnode++;
+    o_rnode *E = &out->node[me];
+    if (IS_LEAF(s, id)) {
+        const o_leaf *lf = &s->leaf[id - s->first_leaf];
+        E->npart = lf->npart;
+        for (int d = 0; d < 3; d++) { E->center[d] = lf->center[d] + sh[d]; E->width[d] = lf->width[d]; }
+        memcpy(E->M, lf->M, sizeof E->M);
+        E->son[0] = out->nbody;
+        for (int q = lf->ipart; q < lf->ipart + lf->npart; q++) {
+            for (int d = 0; d < 3; d++) out->body[3 * (size_t)out->nbody + d] = s->pos[3 * (size_t)q + d] + sh[d];
+            out->nbody++;
+        }
+        E->son[1] = out->nbody;
+        return me;
+    }
+    const o_node *nd = &s->node[id - s->first_node];
+    double dr = 0.0;
+    for (int d = 0; d < 3; d++) {
+        double g = rc[d] - nd->center[d] - sh[d];
+        if (g < 0.0) g = -g;
+        g -= (rw[d] + nd->width[d]) * 0.5;
+        if (g > 0.0) dr += g * g;
+    }
+    dr = sqrt(dr);
+    E->npart = nd->npart;
+    for (int d = 0; d < 3; d++) { E->center[d] = nd->center[d] + sh[d]; E->width[d] = nd->width[d]; }
+    memcpy(E->M, nd->M, sizeof E->M);
+    double wmax = nd->width[0];
+    if (wmax < nd->width[1]) wmax = nd->width[1];
+    if (wmax < nd->width[2]) wmax = nd->width[2];
+    if (dr >= s->p.rcut || wmax < 0.95 * s->p.theta * dr) {
+        E->son[0] = E->son[1] = -1;
+        return me;
+    }
+    for (int c = 0; c < 2; c++) {
+        int k = export_node(s, nd->son[c], rc, rw, sh, out);
+        out->node[me].son[c] = k;
+    }
+    return me;
+}
+
+int po_export(const po_state *s, const double recv_center[3], const double recv_width[3], const double shift[3],
+              int *nnode, int *nbody, int node_cap, int body_cap, void *nodes, double *bodies)
+{
+    if (!s || !s->node || !nnode || !nbody) return PO_ERR_ARG;
+    o_rtree t;
+    t.nnode = t.nbody = 0;
+    t.node = malloc(sizeof(o_rnode) * (size_t)(s->nleaf + s->nnode));
+    t.body = malloc(sizeof(double) * 3 * (size_t)s->n);
+    if (!t.node || !t.body) { free(t.node); free(t.body); return PO_ERR_NOMEM; }
+    export_node(s, s->first_node, recv_center, recv_width, shift, &t);
+    *nnode = t.nnode;
+    *nbody = t.nbody;
+    int rc = PO_OK;
+    if (nodes && bodies) {
+        if (t.nnode > node_cap || t.nbody > body_cap) rc = PO_ERR_ARG;
+        else {
+            memcpy(nodes, t.node, sizeof(o_rnode) * (size_t)t.nnode);
+            memcpy(bodies, t.body, sizeof(double) * 3 * (size_t)t.nbody);
+        }
+    }
+    free(t.node);
+    free(t.body);
+    return rc;
+}
+
 /* ------------------------------------------------------------------ */
 /* pair kernel and list compute                                        */
 /* ------------------------------------------------------------------ */
@@ -692,7 +818,8 @@ static void p2p_target(p2p_job *J, int lf_index)
     o_leaf *T = &s->leaf[lf_index];
     for (long k = J->off[lf_index]; k < J->off[lf_index + 1]; k++) {
         long e = J->order[k];
-        o_leaf *S = LEAF(s, J->l->s[e]);
+        const int received = J->ext && J->l->img[e] >= PO_IMG_RECEIVED;
+        o_leaf *S = received ? NULL : LEAF(s, J->l->s[e]);
         if (!J->ext) {
             for (int q = 0; q < T->npart; q++) {
                 int ip = T->ipart + q;
@@ -706,6 +833,17 @@ static void p2p_target(p2p_job *J, int lf_index)
             }
         } else {
             int img = J->l->img[e];
+            if (img >= PO_IMG_RECEIVED) {
+                /* bodies of a received leaf (src/remotes.c:26-56 on exrbody) */
+                const o_rtree *rt = &s->rt[img - PO_IMG_RECEIVED];
+                const o_rnode *R = &rt->node[J->l->s[e]];
+                for (int ip = T->ipart; ip < T->ipart + T->npart; ip++) {
+                    if (s->part_on && !s->part_on[ip]) continue;
+                    for (int jp = R->son[0]; jp < R->son[1]; jp++)
+                        pair_force(rt->body + 3 * (size_t)jp, s->pos + 3 * ip, p, coeff, s->acc + 3 * ip);
+                }
+                continue;
+            }
             double sh[3];
             int c = 0;
             for (int mi = -1; mi <= 1; mi++)
@@ -781,13 +919,19 @@ static void run_m2l(po_state *s, const o_list *l)
         int im = l->t[e], jm = l->s[e];
         if (s->leaf_on && !(IS_LEAF(s, im) ? s->leaf_on[im - s->first_leaf] : s->node_on[im - s->first_node]))
             continue;
+        const double *ci = geom_center(s, im);
+        double *L = IS_LEAF(s, im) ? LEAF(s, im)->L : NODE(s, im)->L;
+        if (l->img[e] >= PO_IMG_RECEIVED) {
+            /* a received node: its centre already carries the sender's shift */
+            const o_rnode *R = &s->rt[l->img[e] - PO_IMG_RECEIVED].node[jm];
+            po_m2l(ci[0] - R->center[0], ci[1] - R->center[1], ci[2] - R->center[2], R->M, L, s->p.rs);
+            continue;
+        }
         double sh[3] = {0, 0, 0};
         if (l->img[e]) image_shift(&s->p, l->img[e], sh);
         const double *cj = geom_center(s, jm);
         double cjs[3] = {cj[0] + sh[0], cj[1] + sh[1], cj[2] + sh[2]};
-        const double *ci = geom_center(s, im);
         const double *M = IS_LEAF(s, jm) ? LEAF(s, jm)->M : NODE(s, jm)->M;
-        double *L = IS_LEAF(s, im) ? LEAF(s, im)->L : NODE(s, im)->L;
         if (l->img[e])
             po_m2l(ci[0] - cjs[0], ci[1] - cjs[1], ci[2] - cjs[2], M, L, s->p.rs);
         else
@@ -815,7 +959,8 @@ typedef struct {
 
 static void walk_run(o_walker *w, int im, int jm)
 {
-    if (w->image) walk_image(w, im, jm, 0);
+    if (w->image >= PO_IMG_RECEIVED) walk_received(w, &w->s->rt[w->image - PO_IMG_RECEIVED], im, jm, 0);
+    else if (w->image) walk_image(w, im, jm, 0);
     else walk_local(w, im, jm, 0);
 }
 
@@ -855,19 +1000,23 @@ static int list_append(o_list *dst, const o_list *src)
    walk's. */
 static int run_walks(po_state *s, int images)
 {
-    int nimg = images ? NIMG : 1;
-    o_walker top[NIMG];
-    memset(top, 0, sizeof top);
+    /* walks in order: the local tree, its 26 images (on the fly), then the
+       received trees */
+    const int nown = images ? NIMG : 1;
+    int nimg = nown + s->nrt;
+    o_walker *top = calloc((size_t)nimg, sizeof(o_walker));
+    if (!top) return PO_ERR_NOMEM;
     long nsub = 0;
     int rc = PO_OK;
-    for (int img = 0; img < nimg; img++) {
-        top[img].s = s;
-        top[img].image = img;
-        if (img) image_shift(&s->p, img, top[img].shift);
-        top[img].defer_depth = 12;
-        walk_run(&top[img], s->first_node, s->first_node);
-        if (top[img].err) rc = top[img].err;
-        for (long i = 0; i < top[img].nitems; i++) nsub += top[img].items[i].kind == 4;
+    for (int k = 0; k < nimg; k++) {
+        const int img = k < nown ? k : PO_IMG_RECEIVED + (k - nown);
+        top[k].s = s;
+        top[k].image = img;
+        if (img && img < PO_IMG_RECEIVED) image_shift(&s->p, img, top[k].shift);
+        top[k].defer_depth = 12;
+        walk_run(&top[k], s->first_node, img >= PO_IMG_RECEIVED ? 0 : s->first_node);
+        if (top[k].err) rc = top[k].err;
+        for (long i = 0; i < top[k].nitems; i++) nsub += top[k].items[i].kind == 4;
     }
     walk_job J;
     memset(&J, 0, sizeof J);
@@ -876,14 +1025,14 @@ static int run_walks(po_state *s, int images)
     if (!J.sub) rc = PO_ERR_NOMEM;
     if (rc == PO_OK) {
         long k = 0;
-        for (int img = 0; img < nimg; img++)
-            for (long i = 0; i < top[img].nitems; i++) {
-                if (top[img].items[i].kind != 4) continue;
+        for (int t = 0; t < nimg; t++)
+            for (long i = 0; i < top[t].nitems; i++) {
+                if (top[t].items[i].kind != 4) continue;
                 o_walker *w = &J.sub[k++];
                 w->s = s;
-                w->image = img;
-                memcpy(w->shift, top[img].shift, sizeof w->shift);
-                if (push_item(w, 4, top[img].items[i].a, top[img].items[i].b) != 0) rc = PO_ERR_NOMEM;
+                w->image = top[t].image;
+                memcpy(w->shift, top[t].shift, sizeof w->shift);
+                if (push_item(w, 4, top[t].items[i].a, top[t].items[i].b) != 0) rc = PO_ERR_NOMEM;
             }
         J.nsub = nsub;
     }
@@ -901,12 +1050,12 @@ static int run_walks(po_state *s, int images)
         pthread_mutex_destroy(&J.mu);
         /* concatenate in traversal order */
         long k = 0;
-        for (int img = 0; img < nimg && rc == PO_OK; img++) {
-            s->walk_m2l_count += top[img].m2l;
-            for (long i = 0; i < top[img].nitems && rc == PO_OK; i++) {
-                o_item *it = &top[img].items[i];
+        for (int t = 0; t < nimg && rc == PO_OK; t++) {
+            s->walk_m2l_count += top[t].m2l;
+            for (long i = 0; i < top[t].nitems && rc == PO_OK; i++) {
+                o_item *it = &top[t].items[i];
                 if (it->kind != 4) {
-                    if (list_push(&s->list[it->kind], it->a, it->b, img) != 0) rc = PO_ERR_NOMEM;
+                    if (list_push(&s->list[it->kind], it->a, it->b, top[t].image) != 0) rc = PO_ERR_NOMEM;
                     continue;
                 }
                 o_walker *w = &J.sub[k++];
@@ -919,7 +1068,8 @@ static int run_walks(po_state *s, int images)
     }
     for (long i = 0; i < nsub && J.sub; i++) walker_free(&J.sub[i]);
     free(J.sub);
-    for (int img = 0; img < nimg; img++) walker_free(&top[img]);
+    for (int t = 0; t < nimg; t++) walker_free(&top[t]);
+    free(top);
     return rc;
 }
 
@@ -985,17 +1135,38 @@ static int forces(po_state *s, int nt, const int *targets)
     return PO_OK;
 }
 
+/* pairs of the ext P2P list (images and received trees): n_t n_s per task,
+   as src/remotes.c:26-56 counts p2p_count_remote */
+static long long ext_pairs(const po_state *s)
+{
+    long long b = 0;
+    const o_list *l = &s->list[PO_LIST_P2P_EXT];
+    for (long e = 0; e < l->n; e++) {
+        long long ns;
+        if (l->img[e] >= PO_IMG_RECEIVED) {
+            const o_rnode *R = &s->rt[l->img[e] - PO_IMG_RECEIVED].node[l->s[e]];
+            ns = R->son[1] - R->son[0];
+        } else {
+            ns = LEAF(s, l->s[e])->npart;
+        }
+        b += (long long)LEAF(s, l->t[e])->npart * ns;
+    }
+    return b;
+}
+
 /* the whole pass: src/fmm.c:329-360 (construct), 719-770 (prepare),
    909-984 (task), 987-1075 (ext) at one rank.  With targets, the tree,
    walks, counters and multipoles are complete, but forces are formed only
    for the listed particles (P2P into them, M2L into their leaves and
    ancestors, L2L down those paths, L2P on them), in the same operation
    order as the full pass, so their accelerations are identical to it. */
-static int run_pass(po_state *s, const po_params *p, int n, const double *pos_in, int nt, const int *targets,
-                    double *times)
+/* src/fmm.c:180-264 (tree) and 719-747 (P2M, M2M): t[0] tree build and
+   geometry, t[1] multipoles; keep_task: keep a copy of the accelerations
+   after the local task phase */
+static int prepare_pass(po_state *s, const po_params *p, int n, const double *pos_in, int keep_task, double *t)
 {
     init_tables();
-    if (!s || !p || n < 1 || p->maxleaf < 1 || nt < 0) return PO_ERR_ARG;
+    if (!s || !p || n < 1 || p->maxleaf < 1) return PO_ERR_ARG;
     if (n <= p->maxleaf) return PO_ERR_SMALL;
     free_run(s);
     for (int k = 0; k < 4; k++) s->list[k].n = 0;
@@ -1008,14 +1179,14 @@ static int run_pass(po_state *s, const po_params *p, int n, const double *pos_in
     s->pos = malloc(sizeof(double) * 3 * (size_t)n);
     s->perm = malloc(sizeof(int) * (size_t)n);
     s->acc = calloc(3 * (size_t)n, sizeof(double));
-    s->acc_task = targets ? NULL : calloc(3 * (size_t)n, sizeof(double));
+    s->acc_task = keep_task ? calloc(3 * (size_t)n, sizeof(double)) : NULL;
     /* capacity rule of src/fmm.c:203-209 */
     int cap = (int)(2.0 * ((double)n) / ((double)p->maxleaf));
     if (cap > n) cap = n + 1;
     s->nleaf_cap = s->nnode_cap = cap;
     s->leaf = calloc((size_t)cap, sizeof(o_leaf));
     s->node = calloc((size_t)cap, sizeof(o_node));
-    if (!s->pos || !s->perm || !s->acc || (!targets && !s->acc_task) || !s->leaf || !s->node) return PO_ERR_NOMEM;
+    if (!s->pos || !s->perm || !s->acc || (keep_task && !s->acc_task) || !s->leaf || !s->node) return PO_ERR_NOMEM;
     for (int i = 0; i < cap; i++) s->node[i].son[0] = s->node[i].son[1] = -1;
     memcpy(s->pos, pos_in, sizeof(double) * 3 * (size_t)n);
     for (int i = 0; i < n; i++) s->perm[i] = i;
@@ -1024,12 +1195,14 @@ static int run_pass(po_state *s, const po_params *p, int n, const double *pos_in
     s->first_leaf = n;
     s->first_node = n + cap;
     int last_leaf = s->first_leaf, last_node = s->first_node;
-    build(s, 0, 0, n, s->first_node, &last_leaf, &last_node);
+    build(s, s->domain_set ? s->axis0 : 0, 0, n, s->first_node, &last_leaf, &last_node);
     if (s->err) return s->err;
     s->nleaf = last_leaf - s->first_leaf;
     s->nnode = last_node - s->first_node + 1;
     double lo[3] = {0, 0, 0}, hi[3] = {p->boxsize, p->boxsize, p->boxsize};
-    geometry(s, 0, s->first_node, lo, hi);
+    if (s->domain_set)
+        for (int d = 0; d < 3; d++) { lo[d] = s->dom_lo[d]; hi[d] = s->dom_hi[d]; }
+    geometry(s, s->domain_set ? s->axis0 : 0, s->first_node, lo, hi);
     double t1 = wall();
     for (int i = 0; i < s->nleaf; i++) {
         o_leaf *lf = &s->leaf[i];
@@ -1037,19 +1210,30 @@ static int run_pass(po_state *s, const po_params *p, int n, const double *pos_in
     }
     upward(s, s->first_node);
     double t2 = wall();
-    int rc = run_walks(s, p->images);
+    t[0] = t1 - t0;
+    t[1] = t2 - t1;
+    return PO_OK;
+}
+
+static int run_pass(po_state *s, const po_params *p, int n, const double *pos_in, int nt, const int *targets,
+                    double *times)
+{
+    if (nt < 0) return PO_ERR_ARG;
+    double tp[2];
+    int rc = prepare_pass(s, p, n, pos_in, targets == NULL, tp);
     if (rc) return rc;
-    o_list *pe = &s->list[PO_LIST_P2P_EXT];
-    for (long e = 0; e < pe->n; e++)
-        s->p2p_count_remote += (long long)LEAF(s, pe->t[e])->npart * LEAF(s, pe->s[e])->npart;
+    double t2 = wall();
+    rc = run_walks(s, p->images);
+    if (rc) return rc;
+    s->p2p_count_remote = ext_pairs(s);
     double t3 = wall();
 
     rc = forces(s, nt, targets);
     if (rc) return rc;
     double t4 = wall();
     if (times) {
-        times[0] = t1 - t0;   /* tree build and geometry */
-        times[1] = t2 - t1;   /* P2M, M2M */
+        times[0] = tp[0];     /* tree build and geometry */
+        times[1] = tp[1];     /* P2M, M2M */
         times[2] = t3 - t2;   /* local and image walks */
         times[3] = t4 - t3;   /* forces (all particles, or the listed ones) */
     }
@@ -1106,10 +1290,218 @@ void po_pairs(const po_state *s, long long *pairs_local, long long *pairs_image)
         long long nt = LEAF(s, l->t[e])->npart, ns = LEAF(s, l->s[e])->npart;
         a += l->t[e] == l->s[e] ? nt * (nt - 1) : nt * ns;
     }
-    l = &s->list[PO_LIST_P2P_EXT];
-    for (long e = 0; e < l->n; e++) b += (long long)LEAF(s, l->t[e])->npart * LEAF(s, l->s[e])->npart;
+    b = ext_pairs(s);
     *pairs_local = a;
     *pairs_image = b;
+}
+
+/* ------------------------------------------------------------------ */
+/* several ranks, emulated in one process                              */
+/* ------------------------------------------------------------------ */
+/* Domain ids of src/initial.c:197-222: domains are the leaves P-1..2P-2 of
+   a heap-ordered binary tree; rank r owns domain r + mostleft (wrapped). */
+static int most_left(int P)
+{
+    if (P == 1) return 0;
+    int m = 1;
+    while (m < 2 * P - 1) m *= 2;
+    return m / 2 - 1;
+}
+
+static int rank_of_domain(int P, int d) { return (d - most_left(P) + P) % P; }
+
+static double domain_time(int P, int id)
+{
+    if (id >= P - 1) return 1.0;  /* every domain's time is 1 at the first step */
+    return domain_time(P, 2 * id + 1) + domain_time(P, 2 * id + 2);
+}
+
+/* src/domains.c:400-425 (domain_volume_part): split planes dividing each
+   node's box in the ratio of its children's times (equal per domain) */
+static void domain_volume_part(int P, int id, double bl[3], double br[3], int dim, double *split)
+{
+    if (id >= P - 1) return;
+    double tl = domain_time(P, 2 * id + 1), tr = domain_time(P, 2 * id + 2);
+    double frac = bl[dim] + (br[dim] - bl[dim]) * tl / (tl + tr);
+    split[id] = frac;
+    double keep = br[dim];
+    br[dim] = frac;
+    domain_volume_part(P, 2 * id + 1, bl, br, (dim + 1) % 3, split);
+    br[dim] = keep;
+    keep = bl[dim];
+    bl[dim] = frac;
+    domain_volume_part(P, 2 * id + 2, bl, br, (dim + 1) % 3, split);
+    bl[dim] = keep;
+}
+
+/* src/toptree.c:157-182 (center_toptree): each domain's box and the axis
+   its local tree splits first (direct_local_start) */
+static void domain_boxes(int P, int id, int dir, double lo[3], double hi[3], const double *split, double *box,
+                         int *axis)
+{
+    if (id >= P - 1) {
+        int r = rank_of_domain(P, id);
+        for (int d = 0; d < 3; d++) { box[6 * r + d] = lo[d]; box[6 * r + 3 + d] = hi[d]; }
+        axis[r] = dir;
+        return;
+    }
+    double keep = hi[dir];
+    hi[dir] = split[id];
+    domain_boxes(P, 2 * id + 1, (dir + 1) % 3, lo, hi, split, box, axis);
+    hi[dir] = keep;
+    keep = lo[dir];
+    lo[dir] = split[id];
+    domain_boxes(P, 2 * id + 2, (dir + 1) % 3, lo, hi, split, box, axis);
+    lo[dir] = keep;
+}
+
+int po_domains(int P, double boxsize, double *box, int *axis, double *split)
+{
+    if (P < 1 || !box || !axis) return PO_ERR_ARG;
+    double *sp = calloc((size_t)(P > 1 ? P - 1 : 1), sizeof(double));
+    if (!sp) return PO_ERR_NOMEM;
+    double bl[3] = {0, 0, 0}, br[3] = {boxsize, boxsize, boxsize};
+    domain_volume_part(P, 0, bl, br, 0, sp);
+    double lo[3] = {0, 0, 0}, hi[3] = {boxsize, boxsize, boxsize};
+    domain_boxes(P, 0, 0, lo, hi, sp, box, axis);
+    if (split)
+        for (int i = 0; i < P - 1; i++) split[i] = sp[i];
+    free(sp);
+    return PO_OK;
+}
+
+/* src/domains.c:165-298: the rank whose domain holds x (a coordinate above a
+   split plane goes to the upper child) */
+static int rank_of_position(int P, const double *split, const double x[3])
+{
+    int id = 0, D = 0;
+    while (id < P - 1) {
+        id = x[D] > split[id] ? 2 * id + 2 : 2 * id + 1;
+        D = (D + 1) % 3;
+    }
+    return rank_of_domain(P, id);
+}
+
+/* the root's bounds from the top-tree node's box: centre -/+ half the width
+   (src/toptree.c:150-159, src/fmm.c:189-197) */
+static void set_domain(po_state *s, const double lo[3], const double hi[3], int axis)
+{
+    s->domain_set = 1;
+    for (int d = 0; d < 3; d++) {
+        double c = 0.5 * (hi[d] + lo[d]), w = hi[d] - lo[d];
+        s->dom_lo[d] = c - 0.5 * w;
+        s->dom_hi[d] = c + 0.5 * w;
+    }
+    s->axis0 = axis;
+}
+
+/* One force pass over P ranks as src/photoNs.c drives them
+   (fmm_prepare, fmm_task, fmm_ext) with the ranks emulated in turn: each
+   rank's tree covers its domain; fmm_remote(idx, shift) of
+   src/remotes.c:684-751 becomes an export from rank r - idx of its tree
+   shifted by `shift`, pruned against rank r's domain, walked by rank r:
+   the other ranks' trees (shift 0), then for each image shift every
+   rank's shifted tree, in fmm_ext's order.  With explicit_self the rank's
+   own periodic images also go through an export, otherwise they use the
+   single-rank image walk.  acc_out[3n] in input order; counters[16 P] per
+   rank as po_counters; rank_out[n]: each particle's rank. */
+int po_run_domains(int P, const po_params *p, int n, const double *pos_in, int explicit_self, double *acc_out,
+                   long long *counters, int *rank_out)
+{
+    init_tables();
+    if (P < 1 || !p || n < 1 || !pos_in || !acc_out) return PO_ERR_ARG;
+    double *box = malloc(sizeof(double) * 6 * (size_t)P), *split = calloc((size_t)P, sizeof(double));
+    int *axis = malloc(sizeof(int) * (size_t)P), *rank = malloc(sizeof(int) * (size_t)n);
+    int *cnt = calloc((size_t)P, sizeof(int)), *fill = calloc((size_t)P, sizeof(int));
+    int *order = malloc(sizeof(int) * (size_t)n);
+    double *lpos = malloc(sizeof(double) * 3 * (size_t)n);
+    po_state **st = calloc((size_t)P, sizeof(po_state *));
+    int rc = (!box || !split || !axis || !rank || !cnt || !fill || !order || !lpos || !st) ? PO_ERR_NOMEM : PO_OK;
+    if (!rc) rc = po_domains(P, p->boxsize, box, axis, split);
+    if (!rc) {
+        for (int i = 0; i < n; i++) { rank[i] = rank_of_position(P, split, pos_in + 3 * (size_t)i); cnt[rank[i]]++; }
+        for (int r = 1; r < P; r++) fill[r] = fill[r - 1] + cnt[r - 1];
+        for (int i = 0; i < n; i++) order[fill[rank[i]]++] = i;  /* each rank's particles in input order */
+        for (int i = 0; i < n; i++)
+            for (int d = 0; d < 3; d++) lpos[3 * (size_t)i + d] = pos_in[3 * (size_t)order[i] + d];
+        if (rank_out) memcpy(rank_out, rank, sizeof(int) * (size_t)n);
+    }
+    /* fmm_prepare on every rank */
+    int first = 0;
+    for (int r = 0; r < P && !rc; r++) {
+        st[r] = po_create();
+        if (!st[r]) { rc = PO_ERR_NOMEM; break; }
+        set_domain(st[r], box + 6 * r, box + 6 * r + 3, axis[r]);
+        if (cnt[r] <= p->maxleaf) { rc = PO_ERR_SMALL; break; }
+        double t[2];
+        rc = prepare_pass(st[r], p, cnt[r], lpos + 3 * (size_t)first, 0, t);
+        first += cnt[r];
+    }
+    /* the trees each rank receives, in fmm_ext's order; the receiving
+       domain as its root holds it (connect_local_toptree copies every
+       rank's root geometry into the top tree, src/toptree.c:21-40) */
+    for (int r = 0; r < P && !rc; r++) {
+        int maxrt = (P - 1) + (NIMG - 1) * P;
+        st[r]->rt = calloc((size_t)maxrt, sizeof(o_rtree));
+        if (!st[r]->rt) { rc = PO_ERR_NOMEM; break; }
+        double rcen[3], rwid[3];
+        for (int d = 0; d < 3; d++) {
+            rcen[d] = 0.5 * (st[r]->dom_hi[d] + st[r]->dom_lo[d]);
+            rwid[d] = st[r]->dom_hi[d] - st[r]->dom_lo[d];
+        }
+        for (int pass = 0; pass < NIMG && !rc; pass++) {
+            double sh[3] = {0, 0, 0};
+            if (pass) image_shift(p, pass, sh);
+            for (int idx = pass ? 0 : 1; idx < P && !rc; idx++) {
+                if (pass && idx == 0 && !explicit_self) continue;
+                po_state *q = st[(r - idx + P) % P];
+                o_rtree *t = &st[r]->rt[st[r]->nrt];
+                t->node = malloc(sizeof(o_rnode) * (size_t)(q->nleaf + q->nnode));
+                t->body = malloc(sizeof(double) * 3 * (size_t)q->n);
+                if (!t->node || !t->body) { rc = PO_ERR_NOMEM; break; }
+                export_node(q, q->first_node, rcen, rwid, sh, t);
+                st[r]->nrt++;
+            }
+        }
+    }
+    /* fmm_task and fmm_ext on every rank */
+    first = 0;
+    for (int r = 0; r < P && !rc; r++) {
+        po_state *q = st[r];
+        q->walk_m2l_count = 0;
+        rc = run_walks(q, p->images && !explicit_self);
+        if (rc) break;
+        q->p2p_count_remote = ext_pairs(q);
+        rc = forces(q, 0, NULL);
+        if (rc) break;
+        for (int i = 0; i < cnt[r]; i++)
+            for (int d = 0; d < 3; d++)
+                acc_out[3 * (size_t)order[first + q->perm[i]] + d] = q->acc[3 * (size_t)i + d];
+        if (counters) po_counters(q, counters + 16 * (size_t)r);
+        first += cnt[r];
+    }
+    for (int r = 0; r < P && st; r++) {
+        if (!st[r]) continue;
+        for (int k = 0; k < st[r]->nrt; k++) { free(st[r]->rt[k].node); free(st[r]->rt[k].body); }
+        free(st[r]->rt);
+        st[r]->rt = NULL;
+        st[r]->nrt = 0;
+        po_destroy(st[r]);
+    }
+    free(st); free(box); free(split); free(axis); free(rank); free(cnt); free(fill); free(order); free(lpos);
+    return rc;
+}
+
+/* fmm_prepare for one rank's domain (its tree over the domain box from its
+   first axis, multipoles); po_export then gives its exported trees.  lo,
+   hi: the domain's top-tree box. */
+int po_prepare_domain(po_state *s, const po_params *p, const double lo[3], const double hi[3], int axis, int n,
+                      const double *pos_in)
+{
+    if (!s || !p || !lo || !hi || axis < 0 || axis > 2) return PO_ERR_ARG;
+    set_domain(s, lo, hi, axis);
+    double t[2];
+    return prepare_pass(s, p, n, pos_in, 0, t);
 }
 
 void po_counters(const po_state *s, long long *c)

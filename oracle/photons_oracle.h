@@ -61,6 +61,27 @@ int po_forces_sample(po_state *s, int nt, const int *targets, double *acc_out, d
    evaluates them (n_t n_s per task, minus a leaf's self pairs) */
 void po_pairs(const po_state *s, long long *pairs_local, long long *pairs_image);
 
+/* The reference's first domain decomposition at P ranks (src/domains.c:
+   400-459, src/toptree.c:157-182): box[6 r..] = rank r's domain (lo, hi),
+   axis[r] = its local tree's first split axis, split[P-1] = the domain
+   tree's split planes (heap order). */
+int po_domains(int P, double boxsize, double *box, int *axis, double *split);
+/* One pass over P ranks emulated in this process (each rank's tree over its
+   domain; other ranks' and periodic trees exported, pruned and walked as
+   src/remotes.c:60-751 does).  acc_out[3n] in input order, counters[16 P]
+   per rank, rank_out[n] each particle's rank; explicit_self sends a rank's
+   own periodic images through the export too. */
+int po_run_domains(int P, const po_params *p, int n, const double *pos_in, int explicit_self, double *acc_out,
+                   long long *counters, int *rank_out);
+/* fmm_prepare of one rank's domain (lo, hi: its top-tree box; axis: first split) */
+int po_prepare_domain(po_state *s, const po_params *p, const double lo[3], const double hi[3], int axis, int n,
+                      const double *pos_in);
+/* the exported tree of the last pass (RemoteNode layout: int npart, son[2];
+   double width[3], center[3], M[20]; bodies as x, y, z), pruned against the
+   receiving root's centre and width; with nodes/bodies NULL only the sizes */
+int po_export(const po_state *s, const double recv_center[3], const double recv_width[3], const double shift[3],
+              int *nnode, int *nbody, int node_cap, int body_cap, void *nodes, double *bodies);
+
 /* counters[16]: idxP2P, idxM2L, walk_m2l_count, p2p_count_remote, NLEAF, NNODE,
    nleaf, nnode, first_leaf, first_node, direct_local_start(0), n_p2p, n_m2l,
    n_p2p_ext, n_m2l_ext, n_images, in the reference's index space. */

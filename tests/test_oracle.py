@@ -191,3 +191,40 @@ def test_port_sampled_pass_equals_full_pass(port, ics, name, nside, maxleaf):
     assert np.array_equal(a2, acc[tg2]) and secs >= 0
     a3, _ = port.forces_sample(tg)
     assert np.array_equal(a3, acc[tg])
+
+
+def test_port_domain_split_follows_the_reference_rules(port):
+    """src/domains.c:400-425 with equal times and src/toptree.c:157-182:
+    two ranks split x at the middle, three put two domains left of 2/3 L
+    (split again in y), four split x then y; every domain's first axis is
+    the next after its parent's."""
+    box, axis, split = port.domains(2, 100.0)
+    assert np.allclose(box[0], [[0, 0, 0], [50, 100, 100]]) and np.allclose(box[1], [[50, 0, 0], [100, 100, 100]])
+    assert list(axis) == [1, 1] and np.allclose(split, [50])
+    box, axis, split = port.domains(3, 90.0)
+    assert np.allclose(split, [60, 45])
+    assert sorted(map(tuple, box[:, 1].round(9).tolist())) == [(60, 45, 90), (60, 90, 90), (90, 90, 90)]
+    box, axis, split = port.domains(4, 100.0)
+    assert list(axis) == [2, 2, 2, 2] and np.allclose(split, [50, 50, 50])
+
+
+@pytest.mark.parametrize("name,nside,maxleaf", [("grid32", 20, 16), ("nfw128", 24, 8)])
+def test_port_received_trees_reproduce_the_image_walk(port, ics, name, nside, maxleaf):
+    """The restatement of the exported tree (src/remotes.c:60-169) and of
+    the walk against a received tree (:213-552): at one rank, sending the
+    26 periodic images through export + received walk gives the pinned
+    single-rank pass bit for bit; at several ranks both routes for a rank's
+    own images give the same counters and forces to rounding."""
+    pos, p = ics.make(name, nside=nside, maxleaf=maxleaf)
+    full = port.run(pos, p, capture=False, tree=False, nthreads=4)
+    plain = np.empty_like(full["acc"])
+    plain[full["perm"]] = full["acc"]
+    acc, cnt, rank = port.run_domains(pos, p, 1, nthreads=4, explicit_self=True)
+    assert np.array_equal(acc, plain) and (rank == 0).all()
+    for k in COUNTERS[:4] + ["n_p2p_ext", "n_m2l_ext", "nleaf", "nnode"]:
+        assert cnt[0][k] == full["counters"][k], k
+    for P in (2, 3):
+        a, c, r = port.run_domains(pos, p, P, nthreads=4)
+        b, d, _ = port.run_domains(pos, p, P, nthreads=4, explicit_self=True)
+        assert np.bincount(r).size == P and c == d
+        assert np.abs(a - b).max() <= 1e-12 * np.abs(a).max()
