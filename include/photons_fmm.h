@@ -202,6 +202,76 @@ int photons_direct_sum(const photons_params *p, int n, const double *pos, int nt
 int photons_direct_sum_noalloc(const photons_params *p, int n, const double *pos, int nt, const int *targets,
                                double rmax, double *acc, void *cuda_stream);
 
+/* ---- several ranks, one GPU each: the reference's domain decomposition
+   (src/domains.c, src/toptree.c) and its locally essential trees
+   (src/remotes.c:60-169, 684-751).  Each rank builds its tree over its own
+   domain, exports for every other rank (and for every periodic image) its
+   tree shifted and pruned against the receiver's domain, and walks its tree
+   against the trees it receives.  The transport between ranks is the
+   caller's (MPI, NCCL or torch.distributed); the library builds and uses
+   the messages, in the reference's RemoteNode / RemoteBody layouts. ---- */
+/* inc/photoNs.h:177-183 (RemoteNode): a node of an exported tree; son[] are
+   the children's indices in the same array, -1 where the sender pruned
+   them, and for a leaf (npart <= MAXLEAF) the range of its bodies */
+typedef struct {
+    int npart;
+    int son[2];
+    double width[3];
+    double center[3];
+    double M[20];
+} photons_remote_node;
+/* inc/photoNs.h:185-189 (RemoteBody): a body of an exported leaf, shifted */
+typedef struct {
+    double pos[3];
+    double replenish;
+} photons_remote_body;
+/* a rank's domain: its box (the split planes around it) and the axis its
+   local tree splits first (direct_local_start) */
+typedef struct {
+    double lo[3], hi[3];
+    int axis;
+} photons_domain;
+
+/* The first decomposition of the periodic box over nrank ranks, equal work
+   per rank (src/domains.c:400-459, src/toptree.c:157-182, domain ids of
+   src/initial.c:197-222): domains[r] for every rank; split[nrank-1] the
+   domain tree's split planes in heap order (may be NULL).  Host function. */
+int photons_domain_split(int nrank, double boxsize, photons_domain *domains, double *split);
+/* rank[i] of each position pos[3i] under split planes split[nrank-1]
+   (src/domains.c:263-298: above a plane goes to the upper side).  Host. */
+int photons_domain_assign(int nrank, const double *split, int n, const double *pos, int *rank);
+/* Load balance (src/domains.c:22-156): moves the split planes by the
+   measured work time of each rank, relaxed as the reference relaxes them,
+   and writes the new domains (may be NULL).  Host function. */
+int photons_domain_rebalance(int nrank, double boxsize, double *split, const double *rank_time,
+                             photons_domain *domains);
+/* Start this rank's pass (src/fmm.c:719-770 for a domain): the tree of the
+   n positions of this rank's domain, built over the domain box from its
+   first axis, and its multipoles.  Host or device positions per
+   PHOTONS_F_DEVICE_IO; they must stay valid until photons_domain_finish. */
+int photons_domain_prepare(photons_ctx *ctx, const photons_params *p, const photons_domain *dom, int n,
+                           const double *pos);
+/* The tree prepared in ctx shifted by shift[3] and pruned against the
+   receiving rank's domain (src/remotes.c:60-169), in depth-first preorder.
+   Host buffers; *nnode and *nbody receive the sizes.  With nodes and bodies
+   NULL only the sizes; if node_cap or body_cap is too small nothing is
+   written and error 4 (capacity) is returned with the sizes set. */
+int photons_let_export(photons_ctx *ctx, const photons_domain *receiver, const double shift[3],
+                       photons_remote_node *nodes, int node_cap, photons_remote_body *bodies, int body_cap,
+                       int *nnode, int *nbody);
+/* A tree received from another rank (or this rank's own, shifted), kept
+   for photons_domain_finish; host buffers, copied.  Checked: child and body
+   indices must lie in the message. */
+int photons_let_import(photons_ctx *ctx, const photons_remote_node *nodes, int nnode,
+                       const photons_remote_body *bodies, int nbody);
+/* Finish the pass (src/fmm.c:909-1075 with fmm_remote over the received
+   trees): local walk, the 26 periodic images of the local tree, the walks
+   against every received tree (P2P with its bodies, M2L with its pruned
+   nodes), L2L, L2P; acc[3n] in the prepared positions' order (host or
+   device as prepared).  Counters and lists as photons_force_pass leaves
+   them; the image counters include the received trees. */
+int photons_domain_finish(photons_ctx *ctx, double *acc);
+
 /* ---- kick-drift-kick integration on device arrays (src/photoNs.c:141-196,
    257-268).  Products and sums are rounded separately, as in the reference's
    loops, so a step matches it bit for bit given the same accelerations. ---- */

@@ -65,6 +65,17 @@ class PhotonsError(RuntimeError):
     pass
 
 
+class Domain(C.Structure):
+    """A rank's domain: its box and its tree's first split axis."""
+    _fields_ = [("lo", C.c_double * 3), ("hi", C.c_double * 3), ("axis", C.c_int)]
+
+
+# inc/photoNs.h:177-189: RemoteNode (a node of an exported tree) and RemoteBody
+REMOTE_NODE = np.dtype([("npart", "i4"), ("son", "i4", 2), ("width", "f8", 3), ("center", "f8", 3),
+                        ("M", "f8", NMULTI)], align=True)
+REMOTE_BODY = np.dtype([("pos", "f8", 3), ("replenish", "f8")])
+
+
 _lib = None
 
 
@@ -126,6 +137,14 @@ def load_library():
         [C.c_double, C.c_double]
     lib.photons_kdk_step_pm_ordered.argtypes = [C.c_void_p, C.POINTER(Params), C.c_int, C.c_int] + \
         [C.c_void_p] * 5 + [C.c_double, C.c_double]
+    lib.photons_domain_split.argtypes = [C.c_int, C.c_double, C.POINTER(Domain), _dp]
+    lib.photons_domain_assign.argtypes = [C.c_int, _dp, C.c_int, _dp, _ip]
+    lib.photons_domain_rebalance.argtypes = [C.c_int, C.c_double, _dp, _dp, C.POINTER(Domain)]
+    lib.photons_domain_prepare.argtypes = [C.c_void_p, C.POINTER(Params), C.POINTER(Domain), C.c_int, C.c_void_p]
+    lib.photons_let_export.argtypes = [C.c_void_p, C.POINTER(Domain), _dp, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
+                                       _ip, _ip]
+    lib.photons_let_import.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int]
+    lib.photons_domain_finish.argtypes = [C.c_void_p, C.c_void_p]
     _lib = lib
     return lib
 
@@ -237,6 +256,41 @@ class ForcePass:
                                                      C.c_void_p(ids_ptr or None), float(dkh), float(dd)))
         self.n = n
 
+    # ---- a rank's domain pass (several ranks, one GPU each) ----
+    def domain_prepare(self, pos, p, dom, precision=FP32_SPLIT, flags=0):
+        """Start this rank's pass: the tree of its particles over its domain."""
+        self._dom_pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)  # must outlive the pass
+        prm = make_params(p, precision, 0, flags & ~F_DEVICE_IO)
+        _check(self.lib.photons_domain_prepare(self.h, C.byref(prm), C.byref(dom), self._dom_pos.shape[0],
+                                               self._dom_pos.ctypes.data))
+        self.n = self._dom_pos.shape[0]
+
+    def let_export(self, receiver, shift=(0.0, 0.0, 0.0)):
+        """This rank's tree shifted and pruned for `receiver` (a Domain):
+        (nodes, bodies) as REMOTE_NODE / REMOTE_BODY arrays."""
+        sh = np.ascontiguousarray(shift, np.float64)
+        nn, nb = C.c_int(0), C.c_int(0)
+        _check(self.lib.photons_let_export(self.h, C.byref(receiver), _p(sh), None, 0, None, 0, C.byref(nn),
+                                           C.byref(nb)))
+        nodes = np.zeros(nn.value, REMOTE_NODE)
+        bodies = np.zeros(nb.value, REMOTE_BODY)
+        _check(self.lib.photons_let_export(self.h, C.byref(receiver), _p(sh), nodes.ctypes.data, nodes.size,
+                                           bodies.ctypes.data, bodies.size, C.byref(nn), C.byref(nb)))
+        return nodes, bodies
+
+    def let_import(self, nodes, bodies):
+        """Keep a received tree for domain_finish."""
+        nodes = np.ascontiguousarray(nodes, REMOTE_NODE)
+        bodies = np.ascontiguousarray(bodies, REMOTE_BODY)
+        _check(self.lib.photons_let_import(self.h, nodes.ctypes.data, nodes.size, bodies.ctypes.data, bodies.size))
+
+    def domain_finish(self):
+        """Walks, P2P and far field over the local, periodic and received
+        trees: the accelerations (n, 3) in the prepared positions' order."""
+        acc = np.empty((self.n, 3))
+        _check(self.lib.photons_domain_finish(self.h, acc.ctypes.data))
+        return acc
+
     def pm_force(self, pos, p, nside):
         """PM long-range acceleration (n,3) on an nside^3 mesh (host arrays)."""
         pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
@@ -297,6 +351,50 @@ class ForcePass:
                 _check(self.lib.photons_list_copy(self.h, k, _p(t, _ip), _p(s, _ip), _p(im, _ip)))
             out[name] = (t, s, im)
         return out
+
+
+def domain_split(nrank, boxsize):
+    """The reference's first decomposition over nrank ranks: (domains, split planes)."""
+    lib = load_library()
+    doms = (Domain * nrank)()
+    split = np.zeros(max(nrank - 1, 1))
+    _check(lib.photons_domain_split(int(nrank), float(boxsize), doms, _p(split)))
+    return list(doms), split[:nrank - 1].copy()
+
+
+def domain_assign(nrank, split, pos):
+    """The rank of each position under the split planes."""
+    lib = load_library()
+    pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+    split = np.ascontiguousarray(split if len(split) else [0.0], np.float64)
+    rank = np.empty(pos.shape[0], np.int32)
+    _check(lib.photons_domain_assign(int(nrank), _p(split), pos.shape[0], _p(pos), _p(rank, _ip)))
+    return rank
+
+
+def domain_rebalance(nrank, boxsize, split, rank_time):
+    """Split planes moved by the ranks' measured times: (domains, split)."""
+    lib = load_library()
+    split = np.array(split if len(split) else [0.0], np.float64)
+    t = np.ascontiguousarray(rank_time, np.float64)
+    doms = (Domain * nrank)()
+    _check(lib.photons_domain_rebalance(int(nrank), float(boxsize), _p(split), _p(t), doms))
+    return list(doms), split[:nrank - 1].copy()
+
+
+IMAGE_SHIFTS = [(mi, mj, mk) for mi in (-1, 0, 1) for mj in (-1, 0, 1) for mk in (-1, 0, 1) if (mi, mj, mk) != (0, 0, 0)]
+
+
+def let_schedule(rank, nrank):
+    """The exchanges of one rank's pass in fmm_ext's order
+    (src/fmm.c:1020-1045, fmm_remote's srank/rrank, src/remotes.c:690-691):
+    [(send_to, recv_from, shift unit)]: the other ranks unshifted, then for
+    every periodic image every other rank.  A rank's own images are walked
+    on the fly, not exchanged."""
+    out = [((rank + i) % nrank, (rank - i) % nrank, (0, 0, 0)) for i in range(1, nrank)]
+    for s in IMAGE_SHIFTS:
+        out += [((rank + i) % nrank, (rank - i) % nrank, s) for i in range(1, nrank)]
+    return out
 
 
 def op_batch(op, d, inp, inout, rs=1.0):

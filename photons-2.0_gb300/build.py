@@ -18,7 +18,7 @@ LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libphotons_fmm.so")
 INCLUDE = os.path.join(ROOT, "include")
 
-SOURCES = ["scan.cu", "tree.cu", "walk.cu", "p2p.cu", "multipole.cu", "api.cu", "legacy.cu", "direct.cu", "noalloc.cu", "integrate.cu", "snapshot.cu", "pm.cu"]
+SOURCES = ["scan.cu", "tree.cu", "walk.cu", "p2p.cu", "multipole.cu", "api.cu", "legacy.cu", "direct.cu", "noalloc.cu", "domain.cu", "integrate.cu", "snapshot.cu", "pm.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code is not contracted into FMAs (the host operators and integrals
 # follow the reference's separately rounded arithmetic on every host CPU)

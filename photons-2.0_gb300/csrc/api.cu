@@ -145,9 +145,14 @@ static int alloc_tree(photons_ctx *c, int n, int cap)
         c->epoch++;
         b.cap_nodes = cap;
         b.cap_leaves = cap;
-        // unified tree
+    }
+    // unified tree: leaves and nodes (2N/MAXLEAF each at most) and, in a
+    // rank's domain pass, the nodes of the trees it receives
+    const int cu = 2 * cap + 2 + c->imp_reserve_u;
+    if (cu > c->cap_u) {
         ph::TreeBufs &t = c->t;
-        int cu = 2 * cap + 2;
+        c->t.cap_u = c->cap_u = c->mu_cap_leaves = 0;
+        c->epoch++;
         PH_TRY(dalloc(t.ipart, cu)); PH_TRY(dalloc(t.npart, cu)); PH_TRY(dalloc(t.depth, cu));
         PH_TRY(dalloc(t.parent, cu)); PH_TRY(dalloc(t.son0, cu)); PH_TRY(dalloc(t.son1, cu));
         PH_TRY(dalloc(t.cx, cu)); PH_TRY(dalloc(t.cy, cu)); PH_TRY(dalloc(t.cz, cu));
@@ -461,7 +466,8 @@ static int ph_prepare_boxes(photons_ctx *c, int nbox, const photons_params *p, c
     if (n > INT32_MAX / 3) return ph_set_error(PH_ERR_ARG, "%lld particles in one pass exceed the supported count", n);
     photons_params all = p[0];
     PH_TRY(ph_validate(&all, (int)n));  // the 27-bit id space over all boxes
-    PH_TRY(alloc_particles(c, (int)n));
+    if (c->dom_set && nbox != 1) return ph_set_error(PH_ERR_ARG, "a rank's domain pass covers one box");
+    PH_TRY(alloc_particles(c, (int)n + (c->dom_set ? c->imp_reserve_body : 0)));
     PH_TRY(alloc_tree(c, (int)n, (int)cap));
     if (nbox > c->cap_box) {
         c->cap_box = 0;
@@ -475,6 +481,14 @@ static int ph_prepare_boxes(photons_ctx *c, int nbox, const photons_params *p, c
     for (int b = 0; b < nbox; b++) {
         c->h_boxes[b] = box_params(&p[b], first, counts[b]);
         first += counts[b];
+    }
+    c->pp.axis0 = 0;
+    if (c->dom_set) {
+        // a rank's domain: the root's box and first split axis
+        BoxParams &B = c->h_boxes[0];
+        B.domain = 1;
+        for (int d = 0; d < 3; d++) { B.dom_lo[d] = c->dom.lo[d]; B.dom_hi[d] = c->dom.hi[d]; }
+        c->pp.axis0 = c->dom.axis;
     }
     c->b.nbox = nbox;
     c->b.rule_cap = (int)cap;
@@ -638,7 +652,7 @@ int ph_stage_walk(photons_ctx *c, unsigned mask)
     walk_caps(c, p2p_cap, pd_cap, m2l_cap, stack_cap, stage_cap);
     for (int attempt = 0; attempt < 6; attempt++) {
         PH_TRY(alloc_walk(c, p2p_cap, pd_cap, m2l_cap, stack_cap, stage_cap));
-        PH_TRY(ph::walk_lists(c->w, c->t, c->b.cnt, c->b.boxes, c->ndepth, c->pp, mask, c->stream));
+        PH_TRY(ph::walk_lists(c->w, c->t, c->b.cnt, c->b.boxes, c->ndepth, c->pp, mask, c->stream, c->walk_imp));
         PH_CUDA_CHECK(cudaMemcpyAsync(c->ws.c, c->w.ctr, sizeof(c->ws.c), cudaMemcpyDeviceToHost, c->stream));
         PH_CUDA_CHECK(cudaStreamSynchronize(c->stream));
         unsigned long long fl = c->ws.c[ph::WC_FLAGS];
@@ -939,6 +953,7 @@ extern "C" void photons_destroy(photons_ctx *c)
     cudaStreamSynchronize(c->stream);
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
     ph_pm_release(c);
+    ph_domain_release(c);
     cudaFree(c->pm_io);
     free_all(c);
     for (int i = 0; i < EV_COUNT; i++) cudaEventDestroy(c->ev[i]);
@@ -961,6 +976,9 @@ static int force_pass_boxes(photons_ctx *c, int nbox, const photons_params *p, c
     if (!pos || !acc) return ph_set_error(PH_ERR_ARG, "null particle arrays");
     if (!p || !counts || nbox < 1) return ph_set_error(PH_ERR_ARG, "null parameters");
     cudaSetDevice(c->device);
+    // a plain pass covers the whole periodic box (no rank's domain, nothing received)
+    c->dom_set = false;
+    c->walk_imp = ph::WalkImports();
     const int dio = p->flags & PHOTONS_F_DEVICE_IO;
     const unsigned mask = p->image_mask ? p->image_mask : ((1u << PH_NIMG) - 1u);
     const char *g = getenv("PHOTONS_GRAPH");

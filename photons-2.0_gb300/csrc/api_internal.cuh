@@ -85,6 +85,20 @@ struct photons_ctx {
     int cap_box = 0;
     int ndepth = 0;       // depths the walk and far field launch
     unsigned long long epoch = 0;  // bumped by every device (re)allocation
+    // a rank's domain pass (domain.cu): the domain its tree covers, the
+    // trees received from other ranks (host copies until the pass ends),
+    // and the capacity reserved in the unified and particle arrays for them
+    bool dom_set = false;
+    photons_domain dom{};
+    std::vector<photons_remote_node> imp_nodes;
+    std::vector<photons_remote_body> imp_bodies;
+    std::vector<int> imp_first;            // first node of each received tree in imp_nodes
+    int imp_reserve_u = 0, imp_reserve_body = 0;
+    ph::WalkImports walk_imp;               // what the next walk adds to the root's list
+    struct DomainScratch *dsc = nullptr;    // export/import device buffers
+    photons_params dom_params{};            // the prepared pass (for a rebuild with more room)
+    int dom_n = 0;
+    const double *dom_pos = nullptr;
     // the captured pass
     bool capturing = false, have_key = false;
     cudaGraphExec_t gexec = nullptr;
@@ -106,6 +120,7 @@ struct HostTree {
 };
 
 int ph_validate(const photons_params *p, int n);
+void ph_domain_release(photons_ctx *c);
 int ph_stage_build(photons_ctx *c, const photons_params *p, int n, const double *pos, int device_io);
 int ph_stage_walk(photons_ctx *c, unsigned mask);
 int ph_stage_p2p(photons_ctx *c, int precision, int zero);

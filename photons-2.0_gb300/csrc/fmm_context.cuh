@@ -121,10 +121,21 @@ struct WalkStats {
 // Everything below only enqueues work on st; tree sizes are read on the
 // device from tree_cnt (the build counters, BuildBufs::cnt).
 int launch_geom32(const TreeBufs &t, const int *tree_cnt, cudaStream_t st);
+// Trees received from other ranks, appended to the unified arrays from
+// unified id `base` on: the walk adds (root[k], PH_IMG_IMPORT) to the local
+// root's list.  A received node is a leaf iff it holds <= MAXLEAF
+// particles; a node sent without children (son0 < 0) was pruned by its
+// sender.  Only for a pass over one box.
+struct WalkImports {
+    const int *root = nullptr;  // device: first unified id of each received tree
+    int nroot = 0;
+    int base = 0x7fffffff;      // unified id of the first received node
+};
+
 // image_mask: bit 0 the local tree, bit k the k-th periodic image;
 // ndepth = depths to launch (at least the tree's deepest + 1)
 int walk_lists(WalkBufs &w, const TreeBufs &t, const int *tree_cnt, const BoxParams *boxes, int ndepth,
-               const PassParams &p, unsigned image_mask, cudaStream_t st);
+               const PassParams &p, unsigned image_mask, cudaStream_t st, const WalkImports &imp = WalkImports());
 
 int build_tree(BuildBufs &b, TreeBufs &t, const PassParams &p, int levels, cudaStream_t st);
 int read_tree_info(const BuildBufs &b, const TreeBufs &t, int levels, TreeInfo &info);

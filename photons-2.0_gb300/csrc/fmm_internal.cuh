@@ -15,6 +15,10 @@
 
 #define PH_NMULTI 20
 #define PH_NIMG 27
+// image tag of entries whose source lies in a received tree (another
+// rank's exported tree, possibly shifted by a periodic image): the received
+// centres already carry the sender's shift
+#define PH_IMG_IMPORT 27
 
 // interaction entry: unified source id (27 bits) | image index (5 bits)
 #define PH_ENTRY(u, img) ((uint32_t)(u) | ((uint32_t)(img) << 27))
@@ -39,6 +43,7 @@ struct PassParams {
     double boxsize, theta, rs, rcut, eps, mass;
     int maxleaf;
     int images;  // unused by the kernels; the walk takes an image mask
+    int axis0;   // the first split axis (direct_local_start; 0 but for a rank's domain tree)
 };
 
 // One periodic box of a pass.  A pass covers one box or many independent
@@ -54,6 +59,8 @@ struct BoxParams {
     float far_a, far_pa;       // FP32 M2L: ia = 1/(2 rs) and p ia
     int first, count;   // particle range in the concatenated input
     int root;           // unified id of the box's root node (written by the build)
+    int domain;         // 1: the root's box is dom_lo..dom_hi (a rank's domain), else [0, boxsize]^3
+    double dom_lo[3], dom_hi[3];
 };
 
 // ------------------------------------------------------------------
@@ -97,7 +104,7 @@ __device__ __forceinline__ double warp_sum_d(double v)
 // src/fmm.c:1029-1044 (mi, mj, mk from -1 to 1, skipping 0,0,0); img 0 = none
 __host__ __device__ __forceinline__ void image_offsets(int img, int &mi, int &mj, int &mk)
 {
-    if (img == 0) { mi = mj = mk = 0; return; }
+    if (img == 0 || img >= PH_NIMG) { mi = mj = mk = 0; return; }
     int c = img - 1;
     if (c >= 13) c += 1;  // skip the centre cell (index 13 of the 27)
     mi = c / 9 - 1;

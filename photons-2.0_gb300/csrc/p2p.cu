@@ -849,7 +849,8 @@ __global__ void k_mu_pair(const int *tree_cnt, const unsigned long long *walk_fl
             if (e < L) {
                 const uint32_t v = pool[o + e];
                 const int b = PH_ENTRY_ID(v), img = PH_ENTRY_IMG(v), nimg = img_neg(img);
-                if (st && sorted[b] && !(img == 0 && b == t)) {
+                // received leaves (b >= nleaf) have no lists: those entries run one way
+                if (st && b < nleaf && sorted[b] && !(img == 0 && b == t)) {
                     q = mu_find(pool + off[b], cnt[b], PH_ENTRY(t, nimg));
                     if (q >= 0) {
                         const unsigned long long mine = ((unsigned long long)t << 5) | (unsigned)img;

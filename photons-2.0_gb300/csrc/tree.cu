@@ -54,8 +54,11 @@ __global__ void k_init_roots(BuildBufs b)
         b.tn_depth[t] = 0;
         b.tn_parent[t] = -1;
         b.tn_boxid[t] = t;
-        const double c = 0.5 * (B.boxsize + 0.0), w = B.boxsize - 0.0;
         for (int d = 0; d < 3; d++) {
+            // a rank's domain: its top-tree node's centre and width
+            // (src/toptree.c:150-159) give the bounds of src/fmm.c:189-197
+            const double lo = B.domain ? B.dom_lo[d] : 0.0, hi = B.domain ? B.dom_hi[d] : B.boxsize;
+            const double c = 0.5 * (hi + lo), w = hi - lo;
             b.tn_box[d * b.cap_nodes + t] = c - 0.5 * w;
             b.tn_box[(3 + d) * b.cap_nodes + t] = c + 0.5 * w;
         }
@@ -607,7 +610,7 @@ int build_tree(BuildBufs &b, TreeBufs &T, const PassParams &p, int levels, cudaS
     PH_CUDA_CHECK(cudaMemsetAsync(b.leaf_count, 0, sizeof(int) * (levels + 2), st));
     ph::note_launch(), k_init_roots<<<(b.nbox + TB - 1) / TB, TB, 0, st>>>(b);
     for (int d = 0; d < levels; d++) {
-        const int D = d % 3;  // direct_local_start = 0 at one rank; axis cycles (src/fmm.c:99)
+        const int D = (p.axis0 + d) % 3;  // from direct_local_start; the axis cycles (src/fmm.c:99)
         ph::note_launch(), k_level_nch<<<maxb, TB, 0, st>>>(b);
         ph::note_launch(), k_narrow_split<<<maxb, TB, 0, st>>>(b, D, p.maxleaf);
         scan_exclusive_i32(b.tn_nch, b.tn_chunk_base, b.cnt + BC_LEVEL_COUNT, b.cap_nodes, b.cnt + BC_W,

@@ -120,7 +120,15 @@ struct WalkArgs {
     const BoxParams *boxes;  // per box: side, rcut, root
     double theta2, theta;
     float theta2f;
+    WalkImports imp;  // received trees (none outside a rank's domain pass)
+    int maxleaf;
 };
+
+// a source is a leaf: a local leaf, or a received node of <= MAXLEAF particles
+__device__ __forceinline__ bool source_is_leaf(const WalkArgs &A, int b, int nleaf)
+{
+    return b < nleaf || (b >= A.imp.base && A.g.npart[b] <= A.maxleaf);
+}
 
 // sender-side pruning of an image node, src/remotes.c:97-158
 __device__ __forceinline__ bool image_pruned(const WalkArgs &A, int r, double rcut, int b, double s0, double s1,
@@ -215,7 +223,7 @@ __global__ void __launch_bounds__(WALK_TB, MINB) k_walk_level(WalkArgs A)
         const uint32_t *input = nullptr;
         int n_in;
         if (par < 0) {
-            n_in = A.nroot;
+            n_in = A.nroot + A.imp.nroot;
         } else {
             input = W.pd_pool[parity ^ 1] + W.pd_off[par];
             n_in = W.pd_cnt[par];
@@ -237,7 +245,13 @@ __global__ void __launch_bounds__(WALK_TB, MINB) k_walk_level(WalkArgs A)
                     if (lane < k) e[0] = input[in_pos + lane];
                     if (lane + 32 < k) e[1] = input[in_pos + lane + 32];
                 } else {
-                    if (lane < k) e[0] = PH_ENTRY(a, A.root_img[in_pos + lane]);
+                    // the root's list: itself under each selected image, then the received trees
+                    for (int s2 = 0; s2 < 2; s2++) {
+                        const int i = in_pos + lane + 32 * s2;
+                        if (lane + 32 * s2 < k)
+                            e[s2] = i < A.nroot ? PH_ENTRY(a, A.root_img[i])
+                                                : PH_ENTRY(A.imp.root[i - A.nroot], PH_IMG_IMPORT);
+                    }
                 }
                 in_pos += k;
             } else {
@@ -252,7 +266,7 @@ __global__ void __launch_bounds__(WALK_TB, MINB) k_walk_level(WalkArgs A)
                 const bool valid = lane + 32 * s < k;
                 b[s] = PH_ENTRY_ID(e[s]);
                 img[s] = PH_ENTRY_IMG(e[s]);
-                const bool leaf_b = b[s] < nleaf;
+                const bool leaf_b = source_is_leaf(A, b[s], nleaf);
                 const bool self = img[s] == 0 && b[s] == a;
                 need[s] = valid && !self && !(leaf_a && leaf_b);
                 npb[s] = (valid && !self && leaf_a && leaf_b) ? g.npart[b[s]] : 0;
@@ -268,7 +282,7 @@ __global__ void __launch_bounds__(WALK_TB, MINB) k_walk_level(WalkArgs A)
                 kind[s] = OUT_NONE;
                 if (lane + 32 * s >= k) continue;
                 const int bb = b[s], im = img[s];
-                const bool leaf_b = bb < nleaf;
+                const bool leaf_b = source_is_leaf(A, bb, nleaf);
                 if (im == 0 && bb == a) {
                     if (leaf_a) {
                         kind[s] = OUT_P2P;
@@ -309,7 +323,10 @@ __global__ void __launch_bounds__(WALK_TB, MINB) k_walk_level(WalkArgs A)
                         else if (leaf_b) kd = OUT_PUSH;
                         else kd = bigger_a ? OUT_PUSH : OUT_OPEN;
                     } else {
-                        const bool pruned = !leaf_b && image_pruned(A, root, rcut, bb, s0, s1, s2);
+                        // an image node is pruned by the rule of src/remotes.c:97-158 evaluated
+                        // here; a received node came without children when its sender pruned it
+                        const bool pruned = !leaf_b && (im == PH_IMG_IMPORT ? g.son0[bb] < 0
+                                                                            : image_pruned(A, root, rcut, bb, s0, s1, s2));
                         if (leaf_a) kd = (flag == 1 || pruned) ? OUT_M2L : OUT_OPEN;
                         else if (flag == 1) kd = OUT_M2L;
                         else kd = (leaf_b || pruned || bigger_a) ? OUT_PUSH : OUT_OPEN;
@@ -470,7 +487,7 @@ int launch_geom32(const TreeBufs &t, const int *tree_cnt, cudaStream_t st)
 // Enqueue the walk of depths 0..ndepth-1; depths past the tree's deepest
 // exit at once.  Counters and flags stay on the device (w.ctr).
 int walk_lists(WalkBufs &w, const TreeBufs &t, const int *tree_cnt, const BoxParams *boxes, int ndepth,
-               const PassParams &p, unsigned image_mask, cudaStream_t st)
+               const PassParams &p, unsigned image_mask, cudaStream_t st, const WalkImports &imp)
 {
     PH_CUDA_CHECK(cudaMemsetAsync(w.ctr, 0, sizeof(unsigned long long) * WC_N, st));
     WalkArgs A{};
@@ -490,6 +507,8 @@ int walk_lists(WalkBufs &w, const TreeBufs &t, const int *tree_cnt, const BoxPar
         if (image_mask & (1u << img)) A.root_img[A.nroot++] = img;
     A.theta = p.theta;
     A.theta2 = p.theta * p.theta;
+    A.imp = imp;
+    A.maxleaf = p.maxleaf;
     const int blocks = (w.nwarps * 32 + WALK_TB - 1) / WALK_TB;
     for (int d = 0; d < ndepth; d++) {
         A.depth = d;
