@@ -1219,6 +1219,8 @@ static int run_pass(po_state *s, const po_params *p, int n, const double *pos_in
                     double *times)
 {
     if (nt < 0) return PO_ERR_ARG;
+    /* a plain pass: the whole periodic box, nothing received */
+    if (s) { s->domain_set = 0; s->nrt = 0; }
     double tp[2];
     int rc = prepare_pass(s, p, n, pos_in, targets == NULL, tp);
     if (rc) return rc;

@@ -228,3 +228,14 @@ def test_port_received_trees_reproduce_the_image_walk(port, ics, name, nside, ma
         b, d, _ = port.run_domains(pos, p, P, nthreads=4, explicit_self=True)
         assert np.bincount(r).size == P and c == d
         assert np.abs(a - b).max() <= 1e-12 * np.abs(a).max()
+
+
+def test_port_plain_pass_after_a_domain_prepare(port, ics):
+    """A state that prepared one rank's domain runs the next plain pass over
+    the whole box again."""
+    pos, p = ics.make("grid32", nside=16)
+    want = port.run(pos, p, capture=False, tree=False, nthreads=2)["counters"]
+    port.prepare_domain(pos[pos[:, 0] < 0.5 * p["boxsize"]], p, [0, 0, 0], [0.5 * p["boxsize"], p["boxsize"],
+                                                                           p["boxsize"]], 1)
+    got = port.run(pos, p, capture=False, tree=False, nthreads=2)["counters"]
+    assert got == want
