@@ -209,6 +209,10 @@ class PortOracle(_Base):
         lib.po_prepare_domain.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp, C.c_int, C.c_int, _dp]
         lib.po_export.restype = C.c_int
         lib.po_export.argtypes = [C.c_void_p, _dp, _dp, _dp, _ip, _ip, C.c_int, C.c_int, C.c_void_p, _dp]
+        lib.po_import.restype = C.c_int
+        lib.po_import.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, _dp]
+        lib.po_finish_domain.restype = C.c_int
+        lib.po_finish_domain.argtypes = [C.c_void_p, _dp]
         lib.po_forces_sample.restype = C.c_int
         lib.po_forces_sample.argtypes = [C.c_void_p, C.c_int, _ip, _dp, _dp]
         lib.po_list_size.restype = C.c_long
@@ -329,6 +333,25 @@ class PortOracle(_Base):
         if rc != 0:
             raise RuntimeError(f"oracle domains failed with code {rc}")
         return box, axis, split[:nrank - 1]
+
+    def import_tree(self, nodes, bodies):
+        """Keep a received tree (nodes as export returns them, bodies (n, 3))."""
+        nodes = np.ascontiguousarray(nodes)
+        bodies = np.ascontiguousarray(bodies, np.float64).reshape(-1, 3)
+        rc = self.lib.po_import(self.state, nodes.size, nodes.ctypes.data, bodies.shape[0], _ptr(bodies))
+        if rc != 0:
+            raise RuntimeError(f"oracle import failed with code {rc}")
+
+    def finish_domain(self, n):
+        """The prepared domain's pass over the received trees: acc (n, 3)
+        and the counters."""
+        acc = np.empty((n, 3))
+        rc = self.lib.po_finish_domain(self.state, _ptr(acc))
+        if rc != 0:
+            raise RuntimeError(f"oracle domain finish failed with code {rc}")
+        cnt = np.zeros(16, np.int64)
+        self.lib.po_counters(self.state, _ptr(cnt, _lp))
+        return acc, dict(zip(COUNTER_NAMES, (int(c) for c in cnt)))
 
     def run_domains(self, pos, p, nrank, nthreads=1, explicit_self=False):
         """One pass over `nrank` ranks emulated here: acc (n, 3) input

@@ -312,6 +312,8 @@ static void free_run(po_state *s)
 void po_destroy(po_state *s)
 {
     if (!s) return;
+    for (int k = 0; k < s->nrt; k++) { free(s->rt[k].node); free(s->rt[k].body); }
+    free(s->rt);
     free_run(s);
     for (int k = 0; k < 4; k++) { free(s->list[k].t); free(s->list[k].s); free(s->list[k].img); }
     free(s);
@@ -1220,7 +1222,13 @@ static int run_pass(po_state *s, const po_params *p, int n, const double *pos_in
 {
     if (nt < 0) return PO_ERR_ARG;
     /* a plain pass: the whole periodic box, nothing received */
-    if (s) { s->domain_set = 0; s->nrt = 0; }
+    if (s) {
+        s->domain_set = 0;
+        for (int k = 0; k < s->nrt; k++) { free(s->rt[k].node); free(s->rt[k].body); }
+        free(s->rt);
+        s->rt = NULL;
+        s->nrt = 0;
+    }
     double tp[2];
     int rc = prepare_pass(s, p, n, pos_in, targets == NULL, tp);
     if (rc) return rc;
@@ -1504,6 +1512,49 @@ int po_prepare_domain(po_state *s, const po_params *p, const double lo[3], const
     set_domain(s, lo, hi, axis);
     double t[2];
     return prepare_pass(s, p, n, pos_in, 0, t);
+}
+
+/* A tree received from another rank (layout of po_export), kept for
+   po_finish_domain; copied. */
+int po_import(po_state *s, int nnode, const void *nodes, int nbody, const double *bodies)
+{
+    if (!s || !s->node || nnode < 0 || nbody < 0) return PO_ERR_ARG;
+    if (nnode == 0) return PO_OK;
+    o_rtree *rt = realloc(s->rt, sizeof(o_rtree) * (size_t)(s->nrt + 1));
+    if (!rt) return PO_ERR_NOMEM;
+    s->rt = rt;
+    o_rtree *t = &s->rt[s->nrt];
+    t->nnode = nnode;
+    t->nbody = nbody;
+    t->node = malloc(sizeof(o_rnode) * (size_t)nnode);
+    t->body = malloc(sizeof(double) * 3 * (size_t)(nbody ? nbody : 1));
+    if (!t->node || !t->body) { free(t->node); free(t->body); return PO_ERR_NOMEM; }
+    memcpy(t->node, nodes, sizeof(o_rnode) * (size_t)nnode);
+    if (nbody) memcpy(t->body, bodies, sizeof(double) * 3 * (size_t)nbody);
+    s->nrt++;
+    return PO_OK;
+}
+
+/* fmm_task and fmm_ext of a prepared domain over the trees received so far
+   (own periodic images on the fly); acc_out[3n] in the prepared positions'
+   order; the received trees are released */
+int po_finish_domain(po_state *s, double *acc_out)
+{
+    if (!s || !s->node || !acc_out) return PO_ERR_ARG;
+    s->walk_m2l_count = 0;
+    int rc = run_walks(s, s->p.images);
+    if (!rc) {
+        s->p2p_count_remote = ext_pairs(s);
+        rc = forces(s, 0, NULL);
+    }
+    if (!rc)
+        for (int i = 0; i < s->n; i++)
+            for (int d = 0; d < 3; d++) acc_out[3 * (size_t)s->perm[i] + d] = s->acc[3 * (size_t)i + d];
+    for (int k = 0; k < s->nrt; k++) { free(s->rt[k].node); free(s->rt[k].body); }
+    free(s->rt);
+    s->rt = NULL;
+    s->nrt = 0;
+    return rc;
 }
 
 void po_counters(const po_state *s, long long *c)

@@ -82,6 +82,12 @@ int po_prepare_domain(po_state *s, const po_params *p, const double lo[3], const
 int po_export(const po_state *s, const double recv_center[3], const double recv_width[3], const double shift[3],
               int *nnode, int *nbody, int node_cap, int body_cap, void *nodes, double *bodies);
 
+/* a received tree (po_export's layout), kept for po_finish_domain */
+int po_import(po_state *s, int nnode, const void *nodes, int nbody, const double *bodies);
+/* the prepared domain's pass over the received trees: acc_out[3n] in the
+   prepared positions' order */
+int po_finish_domain(po_state *s, double *acc_out);
+
 /* counters[16]: idxP2P, idxM2L, walk_m2l_count, p2p_count_remote, NLEAF, NNODE,
    nleaf, nnode, first_leaf, first_node, direct_local_start(0), n_p2p, n_m2l,
    n_p2p_ext, n_m2l_ext, n_images, in the reference's index space. */
