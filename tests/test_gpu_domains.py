@@ -100,3 +100,74 @@ def test_one_rank_domain_pass_is_the_plain_pass(ph, ics):
     for k in COUNTERS:
         assert c0[k] == c1[k], k
     fp.close()
+
+
+class _ThreadGroup:
+    """A process-group stand-in for ranks run as threads of one process:
+    point-to-point sends through queues (the library's exchange is
+    host-staged, so the ranks' kernels never wait on one another)."""
+
+    def __init__(self, world):
+        import queue
+        self.world = world
+        self.q = {(a, b): queue.Queue() for a in range(world) for b in range(world)}
+
+    def rank_view(self, rank):
+        group = self
+
+        class View:
+            def get_rank(self):
+                return rank
+
+            def get_world_size(self):
+                return group.world
+
+            def get_backend(self):
+                return "gloo"
+
+            def isend(self, t, dst):
+                group.q[(rank, dst)].put(t.clone())
+
+                class Done:
+                    def wait(self):
+                        return True
+                return Done()
+
+            def recv(self, t, src):
+                t.copy_(group.q[(src, rank)].get(timeout=120))
+
+        return View()
+
+
+def test_domain_pass_class_over_ranks_as_threads(ph, ics, port):
+    """photons_gb300.domains.DomainPass, the per-rank driver a
+    torch.distributed job calls, with two ranks as threads sharing this GPU
+    (a context each): the same forces as the oracle's multi-rank pass."""
+    import threading
+    from photons_gb300 import domains
+    pos, p = ics.make("nfw128", nside=28, maxleaf=8)
+    nrank = 2
+    doms, split = ph.domain_split(nrank, p["boxsize"])
+    rank = ph.domain_assign(nrank, split, pos)
+    group = _ThreadGroup(nrank)
+    out, errs = {}, []
+
+    def run(r):
+        try:
+            fp = ph.ForcePass(0)
+            out[r] = domains.DomainPass(ph, fp, group.rank_view(r)).run(pos[rank == r], p, doms, ph.FP64)
+            fp.close()
+        except Exception as e:  # reported below
+            errs.append(e)
+
+    threads = [threading.Thread(target=run, args=(r,)) for r in range(nrank)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join(timeout=300)
+    assert not errs, errs
+    ref, _, rref = port.run_domains(pos, p, nrank, nthreads=4)
+    acc = np.empty_like(pos)
+    for r in range(nrank):
+        acc[rank == r] = out[r]
+    assert rel_err(acc, ref).max() <= 1e-10
