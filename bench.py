@@ -673,7 +673,8 @@ def main():
     e2e_ms = max_over_ranks(max(e0.elapsed_time(e1), loop_ms) / esteps, dist, "cuda")
     e2e_split = dict(zip(("h2d_ms", "device_ms", "d2h_ms", "events_total_ms", "host_call_ms"),
                          (float(np.median([q[i] for q in e2e_parts])) for i in range(5))))
-    e2e_split["host_call_ms_each"] = [round(q[4], 3) for q in e2e_parts]
+    e2e_split["each"] = {"h2d_ms": [round(q[0], 3) for q in e2e_parts], "device_ms": [round(q[1], 3) for q in e2e_parts],
+                         "d2h_ms": [round(q[2], 3) for q in e2e_parts], "host_call_ms": [round(q[4], 3) for q in e2e_parts]}
     acc32 = ha.copy()
 
     if rank != 0:
