@@ -718,8 +718,17 @@ def main():
             extra["parity"] = parity_leg(fp, pos, p, tgt, acc64[tgt], acc32[tgt], os.cpu_count() or 1)
         e = rel_err(acc32, acc64)
         a64 = rel_err(acc64[tgt], ds)
+        peak64 = ph.fp64_fma_peak()
+        c64 = fp.counters()
+        pairs64 = c64["pairs_local"] + c64["pairs_image"]
+        ach64 = FLOPS_PER_PAIR * pairs64 / (t64["p2p"] * 1e-3) / 1e12
         extra["fp64_gpu"] = {"value": n / (ms64 * 1e-3), "ms_per_pass": ms64, "p2p_ms": t64["p2p"],
-                             "speedup_fp32_over_fp64": ms64 / ms}
+                             "speedup_fp32_over_fp64": ms64 / ms,
+                             "roofline": {"bound": "fp64", "kernel": "k_p2p_fp64", "achieved": ach64, "peak": peak64,
+                                          "unit": "TFLOP/s", "frac": ach64 / peak64,
+                                          "peak_source": "DFMA probe measured in this run",
+                                          "work": "%d flops/pair x %d pairs, every pair evaluated one way"
+                                                  % (FLOPS_PER_PAIR, pairs64)}}
         extra["errors"] = {
             "precision_fp32_vs_fp64gpu": {"median": float(np.median(e)), "p99": float(np.percentile(e, 99)),
                                           "max": float(e.max())},

@@ -348,6 +348,8 @@ unsigned long long photons_launch_count(void);
    (float2) FFMA of sm_100+; ~iters x 128 FMAs per thread */
 double photons_fp32_fma_peak(int iters);
 double photons_fp32x2_fma_peak(int iters);
+/* the FP64 one (DFMA chains), the denominator of the FP64 pass's roofline */
+double photons_fp64_fma_peak(int iters);
 
 #ifdef __cplusplus
 }

@@ -112,6 +112,8 @@ def load_library():
     lib.photons_launch_count.argtypes = []
     lib.photons_fp32_fma_peak.restype = C.c_double
     lib.photons_fp32_fma_peak.argtypes = [C.c_int]
+    lib.photons_fp64_fma_peak.restype = C.c_double
+    lib.photons_fp64_fma_peak.argtypes = [C.c_int]
     lib.photons_gpu_error.restype = C.c_char_p
     lib.photons_gpu_status.restype = C.c_int
     for name in ("fmm_construct", "fmm_prepare", "fmm_task", "fmm_ext", "fmm_deconstruct", "build_localtree",
@@ -482,6 +484,14 @@ def drift(n, pos_ptr, vel_ptr, dd, boxsize, stream_ptr=0):
     """pos += vel dd, wrapped into [0, boxsize), on device arrays (asynchronous)."""
     _check(load_library().photons_drift(int(n), C.c_void_p(pos_ptr), C.c_void_p(vel_ptr), float(dd),
                                         float(boxsize), C.c_void_p(stream_ptr)))
+
+
+def fp64_fma_peak(iters=256):
+    lib = load_library()
+    v = lib.photons_fp64_fma_peak(int(iters))
+    if v <= 0:
+        raise PhotonsError("FP64 FMA probe failed: " + lib.photons_gpu_error().decode(errors="replace"))
+    return v
 
 
 def fp32_fma_peak(iters=4096):

@@ -5,7 +5,8 @@
 //    reference for the force pass (the pass truncates by tree cells, this
 //    does not).  Sources are binned into cells of side >= rmax on the host.
 //  * photons_fp32_fma_peak: FFMA throughput probe, the denominator of the
-//    P2P roofline fraction.
+//    P2P roofline fraction; photons_fp64_fma_peak: the DFMA one, for the
+//    FP64 drop-in pass.
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -80,6 +81,22 @@ __global__ void k_fma_probe(float *out, int iters, float seed)
     }
     float s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
     if (s == 1234.5f) out[0] = s;  // keeps the chains live
+}
+
+__global__ void k_dfma_probe(double *out, int iters, double seed)
+{
+    double a0 = seed + threadIdx.x, a1 = a0 + 1.0, a2 = a0 + 2.0, a3 = a0 + 3.0, a4 = a0 + 4.0, a5 = a0 + 5.0,
+           a6 = a0 + 6.0, a7 = a0 + 7.0;
+    const double m = 0.999999999, c = 1e-12;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            a0 = fma(a0, m, c); a1 = fma(a1, m, c); a2 = fma(a2, m, c); a3 = fma(a3, m, c);
+            a4 = fma(a4, m, c); a5 = fma(a5, m, c); a6 = fma(a6, m, c); a7 = fma(a7, m, c);
+        }
+    }
+    double s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+    if (s == 1234.5) out[0] = s;  // keeps the chains live
 }
 
 __global__ void k_fma2_probe(float *out, int iters, float seed)
@@ -215,6 +232,32 @@ extern "C" double photons_fp32_fma_peak(int iters)
     photons_gpu_clear_error();
     if (iters < 1) iters = 4096;
     return fma_probe(iters, false);
+}
+
+// TFLOP/s of DFMA chains (2 flops each) over the whole device
+extern "C" double photons_fp64_fma_peak(int iters)
+{
+    photons_gpu_clear_error();
+    if (iters < 1) iters = 256;
+    double *d = nullptr;
+    if (cudaMalloc(&d, sizeof(double)) != cudaSuccess) { cudaGetLastError(); return -1.0; }
+    const int blocks = ph::device_sm_count() * 8, threads = 256;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    ph::note_launch(), k_dfma_probe<<<blocks, threads>>>(d, iters / 8 + 1, 1.0);  // warm-up
+    cudaEventRecord(a);
+    ph::note_launch(), k_dfma_probe<<<blocks, threads>>>(d, iters, 1.0);
+    cudaEventRecord(b);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(d);
+    if (cudaGetLastError() != cudaSuccess || ms <= 0.f) return -1.0;
+    const double flops = 2.0 * 8.0 * 16.0 * (double)iters * blocks * threads;
+    return flops / (ms * 1e-3) / 1e12;
 }
 
 extern "C" double photons_fp32x2_fma_peak(int iters)
