@@ -94,7 +94,7 @@ static void dfree(T *&p)
 
 
 #define CHUNK_ELEMS 1024
-#define MAX_DEPTH_CAP 2048
+#define MAX_DEPTH_CAP PH_MAX_DEPTH_CAP
 
 // Each grow below first marks its capacity empty and bumps the epoch, then
 // sets the capacity only after every allocation succeeded: a failed
@@ -107,7 +107,7 @@ static int alloc_particles(photons_ctx *c, int n)
     c->cap_n = b.cap_n = 0;
     c->epoch++;
     PH_TRY(dalloc(b.x, n)); PH_TRY(dalloc(b.y, n)); PH_TRY(dalloc(b.z, n));
-    PH_TRY(dalloc(b.perm, n)); PH_TRY(dalloc(b.smallpos, n)); PH_TRY(dalloc(b.bigslot, n));
+    PH_TRY(dalloc(b.perm, n)); PH_TRY(dalloc(b.smallpos, n)); PH_TRY(dalloc(b.bigpos, n));
     PH_TRY(dalloc(c->pos4, n));
     PH_TRY(dalloc(c->ax, n)); PH_TRY(dalloc(c->ay, n)); PH_TRY(dalloc(c->az, n));
     PH_TRY(dalloc(c->io, (size_t)3 * n));
@@ -136,6 +136,7 @@ static int alloc_tree(photons_ctx *c, int n, int cap)
         PH_TRY(dalloc(b.tl_start, cap)); PH_TRY(dalloc(b.tl_len, cap)); PH_TRY(dalloc(b.tl_depth, cap));
         PH_TRY(dalloc(b.tl_parent, cap)); PH_TRY(dalloc(b.tl_final, cap)); PH_TRY(dalloc(b.tl_box, (size_t)6 * cap));
         PH_TRY(dalloc(b.tn_boxid, cap)); PH_TRY(dalloc(b.tl_boxid, cap));
+        PH_TRY(dalloc(b.tn_subroot, cap)); PH_TRY(dalloc(b.tl_subroot, cap));
         const size_t scratch = ph::scan_scratch_elems(cap > chunks ? cap : chunks) + 8;
         PH_TRY(dalloc(b.scan_scratch, scratch));
         b.scan_scratch_elems = scratch;
@@ -162,6 +163,16 @@ static int alloc_tree(photons_ctx *c, int n, int cap)
         PH_TRY(dalloc(t.depth_off, MAX_DEPTH_CAP + 2));
         PH_TRY(dalloc(t.depth_cnt, MAX_DEPTH_CAP + 2));
         t.max_depth_cap = MAX_DEPTH_CAP;
+        t.depth_nblk = 0;
+        const int nblk = ph::depth_sort_blocks(cu);
+        PH_TRY(dalloc(t.depth_blk, (size_t)2 * MAX_DEPTH_CAP * nblk));
+        t.depth_nblk = nblk;
+        const size_t need = ph::scan_scratch_elems(MAX_DEPTH_CAP * nblk) + 8;
+        if (need > b.scan_scratch_elems) {
+            b.scan_scratch_elems = 0;
+            PH_TRY(dalloc(b.scan_scratch, need));
+            b.scan_scratch_elems = need;
+        }
         t.cap_u = cu;
         // per-unified walk bookkeeping and expansions
         ph::WalkBufs &w = c->w;
@@ -184,7 +195,7 @@ static int alloc_tree(photons_ctx *c, int n, int cap)
         b.cap_chunks = 0;
         c->epoch++;
         PH_TRY(dalloc(b.ch_partial, chunks)); PH_TRY(dalloc(b.ch_cnt, chunks)); PH_TRY(dalloc(b.ch_small_base, chunks));
-        PH_TRY(dalloc(b.ch_node, chunks));
+        PH_TRY(dalloc(b.ch_node, chunks)); PH_TRY(dalloc(b.ch_big, chunks));
         c->epoch++;
         b.cap_chunks = chunks;
         size_t need = ph::scan_scratch_elems(cap > chunks ? cap : chunks) + 8;
@@ -245,7 +256,7 @@ static int alloc_walk(photons_ctx *c, long long p2p_cap, long long pd_cap, long 
 static void free_all(photons_ctx *c)
 {
     ph::BuildBufs &b = c->b;
-    void *ptrs[] = {b.x, b.y, b.z, b.perm, b.smallpos, b.bigslot, b.tn_start, b.tn_len, b.tn_depth, b.tn_parent,
+    void *ptrs[] = {b.x, b.y, b.z, b.perm, b.smallpos, b.bigpos, b.tn_start, b.tn_len, b.tn_depth, b.tn_parent,
                     b.tn_child0, b.tn_child1, b.tn_mode, b.tn_S, b.tn_box, b.tn_split, b.tn_nch, b.tn_chunk_base,
                     b.tn_nodeflag, b.tn_leafflag, b.tn_nodebase, b.tn_leafbase, b.tn_sub_nodes, b.tn_sub_leaves,
                     b.tn_pre, b.tn_lbase, b.tl_start, b.tl_len, b.tl_depth, b.tl_parent, b.tl_final, b.tl_box,
@@ -257,7 +268,8 @@ static void free_all(photons_ctx *c)
                     c->az, c->M, c->L, c->io, c->work_counter, c->t.chi, c->t.clo, c->t.w32, c->t.son2, c->M32,
                     b.lvl_begin, b.lvl_count, b.leaf_begin, b.leaf_count, c->t.depth_cnt, b.tn_boxid, b.tl_boxid,
                     c->t.boxid, b.boxes, c->far_gate, c->mu_sorted, c->mu_nrecv, c->mu_slot, c->mu_over,
-                    c->mu_size, c->mu_rbase, c->mu_total, c->mu_scan, c->mu_buf, c->mu_ev, c->mu_nev, c->mu_pq};
+                    c->mu_size, c->mu_rbase, c->mu_total, c->mu_scan, c->mu_buf, c->mu_ev, c->mu_nev, c->mu_pq,
+                    b.tn_subroot, b.tl_subroot, b.ch_big, c->t.depth_blk};
     for (void *p : ptrs)
         if (p) cudaFree(p);
 }
@@ -403,6 +415,20 @@ static int estimate_levels(int n, int maxleaf)
     return lv < MAX_DEPTH_CAP - 1 ? lv : MAX_DEPTH_CAP - 1;
 }
 
+// levels of wide nodes (more than CHUNK_ELEMS particles) to launch: the
+// last build's need with a margin, else an estimate from N; never above the
+// depth bound
+static int tree_top(const photons_ctx *c, int n, int levels)
+{
+    int top = c->hint_top;
+    if (top <= 0) {
+        top = 1;
+        while (top < 60 && (double)n / std::ldexp(1.0, top) > (double)CHUNK_ELEMS) top++;
+        top += 2;
+    }
+    return top < levels ? top : levels;
+}
+
 // validation, capacities and parameters of a pass over n particles
 // the reference's 2N/MAXLEAF node and leaf capacity of one box (src/fmm.c:203-209)
 static int box_cap(int n, int maxleaf)
@@ -520,7 +546,7 @@ static int ph_enqueue_tree(photons_ctx *c, const double *src, int levels)
 {
     cudaStream_t st = c->stream;
     PH_TRY(ph::launch_init_particles(c->b, src, c->n, st));
-    PH_TRY(ph::build_tree(c->b, c->t, c->pp, levels, st));
+    PH_TRY(ph::build_tree(c->b, c->t, c->pp, levels, tree_top(c, c->n, levels), st));
     PH_TRY(ph::launch_geom32(c->t, c->b.cnt, st));
     PH_TRY(ph::launch_leaf_offsets(c->b, c->t, c->pos4, st));
     c->ndepth = levels + 1;
@@ -528,7 +554,8 @@ static int ph_enqueue_tree(photons_ctx *c, const double *src, int levels)
 }
 
 // build flags after the stream has finished: capacity overflow is an error
-// of the reference's rule; PH_FLAG_DEPTH asks for more levels
+// of the reference's rule; PH_FLAG_TOP asks for more levels of wide nodes,
+// PH_FLAG_DEPTH for a deeper bound (*grow: the bound to build again with)
 static int ph_check_build(photons_ctx *c, int flags, int levels, int *grow)
 {
     *grow = 0;
@@ -536,7 +563,13 @@ static int ph_check_build(photons_ctx *c, int flags, int levels, int *grow)
         return ph_set_error(PH_ERR_CAPACITY, "leaf capacity 2N/MAXLEAF=%d exceeded by the mean-split tree", c->b.rule_cap);
     if (flags & PH_FLAG_NODE_CAPACITY)
         return ph_set_error(PH_ERR_CAPACITY, "node capacity 2N/MAXLEAF=%d exceeded by the mean-split tree", c->b.rule_cap);
-    if (flags & PH_FLAG_DEPTH) {
+    if (flags & (PH_FLAG_DEPTH | PH_FLAG_TOP)) {
+        const int top = tree_top(c, c->n, levels);
+        if (flags & PH_FLAG_TOP) c->hint_top = top * 2 > top + 4 ? top * 2 : top + 4;
+        if (!(flags & PH_FLAG_DEPTH) && top < levels) {
+            *grow = levels;
+            return 0;
+        }
         if (levels >= MAX_DEPTH_CAP - 1) return ph_set_error(PH_ERR_DEPTH, "tree deeper than %d levels", MAX_DEPTH_CAP - 1);
         *grow = levels * 2 < MAX_DEPTH_CAP - 1 ? levels * 2 : MAX_DEPTH_CAP - 1;
     }
@@ -550,11 +583,16 @@ static void ph_tree_info_from(photons_ctx *c, const int *h, int levels)
     c->info.depth = h[ph::BC_DEPTH];
     c->info.levels = h[ph::BC_NLEVELS];
     c->info.flags = h[ph::BC_FLAGS];
-    // keep the launch count while it covers the tree with a small margin,
-    // so repeated passes over similar trees reuse one captured graph
-    const int lv = c->info.levels;
+    // keep the launch counts while they cover the tree with a small margin,
+    // so repeated passes over similar trees reuse one captured graph: the
+    // depth bound over the deepest depth, the levels of wide nodes over the
+    // recorded levels (the last of them holds subtree roots only)
+    const int lv = c->info.depth;
     if (levels < lv + 1 || levels > lv + 6) c->hint_levels = lv + 3;
     else c->hint_levels = levels;
+    const int need = c->info.levels > 2 ? c->info.levels - 1 : 1, top = tree_top(c, c->n, levels);
+    if (top < need || top > need + 4) c->hint_top = need + 2;
+    else c->hint_top = top;
 }
 
 static int ph_stage_build_boxes(photons_ctx *c, int nbox, const photons_params *p, const int *counts,
@@ -788,7 +826,7 @@ static PassKey pass_key(photons_ctx *c, const photons_params *p, int n, const do
 {
     PassKey k;
     memset(&k, 0, sizeof k);
-    k.n = n; k.nbox = c->b.nbox; k.levels = levels; k.maxleaf = p->maxleaf; k.precision = p->precision; k.flags = p->flags;
+    k.n = n; k.nbox = c->b.nbox; k.levels = levels; k.top = tree_top(c, n, levels); k.maxleaf = p->maxleaf; k.precision = p->precision; k.flags = p->flags;
     k.dio = dio; k.variant = p2p_variant(); k.nwarps = c->w.nwarps; k.mask = mask;
     k.boxsize = p->boxsize; k.theta = p->theta; k.rs = p->rs; k.rcut = p->rcut; k.eps = p->eps; k.mass = p->mass;
     k.pos = dio ? (const void *)pos : nullptr;

@@ -30,7 +30,7 @@ enum {
 // Everything a captured pass bakes in; a pass with a different key is
 // captured anew.  Zero-filled before use so it compares with memcmp.
 struct PassKey {
-    int n, nbox, levels, maxleaf, precision, flags, dio, variant, nwarps;
+    int n, nbox, levels, top, maxleaf, precision, flags, dio, variant, nwarps;
     unsigned mask;
     double boxsize, theta, rs, rcut, eps, mass;
     const void *pos, *acc;
@@ -81,6 +81,7 @@ struct photons_ctx {
     bool have_tree = false, have_lists = false, have_multipoles = false;
     long long hint_p2p = 0, hint_pd = 0, hint_m2l = 0;
     int hint_levels = 0;  // node levels to launch (0: estimate from N)
+    int hint_top = 0;     // levels of wide nodes to launch (0: estimate from N)
     std::vector<BoxParams> h_boxes;  // this pass's box table (host copy)
     int cap_box = 0;
     int ndepth = 0;       // depths the walk and far field launch

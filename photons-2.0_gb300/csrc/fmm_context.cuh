@@ -16,7 +16,7 @@ struct BuildBufs {
     double *x = nullptr, *y = nullptr, *z = nullptr;
     int *perm = nullptr;
     int *smallpos = nullptr;   // slot -> position of a right-region particle not above the mean
-    int *bigslot = nullptr;    // position -> slot for a left-region particle above the mean (-1 otherwise)
+    int *bigpos = nullptr;     // slot -> position of a left-region particle above the mean
     // temp nodes
     int *tn_start = nullptr, *tn_len = nullptr, *tn_depth = nullptr, *tn_parent = nullptr;
     int *tn_child0 = nullptr, *tn_child1 = nullptr, *tn_mode = nullptr, *tn_S = nullptr;
@@ -25,12 +25,15 @@ struct BuildBufs {
     int *tn_nch = nullptr, *tn_chunk_base = nullptr;
     int *tn_nodeflag = nullptr, *tn_leafflag = nullptr, *tn_nodebase = nullptr, *tn_leafbase = nullptr;
     int *tn_sub_nodes = nullptr, *tn_sub_leaves = nullptr, *tn_pre = nullptr, *tn_lbase = nullptr;
+    int *tn_subroot = nullptr;  // nodes of a shared-memory subtree: the subtree's root
     // temp leaves
     int *tl_start = nullptr, *tl_len = nullptr, *tl_depth = nullptr, *tl_parent = nullptr, *tl_final = nullptr;
+    int *tl_subroot = nullptr;
     double *tl_box = nullptr;  // [6][cap_leaves]
     // chunks
     double *ch_partial = nullptr;
     int *ch_cnt = nullptr, *ch_small_base = nullptr, *ch_node = nullptr;
+    int *ch_big = nullptr;  // left-region particles above the mean, per chunk
     // small device counters
     int *cnt = nullptr;  // see BuildCounter
     int *lvl_begin = nullptr, *lvl_count = nullptr;    // per node level: first temp node, count
@@ -57,8 +60,16 @@ enum BuildCounter {
     BC_NODES = 7,         // temp nodes in total (after the build)
     BC_NLEVELS = 8,       // node levels built
     BC_DEPTH = 9,         // deepest depth holding a node or leaf
-    BC_NCOUNTERS = 12
+    BC_SUB_NODES = 10,    // nodes below the roots of shared-memory subtrees
+    BC_SUB_LEAVES = 11,   // leaves of shared-memory subtrees
+    BC_NEXT_WIDE = 12,    // wide nodes created by the current level
+    BC_DEPTH_CELLS = 13,  // cells of the depth-list counting sort
+    BC_DEPTH_TOTAL = 14,
+    BC_NCOUNTERS = 16
 };
+
+// deepest tree the depth lists hold (depths 0..PH_MAX_DEPTH_CAP-1)
+#define PH_MAX_DEPTH_CAP 2048
 
 // Final tree in unified index space (leaves then nodes).
 struct TreeBufs {
@@ -76,6 +87,8 @@ struct TreeBufs {
     int *depth_list = nullptr;  // [cap_u]
     int *depth_cnt = nullptr;   // [max_depth+1]
     int max_depth_cap = 0;
+    int *depth_blk = nullptr;   // counting-sort cells and their scan, 2 x max_depth_cap x depth_nblk
+    int depth_nblk = 0;
 };
 
 struct TreeInfo {
@@ -137,7 +150,9 @@ struct WalkImports {
 int walk_lists(WalkBufs &w, const TreeBufs &t, const int *tree_cnt, const BoxParams *boxes, int ndepth,
                const PassParams &p, unsigned image_mask, cudaStream_t st, const WalkImports &imp = WalkImports());
 
-int build_tree(BuildBufs &b, TreeBufs &t, const PassParams &p, int levels, cudaStream_t st);
+// top: launched levels of wide nodes (<= levels); levels: depth bound
+int build_tree(BuildBufs &b, TreeBufs &t, const PassParams &p, int levels, int top, cudaStream_t st);
+int depth_sort_blocks(int cap_u);
 int read_tree_info(const BuildBufs &b, const TreeBufs &t, int levels, TreeInfo &info);
 
 }  // namespace ph

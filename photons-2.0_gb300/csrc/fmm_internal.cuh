@@ -38,6 +38,7 @@
 #define PH_FLAG_LEAF_CAPACITY 8u
 #define PH_FLAG_NODE_CAPACITY 16u
 #define PH_FLAG_DEPTH 32u
+#define PH_FLAG_TOP 64u  // wide nodes left after the launched levels of the tree build
 
 struct PassParams {
     double boxsize, theta, rs, rcut, eps, mass;

@@ -1,11 +1,11 @@
 // kd-tree build on the device.
 //
 // Restates src/fmm.c:30-264 (bksort_inplace, build_kdtree, center_kdtree,
-// build_localtree) as a level-synchronous build: every node of one depth
-// is split in the same set of launches.  Per level:
-//   1. each node's particle range is cut into chunks of CHUNK particles
-//      (a node of at most one chunk is split by one warp in k_narrow_split,
-//      which does steps 2-3 for it in one kernel);
+// build_localtree) in two parts.
+//
+// Wide nodes (more than CHUNK particles) are split level-synchronously:
+// every wide node of one depth in the same set of launches.  Per level:
+//   1. each node's particle range is cut into chunks of CHUNK particles;
 //   2. chunk sums of the split coordinate (axis = depth mod 3) and a
 //      fixed-order reduction give the node's mean;
 //   3. the reference's two-ended swap partition (src/fmm.c:58-72) is
@@ -16,6 +16,11 @@
 //      swaps are independent and run in parallel;
 //   4. children with <= MAXLEAF particles become leaves, the others nodes
 //      of the next level; child boxes come from the split plane.
+// A node of at most CHUNK particles is not split by the levels: it roots a
+// subtree that one block builds whole in shared memory (k_subtree_build),
+// every node of it split by one warp with the arithmetic the levels would
+// give a node of one chunk, so the tree is the one a build that splits
+// every depth level by level makes.
 // Special cases follow the reference: a pair splits at its midpoint and is
 // ordered (src/fmm.c:38-47); if no particle lies above the mean the last
 // one goes to the upper child.
@@ -34,10 +39,22 @@
 #define CHUNK 1024
 #define TB 256
 
+// subtree blocks: one warp per node of the subtree level being split
+#define SUB_TB 256
+#define SUB_NW (SUB_TB / 32)
+
+// depth lists: unified ids per block (one warp) of the counting sort
+#define DEPTH_R 4096
+
+// temp-node modes: 0-2 the kinds of a split node (two-ended swap, nothing
+// above the mean, a pair), then the two states of a node not yet split
+#define MODE_DEFERRED 3  // at most CHUNK particles: split by k_subtree_build
+#define MODE_PENDING 4   // wide: split by the levels
+
 namespace ph {
 namespace {
 
-__device__ __forceinline__ const double *axis_ptr(const double *x, const double *y, const double *z, int D)
+__host__ __device__ __forceinline__ const double *axis_ptr(const double *x, const double *y, const double *z, int D)
 {
     return D == 0 ? x : (D == 1 ? y : z);
 }
@@ -54,6 +71,7 @@ __global__ void k_init_roots(BuildBufs b)
         b.tn_depth[t] = 0;
         b.tn_parent[t] = -1;
         b.tn_boxid[t] = t;
+        b.tn_mode[t] = B.count <= CHUNK ? MODE_DEFERRED : MODE_PENDING;
         for (int d = 0; d < 3; d++) {
             // a rank's domain: its top-tree node's centre and width
             // (src/toptree.c:150-159) give the bounds of src/fmm.c:189-197
@@ -81,13 +99,19 @@ __global__ void k_init_particles(const double *__restrict__ pos, int n, BuildBuf
     }
 }
 
-
+// chunks per node; a deferred node has none and makes no children here
 __global__ void k_level_nch(BuildBufs b)
 {
     const int lb = b.cnt[BC_LEVEL_BEGIN], C = b.cnt[BC_LEVEL_COUNT];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
-        const int len = b.tn_len[lb + i];
-        b.tn_nch[i] = len <= CHUNK ? 0 : (len + CHUNK - 1) / CHUNK;  // one chunk or less: k_narrow_split
+        const int t = lb + i;
+        if (b.tn_mode[t] == MODE_DEFERRED) {
+            b.tn_nch[i] = 0;
+            b.tn_nodeflag[i] = 0;
+            b.tn_leafflag[i] = 0;
+        } else {
+            b.tn_nch[i] = (b.tn_len[t] + CHUNK - 1) / CHUNK;
+        }
     }
 }
 
@@ -103,6 +127,9 @@ __global__ void k_chunk_map(BuildBufs b)
     }
 }
 
+// Chunk sums: lane l adds positions l, l+32, l+64, ... of the chunk in that
+// order, then the warp butterfly.  Loads are issued eight at a time ahead
+// of the adds, which keep their order.
 __global__ void k_chunk_sum(BuildBufs b, int D)
 {
     const int lb = b.cnt[BC_LEVEL_BEGIN];
@@ -116,15 +143,24 @@ __global__ void k_chunk_sum(BuildBufs b, int D)
         int start = b.tn_start[t], len = b.tn_len[t];
         int s0 = (w - b.tn_chunk_base[i]) * CHUNK;
         int s1 = min(len, s0 + CHUNK);
+        const double *cp = coord + start;
         double s = 0.0;
-        for (int k = s0 + lane; k < s1; k += 32) s += coord[start + k];
+        int k = s0 + lane;
+        for (; k + 224 < s1; k += 256) {
+            double v[8];
+#pragma unroll
+            for (int q = 0; q < 8; q++) v[q] = cp[k + 32 * q];
+#pragma unroll
+            for (int q = 0; q < 8; q++) s += v[q];
+        }
+        for (; k < s1; k += 32) s += cp[k];
         s = warp_sum_d(s);
         if (lane == 0) b.ch_partial[w] = s;
     }
 }
 
-// Node means of the nodes of more than one chunk, a warp each:
-// lane-strided sums of the chunk sums, then the warp reduction (fixed order)
+// Node means, a warp each: lane-strided sums of the chunk sums, then the
+// warp reduction (fixed order)
 __global__ void k_node_mean(BuildBufs b, int D)
 {
     const int lb = b.cnt[BC_LEVEL_BEGIN], C = b.cnt[BC_LEVEL_COUNT];
@@ -156,11 +192,29 @@ __global__ void k_chunk_count(BuildBufs b, int D)
         double mean = b.tn_split[t];
         int s0 = (w - b.tn_chunk_base[i]) * CHUNK;
         int s1 = min(len, s0 + CHUNK);
+        const double *cp = coord + start;
         int c = 0;
-        for (int k = s0 + lane; k < s1; k += 32) c += !(coord[start + k] > mean);
+        int k = s0 + lane;
+        for (; k + 224 < s1; k += 256) {
+            double v[8];
+#pragma unroll
+            for (int q = 0; q < 8; q++) v[q] = cp[k + 32 * q];
+#pragma unroll
+            for (int q = 0; q < 8; q++) c += !(v[q] > mean);
+        }
+        for (; k < s1; k += 32) c += !(cp[k] > mean);
         c = __reduce_add_sync(0xffffffffu, c);
         if (lane == 0) b.ch_cnt[w] = c;
     }
+}
+
+// the split kind and lower-child size of a node of len particles, S of them
+// not above the mean
+__device__ __forceinline__ void split_sizes(int len, int S, int &mode, int &left)
+{
+    if (len == 2) { mode = 2; left = 1; }
+    else if (S == len) { mode = 1; left = len - 1; }
+    else { mode = 0; left = S; }
 }
 
 // per node: the child kinds and sizes from the count of particles not above
@@ -168,9 +222,7 @@ __global__ void k_chunk_count(BuildBufs b, int D)
 __device__ __forceinline__ void node_split_finish(BuildBufs &b, int i, int t, int len, int S, int maxleaf)
 {
     int mode, left;
-    if (len == 2) { mode = 2; left = 1; }
-    else if (S == len) { mode = 1; left = len - 1; }
-    else { mode = 0; left = S; }
+    split_sizes(len, S, mode, left);
     b.tn_S[t] = S;
     b.tn_mode[t] = mode;
     int right = len - left;
@@ -181,7 +233,7 @@ __device__ __forceinline__ void node_split_finish(BuildBufs &b, int i, int t, in
     b.tn_leafflag[i] = (left <= maxleaf) + (right <= maxleaf);
 }
 
-// per node of more than one chunk, a warp each: prefix of chunk counts,
+// per wide node of the level, a warp each: prefix of chunk counts,
 // partition sizes, child kinds.  Each lane sums a contiguous block of chunk
 // counts (the prefix is exact integer arithmetic, so the blocking does not
 // change it).
@@ -216,6 +268,7 @@ __global__ void k_make_children(BuildBufs b, int maxleaf, int D)
     int leaves_before = b.cnt[BC_LEAVES];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
         int t = lb + i;
+        if (b.tn_mode[t] == MODE_DEFERRED) continue;
         int start = b.tn_start[t];
         int depth = b.tn_depth[t];
         int sizes[2] = {b.tn_child0[t], b.tn_child1[t]};
@@ -229,6 +282,7 @@ __global__ void k_make_children(BuildBufs b, int maxleaf, int D)
         int lid = leaves_before + b.tn_leafbase[i];
         int code[2];
         int ip = start;
+        int wide = 0;
         for (int c = 0; c < 2; c++) {
             double clo[3] = {lo[0], lo[1], lo[2]}, chi[3] = {hi[0], hi[1], hi[2]};
             if (c == 0) chi[D] = split;
@@ -260,6 +314,8 @@ __global__ void k_make_children(BuildBufs b, int maxleaf, int D)
                     b.tn_depth[nid] = depth + 1;
                     b.tn_parent[nid] = t;
                     b.tn_boxid[nid] = b.tn_boxid[t];
+                    b.tn_mode[nid] = sizes[c] <= CHUNK ? MODE_DEFERRED : MODE_PENDING;
+                    wide += sizes[c] > CHUNK;
                     for (int d = 0; d < 3; d++) {
                         b.tn_box[d * b.cap_nodes + nid] = clo[d];
                         b.tn_box[(3 + d) * b.cap_nodes + nid] = chi[d];
@@ -272,12 +328,15 @@ __global__ void k_make_children(BuildBufs b, int maxleaf, int D)
         }
         b.tn_child0[t] = code[0];
         b.tn_child1[t] = code[1];
+        if (wide) atomicAdd(&b.cnt[BC_NEXT_WIDE], wide);
     }
 }
 
-// close level d: record its node range and the leaves it created, advance.
-// After a capacity overflow no further level is built.
-__global__ void k_level_finish(BuildBufs b, int d)
+// Close level d: record its node range and the leaves it created, advance.
+// When the last launched level (d = top - 1) made deferred nodes only,
+// they are recorded as level top for k_subtree_build.  After a capacity
+// overflow no further level is built.
+__global__ void k_level_finish(BuildBufs b, int d, int top)
 {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         const int C = b.cnt[BC_LEVEL_COUNT], lb = b.cnt[BC_LEVEL_BEGIN];
@@ -292,23 +351,36 @@ __global__ void k_level_finish(BuildBufs b, int d)
         b.leaf_count[d + 1] = b.cnt[BC_NEW_LEAVES];
         b.cnt[BC_LEAVES] += b.cnt[BC_NEW_LEAVES];
         b.cnt[BC_LEVEL_BEGIN] = lb + C;
-        b.cnt[BC_LEVEL_COUNT] = b.cnt[BC_NEXT_NODES];
+        const int next = b.cnt[BC_NEXT_NODES];
+        b.cnt[BC_LEVEL_COUNT] = next;
         b.cnt[BC_NLEVELS] = d + 1;
+        if (d == top - 1 && next > 0 && b.cnt[BC_NEXT_WIDE] == 0) {
+            b.lvl_begin[d + 1] = lb + C;
+            b.lvl_count[d + 1] = next;
+            b.cnt[BC_LEVEL_BEGIN] = lb + C + next;
+            b.cnt[BC_LEVEL_COUNT] = 0;
+            b.cnt[BC_NLEVELS] = d + 2;
+        }
+        b.cnt[BC_NEXT_WIDE] = 0;
     }
 }
 
-// After the last launched level: totals, and PH_FLAG_DEPTH if nodes remain
-// unsplit.  A failed build (capacity or depth) reports an empty tree, so
-// every later stage of the pass has no work and reads nothing stale.
+// After k_subtree_build: totals, and PH_FLAG_TOP if wide nodes remain
+// unsplit after the last launched level.  A failed build (capacity, depth
+// or levels) reports an empty tree, so every later stage of the pass has
+// no work and reads nothing stale.
 __global__ void k_tree_totals(BuildBufs b)
 {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        b.cnt[BC_NODES] = b.cnt[BC_LEVEL_BEGIN];
-        if (b.cnt[BC_LEVEL_COUNT] > 0) b.cnt[BC_FLAGS] |= PH_FLAG_DEPTH;
-        if (b.cnt[BC_FLAGS] & (PH_FLAG_LEAF_CAPACITY | PH_FLAG_NODE_CAPACITY | PH_FLAG_DEPTH)) {
+        if (b.cnt[BC_LEVEL_COUNT] > 0) b.cnt[BC_FLAGS] |= PH_FLAG_TOP;
+        b.cnt[BC_NODES] = b.cnt[BC_LEVEL_BEGIN] + b.cnt[BC_SUB_NODES];
+        b.cnt[BC_LEAVES] += b.cnt[BC_SUB_LEAVES];
+        if (b.cnt[BC_FLAGS] & (PH_FLAG_LEAF_CAPACITY | PH_FLAG_NODE_CAPACITY | PH_FLAG_DEPTH | PH_FLAG_TOP)) {
             b.cnt[BC_NODES] = 0;
             b.cnt[BC_LEAVES] = 0;
             b.cnt[BC_NLEVELS] = 0;
+            b.cnt[BC_SUB_NODES] = 0;
+            b.cnt[BC_SUB_LEAVES] = 0;
         }
     }
 }
@@ -316,9 +388,11 @@ __global__ void k_tree_totals(BuildBufs b)
 // Ranks for the swap partition.  A particle not above the mean that sits in
 // the right region (p >= S) publishes its position under slot S-1-r (r =
 // its rank among such particles, counted from the left); a particle above
-// the mean in the left region (p < S) records slot p-r (its rank among
-// particles above the mean).  Slot k pairs the k-th from the left with the
-// k-th from the right, which is the order src/fmm.c:60-72 swaps them in.
+// the mean in the left region (p < S) publishes its position under slot
+// p-r (its rank among particles above the mean).  Slot k pairs the k-th
+// from the left with the k-th from the right, which is the order
+// src/fmm.c:60-72 swaps them in.  ch_big counts the chunk's left-region
+// particles above the mean, so k_swap walks the chunk's slots.
 __global__ void k_rank(BuildBufs b, int D)
 {
     const int lb = b.cnt[BC_LEVEL_BEGIN];
@@ -336,73 +410,139 @@ __global__ void k_rank(BuildBufs b, int D)
         int S = b.tn_S[t];
         int s0 = (w - b.tn_chunk_base[i]) * CHUNK;
         int s1 = min(len, s0 + CHUNK);
+        const double *cp = coord + start;
+        int *bigpos = b.bigpos + start, *smallpos = b.smallpos + start;
         int run = b.ch_small_base[w];
-        for (int k0 = s0; k0 < s1; k0 += 32) {
-            int p = k0 + lane;
-            bool in = p < s1;
-            bool small = in && !(coord[start + p] > mean);
-            unsigned m = __ballot_sync(0xffffffffu, small);
-            int r = run + __popc(m & lt);
-            if (in) {
-                if (p < S) b.bigslot[start + p] = small ? -1 : (p - r);
-                else if (small) b.smallpos[start + (S - 1 - r)] = p;
+        int nbig = 0;
+        for (int k0 = s0; k0 < s1; k0 += 128) {
+            double v[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int p = k0 + 32 * q + lane;
+                v[q] = p < s1 ? cp[p] : 0.0;
             }
-            run += __popc(m);
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int p = k0 + 32 * q + lane;
+                const bool in = p < s1;
+                const bool small = in && !(v[q] > mean);
+                const unsigned m = __ballot_sync(0xffffffffu, small);
+                const int r = run + __popc(m & lt);
+                if (in) {
+                    if (p < S) { if (!small) bigpos[p - r] = p; }
+                    else if (small) smallpos[S - 1 - r] = p;
+                }
+                nbig += __popc(__ballot_sync(0xffffffffu, in && p < S && !small));
+                run += __popc(m);
+            }
+        }
+        if (lane == 0) b.ch_big[w] = nbig;
+    }
+}
+
+// The swaps of a chunk's slots: its left-region particles above the mean
+// hold slots [s0 - (particles not above the mean before s0), + ch_big);
+// each slot's two particles trade places.  Pairs are disjoint; a lane loads
+// four slots' particles before it stores any.
+__global__ void k_swap(BuildBufs b, int D)
+{
+    const int lb = b.cnt[BC_LEVEL_BEGIN];
+    int W = b.cnt[BC_W];
+    int lane = warp_lane();
+    int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    for (int w = gw; w < W; w += nw) {
+        int i = b.ch_node[w];
+        int t = lb + i;
+        if (b.tn_mode[t] != 0) continue;
+        const int start = b.tn_start[t], S = b.tn_S[t];
+        const int s0 = (w - b.tn_chunk_base[i]) * CHUNK;
+        if (s0 >= S) continue;
+        const int kb = s0 - b.ch_small_base[w], nb = b.ch_big[w];
+        const int *bigpos = b.bigpos + start + kb, *smallpos = b.smallpos + start + kb;
+        for (int k0 = 0; k0 < nb; k0 += 128) {
+            int pi[4], pj[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int k = k0 + 32 * q + lane;
+                pi[q] = k < nb ? start + bigpos[k] : -1;
+                pj[q] = k < nb ? start + smallpos[k] : -1;
+            }
+            double xi[4], yi[4], zi[4], xj[4], yj[4], zj[4];
+            int qi[4], qj[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                if (pi[q] >= 0) {
+                    xi[q] = b.x[pi[q]]; yi[q] = b.y[pi[q]]; zi[q] = b.z[pi[q]]; qi[q] = b.perm[pi[q]];
+                    xj[q] = b.x[pj[q]]; yj[q] = b.y[pj[q]]; zj[q] = b.z[pj[q]]; qj[q] = b.perm[pj[q]];
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                if (pi[q] >= 0) {
+                    b.x[pi[q]] = xj[q]; b.y[pi[q]] = yj[q]; b.z[pi[q]] = zj[q]; b.perm[pi[q]] = qj[q];
+                    b.x[pj[q]] = xi[q]; b.y[pj[q]] = yi[q]; b.z[pj[q]] = zi[q]; b.perm[pj[q]] = qi[q];
+                }
+            }
         }
     }
 }
 
-__device__ __forceinline__ void swap_particles(BuildBufs &b, int i, int j)
+// ---------------- subtrees of at most CHUNK particles ----------------
+struct SubTree {
+    double x[CHUNK], y[CHUNK], z[CHUNK];  // the subtree's particles; then the numbering arrays
+    int perm[CHUNK];
+    unsigned short bigpos[CHUNK], smallpos[CHUNK];  // a node's slots, over its own local range
+    // nodes in creation order (node 0 the subtree root): local range,
+    // parent, child codes (>= 0 node, < 0 ~leaf), split
+    unsigned short n_start[CHUNK], n_len[CHUNK], n_parent[CHUNK];
+    short n_c0[CHUNK], n_c1[CHUNK];
+    double n_split[CHUNK];
+    unsigned short l_start[CHUNK], l_len[CHUNK], l_parent[CHUNK];
+    unsigned short lev[CHUNK + 2];  // first node of each level of the subtree
+    int nnodes, nleaves, fail, nbase, lbase;
+};
+
+__device__ __forceinline__ void sub_swap(SubTree &s, int i, int j)
 {
     double t;
-    t = b.x[i]; b.x[i] = b.x[j]; b.x[j] = t;
-    t = b.y[i]; b.y[i] = b.y[j]; b.y[j] = t;
-    t = b.z[i]; b.z[i] = b.z[j]; b.z[j] = t;
-    int q = b.perm[i]; b.perm[i] = b.perm[j]; b.perm[j] = q;
+    t = s.x[i]; s.x[i] = s.x[j]; s.x[j] = t;
+    t = s.y[i]; s.y[i] = s.y[j]; s.y[j] = t;
+    t = s.z[i]; s.z[i] = s.z[j]; s.z[j] = t;
+    int q = s.perm[i]; s.perm[i] = s.perm[j]; s.perm[j] = q;
 }
 
-// Nodes of at most one chunk, a warp each, in one kernel while the node's
-// data is in cache: the sum, mean, count, child kinds, ranks and swaps that
-// k_chunk_sum, k_node_mean, k_chunk_count, k_node_split, k_rank and k_swap
-// give a node of one chunk, with the same lane order and reductions (the
-// chunk sum is lane 0's butterfly result; the mean adds it to 0.0 first, as
-// the one-term reduction of k_node_mean does).
-__global__ void k_narrow_split(BuildBufs b, int D, int maxleaf)
+// One warp splits node i of the subtree (at the given depth): the mean,
+// count, ranks and swaps a node of one chunk gets, with the same lane order
+// and reductions (the sum is lane 0's butterfly result added to 0.0, as the
+// one-term reduction of k_node_mean does), then its two children.
+__device__ void sub_split_node(SubTree &s, int i, int depth, int axis0, int maxleaf, int levels)
 {
-    const int lb = b.cnt[BC_LEVEL_BEGIN], C = b.cnt[BC_LEVEL_COUNT];
-    const double *coord = axis_ptr(b.x, b.y, b.z, D);
     const int lane = warp_lane();
     const unsigned lt = (1u << lane) - 1u;
-    int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-    for (int i = gw; i < C; i += nw) {
-        if (b.tn_nch[i] != 0) continue;
-        const int t = lb + i;
-        const int start = b.tn_start[t], len = b.tn_len[t];
-        const double *cd = coord + start;
-        double mean;
-        if (len == 2) {
-            mean = 0.5 * (cd[0] + cd[1]);
-        } else {
-            double s = 0.0;
-            for (int k = lane; k < len; k += 32) s += cd[k];
-            s = __shfl_sync(0xffffffffu, warp_sum_d(s), 0);
-            double m = 0.0;
-            m += s;
-            mean = m / (double)len;
-        }
-        int c = 0;
-        for (int k = lane; k < len; k += 32) c += !(cd[k] > mean);
-        const int S = __reduce_add_sync(0xffffffffu, c);
-        if (lane == 0) {
-            b.tn_split[t] = mean;
-            node_split_finish(b, i, t, len, S, maxleaf);
-        }
-        if (len == 2) {
-            if (lane == 0 && cd[0] > cd[1]) swap_particles(b, start, start + 1);
-            continue;
-        }
-        if (S == len) continue;  // nothing above the mean: the last particle goes up, no swaps
-        int run = 0;
+    const int ns = s.n_start[i], len = s.n_len[i];
+    const int D = (axis0 + depth) % 3;
+    const double *cd = axis_ptr(s.x, s.y, s.z, D) + ns;
+    double mean;
+    if (len == 2) {
+        mean = 0.5 * (cd[0] + cd[1]);
+    } else {
+        double sum = 0.0;
+        for (int k = lane; k < len; k += 32) sum += cd[k];
+        sum = __shfl_sync(0xffffffffu, warp_sum_d(sum), 0);
+        double m = 0.0;
+        m += sum;
+        mean = m / (double)len;
+    }
+    int c = 0;
+    for (int k = lane; k < len; k += 32) c += !(cd[k] > mean);
+    const int S = __reduce_add_sync(0xffffffffu, c);
+    int mode, left;
+    split_sizes(len, S, mode, left);
+    if (len == 2) {
+        if (lane == 0 && cd[0] > cd[1]) sub_swap(s, ns, ns + 1);
+    } else if (mode == 0) {
+        unsigned short *bigpos = s.bigpos + ns, *smallpos = s.smallpos + ns;
+        int run = 0, nbig = 0;
         for (int k0 = 0; k0 < len; k0 += 32) {
             const int p = k0 + lane;
             const bool in = p < len;
@@ -410,56 +550,218 @@ __global__ void k_narrow_split(BuildBufs b, int D, int maxleaf)
             const unsigned m = __ballot_sync(0xffffffffu, small);
             const int r = run + __popc(m & lt);
             if (in) {
-                if (p < S) b.bigslot[start + p] = small ? -1 : (p - r);
-                else if (small) b.smallpos[start + (S - 1 - r)] = p;
+                if (p < S) { if (!small) bigpos[p - r] = (unsigned short)p; }
+                else if (small) smallpos[S - 1 - r] = (unsigned short)p;
             }
+            nbig += __popc(__ballot_sync(0xffffffffu, in && p < S && !small));
             run += __popc(m);
         }
         __syncwarp();
-        for (int p = lane; p < S; p += 32) {
-            const int k = b.bigslot[start + p];
-            if (k >= 0) swap_particles(b, start + p, start + b.smallpos[start + k]);
+        for (int k = lane; k < nbig; k += 32) sub_swap(s, ns + bigpos[k], ns + smallpos[k]);
+    }
+    __syncwarp();
+    if (lane == 0) {
+        s.n_split[i] = mean;
+        const int sizes[2] = {left, len - left};
+        int off = ns;
+        for (int ch = 0; ch < 2; ch++) {
+            int code;
+            if (sizes[ch] <= maxleaf) {
+                const int j = atomicAdd(&s.nleaves, 1);
+                s.l_start[j] = (unsigned short)off;
+                s.l_len[j] = (unsigned short)sizes[ch];
+                s.l_parent[j] = (unsigned short)i;
+                code = ~j;
+            } else {
+                if (depth + 1 >= levels) s.fail = 1;  // a node below the launched depths
+                const int j = atomicAdd(&s.nnodes, 1);
+                s.n_start[j] = (unsigned short)off;
+                s.n_len[j] = (unsigned short)sizes[ch];
+                s.n_parent[j] = (unsigned short)i;
+                code = j;
+            }
+            if (ch == 0) s.n_c0[i] = (short)code;
+            else s.n_c1[i] = (short)code;
+            off += sizes[ch];
         }
-        __syncwarp();
     }
 }
 
-// Each pair is exchanged by the thread of its left-region member only, so
-// the exchanges are disjoint.
-__global__ void k_swap(BuildBufs b, int D)
+// One block per deferred node: load its particles into shared memory, split
+// its subtree level by level (a warp per node), write the particles back,
+// number the subtree's nodes in preorder and its leaves depth-first, then
+// write them into the temp arrays after the level-built ones, with boxes
+// from the split planes.  A subtree node's own preorder number goes to
+// tn_pre and its root to tn_subroot (leaves: tl_final, tl_subroot);
+// k_subtree_number adds the root's numbers once the levels are numbered.
+// Every barrier is reached by all threads of the block: the loop bounds and
+// the failure flag are read between two barriers.
+__global__ void __launch_bounds__(SUB_TB) k_subtree_build(BuildBufs b, int axis0, int maxleaf, int levels)
 {
-    const int lb = b.cnt[BC_LEVEL_BEGIN];
-    const double *coord = axis_ptr(b.x, b.y, b.z, D);
-    int W = b.cnt[BC_W];
-    int lane = warp_lane();
-    int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-    for (int w = gw; w < W; w += nw) {
-        int i = b.ch_node[w];
-        int t = lb + i;
-        int mode = b.tn_mode[t];
-        int start = b.tn_start[t], len = b.tn_len[t];
-        if (mode == 2) {
-            if (lane == 0 && coord[start] > coord[start + 1]) swap_particles(b, start, start + 1);
+    extern __shared__ __align__(16) unsigned char sub_smem[];
+    SubTree &s = *reinterpret_cast<SubTree *>(sub_smem);
+    if (b.cnt[BC_LEVEL_COUNT] > 0 || (b.cnt[BC_FLAGS] & (PH_FLAG_LEAF_CAPACITY | PH_FLAG_NODE_CAPACITY))) return;
+    const int T0 = b.cnt[BC_LEVEL_BEGIN], L0 = b.cnt[BC_LEAVES];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int t = blockIdx.x; t < T0; t += gridDim.x) {
+        if (b.tn_mode[t] != MODE_DEFERRED) continue;
+        const int start = b.tn_start[t], len = b.tn_len[t], rd = b.tn_depth[t];
+        for (int k = tid; k < len; k += SUB_TB) {
+            s.x[k] = b.x[start + k];
+            s.y[k] = b.y[start + k];
+            s.z[k] = b.z[start + k];
+            s.perm[k] = b.perm[start + k];
+        }
+        if (tid == 0) {
+            s.nnodes = 1;
+            s.nleaves = 0;
+            s.n_start[0] = 0;
+            s.n_len[0] = (unsigned short)len;
+            s.n_parent[0] = 0xFFFFu;
+            s.lev[0] = 0;
+            s.fail = 0;
+        }
+        __syncthreads();
+        int failed = rd >= levels;
+        int nlev = 0, lbeg = 0, lend = 1;
+        while (lbeg < lend && !failed) {
+            for (int i = lbeg + warp; i < lend; i += SUB_NW) sub_split_node(s, i, rd + nlev, axis0, maxleaf, levels);
+            __syncthreads();
+            lbeg = lend;
+            lend = s.nnodes;
+            failed = s.fail;
+            nlev++;
+            if (tid == 0) s.lev[nlev] = (unsigned short)lbeg;
+            __syncthreads();
+        }
+        if (failed) {
+            if (tid == 0) atomicOr(&b.cnt[BC_FLAGS], PH_FLAG_DEPTH);
+            __syncthreads();
             continue;
         }
-        if (mode != 0) continue;
-        int S = b.tn_S[t];
-        int s0 = (w - b.tn_chunk_base[i]) * CHUNK;
-        int s1 = min(min(len, s0 + CHUNK), S);
-        for (int p = s0 + lane; p < s1; p += 32) {
-            int k = b.bigslot[start + p];
-            if (k >= 0) swap_particles(b, start + p, start + b.smallpos[start + k]);
+        for (int k = tid; k < len; k += SUB_TB) {
+            b.x[start + k] = s.x[k];
+            b.y[start + k] = s.y[k];
+            b.z[start + k] = s.z[k];
+            b.perm[start + k] = s.perm[k];
         }
+        __syncthreads();
+        // numbering arrays over the particle arrays (5 x CHUNK shorts in 3 x CHUNK doubles)
+        unsigned short *sn = reinterpret_cast<unsigned short *>(s.x);
+        unsigned short *sl = sn + CHUNK, *pre = sl + CHUNK, *lb = pre + CHUNK, *lfin = lb + CHUNK;
+        for (int L = nlev - 1; L >= 0; L--) {
+            for (int i = s.lev[L] + tid; i < s.lev[L + 1]; i += SUB_TB) {
+                const int c0 = s.n_c0[i], c1 = s.n_c1[i];
+                sn[i] = (unsigned short)(1 + (c0 >= 0 ? sn[c0] : 0) + (c1 >= 0 ? sn[c1] : 0));
+                sl[i] = (unsigned short)((c0 >= 0 ? sl[c0] : 1) + (c1 >= 0 ? sl[c1] : 1));
+            }
+            __syncthreads();
+        }
+        if (tid == 0) {
+            const int ntot = sn[0], ltot = sl[0];
+            const int nb = atomicAdd(&b.cnt[BC_SUB_NODES], ntot - 1);
+            const int lbg = atomicAdd(&b.cnt[BC_SUB_LEAVES], ltot);
+            s.nbase = T0 + nb;
+            s.lbase = L0 + lbg;
+            if (T0 + nb + ntot - 1 > b.rule_cap) {
+                atomicOr(&b.cnt[BC_FLAGS], PH_FLAG_NODE_CAPACITY);
+                s.fail = 1;
+            }
+            if (L0 + lbg + ltot > b.rule_cap) {
+                atomicOr(&b.cnt[BC_FLAGS], PH_FLAG_LEAF_CAPACITY);
+                s.fail = 1;
+            }
+            b.tn_sub_nodes[t] = ntot;
+            b.tn_sub_leaves[t] = ltot;
+            pre[0] = 0;
+            lb[0] = 0;
+        }
+        __syncthreads();
+        failed = s.fail;
+        __syncthreads();
+        if (failed) continue;
+        for (int L = 0; L < nlev; L++) {
+            for (int i = s.lev[L] + tid; i < s.lev[L + 1]; i += SUB_TB) {
+                const int c0 = s.n_c0[i], c1 = s.n_c1[i];
+                const int P = pre[i], B = lb[i];
+                const int off_n = c0 >= 0 ? sn[c0] : 0, off_l = c0 >= 0 ? sl[c0] : 1;
+                if (c0 >= 0) { pre[c0] = (unsigned short)(P + 1); lb[c0] = (unsigned short)B; }
+                else lfin[~c0] = (unsigned short)B;
+                if (c1 >= 0) { pre[c1] = (unsigned short)(P + 1 + off_n); lb[c1] = (unsigned short)(B + off_l); }
+                else lfin[~c1] = (unsigned short)(B + off_l);
+            }
+            __syncthreads();
+        }
+        const int nbase = s.nbase, lbase = s.lbase, boxid = b.tn_boxid[t];
+        // nodes level by level: a node's box is its parent's, written a level earlier, cut at the parent's split
+        for (int L = 0; L < nlev; L++) {
+            for (int i = s.lev[L] + tid; i < s.lev[L + 1]; i += SUB_TB) {
+                const int ti = i == 0 ? t : nbase + pre[i] - 1;
+                const int c0 = s.n_c0[i], c1 = s.n_c1[i];
+                b.tn_child0[ti] = c0 >= 0 ? nbase + pre[c0] - 1 : ~(lbase + lfin[~c0]);
+                b.tn_child1[ti] = c1 >= 0 ? nbase + pre[c1] - 1 : ~(lbase + lfin[~c1]);
+                b.tn_split[ti] = s.n_split[i];
+                if (i == 0) continue;
+                const int par = s.n_parent[i];
+                const int tp = par == 0 ? t : nbase + pre[par] - 1;
+                b.tn_start[ti] = start + s.n_start[i];
+                b.tn_len[ti] = s.n_len[i];
+                b.tn_depth[ti] = rd + L;
+                b.tn_parent[ti] = tp;
+                b.tn_boxid[ti] = boxid;
+                b.tn_pre[ti] = pre[i];
+                b.tn_subroot[ti] = t;
+                const int Dp = (axis0 + rd + L - 1) % 3;
+                const bool upper = s.n_c0[par] != i;
+                for (int d = 0; d < 3; d++) {
+                    double lo = b.tn_box[d * b.cap_nodes + tp], hi = b.tn_box[(3 + d) * b.cap_nodes + tp];
+                    if (d == Dp) {
+                        if (upper) lo = s.n_split[par];
+                        else hi = s.n_split[par];
+                    }
+                    b.tn_box[d * b.cap_nodes + ti] = lo;
+                    b.tn_box[(3 + d) * b.cap_nodes + ti] = hi;
+                }
+            }
+            __syncthreads();
+        }
+        for (int j = tid; j < s.nleaves; j += SUB_TB) {
+            const int tl = lbase + lfin[j];
+            const int par = s.l_parent[j];
+            const int tp = par == 0 ? t : nbase + pre[par] - 1;
+            const int pd = b.tn_depth[tp];
+            b.tl_start[tl] = start + s.l_start[j];
+            b.tl_len[tl] = s.l_len[j];
+            b.tl_depth[tl] = pd + 1;
+            b.tl_parent[tl] = tp;
+            b.tl_boxid[tl] = boxid;
+            b.tl_final[tl] = lfin[j];
+            b.tl_subroot[tl] = t;
+            const int Dp = (axis0 + pd) % 3;
+            const bool upper = s.n_c0[par] != ~j;
+            for (int d = 0; d < 3; d++) {
+                double lo = b.tn_box[d * b.cap_nodes + tp], hi = b.tn_box[(3 + d) * b.cap_nodes + tp];
+                if (d == Dp) {
+                    if (upper) lo = s.n_split[par];
+                    else hi = s.n_split[par];
+                }
+                b.tl_box[d * b.cap_leaves + tl] = lo;
+                b.tl_box[(3 + d) * b.cap_leaves + tl] = hi;
+            }
+        }
+        __syncthreads();
     }
 }
 
 // ---------------- renumbering ----------------
+// Level nodes bottom-up; a deferred node's counts come from k_subtree_build.
 __global__ void k_subtree_counts(BuildBufs b, int d)
 {
     if (d >= b.cnt[BC_NLEVELS]) return;
     const int lb = b.lvl_begin[d], C = b.lvl_count[d];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
         int t = lb + i;
+        if (b.tn_mode[t] == MODE_DEFERRED) continue;
         int sn = 1, sl = 0;
         int c[2] = {b.tn_child0[t], b.tn_child1[t]};
         for (int k = 0; k < 2; k++) {
@@ -486,13 +788,15 @@ __global__ void k_root_bases(BuildBufs b)
     }
 }
 
-// preorder node numbers and depth-first leaf numbers, src/fmm.c:101-118
+// preorder node numbers and depth-first leaf numbers, src/fmm.c:101-118;
+// a deferred node's subtree is numbered by k_subtree_number
 __global__ void k_number(BuildBufs b, int d)
 {
     if (d >= b.cnt[BC_NLEVELS]) return;
     const int lb = b.lvl_begin[d], C = b.lvl_count[d];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
         int t = lb + i;
+        if (b.tn_mode[t] == MODE_DEFERRED) continue;
         int pre = b.tn_pre[t], lbase = b.tn_lbase[t];
         int c0 = b.tn_child0[t], c1 = b.tn_child1[t];
         int off_nodes, off_leaves;
@@ -501,6 +805,17 @@ __global__ void k_number(BuildBufs b, int d)
         if (PH_IS_LEAF_CODE(c1)) b.tl_final[~c1] = lbase + off_leaves;
         else { b.tn_pre[c1] = pre + 1 + off_nodes; b.tn_lbase[c1] = lbase + off_leaves; }
     }
+}
+
+// subtree nodes and leaves: the subtree root's numbers plus their own
+__global__ void k_subtree_number(BuildBufs b)
+{
+    const int nodes = b.cnt[BC_NODES], leaves = b.cnt[BC_LEAVES];
+    const int t0 = nodes - b.cnt[BC_SUB_NODES], l0 = leaves - b.cnt[BC_SUB_LEAVES];
+    for (int t = t0 + blockIdx.x * blockDim.x + threadIdx.x; t < nodes; t += gridDim.x * blockDim.x)
+        b.tn_pre[t] += b.tn_pre[b.tn_subroot[t]];
+    for (int l = l0 + blockIdx.x * blockDim.x + threadIdx.x; l < leaves; l += gridDim.x * blockDim.x)
+        b.tl_final[l] += b.tn_lbase[b.tl_subroot[l]];
 }
 
 __device__ __forceinline__ void write_geom(TreeBufs &T, int u, const double *box, int cap, int idx)
@@ -551,39 +866,61 @@ __global__ void k_scatter_leaves(BuildBufs b, TreeBufs T)
     }
 }
 
-// depth lists: depth d holds the level-d nodes (temp order) then the leaves
-// created by level d-1 (temp order); offsets by a one-thread prefix
-__global__ void k_depth_offsets(BuildBufs b, TreeBufs T, int ndepth)
+// ---------------- depth lists ----------------
+// A stable counting sort of the unified ids by depth: depth d's list holds
+// its leaves (depth-first order) then its nodes (preorder).  Block k counts
+// the depths of ids [k R, (k+1) R) into cells (depth, block), stored depth
+// by depth; an exclusive scan of the cells gives each block its first slot
+// per depth.
+__global__ void __launch_bounds__(32) k_depth_count(BuildBufs b, TreeBufs T, int ndepth)
 {
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        int off = 0;
-        const int nlev = b.cnt[BC_NLEVELS];
-        int deepest = 0;
-        for (int d = 0; d < ndepth; d++) {
-            T.depth_off[d] = off;
-            const int nc = d < nlev ? b.lvl_count[d] : 0;
-            const int lc = d <= nlev ? b.leaf_count[d] : 0;
-            T.depth_cnt[d] = nc + lc;
-            if (nc + lc) deepest = d;
-            off += nc + lc;
-        }
-        T.depth_off[ndepth] = off;
-        b.cnt[BC_DEPTH] = deepest;
+    __shared__ int h[PH_MAX_DEPTH_CAP + 2];
+    const int nu = b.cnt[BC_NODES] + b.cnt[BC_LEAVES], nblk = gridDim.x, k = blockIdx.x, lane = threadIdx.x;
+    for (int d = lane; d < ndepth; d += 32) h[d] = 0;
+    __syncwarp();
+    const int u0 = k * DEPTH_R, u1 = min(nu, u0 + DEPTH_R);
+    for (int u = u0 + lane; u < u1; u += 32) {
+        const int d = T.depth[u];
+        if (d >= 0 && d < ndepth) atomicAdd(&h[d], 1);
     }
+    __syncwarp();
+    for (int d = lane; d < ndepth; d += 32) T.depth_blk[d * nblk + k] = h[d];
+    if (k == 0 && lane == 0) b.cnt[BC_DEPTH_CELLS] = ndepth * nblk;
 }
 
-__global__ void k_depth_lists(BuildBufs b, TreeBufs T)
+__global__ void __launch_bounds__(32) k_depth_place(BuildBufs b, TreeBufs T, int ndepth)
 {
-    const int d = blockIdx.y;
-    const int nlev = b.cnt[BC_NLEVELS], nleaves = b.cnt[BC_LEAVES];
-    const int node_c = d < nlev ? b.lvl_count[d] : 0;
-    const int node_b = d < nlev ? b.lvl_begin[d] : 0;
-    const int leaf_c = d <= nlev ? b.leaf_count[d] : 0, leaf_b = d <= nlev ? b.leaf_begin[d] : 0;
-    const int off = T.depth_off[d];
-    const int tot = node_c + leaf_c;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += gridDim.x * blockDim.x) {
-        const int u = (i < node_c) ? nleaves + b.tn_pre[node_b + i] : b.tl_final[leaf_b + (i - node_c)];
-        T.depth_list[off + i] = u;
+    __shared__ int cur[PH_MAX_DEPTH_CAP + 2];
+    const int nu = b.cnt[BC_NODES] + b.cnt[BC_LEAVES], nblk = gridDim.x, k = blockIdx.x, lane = threadIdx.x;
+    const unsigned lt = (1u << lane) - 1u;
+    const int *first = T.depth_blk + (size_t)ndepth * nblk;  // the scanned cells
+    for (int d = lane; d < ndepth; d += 32) cur[d] = first[d * nblk + k];
+    if (k == 0) {
+        // per-depth offsets and counts, and the deepest depth holding an id
+        int deepest = 0;
+        for (int d = lane; d < ndepth; d += 32) {
+            const int o = first[d * nblk], e = d + 1 < ndepth ? first[(d + 1) * nblk] : nu;
+            T.depth_off[d] = o;
+            T.depth_cnt[d] = e - o;
+            if (e > o) deepest = d;
+        }
+        deepest = __reduce_max_sync(0xffffffffu, deepest);
+        if (lane == 0) {
+            T.depth_off[ndepth] = nu;
+            b.cnt[BC_DEPTH] = deepest;
+        }
+    }
+    __syncwarp();
+    const int u0 = k * DEPTH_R, u1 = min(nu, u0 + DEPTH_R);
+    for (int base = u0; base < u1; base += 32) {
+        const int u = base + lane;
+        int d = u < u1 ? T.depth[u] : -1;
+        if (d >= ndepth) d = -1;
+        const unsigned same = __match_any_sync(0xffffffffu, d);
+        if (d >= 0) T.depth_list[cur[d] + __popc(same & lt)] = u;
+        __syncwarp();
+        if (d >= 0 && (same & lt) == 0) cur[d] += __popc(same);
+        __syncwarp();
     }
 }
 
@@ -596,23 +933,36 @@ int launch_init_particles(BuildBufs &b, const double *pos, int n, cudaStream_t s
     return 0;
 }
 
-// Enqueue the whole build for at most `levels` node levels; no host sync.
-// Levels past the real depth exit at once.  If nodes remain after the last
-// level, PH_FLAG_DEPTH is raised in b.cnt[BC_FLAGS] (the caller grows
-// `levels` and builds again); capacity overflows raise their flags there too.
-// Depth lists cover depths 0..levels.
-int build_tree(BuildBufs &b, TreeBufs &T, const PassParams &p, int levels, cudaStream_t st)
+int depth_sort_blocks(int cap_u) { return (cap_u + DEPTH_R - 1) / DEPTH_R; }
+
+// Enqueue the whole build, no host sync: at most `top` levels of wide
+// nodes, then the subtrees, with nodes at depths < `levels`.  Levels past
+// the last wide node exit at once.  Wide nodes left after `top` levels
+// raise PH_FLAG_TOP in b.cnt[BC_FLAGS] and a node at depth `levels` raises
+// PH_FLAG_DEPTH (the caller grows the count and builds again); capacity
+// overflows raise their flags there too.  Depth lists cover depths
+// 0..levels.
+int build_tree(BuildBufs &b, TreeBufs &T, const PassParams &p, int levels, int top, cudaStream_t st)
 {
     const int maxb = device_sm_count() * 8;
-    if (levels < 1 || levels + 1 > T.max_depth_cap)
+    if (levels < 1 || levels + 1 > T.max_depth_cap || T.max_depth_cap > PH_MAX_DEPTH_CAP)
         return ph_set_error(7, "tree deeper than %d levels", T.max_depth_cap - 1);
-    PH_CUDA_CHECK(cudaMemsetAsync(b.lvl_count, 0, sizeof(int) * (levels + 1), st));
-    PH_CUDA_CHECK(cudaMemsetAsync(b.leaf_count, 0, sizeof(int) * (levels + 2), st));
+    if (top < 1 || top > levels) top = levels;
+    const int ndepth = levels + 1;  // leaves can sit one level below the deepest nodes
+    const int nblk = T.depth_nblk;
+    if (nblk < 1 || nblk != depth_sort_blocks(T.cap_u)) return ph_set_error(7, "depth-sort buffers not allocated");
+    static bool sub_attr = false;
+    if (!sub_attr) {
+        PH_CUDA_CHECK(cudaFuncSetAttribute(k_subtree_build, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)sizeof(SubTree)));
+        sub_attr = true;
+    }
+    PH_CUDA_CHECK(cudaMemsetAsync(b.lvl_count, 0, sizeof(int) * (top + 2), st));
+    PH_CUDA_CHECK(cudaMemsetAsync(b.leaf_count, 0, sizeof(int) * (top + 2), st));
     ph::note_launch(), k_init_roots<<<(b.nbox + TB - 1) / TB, TB, 0, st>>>(b);
-    for (int d = 0; d < levels; d++) {
+    for (int d = 0; d < top; d++) {
         const int D = (p.axis0 + d) % 3;  // from direct_local_start; the axis cycles (src/fmm.c:99)
         ph::note_launch(), k_level_nch<<<maxb, TB, 0, st>>>(b);
-        ph::note_launch(), k_narrow_split<<<maxb, TB, 0, st>>>(b, D, p.maxleaf);
         scan_exclusive_i32(b.tn_nch, b.tn_chunk_base, b.cnt + BC_LEVEL_COUNT, b.cap_nodes, b.cnt + BC_W,
                            b.scan_scratch, b.scan_scratch_elems, st);
         ph::note_launch(), k_chunk_map<<<maxb, TB, 0, st>>>(b);
@@ -627,18 +977,22 @@ int build_tree(BuildBufs &b, TreeBufs &T, const PassParams &p, int levels, cudaS
         ph::note_launch(), k_make_children<<<maxb, TB, 0, st>>>(b, p.maxleaf, D);
         ph::note_launch(), k_rank<<<maxb, TB, 0, st>>>(b, D);
         ph::note_launch(), k_swap<<<maxb, TB, 0, st>>>(b, D);
-        ph::note_launch(), k_level_finish<<<1, 1, 0, st>>>(b, d);
+        ph::note_launch(), k_level_finish<<<1, 1, 0, st>>>(b, d, top);
     }
+    ph::note_launch(), k_subtree_build<<<device_sm_count() * 3, SUB_TB, sizeof(SubTree), st>>>(b, p.axis0, p.maxleaf,
+                                                                                                levels);
     ph::note_launch(), k_tree_totals<<<1, 1, 0, st>>>(b);
-    // subtree sizes bottom-up, numbers top-down
-    for (int d = levels - 1; d >= 0; d--) ph::note_launch(), k_subtree_counts<<<maxb, TB, 0, st>>>(b, d);
+    // subtree sizes bottom-up, numbers top-down, over the recorded levels (top + 1 at most)
+    for (int d = top; d >= 0; d--) ph::note_launch(), k_subtree_counts<<<maxb, TB, 0, st>>>(b, d);
     ph::note_launch(), k_root_bases<<<1, 1, 0, st>>>(b);
-    for (int d = 0; d < levels; d++) ph::note_launch(), k_number<<<maxb, TB, 0, st>>>(b, d);
+    for (int d = 0; d <= top; d++) ph::note_launch(), k_number<<<maxb, TB, 0, st>>>(b, d);
+    ph::note_launch(), k_subtree_number<<<maxb, TB, 0, st>>>(b);
     ph::note_launch(), k_scatter_nodes<<<maxb, TB, 0, st>>>(b, T);
     ph::note_launch(), k_scatter_leaves<<<maxb, TB, 0, st>>>(b, T);
-    const int ndepth = levels + 1;  // leaves can sit one level below the deepest nodes
-    ph::note_launch(), k_depth_offsets<<<1, 1, 0, st>>>(b, T, ndepth);
-    ph::note_launch(), k_depth_lists<<<dim3(64, ndepth), TB, 0, st>>>(b, T);
+    ph::note_launch(), k_depth_count<<<nblk, 32, 0, st>>>(b, T, ndepth);
+    scan_exclusive_i32(T.depth_blk, T.depth_blk + (size_t)ndepth * nblk, b.cnt + BC_DEPTH_CELLS, ndepth * nblk,
+                       b.cnt + BC_DEPTH_TOTAL, b.scan_scratch, b.scan_scratch_elems, st);
+    ph::note_launch(), k_depth_place<<<nblk, 32, 0, st>>>(b, T, ndepth);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }
