@@ -302,15 +302,18 @@ static int p2p_variant()
     return 2;
 }
 
+// floats per reaction value: an FP64 pass keeps doubles in the float buffer
+static long long mu_per_value(int precision) { return precision == PHOTONS_FP64 ? 2 : 1; }
+
 // the reaction buffer of the mutual kernel (floats); grown from the last
 // pass's need, which the device reports when it did not fit
 // A reaction buffer that was too small made the pass evaluate every pair
 // one way (correct, but not the mutual kernel's rounding); size it and
 // report that the pass should be repeated, so results never depend on
 // whether an earlier pass had already grown the buffer.
-static bool mutual_feedback(photons_ctx *c, int over, long long need)
+static bool mutual_feedback(photons_ctx *c, int over, long long need, int precision)
 {
-    if (!over || need <= c->mu_buf_cap) return false;
+    if (!over || need <= c->mu_buf_cap / mu_per_value(precision)) return false;
     c->hint_mubuf = need + need / 16 + 4096;
     return true;
 }
@@ -325,10 +328,14 @@ static bool mutual_feedback(photons_ctx *c, int over, long long need)
 #ifndef MU_MIN_LEAF
 #define MU_MIN_LEAF 48
 #endif
+// FP64 passes use mutual pairs at every leaf size: the pair force is ~70
+// FP64 operations, so evaluating each symmetric pair once halves the pass
+// whatever the pairing costs.
 static bool uses_mutual(const photons_ctx *c, int precision)
 {
-    return precision != PHOTONS_FP64 && p2p_variant() == 2 && c->pp.maxleaf >= MU_MIN_LEAF &&
-           c->pp.maxleaf <= 64 && !c->mu_off && !(c->pass_flags & PHOTONS_F_ONE_WAY);
+    if (c->mu_off || (c->pass_flags & PHOTONS_F_ONE_WAY)) return false;
+    if (precision == PHOTONS_FP64) return true;
+    return p2p_variant() == 2 && c->pp.maxleaf >= MU_MIN_LEAF && c->pp.maxleaf <= 64;
 }
 
 // buffers of the mutual kernel, only for passes that run it: per-entry
@@ -339,7 +346,7 @@ static int alloc_mutual(photons_ctx *c, int precision)
     // first guess: about half of a leaf's ~110-250 list entries received, 3
     // floats per particle and entry (256^3 leaf 64 needs ~180 per particle);
     // a pass that needs more repeats once with the measured size
-    long long want = c->hint_mubuf ? c->hint_mubuf : (long long)c->n * 192 + 4096;
+    long long want = (c->hint_mubuf ? c->hint_mubuf : (long long)c->n * 192 + 4096) * mu_per_value(precision);
     // the reaction slots take ~700 bytes per particle: where they would not
     // leave 1 GB of the device free, this context evaluates every pair one way
     size_t grow = 0, free_b = 0, total_b = 0;
@@ -744,8 +751,8 @@ int ph_stage_p2p(photons_ctx *c, int precision, int zero)
         m.sorted = c->mu_sorted; m.nrecv = c->mu_nrecv; m.size = c->mu_size; m.rbase = c->mu_rbase;
         m.total = c->mu_total; m.scan_scratch = c->mu_scan; m.slot = c->mu_slot; m.over = c->mu_over;
         m.ev = c->mu_ev; m.nev = c->mu_nev; m.maxleaf = c->pp.maxleaf; m.pq = c->mu_pq;
-        m.buf = c->mu_buf; m.buf_cap = c->mu_buf_cap; m.cap_leaves = c->mu_cap_leaves;
-        PH_TRY(ph::launch_p2p_mutual(a, m, st));
+        m.buf = c->mu_buf; m.buf_cap = c->mu_buf_cap / mu_per_value(precision); m.cap_leaves = c->mu_cap_leaves;
+        PH_TRY(ph::launch_p2p_mutual(a, m, precision == PHOTONS_FP64, st));
     } else {
         if (a.variant == 2) a.variant = 0;
         PH_TRY(ph::launch_p2p(a, precision == PHOTONS_FP64, st));
@@ -949,7 +956,7 @@ static int force_pass_graph(photons_ctx *c, int nbox, const photons_params *p, c
             continue;
         }
         // the reaction total means something only once tree and lists are complete
-        if (mutual_feedback(c, mu_over, mu_need)) continue;
+        if (mutual_feedback(c, mu_over, mu_need, p->precision)) continue;
         c->info.depth_off.resize(c->info.depth + 2);
         c->have_lists = true;
         c->mask = mask;
@@ -1045,7 +1052,7 @@ static int force_pass_boxes(photons_ctx *c, int nbox, const photons_params *p, c
             int mu_over = 0;
             PH_CUDA_CHECK(cudaMemcpy(&mu_need, c->mu_total, sizeof mu_need, cudaMemcpyDeviceToHost));
             PH_CUDA_CHECK(cudaMemcpy(&mu_over, c->mu_over, sizeof mu_over, cudaMemcpyDeviceToHost));
-            if (!mutual_feedback(c, mu_over, mu_need)) break;
+            if (!mutual_feedback(c, mu_over, mu_need, p->precision)) break;
         }
     }
     c->last_flags = p->flags;

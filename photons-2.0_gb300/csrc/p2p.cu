@@ -578,6 +578,32 @@ __global__ void __launch_bounds__(P2P_TB, P2P_MINB) k_p2p_split_packed(P2PArgs A
 // ---------------------------------------------------------------------
 // FP64 kernel: the reference's arithmetic
 // ---------------------------------------------------------------------
+// m g(u) / max(r, eps)^3 for a source dx away.  Fast form (the default):
+// the same quantities with fewer FP64 operations (GB300's FP64 rate is 1/64
+// of FP32): 1/r from rsqrt, and erfc(u) + c u exp(-u^2) as exp(-u^2)
+// (erfcx(u) + c u), one exponential; two coincident particles get the
+// softened factor (r = 0 < eps) as in the reference.
+__device__ __forceinline__ double pair_ir3_fp64(double dx, double dy, double dz, double eps, double soft3,
+                                                double mass, double rs, double hrs, double coeff)
+{
+#if P2P_FP64_FAST
+    (void)rs;
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    const double rinv = r2 > 0.0 ? rsqrt(r2) : 0.0;
+    const double dr = r2 * rinv;
+    double ir3 = (dr < eps) ? soft3 : mass * (rinv * rinv * rinv);
+    const double drs = dr * hrs;
+    ir3 *= exp(-drs * drs) * (erfcx(drs) + coeff * drs);
+#else
+    (void)hrs;
+    double dr = sqrt(dx * dx + dy * dy + dz * dz);
+    double ir3 = (dr < eps) ? soft3 : mass / (dr * dr * dr);
+    double drs = 0.5 * dr / rs;
+    ir3 *= (erfc(drs) + coeff * drs * exp(-drs * drs));
+#endif
+    return ir3;
+}
+
 struct Src64 {
     double x, y, z;
     int idx;
@@ -652,22 +678,7 @@ __global__ void __launch_bounds__(P2P_TB) k_p2p_fp64(P2PArgs A)
                         Src64 sj = src[j];
                         if (sj.idx == ip) continue;
                         double dx = sj.x - px, dy = sj.y - py, dz = sj.z - pz;
-#if P2P_FP64_FAST
-                        // the same quantities with fewer FP64 operations (GB300's FP64
-                        // rate is 1/64 of FP32): 1/r from rsqrt, and erfc(u) + c u
-                        // exp(-u^2) as exp(-u^2) (erfcx(u) + c u), one exponential
-                        const double r2 = dx * dx + dy * dy + dz * dz;
-                        const double rinv = rsqrt(r2);
-                        const double dr = r2 * rinv;
-                        double ir3 = (dr < eps) ? soft3 : mass * (rinv * rinv * rinv);
-                        const double drs = dr * hrs;
-                        ir3 *= exp(-drs * drs) * (erfcx(drs) + coeff * drs);
-#else
-                        double dr = sqrt(dx * dx + dy * dy + dz * dz);
-                        double ir3 = (dr < eps) ? soft3 : mass / (dr * dr * dr);
-                        double drs = 0.5 * dr / rs;
-                        ir3 *= (erfc(drs) + coeff * drs * exp(-drs * drs));
-#endif
+                        const double ir3 = pair_ir3_fp64(dx, dy, dz, eps, soft3, mass, rs, hrs, coeff);
                         ax += dx * ir3;
                         ay += dy * ir3;
                         az += dz * ir3;
@@ -814,6 +825,10 @@ __device__ __forceinline__ int mu_find(const uint32_t *lst, int L, uint32_t v)
 // floats per component row of a reaction slot: n rounded up to 32, so that
 // every row starts on a 128-byte line
 __host__ __device__ __forceinline__ int mu_row(int n) { return (n + 31) & ~31; }
+// the same at granularity g (a power of two): FP64 slots pad rows to 4
+// doubles, so that leaves of a few particles do not take rows of 32
+__host__ __device__ __forceinline__ int mu_row_g(int n, int g) { return (n + g - 1) & ~(g - 1); }
+#define MU64_ROW 4
 
 // the image with the opposite shift (the partner of an image entry)
 __device__ __forceinline__ int img_neg(int img)
@@ -832,7 +847,7 @@ __device__ __forceinline__ int img_neg(int img)
 // the received rank, or the partner's position in b's list.
 __global__ void k_mu_pair(const int *tree_cnt, const unsigned long long *walk_flags, const uint32_t *pool,
                           const long long *off, const int *cnt, const int *npart, const int *sorted, int *slot,
-                          int *pq, int *nrecv, long long *size)
+                          int *pq, int *nrecv, long long *size, int rowg)
 {
     const int lane = warp_lane();
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
@@ -868,7 +883,7 @@ __global__ void k_mu_pair(const int *tree_cnt, const unsigned long long *walk_fl
         }
         if (lane == 0) {
             nrecv[t] = recv;
-            size[t] = (long long)recv * mu_row(npart[t]) * 3;
+            size[t] = (long long)recv * mu_row_g(npart[t], rowg) * 3;
         }
     }
 }
@@ -1288,6 +1303,157 @@ __global__ void __launch_bounds__(256, 3) k_mu_gather(P2PArgs A, const int *slot
     }
 }
 
+// ---------------------------------------------------------------------
+// FP64 P2P with mutual pairs: the pairing of the FP32 kernel (each
+// symmetric leaf pair, local or image, evaluated once by its owner) with
+// the FP64 pass's pair force.  One warp per target leaf.  Lanes are 8
+// target groups x 4 source groups (lane = 4 tg + sg): target q belongs to
+// group q mod 8, a lane holds up to T = 8 of them (64 per chunk; larger
+// leaves run in chunks of 64), and takes sources sg, sg + 4, ... of each
+// entry, staged with the image shift in shared memory.  For an owned entry
+// the reaction on a source is summed over the 8 target groups (butterfly,
+// lane tg = 0's sum kept) and stored in the pair's slot (x, y, z rows of
+// r = n rounded up to 4 doubles; a second chunk adds to it).  Target sums
+// are combined over the 4 source groups at the end.  k_mu_gather64 adds
+// each leaf's received slots in list order.
+// ---------------------------------------------------------------------
+#define MU64_TB 256
+#define MU64_WARPS (MU64_TB / 32)
+
+template <int T>
+__device__ __forceinline__ void mu64_chunk(const P2PArgs &A, const int2 *ev, int ne, const long long *rbase,
+                                           double *rbuf, int t, int it, int q0, int nq, double *stage, int lane)
+{
+    const int tg = lane >> 2, sg = lane & 3;
+    const BoxParams &B = A.boxes[A.boxid[t]];
+    const double eps = B.eps, mass = B.mass, rs = B.rs, boxL = B.boxsize;
+    const double soft3 = mass / (eps * eps * eps), hrs = 0.5 / rs, coeff = 2.0 / sqrt(M_PI);
+    double px[T], py[T], pz[T], ax[T], ay[T], az[T];
+#pragma unroll
+    for (int k = 0; k < T; k++) {
+        const int q = 8 * k + tg;
+        px[k] = py[k] = pz[k] = 0.0;
+        if (q < nq) { px[k] = A.px[it + q0 + q]; py[k] = A.py[it + q0 + q]; pz[k] = A.pz[it + q0 + q]; }
+        ax[k] = ay[k] = az[k] = 0.0;
+    }
+    for (int e = 0; e < ne; e++) {
+        const int2 en = ev[e];
+        const int s = PH_ENTRY_ID((uint32_t)en.x), img = PH_ENTRY_IMG((uint32_t)en.x);
+        const int is = A.ipart[s], ns = A.npart[s];
+        double h0 = 0.0, h1 = 0.0, h2 = 0.0;
+        if (img) leaf_shift(img, boxL, h0, h1, h2);
+        __syncwarp();
+        for (int j = lane; j < ns; j += 32) {
+            stage[3 * j] = A.px[is + j] + h0;
+            stage[3 * j + 1] = A.py[is + j] + h1;
+            stage[3 * j + 2] = A.pz[is + j] + h2;
+        }
+        __syncwarp();
+        const bool self = img == 0 && s == t;
+        const bool owned = en.y >= 0;
+        const int row = mu_row_g(ns, MU64_ROW);
+        double *out = owned ? rbuf + rbase[s] + (long long)en.y * 3 * row : nullptr;
+        for (int j0 = 0; j0 < ns; j0 += 4) {
+            const int j = j0 + sg;
+            double rx = 0.0, ry = 0.0, rz = 0.0;
+            if (j < ns) {
+                const double sx = stage[3 * j], sy = stage[3 * j + 1], sz = stage[3 * j + 2];
+#pragma unroll
+                for (int k = 0; k < T; k++) {
+                    const int q = 8 * k + tg;
+                    if (q < nq && !(self && q0 + q == j)) {
+                        const double dx = sx - px[k], dy = sy - py[k], dz = sz - pz[k];
+                        const double ir3 = pair_ir3_fp64(dx, dy, dz, eps, soft3, mass, rs, hrs, coeff);
+                        const double fx = dx * ir3, fy = dy * ir3, fz = dz * ir3;
+                        ax[k] += fx; ay[k] += fy; az[k] += fz;
+                        rx -= fx; ry -= fy; rz -= fz;
+                    }
+                }
+            }
+            if (owned) {
+#pragma unroll
+                for (int o = 4; o < 32; o <<= 1) {
+                    rx += __shfl_xor_sync(0xffffffffu, rx, o);
+                    ry += __shfl_xor_sync(0xffffffffu, ry, o);
+                    rz += __shfl_xor_sync(0xffffffffu, rz, o);
+                }
+                if (tg == 0 && j < ns) {
+                    if (q0 == 0) { out[j] = rx; out[row + j] = ry; out[2 * row + j] = rz; }
+                    else { out[j] += rx; out[row + j] += ry; out[2 * row + j] += rz; }
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < T; k++) {
+#pragma unroll
+        for (int o = 1; o < 4; o <<= 1) {
+            ax[k] += __shfl_xor_sync(0xffffffffu, ax[k], o);
+            ay[k] += __shfl_xor_sync(0xffffffffu, ay[k], o);
+            az[k] += __shfl_xor_sync(0xffffffffu, az[k], o);
+        }
+        const int q = 8 * k + tg;
+        if (sg == 0 && q < nq) {
+            A.ax[it + q0 + q] += ax[k];
+            A.ay[it + q0 + q] += ay[k];
+            A.az[it + q0 + q] += az[k];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(MU64_TB, 1) k_p2p_mutual64(P2PArgs A, const int2 *ev, const int *nev,
+                                                            const long long *rbase, double *rbuf)
+{
+    __shared__ double s_stage[MU64_WARPS][3 * PH_MAX_LEAF];
+    const int lane = warp_lane(), wib = threadIdx.x >> 5;
+    const int nleaf = p2p_targets(A);
+    for (;;) {
+        int t;
+        if (lane == 0) t = atomicAdd(A.work_counter, 1);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= nleaf) break;
+        const int nt = A.npart[t], it = A.ipart[t];
+        const int ne = nev[t];
+        const int2 *evt = ev + A.p2p_off[t];
+        for (int q0 = 0; q0 < nt; q0 += 64) {
+            const int nq = min(64, nt - q0);
+            if (nq > 32) mu64_chunk<8>(A, evt, ne, rbase, rbuf, t, it, q0, nq, s_stage[wib], lane);
+            else if (nq > 16) mu64_chunk<4>(A, evt, ne, rbase, rbuf, t, it, q0, nq, s_stage[wib], lane);
+            else mu64_chunk<2>(A, evt, ne, rbase, rbuf, t, it, q0, nq, s_stage[wib], lane);
+        }
+    }
+}
+
+// each leaf adds the FP64 reactions its owners left in its slots, the
+// received entries in list order (received entry k at rbase + 3 k r).
+// With the reaction buffer too small (over) every entry ran one way and no
+// slot holds anything.
+__global__ void k_mu_gather64(P2PArgs A, const int *over, const int *nrecv, const long long *rbase,
+                              const double *rbuf)
+{
+    const int lane = warp_lane();
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    const int nleaf = *over ? 0 : p2p_targets(A);
+    for (int t = gw; t < nleaf; t += nw) {
+        const int nt = A.npart[t], it = A.ipart[t], nr = nrecv[t];
+        if (nr == 0 || nt == 0) continue;
+        const int rl = mu_row_g(nt, MU64_ROW);
+        const double *base = rbuf + rbase[t];
+        for (int j = lane; j < nt; j += 32) {
+            double v0 = 0.0, v1 = 0.0, v2 = 0.0;
+            for (int k = 0; k < nr; k++) {
+                const double *src = base + (long long)k * 3 * rl + j;
+                v0 += src[0];
+                v1 += src[rl];
+                v2 += src[2 * rl];
+            }
+            A.ax[it + j] += v0;
+            A.ay[it + j] += v1;
+            A.az[it + j] += v2;
+        }
+    }
+}
+
 // One leaf pair in FP64, the entry points of inc/kernels.h: forces on the
 // nt targets at tpos (particle indices tfirst..) from the ns sources at spos
 // (indices sfirst..), a source skipped where its index is the target's (a
@@ -1314,7 +1480,7 @@ __global__ void k_leaf_pair_fp64(const double *tpos, int nt, int tfirst, const d
             ir3 *= (erfc(drs) + coeff * drs * exp(-drs * drs));
         } else {
             const double r2 = dx * dx + dy * dy + dz * dz;
-            const double rinv = rsqrt(r2);
+            const double rinv = r2 > 0.0 ? rsqrt(r2) : 0.0;
             const double dr = r2 * rinv;
             ir3 = (dr < eps) ? soft3 : mass * (rinv * rinv * rinv);
             const double drs = dr * hrs;
@@ -1368,17 +1534,27 @@ int launch_leaf_offsets(const BuildBufs &b, const TreeBufs &t, float4 *pos4, cud
     return 0;
 }
 
-int launch_p2p_mutual(const P2PArgs &a, const MutualBufs &m, cudaStream_t st)
+int launch_p2p_mutual(const P2PArgs &a, const MutualBufs &m, int fp64, cudaStream_t st)
 {
     PH_CUDA_CHECK(cudaMemsetAsync(a.work_counter, 0, sizeof(int), st));
     const int sms = device_sm_count();
     ph::note_launch(), k_mu_sort<<<sms * 4, 256, 0, st>>>(a.tree_cnt, a.walk_flags, m.pool, a.p2p_off, a.p2p_cnt,
                                                            m.sorted);
     ph::note_launch(), k_mu_pair<<<sms * 8, 256, 0, st>>>(a.tree_cnt, a.walk_flags, m.pool, a.p2p_off, a.p2p_cnt,
-                                                           a.npart, m.sorted, m.slot, m.pq, m.nrecv, m.size);
+                                                           a.npart, m.sorted, m.slot, m.pq, m.nrecv, m.size,
+                                                           fp64 ? MU64_ROW : 32);
     scan_exclusive_i64(m.size, m.rbase, a.tree_cnt + BC_LEAVES, m.cap_leaves, m.total, m.scan_scratch, st);
     ph::note_launch(), k_mu_slots<<<sms * 8, 256, 0, st>>>(a.tree_cnt, a.walk_flags, m.pool, a.p2p_off, a.p2p_cnt,
                                                             m.total, m.buf_cap, m.pq, m.slot, m.ev, m.nev, m.over);
+    if (fp64) {
+        double *rbuf = reinterpret_cast<double *>(m.buf);
+        // one block of 8 warps per SM (194 registers): the FP64 pipe, at 1/64
+        // of the FP32 rate, is saturated by far fewer warps than that
+        ph::note_launch(), k_p2p_mutual64<<<sms, MU64_TB, 0, st>>>(a, m.ev, m.nev, m.rbase, rbuf);
+        ph::note_launch(), k_mu_gather64<<<sms * 4, 256, 0, st>>>(a, m.over, m.nrecv, m.rbase, rbuf);
+        PH_CUDA_CHECK(cudaGetLastError());
+        return 0;
+    }
     // the build: shape 0 picks by MAXLEAF (three blocks per SM with two
     // chains from leaf 60, else four blocks with one chain and the 6-target
     // path); 1-4 name a build for the autotuner (PHOTONS_F_P2P_SHAPE)

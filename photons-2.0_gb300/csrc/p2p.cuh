@@ -41,7 +41,7 @@ struct P2PArgs {
     int shape;    // mutual kernel build (0: by MAXLEAF; see launch_p2p_mutual)
 };
 
-// buffers of the mutual FP32 kernel (see launch_p2p_mutual)
+// buffers of the mutual kernels, FP32 and FP64 (see launch_p2p_mutual)
 struct MutualBufs {
     uint32_t *pool;          // the P2P pool, each target's list sorted in place
     int *sorted, *nrecv;     // per leaf: list sorted; received (lower-id) entries
@@ -50,8 +50,8 @@ struct MutualBufs {
     long long *scan_scratch;
     int *slot;               // per pool entry: owner rank, -2 received, -1 one way
     int *over;               // device: 1 if the reaction buffer was too small (all one way)
-    float *buf;              // reactions
-    long long buf_cap;       // floats
+    float *buf;              // reactions (FP64 passes: doubles over the same bytes)
+    long long buf_cap;       // reaction values that fit (floats, or doubles in an FP64 pass)
     int cap_leaves;
     int2 *ev;                // per pool offset: the entries a target evaluates, packed in list order
     int *nev;                // per leaf: their number
@@ -62,7 +62,7 @@ struct MutualBufs {
 SplitConsts make_split_consts(const PassParams &p);
 // FP32 P2P with mutual pairs (MAXLEAF <= 64; chosen for 48-64): sorts the
 // lists, pairs the entries, evaluates, adds the received reactions
-int launch_p2p_mutual(const P2PArgs &a, const MutualBufs &m, cudaStream_t st);
+int launch_p2p_mutual(const P2PArgs &a, const MutualBufs &m, int fp64, cudaStream_t st);
 double split_sig(const PassParams &p);
 int launch_leaf_offsets(const BuildBufs &b, const TreeBufs &t, float4 *pos4, cudaStream_t st);
 int launch_p2p(const P2PArgs &a, int fp64, cudaStream_t st);

@@ -286,6 +286,22 @@ def test_fp32_split_precision_clustered(ph, fp, ics, nside, maxleaf):
     assert np.percentile(e, 99) <= 2e-5, np.percentile(e, 99)
 
 
+@pytest.mark.parametrize("workload,nside,maxleaf", [("zeldovich256", 32, 64), ("nfw128", 32, 16),
+                                                    ("nfw128", 24, 100), ("grid32", 16, 8)])
+def test_fp64_mutual_matches_one_way(ph, ics, workload, nside, maxleaf):
+    """FP64 passes evaluate each symmetric leaf pair (local or periodic
+    image) once, reactions through the slot buffer: the same forces as the
+    one-way FP64 kernel to FP64 rounding, deterministic from pass to pass.
+    Leaf 100 runs targets in two chunks of up to 64."""
+    pos, p = ics.make(workload, nside=nside, maxleaf=maxleaf)
+    fp = ph.ForcePass(0)
+    mutual = fp.run(pos, p, precision=ph.FP64)
+    again = fp.run(pos, p, precision=ph.FP64)
+    one_way = ph.ForcePass(0).run(pos, p, precision=ph.FP64, flags=ph.F_ONE_WAY)
+    assert np.array_equal(mutual, again)
+    assert rel_err(mutual, one_way, p).max() <= 1e-12
+
+
 def _full_size_parity(ph, fp, port, pos, p, precision, tol, nsub=10000):
     """The GPU pass against the oracle at a workload's full size: counters,
     the tree-order permutation, every list as a multiset, and the forces on
