@@ -66,7 +66,9 @@ void fmm_remote(int idx, double shift[3]);
    fmm_prepare), added to part[].acc as src/fmm.c:823-868 adds a task.  The
    reference declares these but never defines them.  p2p_kernel evaluates
    the pair force as src/fmm.c:834-852 writes it; p2p_kernel_rinvsqrt the
-   same force with 1/r from the reciprocal square root and one exponential;
+   same force with 1/r from the reciprocal square root and the split
+   factor erfc(u) + (2/sqrt(pi)) u exp(-u^2) from piecewise polynomials
+   (within 2.8e-17 of it), the FP64 pass's form;
    p2p_kernel_inleaf a leaf with itself (jnode == inode), self pairs skipped. */
 void p2p_kernel(int inode, int jnode);
 void p2p_kernel_rinvsqrt(int inode, int jnode);
@@ -350,6 +352,11 @@ double photons_fp32_fma_peak(int iters);
 double photons_fp32x2_fma_peak(int iters);
 /* the FP64 one (DFMA chains), the denominator of the FP64 pass's roofline */
 double photons_fp64_fma_peak(int iters);
+/* the FP64 kernels' split factor erfc(u) + (2/sqrt(pi)) u exp(-u^2) at n
+   host points u >= 0, evaluated on the device: their piecewise polynomials,
+   or with exact != 0 erfc and exp as src/fmm.c:846-848 writes them (a check
+   of the polynomials); 0 or an error code */
+int photons_split_factor_fp64(const double *u, int n, int exact, double *g);
 
 #ifdef __cplusplus
 }

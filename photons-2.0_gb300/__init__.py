@@ -114,6 +114,7 @@ def load_library():
     lib.photons_fp32_fma_peak.argtypes = [C.c_int]
     lib.photons_fp64_fma_peak.restype = C.c_double
     lib.photons_fp64_fma_peak.argtypes = [C.c_int]
+    lib.photons_split_factor_fp64.argtypes = [_dp, C.c_int, C.c_int, _dp]
     lib.photons_gpu_error.restype = C.c_char_p
     lib.photons_gpu_status.restype = C.c_int
     for name in ("fmm_construct", "fmm_prepare", "fmm_task", "fmm_ext", "fmm_deconstruct", "build_localtree",
@@ -492,6 +493,16 @@ def fp64_fma_peak(iters=256):
     if v <= 0:
         raise PhotonsError("FP64 FMA probe failed: " + lib.photons_gpu_error().decode(errors="replace"))
     return v
+
+
+def split_factor_fp64(u, exact=False):
+    """The FP64 kernels' split factor erfc(u) + (2/sqrt(pi)) u exp(-u^2) at
+    the points u >= 0, on the device: their piecewise polynomials, or with
+    exact=True erfc and exp."""
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    g = np.empty_like(u)
+    _check(load_library().photons_split_factor_fp64(_p(u, _dp), int(u.size), int(bool(exact)), _p(g, _dp)))
+    return g
 
 
 def fp32_fma_peak(iters=4096):

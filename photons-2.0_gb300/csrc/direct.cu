@@ -266,3 +266,24 @@ extern "C" double photons_fp32x2_fma_peak(int iters)
     if (iters < 1) iters = 4096;
     return fma_probe(iters, true);
 }
+
+// the FP64 pair factor's split term erfc(u) + (2/sqrt(pi)) u exp(-u^2) at n
+// host points: the piecewise polynomials of the FP64 kernels, or (exact)
+// erfc and exp as src/fmm.c:846-848 writes them
+extern "C" int photons_split_factor_fp64(const double *u, int n, int exact, double *g)
+{
+    photons_gpu_clear_error();
+    if (n < 0 || (n > 0 && (!u || !g))) return ph_set_error(PH_ERR_ARG, "bad split-factor arguments");
+    if (n == 0) return 0;
+    double *d = nullptr;
+    PH_CUDA_CHECK(cudaMalloc(&d, sizeof(double) * 2 * (size_t)n));
+    int rc = 0;
+    cudaError_t e = cudaMemcpy(d, u, sizeof(double) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        rc = ph::launch_split_factor_fp64(d, n, exact, d + n, 0);
+        if (!rc) e = cudaMemcpy(g, d + n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    }
+    if (!rc && e != cudaSuccess) rc = ph_set_cuda_error(e, "split factor", __FILE__, __LINE__);
+    cudaFree(d);
+    return rc;
+}

@@ -298,7 +298,8 @@ extern "C" void fmm_remote(int idx, double shift[3])
 //   p2p_kernel           the pair force as src/fmm.c:834-852 writes it
 //                        (sqrt, division, erfc, exp)
 //   p2p_kernel_rinvsqrt  the same force with 1/r from the reciprocal
-//                        square root and one exponential (the FP64 pass's form)
+//                        square root and the split factor from piecewise
+//                        polynomials (the FP64 pass's form)
 //   p2p_kernel_inleaf    a leaf with itself (jnode must equal inode), self
 //                        pairs skipped
 // ------------------------------------------------------------------

@@ -23,14 +23,16 @@
 // FP64 variant: the reference's pair force in FP64 on absolute positions,
 // image positions formed as pos + shift like the exported bodies of
 // src/remotes.c:83-89, self pair skipped by index.  1/r comes from rsqrt and
-// erfc(u) + (2/sqrt(pi)) u exp(-u^2) from exp(-u^2) (erfcx(u) + ...), one
-// exponential, which is fewer FP64 operations than the reference's sqrt,
-// division, erfc and exp and agrees with them to ~1e-15 relative.
+// g(u) = erfc(u) + (2/sqrt(pi)) u exp(-u^2) from piecewise polynomials
+// (fit_split_fp64.py, within 2.8e-17 of g), which is fewer FP64 operations
+// than the reference's sqrt, division, erfc and exp and agrees with them to
+// a few ulp of the force.
 #include <cmath>
 
 #include "fmm_context.cuh"
 #include "p2p.cuh"
 #include "split_kernel_coeffs.h"
+#include "split_fp64_table.h"
 
 #define P2P_TB 256
 #define P2P_WARPS (P2P_TB / 32)
@@ -578,13 +580,40 @@ __global__ void __launch_bounds__(P2P_TB, P2P_MINB) k_p2p_split_packed(P2PArgs A
 // ---------------------------------------------------------------------
 // FP64 kernel: the reference's arithmetic
 // ---------------------------------------------------------------------
+// g(u) = erfc(u) + (2/sqrt(pi)) u exp(-u^2) (src/fmm.c:846-848) in FP64:
+// piecewise polynomials of degree 12 on intervals of 1/4 (coefficients by
+// fit_split_fp64.py, within 2.8e-17 of g on [0, 8)), erfc and exp beyond.
+// tab: the coefficients k-major, [k][interval], in shared or global memory.
+__device__ const double g_split64[SPLIT64_DEG + 1][SPLIT64_NI] = SPLIT64_C_INIT;
+#define SPLIT64_N ((SPLIT64_DEG + 1) * SPLIT64_NI)
+
+__device__ __forceinline__ double split_g_fp64(double u, const double *tab, double coeff)
+{
+    if (u < SPLIT64_NI * SPLIT64_W) {
+        const int i = (int)(u * SPLIT64_INVW);
+        const double d = u - ((double)i + 0.5) * SPLIT64_W;
+        double acc = tab[SPLIT64_DEG * SPLIT64_NI + i];
+#pragma unroll
+        for (int k = SPLIT64_DEG - 1; k >= 0; k--) acc = fma(acc, d, tab[k * SPLIT64_NI + i]);
+        return acc;
+    }
+    return erfc(u) + coeff * u * exp(-u * u);
+}
+
+// a block's copy of the coefficients in shared memory
+__device__ __forceinline__ void load_split64(double *s_tab)
+{
+    for (int i = threadIdx.x; i < SPLIT64_N; i += blockDim.x) s_tab[i] = (&g_split64[0][0])[i];
+    __syncthreads();
+}
+
 // m g(u) / max(r, eps)^3 for a source dx away.  Fast form (the default):
 // the same quantities with fewer FP64 operations (GB300's FP64 rate is 1/64
-// of FP32): 1/r from rsqrt, and erfc(u) + c u exp(-u^2) as exp(-u^2)
-// (erfcx(u) + c u), one exponential; two coincident particles get the
-// softened factor (r = 0 < eps) as in the reference.
+// of FP32): 1/r from rsqrt and g from the piecewise polynomials; two
+// coincident particles get the softened factor (r = 0 < eps) as in the
+// reference.
 __device__ __forceinline__ double pair_ir3_fp64(double dx, double dy, double dz, double eps, double soft3,
-                                                double mass, double rs, double hrs, double coeff)
+                                                double mass, double rs, double hrs, double coeff, const double *tab)
 {
 #if P2P_FP64_FAST
     (void)rs;
@@ -592,10 +621,10 @@ __device__ __forceinline__ double pair_ir3_fp64(double dx, double dy, double dz,
     const double rinv = r2 > 0.0 ? rsqrt(r2) : 0.0;
     const double dr = r2 * rinv;
     double ir3 = (dr < eps) ? soft3 : mass * (rinv * rinv * rinv);
-    const double drs = dr * hrs;
-    ir3 *= exp(-drs * drs) * (erfcx(drs) + coeff * drs);
+    ir3 *= split_g_fp64(dr * hrs, tab, coeff);
 #else
     (void)hrs;
+    (void)tab;
     double dr = sqrt(dx * dx + dy * dy + dz * dz);
     double ir3 = (dr < eps) ? soft3 : mass / (dr * dr * dr);
     double drs = 0.5 * dr / rs;
@@ -614,6 +643,8 @@ __global__ void __launch_bounds__(P2P_TB) k_p2p_fp64(P2PArgs A)
 {
     __shared__ Src64 s_src[P2P_WARPS][STAGE64];
     __shared__ double s_red[P2P_WARPS][32][3];
+    __shared__ double s_tab[SPLIT64_N];
+    load_split64(s_tab);
     const int lane = warp_lane();
     const int wib = threadIdx.x >> 5;
     Src64 *src = s_src[wib];
@@ -678,7 +709,7 @@ __global__ void __launch_bounds__(P2P_TB) k_p2p_fp64(P2PArgs A)
                         Src64 sj = src[j];
                         if (sj.idx == ip) continue;
                         double dx = sj.x - px, dy = sj.y - py, dz = sj.z - pz;
-                        const double ir3 = pair_ir3_fp64(dx, dy, dz, eps, soft3, mass, rs, hrs, coeff);
+                        const double ir3 = pair_ir3_fp64(dx, dy, dz, eps, soft3, mass, rs, hrs, coeff, s_tab);
                         ax += dx * ir3;
                         ay += dy * ir3;
                         az += dz * ir3;
@@ -1322,7 +1353,8 @@ __global__ void __launch_bounds__(256, 3) k_mu_gather(P2PArgs A, const int *slot
 
 template <int T>
 __device__ __forceinline__ void mu64_chunk(const P2PArgs &A, const int2 *ev, int ne, const long long *rbase,
-                                           double *rbuf, int t, int it, int q0, int nq, double *stage, int lane)
+                                           double *rbuf, int t, int it, int q0, int nq, double *stage,
+                                           const double *tab, int lane)
 {
     const int tg = lane >> 2, sg = lane & 3;
     const BoxParams &B = A.boxes[A.boxid[t]];
@@ -1363,7 +1395,7 @@ __device__ __forceinline__ void mu64_chunk(const P2PArgs &A, const int2 *ev, int
                     const int q = 8 * k + tg;
                     if (q < nq && !(self && q0 + q == j)) {
                         const double dx = sx - px[k], dy = sy - py[k], dz = sz - pz[k];
-                        const double ir3 = pair_ir3_fp64(dx, dy, dz, eps, soft3, mass, rs, hrs, coeff);
+                        const double ir3 = pair_ir3_fp64(dx, dy, dz, eps, soft3, mass, rs, hrs, coeff, tab);
                         const double fx = dx * ir3, fy = dy * ir3, fz = dz * ir3;
                         ax[k] += fx; ay[k] += fy; az[k] += fz;
                         rx -= fx; ry -= fy; rz -= fz;
@@ -1405,6 +1437,8 @@ __global__ void __launch_bounds__(MU64_TB, 1) k_p2p_mutual64(P2PArgs A, const in
                                                             const long long *rbase, double *rbuf)
 {
     __shared__ double s_stage[MU64_WARPS][3 * PH_MAX_LEAF];
+    __shared__ double s_tab[SPLIT64_N];
+    load_split64(s_tab);
     const int lane = warp_lane(), wib = threadIdx.x >> 5;
     const int nleaf = p2p_targets(A);
     for (;;) {
@@ -1417,9 +1451,9 @@ __global__ void __launch_bounds__(MU64_TB, 1) k_p2p_mutual64(P2PArgs A, const in
         const int2 *evt = ev + A.p2p_off[t];
         for (int q0 = 0; q0 < nt; q0 += 64) {
             const int nq = min(64, nt - q0);
-            if (nq > 32) mu64_chunk<8>(A, evt, ne, rbase, rbuf, t, it, q0, nq, s_stage[wib], lane);
-            else if (nq > 16) mu64_chunk<4>(A, evt, ne, rbase, rbuf, t, it, q0, nq, s_stage[wib], lane);
-            else mu64_chunk<2>(A, evt, ne, rbase, rbuf, t, it, q0, nq, s_stage[wib], lane);
+            if (nq > 32) mu64_chunk<8>(A, evt, ne, rbase, rbuf, t, it, q0, nq, s_stage[wib], s_tab, lane);
+            else if (nq > 16) mu64_chunk<4>(A, evt, ne, rbase, rbuf, t, it, q0, nq, s_stage[wib], s_tab, lane);
+            else mu64_chunk<2>(A, evt, ne, rbase, rbuf, t, it, q0, nq, s_stage[wib], s_tab, lane);
         }
     }
 }
@@ -1459,8 +1493,8 @@ __global__ void k_mu_gather64(P2PArgs A, const int *over, const int *nrecv, cons
 // (indices sfirst..), a source skipped where its index is the target's (a
 // leaf with itself), summed per target in source order as
 // src/fmm.c:823-855 sums a task.  exact: sqrt, division, erfc and exp as the
-// reference writes them; otherwise 1/r from rsqrt and one exponential with
-// erfcx (the FP64 pass's form).  out[3 q + d] = the target's sum.
+// reference writes them; otherwise 1/r from rsqrt and g from the piecewise
+// polynomials (the FP64 pass's form).  out[3 q + d] = the target's sum.
 __global__ void k_leaf_pair_fp64(const double *tpos, int nt, int tfirst, const double *spos, int ns, int sfirst,
                                  double eps, double mass, double rs, int exact, double *out)
 {
@@ -1479,12 +1513,7 @@ __global__ void k_leaf_pair_fp64(const double *tpos, int nt, int tfirst, const d
             const double drs = 0.5 * dr / rs;
             ir3 *= (erfc(drs) + coeff * drs * exp(-drs * drs));
         } else {
-            const double r2 = dx * dx + dy * dy + dz * dz;
-            const double rinv = r2 > 0.0 ? rsqrt(r2) : 0.0;
-            const double dr = r2 * rinv;
-            ir3 = (dr < eps) ? soft3 : mass * (rinv * rinv * rinv);
-            const double drs = dr * hrs;
-            ir3 *= exp(-drs * drs) * (erfcx(drs) + coeff * drs);
+            ir3 = pair_ir3_fp64(dx, dy, dz, eps, soft3, mass, rs, hrs, coeff, &g_split64[0][0]);
         }
         ax += dx * ir3;
         ay += dy * ir3;
@@ -1493,6 +1522,17 @@ __global__ void k_leaf_pair_fp64(const double *tpos, int nt, int tfirst, const d
     out[3 * q] = ax;
     out[3 * q + 1] = ay;
     out[3 * q + 2] = az;
+}
+
+// the FP64 split factor g(u) at n points: the piecewise polynomials of the
+// FP64 kernels, or (exact) erfc and exp as src/fmm.c:846-848 writes them
+__global__ void k_split_factor_fp64(const double *u, int n, int exact, double *g)
+{
+    const double coeff = 2.0 / sqrt(M_PI);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double x = u[i];
+        g[i] = exact ? erfc(x) + coeff * x * exp(-x * x) : split_g_fp64(x, &g_split64[0][0], coeff);
+    }
 }
 
 }  // namespace
@@ -1598,6 +1638,14 @@ int launch_p2p(const P2PArgs &a, int fp64, cudaStream_t st)
     if (fp64) ph::note_launch(), k_p2p_fp64<<<blocks, P2P_TB, 0, st>>>(a);
     else if (a.variant == 1) ph::note_launch(), k_p2p_split<<<blocks, P2P_TB, 0, st>>>(a);
     else ph::note_launch(), k_p2p_split_packed<<<blocks, P2P_TB, 0, st>>>(a);
+    PH_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
+int launch_split_factor_fp64(const double *u, int n, int exact, double *g, cudaStream_t st)
+{
+    if (n <= 0) return 0;
+    ph::note_launch(), k_split_factor_fp64<<<(n + 255) / 256, 256, 0, st>>>(u, n, exact, g);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }

@@ -63,6 +63,8 @@ SplitConsts make_split_consts(const PassParams &p);
 // FP32 P2P with mutual pairs (MAXLEAF <= 64; chosen for 48-64): sorts the
 // lists, pairs the entries, evaluates, adds the received reactions
 int launch_p2p_mutual(const P2PArgs &a, const MutualBufs &m, int fp64, cudaStream_t st);
+// the FP64 kernels' split factor g(u) at n device points (exact: erfc and exp)
+int launch_split_factor_fp64(const double *u, int n, int exact, double *g, cudaStream_t st);
 double split_sig(const PassParams &p);
 int launch_leaf_offsets(const BuildBufs &b, const TreeBufs &t, float4 *pos4, cudaStream_t st);
 int launch_p2p(const P2PArgs &a, int fp64, cudaStream_t st);
