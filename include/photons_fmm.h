@@ -68,7 +68,7 @@ void fmm_remote(int idx, double shift[3]);
    the pair force as src/fmm.c:834-852 writes it; p2p_kernel_rinvsqrt the
    same force with 1/r from the reciprocal square root and the split
    factor erfc(u) + (2/sqrt(pi)) u exp(-u^2) from piecewise polynomials
-   (within 2.8e-17 of it), the FP64 pass's form;
+   (within 5.3e-17 of it), the FP64 pass's form;
    p2p_kernel_inleaf a leaf with itself (jnode == inode), self pairs skipped. */
 void p2p_kernel(int inode, int jnode);
 void p2p_kernel_rinvsqrt(int inode, int jnode);

@@ -17,9 +17,9 @@ Run:  python fit_split_fp64.py > split_fp64_table.h
 import mpmath as mp
 import numpy as np
 
-W = mp.mpf(1) / 4
-NI = 32
-DEG = 12
+W = mp.mpf(1) / 16
+NI = 128
+DEG = 8
 
 
 def g(u):
@@ -48,7 +48,7 @@ def main():
     worst_abs = worst_rel = 0.0
     for i in range(NI):
         m = (i + mp.mpf(1) / 2) * W
-        for x in np.linspace(-0.125, 0.125, 1500, endpoint=False):
+        for x in np.linspace(-float(W) / 2, float(W) / 2, 1500, endpoint=False):
             d = mp.mpf(float(x))
             acc = mp.mpf(0)
             for k in range(DEG, -1, -1):

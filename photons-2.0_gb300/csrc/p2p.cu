@@ -24,7 +24,7 @@
 // image positions formed as pos + shift like the exported bodies of
 // src/remotes.c:83-89, self pair skipped by index.  1/r comes from rsqrt and
 // g(u) = erfc(u) + (2/sqrt(pi)) u exp(-u^2) from piecewise polynomials
-// (fit_split_fp64.py, within 2.8e-17 of g), which is fewer FP64 operations
+// (fit_split_fp64.py, within 5.3e-17 of g), which is fewer FP64 operations
 // than the reference's sqrt, division, erfc and exp and agrees with them to
 // a few ulp of the force.
 #include <cmath>
@@ -581,8 +581,8 @@ __global__ void __launch_bounds__(P2P_TB, P2P_MINB) k_p2p_split_packed(P2PArgs A
 // FP64 kernel: the reference's arithmetic
 // ---------------------------------------------------------------------
 // g(u) = erfc(u) + (2/sqrt(pi)) u exp(-u^2) (src/fmm.c:846-848) in FP64:
-// piecewise polynomials of degree 12 on intervals of 1/4 (coefficients by
-// fit_split_fp64.py, within 2.8e-17 of g on [0, 8)), erfc and exp beyond.
+// piecewise polynomials of degree 8 on intervals of 1/16 (coefficients by
+// fit_split_fp64.py, within 5.3e-17 of g on [0, 8)), erfc and exp beyond.
 // tab: the coefficients k-major, [k][interval], in shared or global memory.
 __device__ const double g_split64[SPLIT64_DEG + 1][SPLIT64_NI] = SPLIT64_C_INIT;
 #define SPLIT64_N ((SPLIT64_DEG + 1) * SPLIT64_NI)
