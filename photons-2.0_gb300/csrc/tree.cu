@@ -42,6 +42,7 @@
 // subtree blocks: one warp per node of the subtree level being split
 #define SUB_TB 256
 #define SUB_NW (SUB_TB / 32)
+#define SUB_FAIL (1 << 20)  // failure mark in a subtree's node counters (above any node count)
 
 // depth lists: unified ids per block (one warp) of the counting sort
 #define DEPTH_R 4096
@@ -57,6 +58,17 @@ namespace {
 __host__ __device__ __forceinline__ const double *axis_ptr(const double *x, const double *y, const double *z, int D)
 {
     return D == 0 ? x : (D == 1 ? y : z);
+}
+
+// An integer key that orders doubles as the FP64 comparison does (both
+// zeros equal), so that !(x > mean) is key(x) <= key(mean) on the integer
+// pipe; GB300's FP64 pipe runs at 1/64 of the FP32 rate.  Exact for every
+// non-NaN x.
+__device__ __forceinline__ long long order_key(double x)
+{
+    const long long b = __double_as_longlong(x);
+    if ((b & 0x7FFFFFFFFFFFFFFFLL) == 0) return 0;
+    return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFLL);
 }
 
 // one root per box: its particle range and the box [0, L]^3 as
@@ -189,7 +201,7 @@ __global__ void k_chunk_count(BuildBufs b, int D)
         int i = b.ch_node[w];
         int t = lb + i;
         int start = b.tn_start[t], len = b.tn_len[t];
-        double mean = b.tn_split[t];
+        const long long km = order_key(b.tn_split[t]);
         int s0 = (w - b.tn_chunk_base[i]) * CHUNK;
         int s1 = min(len, s0 + CHUNK);
         const double *cp = coord + start;
@@ -200,9 +212,9 @@ __global__ void k_chunk_count(BuildBufs b, int D)
 #pragma unroll
             for (int q = 0; q < 8; q++) v[q] = cp[k + 32 * q];
 #pragma unroll
-            for (int q = 0; q < 8; q++) c += !(v[q] > mean);
+            for (int q = 0; q < 8; q++) c += order_key(v[q]) <= km;
         }
-        for (; k < s1; k += 32) c += !(cp[k] > mean);
+        for (; k < s1; k += 32) c += order_key(cp[k]) <= km;
         c = __reduce_add_sync(0xffffffffu, c);
         if (lane == 0) b.ch_cnt[w] = c;
     }
@@ -406,7 +418,7 @@ __global__ void k_rank(BuildBufs b, int D)
         int t = lb + i;
         if (b.tn_mode[t] != 0) continue;
         int start = b.tn_start[t], len = b.tn_len[t];
-        double mean = b.tn_split[t];
+        const long long km = order_key(b.tn_split[t]);
         int S = b.tn_S[t];
         int s0 = (w - b.tn_chunk_base[i]) * CHUNK;
         int s1 = min(len, s0 + CHUNK);
@@ -425,7 +437,7 @@ __global__ void k_rank(BuildBufs b, int D)
             for (int q = 0; q < 4; q++) {
                 const int p = k0 + 32 * q + lane;
                 const bool in = p < s1;
-                const bool small = in && !(v[q] > mean);
+                const bool small = in && order_key(v[q]) <= km;
                 const unsigned m = __ballot_sync(0xffffffffu, small);
                 const int r = run + __popc(m & lt);
                 if (in) {
@@ -488,18 +500,25 @@ __global__ void k_swap(BuildBufs b, int D)
 }
 
 // ---------------- subtrees of at most CHUNK particles ----------------
+// Shared memory of one subtree block, 53.3 KB: four blocks per SM.
 struct SubTree {
-    double x[CHUNK], y[CHUNK], z[CHUNK];  // the subtree's particles; then the numbering arrays
-    int perm[CHUNK];
+    // the subtree's particles; once written back, the region holds the
+    // original permutation (bytes 0-4095) and the numbering arrays
+    double x[CHUNK], y[CHUNK], z[CHUNK];
+    unsigned short loc[CHUNK];                      // subtree-local index of the particle at each position
     unsigned short bigpos[CHUNK], smallpos[CHUNK];  // a node's slots, over its own local range
-    // nodes in creation order (node 0 the subtree root): local range,
-    // parent, child codes (>= 0 node, < 0 ~leaf), split
-    unsigned short n_start[CHUNK], n_len[CHUNK], n_parent[CHUNK];
+    // nodes by level in creation order (node 0 the subtree root): local
+    // range, child codes (>= 0 node, < 0 ~leaf), split
+    unsigned short n_start[CHUNK], n_len[CHUNK];
     short n_c0[CHUNK], n_c1[CHUNK];
     double n_split[CHUNK];
-    unsigned short l_start[CHUNK], l_len[CHUNK], l_parent[CHUNK];
+    unsigned short l_start[CHUNK], l_len[CHUNK];
     unsigned short lev[CHUNK + 2];  // first node of each level of the subtree
-    int nnodes, nleaves, fail, nbase, lbase;
+    // nodes made by a level are numbered after the level's end through
+    // counter (L + 1) mod 3, which also records a failure (see
+    // k_subtree_build)
+    int nalloc[3];
+    int nleaves, fail, nbase, lbase;
 };
 
 __device__ __forceinline__ void sub_swap(SubTree &s, int i, int j)
@@ -508,14 +527,15 @@ __device__ __forceinline__ void sub_swap(SubTree &s, int i, int j)
     t = s.x[i]; s.x[i] = s.x[j]; s.x[j] = t;
     t = s.y[i]; s.y[i] = s.y[j]; s.y[j] = t;
     t = s.z[i]; s.z[i] = s.z[j]; s.z[j] = t;
-    int q = s.perm[i]; s.perm[i] = s.perm[j]; s.perm[j] = q;
+    const unsigned short q = s.loc[i]; s.loc[i] = s.loc[j]; s.loc[j] = q;
 }
 
-// One warp splits node i of the subtree (at the given depth): the mean,
-// count, ranks and swaps a node of one chunk gets, with the same lane order
-// and reductions (the sum is lane 0's butterfly result added to 0.0, as the
-// one-term reduction of k_node_mean does), then its two children.
-__device__ void sub_split_node(SubTree &s, int i, int depth, int axis0, int maxleaf, int levels)
+// One warp splits node i of the subtree (at depth `depth`, level L of the
+// subtree whose nodes end at lend): the mean, count, ranks and swaps a node
+// of one chunk gets, with the same lane order and reductions (the sum is
+// lane 0's butterfly result added to 0.0, as the one-term reduction of
+// k_node_mean does), then its two children.
+__device__ void sub_split_node(SubTree &s, int i, int depth, int L, int lend, int axis0, int maxleaf, int levels)
 {
     const int lane = warp_lane();
     const unsigned lt = (1u << lane) - 1u;
@@ -533,8 +553,9 @@ __device__ void sub_split_node(SubTree &s, int i, int depth, int axis0, int maxl
         m += sum;
         mean = m / (double)len;
     }
+    const long long km = order_key(mean);
     int c = 0;
-    for (int k = lane; k < len; k += 32) c += !(cd[k] > mean);
+    for (int k = lane; k < len; k += 32) c += order_key(cd[k]) <= km;
     const int S = __reduce_add_sync(0xffffffffu, c);
     int mode, left;
     split_sizes(len, S, mode, left);
@@ -546,7 +567,7 @@ __device__ void sub_split_node(SubTree &s, int i, int depth, int axis0, int maxl
         for (int k0 = 0; k0 < len; k0 += 32) {
             const int p = k0 + lane;
             const bool in = p < len;
-            const bool small = in && !(cd[p] > mean);
+            const bool small = in && order_key(cd[p]) <= km;
             const unsigned m = __ballot_sync(0xffffffffu, small);
             const int r = run + __popc(m & lt);
             if (in) {
@@ -570,14 +591,13 @@ __device__ void sub_split_node(SubTree &s, int i, int depth, int axis0, int maxl
                 const int j = atomicAdd(&s.nleaves, 1);
                 s.l_start[j] = (unsigned short)off;
                 s.l_len[j] = (unsigned short)sizes[ch];
-                s.l_parent[j] = (unsigned short)i;
                 code = ~j;
             } else {
-                if (depth + 1 >= levels) s.fail = 1;  // a node below the launched depths
-                const int j = atomicAdd(&s.nnodes, 1);
+                // a node below the launched depths fails the subtree
+                const int j = lend + (atomicAdd(&s.nalloc[(L + 1) % 3], depth + 1 >= levels ? SUB_FAIL + 1 : 1) &
+                                      (SUB_FAIL - 1));
                 s.n_start[j] = (unsigned short)off;
                 s.n_len[j] = (unsigned short)sizes[ch];
-                s.n_parent[j] = (unsigned short)i;
                 code = j;
             }
             if (ch == 0) s.n_c0[i] = (short)code;
@@ -594,8 +614,12 @@ __device__ void sub_split_node(SubTree &s, int i, int depth, int axis0, int maxl
 // from the split planes.  A subtree node's own preorder number goes to
 // tn_pre and its root to tn_subroot (leaves: tl_final, tl_subroot);
 // k_subtree_number adds the root's numbers once the levels are numbered.
-// Every barrier is reached by all threads of the block: the loop bounds and
-// the failure flag are read between two barriers.
+// Every barrier is reached by all threads of the block: loop bounds and
+// failure flags are read after a barrier and not written again before the
+// next one.  Level L numbers its new nodes through counter (L + 1) mod 3
+// (a failure adds SUB_FAIL to it), which thread 0 cleared during level
+// L - 1; counter (L + 2) mod 3, last read after level L - 2, is cleared
+// during level L.  So one barrier per level.
 __global__ void __launch_bounds__(SUB_TB) k_subtree_build(BuildBufs b, int axis0, int maxleaf, int levels)
 {
     extern __shared__ __align__(16) unsigned char sub_smem[];
@@ -603,6 +627,10 @@ __global__ void __launch_bounds__(SUB_TB) k_subtree_build(BuildBufs b, int axis0
     if (b.cnt[BC_LEVEL_COUNT] > 0 || (b.cnt[BC_FLAGS] & (PH_FLAG_LEAF_CAPACITY | PH_FLAG_NODE_CAPACITY))) return;
     const int T0 = b.cnt[BC_LEVEL_BEGIN], L0 = b.cnt[BC_LEAVES];
     const int tid = threadIdx.x, warp = tid >> 5;
+    int *operm = reinterpret_cast<int *>(s.x);
+    unsigned short *sn = reinterpret_cast<unsigned short *>(s.x) + 2 * CHUNK;
+    unsigned short *sl = sn + CHUNK, *pre = sl + CHUNK, *lb = pre + CHUNK, *lfin = lb + CHUNK;
+    unsigned short *npar = lfin + CHUNK, *lpar = npar + CHUNK;
     for (int t = blockIdx.x; t < T0; t += gridDim.x) {
         if (b.tn_mode[t] != MODE_DEFERRED) continue;
         const int start = b.tn_start[t], len = b.tn_len[t], rd = b.tn_depth[t];
@@ -610,14 +638,13 @@ __global__ void __launch_bounds__(SUB_TB) k_subtree_build(BuildBufs b, int axis0
             s.x[k] = b.x[start + k];
             s.y[k] = b.y[start + k];
             s.z[k] = b.z[start + k];
-            s.perm[k] = b.perm[start + k];
+            s.loc[k] = (unsigned short)k;
         }
         if (tid == 0) {
-            s.nnodes = 1;
+            s.nalloc[1] = 0;
             s.nleaves = 0;
             s.n_start[0] = 0;
             s.n_len[0] = (unsigned short)len;
-            s.n_parent[0] = 0xFFFFu;
             s.lev[0] = 0;
             s.fail = 0;
         }
@@ -625,38 +652,46 @@ __global__ void __launch_bounds__(SUB_TB) k_subtree_build(BuildBufs b, int axis0
         int failed = rd >= levels;
         int nlev = 0, lbeg = 0, lend = 1;
         while (lbeg < lend && !failed) {
-            for (int i = lbeg + warp; i < lend; i += SUB_NW) sub_split_node(s, i, rd + nlev, axis0, maxleaf, levels);
+            if (tid == 0) s.nalloc[(nlev + 2) % 3] = 0;
+            for (int i = lbeg + warp; i < lend; i += SUB_NW)
+                sub_split_node(s, i, rd + nlev, nlev, lend, axis0, maxleaf, levels);
             __syncthreads();
+            const int got = s.nalloc[(nlev + 1) % 3];
             lbeg = lend;
-            lend = s.nnodes;
-            failed = s.fail;
+            lend += got & (SUB_FAIL - 1);
+            failed = got >= SUB_FAIL;
             nlev++;
             if (tid == 0) s.lev[nlev] = (unsigned short)lbeg;
-            __syncthreads();
         }
+        __syncthreads();  // lev[] complete
         if (failed) {
             if (tid == 0) atomicOr(&b.cnt[BC_FLAGS], PH_FLAG_DEPTH);
-            __syncthreads();
-            continue;
+            continue;  // the next subtree's first writes follow a barrier all threads passed
         }
         for (int k = tid; k < len; k += SUB_TB) {
             b.x[start + k] = s.x[k];
             b.y[start + k] = s.y[k];
             b.z[start + k] = s.z[k];
-            b.perm[start + k] = s.perm[k];
         }
+        __syncthreads();  // x, y, z read: their region now takes the original permutation
+        for (int k = tid; k < len; k += SUB_TB) operm[k] = b.perm[start + k];
         __syncthreads();
-        // numbering arrays over the particle arrays (5 x CHUNK shorts in 3 x CHUNK doubles)
-        unsigned short *sn = reinterpret_cast<unsigned short *>(s.x);
-        unsigned short *sl = sn + CHUNK, *pre = sl + CHUNK, *lb = pre + CHUNK, *lfin = lb + CHUNK;
+        for (int k = tid; k < len; k += SUB_TB) b.perm[start + k] = operm[s.loc[k]];
+        // parents from the child codes; subtree sizes bottom-up
+        for (int i = tid; i < lend; i += SUB_TB) {
+            const int c0 = s.n_c0[i], c1 = s.n_c1[i];
+            if (c0 >= 0) npar[c0] = (unsigned short)i; else lpar[~c0] = (unsigned short)i;
+            if (c1 >= 0) npar[c1] = (unsigned short)i; else lpar[~c1] = (unsigned short)i;
+        }
         for (int L = nlev - 1; L >= 0; L--) {
+            __syncthreads();
             for (int i = s.lev[L] + tid; i < s.lev[L + 1]; i += SUB_TB) {
                 const int c0 = s.n_c0[i], c1 = s.n_c1[i];
                 sn[i] = (unsigned short)(1 + (c0 >= 0 ? sn[c0] : 0) + (c1 >= 0 ? sn[c1] : 0));
                 sl[i] = (unsigned short)((c0 >= 0 ? sl[c0] : 1) + (c1 >= 0 ? sl[c1] : 1));
             }
-            __syncthreads();
         }
+        __syncthreads();
         if (tid == 0) {
             const int ntot = sn[0], ltot = sl[0];
             const int nb = atomicAdd(&b.cnt[BC_SUB_NODES], ntot - 1);
@@ -702,7 +737,7 @@ __global__ void __launch_bounds__(SUB_TB) k_subtree_build(BuildBufs b, int axis0
                 b.tn_child1[ti] = c1 >= 0 ? nbase + pre[c1] - 1 : ~(lbase + lfin[~c1]);
                 b.tn_split[ti] = s.n_split[i];
                 if (i == 0) continue;
-                const int par = s.n_parent[i];
+                const int par = npar[i];
                 const int tp = par == 0 ? t : nbase + pre[par] - 1;
                 b.tn_start[ti] = start + s.n_start[i];
                 b.tn_len[ti] = s.n_len[i];
@@ -727,7 +762,7 @@ __global__ void __launch_bounds__(SUB_TB) k_subtree_build(BuildBufs b, int axis0
         }
         for (int j = tid; j < s.nleaves; j += SUB_TB) {
             const int tl = lbase + lfin[j];
-            const int par = s.l_parent[j];
+            const int par = lpar[j];
             const int tp = par == 0 ? t : nbase + pre[par] - 1;
             const int pd = b.tn_depth[tp];
             b.tl_start[tl] = start + s.l_start[j];
@@ -979,7 +1014,7 @@ int build_tree(BuildBufs &b, TreeBufs &T, const PassParams &p, int levels, int t
         ph::note_launch(), k_swap<<<maxb, TB, 0, st>>>(b, D);
         ph::note_launch(), k_level_finish<<<1, 1, 0, st>>>(b, d, top);
     }
-    ph::note_launch(), k_subtree_build<<<device_sm_count() * 3, SUB_TB, sizeof(SubTree), st>>>(b, p.axis0, p.maxleaf,
+    ph::note_launch(), k_subtree_build<<<device_sm_count() * 4, SUB_TB, sizeof(SubTree), st>>>(b, p.axis0, p.maxleaf,
                                                                                                 levels);
     ph::note_launch(), k_tree_totals<<<1, 1, 0, st>>>(b);
     // subtree sizes bottom-up, numbers top-down, over the recorded levels (top + 1 at most)
