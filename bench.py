@@ -586,6 +586,7 @@ def main():
     torch.cuda.synchronize()
     free0, total_hbm = torch.cuda.mem_get_info()
     fp = ph.ForcePass(local)
+    tuned = None
     tune = None
     pflags = 0  # the autotuner's kernel choice: PHOTONS_F_ONE_WAY, or the mutual kernel's build (shape bits)
     if not args.maxleaf:
@@ -600,8 +601,15 @@ def main():
                 "error_bound_median": args.error_bound, "candidates": table,
                 "score": "fastest pass with median error vs the FP64 direct sum <= bound (2000-particle sample)"}
         # the candidates' smaller leaves grew the context's list pools: time the
-        # chosen configuration in a fresh context sized for it alone
-        fp.close()
+        # chosen configuration in a fresh context sized for it alone.  The
+        # tuning context stays allocated until the host-buffer leg has run:
+        # on GB300 hosts, freeing its buffers was followed by seconds of
+        # host-link copies slowed ten-fold for ~20 ms every ~0.5 s (device
+        # work unaffected), which a serving process that keeps its context
+        # never sees.
+        tuned = fp
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
         fp = ph.ForcePass(local)
     stream = torch.cuda.current_stream()
     fp.set_stream(stream.cuda_stream)
@@ -676,6 +684,8 @@ def main():
     e2e_split["each"] = {"h2d_ms": [round(q[0], 3) for q in e2e_parts], "device_ms": [round(q[1], 3) for q in e2e_parts],
                          "d2h_ms": [round(q[2], 3) for q in e2e_parts], "host_call_ms": [round(q[4], 3) for q in e2e_parts]}
     acc32 = ha.copy()
+    if tuned is not None:
+        tuned.close()
 
     if rank != 0:
         if dist:
