@@ -364,8 +364,10 @@ __global__ void k_m_to_f32(const double *M, float *M32, const int *tree_cnt, con
 // by a fixed butterfly (lane 0's result) and added to the FP64 L
 __global__ void k_m2l_f32(const int *tree_cnt, const unsigned long long *walk_flags, const uint32_t *pool,
                           const long long *off, const int *cnt, const float4 *chi, const float4 *clo, const float *M32,
-                          double *Lout, const int *boxid, const BoxParams *boxes, FarConsts F, int *work)
+                          double *Lout, const int *boxid, const BoxParams *boxes, FarConsts F, int *work,
+                          const int *gate)
 {
+    if (gate && !*gate) return;  // no M2L task in this pass
     const int nunified = *walk_flags ? 0 : tree_cnt[BC_LEAVES] + tree_cnt[BC_NODES];
     const int lane = threadIdx.x & 31;
     for (;;) {
@@ -516,7 +518,7 @@ int run_m2l_f32(const MultipoleArgs &a, float *M32, cudaStream_t st)
     PH_CUDA_CHECK(cudaMemsetAsync(a.work, 0, sizeof(int), st));
     ph::note_launch(), k_m2l_f32<<<grid_cap(), MP_TB, 0, st>>>(a.tree_cnt, a.walk_flags, a.m2l_pool, a.m2l_off,
                                                                  a.m2l_cnt, a.chi, a.clo, M32, a.L, a.boxid, a.boxes, F,
-                                                                 a.work);
+                                                                 a.work, a.gate_l);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
 }

@@ -607,6 +607,64 @@ __device__ __forceinline__ void load_split64(double *s_tab)
     __syncthreads();
 }
 
+// the same with row k scaled by W^k (exact: W is a power of two), for the
+// variable d' = d / W = t - (i + 1/2), t = u / W: Horner over the scaled
+// rows gives bit for bit the unscaled result
+__device__ __forceinline__ void load_split64_scaled(double *s_tab)
+{
+    for (int i = threadIdx.x; i < SPLIT64_N; i += blockDim.x) {
+        const int k = i / SPLIT64_NI;
+        s_tab[i] = ldexp((&g_split64[0][0])[i], -4 * k);
+    }
+    static_assert(SPLIT64_INVW == 16, "scaled rows assume intervals of 1/16");
+    __syncthreads();
+}
+
+// Per-leaf constants of the mass-free FP64 pair factor
+struct Pair64 {
+    long long eps_bits, tmax_bits;  // eps and SPLIT64_NI as ordered bit patterns
+    double ieps3, hrs, hrs_n, coeff;
+};
+
+__device__ __forceinline__ Pair64 pair64_consts(double eps, double rs)
+{
+    Pair64 c;
+    c.eps_bits = __double_as_longlong(eps);
+    c.tmax_bits = __double_as_longlong((double)SPLIT64_NI);
+    c.ieps3 = 1.0 / (eps * eps * eps);
+    c.hrs = 0.5 / rs;
+    c.hrs_n = c.hrs * SPLIT64_INVW;
+    c.coeff = 2.0 / sqrt(M_PI);
+    return c;
+}
+
+// g(u) / max(r, eps)^3 for a source dx away, u = r / 2rs; the caller
+// applies the mass once per target and per reaction slot.  r, eps and t
+// are non-negative, so their comparisons run on bit patterns (integer pipe);
+// t = u / W scales exactly, and the scaled rows (load_split64_scaled) give
+// the g of split_g_fp64.  Two coincident particles get the softened factor.
+__device__ __forceinline__ double pair_f_fp64(double dx, double dy, double dz, const Pair64 &c, const double *tabn)
+{
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    const double rinv = __double_as_longlong(r2) == 0 ? 0.0 : rsqrt(r2);
+    const double dr = r2 * rinv;
+    const double w = __double_as_longlong(dr) < c.eps_bits ? c.ieps3 : rinv * rinv * rinv;
+    const double t = dr * c.hrs_n;
+    double g;
+    if (__double_as_longlong(t) < c.tmax_bits) {
+        const int i = (int)t;
+        const double d = t - ((double)i + 0.5);
+        double acc = tabn[SPLIT64_DEG * SPLIT64_NI + i];
+#pragma unroll
+        for (int k = SPLIT64_DEG - 1; k >= 0; k--) acc = fma(acc, d, tabn[k * SPLIT64_NI + i]);
+        g = acc;
+    } else {
+        const double u = dr * c.hrs;
+        g = erfc(u) + c.coeff * u * exp(-u * u);
+    }
+    return w * g;
+}
+
 // m g(u) / max(r, eps)^3 for a source dx away.  Fast form (the default):
 // the same quantities with fewer FP64 operations (GB300's FP64 rate is 1/64
 // of FP32): 1/r from rsqrt and g from the piecewise polynomials; two
@@ -1345,7 +1403,9 @@ __global__ void __launch_bounds__(256, 3) k_mu_gather(P2PArgs A, const int *slot
 // the reaction on a source is summed over the 8 target groups (butterfly,
 // lane tg = 0's sum kept) and stored in the pair's slot (x, y, z rows of
 // r = n rounded up to 4 doubles; a second chunk adds to it).  Target sums
-// are combined over the 4 source groups at the end.  k_mu_gather64 adds
+// are combined over the 4 source groups at the end.  The pair factor is
+// pair_f_fp64's, without the mass, which multiplies each target sum and
+// each reaction slot once; sums accumulate by FMA.  k_mu_gather64 adds
 // each leaf's received slots in list order.
 // ---------------------------------------------------------------------
 #define MU64_TB 256
@@ -1358,8 +1418,8 @@ __device__ __forceinline__ void mu64_chunk(const P2PArgs &A, const int2 *ev, int
 {
     const int tg = lane >> 2, sg = lane & 3;
     const BoxParams &B = A.boxes[A.boxid[t]];
-    const double eps = B.eps, mass = B.mass, rs = B.rs, boxL = B.boxsize;
-    const double soft3 = mass / (eps * eps * eps), hrs = 0.5 / rs, coeff = 2.0 / sqrt(M_PI);
+    const double mass = B.mass, boxL = B.boxsize;
+    const Pair64 pc = pair64_consts(B.eps, B.rs);
     double px[T], py[T], pz[T], ax[T], ay[T], az[T];
 #pragma unroll
     for (int k = 0; k < T; k++) {
@@ -1395,10 +1455,9 @@ __device__ __forceinline__ void mu64_chunk(const P2PArgs &A, const int2 *ev, int
                     const int q = 8 * k + tg;
                     if (q < nq && !(self && q0 + q == j)) {
                         const double dx = sx - px[k], dy = sy - py[k], dz = sz - pz[k];
-                        const double ir3 = pair_ir3_fp64(dx, dy, dz, eps, soft3, mass, rs, hrs, coeff, tab);
-                        const double fx = dx * ir3, fy = dy * ir3, fz = dz * ir3;
-                        ax[k] += fx; ay[k] += fy; az[k] += fz;
-                        rx -= fx; ry -= fy; rz -= fz;
+                        const double f = pair_f_fp64(dx, dy, dz, pc, tab);
+                        ax[k] = fma(dx, f, ax[k]); ay[k] = fma(dy, f, ay[k]); az[k] = fma(dz, f, az[k]);
+                        rx = fma(-dx, f, rx); ry = fma(-dy, f, ry); rz = fma(-dz, f, rz);
                     }
                 }
             }
@@ -1410,6 +1469,7 @@ __device__ __forceinline__ void mu64_chunk(const P2PArgs &A, const int2 *ev, int
                     rz += __shfl_xor_sync(0xffffffffu, rz, o);
                 }
                 if (tg == 0 && j < ns) {
+                    rx *= mass; ry *= mass; rz *= mass;
                     if (q0 == 0) { out[j] = rx; out[row + j] = ry; out[2 * row + j] = rz; }
                     else { out[j] += rx; out[row + j] += ry; out[2 * row + j] += rz; }
                 }
@@ -1426,9 +1486,9 @@ __device__ __forceinline__ void mu64_chunk(const P2PArgs &A, const int2 *ev, int
         }
         const int q = 8 * k + tg;
         if (sg == 0 && q < nq) {
-            A.ax[it + q0 + q] += ax[k];
-            A.ay[it + q0 + q] += ay[k];
-            A.az[it + q0 + q] += az[k];
+            A.ax[it + q0 + q] += ax[k] * mass;
+            A.ay[it + q0 + q] += ay[k] * mass;
+            A.az[it + q0 + q] += az[k] * mass;
         }
     }
 }
@@ -1438,7 +1498,7 @@ __global__ void __launch_bounds__(MU64_TB, 1) k_p2p_mutual64(P2PArgs A, const in
 {
     __shared__ double s_stage[MU64_WARPS][3 * PH_MAX_LEAF];
     __shared__ double s_tab[SPLIT64_N];
-    load_split64(s_tab);
+    load_split64_scaled(s_tab);
     const int lane = warp_lane(), wib = threadIdx.x >> 5;
     const int nleaf = p2p_targets(A);
     for (;;) {
