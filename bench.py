@@ -623,35 +623,12 @@ def main():
     for _ in range(max(3, args.warmup)):
         step()
     torch.cuda.synchronize()
-    hbm_used = free0 - torch.cuda.mem_get_info()[0]
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    sampler = ClockSampler(local) if rank == 0 else None
-    if sampler:
-        sampler.start()
-    launches0 = ph.load_library().photons_launch_count()
-    p2p_ms, phase = [], []
+    # end to end through the C ABI: pinned host buffers in, host buffers out.
+    # Timed before the device-buffer loop: on GB300 hosts, host-link copies
+    # timed after it ran ten-fold slower for ~20 ms every ~0.5 s in some
+    # runs (device work unaffected), which this order did not show.
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        step()
-        t = fp.timings()
-        p2p_ms.append(t["p2p"])
-        phase.append(t)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    launches = ph.load_library().photons_launch_count() - launches0
-    clocks = sampler.stop() if sampler else None
-    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, dist, "cuda")
-    counters = fp.counters()
-    pairs = counters["pairs_local"] + counters["pairs_image"]
-    value = n * world / (ms * 1e-3)
-
-    # end to end through the C ABI: pinned host buffers in, host buffers out
     hpos = torch.from_numpy(pos).pin_memory()
     hacc = torch.empty_like(hpos).pin_memory()
     hp, ha = hpos.numpy(), hacc.numpy()
@@ -683,6 +660,34 @@ def main():
                          (float(np.median([q[i] for q in e2e_parts])) for i in range(5))))
     e2e_split["each"] = {"h2d_ms": [round(q[0], 3) for q in e2e_parts], "device_ms": [round(q[1], 3) for q in e2e_parts],
                          "d2h_ms": [round(q[2], 3) for q in e2e_parts], "host_call_ms": [round(q[4], 3) for q in e2e_parts]}
+    hbm_used = free0 - torch.cuda.mem_get_info()[0]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local) if rank == 0 else None
+    if sampler:
+        sampler.start()
+    launches0 = ph.load_library().photons_launch_count()
+    p2p_ms, phase = [], []
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+        t = fp.timings()
+        p2p_ms.append(t["p2p"])
+        phase.append(t)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    launches = ph.load_library().photons_launch_count() - launches0
+    clocks = sampler.stop() if sampler else None
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, dist, "cuda")
+    counters = fp.counters()
+    pairs = counters["pairs_local"] + counters["pairs_image"]
+    value = n * world / (ms * 1e-3)
+
     acc32 = ha.copy()
     if tuned is not None:
         tuned.close()
