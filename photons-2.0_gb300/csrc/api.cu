@@ -195,7 +195,7 @@ static int alloc_tree(photons_ctx *c, int n, int cap)
         b.cap_chunks = 0;
         c->epoch++;
         PH_TRY(dalloc(b.ch_partial, chunks)); PH_TRY(dalloc(b.ch_cnt, chunks)); PH_TRY(dalloc(b.ch_small_base, chunks));
-        PH_TRY(dalloc(b.ch_node, chunks)); PH_TRY(dalloc(b.ch_big, chunks));
+        PH_TRY(dalloc(b.ch_node, chunks)); PH_TRY(dalloc(b.ch_swap, chunks));
         c->epoch++;
         b.cap_chunks = chunks;
         size_t need = ph::scan_scratch_elems(cap > chunks ? cap : chunks) + 8;
@@ -269,7 +269,7 @@ static void free_all(photons_ctx *c)
                     b.lvl_begin, b.lvl_count, b.leaf_begin, b.leaf_count, c->t.depth_cnt, b.tn_boxid, b.tl_boxid,
                     c->t.boxid, b.boxes, c->far_gate, c->mu_sorted, c->mu_nrecv, c->mu_slot, c->mu_over,
                     c->mu_size, c->mu_rbase, c->mu_total, c->mu_scan, c->mu_buf, c->mu_ev, c->mu_nev, c->mu_pq,
-                    b.tn_subroot, b.tl_subroot, b.ch_big, c->t.depth_blk};
+                    b.tn_subroot, b.tl_subroot, b.ch_swap, c->t.depth_blk};
     for (void *p : ptrs)
         if (p) cudaFree(p);
 }
@@ -969,6 +969,140 @@ static int force_pass_graph(photons_ctx *c, int nbox, const photons_params *p, c
 }
 
 // ------------------------------------------------------------------
+// one kick-drift-kick step as one captured graph
+// ------------------------------------------------------------------
+namespace {
+
+// 1 when the pass just run did not fit (tree capacity, depth or levels,
+// walk pools, or a reaction buffer too small for its mutual pairs): the
+// captured step's second kick then leaves the velocities alone
+__global__ void k_pass_failed(const int *tree_cnt, const unsigned long long *walk_ctr, const int *mu_over, int *out)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        *out = (tree_cnt[ph::BC_FLAGS] & (PH_FLAG_LEAF_CAPACITY | PH_FLAG_NODE_CAPACITY | PH_FLAG_DEPTH | PH_FLAG_TOP)) ||
+               walk_ctr[ph::WC_FLAGS] != 0 || *mu_over != 0;
+}
+
+}  // namespace
+
+static int capture_kdk(photons_ctx *c, const photons_params *q, int n, double *pos, double *vel, double *acc,
+                       int levels, unsigned mask)
+{
+    if (c->kexec) cudaGraphExecDestroy(c->kexec);
+    c->kexec = nullptr;
+    c->have_kkey = false;
+    cudaStream_t st = c->stream;
+    PH_CUDA_CHECK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    c->capturing = true;
+    unsigned long long tally = 0;
+    ph::t_capture_tally = &tally;
+    int rc = ph_enqueue_kick_dev(n, vel, acc, c->kdk_f, nullptr, st);
+    if (!rc) rc = ph_enqueue_drift_dev(n, pos, vel, c->kdk_f + 1, q->boxsize, st);
+    if (!rc) rc = ph_enqueue_pass(c, q, pos, acc, levels, mask);
+    if (!rc) {
+        ph::note_launch(), k_pass_failed<<<1, 1, 0, st>>>(c->b.cnt, c->w.ctr, c->mu_over, c->kdk_skip);
+        if (cudaGetLastError() != cudaSuccess) rc = ph_set_error(PH_ERR_CUDA, "k_pass_failed launch");
+    }
+    if (!rc) rc = ph_enqueue_kick_dev(n, vel, acc, c->kdk_f, c->kdk_skip, st);
+    ph::t_capture_tally = nullptr;
+    c->kdk_kernels = tally;
+    c->capturing = false;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (!rc && e != cudaSuccess) rc = ph_set_cuda_error(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+    if (!rc) {
+        e = cudaGraphInstantiate(&c->kexec, g, 0);
+        if (e != cudaSuccess) {
+            c->kexec = nullptr;
+            rc = ph_set_cuda_error(e, "cudaGraphInstantiate", __FILE__, __LINE__);
+        }
+    }
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return rc;
+}
+
+// The step runs as one graph (kick, drift, the pass, the second kick) once
+// the pass has a captured graph whose key matches this one's: its
+// capacities fitted the last pass over these arrays.  Should this pass not
+// fit after all (particles moved), the second kick stops itself on the
+// device and the caller repeats the pass the usual way, with growth and
+// retries, then kicks; the first kick and the drift are never repeated.
+int ph_kdk_graph_step(photons_ctx *c, const photons_params *q, int n, double *pos, double *vel, double *acc,
+                      double dkh, double dd, int *done)
+{
+    *done = KDK_NOT_RUN;
+    const char *genv = getenv("PHOTONS_GRAPH");
+    if ((genv && !strcmp(genv, "0")) || n <= 0 || !pos || !vel || !acc) return 0;
+    c->dom_set = false;
+    c->walk_imp = ph::WalkImports();
+    PH_TRY(ph_prepare_boxes(c, 1, q, &n));
+    const unsigned mask = q->image_mask ? q->image_mask : ((1u << PH_NIMG) - 1u);
+    const int levels = c->hint_levels ? c->hint_levels : estimate_levels(n, q->maxleaf);
+    long long p2p_cap, pd_cap, m2l_cap;
+    int stack_cap, stage_cap;
+    walk_caps(c, p2p_cap, pd_cap, m2l_cap, stack_cap, stage_cap);
+    PH_TRY(alloc_walk(c, p2p_cap, pd_cap, m2l_cap, stack_cap, stage_cap));
+    PH_TRY(alloc_mutual(c, q->precision));
+    const PassKey k = pass_key(c, q, n, pos, acc, 1, levels, mask);
+    if (!c->gexec || !c->have_key || memcmp(&k, &c->key, sizeof k) != 0) return 0;
+    if (!c->kdk_f) { PH_TRY(dalloc(c->kdk_f, 2)); c->have_kkey = false; }
+    if (!c->kdk_skip) { PH_TRY(dalloc(c->kdk_skip, 1)); c->have_kkey = false; }
+    cudaStream_t st = c->stream;
+    if (!c->kexec || !c->have_kkey || memcmp(&k, &c->kkey, sizeof k) != 0 || c->kkey_vel != vel ||
+        c->kkey_box != q->boxsize) {
+        PH_TRY(capture_kdk(c, q, n, pos, vel, acc, levels, mask));
+        c->kkey = k;
+        c->kkey_vel = vel;
+        c->kkey_box = q->boxsize;
+        c->have_kkey = true;
+    }
+    const double f[2] = {dkh, dd};
+    PH_CUDA_CHECK(cudaMemcpyAsync(c->kdk_f, f, sizeof f, cudaMemcpyHostToDevice, st));
+    PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_START], st));
+    PH_TRY(ph_upload_boxes(c));
+    PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_UPLOADED], st));
+    PH_CUDA_CHECK(cudaGraphLaunch(c->kexec, st));
+    ph::g_launches += c->kdk_kernels;
+    PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_END], st));
+    int h[ph::BC_NCOUNTERS];
+    PH_CUDA_CHECK(cudaMemcpyAsync(h, c->b.cnt, sizeof h, cudaMemcpyDeviceToHost, st));
+    PH_CUDA_CHECK(cudaMemcpyAsync(c->ws.c, c->w.ctr, sizeof(c->ws.c), cudaMemcpyDeviceToHost, st));
+    c->info.depth_off.resize(levels + 2);
+    PH_CUDA_CHECK(cudaMemcpyAsync(c->info.depth_off.data(), c->t.depth_off, sizeof(int) * (levels + 2),
+                                  cudaMemcpyDeviceToHost, st));
+    long long mu_need = 0;
+    int mu_over = 0;
+    PH_CUDA_CHECK(cudaMemcpyAsync(&mu_need, c->mu_total, sizeof mu_need, cudaMemcpyDeviceToHost, st));
+    PH_CUDA_CHECK(cudaMemcpyAsync(&mu_over, c->mu_over, sizeof mu_over, cudaMemcpyDeviceToHost, st));
+    PH_CUDA_CHECK(cudaStreamSynchronize(st));
+    int grow = 0;
+    PH_TRY(ph_check_build(c, h[ph::BC_FLAGS], levels, &grow));
+    const unsigned long long fl = c->ws.c[ph::WC_FLAGS];
+    if (grow || fl) {
+        // the caller's pass grows what did not fit (its own checks repeat these)
+        *done = KDK_PASS_AGAIN;
+        return 0;
+    }
+    if (mu_over) {
+        mutual_feedback(c, mu_over, mu_need, q->precision);
+        *done = KDK_PASS_AGAIN;
+        return 0;
+    }
+    ph_tree_info_from(c, h, levels);
+    c->have_tree = true;
+    c->info.depth_off.resize(c->info.depth + 2);
+    c->have_lists = true;
+    c->mask = mask;
+    const bool any_m2l = c->ws.c[ph::WC_M2L_LOCAL] + c->ws.c[ph::WC_M2L_IMAGE] > 0;
+    c->have_multipoles = (!(q->flags & PHOTONS_F_NO_FARFIELD) && any_m2l) || (q->flags & PHOTONS_F_MULTIPOLES);
+    c->last_flags = q->flags;
+    c->precision = q->precision;
+    *done = KDK_DONE;
+    return 0;
+}
+
+// ------------------------------------------------------------------
 // C ABI
 // ------------------------------------------------------------------
 extern "C" photons_ctx *photons_create(int device)
@@ -997,6 +1131,9 @@ extern "C" void photons_destroy(photons_ctx *c)
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    if (c->kexec) cudaGraphExecDestroy(c->kexec);
+    cudaFree(c->kdk_f);
+    cudaFree(c->kdk_skip);
     ph_pm_release(c);
     ph_domain_release(c);
     cudaFree(c->pm_io);

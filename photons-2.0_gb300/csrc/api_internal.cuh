@@ -105,6 +105,16 @@ struct photons_ctx {
     cudaGraphExec_t gexec = nullptr;
     unsigned long long graph_kernels = 0;  // kernel nodes of gexec
     PassKey key{};
+    // the captured kick-drift-kick step: the pass's key, velocity array and
+    // box side; device factors (dkh, dd) and the flag that stops the second kick
+    cudaGraphExec_t kexec = nullptr;
+    unsigned long long kdk_kernels = 0;
+    bool have_kkey = false;
+    PassKey kkey{};
+    const double *kkey_vel = nullptr;
+    double kkey_box = 0.0;
+    double *kdk_f = nullptr;
+    int *kdk_skip = nullptr;
 };
 
 // return a nonzero status code from the enclosing function
@@ -121,6 +131,17 @@ struct HostTree {
 };
 
 int ph_validate(const photons_params *p, int n);
+// kick and drift with the factor in device memory (integrate.cu)
+int ph_enqueue_kick_dev(int n, double *vel, const double *acc, const double *dkh, const int *skip, cudaStream_t st);
+int ph_enqueue_drift_dev(int n, double *pos, const double *vel, const double *dd, double L, cudaStream_t st);
+// One kick-drift-kick step as one captured graph (api.cu).  *done:
+// KDK_DONE the step ran whole; KDK_NOT_RUN nothing ran (no graph yet for
+// this pass: the caller runs the step one launch at a time); KDK_PASS_AGAIN
+// the kick and drift ran but the pass did not fit (its flags stopped the
+// second kick): the caller runs the pass and the second kick.
+enum { KDK_NOT_RUN = 0, KDK_DONE = 1, KDK_PASS_AGAIN = 2 };
+int ph_kdk_graph_step(photons_ctx *c, const photons_params *q, int n, double *pos, double *vel, double *acc,
+                      double dkh, double dd, int *done);
 void ph_domain_release(photons_ctx *c);
 int ph_stage_build(photons_ctx *c, const photons_params *p, int n, const double *pos, int device_io);
 int ph_stage_walk(photons_ctx *c, unsigned mask);

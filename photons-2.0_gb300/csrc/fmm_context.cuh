@@ -33,7 +33,7 @@ struct BuildBufs {
     // chunks
     double *ch_partial = nullptr;
     int *ch_cnt = nullptr, *ch_small_base = nullptr, *ch_node = nullptr;
-    int *ch_big = nullptr;  // left-region particles above the mean, per chunk
+    int4 *ch_swap = nullptr;  // per chunk: node start, first slot, slots to swap
     // small device counters
     int *cnt = nullptr;  // see BuildCounter
     int *lvl_begin = nullptr, *lvl_count = nullptr;    // per node level: first temp node, count

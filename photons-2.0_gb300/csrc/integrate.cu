@@ -84,6 +84,46 @@ __global__ void k_drift(double *__restrict__ pos, const double *__restrict__ vel
         pos[m - 1] = wrap_coord(__dadd_rn(pos[m - 1], __dmul_rn(vel[m - 1], dd)), L, Lb);
 }
 
+// The same kick and drift with the factor read from device memory, for a
+// step captured once as a graph and launched with new factors each time;
+// a nonzero *skip (the pass before it failed to fit) leaves vel as it is.
+__global__ void k_kick_dev(double *__restrict__ vel, const double *__restrict__ acc, const double *f,
+                           const int *skip, long long m)
+{
+    if (skip && *skip) return;
+    const double dkh = *f;
+    const long long m2 = m >> 1;
+    double2 *v2 = reinterpret_cast<double2 *>(vel);
+    const double2 *a2 = reinterpret_cast<const double2 *>(acc);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m2; i += (long long)gridDim.x * blockDim.x) {
+        double2 v = v2[i];
+        const double2 a = a2[i];
+        v.x = __dadd_rn(v.x, __dmul_rn(a.x, dkh));
+        v.y = __dadd_rn(v.y, __dmul_rn(a.y, dkh));
+        v2[i] = v;
+    }
+    if ((m & 1) && blockIdx.x == 0 && threadIdx.x == 0) vel[m - 1] = __dadd_rn(vel[m - 1], __dmul_rn(acc[m - 1], dkh));
+}
+
+__global__ void k_drift_dev(double *__restrict__ pos, const double *__restrict__ vel, const double *f, double L,
+                            long long m)
+{
+    const double dd = *f;
+    const long long m2 = m >> 1;
+    const long long Lb = __double_as_longlong(L);
+    double2 *p2 = reinterpret_cast<double2 *>(pos);
+    const double2 *v2 = reinterpret_cast<const double2 *>(vel);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m2; i += (long long)gridDim.x * blockDim.x) {
+        double2 p = p2[i];
+        const double2 v = v2[i];
+        p.x = wrap_coord(__dadd_rn(p.x, __dmul_rn(v.x, dd)), L, Lb);
+        p.y = wrap_coord(__dadd_rn(p.y, __dmul_rn(v.y, dd)), L, Lb);
+        p2[i] = p;
+    }
+    if ((m & 1) && blockIdx.x == 0 && threadIdx.x == 0)
+        pos[m - 1] = wrap_coord(__dadd_rn(pos[m - 1], __dmul_rn(vel[m - 1], dd)), L, Lb);
+}
+
 bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
 
 int enqueue_kick(int n, double *vel, const double *acc, double dkh, cudaStream_t st)
@@ -174,6 +214,27 @@ extern "C" int photons_drift(int n, double *pos, const double *vel, double dd, d
     return enqueue_drift(n, pos, vel, dd, boxsize, (cudaStream_t)cuda_stream);
 }
 
+// launchers of the device-factor kernels (the captured step in api.cu)
+int ph_enqueue_kick_dev(int n, double *vel, const double *acc, const double *dkh, const int *skip, cudaStream_t st)
+{
+    if (n < 0 || (n > 0 && (!vel || !acc || !dkh))) return ph_set_error(PH_ERR_ARG, "bad kick arguments");
+    if (!aligned16(vel) || !aligned16(acc)) return ph_set_error(PH_ERR_ARG, "kick arrays must be 16-byte aligned");
+    if (n == 0) return 0;
+    ph::note_launch(), k_kick_dev<<<ph::device_sm_count() * 8, 256, 0, st>>>(vel, acc, dkh, skip, 3LL * n);
+    PH_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
+int ph_enqueue_drift_dev(int n, double *pos, const double *vel, const double *dd, double L, cudaStream_t st)
+{
+    if (n < 0 || (n > 0 && (!pos || !vel || !dd)) || !(L > 0)) return ph_set_error(PH_ERR_ARG, "bad drift arguments");
+    if (!aligned16(pos) || !aligned16(vel)) return ph_set_error(PH_ERR_ARG, "drift arrays must be 16-byte aligned");
+    if (n == 0) return 0;
+    ph::note_launch(), k_drift_dev<<<ph::device_sm_count() * 8, 256, 0, st>>>(pos, vel, dd, L, 3LL * n);
+    PH_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
 extern "C" int photons_kdk_step(photons_ctx *c, const photons_params *p, int n, double *pos, double *vel,
                                 double *acc, double dkh, double dd)
 {
@@ -181,11 +242,19 @@ extern "C" int photons_kdk_step(photons_ctx *c, const photons_params *p, int n, 
     if (!c || !p) return ph_set_error(PH_ERR_ARG, "null argument");
     cudaSetDevice(c->device);
     cudaStream_t st = c->stream;
-    PH_TRY(enqueue_kick(n, vel, acc, dkh, st));
-    PH_TRY(enqueue_drift(n, pos, vel, dd, p->boxsize, st));
     photons_params q = *p;
     q.flags |= PHOTONS_F_DEVICE_IO;
     q.flags &= ~PHOTONS_F_TREE_ORDER;
+    // the whole step as one captured graph once this pass's own graph fits
+    // (ph_kdk_graph_step); otherwise, or to repeat a pass that did not fit
+    // after the graph's kick and drift, the steps one by one
+    int done = 0;
+    PH_TRY(ph_kdk_graph_step(c, &q, n, pos, vel, acc, dkh, dd, &done));
+    if (done == KDK_DONE) return 0;
+    if (done == KDK_NOT_RUN) {
+        PH_TRY(enqueue_kick(n, vel, acc, dkh, st));
+        PH_TRY(enqueue_drift(n, pos, vel, dd, p->boxsize, st));
+    }
     PH_TRY(photons_force_pass(c, &q, n, pos, acc));
     PH_TRY(enqueue_kick(n, vel, acc, dkh, st));
     PH_CUDA_CHECK(cudaStreamSynchronize(st));

@@ -403,8 +403,9 @@ __global__ void k_tree_totals(BuildBufs b)
 // the mean in the left region (p < S) publishes its position under slot
 // p-r (its rank among particles above the mean).  Slot k pairs the k-th
 // from the left with the k-th from the right, which is the order
-// src/fmm.c:60-72 swaps them in.  ch_big counts the chunk's left-region
-// particles above the mean, so k_swap walks the chunk's slots.
+// src/fmm.c:60-72 swaps them in.  ch_swap records each chunk's slots
+// (the left-region particles above the mean), so k_swap reads one record
+// per chunk.
 __global__ void k_rank(BuildBufs b, int D)
 {
     const int lb = b.cnt[BC_LEVEL_BEGIN];
@@ -416,7 +417,10 @@ __global__ void k_rank(BuildBufs b, int D)
     for (int w = gw; w < W; w += nw) {
         int i = b.ch_node[w];
         int t = lb + i;
-        if (b.tn_mode[t] != 0) continue;
+        if (b.tn_mode[t] != 0) {
+            if (lane == 0) b.ch_swap[w] = make_int4(0, 0, 0, 0);
+            continue;
+        }
         int start = b.tn_start[t], len = b.tn_len[t];
         const long long km = order_key(b.tn_split[t]);
         int S = b.tn_S[t];
@@ -424,7 +428,8 @@ __global__ void k_rank(BuildBufs b, int D)
         int s1 = min(len, s0 + CHUNK);
         const double *cp = coord + start;
         int *bigpos = b.bigpos + start, *smallpos = b.smallpos + start;
-        int run = b.ch_small_base[w];
+        const int small_before = b.ch_small_base[w];
+        int run = small_before;
         int nbig = 0;
         for (int k0 = s0; k0 < s1; k0 += 128) {
             double v[4];
@@ -448,28 +453,26 @@ __global__ void k_rank(BuildBufs b, int D)
                 run += __popc(m);
             }
         }
-        if (lane == 0) b.ch_big[w] = nbig;
+        // the chunk's swaps for k_swap: its node's first particle, its first
+        // slot and its number of slots (none once s0 >= S)
+        if (lane == 0) b.ch_swap[w] = make_int4(start, s0 - small_before, s0 < S ? nbig : 0, 0);
     }
 }
 
 // The swaps of a chunk's slots: its left-region particles above the mean
-// hold slots [s0 - (particles not above the mean before s0), + ch_big);
-// each slot's two particles trade places.  Pairs are disjoint; a lane loads
-// four slots' particles before it stores any.
+// hold slots [s0 - (particles not above the mean before s0), + their
+// number), as k_rank recorded in ch_swap; each slot's two particles trade
+// places.  Pairs are disjoint; a lane loads four slots' particles before it
+// stores any.
 __global__ void k_swap(BuildBufs b, int D)
 {
-    const int lb = b.cnt[BC_LEVEL_BEGIN];
     int W = b.cnt[BC_W];
     int lane = warp_lane();
     int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
     for (int w = gw; w < W; w += nw) {
-        int i = b.ch_node[w];
-        int t = lb + i;
-        if (b.tn_mode[t] != 0) continue;
-        const int start = b.tn_start[t], S = b.tn_S[t];
-        const int s0 = (w - b.tn_chunk_base[i]) * CHUNK;
-        if (s0 >= S) continue;
-        const int kb = s0 - b.ch_small_base[w], nb = b.ch_big[w];
+        const int4 c = b.ch_swap[w];
+        const int start = c.x, kb = c.y, nb = c.z;
+        if (nb == 0) continue;
         const int *bigpos = b.bigpos + start + kb, *smallpos = b.smallpos + start + kb;
         for (int k0 = 0; k0 < nb; k0 += 128) {
             int pi[4], pj[4];

@@ -162,6 +162,39 @@ def _kdk_factors(ph):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["FP64", "FP32_SPLIT"])
+def test_kdk_steps_as_one_graph_match_the_steps_one_by_one(ph, ics, precision):
+    """From the second step on, photons_kdk_step runs the kick, the drift,
+    the force pass and the second kick as one captured graph (the pass's own
+    graph has run with the same key), with new factors every step: over
+    several steps positions, velocities and accelerations equal the same
+    steps launched one by one in another context, bit for bit."""
+    torch = pytest.importorskip("torch")
+    pos, p = ics.make("zeldovich512", nside=24, maxleaf=16)
+    n = pos.shape[0]
+    vel = np.random.default_rng(5).standard_normal(pos.shape) * 0.5
+    dkh, dd = _kdk_factors(ph)
+    prec = getattr(ph, precision)
+    fa, fb = ph.ForcePass(0), ph.ForcePass(0)
+    acc0 = fa.run(pos, p, precision=prec)
+    a = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in (pos, vel, acc0)]
+    b = [t.clone() for t in a]
+    stream = torch.cuda.current_stream()
+    fb.set_stream(stream.cuda_stream)
+    torch.cuda.synchronize()
+    for step in range(4):
+        k, d = dkh * (1 + 0.1 * step), dd * (1 - 0.05 * step)
+        fa.kdk_step_device(*(t.data_ptr() for t in a), n, p, k, d, precision=prec)
+        ph.kick(n, b[1].data_ptr(), b[2].data_ptr(), k, stream.cuda_stream)
+        ph.drift(n, b[0].data_ptr(), b[1].data_ptr(), d, p["boxsize"], stream.cuda_stream)
+        fb.run_device(b[0].data_ptr(), b[2].data_ptr(), n, p, precision=prec)
+        ph.kick(n, b[1].data_ptr(), b[2].data_ptr(), k, stream.cuda_stream)
+        torch.cuda.synchronize()
+        for x, y in zip(a, b):
+            assert torch.equal(x, y), step
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("maxleaf", [16, 64])
 def test_ordered_kdk_step_is_the_step_in_tree_order(ph, ics, maxleaf):
     """photons_kdk_step_ordered leaves pos, vel, acc and ids in the pass's
