@@ -514,15 +514,16 @@ def run_boxes_bench(args):
         a64.append(rel_err(acc64[offs[i] + tg], ds))
     a32, a64 = np.concatenate(a32), np.concatenate(a64)
     # end to end: host arrays through the batched C-ABI call
-    hpos = torch.from_numpy(pos).pin_memory()
-    hacc = torch.empty_like(hpos).pin_memory()
+    hpos = ph.host_array(pos.shape)  # pinned by the library (cudaHostAlloc)
+    hpos[:] = pos
+    hacc = ph.host_array(pos.shape)
     hp32 = (ph.Params * len(boxes))()
     for i, (_, p) in enumerate(boxes):
         hp32[i] = ph.make_params(p, ph.FP32_SPLIT, 0, 0)
 
     def e2e():
-        rc = lib.photons_force_pass_boxes(fp.h, len(boxes), hp32, cptr, C.c_void_p(hpos.data_ptr()),
-                                          C.c_void_p(hacc.data_ptr()))
+        rc = lib.photons_force_pass_boxes(fp.h, len(boxes), hp32, cptr, C.c_void_p(hpos.ctypes.data),
+                                          C.c_void_p(hacc.ctypes.data))
         if rc:
             raise RuntimeError(lib.photons_gpu_error().decode())
 
@@ -629,9 +630,9 @@ def main():
     # runs (device work unaffected), which this order did not show.
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    hpos = torch.from_numpy(pos).pin_memory()
-    hacc = torch.empty_like(hpos).pin_memory()
-    hp, ha = hpos.numpy(), hacc.numpy()
+    hp = ph.host_array(pos.shape)  # pinned by the library (cudaHostAlloc)
+    hp[:] = pos
+    ha = ph.host_array(pos.shape)
     for _ in range(3):  # the host-buffer pass is captured as its own graph on first use
         fp.run(hp, p, precision=ph.FP32_SPLIT, flags=pflags, out=ha)
     torch.cuda.synchronize()

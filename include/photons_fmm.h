@@ -23,6 +23,8 @@
 #ifndef PHOTONS_FMM_H
 #define PHOTONS_FMM_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -345,6 +347,11 @@ int photons_kdk_step_pm_ordered(photons_ctx *ctx, const photons_params *p, int n
 
 /* kernels launched by this library so far (all contexts) */
 unsigned long long photons_launch_count(void);
+
+/* pinned host memory for the host-buffer pass (its copies then run at the
+   host link's rate); NULL and an error message if it cannot be had */
+void *photons_host_alloc(size_t bytes);
+void photons_host_free(void *p);
 
 /* FP32 FMA throughput probes: TFLOP/s of FFMA chains, and of the paired
    (float2) FFMA of sm_100+; ~iters x 128 FMAs per thread */

@@ -115,6 +115,9 @@ def load_library():
     lib.photons_fp64_fma_peak.restype = C.c_double
     lib.photons_fp64_fma_peak.argtypes = [C.c_int]
     lib.photons_split_factor_fp64.argtypes = [_dp, C.c_int, C.c_int, _dp]
+    lib.photons_host_alloc.restype = C.c_void_p
+    lib.photons_host_alloc.argtypes = [C.c_size_t]
+    lib.photons_host_free.argtypes = [C.c_void_p]
     lib.photons_gpu_error.restype = C.c_char_p
     lib.photons_gpu_status.restype = C.c_int
     for name in ("fmm_construct", "fmm_prepare", "fmm_task", "fmm_ext", "fmm_deconstruct", "build_localtree",
@@ -493,6 +496,24 @@ def fp64_fma_peak(iters=256):
     if v <= 0:
         raise PhotonsError("FP64 FMA probe failed: " + lib.photons_gpu_error().decode(errors="replace"))
     return v
+
+
+def host_array(shape, dtype=np.float64):
+    """A numpy array in pinned host memory from photons_host_alloc (freed
+    with the array), for the host-buffer pass: its copies then run at the
+    host link's rate."""
+    import weakref
+
+    dtype = np.dtype(dtype)
+    count = int(np.prod(shape))
+    nbytes = max(1, count * dtype.itemsize)
+    lib = load_library()
+    ptr = lib.photons_host_alloc(nbytes)
+    if not ptr:
+        raise PhotonsError("pinned host allocation failed: " + lib.photons_gpu_error().decode(errors="replace"))
+    buf = (C.c_char * nbytes).from_address(ptr)
+    weakref.finalize(buf, lib.photons_host_free, C.c_void_p(ptr))
+    return np.frombuffer(buf, dtype=dtype, count=count).reshape(shape)
 
 
 def split_factor_fp64(u, exact=False):
