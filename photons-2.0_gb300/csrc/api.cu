@@ -4,6 +4,7 @@
 //   upload -> tree build -> leaf offsets -> dual-tree walk -> P2P
 //   -> [P2M, M2M, M2L, L2L, L2P when any M2L task exists] -> gather/download
 // The reference-named entry points (legacy.cu) reuse the same stages.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -1258,7 +1259,7 @@ extern "C" int photons_get_counters(photons_ctx *c, long long *out, int n)
     v[18] = c->info.depth;
     v[19] = (long long)w[ph::WC_MAX_STACK];
     v[20] = (long long)w[ph::WC_MAX_STAGE];
-    v[21] = (long long)w[ph::WC_PD_MAX];
+    v[21] = (long long)std::max(w[ph::WC_PD_MAX], std::max(w[ph::WC_PD_FILL0], w[ph::WC_PD_FILL1]));
     v[22] = (long long)w[ph::WC_P2P_FILL];
     v[23] = (long long)w[ph::WC_M2L_FILL];
     for (int i = 0; i < n && i < 32; i++) out[i] = v[i];

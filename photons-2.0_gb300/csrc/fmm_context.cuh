@@ -102,7 +102,7 @@ enum WalkCounter {
     WC_PD_FILL0 = 0, WC_PD_FILL1, WC_P2P_FILL, WC_M2L_FILL,
     WC_P2P_LOCAL, WC_P2P_IMAGE, WC_M2L_LOCAL, WC_M2L_IMAGE,
     WC_PAIRS_LOCAL, WC_PAIRS_IMAGE, WC_FLAGS, WC_MAX_STACK, WC_MAX_STAGE, WC_PD_MAX,
-    WC_WORK,  // next target of the depth being walked (reset between depths)
+    WC_WORK0, WC_WORK1,  // next target of the depth being walked (depth parity)
     WC_N
 };
 

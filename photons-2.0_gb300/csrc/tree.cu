@@ -44,6 +44,9 @@
 #define SUB_NW (SUB_TB / 32)
 #define SUB_FAIL (1 << 20)  // failure mark in a subtree's node counters (above any node count)
 
+// levels of at most this many nodes run their bookkeeping in one block
+#define SMALL_LEVEL 4096
+
 // depth lists: unified ids per block (one warp) of the counting sort
 #define DEPTH_R 4096
 
@@ -112,31 +115,37 @@ __global__ void k_init_particles(const double *__restrict__ pos, int n, BuildBuf
 }
 
 // chunks per node; a deferred node has none and makes no children here
-__global__ void k_level_nch(BuildBufs b)
+__device__ __forceinline__ void level_nch_node(BuildBufs &b, int lb, int i)
 {
-    const int lb = b.cnt[BC_LEVEL_BEGIN], C = b.cnt[BC_LEVEL_COUNT];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
-        const int t = lb + i;
-        if (b.tn_mode[t] == MODE_DEFERRED) {
-            b.tn_nch[i] = 0;
-            b.tn_nodeflag[i] = 0;
-            b.tn_leafflag[i] = 0;
-        } else {
-            b.tn_nch[i] = (b.tn_len[t] + CHUNK - 1) / CHUNK;
-        }
+    const int t = lb + i;
+    if (b.tn_mode[t] == MODE_DEFERRED) {
+        b.tn_nch[i] = 0;
+        b.tn_nodeflag[i] = 0;
+        b.tn_leafflag[i] = 0;
+    } else {
+        b.tn_nch[i] = (b.tn_len[t] + CHUNK - 1) / CHUNK;
     }
 }
 
-// chunk -> level-local node index, written once per level
+__global__ void k_level_nch(BuildBufs b)
+{
+    const int lb = b.cnt[BC_LEVEL_BEGIN], C = b.cnt[BC_LEVEL_COUNT];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) level_nch_node(b, lb, i);
+}
+
+// chunk -> level-local node index, written once per level (a warp per node)
+__device__ __forceinline__ void chunk_map_node(BuildBufs &b, int i, int lane)
+{
+    const int c0 = b.tn_chunk_base[i], nc = b.tn_nch[i];
+    for (int k = lane; k < nc; k += 32) b.ch_node[c0 + k] = i;
+}
+
 __global__ void k_chunk_map(BuildBufs b)
 {
     const int C = b.cnt[BC_LEVEL_COUNT];
     int lane = warp_lane();
     int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-    for (int i = gw; i < C; i += nw) {
-        int c0 = b.tn_chunk_base[i], nc = b.tn_nch[i];
-        for (int k = lane; k < nc; k += 32) b.ch_node[c0 + k] = i;
-    }
+    for (int i = gw; i < C; i += nw) chunk_map_node(b, i, lane);
 }
 
 // Chunk sums: lane l adds positions l, l+32, l+64, ... of the chunk in that
@@ -249,38 +258,40 @@ __device__ __forceinline__ void node_split_finish(BuildBufs &b, int i, int t, in
 // partition sizes, child kinds.  Each lane sums a contiguous block of chunk
 // counts (the prefix is exact integer arithmetic, so the blocking does not
 // change it).
+__device__ __forceinline__ void node_split_node(BuildBufs &b, int lb, int i, int lane, int maxleaf)
+{
+    const int nc = b.tn_nch[i];
+    if (nc == 0) return;
+    const int t = lb + i, c0 = b.tn_chunk_base[i];
+    const int per = (nc + 31) / 32;
+    const int kb = min(nc, lane * per), ke = min(nc, kb + per);
+    int own = 0;
+#pragma unroll 8
+    for (int k = kb; k < ke; k++) own += b.ch_cnt[c0 + k];
+    const int incl = warp_incl_scan(own);
+    int run = incl - own;
+    for (int k = kb; k < ke; k++) {
+        b.ch_small_base[c0 + k] = run;
+        run += b.ch_cnt[c0 + k];
+    }
+    const int S = shfl(incl, 31);
+    if (lane == 0) node_split_finish(b, i, t, b.tn_len[t], S, maxleaf);
+}
+
 __global__ void k_node_split(BuildBufs b, int maxleaf)
 {
     const int lb = b.cnt[BC_LEVEL_BEGIN], C = b.cnt[BC_LEVEL_COUNT];
     int lane = warp_lane();
     int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-    for (int i = gw; i < C; i += nw) {
-        const int nc = b.tn_nch[i];
-        if (nc == 0) continue;
-        const int t = lb + i, c0 = b.tn_chunk_base[i];
-        const int per = (nc + 31) / 32;
-        const int kb = min(nc, lane * per), ke = min(nc, kb + per);
-        int own = 0;
-#pragma unroll 8
-        for (int k = kb; k < ke; k++) own += b.ch_cnt[c0 + k];
-        const int incl = warp_incl_scan(own);
-        int run = incl - own;
-        for (int k = kb; k < ke; k++) {
-            b.ch_small_base[c0 + k] = run;
-            run += b.ch_cnt[c0 + k];
-        }
-        const int S = shfl(incl, 31);
-        if (lane == 0) node_split_finish(b, i, t, b.tn_len[t], S, maxleaf);
-    }
+    for (int i = gw; i < C; i += nw) node_split_node(b, lb, i, lane, maxleaf);
 }
 
-__global__ void k_make_children(BuildBufs b, int maxleaf, int D)
+__device__ __forceinline__ void make_children_node(BuildBufs &b, int lb, int C, int leaves_before, int i, int maxleaf,
+                                                   int D)
 {
-    const int lb = b.cnt[BC_LEVEL_BEGIN], C = b.cnt[BC_LEVEL_COUNT];
-    int leaves_before = b.cnt[BC_LEAVES];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
+    {
         int t = lb + i;
-        if (b.tn_mode[t] == MODE_DEFERRED) continue;
+        if (b.tn_mode[t] == MODE_DEFERRED) return;
         int start = b.tn_start[t];
         int depth = b.tn_depth[t];
         int sizes[2] = {b.tn_child0[t], b.tn_child1[t]};
@@ -344,13 +355,21 @@ __global__ void k_make_children(BuildBufs b, int maxleaf, int D)
     }
 }
 
+__global__ void k_make_children(BuildBufs b, int maxleaf, int D)
+{
+    const int lb = b.cnt[BC_LEVEL_BEGIN], C = b.cnt[BC_LEVEL_COUNT];
+    const int leaves_before = b.cnt[BC_LEAVES];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x)
+        make_children_node(b, lb, C, leaves_before, i, maxleaf, D);
+}
+
 // Close level d: record its node range and the leaves it created, advance.
 // When the last launched level (d = top - 1) made deferred nodes only,
 // they are recorded as level top for k_subtree_build.  After a capacity
 // overflow no further level is built.
-__global__ void k_level_finish(BuildBufs b, int d, int top)
+__device__ void level_finish(BuildBufs &b, int d, int top)
 {
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    {
         const int C = b.cnt[BC_LEVEL_COUNT], lb = b.cnt[BC_LEVEL_BEGIN];
         if (C == 0) return;
         if (b.cnt[BC_FLAGS] & (PH_FLAG_LEAF_CAPACITY | PH_FLAG_NODE_CAPACITY)) {
@@ -375,6 +394,76 @@ __global__ void k_level_finish(BuildBufs b, int d, int top)
         }
         b.cnt[BC_NEXT_WIDE] = 0;
     }
+}
+
+__global__ void k_level_finish(BuildBufs b, int d, int top)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0) level_finish(b, d, top);
+}
+
+// ---------------- one block for the bookkeeping of a small level ----------------
+// A level of at most SMALL_LEVEL nodes (the first levels) runs its per-node
+// bookkeeping in single-block kernels: the same per-node work as the
+// kernels above, the scans in one block.  k_level_plan closes the level
+// before (when that was small too), then counts chunks, numbers them and
+// maps them to nodes; k_level_close splits the nodes, numbers the children
+// and makes them.  Integer work throughout, so the tree is unchanged.
+#define SMALL_TB 1024
+
+// exclusive scan of in[0, n) into out by the whole block; returns the total
+__device__ int block_scan_excl(const int *in, int *out, int n, int *s_warp)
+{
+    const int lane = warp_lane(), warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    int carry = 0;
+    for (int base = 0; base < n; base += blockDim.x) {
+        const int i = base + threadIdx.x;
+        const int v = i < n ? in[i] : 0;
+        const int incl = warp_incl_scan(v);
+        if (lane == 31) s_warp[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            const int w = lane < nwarps ? s_warp[lane] : 0;
+            const int wi = warp_incl_scan(w);
+            s_warp[lane] = wi - w;
+            if (lane == 31) s_warp[32] = wi;
+        }
+        __syncthreads();
+        if (i < n) out[i] = carry + s_warp[warp] + incl - v;
+        carry += s_warp[32];
+        __syncthreads();
+    }
+    return carry;
+}
+
+__global__ void __launch_bounds__(SMALL_TB) k_level_plan(BuildBufs b, int finish_prev, int top)
+{
+    __shared__ int s_warp[33];
+    if (finish_prev >= 0 && threadIdx.x == 0) level_finish(b, finish_prev, top);
+    __syncthreads();
+    const int lb = b.cnt[BC_LEVEL_BEGIN], C = b.cnt[BC_LEVEL_COUNT];
+    for (int i = threadIdx.x; i < C; i += blockDim.x) level_nch_node(b, lb, i);
+    __syncthreads();
+    const int W = block_scan_excl(b.tn_nch, b.tn_chunk_base, C, s_warp);
+    if (threadIdx.x == 0) b.cnt[BC_W] = W;
+    const int lane = warp_lane();
+    for (int i = threadIdx.x >> 5; i < C; i += blockDim.x >> 5) chunk_map_node(b, i, lane);
+}
+
+__global__ void __launch_bounds__(SMALL_TB) k_level_close(BuildBufs b, int maxleaf, int D)
+{
+    __shared__ int s_warp[33];
+    const int lb = b.cnt[BC_LEVEL_BEGIN], C = b.cnt[BC_LEVEL_COUNT];
+    const int lane = warp_lane();
+    for (int i = threadIdx.x >> 5; i < C; i += blockDim.x >> 5) node_split_node(b, lb, i, lane, maxleaf);
+    __syncthreads();
+    const int next = block_scan_excl(b.tn_nodeflag, b.tn_nodebase, C, s_warp);
+    const int fresh = block_scan_excl(b.tn_leafflag, b.tn_leafbase, C, s_warp);
+    if (threadIdx.x == 0) {
+        b.cnt[BC_NEXT_NODES] = next;
+        b.cnt[BC_NEW_LEAVES] = fresh;
+    }
+    const int leaves_before = b.cnt[BC_LEAVES];
+    for (int i = threadIdx.x; i < C; i += blockDim.x) make_children_node(b, lb, C, leaves_before, i, maxleaf, D);
 }
 
 // After k_subtree_build: totals, and PH_FLAG_TOP if wide nodes remain
@@ -998,25 +1087,44 @@ int build_tree(BuildBufs &b, TreeBufs &T, const PassParams &p, int levels, int t
     PH_CUDA_CHECK(cudaMemsetAsync(b.lvl_count, 0, sizeof(int) * (top + 2), st));
     PH_CUDA_CHECK(cudaMemsetAsync(b.leaf_count, 0, sizeof(int) * (top + 2), st));
     ph::note_launch(), k_init_roots<<<(b.nbox + TB - 1) / TB, TB, 0, st>>>(b);
+    // a level has at most nbox 2^d nodes: the first levels are small enough for
+    // single-block bookkeeping (7 launches a level instead of 19)
+    bool pending = false;  // a small level whose k_level_finish is still to come
     for (int d = 0; d < top; d++) {
         const int D = (p.axis0 + d) % 3;  // from direct_local_start; the axis cycles (src/fmm.c:99)
-        ph::note_launch(), k_level_nch<<<maxb, TB, 0, st>>>(b);
-        scan_exclusive_i32(b.tn_nch, b.tn_chunk_base, b.cnt + BC_LEVEL_COUNT, b.cap_nodes, b.cnt + BC_W,
-                           b.scan_scratch, b.scan_scratch_elems, st);
-        ph::note_launch(), k_chunk_map<<<maxb, TB, 0, st>>>(b);
+        const bool small = d < 24 && ((long long)b.nbox << d) <= SMALL_LEVEL;
+        if (small) {
+            ph::note_launch(), k_level_plan<<<1, SMALL_TB, 0, st>>>(b, pending ? d - 1 : -1, top);
+        } else {
+            if (pending) ph::note_launch(), k_level_finish<<<1, 1, 0, st>>>(b, d - 1, top);
+            ph::note_launch(), k_level_nch<<<maxb, TB, 0, st>>>(b);
+            scan_exclusive_i32(b.tn_nch, b.tn_chunk_base, b.cnt + BC_LEVEL_COUNT, b.cap_nodes, b.cnt + BC_W,
+                               b.scan_scratch, b.scan_scratch_elems, st);
+            ph::note_launch(), k_chunk_map<<<maxb, TB, 0, st>>>(b);
+        }
         ph::note_launch(), k_chunk_sum<<<maxb, TB, 0, st>>>(b, D);
         ph::note_launch(), k_node_mean<<<maxb, TB, 0, st>>>(b, D);
         ph::note_launch(), k_chunk_count<<<maxb, TB, 0, st>>>(b, D);
-        ph::note_launch(), k_node_split<<<maxb, TB, 0, st>>>(b, p.maxleaf);
-        scan_exclusive_i32(b.tn_nodeflag, b.tn_nodebase, b.cnt + BC_LEVEL_COUNT, b.cap_nodes, b.cnt + BC_NEXT_NODES,
-                           b.scan_scratch, b.scan_scratch_elems, st);
-        scan_exclusive_i32(b.tn_leafflag, b.tn_leafbase, b.cnt + BC_LEVEL_COUNT, b.cap_nodes, b.cnt + BC_NEW_LEAVES,
-                           b.scan_scratch, b.scan_scratch_elems, st);
-        ph::note_launch(), k_make_children<<<maxb, TB, 0, st>>>(b, p.maxleaf, D);
+        if (small) {
+            ph::note_launch(), k_level_close<<<1, SMALL_TB, 0, st>>>(b, p.maxleaf, D);
+        } else {
+            ph::note_launch(), k_node_split<<<maxb, TB, 0, st>>>(b, p.maxleaf);
+            scan_exclusive_i32(b.tn_nodeflag, b.tn_nodebase, b.cnt + BC_LEVEL_COUNT, b.cap_nodes,
+                               b.cnt + BC_NEXT_NODES, b.scan_scratch, b.scan_scratch_elems, st);
+            scan_exclusive_i32(b.tn_leafflag, b.tn_leafbase, b.cnt + BC_LEVEL_COUNT, b.cap_nodes,
+                               b.cnt + BC_NEW_LEAVES, b.scan_scratch, b.scan_scratch_elems, st);
+            ph::note_launch(), k_make_children<<<maxb, TB, 0, st>>>(b, p.maxleaf, D);
+        }
         ph::note_launch(), k_rank<<<maxb, TB, 0, st>>>(b, D);
         ph::note_launch(), k_swap<<<maxb, TB, 0, st>>>(b, D);
-        ph::note_launch(), k_level_finish<<<1, 1, 0, st>>>(b, d, top);
+        if (small) {
+            pending = true;
+        } else {
+            ph::note_launch(), k_level_finish<<<1, 1, 0, st>>>(b, d, top);
+            pending = false;
+        }
     }
+    if (pending) ph::note_launch(), k_level_finish<<<1, 1, 0, st>>>(b, top - 1, top);
     ph::note_launch(), k_subtree_build<<<device_sm_count() * 4, SUB_TB, sizeof(SubTree), st>>>(b, p.axis0, p.maxleaf,
                                                                                                 levels);
     ph::note_launch(), k_tree_totals<<<1, 1, 0, st>>>(b);

@@ -182,6 +182,16 @@ __global__ void __launch_bounds__(WALK_TB, MINB) k_walk_level(WalkArgs A)
     const int lane = warp_lane();
     const unsigned lt = (1u << lane) - 1u;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    // this depth counts in the counters of its parity; the other parity's,
+    // last used by the depth before, are reset for the next depth (which
+    // starts after this kernel), its pool fill kept in WC_PD_MAX
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const int o = (A.depth + 1) & 1;
+        const unsigned long long f = W.ctr[WC_PD_FILL0 + o];
+        if (f > W.ctr[WC_PD_MAX]) W.ctr[WC_PD_MAX] = f;
+        W.ctr[WC_PD_FILL0 + o] = 0;
+        W.ctr[WC_WORK0 + o] = 0;
+    }
     if (gw >= W.nwarps) return;
     uint32_t *stack = W.scratch + (size_t)gw * (W.stack_cap + 3 * W.stage_cap);
     uint32_t *st_p2p = stack + W.stack_cap;
@@ -203,7 +213,7 @@ __global__ void __launch_bounds__(WALK_TB, MINB) k_walk_level(WalkArgs A)
     // more than tenfold on clustered input); each is expanded by one warp
     for (;;) {
         unsigned long long tk = 0;
-        if (lane == 0) tk = atomicAdd(&W.ctr[WC_WORK], 1ULL);
+        if (lane == 0) tk = atomicAdd(&W.ctr[WC_WORK0 + parity], 1ULL);
         const long long ti = list_begin + (long long)__shfl_sync(0xffffffffu, tk, 0);
         if (ti >= list_end) break;
         const int a = A.depth_list[ti];
@@ -444,18 +454,6 @@ __global__ void __launch_bounds__(WALK_TB, MINB) k_walk_level(WalkArgs A)
     }
 }
 
-__global__ void k_walk_level_done(WalkBufs W, int depth)
-{
-    // the pool written by this depth is read by the next; the next depth
-    // writes the other pool, whose fill starts from zero
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        unsigned long long f = W.ctr[WC_PD_FILL0 + (depth & 1)];
-        if (f > W.ctr[WC_PD_MAX]) W.ctr[WC_PD_MAX] = f;
-        W.ctr[WC_PD_FILL0 + ((depth + 1) & 1)] = 0;
-        W.ctr[WC_WORK] = 0;
-    }
-}
-
 // FP32 copies of the geometry for every unified id: centre as hi + lo,
 // widths and width sum rounded
 __global__ void k_geom32(const double *cx, const double *cy, const double *cz, const double *wx, const double *wy,
@@ -516,7 +514,6 @@ int walk_lists(WalkBufs &w, const TreeBufs &t, const int *tree_cnt, const BoxPar
             ph::note_launch(), k_walk_level<3><<<blocks, WALK_TB, 0, st>>>(A);
         else
             ph::note_launch(), k_walk_level<2><<<blocks, WALK_TB, 0, st>>>(A);
-        ph::note_launch(), k_walk_level_done<<<1, 1, 0, st>>>(w, d);
     }
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;
