@@ -4,7 +4,8 @@
 // build_localtree) in two parts.
 //
 // Wide nodes (more than CHUNK particles) are split level-synchronously:
-// every wide node of one depth in the same set of launches.  Per level:
+// every wide node of one depth in the same set of launches (the per-node
+// bookkeeping of the first, small levels in single blocks).  Per level:
 //   1. each node's particle range is cut into chunks of CHUNK particles;
 //   2. chunk sums of the split coordinate (axis = depth mod 3) and a
 //      fixed-order reduction give the node's mean;
@@ -45,7 +46,7 @@
 #define SUB_FAIL (1 << 20)  // failure mark in a subtree's node counters (above any node count)
 
 // levels of at most this many nodes run their bookkeeping in one block
-#define SMALL_LEVEL 4096
+#define SMALL_LEVEL 32
 
 // depth lists: unified ids per block (one warp) of the counting sort
 #define DEPTH_R 4096
@@ -1078,11 +1079,15 @@ int build_tree(BuildBufs &b, TreeBufs &T, const PassParams &p, int levels, int t
     const int ndepth = levels + 1;  // leaves can sit one level below the deepest nodes
     const int nblk = T.depth_nblk;
     if (nblk < 1 || nblk != depth_sort_blocks(T.cap_u)) return ph_set_error(7, "depth-sort buffers not allocated");
-    static bool sub_attr = false;
-    if (!sub_attr) {
+    // the subtree blocks' shared memory is above the 48 KB default: allowed
+    // once per device
+    static bool sub_attr[64] = {};
+    int dev = 0;
+    PH_CUDA_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64 || !sub_attr[dev]) {
         PH_CUDA_CHECK(cudaFuncSetAttribute(k_subtree_build, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)sizeof(SubTree)));
-        sub_attr = true;
+        if (dev >= 0 && dev < 64) sub_attr[dev] = true;
     }
     PH_CUDA_CHECK(cudaMemsetAsync(b.lvl_count, 0, sizeof(int) * (top + 2), st));
     PH_CUDA_CHECK(cudaMemsetAsync(b.leaf_count, 0, sizeof(int) * (top + 2), st));
