@@ -84,6 +84,16 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float a)
     s = t;
 }
 
+// kahan_add on both halves of a float2 with the paired FP32 instructions:
+// per element the same operations and roundings
+__device__ __forceinline__ void kahan_add2(float2 &s, float2 &c, float2 a)
+{
+    const float2 y = __fadd2_rn(a, make_float2(-c.x, -c.y));
+    const float2 t = __fadd2_rn(s, y);
+    c = __fadd2_rn(__fadd2_rn(t, make_float2(-s.x, -s.y)), make_float2(-y.x, -y.y));
+    s = t;
+}
+
 __device__ __forceinline__ void leaf_shift(int img, double L, double &s0, double &s1, double &s2)
 {
     int mi, mj, mk;
@@ -1084,8 +1094,11 @@ __device__ __forceinline__ void mu_target(const P2PArgs &A, const int2 *ev, int 
         ny[p] = make_float2(-o0.y, -o1.y);
         nz[p] = make_float2(-o0.z, -o1.z);
     }
+    // running sums: float2 (targets 2p, 2p + 1) per component, [value][lane];
+    // their compensations 3 TP values further
+    float2 *acc2 = reinterpret_cast<float2 *>(accw);
 #pragma unroll
-    for (int k = 0; k < 6 * T; k++) accw[k * 32 + lane] = 0.f;
+    for (int k = 0; k < 3 * T; k++) acc2[k * 32 + lane] = f2(0.f);
     // partial sums run over up to MU_FLUSH evaluated entries (at most 64 terms
     // per lane) before they join the compensated running sums
     float2 ax[TP], ay[TP], az[TP];
@@ -1189,10 +1202,9 @@ __device__ __forceinline__ void mu_target(const P2PArgs &A, const int2 *ev, int 
                 pending = 0;
 #pragma unroll
                 for (int p = 0; p < TP; p++) {
-                    const float v[6] = {ax[p].x, ay[p].x, az[p].x, ax[p].y, ay[p].y, az[p].y};
-#pragma unroll
-                    for (int k = 0; k < 6; k++)
-                        kahan_add(accw[(6 * p + k) * 32 + lane], accw[(3 * T + 6 * p + k) * 32 + lane], v[k]);
+                    kahan_add2(acc2[(3 * p + 0) * 32 + lane], acc2[(3 * TP + 3 * p + 0) * 32 + lane], ax[p]);
+                    kahan_add2(acc2[(3 * p + 1) * 32 + lane], acc2[(3 * TP + 3 * p + 1) * 32 + lane], ay[p]);
+                    kahan_add2(acc2[(3 * p + 2) * 32 + lane], acc2[(3 * TP + 3 * p + 2) * 32 + lane], az[p]);
                     ax[p] = ay[p] = az[p] = f2(0.f);
                 }
             }
@@ -1202,16 +1214,15 @@ __device__ __forceinline__ void mu_target(const P2PArgs &A, const int2 *ev, int 
     }
 #pragma unroll
     for (int p = 0; p < TP; p++) {
-        const float v[6] = {ax[p].x, ay[p].x, az[p].x, ax[p].y, ay[p].y, az[p].y};
-#pragma unroll
-        for (int k = 0; k < 6; k++)
-            kahan_add(accw[(6 * p + k) * 32 + lane], accw[(3 * T + 6 * p + k) * 32 + lane], v[k]);
+        kahan_add2(acc2[(3 * p + 0) * 32 + lane], acc2[(3 * TP + 3 * p + 0) * 32 + lane], ax[p]);
+        kahan_add2(acc2[(3 * p + 1) * 32 + lane], acc2[(3 * TP + 3 * p + 1) * 32 + lane], ay[p]);
+        kahan_add2(acc2[(3 * p + 2) * 32 + lane], acc2[(3 * TP + 3 * p + 2) * 32 + lane], az[p]);
     }
     __syncwarp();
     // targets: each lane takes one or two, summing its 4 source groups in order
     const double scale = A.boxes[A.boxid[t]].acc_scale;
     for (int tq = lane; tq < nt; tq += 32) {
-        const int tgq = tq / T, q = tq - tgq * T;
+        const int tgq = tq / T, q = tq - tgq * T, qp = q >> 1, qh = q & 1;
         float v[3], cmp[3];
 #pragma unroll
         for (int d = 0; d < 3; d++) {
@@ -1220,8 +1231,9 @@ __device__ __forceinline__ void mu_target(const P2PArgs &A, const int2 *ev, int 
 #pragma unroll
             for (int g = 0; g < 4; g++) {
                 const int l = tgq * 4 + g;
-                kahan_add(v[d], cmp[d], accw[(3 * q + d) * 32 + l]);
-                kahan_add(v[d], cmp[d], -accw[(3 * T + 3 * q + d) * 32 + l]);
+                const float2 sv = acc2[(3 * qp + d) * 32 + l], cv = acc2[(3 * TP + 3 * qp + d) * 32 + l];
+                kahan_add(v[d], cmp[d], qh ? sv.y : sv.x);
+                kahan_add(v[d], cmp[d], -(qh ? cv.y : cv.x));
             }
         }
         A.ax[it + tq] += ((double)v[0] - (double)cmp[0]) * scale;
@@ -1242,7 +1254,7 @@ __global__ void __launch_bounds__(MU_TB, MINB) k_p2p_mutual(P2PArgs A, const int
     __shared__ __align__(16) float4 s_src[MU_WARPS][2 * 64];  // two stages
     __shared__ __align__(16) MuEntry s_meta[MU_WARPS][32];
     __shared__ __align__(16) float s_red[MU_WARPS][MU_BATCH * 24];
-    __shared__ float s_acc[MU_WARPS][48 * 32];  // Kahan sum and compensation of up to 8 targets x 3, per lane
+    __shared__ __align__(16) float s_acc[MU_WARPS][48 * 32];  // Kahan sums and compensations, up to 8 targets x 3, per lane (read as float2)
     const int lane = warp_lane(), wib = threadIdx.x >> 5;
     SplitConsts K = A.k;
 
