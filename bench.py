@@ -43,7 +43,7 @@ FLOPS_PER_PAIR = 36
 # launch on the 128^3 workload of the same density, scaled by the particle
 # count (x8; traffic grows in proportion).  The capture command and figures
 # are kept with the kernel's profile summary.
-TRAFFIC_PER_LAUNCH_256 = {"k_p2p_mutual": 13.05e9, "k_p2p_split_packed": 1.27e9}
+TRAFFIC_PER_LAUNCH_256 = {"k_p2p_mutual": 13.08e9, "k_p2p_split_packed": 1.27e9}
 # MAXLEAF the GPU arm's autotuner picks for each workload on GB300 (the
 # fastest leaf within the 1e-4 median error bound); the CPU baselines run
 # the same leaf so that both arms compute the same lists at the same error
