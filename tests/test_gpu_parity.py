@@ -302,6 +302,20 @@ def test_fp64_mutual_matches_one_way(ph, ics, workload, nside, maxleaf):
     assert rel_err(mutual, one_way, p).max() <= 1e-12
 
 
+def test_pass_with_library_pinned_buffers(ph, ics):
+    """Host buffers from photons_host_alloc (ph.host_array) give the same
+    forces as any host array, and are released with the array."""
+    pos, p = ics.make("zeldovich256", nside=24, maxleaf=64)
+    fp = ph.ForcePass(0)
+    plain = fp.run(pos, p, precision=ph.FP32_SPLIT)
+    hp = ph.host_array(pos.shape)
+    hp[:] = pos
+    ha = ph.host_array(pos.shape)
+    fp.run(hp, p, precision=ph.FP32_SPLIT, out=ha)
+    assert np.array_equal(ha, plain)
+    del hp, ha
+
+
 def _full_size_parity(ph, fp, port, pos, p, precision, tol, nsub=10000):
     """The GPU pass against the oracle at a workload's full size: counters,
     the tree-order permutation, every list as a multiset, and the forces on

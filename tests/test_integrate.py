@@ -195,6 +195,57 @@ def test_kdk_steps_as_one_graph_match_the_steps_one_by_one(ph, ics, precision):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("precision,maxleaf", [("FP32_SPLIT", 48), ("FP64", 16)])
+def test_kdk_graph_step_whose_pass_outgrows_the_last_one(ph, ics, precision, maxleaf):
+    """The captured step's pass does not fit what the previous pass needed:
+    velocities toward the box centre gather the particles (each drift
+    shrinks their distances to the centre by a quarter), so the list
+    entries per leaf double from step to step and outgrow the mutual
+    kernel's reaction buffer (its first guess, or what the last pass needed
+    with 1/16 to spare).  The graph's second kick then stops itself and the
+    call repeats the pass with a larger buffer (more launches than a step
+    that fits, the last one here, which does not drift); positions,
+    velocities and accelerations still equal the steps launched one by one,
+    bit for bit.  Three drifts are as far as this input goes: on the fourth
+    the mean-split tree needs more than 2N/MAXLEAF nodes, the reference's
+    capacity."""
+    torch = pytest.importorskip("torch")
+    n = 32 ** 3
+    L = 64.0
+    p = ics.force_params(n, L, 128, theta=0.5, maxleaf=maxleaf)  # rcut 2.8
+    prec = getattr(ph, precision)
+    rng = np.random.default_rng(11)
+    pos = rng.uniform(0.25 * L, 0.75 * L, (n, 3))
+    dd = 0.01
+    vel = -(pos - 0.5 * L) / (4.0 * dd)
+    dkh = 1e-9  # the kicks stay tiny, so the motion is the drift's
+    fa, fb = ph.ForcePass(0), ph.ForcePass(0)
+    acc0 = fa.run(pos, p, precision=prec)
+    a = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in (pos, vel, acc0)]
+    b = [t.clone() for t in a]
+    stream = torch.cuda.current_stream()
+    fb.set_stream(stream.cuda_stream)
+    torch.cuda.synchronize()
+    count = ph.load_library().photons_launch_count
+    pairs, launches = [], []
+    for step, d in enumerate((dd, dd, dd, 0.0)):
+        l0 = count()
+        fa.kdk_step_device(*(t.data_ptr() for t in a), n, p, dkh, d, precision=prec)
+        launches.append(count() - l0)
+        c = fa.counters()
+        pairs.append(c["pairs_local"] + c["pairs_image"])
+        ph.kick(n, b[1].data_ptr(), b[2].data_ptr(), dkh, stream.cuda_stream)
+        ph.drift(n, b[0].data_ptr(), b[1].data_ptr(), d, L, stream.cuda_stream)
+        fb.run_device(b[0].data_ptr(), b[2].data_ptr(), n, p, precision=prec)
+        ph.kick(n, b[1].data_ptr(), b[2].data_ptr(), dkh, stream.cuda_stream)
+        torch.cuda.synchronize()
+        for x, y in zip(a, b):
+            assert torch.equal(x, y), step
+    assert pairs[1] > 1.5 * pairs[0] and pairs[2] > 1.5 * pairs[1] and pairs[3] == pairs[2]
+    assert launches[2] > launches[3]  # the repeated pass
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("maxleaf", [16, 64])
 def test_ordered_kdk_step_is_the_step_in_tree_order(ph, ics, maxleaf):
     """photons_kdk_step_ordered leaves pos, vel, acc and ids in the pass's
