@@ -597,7 +597,8 @@ def main():
         p["maxleaf"] = best
         one_way = bool(pflags & ph.F_ONE_WAY) or best < 48
         tune = {"chosen_maxleaf": best,
-                "chosen_kernel": "one-way" if one_way else "mutual shape %d" % ((pflags >> 8) & 15),
+                "chosen_kernel": "one-way" if one_way else "mutual shape %d%s" % (
+                    (pflags >> 8) & 15, ", sources by TMA bulk copies" if pflags & ph.F_P2P_BULK else ""),
                 "chosen_flags": pflags,
                 "error_bound_median": args.error_bound, "candidates": table,
                 "score": "fastest pass with median error vs the FP64 direct sum <= bound (2000-particle sample)"}

@@ -121,10 +121,12 @@ typedef struct photons_params {
 #define PHOTONS_F_MULTIPOLES 8      /* compute P2M/M2M even when no M2L task exists */
 #define PHOTONS_F_KEEP_LISTS 16     /* keep lists for photons_list_* */
 #define PHOTONS_F_ONE_WAY 32        /* FP32: every pair one way (no mutual pairs, no reaction slots) */
-/* FP32 mutual P2P kernel build (bits 8-11): 0 chosen by MAXLEAF; 1 three
-   blocks per SM, two dependency chains; 2 four blocks, one chain, 6-target
-   path; 3 three blocks, one chain; 4 four blocks, two chains.  The builds
-   give identical forces; the autotuner times them. */
+#define PHOTONS_F_P2P_BULK 64      /* FP32 mutual kernel: source leaves staged by TMA bulk copies */
+/* FP32 mutual P2P kernel build (bits 8-11): 0 the default (build 2); 1
+   three blocks per SM, two dependency chains; 2 four blocks, one chain,
+   6-target path; 3 three blocks, one chain; 4 four blocks, two chains.  The
+   builds give the same forces to FP32 rounding, either source staging
+   (PHOTONS_F_P2P_BULK) the same bits; the autotuner times them. */
 #define PHOTONS_F_P2P_SHAPE(s) ((s) << 8)
 #define PHOTONS_F_SHAPE_OF(f) (((f) >> 8) & 15)
 #define PHOTONS_P2P_SHAPES 5

@@ -32,6 +32,7 @@ F_NO_FARFIELD = 4
 F_MULTIPOLES = 8
 F_KEEP_LISTS = 16
 F_ONE_WAY = 32
+F_P2P_BULK = 64  # FP32 mutual kernel: source leaves staged by TMA bulk copies
 P2P_SHAPES = 5
 
 
@@ -619,8 +620,10 @@ def autotune_leaf(fp, pos, p, candidates=(16, 24, 32, 48, 64), error_bound=1e-4,
     (F_ONE_WAY), so both are timed there.  Kernel shape (with `shapes`): at
     the chosen leaf size, when the mutual kernel won, each of its builds
     (resident blocks per SM, interleaved dependency chains, the 6-target
-    path; F_P2P_SHAPE) is timed and the fastest kept.  All of these give the
-    same forces to FP32 rounding.
+    path; F_P2P_SHAPE), with source leaves staged by per-lane cp.async or by
+    TMA bulk copies (F_P2P_BULK), is timed and the fastest kept.  All of
+    these give the same forces to FP32 rounding (the two stagings, the same
+    bits).
 
     Returns (best_leaf, table, flags): table lists, per candidate, the pass
     time on the device (ms, CUDA events: tree, walk, P2P, far field,
@@ -660,7 +663,9 @@ def autotune_leaf(fp, pos, p, candidates=(16, 24, 32, 48, 64), error_bound=1e-4,
     best = min(ok, key=lambda t: t["ms"]) if ok else min(table, key=lambda t: t["median"])
     if shapes and precision == FP32_SPLIT and best["kernel"] == "mutual":
         leaf = best["maxleaf"]
-        for flags, kernel in [(F_P2P_SHAPE(sh), "mutual shape %d" % sh) for sh in range(1, P2P_SHAPES)]:
+        builds = [(F_P2P_SHAPE(sh) | bulk, "mutual shape %d%s" % (sh, " bulk" if bulk else ""))
+                  for sh in range(1, P2P_SHAPES) for bulk in (0, F_P2P_BULK)]
+        for flags, kernel in builds:
             row = trial(leaf, flags, kernel)
             if row["ms"] < best["ms"] and row["median"] <= max(error_bound, best["median"]):
                 best = row

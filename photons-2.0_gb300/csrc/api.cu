@@ -336,9 +336,17 @@ static long long mu_per_value(int precision) { return precision == PHOTONS_FP64 
 // whether an earlier pass had already grown the buffer.
 static bool mutual_feedback(photons_ctx *c, int over, long long need, int precision)
 {
-    if (!over || need <= c->mu_buf_cap / mu_per_value(precision)) return false;
+    if (!(over & 1) || need <= c->mu_buf_cap / mu_per_value(precision)) return false;
     c->hint_mubuf = need + need / 16 + 4096;
     return true;
+}
+
+// bit 1 of the mutual kernel's flag: a source-staging bulk copy did not
+// land within the kernel's time limit, and the warps that waited stopped
+static int mutual_status(int over)
+{
+    if (over & 2) return ph_set_error(PH_ERR_CUDA, "P2P source staging: a bulk copy did not complete in time");
+    return 0;
 }
 
 // Mutual pairs from leaf size 48.  At leaf 32 they win on near-uniform
@@ -767,6 +775,7 @@ int ph_stage_p2p(photons_ctx *c, int precision, int zero)
     a.k = ph::make_split_consts(c->pp);
     a.variant = p2p_variant();
     a.shape = PHOTONS_F_SHAPE_OF(c->pass_flags);
+    a.bulk = (c->pass_flags & PHOTONS_F_P2P_BULK) ? 1 : 0;
     PH_TRY(ph_record(c, EV_P2P_BEGIN));
     if (uses_mutual(c, precision)) {
         ph::MutualBufs m;
@@ -978,6 +987,7 @@ static int force_pass_graph(photons_ctx *c, int nbox, const photons_params *p, c
             grow_walk_caps(c, fl, p2p_cap, pd_cap, m2l_cap, stack_cap, stage_cap);
             continue;
         }
+        PH_TRY(mutual_status(mu_over));
         // the reaction total means something only once tree and lists are complete
         if (mutual_feedback(c, mu_over, mu_need, p->precision)) continue;
         c->info.depth_off.resize(c->info.depth + 2);
@@ -1107,6 +1117,7 @@ int ph_kdk_graph_step(photons_ctx *c, const photons_params *q, int n, double *po
         *done = KDK_PASS_AGAIN;
         return 0;
     }
+    PH_TRY(mutual_status(mu_over));
     if (mu_over) {
         mutual_feedback(c, mu_over, mu_need, q->precision);
         *done = KDK_PASS_AGAIN;
@@ -1212,6 +1223,7 @@ static int force_pass_boxes(photons_ctx *c, int nbox, const photons_params *p, c
             int mu_over = 0;
             PH_CUDA_CHECK(cudaMemcpy(&mu_need, c->mu_total, sizeof mu_need, cudaMemcpyDeviceToHost));
             PH_CUDA_CHECK(cudaMemcpy(&mu_over, c->mu_over, sizeof mu_over, cudaMemcpyDeviceToHost));
+            PH_TRY(mutual_status(mu_over));
             if (!mutual_feedback(c, mu_over, mu_need, p->precision)) break;
         }
     }

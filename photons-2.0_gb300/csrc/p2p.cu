@@ -1029,9 +1029,27 @@ __global__ void k_mu_slots(const int *tree_cnt, const unsigned long long *walk_f
 // target, scaled), source range, and where its reactions go
 struct MuEntry {
     float d0, d1, d2;
-    int is, ns, owned;
-    long long out;  // float offset of the pair's slot in the reaction buffer
+    int is, ns;
+    long long out;  // float offset of the pair's slot in the reaction buffer; -1: evaluated one way
 };
+
+// an entry as a warp keeps it in shared memory (24 bytes): ns (at most 64)
+// in the low byte of the slot offset
+struct MuMeta {
+    float d0, d1, d2;
+    int is;
+    long long on;
+};
+
+__device__ __forceinline__ MuMeta mu_pack(const MuEntry &E)
+{
+    return MuMeta{E.d0, E.d1, E.d2, E.is, (long long)((unsigned long long)E.out << 8) | E.ns};
+}
+
+__device__ __forceinline__ MuEntry mu_unpack(const MuMeta &M)
+{
+    return MuEntry{M.d0, M.d1, M.d2, M.is, (int)(M.on & 255), M.on >> 8};
+}
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 {
@@ -1048,9 +1066,69 @@ __device__ __forceinline__ void mu_issue(const float4 *__restrict__ pos4, const 
     if (lane + 32 < E.ns) cp_async16(buf + lane + 32, pos4 + E.is + lane + 32);
 }
 
-// once a lane's own copies have landed: scale and shift them in place
-// (relative to the target centre); padding is far away
-__device__ __forceinline__ void mu_place(const MuEntry &E, float4 *buf, float sig, int lane)
+// The same copy as one TMA bulk copy (cp.async.bulk): lane 0 arms the
+// stage's mbarrier with the byte count and issues the copy; the warp waits
+// on the barrier's phase.  A source leaf is contiguous in tree order, 16
+// bytes a particle, so the source address, the shared stage and the size
+// (16 ns bytes, at most 1 KB) are all multiples of 16.
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(bar)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
+
+// orders this thread's generic accesses to shared memory before later
+// bulk-copy writes to it
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
+__device__ __forceinline__ void mu_issue_bulk(const float4 *__restrict__ pos4, const MuEntry &E, float4 *buf,
+                                              unsigned long long *bar, int lane)
+{
+    if (lane != 0 || E.ns <= 0) return;
+    const unsigned bytes = 16u * (unsigned)E.ns, b = smem_addr(bar);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(b), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                     smem_addr(buf)),
+                 "l"(pos4 + E.is), "r"(bytes), "r"(b)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(unsigned long long *bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(ok)
+                 : "r"(smem_addr(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+    return t;
+}
+
+// waits for the barrier's phase; gives up after two seconds of global time
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity)
+{
+    if (mbar_try(bar, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    for (unsigned i = 1;; i++) {
+        if (mbar_try(bar, parity)) return true;
+        if ((i & 63u) == 0 && global_ns() - t0 > 2000000000ull) return false;
+    }
+}
+
+// once the copies have landed: scale and shift them (relative to the
+// target centre) from raw into buf, which may be the same stage; padding is
+// far away
+__device__ __forceinline__ void mu_place(const MuEntry &E, const float4 *raw, float4 *buf, float sig, int lane)
 {
     const float far = 1e18f;
 #pragma unroll
@@ -1058,7 +1136,7 @@ __device__ __forceinline__ void mu_place(const MuEntry &E, float4 *buf, float si
         const int j = lane + 32 * h;
         float4 v = make_float4(far, far, far, 0.f);
         if (j < E.ns) {
-            const float4 o = buf[j];
+            const float4 o = raw[j];
             v = make_float4(fmaf(o.x, sig, E.d0), fmaf(o.y, sig, E.d1), fmaf(o.z, sig, E.d2), 0.f);
         }
         buf[j] = v;
@@ -1069,12 +1147,16 @@ __device__ __forceinline__ void mu_place(const MuEntry &E, float4 *buf, float si
 // particles, 4: up to 32), eight target groups x four source groups.
 // Entries come in batches of 32: each lane loads one entry's metadata into
 // shared memory, then the warp walks the batch with the next entry's
-// sources in flight (cp.async into the second stage) while it evaluates
-// the current one.
-template <int T, int ILR>
-__device__ __forceinline__ void mu_target(const P2PArgs &A, const int2 *ev, int ne, const long long *rbase,
+// sources in flight (into the second stage) while it evaluates the current
+// one.  BULK: one TMA bulk copy per entry into the stage, completing on
+// that stage's mbarrier (bars[c], its phase parity in bit c of phase); else
+// per-lane cp.async.  Returns false if a bulk copy did not land within the
+// wait's time limit (bit 1 set in *fail).
+template <int T, int ILR, bool BULK>
+__device__ __forceinline__ bool mu_target(const P2PArgs &A, const int2 *ev, int ne, const long long *rbase,
                                           float *rbuf, int t, int nt, int it, const SplitConsts &K, float Lhi,
-                                          float Llo, float4 *src, MuEntry *meta, float *red, float *accw, int lane)
+                                          float Llo, float4 *src, MuMeta *meta, float *red, float *accw,
+                                          unsigned long long *bars, unsigned &phase, int *fail, int lane)
 {
     constexpr int TP = T / 2;  // target pairs per lane
     const int tg = lane >> 2, sg = lane & 3;
@@ -1119,24 +1201,47 @@ __device__ __forceinline__ void mu_target(const P2PArgs &A, const int2 *ev, int 
             m.d2 = centre_diff(csh.z, csl.z, cth.z, ctl.z, mk, Lhi, Llo) * K.sig;
             m.is = A.ipart[s];
             m.ns = A.npart[s];
-            m.owned = en.y >= 0;
-            m.out = en.y >= 0 ? rbase[s] + (long long)en.y * mu_row(m.ns) * 3 : 0;
-            meta[lane] = m;
+            m.out = en.y >= 0 ? rbase[s] + (long long)en.y * mu_row(m.ns) * 3 : -1;
+            meta[lane] = mu_pack(m);
         }
         __syncwarp();
         int cur = 0;
-        mu_issue(A.pos4, meta[0], src, lane);
-        cp_async_commit();
-        for (int kk = 0; kk < kmax; kk++) {
-            const MuEntry E = meta[kk];
-            float4 *stage = src + 64 * cur;
-            if (kk + 1 < kmax) mu_issue(A.pos4, meta[kk + 1], src + 64 * (cur ^ 1), lane);
+        if constexpr (BULK) {
+            mu_issue_bulk(A.pos4, mu_unpack(meta[0]), src, bars, lane);
+        } else {
+            mu_issue(A.pos4, mu_unpack(meta[0]), src, lane);
             cp_async_commit();
-            cp_async_wait_prev();
-            mu_place(E, stage, K.sig, lane);
+        }
+        for (int kk = 0; kk < kmax; kk++) {
+            const MuEntry E = mu_unpack(meta[kk]);
+            float4 *stage = src + 64 * cur;
+            if constexpr (BULK) {
+                // the next entry's copy goes to the other stage (mbarrier
+                // bars[cur ^ 1]) before this one's is awaited
+                if (kk + 1 < kmax) mu_issue_bulk(A.pos4, mu_unpack(meta[kk + 1]), src + 64 * (cur ^ 1),
+                                                 bars + (cur ^ 1), lane);
+                if (E.ns > 0) {
+                    // one answer for the warp, so that it stops or goes on as a whole
+                    if (!__all_sync(0xffffffffu, mbar_wait(bars + cur, (phase >> cur) & 1u))) {
+                        // a copy that never landed: record it, give the other
+                        // stage's copy its own time limit, and stop this warp
+                        if (lane == 0) atomicOr(fail, 2);
+                        if (kk + 1 < kmax && mu_unpack(meta[kk + 1]).ns > 0)
+                            mbar_wait(bars + (cur ^ 1), (phase >> (cur ^ 1)) & 1u);
+                        return false;
+                    }
+                    phase ^= 1u << cur;
+                }
+                mu_place(E, stage, stage, K.sig, lane);
+            } else {
+                if (kk + 1 < kmax) mu_issue(A.pos4, mu_unpack(meta[kk + 1]), src + 64 * (cur ^ 1), lane);
+                cp_async_commit();
+                cp_async_wait_prev();
+                mu_place(E, stage, stage, K.sig, lane);
+            }
             __syncwarp();
             const int ns = E.ns;
-            const bool owned = E.owned;
+            const bool owned = E.out >= 0;
             for (int c0 = 0; c0 < ns; c0 += MU_BATCH) {
                 // the batch's sources spread evenly over the four source groups
                 const int nr = min(MU_BATCH / 4, (ns - c0 + 3) >> 2);
@@ -1208,6 +1313,8 @@ __device__ __forceinline__ void mu_target(const P2PArgs &A, const int2 *ev, int 
                     ax[p] = ay[p] = az[p] = f2(0.f);
                 }
             }
+            // the stage is rewritten by a bulk copy in the next entry
+            if constexpr (BULK) fence_proxy_async();
             __syncwarp();
             cur ^= 1;
         }
@@ -1241,22 +1348,33 @@ __device__ __forceinline__ void mu_target(const P2PArgs &A, const int2 *ev, int 
         A.az[it + tq] += ((double)v[2] - (double)cmp[2]) * scale;
     }
     __syncwarp();
+    return true;
 }
 
-template <int MINB, int ILR, bool T6>
+template <int MINB, int ILR, bool T6, bool BULK>
 __global__ void __launch_bounds__(MU_TB, MINB) k_p2p_mutual(P2PArgs A, const int2 *ev, const int *nev,
-                                                            const long long *rbase, float *rbuf)
+                                                            const long long *rbase, float *rbuf, int *fail)
 {
     // shared layouts avoid bank conflicts: a batch's source k (of 32) is
     // read by source group k % 4, so the four groups read adjacent float4s;
     // reactions [source][component][target group] with a 24-word source
     // stride; running sums [value][lane].  12 KB per warp.
     __shared__ __align__(16) float4 s_src[MU_WARPS][2 * 64];  // two stages
-    __shared__ __align__(16) MuEntry s_meta[MU_WARPS][32];
+    __shared__ __align__(16) MuMeta s_meta[MU_WARPS][32];
     __shared__ __align__(16) float s_red[MU_WARPS][MU_BATCH * 24];
     __shared__ __align__(16) float s_acc[MU_WARPS][48 * 32];  // Kahan sums and compensations, up to 8 targets x 3, per lane (read as float2)
+    __shared__ __align__(8) unsigned long long s_bar[MU_WARPS][2];  // the stages' mbarriers (BULK)
     const int lane = warp_lane(), wib = threadIdx.x >> 5;
     SplitConsts K = A.k;
+    unsigned phase = 0;
+    if constexpr (BULK) {
+        if (lane == 0) {
+            mbar_init(&s_bar[wib][0]);
+            mbar_init(&s_bar[wib][1]);
+            mbar_init_fence();
+        }
+        __syncwarp();
+    }
 
     const int nleaf = p2p_targets(A);
     for (;;) {
@@ -1276,15 +1394,17 @@ __global__ void __launch_bounds__(MU_TB, MINB) k_p2p_mutual(P2PArgs A, const int
         // the narrow build gives leaves of 33-48 particles 6 targets per lane
         // (48 slots; 128^3 NFW at leaf 48: 39.4 against 47.4 ms with 64);
         // in the wide build the extra path cost 1.3 % at 256^3 leaf 64
+        bool ok;
         if (nt > 48 || (nt > 32 && !T6))
-            mu_target<8, ILR>(A, evt, ne, rbase, rbuf, t, nt, it, K, B.Lhi, B.Llo, s_src[wib], s_meta[wib], s_red[wib],
-                         s_acc[wib], lane);
+            ok = mu_target<8, ILR, BULK>(A, evt, ne, rbase, rbuf, t, nt, it, K, B.Lhi, B.Llo, s_src[wib], s_meta[wib],
+                                         s_red[wib], s_acc[wib], s_bar[wib], phase, fail, lane);
         else if (nt > 32)
-            mu_target<6, ILR>(A, evt, ne, rbase, rbuf, t, nt, it, K, B.Lhi, B.Llo, s_src[wib], s_meta[wib], s_red[wib],
-                         s_acc[wib], lane);
+            ok = mu_target<6, ILR, BULK>(A, evt, ne, rbase, rbuf, t, nt, it, K, B.Lhi, B.Llo, s_src[wib], s_meta[wib],
+                                         s_red[wib], s_acc[wib], s_bar[wib], phase, fail, lane);
         else
-            mu_target<4, ILR>(A, evt, ne, rbase, rbuf, t, nt, it, K, B.Lhi, B.Llo, s_src[wib], s_meta[wib], s_red[wib],
-                         s_acc[wib], lane);
+            ok = mu_target<4, ILR, BULK>(A, evt, ne, rbase, rbuf, t, nt, it, K, B.Lhi, B.Llo, s_src[wib], s_meta[wib],
+                                         s_red[wib], s_acc[wib], s_bar[wib], phase, fail, lane);
+        if (!ok) return;
     }
 }
 
@@ -1646,6 +1766,25 @@ int launch_leaf_offsets(const BuildBufs &b, const TreeBufs &t, float4 *pos4, cud
     return 0;
 }
 
+template <int MINB, int ILR, bool T6, bool BULK>
+static int launch_mutual_one(const P2PArgs &a, const MutualBufs &m, int sms, cudaStream_t st)
+{
+    ph::note_launch(), k_p2p_mutual<MINB, ILR, T6, BULK><<<sms * MINB, MU_TB, 0, st>>>(a, m.ev, m.nev, m.rbase, m.buf,
+                                                                                      m.over);
+    return 0;
+}
+
+template <bool BULK>
+static int launch_mutual_build(const P2PArgs &a, const MutualBufs &m, int shape, int sms, cudaStream_t st)
+{
+    switch (shape) {
+    case 1: return launch_mutual_one<3, 2, false, BULK>(a, m, sms, st);
+    case 2: return launch_mutual_one<4, 1, true, BULK>(a, m, sms, st);
+    case 3: return launch_mutual_one<3, 1, false, BULK>(a, m, sms, st);
+    default: return launch_mutual_one<4, 2, true, BULK>(a, m, sms, st);
+    }
+}
+
 int launch_p2p_mutual(const P2PArgs &a, const MutualBufs &m, int fp64, cudaStream_t st)
 {
     PH_CUDA_CHECK(cudaMemsetAsync(a.work_counter, 0, sizeof(int), st));
@@ -1667,25 +1806,14 @@ int launch_p2p_mutual(const P2PArgs &a, const MutualBufs &m, int fp64, cudaStrea
         PH_CUDA_CHECK(cudaGetLastError());
         return 0;
     }
-    // the build: shape 0 picks by MAXLEAF (three blocks per SM with two
-    // chains from leaf 60, else four blocks with one chain and the 6-target
-    // path); 1-4 name a build for the autotuner (PHOTONS_F_P2P_SHAPE)
+    // the build: shape 0 is build 2 (four blocks per SM, one chain, the
+    // 6-target path: 256^3 leaf 64 P2P phase 60.3 ms against 61.6 for build
+    // 1); 1-4 name a build for the autotuner (PHOTONS_F_P2P_SHAPE)
     int shape = a.shape;
-    if (shape == 0) shape = m.maxleaf >= 60 ? 1 : 2;
-    switch (shape) {
-    case 1:
-        ph::note_launch(), k_p2p_mutual<3, 2, false><<<sms * 3, MU_TB, 0, st>>>(a, m.ev, m.nev, m.rbase, m.buf);
-        break;
-    case 2:
-        ph::note_launch(), k_p2p_mutual<4, 1, true><<<sms * 4, MU_TB, 0, st>>>(a, m.ev, m.nev, m.rbase, m.buf);
-        break;
-    case 3:
-        ph::note_launch(), k_p2p_mutual<3, 1, false><<<sms * 3, MU_TB, 0, st>>>(a, m.ev, m.nev, m.rbase, m.buf);
-        break;
-    default:
-        ph::note_launch(), k_p2p_mutual<4, 2, true><<<sms * 4, MU_TB, 0, st>>>(a, m.ev, m.nev, m.rbase, m.buf);
-        break;
-    }
+    if (shape == 0) shape = 2;
+    const int rc = a.bulk ? launch_mutual_build<true>(a, m, shape, sms, st)
+                          : launch_mutual_build<false>(a, m, shape, sms, st);
+    if (rc) return rc;
     ph::note_launch(), k_mu_gather<<<sms * 3, 256, 0, st>>>(a, m.slot, m.nrecv, m.rbase, m.buf);
     PH_CUDA_CHECK(cudaGetLastError());
     return 0;

@@ -39,6 +39,7 @@ struct P2PArgs {
     SplitConsts k;                  // scalar kernel: all fields; packed: the polynomial coefficients
     int variant;  // FP32: 0 packed (default), 1 scalar
     int shape;    // mutual kernel build (0: by MAXLEAF; see launch_p2p_mutual)
+    int bulk;     // mutual kernel: stage source leaves with TMA bulk copies (else per-lane cp.async)
 };
 
 // buffers of the mutual kernels, FP32 and FP64 (see launch_p2p_mutual)
@@ -49,7 +50,8 @@ struct MutualBufs {
     long long *total;        // device: floats needed
     long long *scan_scratch;
     int *slot;               // per pool entry: owner rank, -2 received, -1 one way
-    int *over;               // device: 1 if the reaction buffer was too small (all one way)
+    int *over;               // device: bit 0 the reaction buffer was too small (all one way);
+                             // bit 1 a source-staging copy did not land in time (pass failed)
     float *buf;              // reactions (FP64 passes: doubles over the same bytes)
     long long buf_cap;       // reaction values that fit (floats, or doubles in an FP64 pass)
     int cap_leaves;

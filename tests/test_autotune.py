@@ -113,20 +113,26 @@ def test_fp64_times_one_kernel_per_leaf(ph, setup):
 
 def test_kernel_builds_timed_at_the_chosen_leaf(ph, setup):
     """With shapes on, a mutual-kernel choice is re-timed in every build of
-    that kernel and the fastest within the bound wins; a one-way choice is
-    not re-timed."""
+    that kernel, with either source staging (cp.async or TMA bulk copies),
+    and the fastest within the bound wins; a one-way choice is not
+    re-timed."""
     pos, truth, p = setup
     ow = ph.F_ONE_WAY
     ms = {(32, 0): 9.0, (64, 0): 5.0, (64, ow): 7.0}
     err = {(32, 0): 9e-5, (64, 0): 2e-5, (64, ow): 2e-5}
     for sh in range(1, ph.P2P_SHAPES):
-        ms[(64, ph.F_P2P_SHAPE(sh))] = 5.0 + 0.1 * sh
-        err[(64, ph.F_P2P_SHAPE(sh))] = 2e-5
+        for bulk in (0, ph.F_P2P_BULK):
+            ms[(64, ph.F_P2P_SHAPE(sh) | bulk)] = 5.0 + 0.1 * sh + (0.05 if bulk else 0.0)
+            err[(64, ph.F_P2P_SHAPE(sh) | bulk)] = 2e-5
     ms[(64, ph.F_P2P_SHAPE(3))] = 4.2
     fp = StandInPass(truth, ms, err)
     best, table, flags = ph.autotune_leaf(fp, pos, p, candidates=(32, 64), sample=100, repeats=1)
     assert (best, flags) == (64, ph.F_P2P_SHAPE(3))
     assert {k for k, _ in fp.runs} == set(ms)
+    ms[(64, ph.F_P2P_SHAPE(4) | ph.F_P2P_BULK)] = 4.1
+    fp = StandInPass(truth, ms, err)
+    best, table, flags = ph.autotune_leaf(fp, pos, p, candidates=(32, 64), sample=100, repeats=1)
+    assert (best, flags) == (64, ph.F_P2P_SHAPE(4) | ph.F_P2P_BULK)
     ms2 = {(32, 0): 3.0}
     fp = StandInPass(truth, ms2, {(32, 0): 9e-5})
     best, _, flags = ph.autotune_leaf(fp, pos, p, candidates=(32,), sample=100, repeats=1)

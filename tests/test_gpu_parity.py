@@ -159,9 +159,9 @@ def test_mutual_pairs_match_one_way(ph, ics, monkeypatch, workload, nside, maxle
     """The FP32 kernel that evaluates each symmetric leaf pair (local or
     periodic image) once, reactions through a buffer, against the one-way
     kernel and the FP64 pass: the same forces to FP32 rounding,
-    deterministic from pass to pass.  Covers both builds (leaf 60+ and
-    below), the 48-slot tile (halo leaves of 33-48 particles) and lists
-    too long to pair."""
+    deterministic from pass to pass.  Covers the default build at leaf
+    48-64, the 48-slot tile (halo leaves of 33-48 particles) and lists too
+    long to pair (every build: the next test)."""
     pos, p = ics.make(workload, nside=nside, maxleaf=maxleaf)
     fp = ph.ForcePass(0)
     a64 = fp.run(pos, p, precision=ph.FP64)
@@ -197,6 +197,20 @@ def test_every_p2p_build_gives_the_same_forces(ph, ics, workload, nside, maxleaf
         assert np.median(rel_err(a, base, p)) <= 1e-6, shape
     with pytest.raises(ph.PhotonsError, match="shape"):
         fp.run(pos, p, precision=ph.FP32_SPLIT, flags=ph.F_P2P_SHAPE(ph.P2P_SHAPES))
+    fp.close()
+
+
+@pytest.mark.parametrize("workload,nside,maxleaf", [("zeldovich256", 32, 64), ("nfw128", 32, 48)])
+def test_bulk_staged_sources_give_the_same_forces(ph, ics, workload, nside, maxleaf):
+    """Source leaves staged by TMA bulk copies (one copy per entry,
+    completing on the stage's mbarrier) or by per-lane cp.async: the same
+    bytes reach shared memory, so every build gives bit-identical forces."""
+    pos, p = ics.make(workload, nside=nside, maxleaf=maxleaf)
+    fp = ph.ForcePass(0)
+    for shape in range(ph.P2P_SHAPES):
+        a = fp.run(pos, p, precision=ph.FP32_SPLIT, flags=ph.F_P2P_SHAPE(shape))
+        b = fp.run(pos, p, precision=ph.FP32_SPLIT, flags=ph.F_P2P_SHAPE(shape) | ph.F_P2P_BULK)
+        assert np.array_equal(a, b), shape
     fp.close()
 
 
