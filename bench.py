@@ -43,7 +43,7 @@ FLOPS_PER_PAIR = 36
 # launch on the 128^3 workload of the same density, scaled by the particle
 # count (x8; traffic grows in proportion).  The capture command and figures
 # are kept with the kernel's profile summary.
-TRAFFIC_PER_LAUNCH_256 = {"k_p2p_mutual": 13.08e9, "k_p2p_split_packed": 1.27e9}
+TRAFFIC_PER_LAUNCH_256 = {"k_p2p_mutual": 13.12e9, "k_p2p_split_packed": 1.27e9}
 # MAXLEAF the GPU arm's autotuner picks for each workload on GB300 (the
 # fastest leaf within the 1e-4 median error bound); the CPU baselines run
 # the same leaf so that both arms compute the same lists at the same error
@@ -69,6 +69,9 @@ def parse():
                          "L=1000 at 512^3; nfw128: 50%% uniform + 50%% in NFW halos, L=200 at 128^3; "
                          "boxes256: 256 independent Plummer + uniform boxes of 16^3-64^3 particles in one pass")
     ap.add_argument("--kdk", action="store_true", help="also time device-resident kick-drift-kick steps")
+    ap.add_argument("--pass-flags", type=int, default=0,
+                    help="with --maxleaf: PHOTONS_F_* flags of the timed pass (e.g. 512: mutual build 2, "
+                         "64: sources staged by TMA bulk copies)")
     return ap.parse_args()
 
 
@@ -589,7 +592,9 @@ def main():
     fp = ph.ForcePass(local)
     tuned = None
     tune = None
-    pflags = 0  # the autotuner's kernel choice: PHOTONS_F_ONE_WAY, or the mutual kernel's build (shape bits)
+    # the autotuner's kernel choice (PHOTONS_F_ONE_WAY, or the mutual kernel's
+    # build and staging), else the caller's
+    pflags = args.pass_flags
     if not args.maxleaf:
         best, table, pflags = ph.autotune_leaf(fp, pos, p, error_bound=args.error_bound)
         best = broadcast_from_rank0(best, dist, "cuda")  # every replica runs rank 0's choice
