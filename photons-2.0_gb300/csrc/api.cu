@@ -325,6 +325,16 @@ static int p2p_variant()
     return 2;
 }
 
+// Test hook for the time limit of the bulk-staging waits: with
+// PHOTONS_TEST_STAGE_SHORTFALL=1 each bulk copy's mbarrier is armed for 16
+// bytes more than the copy brings, so every staging wait runs out (after
+// two seconds) and the pass fails with an error; the context stays usable.
+static int stage_shortfall()
+{
+    const char *v = getenv("PHOTONS_TEST_STAGE_SHORTFALL");
+    return v && !strcmp(v, "1") ? 16 : 0;
+}
+
 // floats per reaction value: an FP64 pass keeps doubles in the float buffer
 static long long mu_per_value(int precision) { return precision == PHOTONS_FP64 ? 2 : 1; }
 
@@ -776,6 +786,7 @@ int ph_stage_p2p(photons_ctx *c, int precision, int zero)
     a.variant = p2p_variant();
     a.shape = PHOTONS_F_SHAPE_OF(c->pass_flags);
     a.bulk = (c->pass_flags & PHOTONS_F_P2P_BULK) ? 1 : 0;
+    a.stage_extra = stage_shortfall();
     PH_TRY(ph_record(c, EV_P2P_BEGIN));
     if (uses_mutual(c, precision)) {
         ph::MutualBufs m;
@@ -867,6 +878,7 @@ static PassKey pass_key(photons_ctx *c, const photons_params *p, int n, const do
     memset(&k, 0, sizeof k);
     k.n = n; k.nbox = c->b.nbox; k.levels = levels; k.top = tree_top(c, n, levels); k.maxleaf = p->maxleaf; k.precision = p->precision; k.flags = p->flags;
     k.dio = dio; k.variant = p2p_variant(); k.nwarps = c->w.nwarps; k.mask = mask;
+    k.stage_extra = stage_shortfall();
     k.boxsize = p->boxsize; k.theta = p->theta; k.rs = p->rs; k.rcut = p->rcut; k.eps = p->eps; k.mass = p->mass;
     k.pos = dio ? (const void *)pos : nullptr;
     k.acc = dio ? (const void *)acc : nullptr;

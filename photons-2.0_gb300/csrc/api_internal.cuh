@@ -30,7 +30,7 @@ enum {
 // Everything a captured pass bakes in; a pass with a different key is
 // captured anew.  Zero-filled before use so it compares with memcmp.
 struct PassKey {
-    int n, nbox, levels, top, maxleaf, precision, flags, dio, variant, nwarps;
+    int n, nbox, levels, top, maxleaf, precision, flags, dio, variant, nwarps, stage_extra;
     unsigned mask;
     double boxsize, theta, rs, rcut, eps, mass;
     const void *pos, *acc;

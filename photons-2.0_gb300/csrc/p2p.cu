@@ -1084,12 +1084,15 @@ __device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier
 // bulk-copy writes to it
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
 
+// (extra: bytes the barrier expects beyond the copy, 0 but in the test of
+// the wait's time limit)
 __device__ __forceinline__ void mu_issue_bulk(const float4 *__restrict__ pos4, const MuEntry &E, float4 *buf,
-                                              unsigned long long *bar, int lane)
+                                              unsigned long long *bar, int lane, int extra)
 {
     if (lane != 0 || E.ns <= 0) return;
     const unsigned bytes = 16u * (unsigned)E.ns, b = smem_addr(bar);
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(b), "r"(bytes) : "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(b), "r"(bytes + (unsigned)extra)
+                 : "memory");
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
                      smem_addr(buf)),
                  "l"(pos4 + E.is), "r"(bytes), "r"(b)
@@ -1207,7 +1210,7 @@ __device__ __forceinline__ bool mu_target(const P2PArgs &A, const int2 *ev, int 
         __syncwarp();
         int cur = 0;
         if constexpr (BULK) {
-            mu_issue_bulk(A.pos4, mu_unpack(meta[0]), src, bars, lane);
+            mu_issue_bulk(A.pos4, mu_unpack(meta[0]), src, bars, lane, A.stage_extra);
         } else {
             mu_issue(A.pos4, mu_unpack(meta[0]), src, lane);
             cp_async_commit();
@@ -1219,7 +1222,7 @@ __device__ __forceinline__ bool mu_target(const P2PArgs &A, const int2 *ev, int 
                 // the next entry's copy goes to the other stage (mbarrier
                 // bars[cur ^ 1]) before this one's is awaited
                 if (kk + 1 < kmax) mu_issue_bulk(A.pos4, mu_unpack(meta[kk + 1]), src + 64 * (cur ^ 1),
-                                                 bars + (cur ^ 1), lane);
+                                                 bars + (cur ^ 1), lane, A.stage_extra);
                 if (E.ns > 0) {
                     // one answer for the warp, so that it stops or goes on as a whole
                     if (!__all_sync(0xffffffffu, mbar_wait(bars + cur, (phase >> cur) & 1u))) {

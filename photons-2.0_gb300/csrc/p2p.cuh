@@ -40,6 +40,7 @@ struct P2PArgs {
     int variant;  // FP32: 0 packed (default), 1 scalar
     int shape;    // mutual kernel build (0: by MAXLEAF; see launch_p2p_mutual)
     int bulk;     // mutual kernel: stage source leaves with TMA bulk copies (else per-lane cp.async)
+    int stage_extra;  // bytes each bulk copy's mbarrier expects beyond the copy (0; a test sets 16)
 };
 
 // buffers of the mutual kernels, FP32 and FP64 (see launch_p2p_mutual)

@@ -214,6 +214,26 @@ def test_bulk_staged_sources_give_the_same_forces(ph, ics, workload, nside, maxl
     fp.close()
 
 
+def test_bulk_staging_wait_has_a_time_limit(ph, ics, monkeypatch):
+    """A bulk copy whose mbarrier never completes (the test hook arms it for
+    16 bytes more than the copy brings): every staging wait gives up after
+    its two-second limit, the pass fails with an error instead of hanging,
+    and the context then runs the same pass correctly."""
+    import time
+
+    pos, p = ics.make("zeldovich256", nside=16, maxleaf=64)
+    fp = ph.ForcePass(0)
+    good = fp.run(pos, p, precision=ph.FP32_SPLIT, flags=ph.F_P2P_BULK)
+    monkeypatch.setenv("PHOTONS_TEST_STAGE_SHORTFALL", "1")
+    t0 = time.time()
+    with pytest.raises(ph.PhotonsError, match="bulk copy did not complete"):
+        fp.run(pos, p, precision=ph.FP32_SPLIT, flags=ph.F_P2P_BULK)
+    assert time.time() - t0 < 60
+    monkeypatch.delenv("PHOTONS_TEST_STAGE_SHORTFALL")
+    assert np.array_equal(fp.run(pos, p, precision=ph.FP32_SPLIT, flags=ph.F_P2P_BULK), good)
+    fp.close()
+
+
 def test_mutual_pairs_graph_and_stage_paths_agree(ph, ics, monkeypatch):
     """The mutual kernel inside the captured graph and launched stage by
     stage (where the reaction buffer is sized between the stages) agree
