@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
+#include <cstddef>
 #include <cstdio>
 #include <cstdlib>
 #include <cstdint>
@@ -302,6 +303,43 @@ static void free_all(photons_ctx *c)
 // ------------------------------------------------------------------
 namespace {
 
+// a copy between device memory and pinned host memory that the device
+// addresses directly (over the host link); 16-byte elements where both
+// pointers allow, else 8-byte ones
+__global__ void k_copy_host(const double *__restrict__ src, double *__restrict__ dst, size_t count)
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x, t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0) {
+        const double2 *s2 = reinterpret_cast<const double2 *>(src);
+        double2 *d2 = reinterpret_cast<double2 *>(dst);
+        const size_t n2 = count / 2;
+        size_t i = t;
+        for (; i + 3 * stride < n2; i += 4 * stride) {
+            const double2 a = s2[i], b = s2[i + stride], c = s2[i + 2 * stride], d = s2[i + 3 * stride];
+            d2[i] = a; d2[i + stride] = b; d2[i + 2 * stride] = c; d2[i + 3 * stride] = d;
+        }
+        for (; i < n2; i += stride) d2[i] = s2[i];
+        if (t == 0 && (count & 1)) dst[count - 1] = src[count - 1];
+    } else {
+        for (size_t i = t; i < count; i += stride) dst[i] = src[i];
+    }
+}
+
+// the pass's counters into the host-side report (one block)
+__global__ void k_pass_report(const int *cnt, const unsigned long long *wc, const int *depth_off, int ndepth_off,
+                              const long long *mu_total, const int *mu_over, PassReport *out)
+{
+    const int t = threadIdx.x;
+    if (t < ph::BC_NCOUNTERS) out->cnt[t] = cnt[t];
+    if (t < ph::WC_N) out->wc[t] = wc[t];
+    for (int i = t; i < ndepth_off; i += blockDim.x) out->depth_off[i] = depth_off[i];
+    if (t == 0) {
+        out->mu_need = mu_total ? *mu_total : 0;
+        out->mu_over = mu_over ? *mu_over : 0;
+        out->ndepth_off = ndepth_off;
+    }
+}
+
 __global__ void k_gather_out(const int *perm, const double *ax, const double *ay, const double *az, int n, double *out,
                              int tree_order)
 {
@@ -314,6 +352,99 @@ __global__ void k_gather_out(const int *perm, const double *ax, const double *ay
 }
 
 }  // namespace
+
+// The device address of a host buffer of `bytes` bytes when the whole range
+// is pinned host memory mapped for this device (cudaHostAlloc, or host
+// memory registered with the runtime), else null.
+static const void *mapped_host(const void *p, size_t bytes)
+{
+    if (!p || !bytes) return nullptr;
+    cudaPointerAttributes a0, a1;
+    const char *q = static_cast<const char *>(p);
+    if (cudaPointerGetAttributes(&a0, q) != cudaSuccess || cudaPointerGetAttributes(&a1, q + bytes - 1) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer || !a1.devicePointer)
+        return nullptr;
+    if (static_cast<const char *>(a1.devicePointer) - static_cast<const char *>(a0.devicePointer) != (ptrdiff_t)(bytes - 1))
+        return nullptr;
+    return a0.devicePointer;
+}
+
+// Host <-> device copies of a pass's positions and accelerations.  Pinned
+// host buffers that the device addresses are copied by a kernel over the
+// host link, at the copy engines' rate (211 / 193 GB/s at 256^3); the copy
+// engines' own copies stall for tens of milliseconds a few times a second
+// for minutes after another process has freed large device allocations,
+// and the kernel's do not.  Other host memory goes through cudaMemcpyAsync.
+static int ph_copy_host(photons_ctx *c, double *dst, const double *src, size_t count, bool to_device)
+{
+    const size_t bytes = sizeof(double) * count;
+    const void *m = mapped_host(to_device ? static_cast<const void *>(src) : static_cast<const void *>(dst), bytes);
+    if (!m) {
+        PH_CUDA_CHECK(cudaMemcpyAsync(dst, src, bytes, to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost,
+                                      c->stream));
+        return 0;
+    }
+    const double *s = to_device ? static_cast<const double *>(m) : src;
+    double *d = to_device ? dst : static_cast<double *>(const_cast<void *>(m));
+    ph::note_launch(), k_copy_host<<<ph::device_sm_count() * 4, 512, 0, c->stream>>>(s, d, count);
+    PH_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
+// the context's pinned host report and a box staging area of >= nbox entries
+static int ensure_host_link(photons_ctx *c, int nbox)
+{
+    void *d = nullptr;
+    if (!c->ev_hlink) PH_CUDA_CHECK(cudaEventCreateWithFlags(&c->ev_hlink, cudaEventDisableTiming));
+    if (!c->rep) {
+        PH_CUDA_CHECK(cudaHostAlloc(reinterpret_cast<void **>(&c->rep), sizeof(PassReport),
+                                    cudaHostAllocPortable | cudaHostAllocMapped));
+        PH_CUDA_CHECK(cudaHostGetDevicePointer(&d, c->rep, 0));
+        c->rep_dev = static_cast<PassReport *>(d);
+    }
+    if (c->hbox_cap < nbox) {
+        PH_CUDA_CHECK(cudaEventSynchronize(c->ev_hlink));
+        if (c->hbox) cudaFreeHost(c->hbox);
+        c->hbox = nullptr;
+        c->hbox_dev = nullptr;
+        c->hbox_cap = 0;
+        PH_CUDA_CHECK(cudaHostAlloc(reinterpret_cast<void **>(&c->hbox), sizeof(BoxParams) * (size_t)nbox,
+                                    cudaHostAllocPortable | cudaHostAllocMapped));
+        PH_CUDA_CHECK(cudaHostGetDevicePointer(&d, c->hbox, 0));
+        c->hbox_dev = static_cast<BoxParams *>(d);
+        c->hbox_cap = nbox;
+    }
+    return 0;
+}
+
+// the pass's counters into c->rep (read them after the stream has finished)
+static int ph_enqueue_report(photons_ctx *c, int ndepth_off)
+{
+    PH_TRY(ensure_host_link(c, 1));
+    ph::note_launch(), k_pass_report<<<1, 256, 0, c->stream>>>(c->b.cnt, c->w.ctr, c->t.depth_off, ndepth_off,
+                                                                c->mu_total, c->mu_over, c->rep_dev);
+    PH_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
+// enqueue the report, wait for the stream, and read it: build counters,
+// walk counters (into c->ws), depth offsets (levels + 2, into c->info) and
+// the mutual kernel's reaction need and flag
+static int ph_read_report(photons_ctx *c, int levels, int *h, long long *mu_need, int *mu_over)
+{
+    PH_TRY(ph_enqueue_report(c, levels + 2));
+    PH_CUDA_CHECK(cudaStreamSynchronize(c->stream));
+    const PassReport *r = c->rep;
+    memcpy(h, r->cnt, sizeof(int) * ph::BC_NCOUNTERS);
+    memcpy(c->ws.c, r->wc, sizeof(c->ws.c));
+    c->info.depth_off.assign(r->depth_off, r->depth_off + levels + 2);
+    *mu_need = r->mu_need;
+    *mu_over = r->mu_over;
+    return 0;
+}
 
 // FP32 P2P kernel: 2 mutual pairs (the default; used for MAXLEAF 48-64),
 // 0 packed one-way pairs, 1 scalar (PHOTONS_P2P_KERNEL=mutual|packed|scalar)
@@ -582,10 +713,20 @@ static int ph_prepare_boxes(photons_ctx *c, int nbox, const photons_params *p, c
 }
 
 // the box table for this pass (before the build; the build writes the roots)
+// the box table, staged in pinned host memory and copied by a kernel (the
+// staging is rewritten only after the last kernel that read it has run)
 static int ph_upload_boxes(photons_ctx *c)
 {
-    PH_CUDA_CHECK(cudaMemcpyAsync(c->b.boxes, c->h_boxes.data(), sizeof(BoxParams) * c->h_boxes.size(),
-                                  cudaMemcpyHostToDevice, c->stream));
+    const int nbox = (int)c->h_boxes.size();
+    PH_TRY(ensure_host_link(c, nbox));
+    PH_CUDA_CHECK(cudaEventSynchronize(c->ev_hlink));
+    memcpy(c->hbox, c->h_boxes.data(), sizeof(BoxParams) * (size_t)nbox);
+    static_assert(sizeof(BoxParams) % sizeof(double) == 0, "box table copied as doubles");
+    ph::note_launch(), k_copy_host<<<1, 256, 0, c->stream>>>(reinterpret_cast<const double *>(c->hbox_dev),
+                                                              reinterpret_cast<double *>(c->b.boxes),
+                                                              sizeof(BoxParams) * (size_t)nbox / sizeof(double));
+    PH_CUDA_CHECK(cudaGetLastError());
+    PH_CUDA_CHECK(cudaEventRecord(c->ev_hlink, c->stream));
     return 0;
 }
 
@@ -653,7 +794,7 @@ static int ph_stage_build_boxes(photons_ctx *c, int nbox, const photons_params *
     const double *src = pos;
     PH_TRY(ph_record(c, EV_START));
     if (!device_io) {
-        PH_CUDA_CHECK(cudaMemcpyAsync(c->io, pos, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, st));
+        PH_TRY(ph_copy_host(c, c->io, pos, (size_t)3 * n, true));
         src = c->io;
     }
     PH_TRY(ph_record(c, EV_UPLOADED));
@@ -862,9 +1003,7 @@ static int ph_enqueue_gather(photons_ctx *c, double *dst, int tree_order)
 int ph_stage_output(photons_ctx *c, double *acc, int device_io, int tree_order)
 {
     PH_TRY(ph_enqueue_gather(c, device_io ? acc : c->io, tree_order));
-    if (!device_io)
-        PH_CUDA_CHECK(cudaMemcpyAsync(acc, c->io, sizeof(double) * 3 * (size_t)c->n, cudaMemcpyDeviceToHost,
-                                      c->stream));
+    if (!device_io) PH_TRY(ph_copy_host(c, acc, c->io, (size_t)3 * c->n, false));
     return ph_record(c, EV_END);
 }
 
@@ -972,23 +1111,16 @@ static int force_pass_graph(photons_ctx *c, int nbox, const photons_params *p, c
         }
         PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_START], st));
         PH_TRY(ph_upload_boxes(c));
-        if (!dio) PH_CUDA_CHECK(cudaMemcpyAsync(c->io, pos, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, st));
+        if (!dio) PH_TRY(ph_copy_host(c, c->io, pos, (size_t)3 * n, true));
         PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_UPLOADED], st));
         PH_CUDA_CHECK(cudaGraphLaunch(c->gexec, st));
         ph::g_launches += c->graph_kernels;
-        if (!dio) PH_CUDA_CHECK(cudaMemcpyAsync(acc, c->io, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost, st));
+        if (!dio) PH_TRY(ph_copy_host(c, acc, c->io, (size_t)3 * n, false));
         PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_END], st));
         int h[ph::BC_NCOUNTERS];
-        PH_CUDA_CHECK(cudaMemcpyAsync(h, c->b.cnt, sizeof h, cudaMemcpyDeviceToHost, st));
-        PH_CUDA_CHECK(cudaMemcpyAsync(c->ws.c, c->w.ctr, sizeof(c->ws.c), cudaMemcpyDeviceToHost, st));
-        c->info.depth_off.resize(levels + 2);
-        PH_CUDA_CHECK(cudaMemcpyAsync(c->info.depth_off.data(), c->t.depth_off, sizeof(int) * (levels + 2),
-                                      cudaMemcpyDeviceToHost, st));
         long long mu_need = 0;
         int mu_over = 0;
-        PH_CUDA_CHECK(cudaMemcpyAsync(&mu_need, c->mu_total, sizeof mu_need, cudaMemcpyDeviceToHost, st));
-        PH_CUDA_CHECK(cudaMemcpyAsync(&mu_over, c->mu_over, sizeof mu_over, cudaMemcpyDeviceToHost, st));
-        PH_CUDA_CHECK(cudaStreamSynchronize(st));
+        PH_TRY(ph_read_report(c, levels, h, &mu_need, &mu_over));
         int grow = 0;
         PH_TRY(ph_check_build(c, h[ph::BC_FLAGS], levels, &grow));
         if (grow) { levels = grow; continue; }
@@ -1102,8 +1234,16 @@ int ph_kdk_graph_step(photons_ctx *c, const photons_params *q, int n, double *po
         c->kkey_box = q->boxsize;
         c->have_kkey = true;
     }
-    const double f[2] = {dkh, dd};
-    PH_CUDA_CHECK(cudaMemcpyAsync(c->kdk_f, f, sizeof f, cudaMemcpyHostToDevice, st));
+    // the factors through the pinned staging, copied by a kernel
+    PH_TRY(ensure_host_link(c, 1));
+    PH_CUDA_CHECK(cudaEventSynchronize(c->ev_hlink));
+    c->rep->kdk_f[0] = dkh;
+    c->rep->kdk_f[1] = dd;
+    const double *fdev = reinterpret_cast<const double *>(reinterpret_cast<const char *>(c->rep_dev) +
+                                                           offsetof(PassReport, kdk_f));
+    ph::note_launch(), k_copy_host<<<1, 32, 0, st>>>(fdev, c->kdk_f, 2);
+    PH_CUDA_CHECK(cudaGetLastError());
+    PH_CUDA_CHECK(cudaEventRecord(c->ev_hlink, st));
     PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_START], st));
     PH_TRY(ph_upload_boxes(c));
     PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_UPLOADED], st));
@@ -1111,16 +1251,9 @@ int ph_kdk_graph_step(photons_ctx *c, const photons_params *q, int n, double *po
     ph::g_launches += c->kdk_kernels;
     PH_CUDA_CHECK(cudaEventRecord(c->ev[EV_END], st));
     int h[ph::BC_NCOUNTERS];
-    PH_CUDA_CHECK(cudaMemcpyAsync(h, c->b.cnt, sizeof h, cudaMemcpyDeviceToHost, st));
-    PH_CUDA_CHECK(cudaMemcpyAsync(c->ws.c, c->w.ctr, sizeof(c->ws.c), cudaMemcpyDeviceToHost, st));
-    c->info.depth_off.resize(levels + 2);
-    PH_CUDA_CHECK(cudaMemcpyAsync(c->info.depth_off.data(), c->t.depth_off, sizeof(int) * (levels + 2),
-                                  cudaMemcpyDeviceToHost, st));
     long long mu_need = 0;
     int mu_over = 0;
-    PH_CUDA_CHECK(cudaMemcpyAsync(&mu_need, c->mu_total, sizeof mu_need, cudaMemcpyDeviceToHost, st));
-    PH_CUDA_CHECK(cudaMemcpyAsync(&mu_over, c->mu_over, sizeof mu_over, cudaMemcpyDeviceToHost, st));
-    PH_CUDA_CHECK(cudaStreamSynchronize(st));
+    PH_TRY(ph_read_report(c, levels, h, &mu_need, &mu_over));
     int grow = 0;
     PH_TRY(ph_check_build(c, h[ph::BC_FLAGS], levels, &grow));
     const unsigned long long fl = c->ws.c[ph::WC_FLAGS];
@@ -1180,6 +1313,9 @@ extern "C" void photons_destroy(photons_ctx *c)
     if (c->kexec) cudaGraphExecDestroy(c->kexec);
     cudaFree(c->kdk_f);
     cudaFree(c->kdk_skip);
+    if (c->rep) cudaFreeHost(c->rep);
+    if (c->hbox) cudaFreeHost(c->hbox);
+    if (c->ev_hlink) cudaEventDestroy(c->ev_hlink);
     ph_pm_release(c);
     ph_domain_release(c);
     cudaFree(c->pm_io);

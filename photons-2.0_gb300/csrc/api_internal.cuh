@@ -38,6 +38,19 @@ struct PassKey {
     unsigned long long epoch;
 };
 
+// What a pass leaves for the host, written by one kernel into pinned host
+// memory the device addresses (read after the stream has finished), and the
+// kick-drift-kick factors the host puts there for the next step
+struct PassReport {
+    int cnt[ph::BC_NCOUNTERS];
+    unsigned long long wc[ph::WC_N];
+    long long mu_need;
+    int mu_over;
+    int ndepth_off;
+    int depth_off[PH_MAX_DEPTH_CAP + 2];
+    double kdk_f[2];
+};
+
 struct photons_ctx {
     int device = 0;
     cudaStream_t own_stream = nullptr, stream = nullptr;
@@ -115,6 +128,13 @@ struct photons_ctx {
     double kkey_box = 0.0;
     double *kdk_f = nullptr;
     int *kdk_skip = nullptr;
+    // pinned host memory the device addresses: the pass report, and the box
+    // table staged for upload (hbox_cap entries); ev_hlink is recorded after
+    // the last kernel that read the staged inputs
+    PassReport *rep = nullptr, *rep_dev = nullptr;
+    BoxParams *hbox = nullptr, *hbox_dev = nullptr;
+    int hbox_cap = 0;
+    cudaEvent_t ev_hlink = nullptr;
 };
 
 // return a nonzero status code from the enclosing function
