@@ -350,8 +350,9 @@ int photons_kdk_step_pm_ordered(photons_ctx *ctx, const photons_params *p, int n
 /* kernels launched by this library so far (all contexts) */
 unsigned long long photons_launch_count(void);
 
-/* pinned host memory for the host-buffer pass (its copies then run at the
-   host link's rate); NULL and an error message if it cannot be had */
+/* pinned host memory for the host-buffer pass: the pass's kernels read and
+   write it over the host link (so do they any pinned memory the device
+   addresses); NULL and an error message if it cannot be had */
 void *photons_host_alloc(size_t bytes);
 void photons_host_free(void *p);
 
