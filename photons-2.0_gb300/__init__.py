@@ -501,8 +501,8 @@ def fp64_fma_peak(iters=256):
 
 def host_array(shape, dtype=np.float64):
     """A numpy array in pinned host memory from photons_host_alloc (freed
-    with the array), for the host-buffer pass: its copies then run at the
-    host link's rate."""
+    with the array), for the host-buffer pass: the pass's kernels read and
+    write it over the host link, at the link's rate."""
     import weakref
 
     dtype = np.dtype(dtype)

@@ -337,8 +337,11 @@ def test_fp64_mutual_matches_one_way(ph, ics, workload, nside, maxleaf):
 
 
 def test_pass_with_library_pinned_buffers(ph, ics):
-    """Host buffers from photons_host_alloc (ph.host_array) give the same
-    forces as any host array, and are released with the array."""
+    """Host buffers from photons_host_alloc (ph.host_array), which the
+    pass's kernels read and write over the host link, give the same forces
+    as pageable host arrays (copied by cudaMemcpyAsync), also through views
+    that start 8 bytes off a 16-byte boundary (the copy kernel's 8-byte
+    path), and are released with the array."""
     pos, p = ics.make("zeldovich256", nside=24, maxleaf=64)
     fp = ph.ForcePass(0)
     plain = fp.run(pos, p, precision=ph.FP32_SPLIT)
@@ -347,7 +350,15 @@ def test_pass_with_library_pinned_buffers(ph, ics):
     ha = ph.host_array(pos.shape)
     fp.run(hp, p, precision=ph.FP32_SPLIT, out=ha)
     assert np.array_equal(ha, plain)
-    del hp, ha
+    n = pos.shape[0]
+    hp2 = ph.host_array((3 * n + 1,))
+    ha2 = ph.host_array((3 * n + 1,))
+    vp, va = hp2[1:].reshape(n, 3), ha2[1:].reshape(n, 3)  # 8 bytes into the pinned blocks
+    assert vp.ctypes.data % 16 == 8 and va.ctypes.data % 16 == 8
+    vp[:] = pos
+    fp.run(vp, p, precision=ph.FP32_SPLIT, out=va)
+    assert np.array_equal(va, plain)
+    del hp, ha, vp, va, hp2, ha2
 
 
 def _full_size_parity(ph, fp, port, pos, p, precision, tol, nsub=10000):
