@@ -871,6 +871,44 @@ constexpr int kMuUnroll = MU_UNROLL;
 #define MU_BATCH 32  // sources per reaction reduction (32 or 16)
 #endif
 
+// Bitonic sort of a list of at most 32 R entries in registers: entry
+// i = 32 r + lane in v[r] (padding 0xffffffff sorts last).  Partners at
+// distance j >= 32 are in the same lane, the others one shuffle away.
+template <int R>
+__device__ __forceinline__ void mu_sort_regs(uint32_t *lst, int L, int lane)
+{
+    uint32_t v[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) v[r] = 32 * r + lane < L ? lst[32 * r + lane] : 0xffffffffu;
+#pragma unroll
+    for (int k = 2; k <= 32 * R; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j >= 32) {
+                const int jr = j >> 5;
+#pragma unroll
+                for (int r = 0; r < R; r++) {
+                    if (r & jr) continue;
+                    const int r2 = r | jr;
+                    const bool up = ((32 * r + lane) & k) == 0;
+                    const uint32_t a = v[r], b = v[r2];
+                    if ((a > b) == up) { v[r] = b; v[r2] = a; }
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < R; r++) {
+                    const uint32_t o = __shfl_xor_sync(0xffffffffu, v[r], j);
+                    const bool up = ((32 * r + lane) & k) == 0, low = (lane & j) == 0;
+                    v[r] = (low == up) ? min(v[r], o) : max(v[r], o);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++)
+        if (32 * r + lane < L) lst[32 * r + lane] = v[r];
+}
+
 __global__ void __launch_bounds__(256) k_mu_sort(const int *tree_cnt, const unsigned long long *walk_flags,
                                                   uint32_t *pool, const long long *off, const int *cnt, int *sorted)
 {
@@ -883,7 +921,16 @@ __global__ void __launch_bounds__(256) k_mu_sort(const int *tree_cnt, const unsi
         const int L = cnt[t];
         uint32_t *lst = pool + off[t];
         const int ok = L <= MU_SORT_MAX;
-        if (ok && L > 1) {
+        // lists of up to 256 entries (most of them) are sorted in registers
+        if (L > 1 && L <= 32) {
+            mu_sort_regs<1>(lst, L, lane);
+        } else if (L > 32 && L <= 64) {
+            mu_sort_regs<2>(lst, L, lane);
+        } else if (L > 64 && L <= 128) {
+            mu_sort_regs<4>(lst, L, lane);
+        } else if (L > 128 && L <= 256) {
+            mu_sort_regs<8>(lst, L, lane);
+        } else if (ok && L > 1) {
             int P = 2;
             while (P < L) P <<= 1;
             for (int i = lane; i < P; i += 32) buf[i] = i < L ? lst[i] : 0xffffffffu;
