@@ -862,11 +862,11 @@ constexpr int kMuUnroll = MU_UNROLL;
 // up to 8192 entries with a block each, so that halo leaves pair too, made
 // 128^3 NFW at leaf 48 slower: 46.6 against 39.4 ms.)
 #define MU_SORT_MAX 1024
-// Two builds of the kernel, chosen by MAXLEAF: for leaves of up to 64
-// (mostly 8 targets per lane) 3 resident blocks per SM (158 registers) with
-// two target pairs evaluated stage by stage together; below 60, 4 blocks
-// (126 registers) and one pair at a time (256^3: 65.3 vs 66.4 ms at leaf 64,
-// 55.5 vs 59.6 ms at leaf 48)
+// Four builds of the kernel (launch_p2p_mutual): 3 or 4 resident blocks per
+// SM, one or two target pairs evaluated stage by stage together; the
+// default is 4 blocks, one pair at a time, with the 6-target path for
+// leaves of 33-48 (256^3 leaf 64: P2P phase 60.3 against 61.6 ms for 3
+// blocks and two pairs)
 #ifndef MU_BATCH
 #define MU_BATCH 32  // sources per reaction reduction (32 or 16)
 #endif
