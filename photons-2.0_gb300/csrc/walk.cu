@@ -120,6 +120,7 @@ struct WalkArgs {
     const BoxParams *boxes;  // per box: side, rcut, root
     double theta2, theta;
     float theta2f;
+    float prune_k2f;  // (0.95 theta)^2 in FP32: the image pruning rule's width test
     WalkImports imp;  // received trees (none outside a rank's domain pass)
     int maxleaf;
 };
@@ -152,6 +153,33 @@ __device__ __forceinline__ bool image_pruned(const WalkArgs &A, int r, double rc
     if (wmax < bw[2]) wmax = bw[2];
     if (dr >= rcut) return true;
     return wmax < __dmul_rn(__dmul_rn(0.95, A.theta), dr);
+}
+
+// The pruning rule in FP32 with error margins, as acceptance_fp32 does the
+// MAC: 1 pruned, 0 not, -2 too close to a threshold (the caller evaluates
+// image_pruned).  d = (c_b + shift) - c_r from the hi/lo centres (relative
+// error ~1e-7), FP32 widths of the receiving root r and of node b.
+__device__ __forceinline__ int image_pruned_fp32(float d0, float d1, float d2, float4 rw, float4 bw, float rc2,
+                                                 float k2)
+{
+    const float h0 = (rw.x + bw.x) * 0.5f, h1 = (rw.y + bw.y) * 0.5f, h2 = (rw.z + bw.z) * 0.5f;
+    const float a0 = fabsf(d0), a1 = fabsf(d1), a2 = fabsf(d2);
+    const float u0 = a0 + h0, u1 = a1 + h1, u2 = a2 + h2;  // error scale of each gap
+    float g0 = a0 - h0, g1 = a1 - h1, g2 = a2 - h2;
+    g0 = g0 > 0.f ? g0 : 0.f;
+    g1 = g1 > 0.f ? g1 : 0.f;
+    g2 = g2 > 0.f ? g2 : 0.f;
+    const float dm2 = g0 * g0 + g1 * g1 + g2 * g2;
+    const float edm = 4e-6f * (g0 * u0 + g1 * u1 + g2 * u2) + 1e-6f * (dm2 + rc2);
+    if (dm2 >= rc2 + edm) return 1;  // dr >= rcut
+    if (dm2 > rc2 - edm) return -2;
+    // wmax < 0.95 theta dr, squared (k2 = (0.95 theta)^2)
+    const float wmax = fmaxf(bw.x, fmaxf(bw.y, bw.z));
+    const float lhs = wmax * wmax, rhs = k2 * dm2;
+    const float ew = 2e-6f * (lhs + rhs) + k2 * edm;
+    if (lhs < rhs - ew) return 1;
+    if (lhs > rhs + ew) return 0;
+    return -2;
 }
 
 enum { OUT_NONE = 0, OUT_P2P = 1, OUT_M2L = 2, OUT_PUSH = 3, OUT_OPEN = 4, OUT_SELF_PUSH = 5 };
@@ -314,11 +342,16 @@ __global__ void __launch_bounds__(WALK_TB, MINB) k_walk_level(WalkArgs A)
                     const float e2 = centre_diff32(bh[s].z, bl[s].z, ah.z, al.z, mk, Lhi, Llo);
                     int flag = acceptance_fp32(aw.x, aw.y, aw.z, bw[s].x, bw[s].y, bw[s].z, e0, e1, e2, A.theta2f,
                                                c2f);
-                    const double s0 = mi * boxL, s1 = mj * boxL, s2 = mk * boxL;
+                    // the image shift in FP64 only where an exact decision needs it
+                    // (GB300 runs FP64 at 1/64 of the FP32 rate)
                     if (flag == -2) {
                         // image node centre = local centre + shift (src/remotes.c:123-125)
                         double cb0 = g.cx[bb], cb1 = g.cy[bb], cb2 = g.cz[bb];
-                        if (im) { cb0 = __dadd_rn(cb0, s0); cb1 = __dadd_rn(cb1, s1); cb2 = __dadd_rn(cb2, s2); }
+                        if (im) {
+                            cb0 = __dadd_rn(cb0, mi * boxL);
+                            cb1 = __dadd_rn(cb1, mj * boxL);
+                            cb2 = __dadd_rn(cb2, mk * boxL);
+                        }
                         flag = acceptance_fp64(wa0, wa1, wa2, g.wx[bb], g.wy[bb], g.wz[bb], __dsub_rn(ca0, cb0),
                                                __dsub_rn(ca1, cb1), __dsub_rn(ca2, cb2), A.theta2, c2);
                     }
@@ -335,8 +368,21 @@ __global__ void __launch_bounds__(WALK_TB, MINB) k_walk_level(WalkArgs A)
                     } else {
                         // an image node is pruned by the rule of src/remotes.c:97-158 evaluated
                         // here; a received node came without children when its sender pruned it
-                        const bool pruned = !leaf_b && (im == PH_IMG_IMPORT ? g.son0[bb] < 0
-                                                                            : image_pruned(A, root, rcut, bb, s0, s1, s2));
+                        bool pruned = false;
+                        if (!leaf_b) {
+                            if (im == PH_IMG_IMPORT) {
+                                pruned = g.son0[bb] < 0;
+                            } else {
+                                // the receiving root's centre against the node's, in FP32 first
+                                const float4 rh = g.chi[root], rl = g.clo[root], rw = g.w32[root];
+                                const float f0 = centre_diff32(bh[s].x, bl[s].x, rh.x, rl.x, mi, Lhi, Llo);
+                                const float f1 = centre_diff32(bh[s].y, bl[s].y, rh.y, rl.y, mj, Lhi, Llo);
+                                const float f2 = centre_diff32(bh[s].z, bl[s].z, rh.z, rl.z, mk, Lhi, Llo);
+                                const int pr = image_pruned_fp32(f0, f1, f2, rw, bw[s], c2f, A.prune_k2f);
+                                pruned = pr == -2 ? image_pruned(A, root, rcut, bb, mi * boxL, mj * boxL, mk * boxL)
+                                                  : pr == 1;
+                            }
+                        }
                         if (leaf_a) kd = (flag == 1 || pruned) ? OUT_M2L : OUT_OPEN;
                         else if (flag == 1) kd = OUT_M2L;
                         else kd = (leaf_b || pruned || bigger_a) ? OUT_PUSH : OUT_OPEN;
@@ -494,6 +540,7 @@ int walk_lists(WalkBufs &w, const TreeBufs &t, const int *tree_cnt, const BoxPar
     A.g.son0 = t.son0; A.g.son1 = t.son1; A.g.npart = t.npart; A.g.parent = t.parent;
     A.g.chi = t.chi; A.g.clo = t.clo; A.g.w32 = t.w32; A.g.son = t.son2;
     A.theta2f = (float)(p.theta * p.theta);
+    A.prune_k2f = (float)((0.95 * p.theta) * (0.95 * p.theta));
     A.boxid = t.boxid;
     A.boxes = boxes;
     A.w = w;
