@@ -90,7 +90,16 @@ __device__ __forceinline__ int acceptance_fp32(float wi0, float wi1, float wi2, 
     const float S = g0 + g1 + g2;
     const float eS = 2e-6f * (u0 + u1 + u2);
     if (S < 1e-4f - eS) return 0;        // touching
-    if (S < 1e-4f + eS) return -2;
+    if (S < 1e-4f + eS) {
+        // Near the touching threshold (touching boxes: S = 0 up to FP32
+        // error, which can exceed the window for large boxes) the answer is
+        // 0 on either side of it: the gaps are too small for the cutoff drop
+        // (dm2 <= S^2 < c2), and the opening-angle accept needs
+        // 2 wmax < theta dd with dd <= sqrt(3) (wmax/2 + S), impossible for
+        // theta <= 1 and S < 0.15 wmax/2 (wmax/2: the largest half-width sum)
+        const float smax = 1e-4f + 2.f * eS, hw = fmaxf(w0, fmaxf(w1, w2));
+        return (theta2 <= 1.f && smax < 0.1f * hw && smax * smax < c2) ? 0 : -2;
+    }
     const float dm2 = g0 * g0 + g1 * g1 + g2 * g2;
     const float edm = 4e-6f * (g0 * u0 + g1 * u1 + g2 * u2) + 1e-6f * (dm2 + c2);
     if (dm2 >= c2 + edm) return -1;      // beyond the cutoff
