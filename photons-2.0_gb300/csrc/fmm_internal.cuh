@@ -137,6 +137,10 @@ inline void note_launch()
 // cap elements); writes total to *total (device) if total != nullptr.
 void scan_exclusive_i32(const int *in, int *out, const int *n_ptr, int cap, int *total, int *scratch,
                         size_t scratch_elems, cudaStream_t st);
+// the same for a count the host knows is at most nmax (<= cap): counts of
+// at most 65,536 are scanned in one block, one launch
+void scan_exclusive_i32_bounded(const int *in, int *out, const int *n_ptr, int cap, int nmax, int *total,
+                                int *scratch, size_t scratch_elems, cudaStream_t st);
 size_t scan_scratch_elems(int cap);
 // the same over 64-bit values; scratch holds scan_scratch_elems(cap) values
 void scan_exclusive_i64(const long long *in, long long *out, const int *n_ptr, int cap, long long *total,

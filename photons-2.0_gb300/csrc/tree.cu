@@ -1095,6 +1095,10 @@ int build_tree(BuildBufs &b, TreeBufs &T, const PassParams &p, int levels, int t
     // a level has at most nbox 2^d nodes: the first levels are small enough for
     // single-block bookkeeping (7 launches a level instead of 19)
     bool pending = false;  // a small level whose k_level_finish is still to come
+    // nodes of one level: the roots, or the children of the level above's
+    // wide nodes (more than CHUNK particles each, so at most N / CHUNK)
+    const long long lvl_bound = 2LL * (b.cap_n / CHUNK) + 2LL * b.nbox + 2;
+    const int lvl_max = lvl_bound < b.cap_nodes ? (int)lvl_bound : b.cap_nodes;
     for (int d = 0; d < top; d++) {
         const int D = (p.axis0 + d) % 3;  // from direct_local_start; the axis cycles (src/fmm.c:99)
         const bool small = d < 24 && ((long long)b.nbox << d) <= SMALL_LEVEL;
@@ -1103,8 +1107,8 @@ int build_tree(BuildBufs &b, TreeBufs &T, const PassParams &p, int levels, int t
         } else {
             if (pending) ph::note_launch(), k_level_finish<<<1, 1, 0, st>>>(b, d - 1, top);
             ph::note_launch(), k_level_nch<<<maxb, TB, 0, st>>>(b);
-            scan_exclusive_i32(b.tn_nch, b.tn_chunk_base, b.cnt + BC_LEVEL_COUNT, b.cap_nodes, b.cnt + BC_W,
-                               b.scan_scratch, b.scan_scratch_elems, st);
+            scan_exclusive_i32_bounded(b.tn_nch, b.tn_chunk_base, b.cnt + BC_LEVEL_COUNT, b.cap_nodes, lvl_max,
+                                       b.cnt + BC_W, b.scan_scratch, b.scan_scratch_elems, st);
             ph::note_launch(), k_chunk_map<<<maxb, TB, 0, st>>>(b);
         }
         ph::note_launch(), k_chunk_sum<<<maxb, TB, 0, st>>>(b, D);
@@ -1114,10 +1118,10 @@ int build_tree(BuildBufs &b, TreeBufs &T, const PassParams &p, int levels, int t
             ph::note_launch(), k_level_close<<<1, SMALL_TB, 0, st>>>(b, p.maxleaf, D);
         } else {
             ph::note_launch(), k_node_split<<<maxb, TB, 0, st>>>(b, p.maxleaf);
-            scan_exclusive_i32(b.tn_nodeflag, b.tn_nodebase, b.cnt + BC_LEVEL_COUNT, b.cap_nodes,
-                               b.cnt + BC_NEXT_NODES, b.scan_scratch, b.scan_scratch_elems, st);
-            scan_exclusive_i32(b.tn_leafflag, b.tn_leafbase, b.cnt + BC_LEVEL_COUNT, b.cap_nodes,
-                               b.cnt + BC_NEW_LEAVES, b.scan_scratch, b.scan_scratch_elems, st);
+            scan_exclusive_i32_bounded(b.tn_nodeflag, b.tn_nodebase, b.cnt + BC_LEVEL_COUNT, b.cap_nodes, lvl_max,
+                                       b.cnt + BC_NEXT_NODES, b.scan_scratch, b.scan_scratch_elems, st);
+            scan_exclusive_i32_bounded(b.tn_leafflag, b.tn_leafbase, b.cnt + BC_LEVEL_COUNT, b.cap_nodes, lvl_max,
+                                       b.cnt + BC_NEW_LEAVES, b.scan_scratch, b.scan_scratch_elems, st);
             ph::note_launch(), k_make_children<<<maxb, TB, 0, st>>>(b, p.maxleaf, D);
         }
         ph::note_launch(), k_rank<<<maxb, TB, 0, st>>>(b, D);
